@@ -1,0 +1,13 @@
+"""GB300-native Monte Carlo sweep for ETHER (mukkelian/Ether).
+
+The compute path is libether_gpu.so (hand-written sm_103a CUDA behind the C-ABI in
+include/ether_gpu.h); this package is its Python binding and host-side set-up helpers.
+"""
+from . import abi
+from .abi import EtherError, MODEL_ISING, MODEL_XYZ, FLAG_FORCE_GENERAL, \
+    FLAG_PT_REFERENCE_COPY, FLAG_PT_TRUE_ENERGY
+from .model import KB_EV, MB_EV, Lattice, Sweep, couplings, pyrochlore, simple_cubic, units
+
+__all__ = ["abi", "EtherError", "MODEL_ISING", "MODEL_XYZ", "FLAG_FORCE_GENERAL",
+           "FLAG_PT_REFERENCE_COPY", "FLAG_PT_TRUE_ENERGY", "KB_EV", "MB_EV", "Lattice",
+           "Sweep", "couplings", "pyrochlore", "simple_cubic", "units"]

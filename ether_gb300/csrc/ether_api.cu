@@ -1,0 +1,817 @@
+// ether_api.cu -- the C-ABI (include/ether_gpu.h): context set-up and the per-MCS calls.
+//
+// Set-up does on the host, once, what the kernels must not redo per sweep: it reads the
+// reference arrays (ion, nn, j_exc, ...), colours the neighbour graph greedily in site
+// order, lays the sites out colour-major, converts the nn table to CSR in that order,
+// recognises the even periodic simple-cubic lattice (arithmetic neighbours), and builds
+// the FP64 Ising acceptance-threshold tables per temperature slot.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+using namespace ether;
+
+struct ether_ctx {
+    Ctx c;
+};
+
+static thread_local std::string g_err;
+
+static int fail(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+
+void ether::set_error(const std::string &msg) { g_err = msg; }
+
+#define CUDA_TRY(expr)                                                                     \
+    do {                                                                                   \
+        cudaError_t _e = (expr);                                                           \
+        if (_e != cudaSuccess)                                                             \
+            return fail(_e == cudaErrorMemoryAllocation ? ETHER_ERR_NOMEM : ETHER_ERR_CUDA, \
+                        std::string(#expr) + ": " + cudaGetErrorString(_e));               \
+    } while (0)
+
+extern "C" int ether_abi_version(void) { return ETHER_ABI_VERSION; }
+extern "C" const char *ether_last_error(void) { return g_err.c_str(); }
+
+namespace {
+
+template <class T>
+int dev_alloc(Ctx &c, T **p, size_t n) {
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e != cudaSuccess) return fail(ETHER_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    c.device_bytes += n * sizeof(T);
+    return ETHER_OK;
+}
+
+template <class T>
+int dev_upload(Ctx &c, T **p, const std::vector<T> &v) {
+    int rc = dev_alloc(c, p, v.size());
+    if (rc) return rc;
+    if (!v.empty()) CUDA_TRY(cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return ETHER_OK;
+}
+
+struct Nbr {
+    int j;   // 0-based site
+    int b;   // shell
+    int sj;  // 1-based species
+};
+
+// ---------------------------------------------------------------- Ising tables --------
+// Site type = (species, neighbours per (shell, neighbour-species) group).  Index inside a
+// type's half-table = sum over groups of stride_g * (up neighbours in g).
+int build_ising_types(Ctx &c, const std::vector<int> &sp, const std::vector<std::vector<Nbr>> &adj,
+                      std::vector<uint16_t> &itype_site, std::vector<int32_t> &wstride_site) {
+    const int G = c.nsh * c.nsp;
+    std::map<std::vector<int>, int> types;
+    std::vector<std::vector<int>> keys;
+    itype_site.assign(c.N, 0);
+    for (int i = 0; i < c.N; ++i) {
+        std::vector<int> key(G + 1, 0);
+        key[0] = sp[i];
+        for (const Nbr &n : adj[i]) key[1 + n.b * c.nsp + (n.sj - 1)]++;
+        auto it = types.find(key);
+        int id;
+        if (it == types.end()) {
+            id = (int)keys.size();
+            types.emplace(key, id);
+            keys.push_back(key);
+        } else {
+            id = it->second;
+        }
+        itype_site[i] = (uint16_t)id;
+    }
+    if (keys.size() > 65535) return fail(ETHER_ERR_CAPACITY, "too many Ising site types");
+    c.n_types = (int)keys.size();
+    c.h_type_base.assign(c.n_types, 0);
+    c.h_type_half.assign(c.n_types, 0);
+    c.type_groupcount.assign(c.n_types, std::vector<int>(G, 0));
+    c.type_species.assign(c.n_types, 0);
+    std::vector<std::vector<int>> strides(c.n_types, std::vector<int>(G, 0));
+    long total = 0;
+    for (int ty = 0; ty < c.n_types; ++ty) {
+        long half = 1;
+        for (int g = 0; g < G; ++g) {
+            c.type_groupcount[ty][g] = keys[ty][1 + g];
+            strides[ty][g] = (int)half;
+            half *= (keys[ty][1 + g] + 1);
+            if (half > (1L << 22)) return fail(ETHER_ERR_CAPACITY, "Ising threshold table too large");
+        }
+        c.type_species[ty] = keys[ty][0];
+        c.h_type_half[ty] = (int)half;
+        c.h_type_base[ty] = (int)total;
+        total += 2 * half;
+        if (total > (1L << 24)) return fail(ETHER_ERR_CAPACITY, "Ising threshold table too large");
+    }
+    c.table_entries = (int)total;
+    // strides per (type, group); emitted per CSR slot by the caller
+    wstride_site.resize((size_t)c.n_types * G);
+    for (int ty = 0; ty < c.n_types; ++ty)
+        for (int g = 0; g < G; ++g) wstride_site[(size_t)ty * G + g] = strides[ty][g];
+    return ETHER_OK;
+}
+
+// Thresholds for one temperature: the same FP64 expression as the oracle's colour mode.
+void ising_thresholds(const Ctx &c, double beta, uint32_t *thr, uint8_t *always) {
+    const int G = c.nsh * c.nsp;
+    std::vector<int> nup(G);
+    for (int ty = 0; ty < c.n_types; ++ty) {
+        const int si = c.type_species[ty];
+        const std::vector<int> &cnt = c.type_groupcount[ty];
+        const int half = c.h_type_half[ty];
+        const double gms = c.g * c.mb * c.s_len[si - 1];
+        for (int own = 0; own < 2; ++own) {
+            const double sig = own ? 1.0 : -1.0;
+            for (int idx = 0; idx < half; ++idx) {
+                int rem = idx;
+                for (int g = 0; g < G; ++g) {
+                    nup[g] = rem % (cnt[g] + 1);
+                    rem /= (cnt[g] + 1);
+                }
+                double field = 0.0;
+                for (int b = 0; b < c.nsh; ++b)
+                    for (int q = 0; q < c.nsp; ++q) {
+                        const int g = b * c.nsp + q;
+                        const int m = 2 * nup[g] - cnt[g];
+                        const size_t jx = (size_t)b * c.nsp * c.nsp + (size_t)(si - 1) * c.nsp + q;
+                        field += c.h_Jd[3 * jx + 2] * (double)m;
+                    }
+                double dE = (-2.0 * sig) * field;
+                if (c.zeeman) dE += -(gms * ((-2.0 * sig) * c.h[2]));
+                const double p = std::exp(-beta * dE);
+                const size_t e = (size_t)c.h_type_base[ty] + (size_t)own * half + idx;
+                if (p >= 1.0) {
+                    always[e] = 1;
+                    thr[e] = 0xFFFFFFFFu;
+                } else {
+                    const double u = std::ceil(p * 4294967296.0);
+                    if (u >= 4294967296.0) { always[e] = 1; thr[e] = 0xFFFFFFFFu; }
+                    else { always[e] = 0; thr[e] = (uint32_t)u; }
+                }
+            }
+        }
+    }
+}
+
+int upload_ladder(Ctx &c) {
+    std::vector<float> bf(c.n_slots);
+    for (int s = 0; s < c.n_slots; ++s) bf[s] = (float)c.beta_slots[s];
+    CUDA_TRY(cudaMemcpyAsync(c.beta_slot, c.beta_slots.data(), sizeof(double) * c.n_slots,
+                             cudaMemcpyHostToDevice, c.stream));
+    CUDA_TRY(cudaMemcpyAsync(c.beta_slot_f, bf.data(), sizeof(float) * c.n_slots,
+                             cudaMemcpyHostToDevice, c.stream));
+    std::vector<int32_t> sor(c.R), ros(c.R);
+    for (int r = 0; r < c.R; ++r) {
+        sor[r] = r % c.n_slots;
+        ros[r] = r;
+    }
+    CUDA_TRY(cudaMemcpyAsync(c.slot_of_rep, sor.data(), sizeof(int32_t) * c.R, cudaMemcpyHostToDevice, c.stream));
+    CUDA_TRY(cudaMemcpyAsync(c.rep_of_slot, ros.data(), sizeof(int32_t) * c.R, cudaMemcpyHostToDevice, c.stream));
+    if (c.model == 0) {
+        std::vector<uint32_t> thr((size_t)c.n_slots * c.table_entries);
+        std::vector<uint8_t> al((size_t)c.n_slots * c.table_entries);
+        for (int s = 0; s < c.n_slots; ++s)
+            ising_thresholds(c, c.beta_slots[s], thr.data() + (size_t)s * c.table_entries,
+                             al.data() + (size_t)s * c.table_entries);
+        CUDA_TRY(cudaMemcpyAsync(c.thr, thr.data(), thr.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, c.stream));
+        CUDA_TRY(cudaMemcpyAsync(c.always, al.data(), al.size(), cudaMemcpyHostToDevice, c.stream));
+    }
+    CUDA_TRY(cudaStreamSynchronize(c.stream));
+    c.beta_set = true;
+    return ETHER_OK;
+}
+
+void free_ctx(Ctx &c) {
+    void *ptrs[] = {c.t.row_ptr, c.t.nbr, c.t.jidx, c.t.wstride, c.t.species, c.t.itype,
+                    c.t.type_base, c.t.type_half, c.t.J, c.t.Jd, c.t.zee, c.t.zeed, c.t.D,
+                    c.t.mweight, c.t.site_of_storage, c.spins, c.spins4, c.beta_slot,
+                    c.beta_slot_f, c.slot_of_rep, c.rep_of_slot, c.thr, c.always, c.stream_id,
+                    c.step, c.ovrr_step, c.fresh_call, c.acc_count, c.E, c.M, c.sums,
+                    c.partials, c.pt_accepts, c.copy_from};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (c.stream) cudaStreamDestroy(c.stream);
+    c = Ctx();
+}
+
+}  // namespace
+
+extern "C" int ether_create(const ether_desc *d, ether_ctx **out) {
+    if (!d || !out) return fail(ETHER_ERR_ARG, "null descriptor or output pointer");
+    *out = nullptr;
+    if (d->n_sites <= 0 || d->n_species <= 0 || d->n_shells < 0 || d->nbd_capacity < 0 ||
+        d->n_replicas <= 0)
+        return fail(ETHER_ERR_ARG, "non-positive size in descriptor");
+    if (d->model != ETHER_MODEL_ISING && d->model != ETHER_MODEL_XYZ)
+        return fail(ETHER_ERR_ARG, "model must be ETHER_MODEL_ISING or ETHER_MODEL_XYZ");
+    if (!d->ion || !d->s || (d->n_shells > 0 && (!d->nn || !d->j_exc)))
+        return fail(ETHER_ERR_ARG, "missing ion, nn, j_exc or s array");
+    if (d->sia && d->model == ETHER_MODEL_XYZ && !d->sia_vec)
+        return fail(ETHER_ERR_ARG, "sia set but sia_vec is NULL");
+    if (d->n_species > 255) return fail(ETHER_ERR_UNSUPPORTED, "more than 255 species");
+    if ((long)d->n_shells * d->n_species * d->n_species > 65535)
+        return fail(ETHER_ERR_UNSUPPORTED, "too many coupling entries");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(ETHER_ERR_NODEV, "no CUDA device");
+
+    ether_ctx *h = new (std::nothrow) ether_ctx();
+    if (!h) return fail(ETHER_ERR_NOMEM, "host allocation failed");
+    Ctx &c = h->c;
+    c.N = d->n_sites;
+    c.nsp = d->n_species;
+    c.nsh = d->n_shells;
+    c.cap = d->nbd_capacity;
+    c.model = d->model;
+    c.angle = d->angle ? 1 : 0;
+    c.dphi = d->dphi;
+    c.zeeman = d->zeeman ? 1 : 0;
+    c.sia = (d->sia && d->model == ETHER_MODEL_XYZ) ? 1 : 0;
+    for (int k = 0; k < 3; ++k) c.h[k] = d->h[k];
+    c.g = d->g_factor;
+    c.mb = d->mb;
+    c.R = d->n_replicas;
+    c.seed = d->seed;
+    c.flags = d->flags;
+    c.s_len.assign(d->s, d->s + c.nsp);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&c.sm_count, cudaDevAttrMultiProcessorCount, dev);
+
+    auto bail = [&](int rc) {
+        free_ctx(c);
+        delete h;
+        return rc;
+    };
+
+    // ----- species and neighbour lists in the reference's nn order
+    const int N = c.N;
+    std::vector<int> sp(N);
+    for (int i = 0; i < N; ++i) {
+        double v = d->ion[4 + 9 * (size_t)i];
+        int q = (int)v;
+        if (q < 1 || q > c.nsp) return bail(fail(ETHER_ERR_ARG, "ion(4,i) species out of range at site " + std::to_string(i + 1)));
+        sp[i] = q;
+    }
+    std::vector<std::vector<Nbr>> adj(N);
+    const size_t cap1 = (size_t)c.cap + 1;
+    for (int i = 0; i < N; ++i)
+        for (int b = 0; b < c.nsh; ++b) {
+            int cnt = d->nn[b + (size_t)c.nsh * i];
+            if (cnt < 0 || cnt > c.cap) return bail(fail(ETHER_ERR_ARG, "nn count out of range at site " + std::to_string(i + 1)));
+            for (int k = 1; k <= cnt; ++k) {
+                int j = d->nn[b + (size_t)c.nsh * ((size_t)i + (size_t)N * ((size_t)k + cap1))];
+                if (j < 1 || j > N) return bail(fail(ETHER_ERR_ARG, "nn neighbour index out of range at site " + std::to_string(i + 1)));
+                adj[i].push_back(Nbr{j - 1, b, sp[j - 1]});
+            }
+        }
+
+    // ----- greedy colouring over the symmetric closure
+    {
+        std::vector<std::vector<int>> und(N);
+        for (int i = 0; i < N; ++i)
+            for (const Nbr &n : adj[i]) {
+                und[i].push_back(n.j);
+                und[n.j].push_back(i);
+            }
+        c.colour.assign(N, -1);
+        c.ncol = 0;
+        std::vector<int> mark(kMaxColours + 1, -1);
+        for (int i = 0; i < N; ++i) {
+            for (int j : und[i])
+                if (j < i && c.colour[j] >= 0) mark[c.colour[j]] = i;
+            int col = 0;
+            while (col <= kMaxColours && mark[col] == i) ++col;
+            if (col >= kMaxColours) return bail(fail(ETHER_ERR_CAPACITY, "neighbour graph needs more than 64 colours"));
+            c.colour[i] = col;
+            c.ncol = std::max(c.ncol, col + 1);
+        }
+        std::vector<int> cnt(c.ncol, 0);
+        c.rank.assign(N, 0);
+        for (int i = 0; i < N; ++i) c.rank[i] = cnt[c.colour[i]]++;
+        c.col_off[0] = 0;
+        for (int k = 0; k < c.ncol; ++k) c.col_off[k + 1] = c.col_off[k] + cnt[k];
+        c.storage.assign(N, 0);
+        c.site_of_storage.assign(N, 0);
+        for (int i = 0; i < N; ++i) {
+            c.storage[i] = c.col_off[c.colour[i]] + c.rank[i];
+            c.site_of_storage[c.storage[i]] = i;
+        }
+    }
+
+    // ----- simple-cubic fast path: one site per cell, one species, one shell of the six
+    //       periodic nearest neighbours, even extents >= 4
+    c.fast = false;
+    if (!(c.flags & ETHER_FLAG_FORCE_GENERAL) && c.nsp == 1 && c.nsh == 1 && d->basis == 1) {
+        const int L1 = d->sc[0], L2 = d->sc[1], L3 = d->sc[2];
+        bool ok = L1 >= 4 && L2 >= 4 && L3 >= 4 && L1 % 2 == 0 && L2 % 2 == 0 && L3 % 2 == 0 &&
+                  (long)L1 * L2 * L3 == N;
+        for (int i = 0; ok && i < N; ++i) {
+            int x = i % L1, y = (i / L1) % L2, z = i / (L1 * L2);
+            if ((int)adj[i].size() != 6 || c.colour[i] != ((x + y + z) & 1)) { ok = false; break; }
+            int want[6] = {((x + 1) % L1) + L1 * (y + L2 * z), ((x + L1 - 1) % L1) + L1 * (y + L2 * z),
+                           x + L1 * (((y + 1) % L2) + L2 * z), x + L1 * (((y + L2 - 1) % L2) + L2 * z),
+                           x + L1 * (y + L2 * ((z + 1) % L3)), x + L1 * (y + L2 * ((z + L3 - 1) % L3))};
+            std::sort(want, want + 6);
+            int have[6];
+            for (int k = 0; k < 6; ++k) have[k] = adj[i][k].j;
+            for (int k = 0; k < 6; ++k)
+                if (have[k] != want[k]) { ok = false; break; }
+        }
+        if (ok) {
+            c.L[0] = L1; c.L[1] = L2; c.L[2] = L3;
+            const int H = L1 / 2;
+            c.vec_bytes = (H % 16 == 0) ? 16 : (H % 8 == 0) ? 8 : (H % 4 == 0) ? 4 : 0;
+            c.fast = (c.model == ETHER_MODEL_XYZ) || c.vec_bytes > 0;
+        }
+    }
+
+    // ----- couplings
+    const size_t nJ = (size_t)std::max(1, c.nsh) * c.nsp * c.nsp;
+    c.h_Jf.assign(3 * nJ, 0.f);
+    c.h_Jd.assign(3 * nJ, 0.0);
+    for (int b = 0; b < c.nsh; ++b)
+        for (int si = 0; si < c.nsp; ++si)
+            for (int sj = 0; sj < c.nsp; ++sj)
+                for (int k = 0; k < 3; ++k) {
+                    double v = d->j_exc[b + (size_t)c.nsh * (si + (size_t)c.nsp * (sj + (size_t)c.nsp * k))];
+                    size_t jx = (size_t)b * c.nsp * c.nsp + (size_t)si * c.nsp + sj;
+                    c.h_Jd[3 * jx + k] = v;
+                    c.h_Jf[3 * jx + k] = (float)v;
+                }
+    std::vector<float> zee(3 * c.nsp), D(3 * c.nsp, 0.f);
+    std::vector<double> zeed(3 * c.nsp);
+    for (int q = 0; q < c.nsp; ++q) {
+        double gms = c.g * c.mb * c.s_len[q];
+        for (int k = 0; k < 3; ++k) {
+            zeed[3 * q + k] = -(gms * c.h[k]);
+            zee[3 * q + k] = (float)zeed[3 * q + k];
+            if (c.sia) D[3 * q + k] = (float)d->sia_vec[k + 3 * (size_t)q];
+        }
+    }
+
+    // ----- CSR in storage order
+    std::vector<int32_t> row_ptr(N + 1, 0), nbr, wstr;
+    std::vector<uint16_t> jidx;
+    std::vector<uint8_t> spc(N);
+    std::vector<uint16_t> ity(N, 0);
+    std::vector<double> mw(N);
+    std::vector<uint16_t> itype_site;
+    std::vector<int32_t> type_strides;
+    if (c.model == ETHER_MODEL_ISING) {
+        int rc = build_ising_types(c, sp, adj, itype_site, type_strides);
+        if (rc) return bail(rc);
+    }
+    const int G = c.nsh * c.nsp;
+    for (int s = 0; s < N; ++s) {
+        const int i = c.site_of_storage[s];
+        for (const Nbr &n : adj[i]) {
+            nbr.push_back(c.storage[n.j]);
+            jidx.push_back((uint16_t)((size_t)n.b * c.nsp * c.nsp + (size_t)(sp[i] - 1) * c.nsp + (n.sj - 1)));
+            if (c.model == ETHER_MODEL_ISING)
+                wstr.push_back(type_strides[(size_t)itype_site[i] * G + n.b * c.nsp + (n.sj - 1)]);
+        }
+        row_ptr[s + 1] = (int32_t)nbr.size();
+        spc[s] = (uint8_t)sp[i];
+        if (c.model == ETHER_MODEL_ISING) ity[s] = itype_site[i];
+        mw[s] = (d->stgg ? d->stgg[i] : 1.0) * c.s_len[sp[i] - 1];
+    }
+
+    // ----- device
+    CUDA_TRY(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    int rc = ETHER_OK;
+#define TRY(x) do { rc = (x); if (rc) return bail(rc); } while (0)
+    TRY(dev_upload(c, &c.t.row_ptr, row_ptr));
+    TRY(dev_upload(c, &c.t.nbr, nbr));
+    TRY(dev_upload(c, &c.t.jidx, jidx));
+    TRY(dev_upload(c, &c.t.wstride, wstr));
+    TRY(dev_upload(c, &c.t.species, spc));
+    TRY(dev_upload(c, &c.t.itype, ity));
+    TRY(dev_upload(c, &c.t.type_base, c.h_type_base));
+    TRY(dev_upload(c, &c.t.type_half, c.h_type_half));
+    TRY(dev_upload(c, &c.t.J, c.h_Jf));
+    TRY(dev_upload(c, &c.t.Jd, c.h_Jd));
+    TRY(dev_upload(c, &c.t.zee, zee));
+    TRY(dev_upload(c, &c.t.zeed, zeed));
+    TRY(dev_upload(c, &c.t.D, D));
+    TRY(dev_upload(c, &c.t.mweight, mw));
+    TRY(dev_upload(c, &c.t.site_of_storage, c.site_of_storage));
+    const size_t RN = (size_t)c.R * N;
+    if (c.model == ETHER_MODEL_ISING) TRY(dev_alloc(c, &c.spins, RN));
+    else TRY(dev_alloc(c, &c.spins4, RN));
+    TRY(dev_alloc(c, &c.beta_slot, c.R));
+    TRY(dev_alloc(c, &c.beta_slot_f, c.R));
+    TRY(dev_alloc(c, &c.slot_of_rep, c.R));
+    TRY(dev_alloc(c, &c.rep_of_slot, c.R));
+    if (c.model == ETHER_MODEL_ISING) {
+        TRY(dev_alloc(c, &c.thr, (size_t)c.R * c.table_entries));
+        TRY(dev_alloc(c, &c.always, (size_t)c.R * c.table_entries));
+    }
+    TRY(dev_alloc(c, &c.stream_id, c.R));
+    TRY(dev_alloc(c, &c.step, c.R));
+    TRY(dev_alloc(c, &c.ovrr_step, c.R));
+    TRY(dev_alloc(c, &c.fresh_call, c.R));
+    TRY(dev_alloc(c, &c.acc_count, c.R));
+    TRY(dev_alloc(c, &c.E, 2 * (size_t)c.R));
+    TRY(dev_alloc(c, &c.M, 3 * (size_t)c.R));
+    TRY(dev_alloc(c, &c.sums, 7 * (size_t)c.R));
+    c.partial_blocks = energy_blocks(c);
+    TRY(dev_alloc(c, &c.partials, (size_t)c.R * c.partial_blocks * 5));
+    TRY(dev_alloc(c, &c.pt_accepts, 1));
+    TRY(dev_alloc(c, &c.copy_from, c.R));
+#undef TRY
+    std::vector<uint32_t> sid(c.R);
+    std::iota(sid.begin(), sid.end(), 0u);
+    CUDA_TRY(cudaMemcpy(c.stream_id, sid.data(), sizeof(uint32_t) * c.R, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemset(c.step, 0, sizeof(uint32_t) * c.R));
+    CUDA_TRY(cudaMemset(c.ovrr_step, 0, sizeof(uint32_t) * c.R));
+    CUDA_TRY(cudaMemset(c.fresh_call, 0, sizeof(uint32_t) * c.R));
+    CUDA_TRY(cudaMemset(c.acc_count, 0, sizeof(unsigned long long) * c.R));
+    CUDA_TRY(cudaMemset(c.sums, 0, sizeof(double) * 7 * c.R));
+    CUDA_TRY(cudaMemset(c.E, 0, sizeof(double) * 2 * c.R));
+    CUDA_TRY(cudaMemset(c.M, 0, sizeof(double) * 3 * c.R));
+    c.n_slots = c.R;
+    c.n_groups = 1;
+    c.beta_slots.assign(c.R, 0.0);
+    c.beta_set = false;
+    *out = h;
+    int src = ether_set_spins(h, -1, d->ion);
+    if (src) {
+        *out = nullptr;
+        return bail(src);
+    }
+    return ETHER_OK;
+}
+
+extern "C" int ether_destroy(ether_ctx *h) {
+    if (!h) return ETHER_OK;
+    cudaStreamSynchronize(h->c.stream);
+    free_ctx(h->c);
+    delete h;
+    return ETHER_OK;
+}
+
+extern "C" int ether_set_beta(ether_ctx *h, const double *beta) {
+    if (!h || !beta) return fail(ETHER_ERR_ARG, "null argument");
+    Ctx &c = h->c;
+    for (int r = 0; r < c.R; ++r)
+        if (!std::isfinite(beta[r])) return fail(ETHER_ERR_ARG, "beta is not finite for replica " + std::to_string(r));
+    c.n_slots = c.R;
+    c.n_groups = 1;
+    c.beta_slots.assign(beta, beta + c.R);
+    return upload_ladder(c);
+}
+
+extern "C" int ether_set_ladder(ether_ctx *h, int32_t n_slots, const double *beta_slots) {
+    if (!h || !beta_slots) return fail(ETHER_ERR_ARG, "null argument");
+    Ctx &c = h->c;
+    if (n_slots <= 0 || c.R % n_slots != 0) return fail(ETHER_ERR_ARG, "n_slots must divide the replica count");
+    for (int s = 0; s < n_slots; ++s)
+        if (!std::isfinite(beta_slots[s])) return fail(ETHER_ERR_ARG, "beta is not finite for slot " + std::to_string(s));
+    c.n_slots = n_slots;
+    c.n_groups = c.R / n_slots;
+    c.beta_slots.assign(beta_slots, beta_slots + n_slots);
+    return upload_ladder(c);
+}
+
+extern "C" int ether_set_streams(ether_ctx *h, const uint32_t *stream, const uint32_t *step) {
+    if (!h) return fail(ETHER_ERR_ARG, "null context");
+    Ctx &c = h->c;
+    if (stream) CUDA_TRY(cudaMemcpyAsync(c.stream_id, stream, sizeof(uint32_t) * c.R, cudaMemcpyHostToDevice, c.stream));
+    if (step) CUDA_TRY(cudaMemcpyAsync(c.step, step, sizeof(uint32_t) * c.R, cudaMemcpyHostToDevice, c.stream));
+    CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return ETHER_OK;
+}
+
+extern "C" int ether_set_spins(ether_ctx *h, int32_t replica, const double *ion) {
+    if (!h || !ion) return fail(ETHER_ERR_ARG, "null argument");
+    Ctx &c = h->c;
+    if (replica < -1 || replica >= c.R) return fail(ETHER_ERR_ARG, "replica out of range");
+    const int N = c.N;
+    if (c.model == ETHER_MODEL_ISING) {
+        std::vector<uint8_t> v(N);
+        for (int i = 0; i < N; ++i) v[c.storage[i]] = ion[3 + 9 * (size_t)i] > 0.0 ? 1 : 0;
+        for (int r = (replica < 0 ? 0 : replica); r < (replica < 0 ? c.R : replica + 1); ++r)
+            CUDA_TRY(cudaMemcpyAsync(c.spins + (size_t)r * N, v.data(), N, cudaMemcpyHostToDevice, c.stream));
+        CUDA_TRY(cudaStreamSynchronize(c.stream));
+    } else {
+        std::vector<float4> v(N);
+        for (int i = 0; i < N; ++i) {
+            const double *p = ion + 9 * (size_t)i;
+            v[c.storage[i]] = make_float4((float)p[1], (float)p[2], (float)p[3], (float)p[5]);
+        }
+        for (int r = (replica < 0 ? 0 : replica); r < (replica < 0 ? c.R : replica + 1); ++r)
+            CUDA_TRY(cudaMemcpyAsync(c.spins4 + (size_t)r * N, v.data(), sizeof(float4) * N, cudaMemcpyHostToDevice, c.stream));
+        CUDA_TRY(cudaStreamSynchronize(c.stream));
+    }
+    return ETHER_OK;
+}
+
+extern "C" int ether_get_spins(ether_ctx *h, int32_t replica, double *ion) {
+    if (!h || !ion) return fail(ETHER_ERR_ARG, "null argument");
+    Ctx &c = h->c;
+    if (replica < -1 || replica >= c.R) return fail(ETHER_ERR_ARG, "replica out of range");
+    if (replica < 0) replica = 0;
+    const int N = c.N;
+    if (c.model == ETHER_MODEL_ISING) {
+        std::vector<uint8_t> v(N);
+        CUDA_TRY(cudaMemcpyAsync(v.data(), c.spins + (size_t)replica * N, N, cudaMemcpyDeviceToHost, c.stream));
+        CUDA_TRY(cudaStreamSynchronize(c.stream));
+        for (int i = 0; i < N; ++i) ion[3 + 9 * (size_t)i] = v[c.storage[i]] ? 1.0 : -1.0;
+    } else {
+        std::vector<float4> v(N);
+        CUDA_TRY(cudaMemcpyAsync(v.data(), c.spins4 + (size_t)replica * N, sizeof(float4) * N, cudaMemcpyDeviceToHost, c.stream));
+        CUDA_TRY(cudaStreamSynchronize(c.stream));
+        for (int i = 0; i < N; ++i) {
+            double *p = ion + 9 * (size_t)i;
+            const float4 q = v[c.storage[i]];
+            p[1] = q.x; p[2] = q.y; p[3] = q.z; p[5] = q.w;
+        }
+    }
+    return ETHER_OK;
+}
+
+extern "C" int ether_fresh_spins(ether_ctx *h) {
+    if (!h) return fail(ETHER_ERR_ARG, "null context");
+    Ctx &c = h->c;
+    CUDA_TRY(launch_fresh(c));
+    CUDA_TRY(launch_advance(c, c.fresh_call));
+    return ETHER_OK;
+}
+
+static int sweep_once(Ctx &c) {
+    for (int col = 0; col < c.ncol; ++col) {
+        if (c.model == ETHER_MODEL_ISING) CUDA_TRY(launch_ising_sweep(c, col));
+        else CUDA_TRY(launch_xyz_sweep(c, col));
+    }
+    CUDA_TRY(launch_advance(c, c.step));
+    return ETHER_OK;
+}
+
+extern "C" int ether_metropolis(ether_ctx *h, int32_t nsweeps, double *accept) {
+    if (!h) return fail(ETHER_ERR_ARG, "null context");
+    Ctx &c = h->c;
+    if (nsweeps < 0) return fail(ETHER_ERR_ARG, "negative sweep count");
+    if (!c.beta_set) return fail(ETHER_ERR_STATE, "beta not set (ether_set_beta / ether_set_ladder)");
+    std::vector<unsigned long long> before, after;
+    if (accept) {
+        before.resize(c.R);
+        CUDA_TRY(cudaMemcpyAsync(before.data(), c.acc_count, sizeof(unsigned long long) * c.R, cudaMemcpyDeviceToHost, c.stream));
+    }
+    for (int k = 0; k < nsweeps; ++k) {
+        int rc = sweep_once(c);
+        if (rc) return rc;
+    }
+    if (accept) {
+        after.resize(c.R);
+        CUDA_TRY(cudaMemcpyAsync(after.data(), c.acc_count, sizeof(unsigned long long) * c.R, cudaMemcpyDeviceToHost, c.stream));
+        CUDA_TRY(cudaStreamSynchronize(c.stream));
+        for (int r = 0; r < c.R; ++r) accept[r] = (double)(after[r] - before[r]) / c.N;
+    }
+    return ETHER_OK;
+}
+
+static int overrelax_once(Ctx &c, double para) {
+    const int full = (int)std::floor(para);
+    const float part = (float)(para - full);
+    const int npass = full + (part > 0.0f ? 1 : 0);
+    for (int p = 0; p < npass; ++p)
+        for (int col = 0; col < c.ncol; ++col) CUDA_TRY(launch_overrelax(c, col, p, p < full ? 1.0f : part));
+    CUDA_TRY(launch_advance(c, c.ovrr_step));
+    return ETHER_OK;
+}
+
+extern "C" int ether_overrelaxation(ether_ctx *h, double ovrr_para) {
+    if (!h) return fail(ETHER_ERR_ARG, "null context");
+    Ctx &c = h->c;
+    if (c.model != ETHER_MODEL_XYZ) return fail(ETHER_ERR_ARG, "overrelaxation needs the XYZ model");
+    if (!(ovrr_para >= 0.0) || ovrr_para > 1000.0) return fail(ETHER_ERR_ARG, "ovrr_para out of range");
+    return overrelax_once(c, ovrr_para);
+}
+
+extern "C" int ether_tot_energy(ether_ctx *h, double *E) {
+    if (!h) return fail(ETHER_ERR_ARG, "null context");
+    Ctx &c = h->c;
+    CUDA_TRY(launch_energy_mag(c, true));
+    if (E) {
+        CUDA_TRY(cudaMemcpyAsync(E, c.E, sizeof(double) * c.R, cudaMemcpyDeviceToHost, c.stream));
+        CUDA_TRY(cudaStreamSynchronize(c.stream));
+    }
+    return ETHER_OK;
+}
+
+extern "C" int ether_tot_magnetisation(ether_ctx *h, double *M) {
+    if (!h) return fail(ETHER_ERR_ARG, "null context");
+    Ctx &c = h->c;
+    CUDA_TRY(launch_energy_mag(c, false));
+    if (M) {
+        CUDA_TRY(cudaMemcpyAsync(M, c.M, sizeof(double) * 3 * c.R, cudaMemcpyDeviceToHost, c.stream));
+        CUDA_TRY(cudaStreamSynchronize(c.stream));
+    }
+    return ETHER_OK;
+}
+
+extern "C" int ether_observable(ether_ctx *h, int32_t step, int32_t tmcs_eq, int32_t coa) {
+    if (!h) return fail(ETHER_ERR_ARG, "null context");
+    if (coa <= 0) return fail(ETHER_ERR_ARG, "coa must be positive");
+    Ctx &c = h->c;
+    if (step > tmcs_eq && step % coa == 0) {
+        CUDA_TRY(launch_energy_mag(c, true));
+        CUDA_TRY(launch_measure(c));
+    }
+    return ETHER_OK;
+}
+
+extern "C" int ether_zero_avg(ether_ctx *h) {
+    if (!h) return fail(ETHER_ERR_ARG, "null context");
+    Ctx &c = h->c;
+    CUDA_TRY(cudaMemsetAsync(c.sums, 0, sizeof(double) * 7 * c.R, c.stream));
+    return ETHER_OK;
+}
+
+extern "C" int ether_get_sums(ether_ctx *h, double *sums) {
+    if (!h || !sums) return fail(ETHER_ERR_ARG, "null argument");
+    Ctx &c = h->c;
+    CUDA_TRY(cudaMemcpyAsync(sums, c.sums, sizeof(double) * 7 * c.R, cudaMemcpyDeviceToHost, c.stream));
+    CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return ETHER_OK;
+}
+
+// get_eng('avg_eng') (src/get_eng.f90:42-60) and get_mag('avg_mag') (src/get_mag.f90:43-59).
+extern "C" int ether_avg(ether_ctx *h, double *out) {
+    if (!h || !out) return fail(ETHER_ERR_ARG, "null argument");
+    Ctx &c = h->c;
+    std::vector<double> s(7 * (size_t)c.R);
+    int rc = ether_get_sums(h, s.data());
+    if (rc) return rc;
+    for (int g = 0; g < c.n_groups; ++g)
+        for (int sl = 0; sl < c.n_slots; ++sl) {
+            const size_t idx = (size_t)g * c.n_slots + sl;
+            const double *a = s.data() + 7 * idx;
+            const double beta = c.beta_slots[sl];
+            const double n = a[0];
+            const double e = a[1] / n, e2 = a[2] / n, e4 = a[3] / n;
+            const double m = a[4] / n, m2 = a[5] / n, m4 = a[6] / n;
+            double *o = out + 6 * idx;
+            o[0] = e;
+            o[1] = 1.0 - (1.0 / 3.0) * (e4 / (e2 * e2));
+            o[2] = (beta * beta) * (e2 - e * e) * c.N;
+            o[3] = m;
+            o[4] = 1.0 - (1.0 / 3.0) * (m4 / (m2 * m2));
+            o[5] = beta * (m2 - m * m) * c.N;
+        }
+    return ETHER_OK;
+}
+
+// observables_per_repeat (src/observables_per_repeat.f90:29-69) across the REPEAT groups.
+extern "C" int ether_per_repeat(ether_ctx *h, double *mean, double *err) {
+    if (!h || !mean || !err) return fail(ETHER_ERR_ARG, "null argument");
+    Ctx &c = h->c;
+    if (c.n_groups < 2) return fail(ETHER_ERR_STATE, "per-repeat statistics need at least two REPEAT groups");
+    std::vector<double> v(6 * (size_t)c.R);
+    int rc = ether_avg(h, v.data());
+    if (rc) return rc;
+    const double rep = c.n_groups;
+    const double r1 = 1.0 / (rep * (rep - 1.0));
+    for (int sl = 0; sl < c.n_slots; ++sl)
+        for (int q = 0; q < 6; ++q) {
+            double sum = 0.0;
+            for (int g = 0; g < c.n_groups; ++g) sum += v[6 * ((size_t)g * c.n_slots + sl) + q];
+            const double mu = sum / rep;
+            double e = 0.0;
+            for (int g = 0; g < c.n_groups; ++g) {
+                const double d = v[6 * ((size_t)g * c.n_slots + sl) + q] - mu;
+                e += d * d;
+            }
+            mean[6 * sl + q] = mu;
+            err[6 * sl + q] = std::sqrt(r1 * e);
+        }
+    return ETHER_OK;
+}
+
+extern "C" int ether_parallel_tempering(ether_ctx *h, int32_t swap_count, int32_t *accepted) {
+    if (!h) return fail(ETHER_ERR_ARG, "null context");
+    Ctx &c = h->c;
+    if (!c.beta_set) return fail(ETHER_ERR_STATE, "beta not set");
+    CUDA_TRY(launch_energy_mag(c, true));
+    CUDA_TRY(cudaMemsetAsync(c.pt_accepts, 0, sizeof(int32_t), c.stream));
+    CUDA_TRY(launch_pt(c, swap_count));
+    if (accepted) {
+        CUDA_TRY(cudaMemcpyAsync(accepted, c.pt_accepts, sizeof(int32_t), cudaMemcpyDeviceToHost, c.stream));
+        CUDA_TRY(cudaStreamSynchronize(c.stream));
+    }
+    return ETHER_OK;
+}
+
+extern "C" int ether_get_slots(ether_ctx *h, int32_t *slot_of_replica) {
+    if (!h || !slot_of_replica) return fail(ETHER_ERR_ARG, "null argument");
+    Ctx &c = h->c;
+    CUDA_TRY(cudaMemcpyAsync(slot_of_replica, c.slot_of_rep, sizeof(int32_t) * c.R, cudaMemcpyDeviceToHost, c.stream));
+    CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return ETHER_OK;
+}
+
+extern "C" int ether_mcs(ether_ctx *h, const ether_schedule *sch, int32_t step0, int32_t nsteps,
+                         int32_t *swap_count) {
+    if (!h || !sch) return fail(ETHER_ERR_ARG, "null argument");
+    Ctx &c = h->c;
+    if (!c.beta_set) return fail(ETHER_ERR_STATE, "beta not set");
+    if (sch->coa <= 0 || nsteps < 0) return fail(ETHER_ERR_ARG, "coa must be positive and nsteps >= 0");
+    const bool ovrr_on = sch->ovrr && c.model == ETHER_MODEL_XYZ && !c.zeeman && !c.sia && sch->ovrr_mcs > 0;
+    const bool pt_on = sch->pt && sch->exchange_interval > 0;
+    int32_t sc = swap_count ? *swap_count : 0;
+    for (int step = step0 + 1; step <= step0 + nsteps; ++step) {
+        if (ovrr_on && step % sch->ovrr_mcs == 0 && step % sch->coa != 0) {
+            int rc = overrelax_once(c, sch->ovrr_para);
+            if (rc) return rc;
+        }
+        int rc = sweep_once(c);
+        if (rc) return rc;
+        if (pt_on && step % sch->exchange_interval == 0 && step % sch->coa != 0) {
+            ++sc;
+            CUDA_TRY(launch_energy_mag(c, true));
+            CUDA_TRY(launch_pt(c, sc));
+        }
+        if (step > sch->tmcs_eq && step % sch->coa == 0) {
+            CUDA_TRY(launch_energy_mag(c, true));
+            CUDA_TRY(launch_measure(c));
+        }
+    }
+    if (swap_count) *swap_count = sc;
+    return ETHER_OK;
+}
+
+extern "C" int ether_get_accept_counts(ether_ctx *h, uint64_t *counts) {
+    if (!h || !counts) return fail(ETHER_ERR_ARG, "null argument");
+    Ctx &c = h->c;
+    CUDA_TRY(cudaMemcpyAsync(counts, c.acc_count, sizeof(uint64_t) * c.R, cudaMemcpyDeviceToHost, c.stream));
+    CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return ETHER_OK;
+}
+
+extern "C" int ether_reset_accept_counts(ether_ctx *h) {
+    if (!h) return fail(ETHER_ERR_ARG, "null context");
+    Ctx &c = h->c;
+    CUDA_TRY(cudaMemsetAsync(c.acc_count, 0, sizeof(unsigned long long) * c.R, c.stream));
+    return ETHER_OK;
+}
+
+extern "C" int ether_get_info(ether_ctx *h, ether_info *info) {
+    if (!h || !info) return fail(ETHER_ERR_ARG, "null argument");
+    Ctx &c = h->c;
+    info->n_colours = c.ncol;
+    info->fast_path = c.fast ? 1 : 0;
+    info->n_types = c.n_types;
+    info->table_entries = c.table_entries;
+    info->n_slots = c.n_slots;
+    info->n_groups = c.n_groups;
+    info->device_bytes = c.device_bytes;
+    info->kernel_launches = c.launches;
+    return ETHER_OK;
+}
+
+extern "C" int ether_get_colouring(ether_ctx *h, int32_t *colour, int32_t *rank_in_colour) {
+    if (!h) return fail(ETHER_ERR_ARG, "null context");
+    Ctx &c = h->c;
+    if (colour) std::copy(c.colour.begin(), c.colour.end(), colour);
+    if (rank_in_colour) std::copy(c.rank.begin(), c.rank.end(), rank_in_colour);
+    return ETHER_OK;
+}
+
+extern "C" int ether_sync(ether_ctx *h) {
+    if (!h) return fail(ETHER_ERR_ARG, "null context");
+    CUDA_TRY(cudaStreamSynchronize(h->c.stream));
+    return ETHER_OK;
+}
+
+extern "C" int ether_get_stream(ether_ctx *h, void **stream) {
+    if (!h || !stream) return fail(ETHER_ERR_ARG, "null argument");
+    *stream = (void *)h->c.stream;
+    return ETHER_OK;
+}
+
+extern "C" int ether_metropolis_phase(ether_ctx *h, int32_t colour) {
+    if (!h) return fail(ETHER_ERR_ARG, "null context");
+    Ctx &c = h->c;
+    if (!c.beta_set) return fail(ETHER_ERR_STATE, "beta not set");
+    if (colour < 0 || colour >= c.ncol) return fail(ETHER_ERR_ARG, "colour out of range");
+    if (c.model == ETHER_MODEL_ISING) CUDA_TRY(launch_ising_sweep(c, colour));
+    else CUDA_TRY(launch_xyz_sweep(c, colour));
+    return ETHER_OK;
+}
+
+extern "C" int ether_end_sweep(ether_ctx *h) {
+    if (!h) return fail(ETHER_ERR_ARG, "null context");
+    CUDA_TRY(launch_advance(h->c, h->c.step));
+    return ETHER_OK;
+}

@@ -1,0 +1,113 @@
+// internal.h -- context layout shared by the C-ABI implementation and the kernels.
+//
+// Device layout (all replicas of one context share the lattice tables):
+//   * Sites are stored colour-major: storage index s = col_off[colour[i]] + rank_in_colour[i].
+//     For an even simple-cubic lattice this is the two-array checkerboard split
+//     (colour 0 = even x+y+z), and the rank inside a colour class is
+//     (z*L2 + y)*(L1/2) + x/2, so kernels address neighbours arithmetically.
+//   * Ising spins: uint8 0/1 (1 = Sz=+1), spins[r*N + s].  3 B of HBM traffic per update.
+//   * XYZ spins:  float4 (Sx, Sy, Sz, phi), spins4[r*N + s].  48 B per update.
+//   * Neighbours: CSR in storage order (row of s = its reference nn list, shells in
+//     order, neighbours in the reference's increasing-index order), values = storage
+//     indices; per slot a coupling index jidx = b*nsp*nsp + (si-1)*nsp + (sj-1) and, for
+//     Ising, a threshold-table stride.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/ether_gpu.h"
+
+namespace ether {
+
+constexpr int kMaxColours = 64;
+
+struct DevTables {
+    // lattice (storage order)
+    int32_t *row_ptr = nullptr;   // N+1
+    int32_t *nbr = nullptr;       // nnz, storage indices
+    uint16_t *jidx = nullptr;     // nnz
+    int32_t *wstride = nullptr;   // nnz (Ising table strides)
+    uint8_t *species = nullptr;   // N (1-based)
+    uint16_t *itype = nullptr;    // N (Ising table site type)
+    int32_t *type_base = nullptr; // n_types: offset of a type's table inside one slot's table
+    int32_t *type_half = nullptr; // n_types: entries per own-spin half
+    float *J = nullptr;           // nJ * 3 (FP32 couplings)
+    double *Jd = nullptr;         // nJ * 3 (FP64 couplings, Ising energy)
+    float *zee = nullptr;         // nsp * 3: -g mb s H
+    double *zeed = nullptr;       // nsp * 3
+    float *D = nullptr;           // nsp * 3 (SIA)
+    double *mweight = nullptr;    // N: stgg * s(species)
+    int32_t *site_of_storage = nullptr;  // N: 0-based site number of a storage index
+};
+
+struct Ctx {
+    // configuration
+    int N = 0, nsp = 0, nsh = 0, cap = 0, model = 0, angle = 0, zeeman = 0, sia = 0;
+    double dphi = 0, h[3] = {0, 0, 0}, g = 0, mb = 0;
+    int R = 0;
+    uint32_t seed = 0;
+    int flags = 0;
+    // colouring
+    int ncol = 0;
+    int col_off[kMaxColours + 1] = {0};
+    std::vector<int32_t> colour, rank, storage;  // per site (0-based index)
+    std::vector<int32_t> site_of_storage;
+    // fast simple-cubic path
+    bool fast = false;
+    int L[3] = {0, 0, 0};
+    int vec_bytes = 0;  // Ising bytes per thread in the SC kernel
+    // Ising tables
+    int n_types = 0, table_entries = 0;
+    std::vector<int32_t> h_type_base, h_type_half;
+    std::vector<std::vector<int>> type_groupcount;  // per type: neighbours per group
+    std::vector<int32_t> type_species;
+    std::vector<double> s_len;     // spin length per species
+    std::vector<float> h_Jf;       // nJ * 3 FP32 couplings (host copy)
+    std::vector<double> h_Jd;      // nJ * 3 FP64 couplings
+    // PT ladder
+    int n_slots = 0, n_groups = 1;
+    std::vector<double> beta_slots;  // n_slots
+    bool beta_set = false;
+    // device
+    cudaStream_t stream = nullptr;
+    DevTables t;
+    uint8_t *spins = nullptr;    // Ising
+    float4 *spins4 = nullptr;    // XYZ
+    double *beta_slot = nullptr; // n_slots
+    float *beta_slot_f = nullptr;
+    int32_t *slot_of_rep = nullptr;  // R (slot within group)
+    int32_t *rep_of_slot = nullptr;  // R (group*n_slots + slot -> replica)
+    uint32_t *thr = nullptr;     // n_slots * table_entries
+    uint8_t *always = nullptr;   // n_slots * table_entries
+    uint32_t *stream_id = nullptr;  // R
+    uint32_t *step = nullptr;       // R (Metropolis sweep counter)
+    uint32_t *ovrr_step = nullptr;  // R
+    uint32_t *fresh_call = nullptr; // R
+    unsigned long long *acc_count = nullptr;  // R
+    double *E = nullptr;         // 2R: raw energy, exchange part
+    double *M = nullptr;         // 3R
+    double *sums = nullptr;      // 7R (per group*n_slots + slot)
+    double *partials = nullptr;  // scratch for reductions
+    int partial_blocks = 0;
+    int32_t *pt_accepts = nullptr;  // 1
+    int32_t *copy_from = nullptr;   // R (reference-copy PT mode)
+    size_t device_bytes = 0;
+    uint64_t launches = 0;
+    int sm_count = 0;
+};
+
+// kernel launchers (k_*.cu)
+cudaError_t launch_ising_sweep(Ctx &c, int colour);
+cudaError_t launch_xyz_sweep(Ctx &c, int colour);
+cudaError_t launch_overrelax(Ctx &c, int colour, int pass, float part);
+cudaError_t launch_fresh(Ctx &c);
+cudaError_t launch_advance(Ctx &c, uint32_t *counter);
+cudaError_t launch_energy_mag(Ctx &c, bool want_energy);
+cudaError_t launch_measure(Ctx &c);
+cudaError_t launch_pt(Ctx &c, int swap_count);
+int energy_blocks(const Ctx &c);
+void set_error(const std::string &msg);
+
+}  // namespace ether

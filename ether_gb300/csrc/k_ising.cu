@@ -1,0 +1,227 @@
+// k_ising.cu -- Ising Metropolis colour phases (src/Metropolis.f90:39-62 with the
+// Ising branch of update_spin_details.f90:34-35 and Hamiltonian.f90:34-52).
+//
+// Decision: accept iff ΔE <= 0 or u32 < thr, with thr = ceil(2^32 exp(-β ΔE)) taken from a
+// per-temperature table indexed by (site type, own spin, up-neighbour counts per
+// (shell, neighbour species) group).  The table is built in FP64 on the host, so the
+// kernels do integer work only: byte loads, byte sums, one Philox call per 4 sites.
+#include "internal.h"
+#include "rng_math.cuh"
+
+namespace ether {
+
+__device__ __forceinline__ void warp_add_count(unsigned long long *dst, unsigned v) {
+    unsigned s = __reduce_add_sync(0xffffffffu, v);
+    if ((threadIdx.x & 31) == 0 && s) atomicAdd(dst, (unsigned long long)s);
+}
+
+// ------------------------------------------------------------------ general lattice ----
+// One thread = 4 consecutive sites of the colour class (one Philox block).
+__global__ void __launch_bounds__(256)
+ising_csr_kernel(uint8_t *__restrict__ spins, int N, int col_off, int n_c, uint32_t colour,
+                 const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ nbr,
+                 const int32_t *__restrict__ wstride, const uint16_t *__restrict__ itype,
+                 const int32_t *__restrict__ type_base, const int32_t *__restrict__ type_half,
+                 const uint32_t *__restrict__ thr, const uint8_t *__restrict__ always,
+                 int table_entries, const int32_t *__restrict__ slot_of_rep,
+                 const uint32_t *__restrict__ stream_id, const uint32_t *__restrict__ step,
+                 uint32_t seed, unsigned long long *__restrict__ acc_count) {
+    const int r = blockIdx.y;
+    uint8_t *sp = spins + (size_t)r * N;
+    const int slot = slot_of_rep[r];
+    const uint32_t *tb = thr + (size_t)slot * table_entries;
+    const uint8_t *al = always + (size_t)slot * table_entries;
+    const uint32_t k1 = stream_id[r], t = step[r];
+    const uint32_t c3 = kMetro | (colour << 8);
+    const int ng = (n_c + 3) >> 2;
+    unsigned acc = 0;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
+        U4 o = philox((uint32_t)g, t, 0u, c3, seed, k1);
+        uint32_t w[4] = {o.x, o.y, o.z, o.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            int rho = 4 * g + q;
+            if (rho >= n_c) break;
+            int s = col_off + rho;
+            int idx = 0;
+            for (int k = row_ptr[s]; k < row_ptr[s + 1]; ++k) idx += wstride[k] * (int)sp[nbr[k]];
+            int own = sp[s];
+            int ty = itype[s];
+            int e = type_base[ty] + own * type_half[ty] + idx;
+            if (al[e] || w[q] < tb[e]) {
+                sp[s] = (uint8_t)(own ^ 1);
+                ++acc;
+            }
+        }
+    }
+    warp_add_count(acc_count + r, acc);
+}
+
+// ------------------------------------------------------- simple cubic, colour-split ----
+// Colour c array: rho = (z*L2 + y)*H + xh, H = L1/2, site x = 2*xh + ((y+z+c)&1).
+// All six neighbours live in the other colour's array: same xh in rows (y±1,z), (y,z±1),
+// and xh, xh∓1 in row (y,z).  A thread takes W consecutive bytes of one row; byte sums
+// of 0/1 spins never carry (max 6).
+template <int W>
+struct Vec;
+template <>
+struct Vec<4> { uint32_t w[1]; };
+template <>
+struct Vec<8> { uint32_t w[2]; };
+template <>
+struct Vec<16> { uint32_t w[4]; };
+
+template <int W>
+__device__ __forceinline__ Vec<W> ldv(const uint8_t *p) {
+    Vec<W> v;
+    if constexpr (W == 4) {
+        v.w[0] = *reinterpret_cast<const uint32_t *>(p);
+    } else if constexpr (W == 8) {
+        uint2 q = *reinterpret_cast<const uint2 *>(p);
+        v.w[0] = q.x; v.w[1] = q.y;
+    } else {
+        uint4 q = *reinterpret_cast<const uint4 *>(p);
+        v.w[0] = q.x; v.w[1] = q.y; v.w[2] = q.z; v.w[3] = q.w;
+    }
+    return v;
+}
+template <int W>
+__device__ __forceinline__ void stv(uint8_t *p, const Vec<W> &v) {
+    if constexpr (W == 4) {
+        *reinterpret_cast<uint32_t *>(p) = v.w[0];
+    } else if constexpr (W == 8) {
+        *reinterpret_cast<uint2 *>(p) = make_uint2(v.w[0], v.w[1]);
+    } else {
+        *reinterpret_cast<uint4 *>(p) = make_uint4(v.w[0], v.w[1], v.w[2], v.w[3]);
+    }
+}
+
+template <int W>
+__global__ void __launch_bounds__(256)
+ising_sc_kernel(uint8_t *__restrict__ spins, int L1, int L2, int L3, uint32_t colour,
+                const uint32_t *__restrict__ thr, const uint8_t *__restrict__ always,
+                int table_entries, const int32_t *__restrict__ slot_of_rep,
+                const uint32_t *__restrict__ stream_id, const uint32_t *__restrict__ step,
+                uint32_t seed, unsigned long long *__restrict__ acc_count) {
+    constexpr int NW = W / 4;
+    const int r = blockIdx.y;
+    const int H = L1 >> 1;
+    const int half = H * L2 * L3;
+    uint8_t *own_a = spins + (size_t)r * 2 * half + (size_t)colour * half;
+    const uint8_t *opp = spins + (size_t)r * 2 * half + (size_t)(colour ^ 1u) * half;
+    __shared__ uint32_t s_thr[16];
+    __shared__ uint32_t s_alw;
+    if (threadIdx.x < 14) {
+        int slot = slot_of_rep[r];
+        s_thr[threadIdx.x] = thr[(size_t)slot * table_entries + threadIdx.x];
+    }
+    if (threadIdx.x == 0) {
+        int slot = slot_of_rep[r];
+        uint32_t m = 0;
+        for (int e = 0; e < 14; ++e) m |= (uint32_t)(always[(size_t)slot * table_entries + e] != 0) << e;
+        s_alw = m;
+    }
+    __syncthreads();
+    const uint32_t alw = s_alw;
+    const uint32_t k1 = stream_id[r], t = step[r];
+    const uint32_t c3 = kMetro | (colour << 8);
+    const int nvec = half / W;
+    unsigned acc = 0;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nvec; v += gridDim.x * blockDim.x) {
+        const int rho0 = v * W;
+        const int row = rho0 / H;
+        const int xh0 = rho0 - row * H;
+        const int y = row % L2, z = row / L2;
+        const int p = (y + z + (int)colour) & 1;
+        const int ym = (y == 0 ? L2 - 1 : y - 1), yp = (y == L2 - 1 ? 0 : y + 1);
+        const int zm = (z == 0 ? L3 - 1 : z - 1), zp = (z == L3 - 1 ? 0 : z + 1);
+        Vec<W> me = ldv<W>(own_a + rho0);
+        Vec<W> o0 = ldv<W>(opp + rho0);
+        Vec<W> a = ldv<W>(opp + (size_t)(z * L2 + ym) * H + xh0);
+        Vec<W> b = ldv<W>(opp + (size_t)(z * L2 + yp) * H + xh0);
+        Vec<W> c = ldv<W>(opp + (size_t)(zm * L2 + y) * H + xh0);
+        Vec<W> d = ldv<W>(opp + (size_t)(zp * L2 + y) * H + xh0);
+        Vec<W> sh;
+        if (p == 0) {  // neighbour x-1 -> xh-1: shift the row window up by one byte
+            uint32_t edge = opp[(size_t)row * H + (xh0 == 0 ? H - 1 : xh0 - 1)];
+#pragma unroll
+            for (int q = NW - 1; q >= 0; --q) {
+                uint32_t lo = (q == 0) ? edge : (o0.w[q - 1] >> 24);
+                sh.w[q] = (o0.w[q] << 8) | lo;
+            }
+        } else {       // neighbour x+1 -> xh+1: shift down by one byte
+            uint32_t edge = opp[(size_t)row * H + (xh0 + W == H ? 0 : xh0 + W)];
+#pragma unroll
+            for (int q = 0; q < NW; ++q) {
+                uint32_t hi = (q == NW - 1) ? edge : (o0.w[q + 1] & 0xFFu);
+                sh.w[q] = (o0.w[q] >> 8) | (hi << 24);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < NW; ++q) {
+            uint32_t n = o0.w[q] + sh.w[q] + a.w[q] + b.w[q] + c.w[q] + d.w[q];
+            U4 rnd = philox((uint32_t)((rho0 >> 2) + q), t, 0u, c3, seed, k1);
+            uint32_t u[4] = {rnd.x, rnd.y, rnd.z, rnd.w};
+            uint32_t out = me.w[q];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                uint32_t nk = (n >> (8 * k)) & 0xFFu;
+                uint32_t sk = (me.w[q] >> (8 * k)) & 0xFFu;
+                uint32_t e = nk + 7u * sk;
+                uint32_t accept = ((alw >> e) & 1u) | (u[k] < s_thr[e] ? 1u : 0u);
+                out ^= accept << (8 * k);
+                acc += accept;
+            }
+            me.w[q] = out;
+        }
+        stv<W>(own_a + rho0, me);
+    }
+    warp_add_count(acc_count + r, acc);
+}
+
+static int blocks_for(const Ctx &c, long work, int bs) {
+    long need = (work + bs - 1) / bs;
+    long cap = (long)c.sm_count * 8 / (c.R > 0 ? c.R : 1);
+    if (cap < 1) cap = 1;
+    if (need > cap) need = cap;
+    if (need < 1) need = 1;
+    return (int)need;
+}
+
+cudaError_t launch_ising_sweep(Ctx &c, int colour) {
+    const int bs = 256;
+    if (c.fast) {
+        const int half = c.N / 2;
+        const int nvec = half / c.vec_bytes;
+        dim3 grid(blocks_for(c, nvec, bs), c.R);
+        switch (c.vec_bytes) {
+            case 16:
+                ising_sc_kernel<16><<<grid, bs, 0, c.stream>>>(
+                    c.spins, c.L[0], c.L[1], c.L[2], (uint32_t)colour, c.thr, c.always,
+                    c.table_entries, c.slot_of_rep, c.stream_id, c.step, c.seed, c.acc_count);
+                break;
+            case 8:
+                ising_sc_kernel<8><<<grid, bs, 0, c.stream>>>(
+                    c.spins, c.L[0], c.L[1], c.L[2], (uint32_t)colour, c.thr, c.always,
+                    c.table_entries, c.slot_of_rep, c.stream_id, c.step, c.seed, c.acc_count);
+                break;
+            default:
+                ising_sc_kernel<4><<<grid, bs, 0, c.stream>>>(
+                    c.spins, c.L[0], c.L[1], c.L[2], (uint32_t)colour, c.thr, c.always,
+                    c.table_entries, c.slot_of_rep, c.stream_id, c.step, c.seed, c.acc_count);
+                break;
+        }
+    } else {
+        const int n_c = c.col_off[colour + 1] - c.col_off[colour];
+        if (n_c == 0) return cudaSuccess;
+        dim3 grid(blocks_for(c, (n_c + 3) / 4, bs), c.R);
+        ising_csr_kernel<<<grid, bs, 0, c.stream>>>(
+            c.spins, c.N, c.col_off[colour], n_c, (uint32_t)colour, c.t.row_ptr, c.t.nbr,
+            c.t.wstride, c.t.itype, c.t.type_base, c.t.type_half, c.thr, c.always,
+            c.table_entries, c.slot_of_rep, c.stream_id, c.step, c.seed, c.acc_count);
+    }
+    c.launches++;
+    return cudaGetLastError();
+}
+
+}  // namespace ether

@@ -1,0 +1,238 @@
+// k_obs.cu -- energy / magnetisation reductions (src/get_tot_energy.f90:33-47,
+// src/get_tot_magnetisation.f90:32-40), the observable accumulators (src/observable.f90,
+// src/get_eng.f90:36-40, src/get_mag.f90:36-41) and parallel tempering
+// (src/parallel_tempering.f90:39-108).
+//
+// Site energies are FP32 (XYZ) or exact FP64 sums of ±J (Ising); every per-replica total
+// and every accumulator is FP64.  Reductions write per-block partials to scratch memory
+// and a second kernel adds them in a fixed order, so results do not depend on timing.
+#include "internal.h"
+#include "rng_math.cuh"
+
+namespace ether {
+
+constexpr int kRedBs = 256;
+constexpr int kNq = 5;  // E_raw, E_exchange, Mx, My, Mz
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__global__ void __launch_bounds__(kRedBs)
+energy_mag_kernel(const uint8_t *__restrict__ spins, const float4 *__restrict__ spins4, int N,
+                  int model, int zeeman, int sia, const int32_t *__restrict__ row_ptr,
+                  const int32_t *__restrict__ nbr, const uint16_t *__restrict__ jidx,
+                  const float *__restrict__ J, const double *__restrict__ Jd,
+                  const uint8_t *__restrict__ species, const float *__restrict__ zee,
+                  const double *__restrict__ zeed, const float *__restrict__ D,
+                  const double *__restrict__ mweight, double *__restrict__ partials) {
+    const int r = blockIdx.y;
+    double q[kNq] = {0, 0, 0, 0, 0};
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += gridDim.x * blockDim.x) {
+        const double w = mweight[s];
+        if (model == 0) {
+            const uint8_t *sp = spins + (size_t)r * N;
+            const double si = sp[s] ? 1.0 : -1.0;
+            double e = 0.0;
+            for (int k = row_ptr[s]; k < row_ptr[s + 1]; ++k) {
+                double sj = sp[nbr[k]] ? 1.0 : -1.0;
+                e += (si * sj) * Jd[3 * jidx[k] + 2];
+            }
+            q[1] += e;
+            if (zeeman) e += si * zeed[3 * (species[s] - 1) + 2];
+            q[0] += e;
+            q[4] += w * si;
+        } else {
+            const float4 *sp = spins4 + (size_t)r * N;
+            const float4 S = sp[s];
+            float hx = 0.f, hy = 0.f, hz = 0.f;
+            for (int k = row_ptr[s]; k < row_ptr[s + 1]; ++k) {
+                float4 Sj = sp[nbr[k]];
+                const float *Jp = J + 3 * jidx[k];
+                hx = fmaf(Jp[0], Sj.x, hx);
+                hy = fmaf(Jp[1], Sj.y, hy);
+                hz = fmaf(Jp[2], Sj.z, hz);
+            }
+            float e = S.x * hx;
+            e = fmaf(S.y, hy, e);
+            e = fmaf(S.z, hz, e);
+            q[1] += (double)e;
+            if (zeeman || sia) {
+                const int si = species[s] - 1;
+                if (zeeman) {
+                    const float *z = zee + 3 * si;
+                    e = fmaf(S.x, z[0], e);
+                    e = fmaf(S.y, z[1], e);
+                    e = fmaf(S.z, z[2], e);
+                }
+                if (sia) {
+                    const float *d = D + 3 * si;
+                    e = fmaf(d[0], S.x * S.x, e);
+                    e = fmaf(d[1], S.y * S.y, e);
+                    e = fmaf(d[2], S.z * S.z, e);
+                }
+            }
+            q[0] += (double)e;
+            q[2] += w * (double)S.x;
+            q[3] += w * (double)S.y;
+            q[4] += w * (double)S.z;
+        }
+    }
+    __shared__ double sm[kRedBs / 32][kNq];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < kNq; ++j) {
+        double v = warp_sum_d(q[j]);
+        if (lane == 0) sm[wid][j] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < kNq) {
+        double v = 0.0;
+        for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2) v += sm[w2][threadIdx.x];
+        partials[((size_t)r * gridDim.x + blockIdx.x) * kNq + threadIdx.x] = v;
+    }
+}
+
+// One block per replica: sums the partials in index order.
+__global__ void finish_energy_kernel(const double *__restrict__ partials, int nblk, int R,
+                                     double *__restrict__ E, double *__restrict__ M) {
+    const int r = blockIdx.x;
+    __shared__ double sm[kNq][128];
+    for (int j = 0; j < kNq; ++j) {
+        double v = 0.0;
+        for (int b = threadIdx.x; b < nblk; b += blockDim.x) v += partials[((size_t)r * nblk + b) * kNq + j];
+        sm[j][threadIdx.x] = v;
+    }
+    __syncthreads();
+    for (int w = 64; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w)
+            for (int j = 0; j < kNq; ++j) sm[j][threadIdx.x] += sm[j][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        E[r] = sm[0][0];
+        E[R + r] = sm[1][0];
+        M[3 * r + 0] = sm[2][0];
+        M[3 * r + 1] = sm[3][0];
+        M[3 * r + 2] = sm[4][0];
+    }
+}
+
+// get_eng('eng') / get_mag('mag') for every replica, into its (group, slot) accumulator.
+__global__ void measure_kernel(const double *__restrict__ E, const double *__restrict__ M, int N,
+                               int R, int n_slots, const int32_t *__restrict__ slot_of_rep,
+                               double *__restrict__ sums) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    const int idx = (r / n_slots) * n_slots + slot_of_rep[r];
+    const double e = E[r] / (2.0 * N);
+    const double mx = M[3 * r], my = M[3 * r + 1], mz = M[3 * r + 2];
+    const double m = sqrt(mx * mx + my * my + mz * mz) / N;
+    double *a = sums + (size_t)idx * 7;
+    a[0] += 1.0;
+    a[1] += e;
+    a[2] += e * e;
+    a[3] += (e * e) * (e * e);
+    a[4] += m;
+    a[5] += m * m;
+    a[6] += (m * m) * (m * m);
+}
+
+// parallel_tempering: one thread per (group, pair).  Exponent in FP64.
+__global__ void pt_kernel(const double *__restrict__ E, int R, int n_slots, int n_groups,
+                          const double *__restrict__ beta_slot, int32_t *__restrict__ rep_of_slot,
+                          int32_t *__restrict__ slot_of_rep, int32_t *__restrict__ copy_from,
+                          int swap_count, uint32_t seed, int true_energy, int copy_mode,
+                          int32_t *__restrict__ n_acc) {
+    const int npairs = n_slots / 2 + 1;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= npairs * n_groups) return;
+    const int g = tid / npairs, q = tid - g * npairs;
+    const int s = ((swap_count & 1) ? 1 : 0) + 2 * q;
+    if (s + 1 >= n_slots) return;
+    int32_t *ros = rep_of_slot + (size_t)g * n_slots;
+    const int lo = ros[s], hi = ros[s + 1];
+    double elo = E[lo], ehi = E[hi];
+    if (true_energy) {  // bonds once: E = E_ex/2 + (E_raw - E_ex)
+        elo = 0.5 * E[R + lo] + (E[lo] - E[R + lo]);
+        ehi = 0.5 * E[R + hi] + (E[hi] - E[R + hi]);
+    }
+    const double delta = -(beta_slot[s + 1] - beta_slot[s]) * (elo - ehi);
+    bool acc;
+    if (delta > 0.0) acc = true;
+    else {
+        U4 o = philox((uint32_t)s, (uint32_t)swap_count, 0u, kPT, seed, 0x50540000u + (uint32_t)g);
+        acc = ((double)o.x * 0x1p-32) < exp(delta);
+    }
+    if (!acc) return;
+    atomicAdd(n_acc, 1);
+    if (copy_mode) {
+        copy_from[hi] = lo;
+    } else {
+        ros[s] = hi;
+        ros[s + 1] = lo;
+        slot_of_rep[lo] = s + 1;
+        slot_of_rep[hi] = s;
+    }
+}
+
+// Reference-copy PT mode: replica r takes the configuration of replica copy_from[r].
+__global__ void pt_copy_kernel(uint8_t *__restrict__ spins, float4 *__restrict__ spins4, int N,
+                               int model, const int32_t *__restrict__ copy_from) {
+    const int r = blockIdx.y;
+    const int src = copy_from[r];
+    if (src < 0) return;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += gridDim.x * blockDim.x) {
+        if (model == 0) spins[(size_t)r * N + s] = spins[(size_t)src * N + s];
+        else spins4[(size_t)r * N + s] = spins4[(size_t)src * N + s];
+    }
+}
+
+int energy_blocks(const Ctx &c) {
+    long need = (c.N + kRedBs - 1) / kRedBs;
+    long cap = (long)c.sm_count * 4 / (c.R > 0 ? c.R : 1);
+    if (cap < 1) cap = 1;
+    if (need > cap) need = cap;
+    if (need > 4096) need = 4096;
+    return (int)(need < 1 ? 1 : need);
+}
+
+cudaError_t launch_energy_mag(Ctx &c, bool) {
+    const int nblk = c.partial_blocks;
+    dim3 grid(nblk, c.R);
+    energy_mag_kernel<<<grid, kRedBs, 0, c.stream>>>(
+        c.spins, c.spins4, c.N, c.model, c.zeeman, c.sia && c.model == 1, c.t.row_ptr, c.t.nbr,
+        c.t.jidx, c.t.J, c.t.Jd, c.t.species, c.t.zee, c.t.zeed, c.t.D, c.t.mweight, c.partials);
+    finish_energy_kernel<<<c.R, 128, 0, c.stream>>>(c.partials, nblk, c.R, c.E, c.M);
+    c.launches += 2;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_measure(Ctx &c) {
+    measure_kernel<<<(c.R + 127) / 128, 128, 0, c.stream>>>(c.E, c.M, c.N, c.R, c.n_slots,
+                                                            c.slot_of_rep, c.sums);
+    c.launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pt(Ctx &c, int swap_count) {
+    const int copy_mode = (c.flags & ETHER_FLAG_PT_REFERENCE_COPY) ? 1 : 0;
+    const int npairs = c.n_slots / 2 + 1;
+    const int nt = npairs * c.n_groups;
+    if (copy_mode) cudaMemsetAsync(c.copy_from, 0xFF, sizeof(int32_t) * c.R, c.stream);
+    pt_kernel<<<(nt + 127) / 128, 128, 0, c.stream>>>(
+        c.E, c.R, c.n_slots, c.n_groups, c.beta_slot, c.rep_of_slot, c.slot_of_rep, c.copy_from,
+        swap_count, c.seed, (c.flags & ETHER_FLAG_PT_TRUE_ENERGY) ? 1 : 0, copy_mode,
+        c.pt_accepts);
+    c.launches++;
+    if (copy_mode) {
+        dim3 grid(energy_blocks(c), c.R);
+        pt_copy_kernel<<<grid, 256, 0, c.stream>>>(c.spins, c.spins4, c.N, c.model, c.copy_from);
+        c.launches++;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace ether

@@ -1,0 +1,290 @@
+"""Host-side mirror of the reference's set-up for the sweep, on top of the C-ABI.
+
+`Lattice` replaces generate_supercell + getting_nbd (src/generate_supercell.f90,
+src/getting_nbd.f90) through ether_build_lattice; `couplings` replaces j_values.f90 +
+parameters.f90; `Sweep` owns one ether_ctx and exposes the reference's per-MCS routines
+under their reference names.  Arrays keep the reference's Fortran layouts:
+    ion      (N, 9)                 ion(0:8, N)
+    nn       (2, cap+1, N, nsh)     nn(nsh, N, 0:cap, 0:1)
+    j_exc    (3, nsp, nsp, nsh)     j_exc(nsh, nsp, nsp, 3)
+    sia_vec  (nsp, 3)               sia_vec(3, nsp)
+"""
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import abi
+
+KB_EV = 8.617333262e-5      # src/init.f90:47
+MB_EV = 5.7883818060e-5     # src/parameters.f90:41
+
+
+class Lattice:
+    """Supercell + neighbour shells built by ether_build_lattice (O(N))."""
+
+    def __init__(self, basis_cart, basis_species, abc, sc, shells, bc="ccc", checkerboard=False,
+                 tol=1e-5, cap=20):
+        lib = abi.load()
+        self.basis_cart = np.ascontiguousarray(basis_cart, dtype=np.float64).reshape(-1, 3)
+        self.nbasis = self.basis_cart.shape[0]
+        self.basis_species = np.ascontiguousarray(basis_species, dtype=np.int32)
+        self.abc = np.ascontiguousarray(abc, dtype=np.float64).reshape(3, 3)
+        self.sc = np.ascontiguousarray(sc, dtype=np.int32)
+        self.shells = np.ascontiguousarray(shells, dtype=np.float64)
+        self.nsh = len(self.shells)
+        self.cap = int(cap)
+        self.bc = bc
+        self.tol = float(tol)
+        self.checkerboard = bool(checkerboard)
+        self.N = int(np.prod(self.sc)) * self.nbasis
+        self.ion = np.zeros((self.N, 9), dtype=np.float64)
+        self.stgg = np.zeros(self.N, dtype=np.float64)
+        self.nn = np.zeros((2, self.cap + 1, self.N, max(self.nsh, 1)), dtype=np.int32)
+        abi.check(lib.ether_build_lattice(
+            self.nbasis, abi.dptr(self.basis_cart), abi.iptr(self.basis_species),
+            abi.dptr(self.abc), abi.iptr(self.sc), bc.encode(), int(self.checkerboard), self.nsh,
+            abi.dptr(self.shells), self.tol, self.cap, abi.dptr(self.ion), abi.dptr(self.stgg),
+            abi.iptr(self.nn)))
+
+    @property
+    def n_species(self):
+        return int(self.basis_species.max())
+
+
+def simple_cubic(L, bc="ccc", checkerboard=False, cap=20):
+    L = (L, L, L) if np.isscalar(L) else tuple(L)
+    return Lattice([[0.0, 0.0, 0.0]], [1], np.eye(3), L, [1.0], bc=bc,
+                   checkerboard=checkerboard, cap=cap)
+
+
+PYROCHLORE_FRAC = [
+    (0.0, 0.0, 0.0), (0.750000028, 0.25, 0.5), (0.25, 0.750000028, 0.5),
+    (0.25, 0.5, 0.750000028), (0.750000028, 0.5, 0.25), (0.5, 0.750000028, 0.25),
+    (0.5, 0.25, 0.750000028), (0.0, 0.5, 0.5), (0.750000028, 0.750000028, 0.0),
+    (0.25, 0.25, 0.0), (0.25, 0.0, 0.25), (0.750000028, 0.0, 0.750000028),
+    (0.5, 0.0, 0.5), (0.0, 0.750000028, 0.750000028), (0.0, 0.25, 0.25), (0.5, 0.5, 0.0),
+]
+PYROCHLORE_A = 8.4072999954
+
+
+def pyrochlore(n, shells=(2.97243,), cap=20, tol=1e-5):
+    """The 16-site cubic pyrochlore cell of the reference's examples/Pyrochlore deck,
+    replicated n x n x n (fractional -> cartesian as src/frac_to_cart.f90)."""
+    n = (n, n, n) if np.isscalar(n) else tuple(n)
+    abc = np.eye(3) * PYROCHLORE_A
+    cart = np.array([[abc[0, d] * f[0] + abc[1, d] * f[1] + abc[2, d] * f[2] for d in range(3)]
+                     for f in PYROCHLORE_FRAC])
+    return Lattice(cart, [1] * 16, abc, n, list(shells), cap=cap, tol=tol)
+
+
+def couplings(n_species, shells, s, para=None):
+    """j_values.f90:61-86 + parameters.f90:26-38.
+
+    shells: one entry per bond shell: list of (si, sj, (Jxx, Jyy, Jzz)) in meV, species
+    1-based.  j_exc(b,si,sj,:) = J*s(si)*s(sj), symmetric; then divided by J_para when
+    `para` is given, else by 1000 (meV -> eV)."""
+    nsh = len(shells)
+    j = np.zeros((3, n_species, n_species, nsh), dtype=np.float64)
+    s = np.asarray(s, dtype=np.float64)
+    for b, entries in enumerate(shells):
+        for si, sj, J in entries:
+            v = np.asarray(J, dtype=np.float64) * s[si - 1] * s[sj - 1]
+            j[:, si - 1, sj - 1, b] = v
+            j[:, sj - 1, si - 1, b] = v
+    j = j / (abs(para) if para else 1000.0)
+    return np.ascontiguousarray(j)
+
+
+def units(para=None):
+    """(kB, mB, g override) as parameters.f90 sets them."""
+    if para:
+        return 1.0, 1.0, 1.0
+    return KB_EV, MB_EV, None
+
+
+class Sweep:
+    """One ether_ctx: R replicas of a lattice, advanced by the GPU kernels."""
+
+    def __init__(self, ion, nn, j_exc, s, *, model, n_species, n_shells, cap, replicas=1,
+                 seed=1992, angle=False, dphi=0.0, zeeman=False, h=(0.0, 0.0, 0.0),
+                 g_factor=2.0, mb=MB_EV, sia=False, sia_vec=None, stgg=None, sc=(0, 0, 0),
+                 basis=0, flags=0):
+        self.lib = abi.load()
+        self._keep = []
+
+        def keep(a, dt):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=dt)
+            self._keep.append(a)
+            return a
+
+        ion = keep(ion, np.float64)
+        d = abi.Desc()
+        d.n_sites = ion.shape[0] if ion.ndim == 2 else ion.size // 9
+        d.n_species = n_species
+        d.n_shells = n_shells
+        d.nbd_capacity = cap
+        d.model = model
+        d.angle = int(bool(angle))
+        d.dphi = float(dphi)
+        d.zeeman = int(bool(zeeman))
+        for k in range(3):
+            d.h[k] = float(h[k])
+        d.g_factor = float(g_factor)
+        d.mb = float(mb)
+        d.sia = int(bool(sia))
+        d.ion = abi.dptr(ion)
+        d.nn = abi.iptr(keep(nn, np.int32))
+        d.j_exc = abi.dptr(keep(j_exc, np.float64))
+        d.sia_vec = abi.dptr(keep(sia_vec, np.float64))
+        d.s = abi.dptr(keep(s, np.float64))
+        d.stgg = abi.dptr(keep(stgg, np.float64))
+        d.n_replicas = replicas
+        d.seed = seed & 0xFFFFFFFF
+        for k in range(3):
+            d.sc[k] = int(sc[k])
+        d.basis = basis
+        d.flags = flags
+        self.N = d.n_sites
+        self.R = replicas
+        self.model = model
+        h_ = C.c_void_p()
+        abi.check(self.lib.ether_create(C.byref(d), C.byref(h_)))
+        self.h = h_
+        self._keep = []
+
+    @classmethod
+    def from_lattice(cls, lat, j_exc, s, model, **kw):
+        kw.setdefault("stgg", lat.stgg)
+        return cls(lat.ion, lat.nn, j_exc, s, model=model, n_species=j_exc.shape[1],
+                   n_shells=lat.nsh, cap=lat.cap, sc=tuple(int(x) for x in lat.sc),
+                   basis=lat.nbasis, **kw)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ether_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- state
+    def set_beta(self, beta):
+        b = np.ascontiguousarray(np.broadcast_to(np.asarray(beta, np.float64), (self.R,)))
+        abi.check(self.lib.ether_set_beta(self.h, abi.dptr(b)))
+
+    def set_ladder(self, beta_slots):
+        b = np.ascontiguousarray(beta_slots, dtype=np.float64)
+        abi.check(self.lib.ether_set_ladder(self.h, len(b), abi.dptr(b)))
+
+    def set_streams(self, stream=None, step=None):
+        st = None if stream is None else np.ascontiguousarray(stream, dtype=np.uint32)
+        sp = None if step is None else np.ascontiguousarray(step, dtype=np.uint32)
+        abi.check(self.lib.ether_set_streams(self.h, abi.uptr(st), abi.uptr(sp)))
+
+    def set_spins(self, ion, replica=-1):
+        ion = np.ascontiguousarray(ion, dtype=np.float64)
+        abi.check(self.lib.ether_set_spins(self.h, replica, abi.dptr(ion)))
+
+    def get_spins(self, ion, replica=0):
+        out = np.array(ion, dtype=np.float64, copy=True, order="C")
+        abi.check(self.lib.ether_get_spins(self.h, replica, abi.dptr(out)))
+        return out
+
+    # -- reference routines
+    def fresh_spins(self):
+        abi.check(self.lib.ether_fresh_spins(self.h))
+
+    def metropolis(self, nsweeps=1, accept=True):
+        out = np.zeros(self.R, dtype=np.float64) if accept else None
+        abi.check(self.lib.ether_metropolis(self.h, nsweeps, abi.dptr(out)))
+        return out
+
+    def overrelaxation(self, ovrr_para):
+        abi.check(self.lib.ether_overrelaxation(self.h, float(ovrr_para)))
+
+    def tot_energy(self):
+        out = np.zeros(self.R, dtype=np.float64)
+        abi.check(self.lib.ether_tot_energy(self.h, abi.dptr(out)))
+        return out
+
+    def tot_magnetisation(self):
+        out = np.zeros((self.R, 3), dtype=np.float64)
+        abi.check(self.lib.ether_tot_magnetisation(self.h, abi.dptr(out)))
+        return out
+
+    def observable(self, step, tmcs_eq, coa):
+        abi.check(self.lib.ether_observable(self.h, step, tmcs_eq, coa))
+
+    def zero_avg(self):
+        abi.check(self.lib.ether_zero_avg(self.h))
+
+    def sums(self):
+        out = np.zeros((self.R, 7), dtype=np.float64)
+        abi.check(self.lib.ether_get_sums(self.h, abi.dptr(out)))
+        return out
+
+    def avg(self):
+        out = np.zeros((self.R, 6), dtype=np.float64)
+        abi.check(self.lib.ether_avg(self.h, abi.dptr(out)))
+        return out
+
+    def per_repeat(self):
+        info = self.info()
+        mean = np.zeros((info.n_slots, 6), dtype=np.float64)
+        err = np.zeros((info.n_slots, 6), dtype=np.float64)
+        abi.check(self.lib.ether_per_repeat(self.h, abi.dptr(mean), abi.dptr(err)))
+        return mean, err
+
+    def parallel_tempering(self, swap_count):
+        acc = C.c_int32(0)
+        abi.check(self.lib.ether_parallel_tempering(self.h, swap_count, C.byref(acc)))
+        return acc.value
+
+    def slots(self):
+        out = np.zeros(self.R, dtype=np.int32)
+        abi.check(self.lib.ether_get_slots(self.h, abi.iptr(out)))
+        return out
+
+    def mcs(self, step0, nsteps, tmcs_eq, coa, ovrr=False, ovrr_para=0.0, ovrr_mcs=0, pt=False,
+            exchange_interval=11, swap_count=0):
+        s = abi.Schedule(tmcs_eq, coa, int(ovrr), float(ovrr_para), ovrr_mcs, int(pt),
+                         exchange_interval)
+        sc = C.c_int32(swap_count)
+        abi.check(self.lib.ether_mcs(self.h, C.byref(s), step0, nsteps, C.byref(sc)))
+        return sc.value
+
+    def accept_counts(self):
+        out = np.zeros(self.R, dtype=np.uint64)
+        abi.check(self.lib.ether_get_accept_counts(self.h, out.ctypes.data_as(abi.PU64)))
+        return out
+
+    def info(self):
+        i = abi.Info()
+        abi.check(self.lib.ether_get_info(self.h, C.byref(i)))
+        return i
+
+    def colouring(self):
+        col = np.zeros(self.N, dtype=np.int32)
+        rank = np.zeros(self.N, dtype=np.int32)
+        abi.check(self.lib.ether_get_colouring(self.h, abi.iptr(col), abi.iptr(rank)))
+        return col, rank
+
+    def sync(self):
+        abi.check(self.lib.ether_sync(self.h))
+
+    def stream(self):
+        s = C.c_void_p()
+        abi.check(self.lib.ether_get_stream(self.h, C.byref(s)))
+        return s.value or 0
+
+    def phase(self, colour):
+        abi.check(self.lib.ether_metropolis_phase(self.h, colour))
+
+    def end_sweep(self):
+        abi.check(self.lib.ether_end_sweep(self.h))

@@ -1,0 +1,227 @@
+/*
+ * ether_gpu.h -- C-ABI of the GB300 Monte Carlo sweep for ETHER (mukkelian/Ether).
+ *
+ * The reference has no plugin or FFI layer: its hot path is a set of Fortran subroutine
+ * calls inside the MCS loop of src/ether.f90 that share state through `module init`
+ * (src/init.f90:20-98).  Each entry point below replaces one of those calls; the comment
+ * on each names the reference routine (file:line) it stands in for.  A Fortran host binds
+ * them with ISO_C_BINDING (fortran/ether_gpu_mod.f90); C, C++ and Python (ctypes) bind
+ * them directly.
+ *
+ * Conventions
+ *   - Every call returns int: ETHER_OK (0) or a negative ETHER_ERR_* code.  No exception
+ *     crosses the ABI.  ether_last_error() returns a message for the last failure.
+ *   - Arrays are passed in the reference's own Fortran layouts (column-major, 1-based
+ *     values where the reference stores indices):
+ *         ion(0:8, N)              real(8)   ion[c + 9*i]
+ *         nn(nsh, N, 0:cap, 0:1)   integer   nn[b + nsh*(i + N*(k + (cap+1)*t))]
+ *         j_exc(nsh, nsp, nsp, 3)  real(8)   j_exc[b + nsh*(si + nsp*(sj + nsp*c))]
+ *         sia_vec(3, nsp)          real(8)
+ *     j_exc, sia_vec, h are the values after parameters.f90 (eV or J_para units).
+ *   - Host buffers belong to the caller and are never retained after a call returns.
+ *   - A context owns all of its device memory and one CUDA stream.  One host thread per
+ *     context; calls on one context are not re-entrant.
+ *   - A context holds R replicas of the lattice.  A replica is what one MPI rank held in
+ *     the reference (one temperature of one REPEAT); R replicas advance together.
+ */
+#ifndef ETHER_GPU_H
+#define ETHER_GPU_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ETHER_ABI_VERSION 1
+
+enum {
+    ETHER_OK = 0,
+    ETHER_ERR_ARG = -1,         /* invalid argument or inconsistent descriptor            */
+    ETHER_ERR_CUDA = -2,        /* CUDA runtime error (message in ether_last_error)        */
+    ETHER_ERR_NOMEM = -3,       /* device or host allocation failed                       */
+    ETHER_ERR_UNSUPPORTED = -4, /* valid input outside what the kernels implement          */
+    ETHER_ERR_CAPACITY = -5,    /* a table outgrew its fixed capacity                      */
+    ETHER_ERR_TIMEOUT = -6,     /* a bounded device-side wait ran out                      */
+    ETHER_ERR_STATE = -7,       /* call out of order (e.g. no beta set)                    */
+    ETHER_ERR_NODEV = -8,       /* no CUDA device                                          */
+    ETHER_ERR_PARSE = -9        /* malformed input deck (in.ether, j_exchange, ...)         */
+};
+
+enum { ETHER_MODEL_ISING = 0, ETHER_MODEL_XYZ = 1 };
+
+/* Descriptor flags. */
+enum {
+    ETHER_FLAG_FORCE_GENERAL = 1 << 0, /* never use the simple-cubic fast kernels           */
+    ETHER_FLAG_PT_TRUE_ENERGY = 1 << 1,/* PT exponent uses the Hamiltonian energy (bonds
+                                          once) instead of the reference's raw sum          */
+    ETHER_FLAG_PT_REFERENCE_COPY = 1 << 2 /* PT acceptance copies the lower slot's
+                                          configuration into the higher slot (what
+                                          parallel_tempering.f90:92-106 effectively does)
+                                          instead of exchanging the two                     */
+};
+
+typedef struct ether_ctx ether_ctx;
+
+/* Everything `module init` holds that the sweep reads (src/init.f90:28-92). */
+typedef struct ether_desc {
+    int32_t n_sites;      /* total_ions                                                    */
+    int32_t n_species;    /* nspecies                                                      */
+    int32_t n_shells;     /* no_of_nbd                                                     */
+    int32_t nbd_capacity; /* nbd_capacity (nn's third extent is cap+1)                     */
+    int32_t model;        /* ETHER_MODEL_ISING / ETHER_MODEL_XYZ                           */
+    int32_t angle;        /* ANGLE proposal (otherwise Marsaglia)                          */
+    double dphi;          /* ANGLE step in radians                                         */
+    int32_t zeeman;       /* Zeeman term on                                                */
+    double h[3];          /* field                                                         */
+    double g_factor, mb;  /* g and Bohr magneton in the run's units                        */
+    int32_t sia;          /* single-ion anisotropy on (used only for XYZ, as the reference) */
+    const double *ion;    /* ion(0:8, N): ID, Sx, Sy, Sz, species, phi, x, y, z            */
+    const int32_t *nn;    /* nn(nsh, N, 0:cap, 0:1)                                        */
+    const double *j_exc;  /* j_exc(nsh, nsp, nsp, 3)                                       */
+    const double *sia_vec;/* sia_vec(3, nsp) or NULL                                       */
+    const double *s;      /* s(nsp): spin length per species                               */
+    const double *stgg;   /* stgg_ion(N) or NULL (all 1)                                   */
+    int32_t n_replicas;   /* R                                                             */
+    uint32_t seed;        /* SEED tag (src/read_input.f90:119-121)                         */
+    int32_t sc[3];        /* supercell (0 = unknown); enables the simple-cubic kernels     */
+    int32_t basis;        /* lattice_per_unit_cell (0 = unknown)                           */
+    int32_t flags;        /* ETHER_FLAG_*                                                  */
+} ether_desc;
+
+/* Library version / last error (thread-local message of the last failing call). */
+int ether_abi_version(void);
+const char *ether_last_error(void);
+
+/* Replaces the module-init set-up that precedes the MCS loop (src/ether.f90:62-86): copies
+ * the lattice, couplings and initial spins of every replica to the device, colours the
+ * neighbour graph, and builds the kernels' tables. */
+int ether_create(const ether_desc *desc, ether_ctx **out);
+int ether_destroy(ether_ctx *ctx);
+
+/* beta(R): 1/(kB T) per replica (src/ether.f90:142-144).  Replica r sits at temperature
+ * slot r % n_slots of PT group r / n_slots; n_slots = R unless set by ether_set_ladder. */
+int ether_set_beta(ether_ctx *ctx, const double *beta);
+/* PT ladders: R = n_groups * n_slots replicas, each group an independent ladder (one per
+ * REPEAT).  beta_slots(n_slots).  Resets the slot permutation to the identity. */
+int ether_set_ladder(ether_ctx *ctx, int32_t n_slots, const double *beta_slots);
+/* Random streams: replica r draws from Philox key (seed, stream[r]); step[r] is its sweep
+ * counter (NULL keeps the current value).  Plays the role of random_seed(put=...) at
+ * src/ether.f90:154. */
+int ether_set_streams(ether_ctx *ctx, const uint32_t *stream, const uint32_t *step);
+
+/* ion(0:8,N) <-> replica spins.  replica = -1 addresses every replica (set) / replica 0
+ * (get).  Only ion(1:3,:) and ion(5,:) are read or written. */
+int ether_set_spins(ether_ctx *ctx, int32_t replica, const double *ion);
+int ether_get_spins(ether_ctx *ctx, int32_t replica, double *ion);
+
+/* fresh_spins (src/fresh_spins.f90:31-38), called at src/ether.f90:155: Ising flips every
+ * spin, XYZ draws a new Marsaglia / ANGLE state, on every replica. */
+int ether_fresh_spins(ether_ctx *ctx);
+
+/* Metropolis (src/Metropolis.f90:34-68), called at src/ether.f90:172: nsweeps full
+ * colour-ordered sweeps of every replica.  accept(R) (may be NULL) receives the summed
+ * per-sweep acceptance ratios accepted/N. */
+int ether_metropolis(ether_ctx *ctx, int32_t nsweeps, double *accept);
+
+/* overrelaxation (src/overrelaxation.f90:30-61), called at src/ether.f90:168, on every
+ * replica: colour-ordered reflection S' = 2(A.S)/(A.A) A - S, normalised, of each site
+ * with probability ovrr_para (ovrr_para >= 1: floor(ovrr_para) full passes first). */
+int ether_overrelaxation(ether_ctx *ctx, double ovrr_para);
+
+/* get_tot_energy (src/get_tot_energy.f90:33-47), called at src/ether.f90:177: raw sum of
+ * site energies per replica (exchange counted twice, Zeeman and SIA once). E(R). */
+int ether_tot_energy(ether_ctx *ctx, double *E);
+/* get_tot_magnetisation (src/get_tot_magnetisation.f90:32-40): M(3,R). */
+int ether_tot_magnetisation(ether_ctx *ctx, double *M);
+
+/* observable (src/observable.f90:30-43), called at src/ether.f90:201: when
+ * step > tmcs_eq and step % coa == 0, computes E and M and adds e = E/(2N), m = |M|/N,
+ * and their squares and fourth powers to the accumulators of each replica's current
+ * temperature slot (get_eng.f90:36-40, get_mag.f90:36-41). */
+int ether_observable(ether_ctx *ctx, int32_t step, int32_t tmcs_eq, int32_t coa);
+/* zeroes('avg') (src/zeroes.f90:48-55). */
+int ether_zero_avg(ether_ctx *ctx);
+/* Accumulators per temperature slot and group: sums(7, R) = (count, e, e2, e4, m, m2, m4),
+ * slot-major within each group (index = group*n_slots + slot).  get_eng/get_mag('avg_*')
+ * (src/get_eng.f90:42-60, src/get_mag.f90:43-59) and observables_per_repeat
+ * (src/observables_per_repeat.f90:29-69) are ether_avg / ether_per_repeat below. */
+int ether_get_sums(ether_ctx *ctx, double *sums);
+/* 'avg' reductions for every slot: out(6, R) = (<e>, U_E, C_v, <|m|>, U_M, chi). */
+int ether_avg(ether_ctx *ctx, double *out);
+/* observables_per_repeat: mean and error over the n_groups REPEAT groups, per slot.
+ * mean(6, n_slots), err(6, n_slots). */
+int ether_per_repeat(ether_ctx *ctx, double *mean, double *err);
+
+/* parallel_tempering (src/parallel_tempering.f90:39-108), called at src/ether.f90:189-198:
+ * odd/even neighbour pairs of temperature slots in every group, FP64 exponent
+ * delta = -(beta_hi - beta_lo)(E_lo - E_hi), swap of configurations as a swap of slot
+ * indices.  Uses the energies of the last ether_tot_energy / ether_mcs step.  accepted
+ * (may be NULL) receives the number of accepted pairs. */
+int ether_parallel_tempering(ether_ctx *ctx, int32_t swap_count, int32_t *accepted);
+/* slot_of_replica(R). */
+int ether_get_slots(ether_ctx *ctx, int32_t *slot_of_replica);
+
+/* The whole per-MCS body of src/ether.f90:159-203 for steps step0+1 .. step0+nsteps,
+ * on device, replayed from CUDA graphs: OVRR gate (:163-169), Metropolis (:172),
+ * total energy when PT needs it (:177), PT (:189-198), observable (:201). */
+typedef struct ether_schedule {
+    int32_t tmcs_eq;           /* equilibration MCS                                        */
+    int32_t coa;               /* measure every coa steps                                  */
+    int32_t ovrr;              /* OVRR logical                                             */
+    double ovrr_para;          /* fraction of N                                            */
+    int32_t ovrr_mcs;          /* OVRR every ovrr_mcs steps                                */
+    int32_t pt;                /* PT logical                                               */
+    int32_t exchange_interval; /* PT every exchange_interval steps                         */
+} ether_schedule;
+int ether_mcs(ether_ctx *ctx, const ether_schedule *sch, int32_t step0, int32_t nsteps,
+              int32_t *swap_count);
+
+/* Acceptance counters (accepted site updates per replica since the last reset). */
+int ether_get_accept_counts(ether_ctx *ctx, uint64_t *counts);
+int ether_reset_accept_counts(ether_ctx *ctx);
+
+/* Introspection used by tests and tools. */
+typedef struct ether_info {
+    int32_t n_colours;       /* colour classes of the Checkerboard order                   */
+    int32_t fast_path;       /* 1 when the simple-cubic kernels run                        */
+    int32_t n_types;         /* Ising threshold-table site types                           */
+    int32_t table_entries;   /* Ising threshold entries per temperature slot               */
+    int32_t n_slots, n_groups;
+    size_t device_bytes;     /* device memory owned by the context                         */
+    uint64_t kernel_launches;/* kernels launched by this context so far                    */
+} ether_info;
+int ether_get_info(ether_ctx *ctx, ether_info *info);
+/* colour(N) and rank_in_colour(N) of the Checkerboard order. */
+int ether_get_colouring(ether_ctx *ctx, int32_t *colour, int32_t *rank_in_colour);
+/* Block until all work on the context's stream has finished. */
+int ether_sync(ether_ctx *ctx);
+/* The cudaStream_t every kernel of this context is launched on (for event timing or for
+ * ordering a caller's own work after the sweep). */
+int ether_get_stream(ether_ctx *ctx, void **stream);
+/* One colour phase of the Metropolis sweep (the inner part of ether_metropolis), without
+ * advancing the sweep counter; colour in [0, n_colours).  For per-kernel timing and for
+ * hosts that interleave their own work between colour classes. */
+int ether_metropolis_phase(ether_ctx *ctx, int32_t colour);
+/* Advance every replica's sweep counter by one (ends a sweep built from phases). */
+int ether_end_sweep(ether_ctx *ctx);
+
+/* ---------------------------------------------------------------- lattice builder ---- */
+/* generate_supercell + getting_nbd (src/generate_supercell.f90:38-132,
+ * src/getting_nbd.f90:34-82, src/search_nbd.f90:20-64) in O(N) with a cell list, giving
+ * the same neighbour sets in the same order as the reference's O(N^2) search.
+ *   basis_cart(3, nbasis), basis_species(nbasis) 1-based, abc(3,3) rows = lattice vectors,
+ *   bc: 'c' closed / 'o' open per axis, nbd_dis(nsh), tol = nbdfc.
+ *   ion(0:8, N) receives ID, initial spins ((-1)**l for the z component, as
+ *   generate_supercell.f90:42 does for Ising), species and positions;
+ *   stgg(N) (may be NULL) receives the Checkerboard signs (-1)**(i+j+k+l) when
+ *   checkerboard != 0, else 1; nn(nsh, N, 0:cap, 0:1). */
+int ether_build_lattice(int32_t nbasis, const double *basis_cart, const int32_t *basis_species,
+                        const double *abc, const int32_t sc[3], const char bc[3],
+                        int32_t checkerboard, int32_t n_shells, const double *nbd_dis,
+                        double tol, int32_t cap, double *ion, double *stgg, int32_t *nn);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,229 @@
+"""ctypes binding of oracle/_build/libether_oracle.so (TEST INFRASTRUCTURE ONLY).
+
+Used by tests/, __graft_entry__.smoke() and bench.py's CPU baseline as the checker; the
+product never imports it.  Arrays use the reference's Fortran layouts (see
+oracle/ether_oracle.h).
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SO = os.path.join(HERE, "_build", "libether_oracle.so")
+
+PD = C.POINTER(C.c_double)
+PF = C.POINTER(C.c_float)
+PI = C.POINTER(C.c_int32)
+PU = C.POINTER(C.c_uint32)
+
+
+class Sys(C.Structure):
+    _fields_ = [("n_sites", C.c_int), ("n_species", C.c_int), ("n_shells", C.c_int),
+                ("cap", C.c_int), ("model", C.c_int), ("angle", C.c_int), ("dphi", C.c_double),
+                ("zeeman", C.c_int), ("h", C.c_double * 3), ("g_factor", C.c_double),
+                ("mb", C.c_double), ("sia", C.c_int), ("nn", PI), ("j_exc", PD),
+                ("sia_vec", PD), ("s", PD), ("stgg", PD)]
+
+
+class Stream(C.Structure):
+    _fields_ = [("key", C.c_uint32 * 2), ("n", C.c_uint64)]
+
+
+class Acc(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("n", "e", "e2", "e4", "m", "m2", "m4")]
+
+
+class RunCfg(C.Structure):
+    _fields_ = [("tmcs", C.c_int), ("tmcs_eq", C.c_int), ("coa", C.c_int), ("repeat", C.c_int),
+                ("ovrr", C.c_int), ("ovrr_para", C.c_double), ("ovrr_mcs", C.c_int),
+                ("seed", C.c_uint32), ("itemp", C.c_int), ("rank", C.c_int)]
+
+
+_lib = None
+
+
+def build():
+    subprocess.run(["sh", os.path.join(HERE, "build.sh")], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(SO):
+            build()
+        L = C.CDLL(SO)
+        L.orc_philox4x32_10.argtypes = [PU, PU, PU]
+        L.orc_supercell.restype = C.c_int
+        L.orc_supercell.argtypes = [C.c_int, PD, PI, PD, PI, C.c_int, PD, PD]
+        L.orc_neighbours_bruteforce.restype = C.c_int
+        L.orc_neighbours_bruteforce.argtypes = [C.c_int, PD, PD, PI, C.c_char_p, C.c_int, PD,
+                                                C.c_double, C.c_int, PI]
+        L.orc_greedy_colouring.restype = C.c_int
+        L.orc_greedy_colouring.argtypes = [C.c_int, C.c_int, C.c_int, PI, PI, PI]
+        L.orc_hamiltonian.restype = C.c_double
+        L.orc_tot_energy.restype = C.c_double
+        L.orc_tot_energy.argtypes = [C.POINTER(Sys), PD]
+        L.orc_tot_magnetisation.argtypes = [C.POINTER(Sys), PD, PD]
+        L.orc_tot_energy_f32.restype = C.c_double
+        L.orc_tot_energy_f32.argtypes = [C.POINTER(Sys), PD, PF]
+        L.orc_tot_magnetisation_f32.argtypes = [C.POINTER(Sys), PD, PF, PD]
+        L.orc_stream_init.argtypes = [C.POINTER(Stream), C.c_uint32, C.c_uint32]
+        L.orc_stream_uniform.restype = C.c_double
+        L.orc_stream_uniform.argtypes = [C.POINTER(Stream)]
+        L.orc_metropolis_typewriter.restype = C.c_double
+        L.orc_metropolis_typewriter.argtypes = [C.POINTER(Sys), PD, C.c_double, C.POINTER(Stream)]
+        L.orc_fresh_spins_typewriter.argtypes = [C.POINTER(Sys), PD, C.POINTER(Stream)]
+        L.orc_overrelaxation_typewriter.argtypes = [C.POINTER(Sys), PD, C.c_int, C.POINTER(Stream)]
+        L.orc_metropolis_colour.restype = C.c_double
+        L.orc_metropolis_colour.argtypes = [C.POINTER(Sys), PD, PF, C.c_int, C.c_double,
+                                            C.c_uint32, C.c_uint32, C.c_uint32, PI, PI, C.c_int]
+        L.orc_overrelax_colour.argtypes = [C.POINTER(Sys), PD, PF, C.c_double, C.c_uint32,
+                                           C.c_uint32, C.c_uint32, PI, PI, C.c_int]
+        L.orc_fresh_spins_colour.argtypes = [C.POINTER(Sys), PD, PF, C.c_uint32, C.c_uint32,
+                                             C.c_uint32]
+        L.orc_parallel_tempering.restype = C.c_int
+        L.orc_parallel_tempering.argtypes = [C.c_int, PD, PD, PI, C.c_int, C.c_uint32,
+                                             C.c_uint32, C.c_int, PI]
+        L.orc_acc_sample.argtypes = [C.POINTER(Acc), C.c_double, PD, C.c_int]
+        L.orc_acc_average.argtypes = [C.POINTER(Acc), C.c_double, C.c_int, PD]
+        L.orc_per_repeat.argtypes = [C.c_int, PD, PD, PD]
+        L.orc_structure_factor.argtypes = [C.c_int, PD, PD, C.c_int, PD, PD]
+        L.orc_run_temperature.restype = C.c_double
+        L.orc_run_temperature.argtypes = [C.POINTER(Sys), PD, C.c_double, C.POINTER(RunCfg), PD]
+        L.orc_run_temperatures.argtypes = [C.POINTER(Sys), PD, C.c_int, PD, C.POINTER(RunCfg),
+                                           C.c_int, PD, PD]
+        L.orc_expf_neg.restype = C.c_float
+        L.orc_expf_neg.argtypes = [C.c_float]
+        L.orc_sincosf.argtypes = [C.c_float, PF, PF]
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    return None if a is None else a.ctypes.data_as(PD)
+
+
+def _i(a):
+    return None if a is None else a.ctypes.data_as(PI)
+
+
+def _f(a):
+    return None if a is None else a.ctypes.data_as(PF)
+
+
+def philox(ctr, key):
+    c = np.ascontiguousarray(ctr, dtype=np.uint32)
+    k = np.ascontiguousarray(key, dtype=np.uint32)
+    o = np.zeros(4, dtype=np.uint32)
+    lib().orc_philox4x32_10(c.ctypes.data_as(PU), k.ctypes.data_as(PU), o.ctypes.data_as(PU))
+    return o
+
+
+class System:
+    """Holds the arrays of one lattice + couplings and an orc_sys pointing at them."""
+
+    def __init__(self, ion, nn, j_exc, s, *, model, n_species, n_shells, cap, angle=False,
+                 dphi=0.0, zeeman=False, h=(0, 0, 0), g_factor=2.0, mb=5.7883818060e-5,
+                 sia=False, sia_vec=None, stgg=None):
+        self.ion0 = np.ascontiguousarray(ion, dtype=np.float64)
+        self.nn = np.ascontiguousarray(nn, dtype=np.int32)
+        self.j_exc = np.ascontiguousarray(j_exc, dtype=np.float64)
+        self.s = np.ascontiguousarray(s, dtype=np.float64)
+        self.sia_vec = None if sia_vec is None else np.ascontiguousarray(sia_vec, dtype=np.float64)
+        self.stgg = None if stgg is None else np.ascontiguousarray(stgg, dtype=np.float64)
+        self.N = self.ion0.shape[0]
+        y = Sys()
+        y.n_sites, y.n_species, y.n_shells, y.cap = self.N, n_species, n_shells, cap
+        y.model, y.angle, y.dphi = model, int(bool(angle)), float(dphi)
+        y.zeeman = int(bool(zeeman))
+        for k in range(3):
+            y.h[k] = float(h[k])
+        y.g_factor, y.mb, y.sia = float(g_factor), float(mb), int(bool(sia))
+        y.nn, y.j_exc, y.sia_vec = _i(self.nn), _d(self.j_exc), _d(self.sia_vec)
+        y.s, y.stgg = _d(self.s), _d(self.stgg)
+        self.sys = y
+        self.model = model
+
+    @classmethod
+    def from_lattice(cls, lat, j_exc, s, model, **kw):
+        kw.setdefault("stgg", lat.stgg)
+        return cls(lat.ion, lat.nn, j_exc, s, model=model, n_species=j_exc.shape[1],
+                   n_shells=lat.nsh, cap=lat.cap, **kw)
+
+    def p(self):
+        return C.byref(self.sys)
+
+    def colouring(self):
+        col = np.zeros(self.N, dtype=np.int32)
+        rank = np.zeros(self.N, dtype=np.int32)
+        n = lib().orc_greedy_colouring(self.N, self.sys.n_shells, self.sys.cap, _i(self.nn),
+                                       _i(col), _i(rank))
+        return n, col, rank
+
+    def spin4(self, ion):
+        s = np.zeros((self.N, 4), dtype=np.float32)
+        s[:, 0:3] = ion[:, 1:4]
+        s[:, 3] = ion[:, 5]
+        return s
+
+    def tot_energy(self, ion):
+        return lib().orc_tot_energy(self.p(), _d(ion))
+
+    def tot_magnetisation(self, ion):
+        m = np.zeros(3)
+        lib().orc_tot_magnetisation(self.p(), _d(ion), _d(m))
+        return m
+
+    def tot_energy_f32(self, ion, sp4):
+        return lib().orc_tot_energy_f32(self.p(), _d(ion), _f(sp4))
+
+    def tot_magnetisation_f32(self, ion, sp4):
+        m = np.zeros(3)
+        lib().orc_tot_magnetisation_f32(self.p(), _d(ion), _f(sp4), _d(m))
+        return m
+
+    def metropolis_colour(self, ion, sp4, prec, beta, seed, stream, t, col, rank, ncol):
+        return lib().orc_metropolis_colour(self.p(), _d(ion), _f(sp4), prec, beta, seed, stream,
+                                           t, _i(col), _i(rank), ncol)
+
+    def overrelax_colour(self, ion, sp4, frac, seed, stream, t, col, rank, ncol):
+        lib().orc_overrelax_colour(self.p(), _d(ion), _f(sp4), frac, seed, stream, t, _i(col),
+                                   _i(rank), ncol)
+
+    def fresh_spins_colour(self, ion, sp4, seed, stream, call):
+        lib().orc_fresh_spins_colour(self.p(), _d(ion), _f(sp4), seed, stream, call)
+
+    def metropolis_typewriter(self, ion, beta, st):
+        return lib().orc_metropolis_typewriter(self.p(), _d(ion), beta, C.byref(st))
+
+
+def stream(seed, sid):
+    st = Stream()
+    lib().orc_stream_init(C.byref(st), seed, sid)
+    return st
+
+
+def supercell(basis_cart, basis_species, abc, sc, checkerboard=False):
+    bc = np.ascontiguousarray(basis_cart, dtype=np.float64).reshape(-1, 3)
+    bs = np.ascontiguousarray(basis_species, dtype=np.int32)
+    a = np.ascontiguousarray(abc, dtype=np.float64).reshape(3, 3)
+    s = np.ascontiguousarray(sc, dtype=np.int32)
+    N = int(np.prod(s)) * bc.shape[0]
+    ion = np.zeros((N, 9))
+    stgg = np.zeros(N)
+    lib().orc_supercell(bc.shape[0], _d(bc), _i(bs), _d(a), _i(s), int(checkerboard), _d(ion),
+                        _d(stgg))
+    return ion, stgg
+
+
+def neighbours_bruteforce(ion, abc, sc, bc, shells, tol, cap):
+    N = ion.shape[0]
+    sh = np.ascontiguousarray(shells, dtype=np.float64)
+    nn = np.zeros((2, cap + 1, N, len(sh)), dtype=np.int32)
+    a = np.ascontiguousarray(abc, dtype=np.float64).reshape(3, 3)
+    s = np.ascontiguousarray(sc, dtype=np.int32)
+    rc = lib().orc_neighbours_bruteforce(N, _d(np.ascontiguousarray(ion)), _d(a), _i(s),
+                                         bc.encode(), len(sh), _d(sh), tol, cap, _i(nn))
+    return rc, nn

@@ -1,0 +1,184 @@
+"""GPU parity of the Metropolis colour phases against the oracle's Checkerboard mode.
+
+Ising: bit-exact spin trajectories (fixed-stream replay).  XYZ: the GPU's FP32 state equals
+the oracle's FP32 mirror bit for bit, and its observables stay within 1e-5 relative of the
+oracle's FP64 replay over the first 100 sweeps.
+"""
+import numpy as np
+import pytest
+
+import ether_gb300 as eg
+from tests.helpers import beta_of, make_pair, random_ising, random_xyz
+
+pytestmark = pytest.mark.gpu
+
+FM = [[(1, 1, (-1.0, -1.0, -1.0))]]       # ETHER's sign: J < 0 is ferromagnetic
+AFM_J1_J2 = [[(1, 1, (1.0, 1.0, 1.0))], [(1, 1, (-0.1, -0.1, -0.1))]]
+
+
+def ising_replay(lat, shells, kT, sweeps, flags=0, seed=1992, stream=0, **kw):
+    sw, osys = make_pair(lat, eg.MODEL_ISING, shells, flags=flags, seed=seed, **kw)
+    beta = beta_of(kT)
+    sw.set_beta(beta)
+    sw.set_streams(stream=[stream], step=[0])
+    ncol, col, rank = osys.colouring()
+    gcol, grank = sw.colouring()
+    assert ncol == sw.info().n_colours
+    np.testing.assert_array_equal(col, gcol)
+    np.testing.assert_array_equal(rank, grank)
+    ion = random_ising(lat, 7)
+    sw.set_spins(ion)
+    acc_o = []
+    for t in range(sweeps):
+        acc_o.append(osys.metropolis_colour(ion, None, 64, beta, seed, stream, t, col, rank, ncol))
+    acc_g = sw.metropolis(sweeps)
+    g = sw.get_spins(lat.ion)
+    return sw, ion, g, sum(acc_o), acc_g[0]
+
+
+@pytest.mark.parametrize("L,flags", [(8, 0), (16, 0), (8, eg.FLAG_FORCE_GENERAL), (6, 0), (5, 0),
+                                     ((16, 8, 12), 0)])
+@pytest.mark.parametrize("kT", [4.511, 2.0, 10.0])
+def test_ising_sc_bit_exact(L, flags, kT):
+    lat = eg.simple_cubic(L)
+    sw, ion, g, ao, ag = ising_replay(lat, FM, kT, 20, flags=flags)
+    np.testing.assert_array_equal(g[:, 3], ion[:, 3])
+    assert ao == pytest.approx(ag, abs=1e-12)
+    if L == 16 and flags == 0:
+        assert sw.info().fast_path == 1
+
+
+def test_ising_open_bc_and_zeeman_bit_exact():
+    lat = eg.simple_cubic((6, 5, 4), bc="coc")
+    sw, ion, g, ao, ag = ising_replay(lat, FM, 3.0, 15, zeeman=True, h=(0.0, 0.0, 2.0),
+                                      g_factor=2.0)
+    np.testing.assert_array_equal(g[:, 3], ion[:, 3])
+    assert sw.info().n_types > 1
+
+
+def test_ising_pyrochlore_two_shells_bit_exact():
+    lat = eg.pyrochlore(2, shells=(2.97243, 5.1484))
+    lat = eg.Lattice(lat.basis_cart, [1] * 16, lat.abc, (2, 2, 2), [2.97243, 5.1484], tol=1e-3)
+    sw, ion, g, ao, ag = ising_replay(lat, AFM_J1_J2, 1.5, 25)
+    np.testing.assert_array_equal(g[:, 3], ion[:, 3])
+    assert sw.info().n_colours > 2
+
+
+def xyz_replay(lat, shells, kT, sweeps, flags=0, seed=1992, stream=3, **kw):
+    sw, osys = make_pair(lat, eg.MODEL_XYZ, shells, flags=flags, seed=seed, **kw)
+    beta = beta_of(kT)
+    sw.set_beta(beta)
+    sw.set_streams(stream=[stream], step=[0])
+    ncol, col, rank = osys.colouring()
+    ion = random_xyz(lat, 11)
+    sw.set_spins(ion)
+    sp4 = osys.spin4(ion)
+    ion64 = ion.copy()
+    for t in range(sweeps):
+        osys.metropolis_colour(ion, sp4, 32, beta, seed, stream, t, col, rank, ncol)
+        osys.metropolis_colour(ion64, None, 64, beta, seed, stream, t, col, rank, ncol)
+    sw.metropolis(sweeps)
+    g = sw.get_spins(lat.ion)
+    return sw, osys, sp4, ion64, g
+
+
+@pytest.mark.parametrize("L,flags", [(4, 0), (8, 0), (8, eg.FLAG_FORCE_GENERAL), (5, 0)])
+@pytest.mark.parametrize("angle", [False, True])
+def test_xyz_sc_matches_fp32_mirror(L, flags, angle):
+    lat = eg.simple_cubic(L)
+    sw, osys, sp4, ion64, g = xyz_replay(lat, FM, 1.443, 30, flags=flags, angle=angle,
+                                         dphi=np.deg2rad(50.0))
+    np.testing.assert_array_equal(g[:, 1].astype(np.float32), sp4[:, 0])
+    np.testing.assert_array_equal(g[:, 2].astype(np.float32), sp4[:, 1])
+    np.testing.assert_array_equal(g[:, 3].astype(np.float32), sp4[:, 2])
+    np.testing.assert_array_equal(g[:, 5].astype(np.float32), sp4[:, 3])
+
+
+def test_xyz_zeeman_sia_pyrochlore_matches_fp32_mirror():
+    lat = eg.Lattice(eg.pyrochlore(2).basis_cart, [1] * 16, np.eye(3) * eg.model.PYROCHLORE_A,
+                     (2, 2, 2), [2.97243, 5.1484], tol=1e-3)
+    sia = np.array([[0.0, 0.0, -0.2e-3]])
+    sw, osys, sp4, ion64, g = xyz_replay(lat, AFM_J1_J2, 2.0, 20, zeeman=True, h=(0.0, 0.0, 1.0),
+                                         g_factor=2.0, sia=True, sia_vec=sia)
+    np.testing.assert_array_equal(g[:, 1:4].astype(np.float32), sp4[:, 0:3])
+
+
+def test_xyz_observables_within_1e5_of_fp64_over_100_sweeps():
+    """Fixed-stream tolerance check: FP32 GPU vs the FP64 replay of the same draws."""
+    lat = eg.simple_cubic(8)
+    sw, osys, sp4, ion64, g = xyz_replay(lat, FM, 1.443, 100)
+    E_gpu = sw.tot_energy()[0]
+    M_gpu = np.linalg.norm(sw.tot_magnetisation()[0])
+    E_64 = osys.tot_energy(ion64)
+    M_64 = np.linalg.norm(osys.tot_magnetisation(ion64))
+    assert abs(E_gpu - E_64) <= 1e-5 * abs(E_64)
+    assert abs(M_gpu - M_64) <= 1e-5 * abs(M_64)
+
+
+def test_energy_magnetisation_match_oracle():
+    lat = eg.simple_cubic(6, checkerboard=True)
+    for model in (eg.MODEL_ISING, eg.MODEL_XYZ):
+        sw, osys = make_pair(lat, model, FM, zeeman=True, h=(0.3, -0.2, 1.0), g_factor=2.0)
+        ion = random_ising(lat, 3) if model == eg.MODEL_ISING else random_xyz(lat, 3)
+        sw.set_spins(ion)
+        E = sw.tot_energy()[0]
+        M = sw.tot_magnetisation()[0]
+        if model == eg.MODEL_ISING:
+            assert E == pytest.approx(osys.tot_energy(ion), rel=1e-12, abs=1e-15)
+            np.testing.assert_allclose(M, osys.tot_magnetisation(ion), rtol=1e-12, atol=1e-12)
+        else:
+            sp4 = osys.spin4(ion)
+            assert E == pytest.approx(osys.tot_energy_f32(ion, sp4), rel=1e-12)
+            assert E == pytest.approx(osys.tot_energy(ion), rel=1e-5)
+            np.testing.assert_allclose(M, osys.tot_magnetisation_f32(ion, sp4), rtol=1e-12, atol=1e-9)
+
+
+@pytest.mark.parametrize("para", [0.4, 1.0, 1.7])
+def test_overrelaxation_matches_oracle_and_conserves_energy(para):
+    lat = eg.simple_cubic(8)
+    sw, osys = make_pair(lat, eg.MODEL_XYZ, FM)
+    sw.set_beta(1.0)
+    sw.set_streams(stream=[5], step=[0])
+    ion = random_xyz(lat, 5)
+    sw.set_spins(ion)
+    E0 = sw.tot_energy()[0]
+    ncol, col, rank = osys.colouring()
+    sp4 = osys.spin4(ion)
+    osys.overrelax_colour(ion, sp4, para, 1992, 5, 0, col, rank, ncol)
+    sw.overrelaxation(para)
+    g = sw.get_spins(lat.ion)
+    np.testing.assert_array_equal(g[:, 1:4].astype(np.float32), sp4[:, 0:3])
+    E1 = sw.tot_energy()[0]
+    assert E1 == pytest.approx(E0, rel=1e-5)
+
+
+@pytest.mark.parametrize("model,angle", [(eg.MODEL_ISING, False), (eg.MODEL_XYZ, False),
+                                         (eg.MODEL_XYZ, True)])
+def test_fresh_spins_match_oracle(model, angle):
+    lat = eg.simple_cubic(6)
+    sw, osys = make_pair(lat, model, FM, angle=angle, dphi=0.5)
+    sw.set_streams(stream=[9], step=[0])
+    ion = random_ising(lat, 1) if model == eg.MODEL_ISING else random_xyz(lat, 1)
+    sw.set_spins(ion)
+    sp4 = osys.spin4(ion)
+    osys.fresh_spins_colour(ion, sp4, 1992, 9, 0)
+    sw.fresh_spins()
+    g = sw.get_spins(lat.ion)
+    if model == eg.MODEL_ISING:
+        np.testing.assert_array_equal(g[:, 3], ion[:, 3])
+    else:
+        np.testing.assert_array_equal(g[:, 1:4].astype(np.float32), sp4[:, 0:3])
+
+
+def test_replicas_are_independent_streams():
+    lat = eg.simple_cubic(16)
+    sw, osys = make_pair(lat, eg.MODEL_ISING, FM, replicas=4)
+    sw.set_beta([beta_of(4.511)] * 4)
+    sw.set_streams(stream=[0, 1, 0, 2], step=[0, 0, 0, 0])
+    ion = random_ising(lat, 2)
+    sw.set_spins(ion)
+    sw.metropolis(10, accept=False)
+    s = [sw.get_spins(lat.ion, r)[:, 3] for r in range(4)]
+    np.testing.assert_array_equal(s[0], s[2])
+    assert not np.array_equal(s[0], s[1])
+    assert not np.array_equal(s[1], s[3])
