@@ -154,6 +154,7 @@ def run_gpu(model, L, replicas, steps, warmup, rank, world):
     import ether_gb300 as eg
     lat, j, sw, ion, beta = make_workload(model, L, replicas, seed=1992 + 7919 * rank)
     sw.set_spins(ion)
+    variant, tuned_ms = sw.autotune()
     N, R = lat.N, replicas
     ev = Events(sw.stream())
     for _ in range(warmup):
@@ -213,6 +214,7 @@ def run_gpu(model, L, replicas, steps, warmup, rank, world):
         "clocks": clk, "e2e": e2e, "h2d": h2d, "d2h": d2h,
         "accept_mean": float(np.mean(acc)) if acc is not None else None,
         "check_spin_sum": float(out[:, 3].sum()),
+        "variant": variant,
     }
 
 
@@ -265,7 +267,7 @@ def _max_over_ranks(x, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--model", default="ising", choices=["ising", "heisenberg"])
@@ -300,7 +302,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return 0
-        mcs = args.cpu_mcs or 12
+        mcs = args.cpu_mcs or 300
         ref = cpu_reference(model, args.L, mcs, cores)
         line = {"metric": "spin updates/ns", "value": ref["value"], "unit": "spin updates/ns",
                 "impl": "reference", "n_gpus": args.gpus, "steps": args.steps,
@@ -344,7 +346,7 @@ def main():
                      "kernel": "ising_sc_kernel<16> (one colour phase)" if model == 0
                      else "xyz_sc_kernel (one colour phase)",
                      "bytes_per_update": res["bytes_per_update"],
-                     "phase_ms": res["phase_ms"]},
+                     "phase_ms": res["phase_ms"], "autotuned_variant": res["variant"]},
         "e2e": {"value": res["e2e"], "unit": "spin updates/ns",
                 "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"]},
         "gpu_launches": res["launches"],
@@ -352,7 +354,7 @@ def main():
         "accept_ratio": res["accept_mean"],
     }
     if not args.no_cpu:
-        mcs = args.cpu_mcs or 12
+        mcs = args.cpu_mcs or 300
         line["cpu_baseline"] = {k: v for k, v in cpu_reference(model, args.L, mcs, cores).items()
                                 if k in ("value", "unit", "cores", "kind", "sample")}
     print(json.dumps(line))

@@ -97,6 +97,8 @@ SIGNATURES = {
     "ether_get_stream": (C.c_int, [P, C.POINTER(P)]),
     "ether_metropolis_phase": (C.c_int, [P, C.c_int32]),
     "ether_end_sweep": (C.c_int, [P]),
+    "ether_autotune": (C.c_int, [P, PI32, C.POINTER(C.c_float)]),
+    "ether_set_variant": (C.c_int, [P, C.c_int32]),
     "ether_build_lattice": (C.c_int, [C.c_int32, PD, PI32, PD, PI32, C.c_char_p, C.c_int32,
                                       C.c_int32, PD, C.c_double, C.c_int32, PD, PD, PI32]),
 }

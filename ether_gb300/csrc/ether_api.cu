@@ -122,7 +122,10 @@ int build_ising_types(Ctx &c, const std::vector<int> &sp, const std::vector<std:
 }
 
 // Thresholds for one temperature: the same FP64 expression as the oracle's colour mode.
-void ising_thresholds(const Ctx &c, double beta, uint32_t *thr, uint8_t *always) {
+// A site flips iff its uniform u32 u <= T, T = max(ceil(2^32 p), 1) - 1 with
+// p = exp(-beta dE): the reference's -beta dE > log(eta) for eta = u 2^-32, where eta = 0
+// (log = -inf) always accepts.
+void ising_thresholds(const Ctx &c, double beta, uint32_t *thr) {
     const int G = c.nsh * c.nsp;
     std::vector<int> nup(G);
     for (int ty = 0; ty < c.n_types; ++ty) {
@@ -148,15 +151,13 @@ void ising_thresholds(const Ctx &c, double beta, uint32_t *thr, uint8_t *always)
                     }
                 double dE = (-2.0 * sig) * field;
                 if (c.zeeman) dE += -(gms * ((-2.0 * sig) * c.h[2]));
-                const double p = std::exp(-beta * dE);
+                const double q = std::exp(-beta * dE) * 4294967296.0;
                 const size_t e = (size_t)c.h_type_base[ty] + (size_t)own * half + idx;
-                if (p >= 1.0) {
-                    always[e] = 1;
+                if (q >= 4294967296.0) {
                     thr[e] = 0xFFFFFFFFu;
                 } else {
-                    const double u = std::ceil(p * 4294967296.0);
-                    if (u >= 4294967296.0) { always[e] = 1; thr[e] = 0xFFFFFFFFu; }
-                    else { always[e] = 0; thr[e] = (uint32_t)u; }
+                    const double u = std::ceil(q);
+                    thr[e] = u < 1.0 ? 0u : (uint32_t)(u - 1.0);
                 }
             }
         }
@@ -179,12 +180,10 @@ int upload_ladder(Ctx &c) {
     CUDA_TRY(cudaMemcpyAsync(c.rep_of_slot, ros.data(), sizeof(int32_t) * c.R, cudaMemcpyHostToDevice, c.stream));
     if (c.model == 0) {
         std::vector<uint32_t> thr((size_t)c.n_slots * c.table_entries);
-        std::vector<uint8_t> al((size_t)c.n_slots * c.table_entries);
         for (int s = 0; s < c.n_slots; ++s)
-            ising_thresholds(c, c.beta_slots[s], thr.data() + (size_t)s * c.table_entries,
-                             al.data() + (size_t)s * c.table_entries);
+            ising_thresholds(c, c.beta_slots[s], thr.data() + (size_t)s * c.table_entries);
         CUDA_TRY(cudaMemcpyAsync(c.thr, thr.data(), thr.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, c.stream));
-        CUDA_TRY(cudaMemcpyAsync(c.always, al.data(), al.size(), cudaMemcpyHostToDevice, c.stream));
+        CUDA_TRY(cudaStreamSynchronize(c.stream));
     }
     CUDA_TRY(cudaStreamSynchronize(c.stream));
     c.beta_set = true;
@@ -195,7 +194,7 @@ void free_ctx(Ctx &c) {
     void *ptrs[] = {c.t.row_ptr, c.t.nbr, c.t.jidx, c.t.wstride, c.t.species, c.t.itype,
                     c.t.type_base, c.t.type_half, c.t.J, c.t.Jd, c.t.zee, c.t.zeed, c.t.D,
                     c.t.mweight, c.t.site_of_storage, c.spins, c.spins4, c.beta_slot,
-                    c.beta_slot_f, c.slot_of_rep, c.rep_of_slot, c.thr, c.always, c.stream_id,
+                    c.beta_slot_f, c.slot_of_rep, c.rep_of_slot, c.thr, c.stream_id,
                     c.step, c.ovrr_step, c.fresh_call, c.acc_count, c.E, c.M, c.sums,
                     c.partials, c.pt_accepts, c.copy_from};
     for (void *p : ptrs)
@@ -415,7 +414,6 @@ extern "C" int ether_create(const ether_desc *d, ether_ctx **out) {
     TRY(dev_alloc(c, &c.rep_of_slot, c.R));
     if (c.model == ETHER_MODEL_ISING) {
         TRY(dev_alloc(c, &c.thr, (size_t)c.R * c.table_entries));
-        TRY(dev_alloc(c, &c.always, (size_t)c.R * c.table_entries));
     }
     TRY(dev_alloc(c, &c.stream_id, c.R));
     TRY(dev_alloc(c, &c.step, c.R));
@@ -813,5 +811,102 @@ extern "C" int ether_metropolis_phase(ether_ctx *h, int32_t colour) {
 extern "C" int ether_end_sweep(ether_ctx *h) {
     if (!h) return fail(ETHER_ERR_ARG, "null context");
     CUDA_TRY(launch_advance(h->c, h->c.step));
+    return ETHER_OK;
+}
+
+// ---------------------------------------------------------------- autotuner ----------
+// Times every kernel variant of this context's fast path on its own data -- one colour
+// phase of each, with the spins and acceptance counters restored afterwards -- and keeps
+// the fastest.  Choices are cached per size class (model, extents, replicas) for the life
+// of the process, so later contexts of the same shape skip the timing.
+#include <mutex>
+namespace {
+std::mutex g_tune_mu;
+std::map<std::vector<long>, std::pair<int, int>> g_tune_cache;
+}  // namespace
+
+extern "C" int ether_autotune(ether_ctx *h, int32_t *variant, float *best_ms) {
+    if (!h) return fail(ETHER_ERR_ARG, "null context");
+    Ctx &c = h->c;
+    if (variant) *variant = c.vec_bytes * 10 + c.ising_vpt;
+    if (best_ms) *best_ms = 0.f;
+    if (!c.fast || c.model != ETHER_MODEL_ISING) return ETHER_OK;
+    if (!c.beta_set) return fail(ETHER_ERR_STATE, "beta not set");
+    const std::vector<long> key = {c.model, c.L[0], c.L[1], c.L[2], c.R};
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            c.vec_bytes = it->second.first;
+            c.ising_vpt = it->second.second;
+            if (variant) *variant = c.vec_bytes * 10 + c.ising_vpt;
+            return ETHER_OK;
+        }
+    }
+    const size_t bytes = (size_t)c.R * c.N;
+    uint8_t *backup = nullptr;
+    unsigned long long *acc_backup = nullptr;
+    CUDA_TRY(cudaMalloc(&backup, bytes));
+    CUDA_TRY(cudaMalloc(&acc_backup, sizeof(unsigned long long) * c.R));
+    CUDA_TRY(cudaMemcpyAsync(backup, c.spins, bytes, cudaMemcpyDeviceToDevice, c.stream));
+    CUDA_TRY(cudaMemcpyAsync(acc_backup, c.acc_count, sizeof(unsigned long long) * c.R,
+                             cudaMemcpyDeviceToDevice, c.stream));
+    const int H = c.L[0] / 2;
+    int best_w = c.vec_bytes, best_v = c.ising_vpt;
+    float best = 1e30f;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    for (int w : {16, 8, 4}) {
+        if (H % w) continue;
+        for (int v : {1, 2, 4}) {
+            c.vec_bytes = w;
+            c.ising_vpt = v;
+            CUDA_TRY(launch_ising_sweep(c, 0));  // warm-up
+            CUDA_TRY(cudaEventRecord(e0, c.stream));
+            for (int k = 0; k < 3; ++k) {
+                CUDA_TRY(launch_ising_sweep(c, 0));
+                CUDA_TRY(launch_ising_sweep(c, 1));
+            }
+            CUDA_TRY(cudaEventRecord(e1, c.stream));
+            CUDA_TRY(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            ms /= 6.0f;
+            if (ms < best) {
+                best = ms;
+                best_w = w;
+                best_v = v;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c.vec_bytes = best_w;
+    c.ising_vpt = best_v;
+    CUDA_TRY(cudaMemcpyAsync(c.spins, backup, bytes, cudaMemcpyDeviceToDevice, c.stream));
+    CUDA_TRY(cudaMemcpyAsync(c.acc_count, acc_backup, sizeof(unsigned long long) * c.R,
+                             cudaMemcpyDeviceToDevice, c.stream));
+    CUDA_TRY(cudaStreamSynchronize(c.stream));
+    cudaFree(backup);
+    cudaFree(acc_backup);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_cache[key] = {best_w, best_v};
+    }
+    if (variant) *variant = best_w * 10 + best_v;
+    if (best_ms) *best_ms = best;
+    return ETHER_OK;
+}
+
+extern "C" int ether_set_variant(ether_ctx *h, int32_t variant) {
+    if (!h) return fail(ETHER_ERR_ARG, "null context");
+    Ctx &c = h->c;
+    if (!c.fast || c.model != ETHER_MODEL_ISING) return ETHER_OK;
+    const int w = variant / 10, v = variant % 10;
+    if ((w != 4 && w != 8 && w != 16) || (v != 1 && v != 2 && v != 4) || (c.L[0] / 2) % w)
+        return fail(ETHER_ERR_ARG, "variant not available for this lattice");
+    c.vec_bytes = w;
+    c.ising_vpt = v;
     return ETHER_OK;
 }

@@ -79,8 +79,8 @@ struct Ctx {
     float *beta_slot_f = nullptr;
     int32_t *slot_of_rep = nullptr;  // R (slot within group)
     int32_t *rep_of_slot = nullptr;  // R (group*n_slots + slot -> replica)
-    uint32_t *thr = nullptr;     // n_slots * table_entries
-    uint8_t *always = nullptr;   // n_slots * table_entries
+    uint32_t *thr = nullptr;     // n_slots * table_entries: flip iff u32 <= thr
+    int ising_vpt = 1;           // vectors per thread of the simple-cubic Ising kernel
     uint32_t *stream_id = nullptr;  // R
     uint32_t *step = nullptr;       // R (Metropolis sweep counter)
     uint32_t *ovrr_step = nullptr;  // R

@@ -1,10 +1,11 @@
 // k_ising.cu -- Ising Metropolis colour phases (src/Metropolis.f90:39-62 with the
 // Ising branch of update_spin_details.f90:34-35 and Hamiltonian.f90:34-52).
 //
-// Decision: accept iff ΔE <= 0 or u32 < thr, with thr = ceil(2^32 exp(-β ΔE)) taken from a
-// per-temperature table indexed by (site type, own spin, up-neighbour counts per
-// (shell, neighbour species) group).  The table is built in FP64 on the host, so the
-// kernels do integer work only: byte loads, byte sums, one Philox call per 4 sites.
+// Decision: a site flips iff its uniform u32 u <= T, T = max(ceil(2^32 p), 1) - 1 with
+// p = exp(-β ΔE) -- the reference's -βΔE > log(η) for η = u 2^-32, η = 0 included.  T comes
+// from a per-temperature table indexed by (site type, own spin, up-neighbour counts per
+// (shell, neighbour species) group), built in FP64 on the host; the kernels do integer
+// work only: byte loads, byte sums, one Philox call per four sites.
 #include "internal.h"
 #include "rng_math.cuh"
 
@@ -22,21 +23,21 @@ ising_csr_kernel(uint8_t *__restrict__ spins, int N, int col_off, int n_c, uint3
                  const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ nbr,
                  const int32_t *__restrict__ wstride, const uint16_t *__restrict__ itype,
                  const int32_t *__restrict__ type_base, const int32_t *__restrict__ type_half,
-                 const uint32_t *__restrict__ thr, const uint8_t *__restrict__ always,
-                 int table_entries, const int32_t *__restrict__ slot_of_rep,
-                 const uint32_t *__restrict__ stream_id, const uint32_t *__restrict__ step,
-                 uint32_t seed, unsigned long long *__restrict__ acc_count) {
+                 const uint32_t *__restrict__ thr, int table_entries,
+                 const int32_t *__restrict__ slot_of_rep, const uint32_t *__restrict__ stream_id,
+                 const uint32_t *__restrict__ step, uint32_t seed,
+                 unsigned long long *__restrict__ acc_count) {
     const int r = blockIdx.y;
     uint8_t *sp = spins + (size_t)r * N;
     const int slot = slot_of_rep[r];
     const uint32_t *tb = thr + (size_t)slot * table_entries;
-    const uint8_t *al = always + (size_t)slot * table_entries;
-    const uint32_t k1 = stream_id[r], t = step[r];
+    const Keys K = key_schedule(seed, stream_id[r]);
+    const uint32_t t = step[r];
     const uint32_t c3 = kMetro | (colour << 8);
     const int ng = (n_c + 3) >> 2;
     unsigned acc = 0;
     for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
-        U4 o = philox((uint32_t)g, t, 0u, c3, seed, k1);
+        U4 o = philox_k((uint32_t)g, t, 0u, c3, K);
         uint32_t w[4] = {o.x, o.y, o.z, o.w};
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -48,7 +49,7 @@ ising_csr_kernel(uint8_t *__restrict__ spins, int N, int col_off, int n_c, uint3
             int own = sp[s];
             int ty = itype[s];
             int e = type_base[ty] + own * type_half[ty] + idx;
-            if (al[e] || w[q] < tb[e]) {
+            if (w[q] <= tb[e]) {
                 sp[s] = (uint8_t)(own ^ 1);
                 ++acc;
             }
@@ -60,16 +61,13 @@ ising_csr_kernel(uint8_t *__restrict__ spins, int N, int col_off, int n_c, uint3
 // ------------------------------------------------------- simple cubic, colour-split ----
 // Colour c array: rho = (z*L2 + y)*H + xh, H = L1/2, site x = 2*xh + ((y+z+c)&1).
 // All six neighbours live in the other colour's array: same xh in rows (y±1,z), (y,z±1),
-// and xh, xh∓1 in row (y,z).  A thread takes W consecutive bytes of one row; byte sums
-// of 0/1 spins never carry (max 6).
+// and xh, xh∓1 in row (y,z).  A thread takes W consecutive bytes of one row (W | H).
+// Byte sums of 0/1 spins never carry (max 6), and e = n + 7 s (<= 13) is formed for four
+// sites at once.  Flips are applied with one predicated XOR per site and counted with popc.
 template <int W>
-struct Vec;
-template <>
-struct Vec<4> { uint32_t w[1]; };
-template <>
-struct Vec<8> { uint32_t w[2]; };
-template <>
-struct Vec<16> { uint32_t w[4]; };
+struct Vec {
+    uint32_t w[W / 4];
+};
 
 template <int W>
 __device__ __forceinline__ Vec<W> ldv(const uint8_t *p) {
@@ -96,13 +94,13 @@ __device__ __forceinline__ void stv(uint8_t *p, const Vec<W> &v) {
     }
 }
 
-template <int W>
+template <int W, int VPT>
 __global__ void __launch_bounds__(256)
 ising_sc_kernel(uint8_t *__restrict__ spins, int L1, int L2, int L3, uint32_t colour,
-                const uint32_t *__restrict__ thr, const uint8_t *__restrict__ always,
-                int table_entries, const int32_t *__restrict__ slot_of_rep,
-                const uint32_t *__restrict__ stream_id, const uint32_t *__restrict__ step,
-                uint32_t seed, unsigned long long *__restrict__ acc_count) {
+                const uint32_t *__restrict__ thr, int table_entries,
+                const int32_t *__restrict__ slot_of_rep, const uint32_t *__restrict__ stream_id,
+                const uint32_t *__restrict__ step, uint32_t seed,
+                unsigned long long *__restrict__ acc_count) {
     constexpr int NW = W / 4;
     const int r = blockIdx.y;
     const int H = L1 >> 1;
@@ -110,24 +108,17 @@ ising_sc_kernel(uint8_t *__restrict__ spins, int L1, int L2, int L3, uint32_t co
     uint8_t *own_a = spins + (size_t)r * 2 * half + (size_t)colour * half;
     const uint8_t *opp = spins + (size_t)r * 2 * half + (size_t)(colour ^ 1u) * half;
     __shared__ uint32_t s_thr[16];
-    __shared__ uint32_t s_alw;
-    if (threadIdx.x < 14) {
-        int slot = slot_of_rep[r];
-        s_thr[threadIdx.x] = thr[(size_t)slot * table_entries + threadIdx.x];
-    }
-    if (threadIdx.x == 0) {
-        int slot = slot_of_rep[r];
-        uint32_t m = 0;
-        for (int e = 0; e < 14; ++e) m |= (uint32_t)(always[(size_t)slot * table_entries + e] != 0) << e;
-        s_alw = m;
-    }
+    if (threadIdx.x < 14) s_thr[threadIdx.x] = thr[(size_t)slot_of_rep[r] * table_entries + threadIdx.x];
     __syncthreads();
-    const uint32_t alw = s_alw;
-    const uint32_t k1 = stream_id[r], t = step[r];
+    const Keys K = key_schedule(seed, stream_id[r]);
+    const uint32_t t = step[r];
     const uint32_t c3 = kMetro | (colour << 8);
     const int nvec = half / W;
-    unsigned acc = 0;
-    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nvec; v += gridDim.x * blockDim.x) {
+    unsigned flips = 0;
+#pragma unroll
+    for (int j = 0; j < VPT; ++j) {
+        const int v = (blockIdx.x * VPT + j) * blockDim.x + threadIdx.x;
+        if (v >= nvec) break;
         const int rho0 = v * W;
         const int row = rho0 / H;
         const int xh0 = rho0 - row * H;
@@ -141,42 +132,44 @@ ising_sc_kernel(uint8_t *__restrict__ spins, int L1, int L2, int L3, uint32_t co
         Vec<W> b = ldv<W>(opp + (size_t)(z * L2 + yp) * H + xh0);
         Vec<W> c = ldv<W>(opp + (size_t)(zm * L2 + y) * H + xh0);
         Vec<W> d = ldv<W>(opp + (size_t)(zp * L2 + y) * H + xh0);
-        Vec<W> sh;
-        if (p == 0) {  // neighbour x-1 -> xh-1: shift the row window up by one byte
-            uint32_t edge = opp[(size_t)row * H + (xh0 == 0 ? H - 1 : xh0 - 1)];
-#pragma unroll
-            for (int q = NW - 1; q >= 0; --q) {
-                uint32_t lo = (q == 0) ? edge : (o0.w[q - 1] >> 24);
-                sh.w[q] = (o0.w[q] << 8) | lo;
-            }
-        } else {       // neighbour x+1 -> xh+1: shift down by one byte
-            uint32_t edge = opp[(size_t)row * H + (xh0 + W == H ? 0 : xh0 + W)];
-#pragma unroll
-            for (int q = 0; q < NW; ++q) {
-                uint32_t hi = (q == NW - 1) ? edge : (o0.w[q + 1] & 0xFFu);
-                sh.w[q] = (o0.w[q] >> 8) | (hi << 24);
-            }
-        }
+        uint32_t edge;
+        if (p == 0) edge = opp[(size_t)row * H + (xh0 == 0 ? H - 1 : xh0 - 1)];
+        else edge = opp[(size_t)row * H + (xh0 + W == H ? 0 : xh0 + W)];
 #pragma unroll
         for (int q = 0; q < NW; ++q) {
-            uint32_t n = o0.w[q] + sh.w[q] + a.w[q] + b.w[q] + c.w[q] + d.w[q];
-            U4 rnd = philox((uint32_t)((rho0 >> 2) + q), t, 0u, c3, seed, k1);
-            uint32_t u[4] = {rnd.x, rnd.y, rnd.z, rnd.w};
-            uint32_t out = me.w[q];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                uint32_t nk = (n >> (8 * k)) & 0xFFu;
-                uint32_t sk = (me.w[q] >> (8 * k)) & 0xFFu;
-                uint32_t e = nk + 7u * sk;
-                uint32_t accept = ((alw >> e) & 1u) | (u[k] < s_thr[e] ? 1u : 0u);
-                out ^= accept << (8 * k);
-                acc += accept;
+            uint32_t sh;
+            if (p == 0) {  // neighbour x-1 -> xh-1: window shifted up by one byte
+                uint32_t lo = (q == 0) ? (edge << 24) : o0.w[q - 1];
+                sh = __funnelshift_l(lo, o0.w[q], 8);
+            } else {       // neighbour x+1 -> xh+1: window shifted down by one byte
+                uint32_t hi = (q == NW - 1) ? edge : o0.w[q + 1];
+                sh = __funnelshift_r(o0.w[q], hi, 8);
             }
+            const uint32_t s0 = me.w[q];
+            const uint32_t n = o0.w[q] + sh + a.w[q] + b.w[q] + c.w[q] + d.w[q];
+            const uint32_t e4 = n + (s0 << 3) - s0;  // bytewise n + 7 s
+            const U4 rnd = philox_k((uint32_t)((rho0 >> 2) + q), t, 0u, c3, K);
+            uint32_t out = s0;
+            if (rnd.x <= s_thr[e4 & 0xFFu]) out ^= 0x00000001u;
+            if (rnd.y <= s_thr[(e4 >> 8) & 0xFFu]) out ^= 0x00000100u;
+            if (rnd.z <= s_thr[(e4 >> 16) & 0xFFu]) out ^= 0x00010000u;
+            if (rnd.w <= s_thr[e4 >> 24]) out ^= 0x01000000u;
+            flips += __popc(out ^ s0);
             me.w[q] = out;
         }
         stv<W>(own_a + rho0, me);
     }
-    warp_add_count(acc_count + r, acc);
+    warp_add_count(acc_count + r, flips);
+}
+
+template <int W, int VPT>
+static void launch_sc(Ctx &c, int colour) {
+    const int bs = 256;
+    const int nvec = (c.N / 2) / W;
+    dim3 grid((nvec + bs * VPT - 1) / (bs * VPT), c.R);
+    ising_sc_kernel<W, VPT><<<grid, bs, 0, c.stream>>>(
+        c.spins, c.L[0], c.L[1], c.L[2], (uint32_t)colour, c.thr, c.table_entries, c.slot_of_rep,
+        c.stream_id, c.step, c.seed, c.acc_count);
 }
 
 static int blocks_for(const Ctx &c, long work, int bs) {
@@ -191,25 +184,17 @@ static int blocks_for(const Ctx &c, long work, int bs) {
 cudaError_t launch_ising_sweep(Ctx &c, int colour) {
     const int bs = 256;
     if (c.fast) {
-        const int half = c.N / 2;
-        const int nvec = half / c.vec_bytes;
-        dim3 grid(blocks_for(c, nvec, bs), c.R);
-        switch (c.vec_bytes) {
-            case 16:
-                ising_sc_kernel<16><<<grid, bs, 0, c.stream>>>(
-                    c.spins, c.L[0], c.L[1], c.L[2], (uint32_t)colour, c.thr, c.always,
-                    c.table_entries, c.slot_of_rep, c.stream_id, c.step, c.seed, c.acc_count);
-                break;
-            case 8:
-                ising_sc_kernel<8><<<grid, bs, 0, c.stream>>>(
-                    c.spins, c.L[0], c.L[1], c.L[2], (uint32_t)colour, c.thr, c.always,
-                    c.table_entries, c.slot_of_rep, c.stream_id, c.step, c.seed, c.acc_count);
-                break;
-            default:
-                ising_sc_kernel<4><<<grid, bs, 0, c.stream>>>(
-                    c.spins, c.L[0], c.L[1], c.L[2], (uint32_t)colour, c.thr, c.always,
-                    c.table_entries, c.slot_of_rep, c.stream_id, c.step, c.seed, c.acc_count);
-                break;
+        const int key = c.vec_bytes * 10 + c.ising_vpt;
+        switch (key) {
+            case 161: launch_sc<16, 1>(c, colour); break;
+            case 162: launch_sc<16, 2>(c, colour); break;
+            case 164: launch_sc<16, 4>(c, colour); break;
+            case 81: launch_sc<8, 1>(c, colour); break;
+            case 82: launch_sc<8, 2>(c, colour); break;
+            case 84: launch_sc<8, 4>(c, colour); break;
+            case 41: launch_sc<4, 1>(c, colour); break;
+            case 42: launch_sc<4, 2>(c, colour); break;
+            default: launch_sc<4, 4>(c, colour); break;
         }
     } else {
         const int n_c = c.col_off[colour + 1] - c.col_off[colour];
@@ -217,8 +202,8 @@ cudaError_t launch_ising_sweep(Ctx &c, int colour) {
         dim3 grid(blocks_for(c, (n_c + 3) / 4, bs), c.R);
         ising_csr_kernel<<<grid, bs, 0, c.stream>>>(
             c.spins, c.N, c.col_off[colour], n_c, (uint32_t)colour, c.t.row_ptr, c.t.nbr,
-            c.t.wstride, c.t.itype, c.t.type_base, c.t.type_half, c.thr, c.always,
-            c.table_entries, c.slot_of_rep, c.stream_id, c.step, c.seed, c.acc_count);
+            c.t.wstride, c.t.itype, c.t.type_base, c.t.type_half, c.thr, c.table_entries,
+            c.slot_of_rep, c.stream_id, c.step, c.seed, c.acc_count);
     }
     c.launches++;
     return cudaGetLastError();

@@ -213,8 +213,8 @@ ovrr_csr_kernel(float4 *__restrict__ spins4, int N, int col_off, int n_c, uint32
         if (!(a2 > 0.0f)) continue;
         float f = 2.0f * (d / a2);
         float nx = f * hx - S.x, ny = f * hy - S.y, nz = f * hz - S.z;
-        float nr = sqrtf(nx * nx + ny * ny + nz * nz);
-        sp[s] = make_float4(nx / nr, ny / nr, nz / nr, S.w);
+        float inv = 1.0f / sqrtf(nx * nx + ny * ny + nz * nz);
+        sp[s] = make_float4(nx * inv, ny * inv, nz * inv, S.w);
     }
 }
 
@@ -267,8 +267,8 @@ __global__ void fresh_kernel(uint8_t *__restrict__ spins, float4 *__restrict__ s
             nx = rr * cs;
             ny = rr * sn;
         }
-        float nr = sqrtf(nx * nx + ny * ny + nz * nz);
-        spins4[(size_t)r * N + s] = make_float4(nx / nr, ny / nr, nz / nr, nphi);
+        float inv = 1.0f / sqrtf(nx * nx + ny * ny + nz * nz);
+        spins4[(size_t)r * N + s] = make_float4(nx * inv, ny * inv, nz * inv, nphi);
     }
 }
 

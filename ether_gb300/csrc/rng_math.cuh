@@ -45,6 +45,33 @@ ETHER_HD U4 philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t 
     return U4{c0, c1, c2, c3};
 }
 
+// Philox with the ten round keys precomputed once (the key is fixed per replica), so a
+// block costs two 32x32->64 multiplies and two three-input XORs per round.
+struct Keys {
+    uint32_t a[10], b[10];
+};
+ETHER_HD Keys key_schedule(uint32_t k0, uint32_t k1) {
+    Keys K;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        K.a[r] = k0;
+        K.b[r] = k1;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return K;
+}
+ETHER_HD U4 philox_k(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, const Keys &K) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0 = mulhi32(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        uint32_t hi1 = mulhi32(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+        uint32_t n0 = hi1 ^ c1 ^ K.a[r], n2 = hi0 ^ c3 ^ K.b[r];
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    }
+    return U4{c0, c1, c2, c3};
+}
+
 // u32 -> [0,1) with 24 bits, and u32 -> [-1,1) with 24 bits (both exact in FP32).
 ETHER_HD float u01(uint32_t u) { return (float)(u >> 8) * 0x1p-24f; }
 ETHER_HD float upm1(uint32_t u) { return (float)(u >> 8) * 0x1p-23f - 1.0f; }
@@ -61,9 +88,10 @@ ETHER_HD float bits_f(uint32_t b) {
 
 // e^x for x <= 0.  Cody-Waite reduction x = n ln2 + r with a two-part ln2, degree-7
 // Taylor polynomial of e^r (|r| <= ln2/2) in Horner form, times 2^n built from exponent
-// bits.  Flushed to 0 below -87 so that 2^n * p stays a normal number.
+// bits.  Below -87 the result is the smallest normal float: a uniform eta = 0 (log eta =
+// -inf in the reference's test) is still accepted, any larger eta is rejected.
 ETHER_HD float expf_neg(float x) {
-    if (x < -87.0f) return 0.0f;
+    if (x < -87.0f) return 0x1p-126f;
     float n = rintf(x * 1.44269502f);
     float r = x - n * 0.693359375f;
     r = r - n * -2.12194440e-4f;
@@ -152,10 +180,10 @@ ETHER_HD bool propose(bool angle, float dphi, const Spin4 &S, uint32_t c0, uint3
         nx = r * cs;
         ny = r * sn;
     }
-    float nr = sqrtf(nx * nx + ny * ny + nz * nz);
-    out->x = nx / nr;
-    out->y = ny / nr;
-    out->z = nz / nr;
+    float inv = 1.0f / sqrtf(nx * nx + ny * ny + nz * nz);
+    out->x = nx * inv;
+    out->y = ny * inv;
+    out->z = nz * inv;
     out->w = nphi;
     return true;
 }

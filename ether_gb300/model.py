@@ -288,3 +288,12 @@ class Sweep:
 
     def end_sweep(self):
         abi.check(self.lib.ether_end_sweep(self.h))
+
+    def autotune(self):
+        v = C.c_int32(0)
+        ms = C.c_float(0.0)
+        abi.check(self.lib.ether_autotune(self.h, C.byref(v), C.byref(ms)))
+        return v.value, ms.value
+
+    def set_variant(self, variant):
+        abi.check(self.lib.ether_set_variant(self.h, variant))

@@ -206,6 +206,14 @@ int ether_metropolis_phase(ether_ctx *ctx, int32_t colour);
 /* Advance every replica's sweep counter by one (ends a sweep built from phases). */
 int ether_end_sweep(ether_ctx *ctx);
 
+/* Autotuner: times the kernel variants of this context's fast path on its own data
+ * (spins and counters are restored) and keeps the fastest; the choice is cached per size
+ * class for the process.  variant = bytes per thread * 10 + vectors per thread (Ising
+ * simple cubic); best_ms = one colour phase.  Either output may be NULL. */
+int ether_autotune(ether_ctx *ctx, int32_t *variant, float *best_ms);
+/* Force a kernel variant (same encoding as ether_autotune). */
+int ether_set_variant(ether_ctx *ctx, int32_t variant);
+
 /* ---------------------------------------------------------------- lattice builder ---- */
 /* generate_supercell + getting_nbd (src/generate_supercell.f90:38-132,
  * src/getting_nbd.f90:34-82, src/search_nbd.f90:20-64) in O(N) with a cell list, giving

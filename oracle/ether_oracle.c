@@ -56,9 +56,10 @@ static inline double upm1d(uint32_t u) { return (double)(u >> 8) * 0x1p-23 - 1.0
 /* ------------------------------------------------------------- own float math ------- */
 /* exp(x) for x <= 0: Cody-Waite reduction x = n ln2 + r, |r| <= ln2/2, then the degree-7
  * Taylor polynomial of e^r in Horner form, scaled by 2^n built from the exponent bits.
- * Below -87 the result is flushed to 0 so the scaled result never becomes subnormal. */
+ * Below -87 the result is the smallest normal float, so that a uniform eta = 0 (log eta =
+ * -inf in the reference) is still accepted and every larger eta is rejected. */
 float orc_expf_neg(float x) {
-    if (x < -87.0f) return 0.0f;
+    if (x < -87.0f) return 0x1p-126f;
     float n = rintf(x * 1.44269502f);
     float r = x - n * 0.693359375f;
     r = r - n * -2.12194440e-4f;
@@ -509,10 +510,14 @@ static double ising_dE(const orc_sys *sy, const double *ion, int i) {
     return dE;
 }
 
-static uint64_t ising_thr(double beta, double dE) {
-    double p = exp(-beta * dE);
-    if (p >= 1.0) return 4294967296ull;
-    return (uint64_t)ceil(p * 4294967296.0);
+/* Replay acceptance of -beta*dE > log(eta) with eta = u * 2^-32: accept iff u <= T,
+ * T = max(ceil(p * 2^32), 1) - 1, p = exp(-beta*dE).  u = 0 (eta = 0, log = -inf) is always
+ * accepted, exactly as in the reference. */
+static uint32_t ising_thr(double beta, double dE) {
+    double q = exp(-beta * dE) * 4294967296.0;
+    if (q >= 4294967296.0) return 0xFFFFFFFFu;
+    double c = ceil(q);
+    return c < 1.0 ? 0u : (uint32_t)(c - 1.0);
 }
 
 /* One XYZ site update on the FP32 mirror.  Returns 1 when accepted. */
@@ -554,9 +559,8 @@ static int xyz_site_f32(const orc_sys *sy, const double *ion, float *sp4, int i,
         nx = r * cs;
         ny = r * sn;
     }
-    float n2 = nx * nx + ny * ny + nz * nz;
-    float nr = sqrtf(n2);
-    nx = nx / nr; ny = ny / nr; nz = nz / nr;
+    float inv = 1.0f / sqrtf(nx * nx + ny * ny + nz * nz);
+    nx = nx * inv; ny = ny * inv; nz = nz * inv;
     float dx = nx - S[0], dy = ny - S[1], dz = nz - S[2];
     float e = dx * h[0];
     e = fmaf(dy, h[1], e);
@@ -661,7 +665,7 @@ double orc_metropolis_colour(const orc_sys *sy, double *ion, float *spin4, int p
                 philox(rho >> 2, t, 0u, c3, seed, stream, o);
                 uint32_t u = o[rho & 3];
                 double dE = ising_dE(sy, ion, i);
-                if ((uint64_t)u < ising_thr(beta, dE)) {
+                if (u <= ising_thr(beta, dE)) {
                     ION(ion, 3, i) = -ION(ion, 3, i);
                     acc += 1.0;
                 }
@@ -709,8 +713,8 @@ void orc_overrelax_colour(const orc_sys *sy, const double *ion, float *spin4, do
                 float nx = f * h[0] - S[0];
                 float ny = f * h[1] - S[1];
                 float nz = f * h[2] - S[2];
-                float nr = sqrtf(nx * nx + ny * ny + nz * nz);
-                S[0] = nx / nr; S[1] = ny / nr; S[2] = nz / nr;
+                float inv = 1.0f / sqrtf(nx * nx + ny * ny + nz * nz);
+                S[0] = nx * inv; S[1] = ny * inv; S[2] = nz * inv;
             }
         }
     }
@@ -758,8 +762,8 @@ void orc_fresh_spins_colour(const orc_sys *sy, double *ion, float *spin4, uint32
             nx = r * cs;
             ny = r * sn;
         }
-        float nr = sqrtf(nx * nx + ny * ny + nz * nz);
-        S[0] = nx / nr; S[1] = ny / nr; S[2] = nz / nr; S[3] = nphi;
+        float inv = 1.0f / sqrtf(nx * nx + ny * ny + nz * nz);
+        S[0] = nx * inv; S[1] = ny * inv; S[2] = nz * inv; S[3] = nphi;
         for (int c = 0; c < 3; ++c) ION(ion, 1 + c, i) = (double)S[c];
         ION(ion, 5, i) = (double)nphi;
     }

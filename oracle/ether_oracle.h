@@ -54,7 +54,7 @@ typedef struct orc_sys {
 /* ------------------------------------------------------------- lattice build -------- */
 /* generate_supercell (src/generate_supercell.f90:38-132) for the geometry: positions,
  * species and the Checkerboard stagger sign (-1)^(i+j+k+l) (:127).  Initial spins are
- * written by orc_init_spins.  basis_cart[3*l+d] are cartesian basis positions, abc[3*a+d]
+ * written as generate_supercell.f90:42 writes them for Ising (Sz = (-1)**l).  basis_cart[3*l+d] are cartesian basis positions, abc[3*a+d]
  * lattice vector a.  Returns N. */
 int orc_supercell(int nbasis, const double *basis_cart, const int *basis_species,
                   const double *abc, const int sc[3], int checkerboard,
@@ -108,9 +108,10 @@ void orc_overrelaxation_typewriter(const orc_sys *sy, double *ion, int n_steps, 
 /* The same Metropolis step, with the site loop visiting colour 0, 1, ... in order and the
  * random numbers replayed from the counter-based stream shared with the GPU:
  *   key = (seed, stream), counter = (c0, t, c2, purpose | colour<<8).
- * Ising: c0 = rank>>2, c2 = 0, eta = word (rank & 3), accept iff u32 < thr where
- *        thr = ceil(2^32 * min(1, exp(-beta dE))) and dE is evaluated per (shell,
- *        neighbour-species) group.  Spins live in ion(3,:) (= +-1).
+ * Ising: c0 = rank>>2, c2 = 0, u = word (rank & 3), accept iff u <= T where
+ *        T = max(ceil(2^32 exp(-beta dE)), 1) - 1 (clamped to 2^32-1) -- the reference's
+ *        -beta dE > log(eta) for eta = u 2^-32, eta = 0 included -- and dE is evaluated
+ *        per (shell, neighbour-species) group.  Spins live in ion(3,:) (= +-1).
  * XYZ:   c0 = rank, c2 = block.  `prec` = 32 runs the FP32 mirror on spin4 (x,y,z,phi);
  *        prec = 64 runs the same draws in FP64 on ion.
  * Returns accepted / N. */

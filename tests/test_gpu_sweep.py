@@ -16,10 +16,13 @@ FM = [[(1, 1, (-1.0, -1.0, -1.0))]]       # ETHER's sign: J < 0 is ferromagnetic
 AFM_J1_J2 = [[(1, 1, (1.0, 1.0, 1.0))], [(1, 1, (-0.1, -0.1, -0.1))]]
 
 
-def ising_replay(lat, shells, kT, sweeps, flags=0, seed=1992, stream=0, **kw):
+def ising_replay(lat, shells, kT, sweeps, flags=0, seed=1992, stream=0, variant=None,
+                 autotune=False, **kw):
     sw, osys = make_pair(lat, eg.MODEL_ISING, shells, flags=flags, seed=seed, **kw)
     beta = beta_of(kT)
     sw.set_beta(beta)
+    if variant is not None:
+        sw.set_variant(variant)
     sw.set_streams(stream=[stream], step=[0])
     ncol, col, rank = osys.colouring()
     gcol, grank = sw.colouring()
@@ -28,6 +31,8 @@ def ising_replay(lat, shells, kT, sweeps, flags=0, seed=1992, stream=0, **kw):
     np.testing.assert_array_equal(rank, grank)
     ion = random_ising(lat, 7)
     sw.set_spins(ion)
+    if autotune:
+        sw.autotune()
     acc_o = []
     for t in range(sweeps):
         acc_o.append(osys.metropolis_colour(ion, None, 64, beta, seed, stream, t, col, rank, ncol))
@@ -46,6 +51,21 @@ def test_ising_sc_bit_exact(L, flags, kT):
     assert ao == pytest.approx(ag, abs=1e-12)
     if L == 16 and flags == 0:
         assert sw.info().fast_path == 1
+
+
+@pytest.mark.parametrize("variant", [161, 162, 164, 81, 82, 84, 41, 42, 44])
+def test_ising_sc_every_kernel_variant_bit_exact(variant):
+    lat = eg.simple_cubic((32, 8, 6))
+    sw, ion, g, ao, ag = ising_replay(lat, FM, 4.511, 8, variant=variant)
+    np.testing.assert_array_equal(g[:, 3], ion[:, 3])
+    assert ao == pytest.approx(ag, abs=1e-12)
+
+
+def test_autotuner_restores_state_and_stays_bit_exact():
+    lat = eg.simple_cubic(32)
+    sw, ion, g, ao, ag = ising_replay(lat, FM, 4.511, 12, autotune=True)
+    np.testing.assert_array_equal(g[:, 3], ion[:, 3])
+    assert ao == pytest.approx(ag, abs=1e-12)
 
 
 def test_ising_open_bc_and_zeeman_bit_exact():
