@@ -150,11 +150,15 @@ def make_workload(model, L, replicas, seed=1992):
     return lat, j, sw, ion, beta
 
 
-def run_gpu(model, L, replicas, steps, warmup, rank, world):
+def run_gpu(model, L, replicas, steps, warmup, rank, world, force_variant=0):
     import ether_gb300 as eg
     lat, j, sw, ion, beta = make_workload(model, L, replicas, seed=1992 + 7919 * rank)
     sw.set_spins(ion)
-    variant, tuned_ms = sw.autotune()
+    if force_variant:
+        sw.set_variant(force_variant)
+        variant = force_variant
+    else:
+        variant, tuned_ms = sw.autotune()
     N, R = lat.N, replicas
     ev = Events(sw.stream())
     for _ in range(warmup):
@@ -275,6 +279,7 @@ def main():
     ap.add_argument("--replicas", type=int, default=0)
     ap.add_argument("--cpu-mcs", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--variant", type=int, default=0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -317,7 +322,7 @@ def main():
         print(json.dumps(line))
         return 0
 
-    res = run_gpu(model, args.L, replicas, args.steps, args.warmup, rank, world)
+    res = run_gpu(model, args.L, replicas, args.steps, args.warmup, rank, world, args.variant)
     if rank != 0:
         return 0
     peaks = {}

@@ -31,13 +31,13 @@ ising_csr_kernel(uint8_t *__restrict__ spins, int N, int col_off, int n_c, uint3
     uint8_t *sp = spins + (size_t)r * N;
     const int slot = slot_of_rep[r];
     const uint32_t *tb = thr + (size_t)slot * table_entries;
-    const Keys K = key_schedule(seed, stream_id[r]);
+    const uint32_t stream = stream_id[r];
     const uint32_t t = step[r];
     const uint32_t c3 = kMetro | (colour << 8);
     const int ng = (n_c + 3) >> 2;
     unsigned acc = 0;
     for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
-        U4 o = philox_k((uint32_t)g, t, 0u, c3, K);
+        U4 o = draw((uint32_t)g, t, stream, c3, seed);
         uint32_t w[4] = {o.x, o.y, o.z, o.w};
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -110,54 +110,63 @@ ising_sc_kernel(uint8_t *__restrict__ spins, int L1, int L2, int L3, uint32_t co
     __shared__ uint32_t s_thr[16];
     if (threadIdx.x < 14) s_thr[threadIdx.x] = thr[(size_t)slot_of_rep[r] * table_entries + threadIdx.x];
     __syncthreads();
-    const Keys K = key_schedule(seed, stream_id[r]);
+    const uint32_t stream = stream_id[r];
     const uint32_t t = step[r];
     const uint32_t c3 = kMetro | (colour << 8);
     const int nvec = half / W;
     unsigned flips = 0;
+    // loads of all VPT vectors first, so their latencies overlap
+    Vec<W> me[VPT], o0[VPT], a[VPT], b[VPT], c[VPT], d[VPT];
+    uint32_t edge[VPT];
+    int rho0[VPT], par[VPT];
+    bool live[VPT];
 #pragma unroll
     for (int j = 0; j < VPT; ++j) {
         const int v = (blockIdx.x * VPT + j) * blockDim.x + threadIdx.x;
-        if (v >= nvec) break;
-        const int rho0 = v * W;
-        const int row = rho0 / H;
-        const int xh0 = rho0 - row * H;
+        live[j] = v < nvec;
+        const int vv = live[j] ? v : 0;
+        rho0[j] = vv * W;
+        const int row = rho0[j] / H;
+        const int xh0 = rho0[j] - row * H;
         const int y = row % L2, z = row / L2;
-        const int p = (y + z + (int)colour) & 1;
+        par[j] = (y + z + (int)colour) & 1;
         const int ym = (y == 0 ? L2 - 1 : y - 1), yp = (y == L2 - 1 ? 0 : y + 1);
         const int zm = (z == 0 ? L3 - 1 : z - 1), zp = (z == L3 - 1 ? 0 : z + 1);
-        Vec<W> me = ldv<W>(own_a + rho0);
-        Vec<W> o0 = ldv<W>(opp + rho0);
-        Vec<W> a = ldv<W>(opp + (size_t)(z * L2 + ym) * H + xh0);
-        Vec<W> b = ldv<W>(opp + (size_t)(z * L2 + yp) * H + xh0);
-        Vec<W> c = ldv<W>(opp + (size_t)(zm * L2 + y) * H + xh0);
-        Vec<W> d = ldv<W>(opp + (size_t)(zp * L2 + y) * H + xh0);
-        uint32_t edge;
-        if (p == 0) edge = opp[(size_t)row * H + (xh0 == 0 ? H - 1 : xh0 - 1)];
-        else edge = opp[(size_t)row * H + (xh0 + W == H ? 0 : xh0 + W)];
+        me[j] = ldv<W>(own_a + rho0[j]);
+        o0[j] = ldv<W>(opp + rho0[j]);
+        a[j] = ldv<W>(opp + (size_t)(z * L2 + ym) * H + xh0);
+        b[j] = ldv<W>(opp + (size_t)(z * L2 + yp) * H + xh0);
+        c[j] = ldv<W>(opp + (size_t)(zm * L2 + y) * H + xh0);
+        d[j] = ldv<W>(opp + (size_t)(zp * L2 + y) * H + xh0);
+        if (par[j] == 0) edge[j] = opp[(size_t)row * H + (xh0 == 0 ? H - 1 : xh0 - 1)];
+        else edge[j] = opp[(size_t)row * H + (xh0 + W == H ? 0 : xh0 + W)];
+    }
+#pragma unroll
+    for (int j = 0; j < VPT; ++j) {
+        if (!live[j]) break;
 #pragma unroll
         for (int q = 0; q < NW; ++q) {
             uint32_t sh;
-            if (p == 0) {  // neighbour x-1 -> xh-1: window shifted up by one byte
-                uint32_t lo = (q == 0) ? (edge << 24) : o0.w[q - 1];
-                sh = __funnelshift_l(lo, o0.w[q], 8);
-            } else {       // neighbour x+1 -> xh+1: window shifted down by one byte
-                uint32_t hi = (q == NW - 1) ? edge : o0.w[q + 1];
-                sh = __funnelshift_r(o0.w[q], hi, 8);
+            if (par[j] == 0) {  // neighbour x-1 -> xh-1: window shifted up by one byte
+                uint32_t lo = (q == 0) ? (edge[j] << 24) : o0[j].w[q - 1];
+                sh = __funnelshift_l(lo, o0[j].w[q], 8);
+            } else {            // neighbour x+1 -> xh+1: window shifted down by one byte
+                uint32_t hi = (q == NW - 1) ? edge[j] : o0[j].w[q + 1];
+                sh = __funnelshift_r(o0[j].w[q], hi, 8);
             }
-            const uint32_t s0 = me.w[q];
-            const uint32_t n = o0.w[q] + sh + a.w[q] + b.w[q] + c.w[q] + d.w[q];
+            const uint32_t s0 = me[j].w[q];
+            const uint32_t n = o0[j].w[q] + sh + a[j].w[q] + b[j].w[q] + c[j].w[q] + d[j].w[q];
             const uint32_t e4 = n + (s0 << 3) - s0;  // bytewise n + 7 s
-            const U4 rnd = philox_k((uint32_t)((rho0 >> 2) + q), t, 0u, c3, K);
+            const U4 rnd = draw((uint32_t)((rho0[j] >> 2) + q), t, stream, c3, seed);
             uint32_t out = s0;
             if (rnd.x <= s_thr[e4 & 0xFFu]) out ^= 0x00000001u;
             if (rnd.y <= s_thr[(e4 >> 8) & 0xFFu]) out ^= 0x00000100u;
             if (rnd.z <= s_thr[(e4 >> 16) & 0xFFu]) out ^= 0x00010000u;
             if (rnd.w <= s_thr[e4 >> 24]) out ^= 0x01000000u;
             flips += __popc(out ^ s0);
-            me.w[q] = out;
+            me[j].w[q] = out;
         }
-        stv<W>(own_a + rho0, me);
+        stv<W>(own_a + rho0[j], me[j]);
     }
     warp_add_count(acc_count + r, flips);
 }

@@ -163,7 +163,7 @@ __global__ void pt_kernel(const double *__restrict__ E, int R, int n_slots, int 
     bool acc;
     if (delta > 0.0) acc = true;
     else {
-        U4 o = philox((uint32_t)s, (uint32_t)swap_count, 0u, kPT, seed, 0x50540000u + (uint32_t)g);
+        U4 o = draw((uint32_t)s, (uint32_t)swap_count, 0x50540000u + (uint32_t)g, kPT, seed);
         acc = ((double)o.x * 0x1p-32) < exp(delta);
     }
     if (!acc) return;

@@ -55,13 +55,13 @@ __device__ __forceinline__ float delta_e(const XyzParams &P, int s, const float4
 
 __device__ __forceinline__ bool metro_site(const XyzParams &P, float4 *sp, int s, uint32_t rho,
                                            float hx, float hy, float hz, float beta_f,
-                                           uint32_t t, uint32_t c3, uint32_t seed, uint32_t k1) {
+                                           uint32_t t, uint32_t c3, uint32_t seed, uint32_t stream) {
     const float4 S = sp[s];
-    U4 b0 = philox(rho, t, 0u, c3, seed, k1);
+    U4 b0 = draw(rho, t, stream, c3, seed);
     float eta = u01(b0.x);
     Spin4 n;
     Spin4 So{S.x, S.y, S.z, S.w};
-    if (!propose(P.angle != 0, P.dphi, So, rho, t, c3, seed, k1, b0, &n)) return false;
+    if (!propose(P.angle != 0, P.dphi, So, rho, t, stream, c3, seed, b0, &n)) return false;
     float e = delta_e(P, s, S, n, hx, hy, hz);
     bool acc = (e <= 0.0f) || (eta < expf_neg(-(beta_f * e)));
     if (acc) sp[s] = make_float4(n.x, n.y, n.z, n.w);
@@ -192,7 +192,7 @@ ovrr_csr_kernel(float4 *__restrict__ spins4, int N, int col_off, int n_c, uint32
     for (int rho = blockIdx.x * blockDim.x + threadIdx.x; rho < n_c; rho += gridDim.x * blockDim.x) {
         const int s = col_off + rho;
         if (part < 1.0f) {
-            U4 o = philox((uint32_t)rho, t, (uint32_t)pass, c3, seed, k1);
+            U4 o = draw((uint32_t)rho, t, k1, c3 | ((uint32_t)pass << 16), seed);
             if (!(u01(o.x) < part)) continue;
         }
         float hx = 0.f, hy = 0.f, hz = 0.f;
@@ -235,14 +235,14 @@ __global__ void fresh_kernel(uint8_t *__restrict__ spins, float4 *__restrict__ s
         }
         const uint32_t i = (uint32_t)site_of_storage[s];
         float4 S = spins4[(size_t)r * N + s];
-        U4 o = philox(i, call, 0u, kFresh, seed, k1);
+        U4 o = draw(i, call, k1, kFresh, seed);
         float nx, ny, nz, nphi;
         if (!angle) {
             float v1 = 0.f, v2 = 0.f, q = 0.f;
             bool ok = false;
             U4 w = o;
             for (int p = 0; p < kMarsagliaMaxPairs; ++p) {
-                if (p >= 2 && (p & 1) == 0) w = philox(i, call, (uint32_t)(p / 2), kFresh, seed, k1);
+                if (p >= 2 && (p & 1) == 0) w = draw(i, call, k1, kFresh | ((uint32_t)(p / 2) << 16), seed);
                 uint32_t a = (p & 1) ? w.z : w.x;
                 uint32_t b = (p & 1) ? w.w : w.y;
                 v1 = upm1(a);

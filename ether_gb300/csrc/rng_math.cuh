@@ -2,9 +2,11 @@
 //
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) replaces libgfortran's random_number
 // (src/get_random_num.f90:29).  Every draw is addressed by
-//     key     = (seed, stream)                    stream = per replica
-//     counter = (c0, t, c2, purpose | colour << 8)
-// so a draw depends only on (replica, sweep, site), never on thread scheduling.
+//     key     = (seed, 0x45544852)                            the same for a whole launch
+//     counter = (c0, t, stream, purpose | colour << 8 | block << 16)
+// where stream identifies the replica.  A draw depends only on (replica, sweep, site),
+// never on thread scheduling, and because the key is launch-uniform its round schedule is
+// computed once per warp in the uniform datapath instead of in every thread's registers.
 //
 // The kernels are compiled with --fmad=false: every + and * rounds on its own, and the
 // only fused multiply-adds are the explicit fmaf() calls below.  The FP32 results are
@@ -21,6 +23,7 @@
 namespace ether {
 
 enum Purpose : uint32_t { kMetro = 0, kOvrr = 1, kFresh = 2, kPT = 3 };
+constexpr uint32_t kKey1 = 0x45544852u;
 
 struct U4 { uint32_t x, y, z, w; };
 
@@ -45,31 +48,8 @@ ETHER_HD U4 philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t 
     return U4{c0, c1, c2, c3};
 }
 
-// Philox with the ten round keys precomputed once (the key is fixed per replica), so a
-// block costs two 32x32->64 multiplies and two three-input XORs per round.
-struct Keys {
-    uint32_t a[10], b[10];
-};
-ETHER_HD Keys key_schedule(uint32_t k0, uint32_t k1) {
-    Keys K;
-#pragma unroll
-    for (int r = 0; r < 10; ++r) {
-        K.a[r] = k0;
-        K.b[r] = k1;
-        k0 += 0x9E3779B9u;
-        k1 += 0xBB67AE85u;
-    }
-    return K;
-}
-ETHER_HD U4 philox_k(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, const Keys &K) {
-#pragma unroll
-    for (int r = 0; r < 10; ++r) {
-        uint32_t hi0 = mulhi32(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
-        uint32_t hi1 = mulhi32(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
-        uint32_t n0 = hi1 ^ c1 ^ K.a[r], n2 = hi0 ^ c3 ^ K.b[r];
-        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
-    }
-    return U4{c0, c1, c2, c3};
+ETHER_HD U4 draw(uint32_t c0, uint32_t t, uint32_t stream, uint32_t tag, uint32_t seed) {
+    return philox(c0, t, stream, tag, seed, kKey1);
 }
 
 // u32 -> [0,1) with 24 bits, and u32 -> [-1,1) with 24 bits (both exact in FP32).
@@ -135,35 +115,42 @@ constexpr float kPiF = 3.14159274f;
 constexpr float kTwoPiF = 6.28318548f;
 constexpr int kMarsagliaMaxPairs = 64;
 
-// Pair p of a Metropolis proposal: p = 0 uses words 1,2 of block 0 (word 0 is eta);
-// p >= 1 uses block (p+1)/2, words 0,1 for odd p and 2,3 for even p.
-ETHER_HD void metro_pair(uint32_t c0, uint32_t t, uint32_t c3, uint32_t k0, uint32_t k1,
-                         const U4 &b0, int p, uint32_t *a, uint32_t *b) {
-    if (p == 0) { *a = b0.y; *b = b0.z; return; }
-    U4 o = philox(c0, t, (uint32_t)((p + 1) / 2), c3, k0, k1);
-    if (p & 1) { *a = o.x; *b = o.y; } else { *a = o.z; *b = o.w; }
-}
-
-// Proposal of update_spin_details (src/update_spin_details.f90:30-51) in FP32.
-// Marsaglia (George_Marsaglia.f90:29-39) or ANGLE, then normalisation.  Returns false if
-// 64 Marsaglia pairs were all rejected (probability ~1e-43): the site keeps its spin.
+// Proposal of update_spin_details (src/update_spin_details.f90:30-51) in FP32: Marsaglia
+// (George_Marsaglia.f90:29-39) or ANGLE, then normalisation.  The Marsaglia pairs come in
+// order p = 0, 1, 2, ...: pair 0 is words 1,2 of block 0 (word 0 is eta); pair p >= 1 is
+// block (p+1)/2, words 0,1 for odd p and 2,3 for even p.  The first accepted pair wins.
+// Blocks 0 and 1 (pairs 0-2, 99% of sites) are evaluated without branches so a warp does
+// not serialise on the rejection loop; later pairs come from a loop taken by ~1% of sites.
+// Returns false if 64 pairs were all rejected (probability ~1e-43): no proposal.
 struct Spin4 { float x, y, z, w; };
 
+ETHER_HD bool marsaglia(uint32_t c0, uint32_t t, uint32_t stream, uint32_t tag, uint32_t seed,
+                        const U4 &b0, float *v1o, float *v2o, float *so) {
+    const U4 b1 = draw(c0, t, stream, tag | (1u << 16), seed);
+    const float a0 = upm1(b0.y), a1 = upm1(b0.z);
+    const float c0a = upm1(b1.x), c1a = upm1(b1.y);
+    const float d0 = upm1(b1.z), d1 = upm1(b1.w);
+    const float s0 = a0 * a0 + a1 * a1, s1 = c0a * c0a + c1a * c1a, s2 = d0 * d0 + d1 * d1;
+    if (s0 < 1.0f) { *v1o = a0; *v2o = a1; *so = s0; return true; }
+    if (s1 < 1.0f) { *v1o = c0a; *v2o = c1a; *so = s1; return true; }
+    if (s2 < 1.0f) { *v1o = d0; *v2o = d1; *so = s2; return true; }
+    for (int blk = 2; blk <= kMarsagliaMaxPairs / 2; ++blk) {
+        const U4 o = draw(c0, t, stream, tag | ((uint32_t)blk << 16), seed);
+        float v1 = upm1(o.x), v2 = upm1(o.y), s = v1 * v1 + v2 * v2;
+        if (s < 1.0f) { *v1o = v1; *v2o = v2; *so = s; return true; }
+        if (2 * blk == kMarsagliaMaxPairs) break;
+        v1 = upm1(o.z); v2 = upm1(o.w); s = v1 * v1 + v2 * v2;
+        if (s < 1.0f) { *v1o = v1; *v2o = v2; *so = s; return true; }
+    }
+    return false;
+}
+
 ETHER_HD bool propose(bool angle, float dphi, const Spin4 &S, uint32_t c0, uint32_t t,
-                      uint32_t c3, uint32_t k0, uint32_t k1, const U4 &b0, Spin4 *out) {
+                      uint32_t stream, uint32_t tag, uint32_t seed, const U4 &b0, Spin4 *out) {
     float nx, ny, nz, nphi;
     if (!angle) {
-        float v1 = 0.f, v2 = 0.f, s = 0.f;
-        bool ok = false;
-        for (int p = 0; p < kMarsagliaMaxPairs; ++p) {
-            uint32_t a, b;
-            metro_pair(c0, t, c3, k0, k1, b0, p, &a, &b);
-            v1 = upm1(a);
-            v2 = upm1(b);
-            s = v1 * v1 + v2 * v2;
-            if (s < 1.0f) { ok = true; break; }
-        }
-        if (!ok) return false;
+        float v1, v2, s;
+        if (!marsaglia(c0, t, stream, tag, seed, b0, &v1, &v2, &s)) return false;
         float tq = sqrtf(1.0f - s);
         nx = (2.0f * v1) * tq;
         ny = (2.0f * v2) * tq;

@@ -38,9 +38,14 @@ void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t ou
     out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
-static void philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t seed,
-                   uint32_t stream, uint32_t out[4]) {
-    uint32_t c[4] = {c0, c1, c2, c3}, k[2] = {seed, stream};
+/* Counter-based draws of the Checkerboard mode, shared with the GPU kernels:
+ *   key = (seed, 0x45544852), counter = (c0, t, stream, purpose | colour << 8 | block << 16).
+ * The key is the same for every replica of a run, the replica's stream id sits in the
+ * counter. */
+#define ETHER_KEY1 0x45544852u
+static void draw(uint32_t c0, uint32_t t, uint32_t stream, uint32_t tag, uint32_t seed,
+                 uint32_t out[4]) {
+    uint32_t c[4] = {c0, t, stream, tag}, k[2] = {seed, ETHER_KEY1};
     orc_philox4x32_10(c, k, out);
 }
 
@@ -478,7 +483,7 @@ static void metro_pair(uint32_t c0, uint32_t t, uint32_t c3, uint32_t seed, uint
                        const uint32_t blk0[4], int p, uint32_t *a, uint32_t *b) {
     if (p == 0) { *a = blk0[1]; *b = blk0[2]; return; }
     uint32_t o[4];
-    philox(c0, t, (uint32_t)((p + 1) / 2), c3, seed, stream, o);
+    draw(c0, t, stream, c3 | ((uint32_t)((p + 1) / 2) << 16), seed, o);
     if (p & 1) { *a = o[0]; *b = o[1]; } else { *a = o[2]; *b = o[3]; }
 }
 
@@ -528,7 +533,7 @@ static int xyz_site_f32(const orc_sys *sy, const double *ion, float *sp4, int i,
     field_f32(sy, ion, sp4, i, h);
     float *S = sp4 + 4 * (size_t)i;
     uint32_t blk[4];
-    philox(rho, t, 0u, c3, seed, stream, blk);
+    draw(rho, t, stream, c3, seed, blk);
     float eta = u01f(blk[0]);
     float nx, ny, nz, nphi;
     if (!sy->angle) {
@@ -590,7 +595,7 @@ static int xyz_site_f32(const orc_sys *sy, const double *ion, float *sp4, int i,
 static int xyz_site_f64(const orc_sys *sy, double *ion, int i, double beta, uint32_t seed,
                         uint32_t stream, uint32_t t, uint32_t rho, uint32_t c3) {
     uint32_t blk[4];
-    philox(rho, t, 0u, c3, seed, stream, blk);
+    draw(rho, t, stream, c3, seed, blk);
     double eta = u01d(blk[0]);
     double prev[5], upd[5];
     for (int c = 0; c < 5; ++c) prev[c] = ION(ion, 1 + c, i);
@@ -662,7 +667,7 @@ double orc_metropolis_colour(const orc_sys *sy, double *ion, float *spin4, int p
             uint32_t rho = (uint32_t)rank_in_colour[i];
             if (sy->model == 0) {
                 uint32_t o[4];
-                philox(rho >> 2, t, 0u, c3, seed, stream, o);
+                draw(rho >> 2, t, stream, c3, seed, o);
                 uint32_t u = o[rho & 3];
                 double dE = ising_dE(sy, ion, i);
                 if (u <= ising_thr(beta, dE)) {
@@ -696,7 +701,7 @@ void orc_overrelax_colour(const orc_sys *sy, const double *ion, float *spin4, do
                 int i = lists[c][q];
                 if (p == full) {
                     uint32_t o[4];
-                    philox((uint32_t)rank_in_colour[i], t, (uint32_t)p, c3, seed, stream, o);
+                    draw((uint32_t)rank_in_colour[i], t, stream, c3 | ((uint32_t)p << 16), seed, o);
                     if (!(u01f(o[0]) < part)) continue;
                 }
                 float h[3];
@@ -730,7 +735,7 @@ void orc_fresh_spins_colour(const orc_sys *sy, double *ion, float *spin4, uint32
             continue;
         }
         uint32_t o[4];
-        philox((uint32_t)i, call, 0u, P_FRESH, seed, stream, o);
+        draw((uint32_t)i, call, stream, P_FRESH, seed, o);
         float *S = spin4 + 4 * (size_t)i;
         float nx, ny, nz, nphi;
         if (!sy->angle) {
@@ -739,7 +744,7 @@ void orc_fresh_spins_colour(const orc_sys *sy, double *ion, float *spin4, uint32
             for (int p = 0; p < MARSAGLIA_MAX_PAIRS; ++p) {
                 uint32_t w[4];
                 if (p < 2) memcpy(w, o, sizeof(w));
-                else philox((uint32_t)i, call, (uint32_t)(p / 2), P_FRESH, seed, stream, w);
+                else draw((uint32_t)i, call, stream, P_FRESH | ((uint32_t)(p / 2) << 16), seed, w);
                 v1 = upm1f(w[2 * (p & 1)]);
                 v2 = upm1f(w[2 * (p & 1) + 1]);
                 s = v1 * v1 + v2 * v2;
@@ -783,7 +788,7 @@ int orc_parallel_tempering(int n_slots, const double *beta, const double *energy
         if (delta > 0.0) acc = 1;
         else {
             uint32_t o[4];
-            philox((uint32_t)s, (uint32_t)swap_count, 0u, P_PT, seed, 0x50540000u + group, o);
+            draw((uint32_t)s, (uint32_t)swap_count, 0x50540000u + group, P_PT, seed, o);
             double r = (double)o[0] * 0x1p-32;
             acc = r < exp(delta);
         }

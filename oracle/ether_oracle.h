@@ -107,12 +107,12 @@ void orc_overrelaxation_typewriter(const orc_sys *sy, double *ion, int n_steps, 
 /* -------------------------------------------- colour-ordered (Checkerboard) mode ---- */
 /* The same Metropolis step, with the site loop visiting colour 0, 1, ... in order and the
  * random numbers replayed from the counter-based stream shared with the GPU:
- *   key = (seed, stream), counter = (c0, t, c2, purpose | colour<<8).
- * Ising: c0 = rank>>2, c2 = 0, u = word (rank & 3), accept iff u <= T where
+ *   key = (seed, 0x45544852), counter = (c0, t, stream, purpose | colour<<8 | block<<16).
+ * Ising: c0 = rank>>2, block 0, u = word (rank & 3), accept iff u <= T where
  *        T = max(ceil(2^32 exp(-beta dE)), 1) - 1 (clamped to 2^32-1) -- the reference's
  *        -beta dE > log(eta) for eta = u 2^-32, eta = 0 included -- and dE is evaluated
  *        per (shell, neighbour-species) group.  Spins live in ion(3,:) (= +-1).
- * XYZ:   c0 = rank, c2 = block.  `prec` = 32 runs the FP32 mirror on spin4 (x,y,z,phi);
+ * XYZ:   c0 = rank, block = 0, 1, ... (pairs of the Marsaglia rejection loop).  `prec` = 32 runs the FP32 mirror on spin4 (x,y,z,phi);
  *        prec = 64 runs the same draws in FP64 on ion.
  * Returns accepted / N. */
 double orc_metropolis_colour(const orc_sys *sy, double *ion, float *spin4, int prec,
@@ -134,7 +134,7 @@ void orc_fresh_spins_colour(const orc_sys *sy, double *ion, float *spin4, uint32
  * slot_of_rep / rep_of_slot: permutation; energy[rep]; beta[slot].  Pairs (s, s+1) with
  * s even when swap_count is even, odd otherwise.  The lower slot decides; delta =
  * -(beta[s+1]-beta[s])*(E_lo - E_hi); accept iff delta > 0 or u < exp(delta), u from
- * the counter stream key=(seed, 0x50540000 + group), ctr=(s, swap_count, 0, 3).
+ * the counter stream key=(seed, 0x45544852), ctr=(s, swap_count, 0x50540000 + group, 3).
  * mode 0: exchange configurations (swap the permutation); mode 1: the reference's
  * effective behaviour, where only the higher slot adopts the lower slot's configuration
  * (copy_from[hi] = lo).  Returns the number of accepted pairs. */

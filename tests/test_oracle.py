@@ -172,7 +172,7 @@ def test_parallel_tempering_rule():
     # pairs (0,1): delta = -(2-1)*(-1+5) = -4; (2,3): delta = -(4-3)*(-2+10) = -8
     u = []
     for s in (0, 2):
-        o = po.philox([s, 2, 0, 3], [7, 0x50540000])
+        o = po.philox([s, 2, 0x50540000, 3], [7, 0x45544852])
         u.append(o[0] * 2.0 ** -32)
     want = [u[0] < math.exp(-4.0), u[1] < math.exp(-8.0)]
     assert n == sum(want)
