@@ -330,7 +330,7 @@ extern "C" int ether_create(const ether_desc *d, ether_ctx **out) {
         if (ok) {
             c.L[0] = L1; c.L[1] = L2; c.L[2] = L3;
             const int H = L1 / 2;
-            c.vec_bytes = (H % 16 == 0) ? 16 : (H % 8 == 0) ? 8 : (H % 4 == 0) ? 4 : 0;
+            c.vec_bytes = (H % 16 == 0) ? 16 : (H % 8 == 0) ? 8 : 0;
             c.fast = (c.model == ETHER_MODEL_XYZ) || c.vec_bytes > 0;
         }
     }
@@ -857,7 +857,7 @@ extern "C" int ether_autotune(ether_ctx *h, int32_t *variant, float *best_ms) {
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    for (int w : {16, 8, 4}) {
+    for (int w : {16, 8}) {
         if (H % w) continue;
         for (int v : {1, 2, 4}) {
             c.vec_bytes = w;
@@ -904,7 +904,7 @@ extern "C" int ether_set_variant(ether_ctx *h, int32_t variant) {
     Ctx &c = h->c;
     if (!c.fast || c.model != ETHER_MODEL_ISING) return ETHER_OK;
     const int w = variant / 10, v = variant % 10;
-    if ((w != 4 && w != 8 && w != 16) || (v != 1 && v != 2 && v != 4) || (c.L[0] / 2) % w)
+    if ((w != 8 && w != 16) || (v != 1 && v != 2 && v != 4) || (c.L[0] / 2) % w)
         return fail(ETHER_ERR_ARG, "variant not available for this lattice");
     c.vec_bytes = w;
     c.ising_vpt = v;

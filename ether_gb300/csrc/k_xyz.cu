@@ -63,7 +63,9 @@ __device__ __forceinline__ bool metro_site(const XyzParams &P, float4 *sp, int s
     Spin4 So{S.x, S.y, S.z, S.w};
     if (!propose(P.angle != 0, P.dphi, So, rho, t, stream, c3, seed, b0, &n)) return false;
     float e = delta_e(P, s, S, n, hx, hy, hz);
-    bool acc = (e <= 0.0f) || (eta < expf_neg(-(beta_f * e)));
+    // exp evaluated on every lane (no divergent short-circuit); e <= 0 accepts regardless
+    const float p = expf_neg(-(beta_f * fmaxf(e, 0.0f)));
+    bool acc = (e <= 0.0f) || (eta < p);
     if (acc) sp[s] = make_float4(n.x, n.y, n.z, n.w);
     return acc;
 }
@@ -121,12 +123,12 @@ __device__ __forceinline__ Acc3 sc_field(const float4 *__restrict__ opp, int L1,
     int xh_m, xh_p;
     if (p == 0) { xh_m = (xh == 0 ? H - 1 : xh - 1); xh_p = xh; }
     else { xh_m = xh; xh_p = (xh == H - 1 ? 0 : xh + 1); }
-    const float4 Sxm = opp[(size_t)row * H + xh_m];
-    const float4 Sxp = opp[(size_t)row * H + xh_p];
-    const float4 Sym = opp[(size_t)(z * L2 + ym) * H + xh];
-    const float4 Syp = opp[(size_t)(z * L2 + yp) * H + xh];
-    const float4 Szm = opp[(size_t)(zm * L2 + y) * H + xh];
-    const float4 Szp = opp[(size_t)(zp * L2 + y) * H + xh];
+    const float4 Sxm = opp[row * H + xh_m];
+    const float4 Sxp = opp[row * H + xh_p];
+    const float4 Sym = opp[(z * L2 + ym) * H + xh];
+    const float4 Syp = opp[(z * L2 + yp) * H + xh];
+    const float4 Szm = opp[(zm * L2 + y) * H + xh];
+    const float4 Szp = opp[(zp * L2 + y) * H + xh];
     Acc3 h{0.f, 0.f, 0.f};
     // below
     if (z == L3 - 1) { fma3(h, jx, jy, jz, Szp); fma3(h, jx, jy, jz, Szm); }

@@ -666,9 +666,13 @@ double orc_metropolis_colour(const orc_sys *sy, double *ion, float *spin4, int p
             int i = lists[c][q];
             uint32_t rho = (uint32_t)rank_in_colour[i];
             if (sy->model == 0) {
-                uint32_t o[4];
-                draw(rho >> 2, t, stream, c3, seed, o);
-                uint32_t u = o[rho & 3];
+                /* u32 of site rho: high half = halfword (rho & 7) of block 0, low half =
+                 * the same halfword of block 1, of the group rho >> 3. */
+                uint32_t hi[4], lo[4];
+                draw(rho >> 3, t, stream, c3, seed, hi);
+                draw(rho >> 3, t, stream, c3 | (1u << 16), seed, lo);
+                const uint32_t k = rho & 7, sh = 16u * (k & 1u);
+                uint32_t u = (((hi[k >> 1] >> sh) & 0xFFFFu) << 16) | ((lo[k >> 1] >> sh) & 0xFFFFu);
                 double dE = ising_dE(sy, ion, i);
                 if (u <= ising_thr(beta, dE)) {
                     ION(ion, 3, i) = -ION(ion, 3, i);

@@ -108,7 +108,8 @@ void orc_overrelaxation_typewriter(const orc_sys *sy, double *ion, int n_steps, 
 /* The same Metropolis step, with the site loop visiting colour 0, 1, ... in order and the
  * random numbers replayed from the counter-based stream shared with the GPU:
  *   key = (seed, 0x45544852), counter = (c0, t, stream, purpose | colour<<8 | block<<16).
- * Ising: c0 = rank>>2, block 0, u = word (rank & 3), accept iff u <= T where
+ * Ising: c0 = rank>>3; u = (halfword (rank&7) of block 0) << 16 | (same halfword of
+ *        block 1); accept iff u <= T where
  *        T = max(ceil(2^32 exp(-beta dE)), 1) - 1 (clamped to 2^32-1) -- the reference's
  *        -beta dE > log(eta) for eta = u 2^-32, eta = 0 included -- and dE is evaluated
  *        per (shell, neighbour-species) group.  Spins live in ion(3,:) (= +-1).
