@@ -111,3 +111,24 @@ int energy_blocks(const Ctx &c);
 void set_error(const std::string &msg);
 
 }  // namespace ether
+
+namespace ether {
+// Division by a loop-invariant divisor d >= 1 for 0 <= n < 2^31, by multiply and shift
+// (Granlund & Montgomery, "Division by invariant integers using multiplication", PLDI 1994;
+// round-up variant): l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1,
+// n / d = (umulhi(n, m) + n) >> l.  The sum cannot overflow because n < 2^31.
+struct FastDiv {
+    uint32_t d, m, l;
+};
+inline FastDiv make_fastdiv(uint32_t d) {
+    uint32_t l = 0;
+    while ((1ull << l) < d) ++l;
+    const uint64_t m = ((1ull << 32) * ((1ull << l) - d)) / d + 1;
+    return FastDiv{d, (uint32_t)m, l};
+}
+#if defined(__CUDACC__)
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) {
+    return (__umulhi(n, f.m) + n) >> f.l;
+}
+#endif
+}  // namespace ether

@@ -109,10 +109,25 @@ __device__ __forceinline__ void stv(uint8_t *p, const Vec<W> &v) {
     }
 }
 
+// Sites of word q whose high random halves tie with the threshold's high half: decided by
+// the low halves (block 1 of the group).  Returns the XOR mask of the extra flips.  Kept
+// out of line: it runs for about one word in 16000 and must not cost the hot loop registers.
+__device__ __noinline__ uint32_t resolve_ties(uint32_t grp, uint32_t t, uint32_t stream,
+                                              uint32_t c3, uint32_t seed, int odd, uint32_t tie,
+                                              uint32_t e4s, const uint32_t *s_tl) {
+    const U4 rl = draw(grp, t, stream, c3 | (1u << 16), seed);
+    const uint32_t la = odd ? rl.z : rl.x, lb = odd ? rl.w : rl.y;
+    const uint32_t l[4] = {la & 0xFFFFu, la >> 16, lb & 0xFFFFu, lb >> 16};
+    uint32_t m = 0;
+    for (int k = 0; k < 4; ++k)
+        if (((tie >> k) & 1u) && l[k] <= s_tl[((e4s >> (8 * k)) & 0xFFu) >> 2]) m |= 1u << (8 * k);
+    return m;
+}
+
 template <int W, int VPT>
 __global__ void __launch_bounds__(256)
-ising_sc_kernel(uint8_t *__restrict__ spins, int L1, int L2, int L3, uint32_t colour,
-                const uint32_t *__restrict__ thr, int table_entries,
+ising_sc_kernel(uint8_t *__restrict__ spins, int L1, int L2, int L3, FastDiv fH, FastDiv fL2,
+                uint32_t colour, const uint32_t *__restrict__ thr, int table_entries,
                 const int32_t *__restrict__ slot_of_rep, const uint32_t *__restrict__ stream_id,
                 const uint32_t *__restrict__ step, uint32_t seed,
                 unsigned long long *__restrict__ acc_count) {
@@ -130,78 +145,67 @@ ising_sc_kernel(uint8_t *__restrict__ spins, int L1, int L2, int L3, uint32_t co
         s_tl[threadIdx.x] = T & 0xFFFFu;
     }
     __syncthreads();
+    const char *th_bytes = reinterpret_cast<const char *>(s_th);
     const uint32_t stream = stream_id[r];
     const uint32_t t = step[r];
     const uint32_t c3 = kMetro | (colour << 8);
     const int nvec = half / W;
     unsigned flips = 0;
-    // loads of all VPT vectors first, so their latencies overlap
-    Vec<W> me[VPT], o0[VPT], a[VPT], b[VPT], c[VPT], d[VPT];
-    uint32_t edge[VPT];
-    int rho0[VPT], par[VPT];
-    bool live[VPT];
 #pragma unroll
     for (int j = 0; j < VPT; ++j) {
         const int v = (blockIdx.x * VPT + j) * blockDim.x + threadIdx.x;
-        live[j] = v < nvec;
-        const int vv = live[j] ? v : 0;
-        rho0[j] = vv * W;
-        const int row = rho0[j] / H;
-        const int xh0 = rho0[j] - row * H;
-        const int y = row % L2, z = row / L2;
-        par[j] = (y + z + (int)colour) & 1;
+        if (v >= nvec) break;
+        const int rho0 = v * W;
+        const int row = (int)fdiv((uint32_t)rho0, fH);
+        const int xh0 = rho0 - row * H;
+        const int z = (int)fdiv((uint32_t)row, fL2);
+        const int y = row - z * L2;
+        const int par = (y + z + (int)colour) & 1;
         const int ym = (y == 0 ? L2 - 1 : y - 1), yp = (y == L2 - 1 ? 0 : y + 1);
         const int zm = (z == 0 ? L3 - 1 : z - 1), zp = (z == L3 - 1 ? 0 : z + 1);
-        me[j] = ldv<W>(own_a + rho0[j]);
-        o0[j] = ldv<W>(opp + rho0[j]);
-        a[j] = ldv<W>(opp + (z * L2 + ym) * H + xh0);
-        b[j] = ldv<W>(opp + (z * L2 + yp) * H + xh0);
-        c[j] = ldv<W>(opp + (zm * L2 + y) * H + xh0);
-        d[j] = ldv<W>(opp + (zp * L2 + y) * H + xh0);
-        if (par[j] == 0) edge[j] = opp[row * H + (xh0 == 0 ? H - 1 : xh0 - 1)];
-        else edge[j] = opp[row * H + (xh0 + W == H ? 0 : xh0 + W)];
-    }
-#pragma unroll
-    for (int j = 0; j < VPT; ++j) {
-        if (!live[j]) break;
+        Vec<W> me = ldv<W>(own_a + rho0);
+        const Vec<W> o0 = ldv<W>(opp + rho0);
+        const Vec<W> a = ldv<W>(opp + (z * L2 + ym) * H + xh0);
+        const Vec<W> b = ldv<W>(opp + (z * L2 + yp) * H + xh0);
+        const Vec<W> c = ldv<W>(opp + (zm * L2 + y) * H + xh0);
+        const Vec<W> d = ldv<W>(opp + (zp * L2 + y) * H + xh0);
+        const uint32_t edge = par == 0 ? opp[row * H + (xh0 == 0 ? H - 1 : xh0 - 1)]
+                                       : opp[row * H + (xh0 + W == H ? 0 : xh0 + W)];
         U4 rh{0, 0, 0, 0};
 #pragma unroll
         for (int q = 0; q < NW; ++q) {
-            const int grp = (rho0[j] >> 3) + (q >> 1);
-            if ((q & 1) == 0) rh = draw((uint32_t)grp, t, stream, c3, seed);
+            const uint32_t grp = (uint32_t)((rho0 >> 3) + (q >> 1));
+            if ((q & 1) == 0) rh = draw(grp, t, stream, c3, seed);
             uint32_t sh;
-            if (par[j] == 0) {  // neighbour x-1 -> xh-1: window shifted up by one byte
-                uint32_t lo = (q == 0) ? (edge[j] << 24) : o0[j].w[q - 1];
-                sh = __funnelshift_l(lo, o0[j].w[q], 8);
-            } else {            // neighbour x+1 -> xh+1: window shifted down by one byte
-                uint32_t hi = (q == NW - 1) ? edge[j] : o0[j].w[q + 1];
-                sh = __funnelshift_r(o0[j].w[q], hi, 8);
+            if (par == 0) {  // neighbour x-1 -> xh-1: window shifted up by one byte
+                const uint32_t lo = (q == 0) ? (edge << 24) : o0.w[q - 1];
+                sh = __funnelshift_l(lo, o0.w[q], 8);
+            } else {         // neighbour x+1 -> xh+1: window shifted down by one byte
+                const uint32_t hi = (q == NW - 1) ? edge : o0.w[q + 1];
+                sh = __funnelshift_r(o0.w[q], hi, 8);
             }
-            const uint32_t s0 = me[j].w[q];
-            const uint32_t n = o0[j].w[q] + sh + a[j].w[q] + b[j].w[q] + c[j].w[q] + d[j].w[q];
-            const uint32_t e4 = n + (s0 << 3) - s0;  // bytewise n + 7 s
+            const uint32_t s0 = me.w[q];
+            const uint32_t n = o0.w[q] + sh + a.w[q] + b.w[q] + c.w[q] + d.w[q];
+            // bytewise 4*(n + 7 s) <= 52: the byte offsets of the thresholds in s_th
+            const uint32_t e4s = (n + (s0 << 3) - s0) << 2;
+            const uint32_t t0 = *reinterpret_cast<const uint32_t *>(th_bytes + (e4s & 0xFFu));
+            const uint32_t t1 = *reinterpret_cast<const uint32_t *>(th_bytes + __byte_perm(e4s, 0, 0x4441));
+            const uint32_t t2 = *reinterpret_cast<const uint32_t *>(th_bytes + __byte_perm(e4s, 0, 0x4442));
+            const uint32_t t3 = *reinterpret_cast<const uint32_t *>(th_bytes + (e4s >> 24));
             const uint32_t wa = (q & 1) ? rh.z : rh.x, wb = (q & 1) ? rh.w : rh.y;
             const uint32_t u0 = wa & 0xFFFFu, u1 = wa >> 16, u2 = wb & 0xFFFFu, u3 = wb >> 16;
-            const uint32_t t0 = s_th[e4 & 0xFFu], t1 = s_th[(e4 >> 8) & 0xFFu];
-            const uint32_t t2 = s_th[(e4 >> 16) & 0xFFu], t3 = s_th[e4 >> 24];
             uint32_t out = s0;
             if (u0 < t0) out ^= 0x00000001u;
             if (u1 < t1) out ^= 0x00000100u;
             if (u2 < t2) out ^= 0x00010000u;
             if (u3 < t3) out ^= 0x01000000u;
-            if ((u0 == t0) | (u1 == t1) | (u2 == t2) | (u3 == t3)) {  // 2^-16 per site
-                const U4 rl = draw((uint32_t)grp, t, stream, c3 | (1u << 16), seed);
-                const uint32_t la = (q & 1) ? rl.z : rl.x, lb = (q & 1) ? rl.w : rl.y;
-                const uint32_t l[4] = {la & 0xFFFFu, la >> 16, lb & 0xFFFFu, lb >> 16};
-                const uint32_t uu[4] = {u0, u1, u2, u3}, tt[4] = {t0, t1, t2, t3};
-#pragma unroll
-                for (int k = 0; k < 4; ++k)
-                    if (uu[k] == tt[k] && l[k] <= s_tl[(e4 >> (8 * k)) & 0xFFu]) out ^= 1u << (8 * k);
-            }
+            const uint32_t tie = (u0 == t0 ? 1u : 0u) | (u1 == t1 ? 2u : 0u) |
+                                 (u2 == t2 ? 4u : 0u) | (u3 == t3 ? 8u : 0u);
+            if (tie) out ^= resolve_ties(grp, t, stream, c3, seed, q & 1, tie, e4s, s_tl);
             flips += __popc(out ^ s0);
-            me[j].w[q] = out;
+            me.w[q] = out;
         }
-        stv<W>(own_a + rho0[j], me[j]);
+        stv<W>(own_a + rho0, me);
     }
     warp_add_count(acc_count + r, flips);
 }
@@ -212,7 +216,8 @@ static void launch_sc(Ctx &c, int colour) {
     const int nvec = (c.N / 2) / W;
     dim3 grid((nvec + bs * VPT - 1) / (bs * VPT), c.R);
     ising_sc_kernel<W, VPT><<<grid, bs, 0, c.stream>>>(
-        c.spins, c.L[0], c.L[1], c.L[2], (uint32_t)colour, c.thr, c.table_entries, c.slot_of_rep,
+        c.spins, c.L[0], c.L[1], c.L[2], make_fastdiv((uint32_t)(c.L[0] / 2)),
+        make_fastdiv((uint32_t)c.L[1]), (uint32_t)colour, c.thr, c.table_entries, c.slot_of_rep,
         c.stream_id, c.step, c.seed, c.acc_count);
 }
 

@@ -150,7 +150,7 @@ __device__ __forceinline__ Acc3 sc_field(const float4 *__restrict__ opp, int L1,
 }
 
 __global__ void __launch_bounds__(256)
-xyz_sc_kernel(float4 *__restrict__ spins4, int L1, int L2, int L3, uint32_t colour, float jx,
+xyz_sc_kernel(float4 *__restrict__ spins4, int L1, int L2, int L3, FastDiv fH, FastDiv fL2, uint32_t colour, float jx,
               float jy, float jz, XyzParams P, const float *__restrict__ beta_slot_f,
               const int32_t *__restrict__ slot_of_rep, const uint32_t *__restrict__ stream_id,
               const uint32_t *__restrict__ step, uint32_t seed,
@@ -166,9 +166,9 @@ xyz_sc_kernel(float4 *__restrict__ spins4, int L1, int L2, int L3, uint32_t colo
     const uint32_t c3 = kMetro | (colour << 8);
     unsigned acc = 0;
     for (int rho = blockIdx.x * blockDim.x + threadIdx.x; rho < half; rho += gridDim.x * blockDim.x) {
-        const int row = rho / H;
+        const int row = (int)fdiv((uint32_t)rho, fH);
         const int xh = rho - row * H;
-        const int y = row % L2, z = row / L2;
+        const int z = (int)fdiv((uint32_t)row, fL2), y = row - z * L2;
         const int p = (y + z + (int)colour) & 1;
         Acc3 h = sc_field(opp, L1, L2, L3, H, xh, y, z, p, jx, jy, jz);
         acc += metro_site(P, own, rho, (uint32_t)rho, h.x, h.y, h.z, beta_f, t, c3, seed, k1) ? 1u : 0u;
@@ -308,7 +308,7 @@ cudaError_t launch_xyz_sweep(Ctx &c, int colour) {
         dim3 grid(blocks_for_x(c, half, bs), c.R);
         // single shell, single species: J(1,1,1,:)
         float jx = c.h_Jf[0], jy = c.h_Jf[1], jz = c.h_Jf[2];
-        xyz_sc_kernel<<<grid, bs, 0, c.stream>>>(c.spins4, c.L[0], c.L[1], c.L[2],
+        xyz_sc_kernel<<<grid, bs, 0, c.stream>>>(c.spins4, c.L[0], c.L[1], c.L[2], make_fastdiv((uint32_t)(c.L[0] / 2)), make_fastdiv((uint32_t)c.L[1]),
                                                  (uint32_t)colour, jx, jy, jz, P, c.beta_slot_f,
                                                  c.slot_of_rep, c.stream_id, c.step, c.seed,
                                                  c.acc_count);
