@@ -21,6 +21,7 @@ MODEL_ISING, MODEL_XYZ = 0, 1
 FLAG_FORCE_GENERAL = 1 << 0
 FLAG_PT_TRUE_ENERGY = 1 << 1
 FLAG_PT_REFERENCE_COPY = 1 << 2
+FLAG_NO_GRAPHS = 1 << 3
 
 
 class EtherError(RuntimeError):

@@ -196,9 +196,10 @@ void free_ctx(Ctx &c) {
                     c.t.mweight, c.t.site_of_storage, c.spins, c.spins4, c.beta_slot,
                     c.beta_slot_f, c.slot_of_rep, c.rep_of_slot, c.thr, c.stream_id,
                     c.step, c.ovrr_step, c.fresh_call, c.acc_count, c.E, c.M, c.sums,
-                    c.partials, c.pt_accepts, c.copy_from};
+                    c.partials, c.pt_accepts, c.swap_dev, c.copy_from};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    for (auto &kv : c.graphs) cudaGraphExecDestroy(kv.second);
     if (c.stream) cudaStreamDestroy(c.stream);
     c = Ctx();
 }
@@ -426,6 +427,7 @@ extern "C" int ether_create(const ether_desc *d, ether_ctx **out) {
     c.partial_blocks = energy_blocks(c);
     TRY(dev_alloc(c, &c.partials, (size_t)c.R * c.partial_blocks * 5));
     TRY(dev_alloc(c, &c.pt_accepts, 1));
+    TRY(dev_alloc(c, &c.swap_dev, 1));
     TRY(dev_alloc(c, &c.copy_from, c.R));
 #undef TRY
     std::vector<uint32_t> sid(c.R);
@@ -701,8 +703,8 @@ extern "C" int ether_parallel_tempering(ether_ctx *h, int32_t swap_count, int32_
     if (!h) return fail(ETHER_ERR_ARG, "null context");
     Ctx &c = h->c;
     if (!c.beta_set) return fail(ETHER_ERR_STATE, "beta not set");
+    if (swap_count < 0) return fail(ETHER_ERR_ARG, "negative swap_count");
     CUDA_TRY(launch_energy_mag(c, true));
-    CUDA_TRY(cudaMemsetAsync(c.pt_accepts, 0, sizeof(int32_t), c.stream));
     CUDA_TRY(launch_pt(c, swap_count));
     if (accepted) {
         CUDA_TRY(cudaMemcpyAsync(accepted, c.pt_accepts, sizeof(int32_t), cudaMemcpyDeviceToHost, c.stream));
@@ -719,33 +721,107 @@ extern "C" int ether_get_slots(ether_ctx *h, int32_t *slot_of_replica) {
     return ETHER_OK;
 }
 
+// One MCS of src/ether.f90:163-201 given its gates: OVRR (:163-169), Metropolis (:172),
+// total energy + PT when PT runs (:177, :189-198; the swap counter lives on the device),
+// observable on measurement steps (:201).
+static int issue_step(Ctx &c, const ether_schedule *sch, bool ovrr, bool pt, bool meas) {
+    if (ovrr) {
+        int rc = overrelax_once(c, sch->ovrr_para);
+        if (rc) return rc;
+    }
+    int rc = sweep_once(c);
+    if (rc) return rc;
+    if (pt) {
+        CUDA_TRY(launch_energy_mag(c, true));
+        CUDA_TRY(launch_pt(c, -1));
+    }
+    if (meas) {
+        CUDA_TRY(launch_energy_mag(c, true));
+        CUDA_TRY(launch_measure(c));
+    }
+    return ETHER_OK;
+}
+
+// The loop body for steps step0+1 .. step0+nsteps.  Steps are issued in chunks; a chunk's
+// launches depend only on its gate pattern (everything that changes from step to step --
+// sweep counters, PT swap count, slot permutation -- is read from device memory), so each
+// distinct pattern is captured once as a CUDA graph and replayed.  With periodic gates the
+// chunk length is the gates' period, and one or two graphs cover a whole run.
 extern "C" int ether_mcs(ether_ctx *h, const ether_schedule *sch, int32_t step0, int32_t nsteps,
                          int32_t *swap_count) {
     if (!h || !sch) return fail(ETHER_ERR_ARG, "null argument");
     Ctx &c = h->c;
     if (!c.beta_set) return fail(ETHER_ERR_STATE, "beta not set");
-    if (sch->coa <= 0 || nsteps < 0) return fail(ETHER_ERR_ARG, "coa must be positive and nsteps >= 0");
+    if (sch->coa <= 0 || nsteps < 0 || step0 < 0)
+        return fail(ETHER_ERR_ARG, "coa must be positive, step0 and nsteps >= 0");
     const bool ovrr_on = sch->ovrr && c.model == ETHER_MODEL_XYZ && !c.zeeman && !c.sia && sch->ovrr_mcs > 0;
     const bool pt_on = sch->pt && sch->exchange_interval > 0;
-    int32_t sc = swap_count ? *swap_count : 0;
-    for (int step = step0 + 1; step <= step0 + nsteps; ++step) {
-        if (ovrr_on && step % sch->ovrr_mcs == 0 && step % sch->coa != 0) {
-            int rc = overrelax_once(c, sch->ovrr_para);
-            if (rc) return rc;
+    if (pt_on && !(c.flags & ETHER_FLAG_PT_REFERENCE_COPY) && c.n_slots < 2)
+        return fail(ETHER_ERR_STATE, "PT needs a ladder of at least two slots");
+    const int32_t sc0 = swap_count ? *swap_count : 0;
+    CUDA_TRY(cudaMemcpyAsync(c.swap_dev, &sc0, sizeof(int32_t), cudaMemcpyHostToDevice, c.stream));
+    auto gate = [&](int step, bool &ov, bool &pt, bool &me) {
+        ov = ovrr_on && step % sch->ovrr_mcs == 0 && step % sch->coa != 0;
+        pt = pt_on && step % sch->exchange_interval == 0 && step % sch->coa != 0;
+        me = step > sch->tmcs_eq && step % sch->coa == 0;
+    };
+    // chunk length: the period of the gates, kept between 1 and 256 steps
+    long period = sch->coa;
+    auto lcm = [](long x, long y) { long g = x, b = y; while (b) { long t = g % b; g = b; b = t; } return x / g * y; };
+    if (ovrr_on) period = lcm(period, sch->ovrr_mcs);
+    if (pt_on) period = lcm(period, sch->exchange_interval);
+    int chunk = (int)(period <= 256 ? period : 64);
+    while (chunk < 8 && chunk * 2 <= 256) chunk *= 2;
+    const bool use_graphs = !(c.flags & ETHER_FLAG_NO_GRAPHS);
+    int step = step0 + 1;
+    const int last = step0 + nsteps;
+    while (step <= last) {
+        const int n = std::min(chunk, last - step + 1);
+        std::vector<int8_t> sig;
+        sig.reserve(n + 1);
+        bool ov, pt, me;
+        for (int k = 0; k < n; ++k) {
+            gate(step + k, ov, pt, me);
+            sig.push_back((int8_t)((ov ? 1 : 0) | (pt ? 2 : 0) | (me ? 4 : 0)));
         }
-        int rc = sweep_once(c);
-        if (rc) return rc;
-        if (pt_on && step % sch->exchange_interval == 0 && step % sch->coa != 0) {
-            ++sc;
-            CUDA_TRY(launch_energy_mag(c, true));
-            CUDA_TRY(launch_pt(c, sc));
+        if (!use_graphs || n < 4) {
+            for (int k = 0; k < n; ++k) {
+                int rc = issue_step(c, sch, sig[k] & 1, sig[k] & 2, sig[k] & 4);
+                if (rc) return rc;
+            }
+        } else {
+            std::string key(sig.begin(), sig.end());
+            key += std::to_string(c.vec_bytes * 10 + c.ising_vpt) + "/" + std::to_string(sch->ovrr_para);
+            auto it = c.graphs.find(key);
+            if (it == c.graphs.end()) {
+                if (c.graphs.size() >= 64) {
+                    for (auto &kv : c.graphs) cudaGraphExecDestroy(kv.second);
+                    c.graphs.clear();
+                }
+                cudaGraph_t g = nullptr;
+                CUDA_TRY(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+                int rc = ETHER_OK;
+                for (int k = 0; k < n && rc == ETHER_OK; ++k) rc = issue_step(c, sch, sig[k] & 1, sig[k] & 2, sig[k] & 4);
+                cudaError_t ce = cudaStreamEndCapture(c.stream, &g);
+                if (rc) {
+                    if (g) cudaGraphDestroy(g);
+                    return rc;
+                }
+                CUDA_TRY(ce);
+                cudaGraphExec_t ex = nullptr;
+                ce = cudaGraphInstantiate(&ex, g, 0);
+                cudaGraphDestroy(g);
+                CUDA_TRY(ce);
+                it = c.graphs.emplace(key, ex).first;
+            }
+            CUDA_TRY(cudaGraphLaunch(it->second, c.stream));
         }
-        if (step > sch->tmcs_eq && step % sch->coa == 0) {
-            CUDA_TRY(launch_energy_mag(c, true));
-            CUDA_TRY(launch_measure(c));
-        }
+        step += n;
     }
-    if (swap_count) *swap_count = sc;
+    if (swap_count) {
+        CUDA_TRY(cudaMemcpyAsync(swap_count, c.swap_dev, sizeof(int32_t), cudaMemcpyDeviceToHost, c.stream));
+        CUDA_TRY(cudaStreamSynchronize(c.stream));
+    }
     return ETHER_OK;
 }
 

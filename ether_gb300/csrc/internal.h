@@ -14,6 +14,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -92,7 +93,9 @@ struct Ctx {
     double *partials = nullptr;  // scratch for reductions
     int partial_blocks = 0;
     int32_t *pt_accepts = nullptr;  // 1
+    int32_t *swap_dev = nullptr;    // 1: PT swap counter
     int32_t *copy_from = nullptr;   // R (reference-copy PT mode)
+    std::map<std::string, cudaGraphExec_t> graphs;  // ether_mcs chunks by gate pattern
     size_t device_bytes = 0;
     uint64_t launches = 0;
     int sm_count = 0;
@@ -106,7 +109,7 @@ cudaError_t launch_fresh(Ctx &c);
 cudaError_t launch_advance(Ctx &c, uint32_t *counter);
 cudaError_t launch_energy_mag(Ctx &c, bool want_energy);
 cudaError_t launch_measure(Ctx &c);
-cudaError_t launch_pt(Ctx &c, int swap_count);
+cudaError_t launch_pt(Ctx &c, int set_swap_count);
 int energy_blocks(const Ctx &c);
 void set_error(const std::string &msg);
 

@@ -144,8 +144,9 @@ __global__ void measure_kernel(const double *__restrict__ E, const double *__res
 __global__ void pt_kernel(const double *__restrict__ E, int R, int n_slots, int n_groups,
                           const double *__restrict__ beta_slot, int32_t *__restrict__ rep_of_slot,
                           int32_t *__restrict__ slot_of_rep, int32_t *__restrict__ copy_from,
-                          int swap_count, uint32_t seed, int true_energy, int copy_mode,
+                          const int32_t *__restrict__ swap_ptr, uint32_t seed, int true_energy, int copy_mode,
                           int32_t *__restrict__ n_acc) {
+    const int swap_count = *swap_ptr;
     const int npairs = n_slots / 2 + 1;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     if (tid >= npairs * n_groups) return;
@@ -217,14 +218,28 @@ cudaError_t launch_measure(Ctx &c) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_pt(Ctx &c, int swap_count) {
+// PT swap counter, kept on the device so that captured graphs replay correctly.
+__global__ void pt_bump_kernel(int32_t *__restrict__ swap, int32_t *__restrict__ n_acc, int set,
+                               int32_t value) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        *swap = set ? value : *swap + 1;
+        *n_acc = 0;
+    }
+}
+
+// set >= 0: use swap_count = set (ether_parallel_tempering); set < 0: increment the device
+// counter first (the loop of src/ether.f90:190-192 inside ether_mcs).
+cudaError_t launch_pt(Ctx &c, int set_swap_count) {
     const int copy_mode = (c.flags & ETHER_FLAG_PT_REFERENCE_COPY) ? 1 : 0;
     const int npairs = c.n_slots / 2 + 1;
     const int nt = npairs * c.n_groups;
+    pt_bump_kernel<<<1, 32, 0, c.stream>>>(c.swap_dev, c.pt_accepts, set_swap_count >= 0 ? 1 : 0,
+                                           set_swap_count);
+    c.launches++;
     if (copy_mode) cudaMemsetAsync(c.copy_from, 0xFF, sizeof(int32_t) * c.R, c.stream);
     pt_kernel<<<(nt + 127) / 128, 128, 0, c.stream>>>(
         c.E, c.R, c.n_slots, c.n_groups, c.beta_slot, c.rep_of_slot, c.slot_of_rep, c.copy_from,
-        swap_count, c.seed, (c.flags & ETHER_FLAG_PT_TRUE_ENERGY) ? 1 : 0, copy_mode,
+        c.swap_dev, c.seed, (c.flags & ETHER_FLAG_PT_TRUE_ENERGY) ? 1 : 0, copy_mode,
         c.pt_accepts);
     c.launches++;
     if (copy_mode) {

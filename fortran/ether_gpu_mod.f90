@@ -1,0 +1,153 @@
+! ether_gpu_mod.f90 -- ISO_C_BINDING interface of libether_gpu.so (include/ether_gpu.h)
+! for ETHER's Fortran driver.  It replaces, call for call, the routines that the MCS loop
+! of src/ether.f90:152-214 invokes on `module init` state:
+!   fresh_spins             -> ether_fresh_spins
+!   overrelaxation          -> ether_overrelaxation
+!   Metropolis              -> ether_metropolis
+!   get_tot_energy          -> ether_tot_energy
+!   parallel_tempering      -> ether_parallel_tempering
+!   observable              -> ether_observable
+!   get_eng/get_mag('avg')  -> ether_avg
+!   observables_per_repeat  -> ether_per_repeat
+! All arrays keep the layouts of module init (ion(0:8,N), nn(nsh,N,0:cap,0:1),
+! j_exc(nsh,nsp,nsp,3), sia_vec(3,nsp)); they are passed by address and are not retained.
+module ether_gpu_mod
+    use iso_c_binding
+    implicit none
+
+    integer(c_int), parameter :: ETHER_OK = 0
+    integer(c_int), parameter :: ETHER_MODEL_ISING = 0, ETHER_MODEL_XYZ = 1
+    integer(c_int), parameter :: ETHER_FLAG_FORCE_GENERAL = 1
+    integer(c_int), parameter :: ETHER_FLAG_PT_TRUE_ENERGY = 2
+    integer(c_int), parameter :: ETHER_FLAG_PT_REFERENCE_COPY = 4
+
+    type, bind(C) :: ether_desc
+        integer(c_int32_t) :: n_sites, n_species, n_shells, nbd_capacity, model, angle
+        real(c_double)     :: dphi
+        integer(c_int32_t) :: zeeman
+        real(c_double)     :: h(3), g_factor, mb
+        integer(c_int32_t) :: sia
+        type(c_ptr)        :: ion, nn, j_exc, sia_vec, s, stgg
+        integer(c_int32_t) :: n_replicas
+        integer(c_int32_t) :: seed          ! uint32_t in C
+        integer(c_int32_t) :: sc(3), basis, flags
+    end type ether_desc
+
+    type, bind(C) :: ether_schedule
+        integer(c_int32_t) :: tmcs_eq, coa, ovrr
+        real(c_double)     :: ovrr_para
+        integer(c_int32_t) :: ovrr_mcs, pt, exchange_interval
+    end type ether_schedule
+
+    interface
+        integer(c_int) function ether_create(desc, ctx) bind(C, name="ether_create")
+            import :: c_int, c_ptr, ether_desc
+            type(ether_desc), intent(in) :: desc
+            type(c_ptr), intent(out) :: ctx
+        end function
+        integer(c_int) function ether_destroy(ctx) bind(C, name="ether_destroy")
+            import :: c_int, c_ptr
+            type(c_ptr), value :: ctx
+        end function
+        type(c_ptr) function ether_last_error() bind(C, name="ether_last_error")
+            import :: c_ptr
+        end function
+        integer(c_int) function ether_set_beta(ctx, beta) bind(C, name="ether_set_beta")
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(in) :: beta(*)
+        end function
+        integer(c_int) function ether_set_ladder(ctx, n_slots, beta) bind(C, name="ether_set_ladder")
+            import :: c_int, c_ptr, c_double, c_int32_t
+            type(c_ptr), value :: ctx
+            integer(c_int32_t), value :: n_slots
+            real(c_double), intent(in) :: beta(*)
+        end function
+        integer(c_int) function ether_set_streams(ctx, stream, step) bind(C, name="ether_set_streams")
+            import :: c_int, c_ptr, c_int32_t
+            type(c_ptr), value :: ctx
+            integer(c_int32_t), intent(in) :: stream(*), step(*)
+        end function
+        integer(c_int) function ether_set_spins(ctx, replica, ion) bind(C, name="ether_set_spins")
+            import :: c_int, c_ptr, c_double, c_int32_t
+            type(c_ptr), value :: ctx
+            integer(c_int32_t), value :: replica
+            real(c_double), intent(in) :: ion(0:8, *)
+        end function
+        integer(c_int) function ether_get_spins(ctx, replica, ion) bind(C, name="ether_get_spins")
+            import :: c_int, c_ptr, c_double, c_int32_t
+            type(c_ptr), value :: ctx
+            integer(c_int32_t), value :: replica
+            real(c_double), intent(inout) :: ion(0:8, *)
+        end function
+        integer(c_int) function ether_fresh_spins(ctx) bind(C, name="ether_fresh_spins")
+            import :: c_int, c_ptr
+            type(c_ptr), value :: ctx
+        end function
+        integer(c_int) function ether_metropolis(ctx, nsweeps, accept) bind(C, name="ether_metropolis")
+            import :: c_int, c_ptr, c_double, c_int32_t
+            type(c_ptr), value :: ctx
+            integer(c_int32_t), value :: nsweeps
+            real(c_double), intent(out) :: accept(*)
+        end function
+        integer(c_int) function ether_overrelaxation(ctx, ovrr_para) bind(C, name="ether_overrelaxation")
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), value :: ovrr_para
+        end function
+        integer(c_int) function ether_tot_energy(ctx, e) bind(C, name="ether_tot_energy")
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(out) :: e(*)
+        end function
+        integer(c_int) function ether_tot_magnetisation(ctx, m) bind(C, name="ether_tot_magnetisation")
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(out) :: m(3, *)
+        end function
+        integer(c_int) function ether_observable(ctx, step, tmcs_eq, coa) bind(C, name="ether_observable")
+            import :: c_int, c_ptr, c_int32_t
+            type(c_ptr), value :: ctx
+            integer(c_int32_t), value :: step, tmcs_eq, coa
+        end function
+        integer(c_int) function ether_zero_avg(ctx) bind(C, name="ether_zero_avg")
+            import :: c_int, c_ptr
+            type(c_ptr), value :: ctx
+        end function
+        integer(c_int) function ether_avg(ctx, out) bind(C, name="ether_avg")
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(out) :: out(6, *)
+        end function
+        integer(c_int) function ether_per_repeat(ctx, mean, err) bind(C, name="ether_per_repeat")
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(out) :: mean(6, *), err(6, *)
+        end function
+        integer(c_int) function ether_parallel_tempering(ctx, swap_count, accepted) &
+                bind(C, name="ether_parallel_tempering")
+            import :: c_int, c_ptr, c_int32_t
+            type(c_ptr), value :: ctx
+            integer(c_int32_t), value :: swap_count
+            integer(c_int32_t), intent(out) :: accepted
+        end function
+        integer(c_int) function ether_mcs(ctx, sch, step0, nsteps, swap_count) bind(C, name="ether_mcs")
+            import :: c_int, c_ptr, c_int32_t, ether_schedule
+            type(c_ptr), value :: ctx
+            type(ether_schedule), intent(in) :: sch
+            integer(c_int32_t), value :: step0, nsteps
+            integer(c_int32_t), intent(inout) :: swap_count
+        end function
+        integer(c_int) function ether_build_lattice(nbasis, basis_cart, basis_species, abc, sc, bc, &
+                checkerboard, n_shells, nbd_dis, tol, cap, ion, stgg, nn) bind(C, name="ether_build_lattice")
+            import :: c_int, c_int32_t, c_double, c_char
+            integer(c_int32_t), value :: nbasis, checkerboard, n_shells, cap
+            real(c_double), intent(in) :: basis_cart(3, *), abc(3, 3), nbd_dis(*)
+            integer(c_int32_t), intent(in) :: basis_species(*), sc(3)
+            character(kind=c_char), intent(in) :: bc(3)
+            real(c_double), value :: tol
+            real(c_double), intent(out) :: ion(0:8, *), stgg(*)
+            integer(c_int32_t), intent(out) :: nn(*)
+        end function
+    end interface
+end module ether_gpu_mod

@@ -55,10 +55,12 @@ enum {
     ETHER_FLAG_FORCE_GENERAL = 1 << 0, /* never use the simple-cubic fast kernels           */
     ETHER_FLAG_PT_TRUE_ENERGY = 1 << 1,/* PT exponent uses the Hamiltonian energy (bonds
                                           once) instead of the reference's raw sum          */
-    ETHER_FLAG_PT_REFERENCE_COPY = 1 << 2 /* PT acceptance copies the lower slot's
+    ETHER_FLAG_PT_REFERENCE_COPY = 1 << 2,/* PT acceptance copies the lower slot's
                                           configuration into the higher slot (what
                                           parallel_tempering.f90:92-106 effectively does)
                                           instead of exchanging the two                     */
+    ETHER_FLAG_NO_GRAPHS = 1 << 3         /* ether_mcs launches kernels one by one instead of
+                                          replaying captured CUDA graphs                    */
 };
 
 typedef struct ether_ctx ether_ctx;
