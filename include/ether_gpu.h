@@ -216,6 +216,27 @@ int ether_autotune(ether_ctx *ctx, int32_t *variant, float *best_ms);
 /* Force a kernel variant (same encoding as ether_autotune). */
 int ether_set_variant(ether_ctx *ctx, int32_t variant);
 
+/* ------------------------------------------------------------- no-allocation energy ---- */
+/* No counterpart in the reference.  Energy and magnetisation of n_replicas simple-cubic
+ * configurations already in device memory, for callers that cannot allocate device memory
+ * where they need the result (a framework that owns every allocation through its own pool,
+ * an OpenACC / OpenMP-target Fortran driver, a service whose fixed device budget is spent):
+ * ether_tot_energy needs a context, and creating one allocates.  This call allocates nothing.
+ *   spins: device pointer, sites in the reference's order (x fastest), replicas one after
+ *          another; int8 Sz = +-1 (Ising) or float4 (Sx, Sy, Sz, phi) (XYZ).
+ *   L(3): periodic extents (>= 3 each); J(3) = diagonal exchange of the six nearest
+ *   neighbours (j_exc after parameters.f90); zee(3) = -g mB s H (Zeeman), zero if off.
+ *   E(n_replicas), M(3, n_replicas): host arrays, the raw sums of get_tot_energy and
+ *   get_tot_magnetisation (unit stagger and spin length).  stream: cudaStream_t or NULL.
+ * Scratch is 1 MiB of the library's static device memory, shared by all calls: at most 992
+ * replicas per call (ETHER_ERR_CAPACITY beyond, before any memory is touched), and calls
+ * that overlap on the GPU race.  The
+ * first call on a device looks up the scratch address (cudaGetSymbolAddress) and must come
+ * before any stream capture.  Returns after the results are in E and M. */
+int ether_sc_energy_noalloc(int32_t model, const void *spins, const int32_t L[3],
+                            int32_t n_replicas, const double J[3], const double zee[3],
+                            double *E, double *M, void *stream);
+
 /* ---------------------------------------------------------------- lattice builder ---- */
 /* generate_supercell + getting_nbd (src/generate_supercell.f90:38-132,
  * src/getting_nbd.f90:34-82, src/search_nbd.f90:20-64) in O(N) with a cell list, giving
