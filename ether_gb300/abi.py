@@ -100,6 +100,7 @@ SIGNATURES = {
     "ether_end_sweep": (C.c_int, [P]),
     "ether_autotune": (C.c_int, [P, PI32, C.POINTER(C.c_float)]),
     "ether_set_variant": (C.c_int, [P, C.c_int32]),
+    "ether_structure_factor": (C.c_int, [P, PD, PI32, PD, PD, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "ether_sc_energy_noalloc": (C.c_int, [C.c_int32, P, PI32, C.c_int32, PD, PD, PD, PD, P]),
     "ether_build_lattice": (C.c_int, [C.c_int32, PD, PI32, PD, PI32, C.c_char_p, C.c_int32,
                                       C.c_int32, PD, C.c_double, C.c_int32, PD, PD, PI32]),

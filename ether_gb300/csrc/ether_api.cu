@@ -385,6 +385,7 @@ extern "C" int ether_create(const ether_desc *d, ether_ctx **out) {
         spc[s] = (uint8_t)sp[i];
         if (c.model == ETHER_MODEL_ISING) ity[s] = itype_site[i];
         mw[s] = (d->stgg ? d->stgg[i] : 1.0) * c.s_len[sp[i] - 1];
+        for (int k = 0; k < 3; ++k) c.pos.push_back(d->ion[6 + k + 9 * (size_t)i]);
     }
 
     // ----- device
@@ -984,5 +985,40 @@ extern "C" int ether_set_variant(ether_ctx *h, int32_t variant) {
         return fail(ETHER_ERR_ARG, "variant not available for this lattice");
     c.vec_bytes = w;
     c.ising_vpt = v;
+    return ETHER_OK;
+}
+
+// structure_factor (utility/Structure_Factor/structure_factor.f90:99-183) on the tensor cores;
+// see k_sq.cu.  Positions become fractional coordinates of the cell abc (rows = a1, a2, a3).
+extern "C" int ether_structure_factor(ether_ctx *h, const double *abc, const int32_t nq[3],
+                                      const double q0[3], const double dq[3], float *sq,
+                                      float *comp) {
+    if (!h || !abc || !nq || !q0 || !dq || !sq || !comp) return fail(ETHER_ERR_ARG, "null argument");
+    Ctx &c = h->c;
+    // inverse of the matrix whose rows are the lattice vectors: r = sum_a f_a a_a
+    const double *A = abc;
+    const double det = A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
+                       A[2] * (A[3] * A[7] - A[4] * A[6]);
+    if (!(std::fabs(det) > 1e-300)) return fail(ETHER_ERR_ARG, "cell vectors are degenerate");
+    // columns of inv(A^T): f = inv(A^T) r
+    double inv[9];  // inv of A (row-major), f_a = sum_d r_d inv[d*3 + a]
+    inv[0] = (A[4] * A[8] - A[5] * A[7]) / det;
+    inv[1] = -(A[1] * A[8] - A[2] * A[7]) / det;
+    inv[2] = (A[1] * A[5] - A[2] * A[4]) / det;
+    inv[3] = -(A[3] * A[8] - A[5] * A[6]) / det;
+    inv[4] = (A[0] * A[8] - A[2] * A[6]) / det;
+    inv[5] = -(A[0] * A[5] - A[2] * A[3]) / det;
+    inv[6] = (A[3] * A[7] - A[4] * A[6]) / det;
+    inv[7] = -(A[0] * A[7] - A[1] * A[6]) / det;
+    inv[8] = (A[0] * A[4] - A[1] * A[3]) / det;
+    std::vector<double> frac(3 * (size_t)c.N);
+    for (int s = 0; s < c.N; ++s)
+        for (int a = 0; a < 3; ++a)
+            frac[3 * (size_t)s + a] = c.pos[3 * (size_t)s] * inv[0 * 3 + a] + c.pos[3 * (size_t)s + 1] * inv[1 * 3 + a] +
+                                      c.pos[3 * (size_t)s + 2] * inv[2 * 3 + a];
+    std::string msg;
+    const int nqi[3] = {nq[0], nq[1], nq[2]};
+    const int rc = structure_factor_launch(c, frac.data(), nqi, q0, dq, sq, comp, msg);
+    if (rc) return fail(rc, "ether_structure_factor: " + msg);
     return ETHER_OK;
 }

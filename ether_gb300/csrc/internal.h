@@ -65,6 +65,7 @@ struct Ctx {
     std::vector<std::vector<int>> type_groupcount;  // per type: neighbours per group
     std::vector<int32_t> type_species;
     std::vector<double> s_len;     // spin length per species
+    std::vector<double> pos;       // 3N cartesian positions ion(6:8), storage order
     std::vector<float> h_Jf;       // nJ * 3 FP32 couplings (host copy)
     std::vector<double> h_Jd;      // nJ * 3 FP64 couplings
     // PT ladder
@@ -112,6 +113,8 @@ cudaError_t launch_measure(Ctx &c);
 cudaError_t launch_pt(Ctx &c, int set_swap_count);
 int energy_blocks(const Ctx &c);
 void set_error(const std::string &msg);
+int structure_factor_launch(Ctx &c, const double *frac, const int nq[3], const double q0[3],
+                            const double dq[3], float *sq_host, float *comp_host, std::string &msg);
 
 }  // namespace ether
 

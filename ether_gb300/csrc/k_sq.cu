@@ -1,0 +1,460 @@
+// k_sq.cu -- structure factor S(q) (utility/Structure_Factor/structure_factor.f90:99-183) on
+// a 3-D grid of q, as a dense (q x sites) x (sites x spin components) contraction on the
+// fifth-generation tensor cores.
+//
+//   D[2q + c, 3r + a] = sum_i A[2q + c, i] B[i, 3r + a],  A = cos / sin (q.r_i),  B = S_{r,i,a}
+//
+// Both operands are split into BF16 high and low parts (x = hi + lo, lo = bf16(x - hi)) and
+// D = A_hi B_hi + A_hi B_lo + A_lo B_hi is accumulated in FP32 in tensor memory: about 16
+// significant bits per product instead of BF16's 8.
+//
+// One CTA owns a 128-row tile of D (64 q-points: consecutive h1 at fixed h2, h3) and all
+// 3R columns (<= 256).  Per 64-site k-block:
+//   * warps 0-3 generate the A tile in shared memory: phase factors
+//       exp(i q.r) = E1[h1_0 + 16m][i] * E2[h2][i] * E3[h3][i] * b_i^j,  b_i = exp(2 pi i dq_1 u_i)
+//     (complex FP32, restarted every 16 steps from FP64-built tables), split into hi/lo and
+//     stored in the K-major 128-byte-swizzled layout the MMA descriptors describe;
+//   * one thread of warp 4 loads the B_hi / B_lo tiles with TMA (same swizzle) and issues the
+//     12 tcgen05.mma (3 products x 4 K-steps of 16), then tcgen05.commit to the stage's
+//     "empty" barrier;
+//   * two stages: A generation and TMA of block k+1 overlap the MMAs of block k.
+// Epilogue: warps 0-3 read the accumulator with tcgen05.ld (warp w owns TMEM lanes 32w..),
+// pair cos/sin rows with a lane shuffle and write |S(q)|^2 / N^2 and |S_a(q)| / N.
+//
+// Every mbarrier wait is bounded (%globaltimer, 2 s): on expiry the kernel records an error
+// code, stops issuing work, waits (bounded) for the MMAs it issued, frees its TMEM and exits.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+namespace ether {
+namespace sq {
+
+constexpr int kBM = 128;        // rows per tile (64 q-points x cos/sin)
+constexpr int kBK = 64;         // sites per k-block (128 bytes of BF16)
+constexpr int kStages = 2;
+constexpr int kProducers = 128; // warps 0-3
+constexpr int kThreads = 160;   // + warp 4 (TMA + MMA issue)
+constexpr uint64_t kWaitNs = 2000000000ull;
+
+struct Smem {
+    // stage s: A_hi, A_lo (kBM x kBK bf16 each), B_hi, B_lo (BN x kBK bf16 each)
+    // laid out from a 1024-byte aligned base; barriers at the end
+    static constexpr int a_bytes = kBM * kBK * 2;  // 16 KB
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ uint64_t gtime() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+    return ok != 0;
+}
+// Bounded wait: false (and *err set) if the phase did not complete within kWaitNs.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *err, int code) {
+    if (mbar_try(bar, parity)) return true;
+    const uint64_t t0 = gtime();
+    while (!mbar_try(bar, parity)) {
+        if (gtime() - t0 > kWaitNs) {
+            atomicCAS(err, 0, code);
+            return false;
+        }
+    }
+    return true;
+}
+
+// Byte offset of element (row, k) in a K-major, 128-byte-swizzled tile of 64 BF16 columns:
+// 8-row atoms of 1024 bytes, 16-byte chunk index XORed with the row within the atom.
+__device__ __forceinline__ uint32_t swz(int row, int k) {
+    return (uint32_t)((row >> 3) * 1024 + (row & 7) * 128 + ((((k >> 3) ^ (row & 7))) << 4) + (k & 7) * 2);
+}
+
+// UMMA shared-memory descriptor: K-major, SWIZZLE_128B, 8-row stride 1024 bytes.
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);        // start address
+    d |= (uint64_t)1u << 16;                         // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024u >> 4) << 32;               // stride byte offset
+    d |= (uint64_t)1u << 46;                         // descriptor version
+    d |= (uint64_t)2u << 61;                         // SWIZZLE_128B
+    return d;
+}
+
+// Instruction descriptor, kind::f16: BF16 x BF16 -> FP32, both K-major, M = 128, N = n.
+__host__ __device__ constexpr uint32_t make_idesc(int n) {
+    return (1u << 4)                       // D format F32
+           | (1u << 7)                     // A format BF16
+           | (1u << 10)                    // B format BF16
+           | ((uint32_t)(n >> 3) << 17)    // N / 8
+           | ((uint32_t)(kBM >> 4) << 24); // M / 16
+}
+
+__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                     uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+        ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int c0, int c1, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(dst), "l"(map), "r"(c0), "r"(c1), "r"(bar) : "memory");
+}
+
+struct Cplx {
+    float re, im;
+};
+__device__ __forceinline__ Cplx cmul(Cplx a, Cplx b) {
+    return Cplx{fmaf(a.re, b.re, -(a.im * b.im)), fmaf(a.re, b.im, a.im * b.re)};
+}
+
+struct SqParams {
+    int nk;            // k-blocks
+    int M1, M2, M3;    // q-grid extents (M1 % 64 == 0)
+    int N;             // sites (true count)
+    int Kpad;          // sites padded to kBK
+    int R;             // replicas in this launch
+    int BN;            // columns (3R padded to 16)
+    const float2 *E1;  // [M1/16][Kpad]   exp(2 pi i (q0_1 + 16 m dq_1) u_i)
+    const float2 *E2;  // [M2][Kpad]
+    const float2 *E3;  // [M3][Kpad]
+    const float2 *bb;  // [Kpad]          exp(2 pi i dq_1 u_i)
+    float *sq;         // [R][Q]
+    float *comp;       // [R][Q][3]
+    int *err;
+};
+
+__global__ void __launch_bounds__(kThreads, 1)
+sq_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
+          SqParams P) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int b_bytes = P.BN * kBK * 2;
+    const int stage_bytes = 2 * Smem::a_bytes + 2 * b_bytes;  // multiple of 1024 (BN % 16 == 0 -> b_bytes % 2048 == 0)
+    uint8_t *bar_area = base + kStages * stage_bytes;
+    uint64_t *full = reinterpret_cast<uint64_t *>(bar_area);
+    uint64_t *empty = full + kStages;
+    uint64_t *done = empty + kStages;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tile = blockIdx.x;
+    const int tiles1 = P.M1 / 64;
+    const int t1 = tile % tiles1, h2 = (tile / tiles1) % P.M2, h3 = tile / (tiles1 * P.M2);
+    const int h1_0 = t1 * 64;
+
+    if (tid == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(smem_u32(&full[s]), kProducers + 1);
+            mbar_init(smem_u32(&empty[s]), 1);
+        }
+        mbar_init(smem_u32(done), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 4) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(tmem_slot)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = *tmem_slot;
+    bool ok = true;
+
+    if (warp < 4) {
+        // ------------------------------------------------------------- producers ----------
+        const int i = tid & 63;          // site within the k-block
+        const int jh = (tid >> 6) * 32;  // first of the 32 q-points this thread produces
+        for (int kb = 0; kb < P.nk && ok; ++kb) {
+            const int s = kb & 1, f = kb >> 1;
+            if (f >= 1 && !mbar_wait(smem_u32(&empty[s]), (f - 1) & 1, P.err, 1)) { ok = false; break; }
+            uint8_t *a_hi = base + s * stage_bytes;
+            uint8_t *a_lo = a_hi + Smem::a_bytes;
+            const int site = kb * kBK + i;
+            const float2 e2 = P.E2[(size_t)h2 * P.Kpad + site];
+            const float2 e3 = P.E3[(size_t)h3 * P.Kpad + site];
+            const float2 bq = P.bb[site];
+            const Cplx p23 = cmul(Cplx{e2.x, e2.y}, Cplx{e3.x, e3.y});
+            const Cplx b{bq.x, bq.y};
+#pragma unroll
+            for (int half = 0; half < 2; ++half) {
+                const int j0 = jh + 16 * half;
+                const float2 e1 = P.E1[(size_t)((h1_0 + j0) >> 4) * P.Kpad + site];
+                Cplx z = cmul(Cplx{e1.x, e1.y}, p23);
+#pragma unroll 4
+                for (int jj = 0; jj < 16; ++jj) {
+                    const int row = 2 * (j0 + jj);
+                    const __nv_bfloat16 ch = __float2bfloat16_rn(z.re);
+                    const __nv_bfloat16 cl = __float2bfloat16_rn(z.re - __bfloat162float(ch));
+                    const __nv_bfloat16 sh = __float2bfloat16_rn(z.im);
+                    const __nv_bfloat16 sl = __float2bfloat16_rn(z.im - __bfloat162float(sh));
+                    *reinterpret_cast<__nv_bfloat16 *>(a_hi + swz(row, i)) = ch;
+                    *reinterpret_cast<__nv_bfloat16 *>(a_lo + swz(row, i)) = cl;
+                    *reinterpret_cast<__nv_bfloat16 *>(a_hi + swz(row + 1, i)) = sh;
+                    *reinterpret_cast<__nv_bfloat16 *>(a_lo + swz(row + 1, i)) = sl;
+                    z = cmul(z, b);
+                }
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_arrive(smem_u32(&full[s]));
+        }
+    } else if (lane == 0) {
+        // ------------------------------------------------------- TMA + MMA issue --------
+        const uint32_t idesc = make_idesc(P.BN);
+        const uint32_t tx = 2u * (uint32_t)b_bytes;
+        auto issue_tma = [&](int kb) -> bool {
+            const int s = kb & 1, f = kb >> 1;
+            if (f >= 1 && !mbar_wait(smem_u32(&empty[s]), (f - 1) & 1, P.err, 2)) return false;
+            uint8_t *b_hi = base + s * stage_bytes + 2 * Smem::a_bytes;
+            uint8_t *b_lo = b_hi + b_bytes;
+            mbar_arrive_tx(smem_u32(&full[s]), tx);
+            tma_load_2d(smem_u32(b_hi), &map_hi, kb * kBK, 0, smem_u32(&full[s]));
+            tma_load_2d(smem_u32(b_lo), &map_lo, kb * kBK, 0, smem_u32(&full[s]));
+            return true;
+        };
+        int issued = 0;
+        if (P.nk > 0) ok = issue_tma(0);
+        for (int kb = 0; kb < P.nk && ok; ++kb) {
+            if (kb + 1 < P.nk && !issue_tma(kb + 1)) { ok = false; break; }
+            const int s = kb & 1, f = kb >> 1;
+            if (!mbar_wait(smem_u32(&full[s]), f & 1, P.err, 3)) { ok = false; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const uint32_t a_hi = smem_u32(base + s * stage_bytes);
+            const uint32_t a_lo = a_hi + Smem::a_bytes;
+            const uint32_t b_hi = a_hi + 2 * Smem::a_bytes;
+            const uint32_t b_lo = b_hi + b_bytes;
+#pragma unroll
+            for (int kk = 0; kk < kBK / 16; ++kk) {
+                const uint32_t o = kk * 32;  // 16 BF16 along K
+                umma(tmem, make_desc(a_hi + o), make_desc(b_hi + o), idesc, (kb | kk) ? 1u : 0u);
+                umma(tmem, make_desc(a_hi + o), make_desc(b_lo + o), idesc, 1u);
+                umma(tmem, make_desc(a_lo + o), make_desc(b_hi + o), idesc, 1u);
+            }
+            umma_commit(smem_u32(&empty[s]));
+            ++issued;
+        }
+        umma_commit(smem_u32(done));  // arrives once everything issued above has completed
+    }
+
+    // ------------------------------------------------------------------ epilogue ------
+    __syncwarp();
+    const bool fin = mbar_wait(smem_u32(done), 0, P.err, 4);
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    // tcgen05.ld is warp-collective: the whole warp reads, or none of it does
+    const bool go = __all_sync(0xffffffffu, fin && ok) && *(volatile int *)P.err == 0;
+    if (warp < 4 && __all_sync(0xffffffffu, go)) {
+        const int Q = P.M1 * P.M2 * P.M3;
+        const int row = warp * 32 + lane;  // TMEM lane = D row
+        const int qloc = row >> 1;         // rows 2q, 2q+1 = cos, sin
+        const int q = h1_0 + qloc + P.M1 * (h2 + P.M2 * h3);
+        const float invN = 1.0f / (float)P.N;
+        for (int r = 0; r < P.R; ++r) {
+            uint32_t v[4];
+            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(3 * r);
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
+                         : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]) : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            float tot = 0.f, mag[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const float mine = __uint_as_float(v[a]);
+                const float other = __shfl_xor_sync(0xffffffffu, mine, 1);
+                const float m2 = mine * mine + other * other;  // Re^2 + Im^2
+                tot += m2;
+                mag[a] = sqrtf(m2) * invN;
+            }
+            if ((lane & 1) == 0) {
+                P.sq[(size_t)r * Q + q] = tot * invN * invN;
+                float *c = P.comp + ((size_t)r * Q + q) * 3;
+                c[0] = mag[0];
+                c[1] = mag[1];
+                c[2] = mag[2];
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 4) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
+    }
+}
+
+// B = spins in BF16 hi / lo, [BN rows = 3r + a][Kpad sites] (sites in storage order).
+__global__ void sq_prep_b(const uint8_t *__restrict__ spins, const float4 *__restrict__ spins4,
+                          int model, int N, int Kpad, int r0, int R, int BN,
+                          __nv_bfloat16 *__restrict__ bhi, __nv_bfloat16 *__restrict__ blo) {
+    const long total = (long)BN * Kpad;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+        const int n = (int)(e / Kpad), k = (int)(e - (long)n * Kpad);
+        const int r = n / 3, a = n - 3 * r;
+        float x = 0.f;
+        if (r < R && k < N) {
+            if (model == 0) x = (a == 2) ? (spins[(size_t)(r0 + r) * N + k] ? 1.f : -1.f) : 0.f;
+            else {
+                const float4 S = spins4[(size_t)(r0 + r) * N + k];
+                x = a == 0 ? S.x : a == 1 ? S.y : S.z;
+            }
+        }
+        const __nv_bfloat16 h = __float2bfloat16_rn(x);
+        bhi[e] = h;
+        blo[e] = __float2bfloat16_rn(x - __bfloat162float(h));
+    }
+}
+
+}  // namespace sq
+}  // namespace ether
+
+using namespace ether;
+using namespace ether::sq;
+
+namespace {
+PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q;
+        void *p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+}  // namespace
+
+namespace ether {
+// Host driver for ether_structure_factor (declared in the C-ABI, defined in ether_api.cu
+// through this function).
+int structure_factor_launch(Ctx &c, const double *frac /*3N, storage order*/, const int nq[3],
+                            const double q0[3], const double dq[3], float *sq_host,
+                            float *comp_host, std::string &msg) {
+    const int N = c.N;
+    const int Kpad = (N + kBK - 1) / kBK * kBK;
+    const int M1 = nq[0], M2 = nq[1], M3 = nq[2];
+    const long Q = (long)M1 * M2 * M3;
+    if (M1 <= 0 || M2 <= 0 || M3 <= 0 || M1 % 64 != 0) { msg = "nq[0] must be a positive multiple of 64, nq[1], nq[2] positive"; return ETHER_ERR_ARG; }
+    if (Q * 2 > 0x7FFFFFFFL) { msg = "q-grid too large"; return ETHER_ERR_ARG; }
+    PFN_cuTensorMapEncodeTiled_v12000 encode = get_encode();
+    if (!encode) { msg = "cuTensorMapEncodeTiled not available"; return ETHER_ERR_CUDA; }
+    // phase tables in FP64 on the host
+    const double tp = 2.0 * M_PI;
+    std::vector<float2> E1((size_t)(M1 / 16) * Kpad, make_float2(0.f, 0.f));
+    std::vector<float2> E2((size_t)M2 * Kpad, make_float2(0.f, 0.f)), E3((size_t)M3 * Kpad, make_float2(0.f, 0.f));
+    std::vector<float2> bb(Kpad, make_float2(1.f, 0.f));
+    for (int i = 0; i < N; ++i) {
+        const double u = frac[3 * i], v = frac[3 * i + 1], w = frac[3 * i + 2];
+        for (int m = 0; m < M1 / 16; ++m) {
+            const double ph = tp * (q0[0] + 16.0 * m * dq[0]) * u;
+            E1[(size_t)m * Kpad + i] = make_float2((float)cos(ph), (float)sin(ph));
+        }
+        for (int h = 0; h < M2; ++h) {
+            const double ph = tp * (q0[1] + h * dq[1]) * v;
+            E2[(size_t)h * Kpad + i] = make_float2((float)cos(ph), (float)sin(ph));
+        }
+        for (int h = 0; h < M3; ++h) {
+            const double ph = tp * (q0[2] + h * dq[2]) * w;
+            E3[(size_t)h * Kpad + i] = make_float2((float)cos(ph), (float)sin(ph));
+        }
+        const double ph = tp * dq[0] * u;
+        bb[i] = make_float2((float)cos(ph), (float)sin(ph));
+    }
+    const int rmax = 85;  // 3 * 85 = 255 <= 256 columns of TMEM per pass
+    float2 *dE1 = nullptr, *dE2 = nullptr, *dE3 = nullptr, *dbb = nullptr;
+    __nv_bfloat16 *bhi = nullptr, *blo = nullptr;
+    float *dsq = nullptr, *dcomp = nullptr;
+    int *derr = nullptr;
+    int rc = ETHER_OK;
+    const int rpass = std::min(c.R, rmax);
+    const int BNmax = (3 * rpass + 15) / 16 * 16;
+    auto cleanup = [&]() {
+        cudaFree(dE1); cudaFree(dE2); cudaFree(dE3); cudaFree(dbb); cudaFree(bhi); cudaFree(blo);
+        cudaFree(dsq); cudaFree(dcomp); cudaFree(derr);
+    };
+#define SQ_TRY(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { msg = std::string(#x) + ": " + cudaGetErrorString(e_); cleanup(); return ETHER_ERR_CUDA; } } while (0)
+    SQ_TRY(cudaMalloc(&dE1, E1.size() * sizeof(float2)));
+    SQ_TRY(cudaMalloc(&dE2, E2.size() * sizeof(float2)));
+    SQ_TRY(cudaMalloc(&dE3, E3.size() * sizeof(float2)));
+    SQ_TRY(cudaMalloc(&dbb, bb.size() * sizeof(float2)));
+    SQ_TRY(cudaMalloc(&bhi, (size_t)BNmax * Kpad * 2));
+    SQ_TRY(cudaMalloc(&blo, (size_t)BNmax * Kpad * 2));
+    SQ_TRY(cudaMalloc(&dsq, (size_t)rpass * Q * sizeof(float)));
+    SQ_TRY(cudaMalloc(&dcomp, (size_t)rpass * Q * 3 * sizeof(float)));
+    SQ_TRY(cudaMalloc(&derr, sizeof(int)));
+    SQ_TRY(cudaMemcpyAsync(dE1, E1.data(), E1.size() * sizeof(float2), cudaMemcpyHostToDevice, c.stream));
+    SQ_TRY(cudaMemcpyAsync(dE2, E2.data(), E2.size() * sizeof(float2), cudaMemcpyHostToDevice, c.stream));
+    SQ_TRY(cudaMemcpyAsync(dE3, E3.data(), E3.size() * sizeof(float2), cudaMemcpyHostToDevice, c.stream));
+    SQ_TRY(cudaMemcpyAsync(dbb, bb.data(), bb.size() * sizeof(float2), cudaMemcpyHostToDevice, c.stream));
+    for (int r0 = 0; r0 < c.R && rc == ETHER_OK; r0 += rpass) {
+        const int R = std::min(rpass, c.R - r0);
+        const int BN = (3 * R + 15) / 16 * 16;
+        SQ_TRY(cudaMemsetAsync(derr, 0, sizeof(int), c.stream));
+        sq_prep_b<<<std::max(1, std::min(4096, (int)(((long)BN * Kpad + 255) / 256))), 256, 0, c.stream>>>(
+            c.spins, c.spins4, c.model, N, Kpad, r0, R, BN, bhi, blo);
+        c.launches++;
+        CUtensorMap mh, ml;
+        cuuint64_t gdim[2] = {(cuuint64_t)Kpad, (cuuint64_t)BN};
+        cuuint64_t gstride[1] = {(cuuint64_t)Kpad * 2};
+        cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)BN};
+        cuuint32_t estride[2] = {1, 1};
+        CUresult cr = encode(&mh, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, bhi, gdim, gstride, box, estride,
+                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (cr == CUDA_SUCCESS)
+            cr = encode(&ml, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, blo, gdim, gstride, box, estride,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (cr != CUDA_SUCCESS) { msg = "cuTensorMapEncodeTiled failed"; cleanup(); return ETHER_ERR_CUDA; }
+        SqParams P;
+        P.nk = Kpad / kBK;
+        P.M1 = M1; P.M2 = M2; P.M3 = M3;
+        P.N = N; P.Kpad = Kpad; P.R = R; P.BN = BN;
+        P.E1 = dE1; P.E2 = dE2; P.E3 = dE3; P.bb = dbb;
+        P.sq = dsq; P.comp = dcomp; P.err = derr;
+        const int stage_bytes = 2 * Smem::a_bytes + 2 * BN * kBK * 2;
+        const int smem = 1024 + kStages * stage_bytes + 64;
+        SQ_TRY(cudaFuncSetAttribute(sq_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        const int tiles = (int)(Q / 64);
+        sq_kernel<<<tiles, kThreads, smem, c.stream>>>(mh, ml, P);
+        c.launches++;
+        SQ_TRY(cudaGetLastError());
+        int herr = 0;
+        SQ_TRY(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+        SQ_TRY(cudaMemcpyAsync(sq_host + (size_t)r0 * Q, dsq, (size_t)R * Q * sizeof(float), cudaMemcpyDeviceToHost, c.stream));
+        SQ_TRY(cudaMemcpyAsync(comp_host + (size_t)r0 * Q * 3, dcomp, (size_t)R * Q * 3 * sizeof(float), cudaMemcpyDeviceToHost, c.stream));
+        SQ_TRY(cudaStreamSynchronize(c.stream));
+        if (herr) { msg = "structure-factor kernel: a pipeline wait timed out (stage " + std::to_string(herr) + ")"; rc = ETHER_ERR_TIMEOUT; }
+    }
+#undef SQ_TRY
+    cleanup();
+    return rc;
+}
+}  // namespace ether

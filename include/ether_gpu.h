@@ -216,6 +216,17 @@ int ether_autotune(ether_ctx *ctx, int32_t *variant, float *best_ms);
 /* Force a kernel variant (same encoding as ether_autotune). */
 int ether_set_variant(ether_ctx *ctx, int32_t variant);
 
+/* structure_factor (utility/Structure_Factor/structure_factor.f90:99-183) of every replica's
+ * current configuration on a 3-D grid of q, on the tensor cores (BF16 high/low split
+ * products, FP32 accumulation; about 16 significant bits per product).
+ *   q(h) = sum_a (q0[a] + h_a dq[a]) b_a,  h_a = 0 .. nq[a]-1,  b_a the reciprocal vectors of
+ *   the cell abc (rows a1, a2, a3; b_a . a_b = 2 pi delta_ab), nq[0] a multiple of 64.
+ *   sq(Q, R)      = |S(q)|^2 / N^2     (the reference's real(dot_product(Cq, Cq))/N^2)
+ *   comp(3, Q, R) = |S_a(q)| / N        (the reference's abs(S_q_a)/N)
+ *   with q index h1 + nq[0]*(h2 + nq[1]*h3), S_a(q) = sum_i S_i,a exp(i q.r_i). */
+int ether_structure_factor(ether_ctx *ctx, const double *abc, const int32_t nq[3],
+                           const double q0[3], const double dq[3], float *sq, float *comp);
+
 /* ------------------------------------------------------------- no-allocation energy ---- */
 /* No counterpart in the reference.  Energy and magnetisation of n_replicas simple-cubic
  * configurations already in device memory, for callers that cannot allocate device memory
