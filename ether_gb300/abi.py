@@ -57,6 +57,7 @@ class Info(C.Structure):
         ("n_colours", C.c_int32), ("fast_path", C.c_int32), ("n_types", C.c_int32),
         ("table_entries", C.c_int32), ("n_slots", C.c_int32), ("n_groups", C.c_int32),
         ("device_bytes", C.c_size_t), ("kernel_launches", C.c_uint64),
+        ("sq_kernel_ms", C.c_float),
     ]
 
 

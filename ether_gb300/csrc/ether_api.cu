@@ -852,6 +852,7 @@ extern "C" int ether_get_info(ether_ctx *h, ether_info *info) {
     info->n_groups = c.n_groups;
     info->device_bytes = c.device_bytes;
     info->kernel_launches = c.launches;
+    info->sq_kernel_ms = c.sq_ms;
     return ETHER_OK;
 }
 

@@ -99,6 +99,7 @@ struct Ctx {
     std::map<std::string, cudaGraphExec_t> graphs;  // ether_mcs chunks by gate pattern
     size_t device_bytes = 0;
     uint64_t launches = 0;
+    float sq_ms = 0.f;  // last structure-factor kernel time (CUDA events)
     int sm_count = 0;
 };
 

@@ -10,15 +10,15 @@
 //
 // One CTA owns a 128-row tile of D (64 q-points: consecutive h1 at fixed h2, h3) and all
 // 3R columns (<= 256).  Per 64-site k-block:
-//   * warps 0-3 generate the A tile in shared memory: phase factors
+//   * warps 0-7 generate the A tile in shared memory: phase factors
 //       exp(i q.r) = E1[h1_0 + 16m][i] * E2[h2][i] * E3[h3][i] * b_i^j,  b_i = exp(2 pi i dq_1 u_i)
 //     (complex FP32, restarted every 16 steps from FP64-built tables), split into hi/lo and
 //     stored in the K-major 128-byte-swizzled layout the MMA descriptors describe;
-//   * one thread of warp 4 loads the B_hi / B_lo tiles with TMA (same swizzle) and issues the
+//   * one thread of warp 8 loads the B_hi / B_lo tiles with TMA (same swizzle) and issues the
 //     12 tcgen05.mma (3 products x 4 K-steps of 16), then tcgen05.commit to the stage's
 //     "empty" barrier;
 //   * two stages: A generation and TMA of block k+1 overlap the MMAs of block k.
-// Epilogue: warps 0-3 read the accumulator with tcgen05.ld (warp w owns TMEM lanes 32w..),
+// Epilogue: warps 0-7 read the accumulator with tcgen05.ld (warp w owns TMEM lanes 32(w%4)..),
 // pair cos/sin rows with a lane shuffle and write |S(q)|^2 / N^2 and |S_a(q)| / N.
 //
 // Every mbarrier wait is bounded (%globaltimer, 2 s): on expiry the kernel records an error
@@ -39,8 +39,8 @@ namespace sq {
 constexpr int kBM = 128;        // rows per tile (64 q-points x cos/sin)
 constexpr int kBK = 64;         // sites per k-block (128 bytes of BF16)
 constexpr int kStages = 2;
-constexpr int kProducers = 128; // warps 0-3
-constexpr int kThreads = 160;   // + warp 4 (TMA + MMA issue)
+constexpr int kProducers = 256; // warps 0-7
+constexpr int kThreads = 288;   // + warp 8 (TMA + MMA issue)
 constexpr uint64_t kWaitNs = 2000000000ull;
 
 struct Smem {
@@ -180,7 +180,7 @@ sq_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CU
         mbar_init(smem_u32(done), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 4) {
+    if (warp == kProducers / 32) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(tmem_slot)));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
@@ -190,39 +190,48 @@ sq_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CU
     const uint32_t tmem = *tmem_slot;
     bool ok = true;
 
-    if (warp < 4) {
+    if (warp < kProducers / 32) {
         // ------------------------------------------------------------- producers ----------
-        const int i = tid & 63;          // site within the k-block
-        const int jh = (tid >> 6) * 32;  // first of the 32 q-points this thread produces
+        // thread = (site i of the k-block, block of 16 q-points j0 .. j0+15 = rows 32 rq ..)
+        const int i = tid & 63;
+        const int rq = tid >> 6;  // 0..3
+        const int j0 = 16 * rq;
+        // byte offsets of (row, i) for the 8 rows of a swizzle atom (row & 7 = x)
+        uint32_t cx[8];
+#pragma unroll
+        for (int x = 0; x < 8; ++x) cx[x] = (uint32_t)(x * 128 + ((((i >> 3) ^ x)) << 4) + (i & 7) * 2);
+        const uint32_t rowbase = (uint32_t)(rq * 4 * 1024);  // atoms 4 rq .. 4 rq + 3
+        const size_t e1row = (size_t)((h1_0 + j0) >> 4) * P.Kpad;
+        const size_t e2row = (size_t)h2 * P.Kpad, e3row = (size_t)h3 * P.Kpad;
+        // phase factors of the first k-block, then prefetched one block ahead
+        float2 e1 = P.E1[e1row + i], e2 = P.E2[e2row + i], e3 = P.E3[e3row + i], bq = P.bb[i];
         for (int kb = 0; kb < P.nk && ok; ++kb) {
             const int s = kb & 1, f = kb >> 1;
-            if (f >= 1 && !mbar_wait(smem_u32(&empty[s]), (f - 1) & 1, P.err, 1)) { ok = false; break; }
-            uint8_t *a_hi = base + s * stage_bytes;
-            uint8_t *a_lo = a_hi + Smem::a_bytes;
-            const int site = kb * kBK + i;
-            const float2 e2 = P.E2[(size_t)h2 * P.Kpad + site];
-            const float2 e3 = P.E3[(size_t)h3 * P.Kpad + site];
-            const float2 bq = P.bb[site];
             const Cplx p23 = cmul(Cplx{e2.x, e2.y}, Cplx{e3.x, e3.y});
+            Cplx z = cmul(Cplx{e1.x, e1.y}, p23);
             const Cplx b{bq.x, bq.y};
+            if (kb + 1 < P.nk) {
+                const int nxt = (kb + 1) * kBK + i;
+                e1 = P.E1[e1row + nxt];
+                e2 = P.E2[e2row + nxt];
+                e3 = P.E3[e3row + nxt];
+                bq = P.bb[nxt];
+            }
+            if (f >= 1 && !mbar_wait(smem_u32(&empty[s]), (f - 1) & 1, P.err, 1)) { ok = false; break; }
+            uint8_t *a_hi = base + s * stage_bytes + rowbase;
+            uint8_t *a_lo = a_hi + Smem::a_bytes;
 #pragma unroll
-            for (int half = 0; half < 2; ++half) {
-                const int j0 = jh + 16 * half;
-                const float2 e1 = P.E1[(size_t)((h1_0 + j0) >> 4) * P.Kpad + site];
-                Cplx z = cmul(Cplx{e1.x, e1.y}, p23);
-#pragma unroll 4
-                for (int jj = 0; jj < 16; ++jj) {
-                    const int row = 2 * (j0 + jj);
-                    const __nv_bfloat16 ch = __float2bfloat16_rn(z.re);
-                    const __nv_bfloat16 cl = __float2bfloat16_rn(z.re - __bfloat162float(ch));
-                    const __nv_bfloat16 sh = __float2bfloat16_rn(z.im);
-                    const __nv_bfloat16 sl = __float2bfloat16_rn(z.im - __bfloat162float(sh));
-                    *reinterpret_cast<__nv_bfloat16 *>(a_hi + swz(row, i)) = ch;
-                    *reinterpret_cast<__nv_bfloat16 *>(a_lo + swz(row, i)) = cl;
-                    *reinterpret_cast<__nv_bfloat16 *>(a_hi + swz(row + 1, i)) = sh;
-                    *reinterpret_cast<__nv_bfloat16 *>(a_lo + swz(row + 1, i)) = sl;
-                    z = cmul(z, b);
-                }
+            for (int jj = 0; jj < 16; ++jj) {
+                // rows 2(j0+jj) (cos) and 2(j0+jj)+1 (sin): atom jj/4, rows 2(jj%4), 2(jj%4)+1
+                const __nv_bfloat162 hi = __floats2bfloat162_rn(z.re, z.im);
+                const __nv_bfloat162 lo = __floats2bfloat162_rn(z.re - __low2float(hi), z.im - __high2float(hi));
+                const uint32_t oc = (uint32_t)((jj >> 2) * 1024) + cx[2 * (jj & 3)];
+                const uint32_t os = (uint32_t)((jj >> 2) * 1024) + cx[2 * (jj & 3) + 1];
+                *reinterpret_cast<__nv_bfloat16 *>(a_hi + oc) = __low2bfloat16(hi);
+                *reinterpret_cast<__nv_bfloat16 *>(a_hi + os) = __high2bfloat16(hi);
+                *reinterpret_cast<__nv_bfloat16 *>(a_lo + oc) = __low2bfloat16(lo);
+                *reinterpret_cast<__nv_bfloat16 *>(a_lo + os) = __high2bfloat16(lo);
+                z = cmul(z, b);
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             mbar_arrive(smem_u32(&full[s]));
@@ -271,15 +280,18 @@ sq_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CU
     asm volatile("tcgen05.fence::after_thread_sync;");
     // tcgen05.ld is warp-collective: the whole warp reads, or none of it does
     const bool go = __all_sync(0xffffffffu, fin && ok) && *(volatile int *)P.err == 0;
-    if (warp < 4 && __all_sync(0xffffffffu, go)) {
+    if (warp < kProducers / 32 && __all_sync(0xffffffffu, go)) {
+        // warp w reads TMEM lanes 32 (w % 4) ..; warps w and w + 4 share the rows and split
+        // the replicas between them
         const int Q = P.M1 * P.M2 * P.M3;
-        const int row = warp * 32 + lane;  // TMEM lane = D row
+        const int wl = warp & 3;
+        const int row = wl * 32 + lane;    // TMEM lane = D row
         const int qloc = row >> 1;         // rows 2q, 2q+1 = cos, sin
         const int q = h1_0 + qloc + P.M1 * (h2 + P.M2 * h3);
         const float invN = 1.0f / (float)P.N;
-        for (int r = 0; r < P.R; ++r) {
+        for (int r = warp >> 2; r < P.R; r += kProducers / 128) {
             uint32_t v[4];
-            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(3 * r);
+            const uint32_t taddr = tmem + ((uint32_t)(wl * 32) << 16) + (uint32_t)(3 * r);
             asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
                          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]) : "r"(taddr));
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
@@ -303,7 +315,7 @@ sq_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CU
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
-    if (warp == 4) {
+    if (warp == kProducers / 32) {
         asm volatile("tcgen05.fence::after_thread_sync;");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
     }
@@ -443,9 +455,21 @@ int structure_factor_launch(Ctx &c, const double *frac /*3N, storage order*/, co
         const int smem = 1024 + kStages * stage_bytes + 64;
         SQ_TRY(cudaFuncSetAttribute(sq_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         const int tiles = (int)(Q / 64);
+        cudaEvent_t ev0, ev1;
+        SQ_TRY(cudaEventCreate(&ev0));
+        SQ_TRY(cudaEventCreate(&ev1));
+        SQ_TRY(cudaEventRecord(ev0, c.stream));
         sq_kernel<<<tiles, kThreads, smem, c.stream>>>(mh, ml, P);
         c.launches++;
         SQ_TRY(cudaGetLastError());
+        SQ_TRY(cudaEventRecord(ev1, c.stream));
+        SQ_TRY(cudaEventSynchronize(ev1));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev0, ev1);
+        if (r0 == 0) c.sq_ms = 0.f;
+        c.sq_ms += ms;
+        cudaEventDestroy(ev0);
+        cudaEventDestroy(ev1);
         int herr = 0;
         SQ_TRY(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
         SQ_TRY(cudaMemcpyAsync(sq_host + (size_t)r0 * Q, dsq, (size_t)R * Q * sizeof(float), cudaMemcpyDeviceToHost, c.stream));

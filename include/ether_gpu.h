@@ -192,6 +192,7 @@ typedef struct ether_info {
     int32_t n_slots, n_groups;
     size_t device_bytes;     /* device memory owned by the context                         */
     uint64_t kernel_launches;/* kernels launched by this context so far                    */
+    float sq_kernel_ms;      /* CUDA-event time of the last ether_structure_factor's kernels */
 } ether_info;
 int ether_get_info(ether_ctx *ctx, ether_info *info);
 /* colour(N) and rank_in_colour(N) of the Checkerboard order. */
