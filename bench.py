@@ -1,22 +1,27 @@
 #!/usr/bin/env python
-"""Benchmark of the plain Checkerboard Metropolis sweep on one GB300.
+"""Benchmark of ETHER's Monte Carlo sweep on one GB300.
 
-Workload (the L = 64 simple-cubic target): plain colour-ordered Metropolis sweeps of the
-64^3 simple-cubic Ising model at k_B T_c = 4.511 J (J = 1 meV, ferromagnetic), a batch of
+Headline (metric "spin updates/ns"): plain Checkerboard Metropolis sweeps of the 64^3
+simple-cubic Ising model at k_B T_c = 4.511 J (J = 1 meV, ferromagnetic, periodic), a batch of
 R = 1024 independent replicas (each its own Philox stream) so the int8 state (268 MB) is
 larger than the 129 MB L2.  A step is one full sweep (both colour phases) of every replica.
 
-  value  = spin updates / ns over the timed steps (device-resident state, CUDA events)
-  e2e    = same metric through the C-ABI with host buffers: the configuration is uploaded
-           from host memory at the start, each step returns the acceptance ratios to the
-           host (the reference's Metropolis(beta, accept) boundary), the final
-           configuration of replica 0 is read back at the end
-  roofline = dominant kernel (one colour phase) at 3 algorithmic bytes per site update
-  cpu_baseline = the oracle's typewriter restatement of src/Metropolis.f90 +
-           src/get_tot_energy.f90 (what ether.f90 does per MCS), one replica per host core
+  value        spin updates / ns over the timed steps (state resident in HBM, CUDA events)
+  e2e          the same sweeps through the C-ABI from host memory: configuration uploaded at
+               the start, acceptance ratios returned to the host every step (the reference's
+               Metropolis(beta, accept) boundary), replica 0 read back at the end
+  roofline     the dominant kernel (one colour phase) at 3 algorithmic bytes per update
+  cpu_baseline the oracle's typewriter restatement of src/Metropolis.f90 + get_tot_energy per
+               MCS (what src/ether.f90:172-177 does), one replica per host core
 
---impl reference times that CPU restatement on all host cores as the reference arm (the
-Fortran reference itself cannot be built: no gfortran / MPI on this image or the box).
+components (same JSON line): the 64^3 Heisenberg sweep (48 B per update), the structure
+factor on the tensor cores at the pyrochlore size (16-site cell x 12^3 = 27648 sites, 64
+replicas, 64^3 q-grid), and tau_int(|M|) at T_c with the independent samples per second it
+implies.
+
+--impl reference times the oracle's CPU restatement on all host cores (the Fortran reference
+cannot be built: no gfortran / MPI on this image or the GPU machine).
+--model sq times only the structure factor (for profiling).
 """
 import argparse
 import ctypes as C
@@ -48,11 +53,6 @@ def _cudart():
             return C.CDLL(name)
         except OSError:
             pass
-    for d in ("/usr/local/cuda/lib64", "/usr/local/cuda/targets/sbsa-linux/lib",
-              "/usr/local/cuda/targets/x86_64-linux/lib"):
-        p = os.path.join(d, "libcudart.so")
-        if os.path.exists(p):
-            return C.CDLL(p)
     raise RuntimeError("libcudart not found")
 
 
@@ -79,7 +79,7 @@ class Events:
 
 
 class ClockSampler:
-    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    """nvidia-smi samples of SM clock and throttle reasons during a timed region."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -150,7 +150,8 @@ def make_workload(model, L, replicas, seed=1992):
     return lat, j, sw, ion, beta
 
 
-def run_gpu(model, L, replicas, steps, warmup, rank, world, force_variant=0):
+def run_sweeps(model, L, replicas, steps, warmup, rank, world, force_variant=0, clocks=True,
+               e2e=True):
     import ether_gb300 as eg
     lat, j, sw, ion, beta = make_workload(model, L, replicas, seed=1992 + 7919 * rank)
     sw.set_spins(ion)
@@ -158,7 +159,7 @@ def run_gpu(model, L, replicas, steps, warmup, rank, world, force_variant=0):
         sw.set_variant(force_variant)
         variant = force_variant
     else:
-        variant, tuned_ms = sw.autotune()
+        variant, _ = sw.autotune()
     N, R = lat.N, replicas
     ev = Events(sw.stream())
     for _ in range(warmup):
@@ -166,9 +167,10 @@ def run_gpu(model, L, replicas, steps, warmup, rank, world, force_variant=0):
     sw.sync()
     _barrier(world)
     launches0 = sw.info().kernel_launches
-    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")) if world > 1 else 0)
-    clocks.start()
-    time.sleep(0.3)
+    sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")) if world > 1 else 0)
+    if clocks:
+        sampler.start()
+        time.sleep(0.3)
     marks = []
     t0 = ev.record()
     for _ in range(steps):
@@ -183,43 +185,90 @@ def run_gpu(model, L, replicas, steps, warmup, rank, world, force_variant=0):
     sw.sync()
     total_ms = ev.ms(t0, t1)
     phase_ms = [ev.ms(a, b) for a, b, c in marks] + [ev.ms(b, c) for a, b, c in marks]
-    clk = clocks.stop()
+    clk = sampler.stop() if clocks else None
     launches = sw.info().kernel_launches - launches0
     ev.free([t0, t1] + [e for m in marks for e in m])
     _barrier(world)
     total_ms = _max_over_ranks(total_ms, world)
     updates = float(N) * R * steps
     value = updates / (total_ms * 1e6) * world
-    # dominant kernel: one colour phase = R*N/2 updates
     bpu = BYTES_ISING if model == eg.MODEL_ISING else BYTES_HEIS
     phase_avg_ms = float(np.mean(phase_ms))
     achieved_gbs = bpu * (R * N / 2.0) / (phase_avg_ms * 1e-3) / 1e9
-
-    # end to end through the C-ABI with host buffers
-    acc = None
-    t_start = time.perf_counter()
-    sw.set_spins(ion)
-    ev2 = Events(sw.stream())
-    e0 = ev2.record()
-    for _ in range(steps):
-        acc = sw.metropolis(1, accept=True)   # D2H of R doubles every step
-    out = sw.get_spins(lat.ion, 0)
-    e1 = ev2.record()
-    sw.sync()
-    t_e2e = time.perf_counter() - t_start
-    ev2.free([e0, e1])
-    e2e = updates / (t_e2e * 1e9) * world
-    h2d = (N * (1 if model == eg.MODEL_ISING else 16) * R) / steps
-    d2h = 8.0 * R + (N * (1 if model == eg.MODEL_ISING else 16)) / steps
+    res = {"value": value, "ms_per_step": total_ms / steps, "phase_ms": phase_avg_ms,
+           "achieved_gbs": achieved_gbs, "bytes_per_update": bpu, "launches": int(launches),
+           "clocks": clk, "variant": variant}
+    if e2e:
+        acc = None
+        t_start = time.perf_counter()
+        sw.set_spins(ion)
+        for _ in range(steps):
+            acc = sw.metropolis(1, accept=True)   # D2H of R doubles every step
+        sw.get_spins(lat.ion, 0)
+        t_e2e = time.perf_counter() - t_start
+        esize = 1 if model == eg.MODEL_ISING else 16
+        res.update({"e2e": updates / (t_e2e * 1e9) * world,
+                    "h2d": (N * esize * R) / steps,
+                    "d2h": 8.0 * R + (N * esize) / steps,
+                    "accept_mean": float(np.mean(acc))})
     sw.close()
-    return {
-        "value": value, "ms_per_step": total_ms / steps, "phase_ms": phase_avg_ms,
-        "achieved_gbs": achieved_gbs, "bytes_per_update": bpu, "launches": int(launches),
-        "clocks": clk, "e2e": e2e, "h2d": h2d, "d2h": d2h,
-        "accept_mean": float(np.mean(acc)) if acc is not None else None,
-        "check_spin_sum": float(out[:, 3].sum()),
-        "variant": variant,
-    }
+    return res
+
+
+def run_sq(cells=12, replicas=64, M=64, calls=3, warmup=1):
+    """Structure factor of `replicas` pyrochlore configurations (16-site cell x cells^3) on an
+    M^3 q-grid; the fastest kernel time and the tensor throughput."""
+    import ether_gb300 as eg
+    from ether_gb300 import abi
+    lat = eg.pyrochlore(cells)
+    j = eg.couplings(1, [[(1, 1, (1.0, 1.0, 1.0))]], [1.0])
+    sw = eg.Sweep.from_lattice(lat, j, np.array([1.0]), eg.MODEL_XYZ, replicas=replicas)
+    rng = np.random.default_rng(0)
+    ion = lat.ion.copy()
+    v = rng.normal(size=(lat.N, 3))
+    ion[:, 1:4] = v / np.linalg.norm(v, axis=1, keepdims=True)
+    sw.set_spins(ion)
+    nq = np.array([M, M, M], dtype=np.int32)
+    Q = M ** 3
+    sq = np.zeros(replicas * Q, np.float32)
+    comp = np.zeros(replicas * Q * 3, np.float32)
+    abc = (np.eye(3) * eg.model.PYROCHLORE_A).ravel()
+    q0 = np.array([-1.0, -1.0, -1.0])
+    dq = np.array([2.0 / M] * 3)
+    times = []
+    for it in range(warmup + calls):
+        abi.check(sw.lib.ether_structure_factor(
+            sw.h, abi.dptr(abc), abi.iptr(nq), abi.dptr(q0), abi.dptr(dq),
+            sq.ctypes.data_as(C.POINTER(C.c_float)), comp.ctypes.data_as(C.POINTER(C.c_float))))
+        if it >= warmup:
+            times.append(sw.info().sq_kernel_ms)
+    ms = min(times)
+    flops = 3 * 2.0 * (2 * Q) * (3 * replicas) * lat.N   # three BF16 products
+    sw.close()
+    return {"sites": lat.N, "replicas": replicas, "q_points": Q, "kernel_ms": ms,
+            "tensor_tflops": flops / ms / 1e9, "useful_tflops": flops / 3 / ms / 1e9}
+
+
+def run_tau(L=64, replicas=128, equil=20000, sweeps=100000, stride=10):
+    """tau_int(|M|) of the plain Checkerboard sweep at T_c, and the independent samples/s."""
+    import ether_gb300 as eg
+    from ether_gb300.analysis import tau_int
+    lat, j, sw, ion, beta = make_workload(eg.MODEL_ISING, L, replicas, seed=4242)
+    sw.set_spins(ion)
+    sw.autotune()
+    sw.metropolis(equil, accept=False)
+    sw.sync()
+    t = time.perf_counter()
+    m = sw.record_series(sweeps, stride=stride)
+    dt = time.perf_counter() - t
+    tau, err, W = tau_int(m)
+    tau_sweeps = tau * stride
+    sweeps_per_s = sweeps / dt
+    sw.close()
+    return {"L": L, "replicas": replicas, "equilibration_sweeps": equil, "measured_sweeps": sweeps,
+            "stride": stride, "tau_int_absM_sweeps": tau_sweeps, "tau_err_sweeps": err * stride,
+            "window": W, "sweeps_per_s_per_replica": sweeps_per_s,
+            "independent_samples_per_s": replicas * sweeps_per_s / (2.0 * tau_sweeps)}
 
 
 def cpu_reference(model, L, mcs, threads, seed=1992):
@@ -268,18 +317,27 @@ def _max_over_ranks(x, world):
     return float(t.item())
 
 
+def _peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=2000)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--model", default="ising", choices=["ising", "heisenberg"])
+    ap.add_argument("--model", default="ising", choices=["ising", "heisenberg", "sq"])
     ap.add_argument("--L", type=int, default=64)
     ap.add_argument("--replicas", type=int, default=0)
     ap.add_argument("--cpu-mcs", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-components", action="store_true")
     ap.add_argument("--variant", type=int, default=0)
+    ap.add_argument("--sq-cells", type=int, default=12)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -291,9 +349,25 @@ def main():
         dist.init_process_group("gloo")
 
     import ether_gb300 as eg
+    peaks = _peaks()
+    hbm_peak = peaks.get("hbm_gbs") or 6800.0
+    peak_src = "measured" if peaks.get("hbm_gbs") else "fallback"
+    bf16_peak = peaks.get("bf16_tflops") or 1900.0
+    cores = os.cpu_count() or 1
+
+    if args.model == "sq":
+        if rank != 0:
+            return 0
+        r = run_sq(cells=args.sq_cells, replicas=args.replicas or 64, calls=1, warmup=args.warmup)
+        print(json.dumps({"metric": "structure factor kernel ms", "value": r["kernel_ms"],
+                          "unit": "ms", "higher_is_better": False, "detail": r,
+                          "roofline": {"bound": "tensor", "achieved": r["tensor_tflops"],
+                                       "peak": bf16_peak, "unit": "TFLOP/s",
+                                       "frac": r["tensor_tflops"] / bf16_peak}}))
+        return 0
+
     model = eg.MODEL_ISING if args.model == "ising" else eg.MODEL_XYZ
     replicas = args.replicas or (1024 if model == eg.MODEL_ISING else 64)
-    cores = os.cpu_count() or 1
     workload = ("plain checkerboard Metropolis, simple-cubic %d^3 %s at kT_c=%.3f J "
                 "(J=1 meV FM, periodic), %d independent replicas per GPU" %
                 (args.L, "Ising int8" if model == 0 else "Heisenberg float4",
@@ -307,8 +381,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return 0
-        mcs = args.cpu_mcs or 300
-        ref = cpu_reference(model, args.L, mcs, cores)
+        ref = cpu_reference(model, args.L, args.cpu_mcs or 300, cores)
         line = {"metric": "spin updates/ns", "value": ref["value"], "unit": "spin updates/ns",
                 "impl": "reference", "n_gpus": args.gpus, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
@@ -322,21 +395,12 @@ def main():
         print(json.dumps(line))
         return 0
 
-    res = run_gpu(model, args.L, replicas, args.steps, args.warmup, rank, world, args.variant)
+    res = run_sweeps(model, args.L, replicas, args.steps, args.warmup, rank, world, args.variant)
     if rank != 0:
         return 0
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except (OSError, ValueError):
-        pass
-    peak = peaks.get("hbm_gbs")
-    peak_src = "measured" if peak else "fallback"
-    peak = peak or 6800.0
     traffic = None
     try:
-        prof = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
-        traffic = prof.get(args.model)
+        traffic = json.load(open(os.path.join(ROOT, "profiles", "traffic.json"))).get(args.model)
     except (OSError, ValueError):
         pass
     line = {
@@ -345,22 +409,38 @@ def main():
         "ms_per_step": res["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u8" if model == 0 else "f32", "data": "synthetic",
         "config": config,
-        "roofline": {"bound": "hbm", "achieved": res["achieved_gbs"], "peak": peak,
-                     "unit": "GB/s", "frac": res["achieved_gbs"] / peak,
+        "roofline": {"bound": "hbm", "achieved": res["achieved_gbs"], "peak": hbm_peak,
+                     "unit": "GB/s", "frac": res["achieved_gbs"] / hbm_peak,
                      "peak_source": peak_src, "traffic": traffic,
-                     "kernel": "ising_sc_kernel<16> (one colour phase)" if model == 0
-                     else "xyz_sc_kernel (one colour phase)",
-                     "bytes_per_update": res["bytes_per_update"],
-                     "phase_ms": res["phase_ms"], "autotuned_variant": res["variant"]},
+                     "kernel": ("ising_sc_kernel (one colour phase)" if model == 0
+                                else "xyz_sc_kernel (one colour phase)"),
+                     "bytes_per_update": res["bytes_per_update"], "phase_ms": res["phase_ms"],
+                     "autotuned_variant": res["variant"]},
         "e2e": {"value": res["e2e"], "unit": "spin updates/ns",
                 "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"]},
         "gpu_launches": res["launches"],
         "clocks": res["clocks"],
         "accept_ratio": res["accept_mean"],
     }
+    if not args.no_components and model == eg.MODEL_ISING:
+        comp = {}
+        h = run_sweeps(eg.MODEL_XYZ, args.L, 64, 300, 5, rank, 1, clocks=False, e2e=False)
+        comp["heisenberg_sweep"] = {
+            "workload": "simple-cubic %d^3 Heisenberg float4 at kT_c=1.443 J, 64 replicas" % args.L,
+            "value": h["value"], "unit": "spin updates/ns",
+            "roofline": {"bound": "hbm", "achieved": h["achieved_gbs"], "peak": hbm_peak,
+                         "unit": "GB/s", "frac": h["achieved_gbs"] / hbm_peak,
+                         "bytes_per_update": BYTES_HEIS}}
+        s = run_sq(cells=args.sq_cells)
+        comp["structure_factor"] = dict(s, roofline={
+            "bound": "tensor", "achieved": s["tensor_tflops"], "peak": bf16_peak,
+            "unit": "TFLOP/s", "frac": s["tensor_tflops"] / bf16_peak,
+            "note": "BF16 hi/lo split: 3 tensor products per useful product"})
+        comp["tau"] = run_tau(args.L)
+        line["components"] = comp
     if not args.no_cpu:
-        mcs = args.cpu_mcs or 300
-        line["cpu_baseline"] = {k: v for k, v in cpu_reference(model, args.L, mcs, cores).items()
+        line["cpu_baseline"] = {k: v for k, v in
+                                cpu_reference(model, args.L, args.cpu_mcs or 300, cores).items()
                                 if k in ("value", "unit", "cores", "kind", "sample")}
     print(json.dumps(line))
     return 0

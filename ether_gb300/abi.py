@@ -91,6 +91,7 @@ SIGNATURES = {
     "ether_parallel_tempering": (C.c_int, [P, C.c_int32, PI32]),
     "ether_get_slots": (C.c_int, [P, PI32]),
     "ether_mcs": (C.c_int, [P, C.POINTER(Schedule), C.c_int32, C.c_int32, PI32]),
+    "ether_record_series": (C.c_int, [P, C.c_int32, C.c_int32, PD, PD]),
     "ether_get_accept_counts": (C.c_int, [P, PU64]),
     "ether_reset_accept_counts": (C.c_int, [P]),
     "ether_get_info": (C.c_int, [P, C.POINTER(Info)]),

@@ -989,6 +989,44 @@ extern "C" int ether_set_variant(ether_ctx *h, int32_t variant) {
     return ETHER_OK;
 }
 
+// Time series for autocorrelation analysis: nsweeps Metropolis sweeps, and after every
+// stride-th sweep |M| (get_tot_magnetisation) and optionally E (get_tot_energy) of every
+// replica.  absM, E: (nsweeps / stride) x R host arrays (E may be NULL).
+extern "C" int ether_record_series(ether_ctx *h, int32_t nsweeps, int32_t stride, double *absM,
+                                   double *E) {
+    if (!h || !absM) return fail(ETHER_ERR_ARG, "null argument");
+    Ctx &c = h->c;
+    if (nsweeps <= 0 || stride <= 0 || nsweeps / stride <= 0)
+        return fail(ETHER_ERR_ARG, "need nsweeps >= stride >= 1");
+    if (!c.beta_set) return fail(ETHER_ERR_STATE, "beta not set");
+    const int nrec = nsweeps / stride;
+    double *mser = nullptr, *eser = nullptr;
+    const size_t bytes = sizeof(double) * (size_t)nrec * c.R;
+    CUDA_TRY(cudaMalloc(&mser, bytes));
+    if (E && cudaMalloc(&eser, bytes) != cudaSuccess) {
+        cudaFree(mser);
+        return fail(ETHER_ERR_NOMEM, "cudaMalloc of the energy series failed");
+    }
+    int rc = ETHER_OK;
+    int t = 0;
+    for (int k = 1; k <= nsweeps && rc == ETHER_OK; ++k) {
+        rc = sweep_once(c);
+        if (rc == ETHER_OK && k % stride == 0 && t < nrec) {
+            cudaError_t e = launch_record(c, t++, E != nullptr, mser, eser);
+            if (e != cudaSuccess) rc = fail(ETHER_ERR_CUDA, std::string("record: ") + cudaGetErrorString(e));
+        }
+    }
+    if (rc == ETHER_OK) {
+        cudaError_t e = cudaMemcpyAsync(absM, mser, bytes, cudaMemcpyDeviceToHost, c.stream);
+        if (e == cudaSuccess && E) e = cudaMemcpyAsync(E, eser, bytes, cudaMemcpyDeviceToHost, c.stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+        if (e != cudaSuccess) rc = fail(ETHER_ERR_CUDA, std::string("series copy: ") + cudaGetErrorString(e));
+    }
+    cudaFree(mser);
+    if (eser) cudaFree(eser);
+    return rc;
+}
+
 // structure_factor (utility/Structure_Factor/structure_factor.f90:99-183) on the tensor cores;
 // see k_sq.cu.  Positions become fractional coordinates of the cell abc (rows = a1, a2, a3).
 extern "C" int ether_structure_factor(ether_ctx *h, const double *abc, const int32_t nq[3],

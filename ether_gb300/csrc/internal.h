@@ -111,6 +111,7 @@ cudaError_t launch_fresh(Ctx &c);
 cudaError_t launch_advance(Ctx &c, uint32_t *counter);
 cudaError_t launch_energy_mag(Ctx &c, bool want_energy);
 cudaError_t launch_measure(Ctx &c);
+cudaError_t launch_record(Ctx &c, int t, bool want_e, double *mser, double *eser);
 cudaError_t launch_pt(Ctx &c, int set_swap_count);
 int energy_blocks(const Ctx &c);
 void set_error(const std::string &msg);

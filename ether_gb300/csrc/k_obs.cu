@@ -211,6 +211,79 @@ cudaError_t launch_energy_mag(Ctx &c, bool) {
     return cudaGetLastError();
 }
 
+// Magnetisation only (src/get_tot_magnetisation.f90:32-40), no neighbour reads: per-block
+// partial sums of w_s S_s into partials[(r*nblk + b)*kNq + 2..4].
+__global__ void __launch_bounds__(kRedBs)
+mag_kernel(const uint8_t *__restrict__ spins, const float4 *__restrict__ spins4, int N, int model,
+           const double *__restrict__ mweight, double *__restrict__ partials) {
+    const int r = blockIdx.y;
+    double q[3] = {0, 0, 0};
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += gridDim.x * blockDim.x) {
+        const double w = mweight[s];
+        if (model == 0) {
+            q[2] += w * (spins[(size_t)r * N + s] ? 1.0 : -1.0);
+        } else {
+            const float4 S = spins4[(size_t)r * N + s];
+            q[0] += w * (double)S.x;
+            q[1] += w * (double)S.y;
+            q[2] += w * (double)S.z;
+        }
+    }
+    __shared__ double sm[kRedBs / 32][3];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        double v = warp_sum_d(q[j]);
+        if (lane == 0) sm[wid][j] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double v = 0.0;
+        for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2) v += sm[w2][threadIdx.x];
+        partials[((size_t)r * gridDim.x + blockIdx.x) * kNq + 2 + threadIdx.x] = v;
+    }
+}
+
+// One row t of the time series: |M| (and E) of every replica.  from_partials: M is summed
+// here from mag_kernel's partials (in block order); otherwise M and E come from the last
+// energy / magnetisation reduction.
+__global__ void record_kernel(const double *__restrict__ partials, int nblk, int R,
+                              int from_partials, double *__restrict__ M,
+                              const double *__restrict__ E, double *__restrict__ mser,
+                              double *__restrict__ eser, int t) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    double m[3];
+    if (from_partials) {
+        m[0] = m[1] = m[2] = 0.0;
+        for (int b = 0; b < nblk; ++b)
+            for (int j = 0; j < 3; ++j) m[j] += partials[((size_t)r * nblk + b) * kNq + 2 + j];
+        for (int j = 0; j < 3; ++j) M[3 * r + j] = m[j];
+    } else {
+        for (int j = 0; j < 3; ++j) m[j] = M[3 * r + j];
+    }
+    mser[(size_t)t * R + r] = sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+    if (eser) eser[(size_t)t * R + r] = E[r];
+}
+
+cudaError_t launch_record(Ctx &c, int t, bool want_e, double *mser, double *eser) {
+    if (want_e) {
+        cudaError_t e = launch_energy_mag(c, true);
+        if (e != cudaSuccess) return e;
+        record_kernel<<<(c.R + 127) / 128, 128, 0, c.stream>>>(c.partials, c.partial_blocks, c.R, 0,
+                                                                c.M, c.E, mser, eser, t);
+        c.launches++;
+    } else {
+        dim3 grid(c.partial_blocks, c.R);
+        mag_kernel<<<grid, kRedBs, 0, c.stream>>>(c.spins, c.spins4, c.N, c.model, c.t.mweight,
+                                                  c.partials);
+        record_kernel<<<(c.R + 127) / 128, 128, 0, c.stream>>>(c.partials, c.partial_blocks, c.R, 1,
+                                                                c.M, c.E, mser, nullptr, t);
+        c.launches += 2;
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t launch_measure(Ctx &c) {
     measure_kernel<<<(c.R + 127) / 128, 128, 0, c.stream>>>(c.E, c.M, c.N, c.R, c.n_slots,
                                                             c.slot_of_rep, c.sums);

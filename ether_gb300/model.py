@@ -259,6 +259,15 @@ class Sweep:
         abi.check(self.lib.ether_mcs(self.h, C.byref(s), step0, nsteps, C.byref(sc)))
         return sc.value
 
+    def record_series(self, nsweeps, stride=1, energy=False):
+        """nsweeps sweeps; |M| (and E) of every replica after each stride-th sweep.
+        Returns arrays of shape (R, nsweeps // stride)."""
+        n = nsweeps // stride
+        m = np.zeros((n, self.R), dtype=np.float64)
+        e = np.zeros((n, self.R), dtype=np.float64) if energy else None
+        abi.check(self.lib.ether_record_series(self.h, nsweeps, stride, abi.dptr(m), abi.dptr(e)))
+        return (m.T.copy(), e.T.copy()) if energy else m.T.copy()
+
     def accept_counts(self):
         out = np.zeros(self.R, dtype=np.uint64)
         abi.check(self.lib.ether_get_accept_counts(self.h, out.ctypes.data_as(abi.PU64)))

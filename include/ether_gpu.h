@@ -179,6 +179,12 @@ typedef struct ether_schedule {
 int ether_mcs(ether_ctx *ctx, const ether_schedule *sch, int32_t step0, int32_t nsteps,
               int32_t *swap_count);
 
+/* Time series for the integrated autocorrelation time: nsweeps Metropolis sweeps; after
+ * every stride-th sweep |M| (get_tot_magnetisation, src/get_tot_magnetisation.f90:32-40) and,
+ * if E is not NULL, the raw energy (get_tot_energy) of every replica.  absM(R, nsweeps/stride)
+ * and E(R, nsweeps/stride) are host arrays, record-major (index = t*R + r). */
+int ether_record_series(ether_ctx *ctx, int32_t nsweeps, int32_t stride, double *absM, double *E);
+
 /* Acceptance counters (accepted site updates per replica since the last reset). */
 int ether_get_accept_counts(ether_ctx *ctx, uint64_t *counts);
 int ether_reset_accept_counts(ether_ctx *ctx);

@@ -162,3 +162,32 @@ def test_statistical_parity_with_reference_order_run():
     z = np.abs(mean - ref_mean) / np.sqrt(err ** 2 + ref_err ** 2)
     assert np.all(np.isfinite(z))
     assert (z > 2.0).sum() <= 4 and (z > 4.0).sum() == 0, z
+
+
+@pytest.mark.parametrize("model", [eg.MODEL_ISING, eg.MODEL_XYZ])
+def test_record_series_equals_step_by_step(model):
+    lat = eg.simple_cubic(16)
+    runs = []
+    for way in ("series", "steps"):
+        sw, _ = make_pair(lat, model, FM, replicas=3)
+        sw.set_beta([beta_of(k) for k in (4.0, 4.5, 5.0)] if model == eg.MODEL_ISING else
+                    [beta_of(k) for k in (1.2, 1.4, 1.6)])
+        sw.set_streams(stream=[1, 2, 3], step=[0, 0, 0])
+        sw.set_spins(random_ising(lat, 6) if model == eg.MODEL_ISING else random_xyz(lat, 6))
+        if way == "series":
+            m, e = sw.record_series(24, stride=4, energy=True)
+            m2 = sw.record_series(8, stride=2)  # magnetisation-only path
+        else:
+            m = np.zeros((3, 6)); e = np.zeros((3, 6)); m2 = np.zeros((3, 4))
+            for t in range(6):
+                sw.metropolis(4, accept=False)
+                e[:, t] = sw.tot_energy()
+                m[:, t] = np.linalg.norm(sw.tot_magnetisation(), axis=1)
+            for t in range(4):
+                sw.metropolis(2, accept=False)
+                m2[:, t] = np.linalg.norm(sw.tot_magnetisation(), axis=1)
+        runs.append((m, e, m2))
+    (a, b, c), (x, y, z) = runs
+    np.testing.assert_allclose(a, x, rtol=1e-12)
+    np.testing.assert_allclose(b, y, rtol=1e-12)
+    np.testing.assert_allclose(c, z, rtol=1e-12)
