@@ -400,7 +400,8 @@ def main():
         return 0
     traffic = None
     try:
-        traffic = json.load(open(os.path.join(ROOT, "profiles", "traffic.json"))).get(args.model)
+        traffic = (json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+                   .get(args.model) or {}).get("bytes_per_launch")
     except (OSError, ValueError):
         pass
     line = {
