@@ -54,6 +54,30 @@ ETHER_HD U4 draw(uint32_t c0, uint32_t t, uint32_t stream, uint32_t tag, uint32_
     return philox(c0, t, stream, tag, seed, kKey1);
 }
 
+// The ten round keys of the first key word, (seed + r * 0x9E3779B9).  Passed to the hottest
+// kernel as a by-value parameter, so each round XORs with a constant-bank operand instead of
+// recomputing the schedule per thread; the second key word's schedule is a compile-time
+// constant.  Same numbers as draw().
+struct RoundKeys {
+    uint32_t k[10];
+};
+inline RoundKeys round_keys(uint32_t seed) {
+    RoundKeys K;
+    for (int r = 0; r < 10; ++r) K.k[r] = seed + (uint32_t)r * 0x9E3779B9u;
+    return K;
+}
+ETHER_HD U4 draw_rk(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, const RoundKeys &K) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        const uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ K.k[r];
+        const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ (kKey1 + (uint32_t)r * 0xBB67AE85u);
+        c0 = n0; c1 = (uint32_t)p1; c2 = n2; c3 = (uint32_t)p0;
+    }
+    return U4{c0, c1, c2, c3};
+}
+
 // u32 -> [0,1) with 24 bits, and u32 -> [-1,1) with 24 bits (both exact in FP32).
 ETHER_HD float u01(uint32_t u) { return (float)(u >> 8) * 0x1p-24f; }
 ETHER_HD float upm1(uint32_t u) { return (float)(u >> 8) * 0x1p-23f - 1.0f; }

@@ -1,0 +1,214 @@
+// sweep_ising.cuh -- device bodies of the Ising Metropolis colour phase
+// (src/Metropolis.f90:39-62 with the Ising branch of update_spin_details.f90:34-35 and
+// Hamiltonian.f90:34-52), shared by the per-context kernels (k_ising.cu) and the persistent
+// batch kernel (k_batch.cu).
+//
+// Decision: a site flips iff its uniform u32 u <= T, T = max(ceil(2^32 p), 1) - 1 with
+// p = exp(-β ΔE) -- the reference's -βΔE > log(η) for η = u 2^-32, η = 0 included.  T comes
+// from a per-temperature table indexed by (site type, own spin, up-neighbour counts per
+// (shell, neighbour species) group), built in FP64 on the host.
+//
+// Random numbers: the sites of a colour class are taken in groups of eight (rank >> 3).
+// Site k of a group owns halfword k of two Philox blocks: block 0 gives the high 16 bits
+// of its u, block 1 the low 16 bits.  Since u <= T  <=>  uh < Th  or  (uh == Th and
+// ul <= Tl), block 1 is only evaluated when a high half ties (probability 2^-16): one
+// Philox call serves eight site updates, and the decision is still the exact 32-bit one.
+#pragma once
+#include "internal.h"
+#include "rng_math.cuh"
+
+namespace ether {
+
+__device__ __forceinline__ void warp_add_count(unsigned long long *dst, unsigned v) {
+    unsigned s = __reduce_add_sync(0xffffffffu, v);
+    if ((threadIdx.x & 31) == 0 && s) atomicAdd(dst, (unsigned long long)s);
+}
+
+__device__ __forceinline__ uint32_t half_of(const U4 &b, int k) {  // halfword k = 0..7
+    const uint32_t w = (k >> 1) == 0 ? b.x : (k >> 1) == 1 ? b.y : (k >> 1) == 2 ? b.z : b.w;
+    return (k & 1) ? (w >> 16) : (w & 0xFFFFu);
+}
+
+// ------------------------------------------------------------------ general lattice ----
+// One group of eight consecutive sites (ranks 8g .. 8g+7) of colour class `colour`.
+struct IsingCsr {
+    uint8_t *sp;  // this replica's spins
+    int col_off, n_c;
+    const int32_t *row_ptr, *nbr, *wstride;
+    const uint16_t *itype;
+    const int32_t *type_base, *type_half;
+    const uint32_t *tb;  // this replica's temperature slot's thresholds
+};
+__device__ __forceinline__ unsigned ising_csr_group(const IsingCsr &A, int g, uint32_t t,
+                                                    uint32_t stream, uint32_t c3, uint32_t seed) {
+    unsigned acc = 0;
+    const U4 hi = draw((uint32_t)g, t, stream, c3, seed);
+    bool have_lo = false;
+    U4 lo{0, 0, 0, 0};
+    for (int k = 0; k < 8; ++k) {
+        const int rho = 8 * g + k;
+        if (rho >= A.n_c) break;
+        const int s = A.col_off + rho;
+        int idx = 0;
+        for (int q = A.row_ptr[s]; q < A.row_ptr[s + 1]; ++q) idx += A.wstride[q] * (int)A.sp[A.nbr[q]];
+        const int own = A.sp[s];
+        const int ty = A.itype[s];
+        const uint32_t T = A.tb[A.type_base[ty] + own * A.type_half[ty] + idx];
+        const uint32_t uh = half_of(hi, k), th = T >> 16;
+        bool flip = uh < th;
+        if (uh == th) {
+            if (!have_lo) {
+                lo = draw((uint32_t)g, t, stream, c3 | (1u << 16), seed);
+                have_lo = true;
+            }
+            flip = half_of(lo, k) <= (T & 0xFFFFu);
+        }
+        if (flip) {
+            A.sp[s] = (uint8_t)(own ^ 1);
+            ++acc;
+        }
+    }
+    return acc;
+}
+
+// ------------------------------------------------------- simple cubic, colour-split ----
+// Colour c array: rho = (z*L2 + y)*H + xh, H = L1/2, site x = 2*xh + ((y+z+c)&1).
+// All six neighbours live in the other colour's array: same xh in rows (y±1,z), (y,z±1),
+// and xh, xh∓1 in row (y,z).  A thread takes W (8 or 16) consecutive bytes of one row
+// (W | H), i.e. one or two random-number groups.  Byte sums of 0/1 spins never carry
+// (max 6); e = n + 7 s (<= 13) is formed for four sites at once; flips are one predicated
+// XOR per site and are counted with popc.
+template <int W>
+struct Vec {
+    uint32_t w[W / 4];
+};
+
+template <int W>
+__device__ __forceinline__ Vec<W> ldv(const uint8_t *p) {
+    Vec<W> v;
+    if constexpr (W == 8) {
+        uint2 q = *reinterpret_cast<const uint2 *>(p);
+        v.w[0] = q.x; v.w[1] = q.y;
+    } else {
+        uint4 q = *reinterpret_cast<const uint4 *>(p);
+        v.w[0] = q.x; v.w[1] = q.y; v.w[2] = q.z; v.w[3] = q.w;
+    }
+    return v;
+}
+template <int W>
+__device__ __forceinline__ void stv(uint8_t *p, const Vec<W> &v) {
+    if constexpr (W == 8) {
+        *reinterpret_cast<uint2 *>(p) = make_uint2(v.w[0], v.w[1]);
+    } else {
+        *reinterpret_cast<uint4 *>(p) = make_uint4(v.w[0], v.w[1], v.w[2], v.w[3]);
+    }
+}
+
+// Sites of word q whose high random halves tie with the threshold's high half: decided by
+// the low halves (block 1 of the group).  Returns the XOR mask of the extra flips.  Kept
+// out of line: it runs for about one word in 16000 and must not cost the hot loop registers.
+__device__ __noinline__ inline uint32_t resolve_ties(uint32_t grp, uint32_t t, uint32_t stream,
+                                                     uint32_t c3, uint32_t seed, int odd,
+                                                     uint32_t tie, uint32_t e4s,
+                                                     const uint32_t *s_tl) {
+    const U4 rl = draw(grp, t, stream, c3 | (1u << 16), seed);
+    const uint32_t la = odd ? rl.z : rl.x, lb = odd ? rl.w : rl.y;
+    const uint32_t l[4] = {la & 0xFFFFu, la >> 16, lb & 0xFFFFu, lb >> 16};
+    uint32_t m = 0;
+    for (int k = 0; k < 4; ++k)
+        if (((tie >> k) & 1u) && l[k] <= s_tl[((e4s >> (8 * k)) & 0xFFu) >> 2]) m |= 1u << (8 * k);
+    return m;
+}
+
+struct IsingSc {
+    uint8_t *own_a;       // this replica's array of the updated colour
+    const uint8_t *opp;   // ... and of the other colour
+    int L1, L2, L3, H;
+    FastDiv fH, fL2;
+    uint32_t colour;
+};
+
+// VPT vectors of W bytes per thread, vector indices vfirst + j*vstride (j < VPT, < nvec),
+// one after another.  s_th / s_tl: the 14 thresholds' high / low halves in shared memory.
+// Returns the number of flips.
+template <int W, int VPT>
+__device__ __forceinline__ unsigned ising_sc_vectors(const IsingSc &A, int vfirst, int vstride,
+                                                     int nvec, const uint32_t *s_th,
+                                                     const uint32_t *s_tl, uint32_t t,
+                                                     uint32_t stream, uint32_t c3, uint32_t seed,
+                                                     const RoundKeys &K) {
+    static_assert(W == 8 || W == 16, "vector of one or two random-number groups");
+    constexpr int NW = W / 4;
+    const char *th_bytes = reinterpret_cast<const char *>(s_th);
+    const int H = A.H, L2 = A.L2, L3 = A.L3;
+    unsigned flips = 0;
+#pragma unroll
+    for (int j = 0; j < VPT; ++j) {
+        const int v = vfirst + j * vstride;
+        if (v >= nvec) break;
+        const int rho0 = v * W;
+        const int row = (int)fdiv((uint32_t)rho0, A.fH);
+        const int xh0 = rho0 - row * H;
+        const int z = (int)fdiv((uint32_t)row, A.fL2);
+        const int y = row - z * L2;
+        const int par = (y + z + (int)A.colour) & 1;
+        const int ym = (y == 0 ? L2 - 1 : y - 1), yp = (y == L2 - 1 ? 0 : y + 1);
+        const int zm = (z == 0 ? L3 - 1 : z - 1), zp = (z == L3 - 1 ? 0 : z + 1);
+        Vec<W> me = ldv<W>(A.own_a + rho0);
+        const Vec<W> o0 = ldv<W>(A.opp + rho0);
+        const Vec<W> a = ldv<W>(A.opp + (z * L2 + ym) * H + xh0);
+        const Vec<W> b = ldv<W>(A.opp + (z * L2 + yp) * H + xh0);
+        const Vec<W> c = ldv<W>(A.opp + (zm * L2 + y) * H + xh0);
+        const Vec<W> d = ldv<W>(A.opp + (zp * L2 + y) * H + xh0);
+        const uint32_t edge = par == 0 ? A.opp[row * H + (xh0 == 0 ? H - 1 : xh0 - 1)]
+                                       : A.opp[row * H + (xh0 + W == H ? 0 : xh0 + W)];
+        U4 rh{0, 0, 0, 0};
+#pragma unroll
+        for (int q = 0; q < NW; ++q) {
+            const uint32_t grp = (uint32_t)((rho0 >> 3) + (q >> 1));
+            if ((q & 1) == 0) rh = draw_rk(grp, t, stream, c3, K);
+            uint32_t sh;
+            if (par == 0) {  // neighbour x-1 -> xh-1: window shifted up by one byte
+                const uint32_t lo = (q == 0) ? (edge << 24) : o0.w[q - 1];
+                sh = __funnelshift_l(lo, o0.w[q], 8);
+            } else {         // neighbour x+1 -> xh+1: window shifted down by one byte
+                const uint32_t hi = (q == NW - 1) ? edge : o0.w[q + 1];
+                sh = __funnelshift_r(o0.w[q], hi, 8);
+            }
+            const uint32_t s0 = me.w[q];
+            const uint32_t n = o0.w[q] + sh + a.w[q] + b.w[q] + c.w[q] + d.w[q];
+            // bytewise 4*(n + 7 s) <= 52: the byte offsets of the thresholds in s_th
+            const uint32_t e4s = (n + (s0 << 3) - s0) << 2;
+            const uint32_t t0 = *reinterpret_cast<const uint32_t *>(th_bytes + (e4s & 0xFFu));
+            const uint32_t t1 = *reinterpret_cast<const uint32_t *>(th_bytes + __byte_perm(e4s, 0, 0x4441));
+            const uint32_t t2 = *reinterpret_cast<const uint32_t *>(th_bytes + __byte_perm(e4s, 0, 0x4442));
+            const uint32_t t3 = *reinterpret_cast<const uint32_t *>(th_bytes + (e4s >> 24));
+            const uint32_t wa = (q & 1) ? rh.z : rh.x, wb = (q & 1) ? rh.w : rh.y;
+            const uint32_t u0 = wa & 0xFFFFu, u1 = wa >> 16, u2 = wb & 0xFFFFu, u3 = wb >> 16;
+            uint32_t out = s0;
+            if (u0 < t0) out ^= 0x00000001u;
+            if (u1 < t1) out ^= 0x00000100u;
+            if (u2 < t2) out ^= 0x00010000u;
+            if (u3 < t3) out ^= 0x01000000u;
+            const uint32_t tie = (u0 == t0 ? 1u : 0u) | (u1 == t1 ? 2u : 0u) |
+                                 (u2 == t2 ? 4u : 0u) | (u3 == t3 ? 8u : 0u);
+            if (tie) out ^= resolve_ties(grp, t, stream, c3, seed, q & 1, tie, e4s, s_tl);
+            flips += __popc(out ^ s0);
+            me.w[q] = out;
+        }
+        stv<W>(A.own_a + rho0, me);
+    }
+    return flips;
+}
+
+// Loads a replica's 14 simple-cubic thresholds into shared memory (all threads call it).
+__device__ __forceinline__ void load_sc_thresholds(const uint32_t *thr, uint32_t *s_th,
+                                                   uint32_t *s_tl) {
+    if (threadIdx.x < 14) {
+        const uint32_t T = thr[threadIdx.x];
+        s_th[threadIdx.x] = T >> 16;
+        s_tl[threadIdx.x] = T & 0xFFFFu;
+    }
+}
+
+}  // namespace ether
