@@ -271,6 +271,119 @@ def run_tau(L=64, replicas=128, equil=20000, sweeps=100000, stride=10):
             "independent_samples_per_s": replicas * sweeps_per_s / (2.0 * tau_sweeps)}
 
 
+BATCH_SIZES = (8, 12, 16, 24, 32, 48)
+
+
+def make_batch_members(chains=256, ladder=32, seed=1992, grouped=True):
+    """Mixed batch: `chains` chains with L drawn uniformly from BATCH_SIZES, half Ising and
+    half Heisenberg, J = +-1 meV per chain, a `ladder`-temperature geometric ladder each
+    (0.6 .. 1.6 T_c).  grouped: chains with the same (model, L, J) share one context, one
+    ladder group per chain; else one context per chain."""
+    import ether_gb300 as eg
+    rng = np.random.default_rng(seed)
+    groups = {}
+    keys = []
+    for c in range(chains):
+        model = eg.MODEL_ISING if c < chains // 2 else eg.MODEL_XYZ
+        key = (model, int(rng.choice(BATCH_SIZES)), int(rng.choice([-1, 1])))
+        groups[key] = groups.get(key, 0) + 1
+        keys.append(key)
+    items = sorted(groups.items()) if grouped else [(k, 1) for k in keys]
+    members = []
+    for k, ((model, L, sign), n) in enumerate(items):
+        lat = eg.simple_cubic(L)
+        j = eg.couplings(1, [[(1, 1, (sign * J_MEV,) * 3)]], [1.0])
+        sw = eg.Sweep.from_lattice(lat, j, np.array([1.0]), model, replicas=ladder * n,
+                                   seed=seed + 101 * k)
+        ktc = KTC_ISING if model == eg.MODEL_ISING else KTC_HEIS
+        kT = ktc * np.geomspace(0.6, 1.6, ladder)
+        sw.set_ladder(1.0 / (kT * J_MEV * 1e-3))
+        ion = lat.ion.copy()
+        if model == eg.MODEL_ISING:
+            ion[:, 3] = rng.choice([-1.0, 1.0], size=lat.N)
+        else:
+            v = rng.normal(size=(lat.N, 3))
+            ion[:, 1:4] = v / np.linalg.norm(v, axis=1, keepdims=True)
+        sw.set_spins(ion)
+        members.append(sw)
+    return members, groups
+
+
+def _time_batch(members, steps, warmup, config=None):
+    import ether_gb300 as eg
+    b = eg.Batch(members)
+    if config:
+        b.set_config(*config)
+        cfg = tuple(config)
+    else:
+        cfg, _ = b.autotune()
+    b.metropolis(warmup)
+    ev = Events(b.stream())
+    t0 = ev.record()
+    b.metropolis(steps)
+    t1 = ev.record()
+    ms = ev.ms(t0, t1)
+    info = b.info()
+    ev.free([t0, t1])
+    b.close()
+    return ms, info, cfg
+
+
+def _time_plain(members, steps, warmup):
+    for m in members:
+        m.metropolis(warmup, accept=False)
+    for m in members:
+        m.sync()
+    t = time.perf_counter()
+    for _ in range(steps):
+        for m in members:
+            m.metropolis(1, accept=False)
+    for m in members:
+        m.sync()
+    return time.perf_counter() - t
+
+
+def run_batch(steps=200, warmup=5, chains=256, ladder=32, config=None, forms=(False, True),
+              plain=True):
+    """The mixed batch advanced by ether_batch (one persistent kernel per colour phase, one
+    graph per sweep, autotuned tiles) and by each member's own sweeps (per-context kernels
+    on the members' streams), with one context per chain and with chains grouped by
+    (model, L, J)."""
+    import ether_gb300 as eg
+    out = {}
+    for grouped in forms:
+        t = time.perf_counter()
+        members, groups = make_batch_members(chains, ladder, grouped=grouped)
+        setup_s = time.perf_counter() - t
+        ms, info, cfg = _time_batch(members, steps, warmup, config)
+        updates = float(info.site_updates_per_sweep) * steps
+        n_ising = sum(m.N * m.R for m in members if m.model == eg.MODEL_ISING)
+        n_heis = sum(m.N * m.R for m in members if m.model == eg.MODEL_XYZ)
+        bytes_per_sweep = BYTES_ISING * n_ising + BYTES_HEIS * n_heis
+        plain_steps = max(5, steps // 4)
+        plain_s = _time_plain(members, plain_steps, warmup) if plain else float("nan")
+        res = {"contexts": len(members), "setup_s": setup_s,
+               "value": updates / (ms * 1e6), "ms_per_sweep": ms / steps,
+               "tile_config": list(cfg), "kernels_per_sweep": info.kernels_per_sweep,
+               "segments": info.n_segments, "grid": info.grid,
+               "achieved_gbs": bytes_per_sweep / (ms / steps * 1e-3) / 1e9,
+               "plain_value": float(info.site_updates_per_sweep) * plain_steps / (plain_s * 1e9),
+               "plain_kernels_per_sweep": 3 * len(members)}
+        res["speedup_vs_plain"] = res["value"] / res["plain_value"]
+        out["grouped" if grouped else "per_chain"] = res
+        for m in members:
+            m.close()
+    pc = out["per_chain"] if "per_chain" in out else out["grouped"]
+    return {"workload": "%d chains, L ~ U%s, %d Ising + %d Heisenberg, J = +-1 meV, %d-T "
+                        "geometric ladder (0.6-1.6 T_c) each: %d replicas, %.3g spins"
+                        % (chains, list(BATCH_SIZES), chains // 2, chains - chains // 2, ladder,
+                           info.n_replicas, info.site_updates_per_sweep),
+            "value": pc["value"], "unit": "spin updates/ns", "achieved_gbs": pc["achieved_gbs"],
+            "plain_note": "plain = each context's own ether_metropolis per sweep on its own "
+                          "stream (wall clock, host-synchronised)",
+            **out}
+
+
 def cpu_reference(model, L, mcs, threads, seed=1992):
     """The oracle's typewriter restatement of the reference's per-MCS work (Metropolis
     + get_tot_energy), one replica (temperature) per thread."""
@@ -330,7 +443,7 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--model", default="ising", choices=["ising", "heisenberg", "sq"])
+    ap.add_argument("--model", default="ising", choices=["ising", "heisenberg", "sq", "batch"])
     ap.add_argument("--L", type=int, default=64)
     ap.add_argument("--replicas", type=int, default=0)
     ap.add_argument("--cpu-mcs", type=int, default=0)
@@ -338,6 +451,9 @@ def main():
     ap.add_argument("--no-components", action="store_true")
     ap.add_argument("--variant", type=int, default=0)
     ap.add_argument("--sq-cells", type=int, default=12)
+    ap.add_argument("--chains", type=int, default=256)
+    ap.add_argument("--batch-config", default="",
+                    help="threads,units_per_thread,blocks_per_sm,walk (default: autotune)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -364,6 +480,16 @@ def main():
                           "roofline": {"bound": "tensor", "achieved": r["tensor_tflops"],
                                        "peak": bf16_peak, "unit": "TFLOP/s",
                                        "frac": r["tensor_tflops"] / bf16_peak}}))
+        return 0
+
+    if args.model == "batch":
+        if rank != 0:
+            return 0
+        cfg = [int(x) for x in args.batch_config.split(",")] if args.batch_config else None
+        r = run_batch(steps=min(args.steps, 500), warmup=args.warmup, chains=args.chains,
+                      config=cfg, forms=(False,) if cfg else (False, True), plain=not cfg)
+        print(json.dumps({"metric": "spin updates/ns", "value": r["value"],
+                          "unit": "spin updates/ns", "higher_is_better": True, "detail": r}))
         return 0
 
     model = eg.MODEL_ISING if args.model == "ising" else eg.MODEL_XYZ
@@ -437,6 +563,11 @@ def main():
             "bound": "tensor", "achieved": s["tensor_tflops"], "peak": bf16_peak,
             "unit": "TFLOP/s", "frac": s["tensor_tflops"] / bf16_peak,
             "note": "BF16 hi/lo split: 3 tensor products per useful product"})
+        bt = run_batch()
+        bt["roofline"] = {"bound": "hbm", "achieved": bt.pop("achieved_gbs"), "peak": hbm_peak,
+                          "unit": "GB/s", "note": "3 B per Ising and 48 B per Heisenberg update"}
+        bt["roofline"]["frac"] = bt["roofline"]["achieved"] / hbm_peak
+        comp["batch"] = bt
         comp["tau"] = run_tau(args.L)
         line["components"] = comp
     if not args.no_cpu:

@@ -61,6 +61,17 @@ class Info(C.Structure):
     ]
 
 
+class BatchInfo(C.Structure):
+    _fields_ = [
+        ("n_members", C.c_int32), ("n_replicas", C.c_int32), ("threads", C.c_int32),
+        ("units_per_thread", C.c_int32), ("blocks_per_sm", C.c_int32), ("grid", C.c_int32),
+        ("walk", C.c_int32),
+        ("n_segments", C.c_int32), ("kernels_per_sweep", C.c_int32),
+        ("site_updates_per_sweep", C.c_int64), ("kernel_launches", C.c_uint64),
+        ("last_sweep_ms", C.c_float),
+    ]
+
+
 P = C.c_void_p
 PD = C.POINTER(C.c_double)
 PI32 = C.POINTER(C.c_int32)
@@ -103,6 +114,13 @@ SIGNATURES = {
     "ether_autotune": (C.c_int, [P, PI32, C.POINTER(C.c_float)]),
     "ether_set_variant": (C.c_int, [P, C.c_int32]),
     "ether_structure_factor": (C.c_int, [P, PD, PI32, PD, PD, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "ether_batch_create": (C.c_int, [C.POINTER(P), C.c_int32, C.POINTER(P)]),
+    "ether_batch_destroy": (C.c_int, [P]),
+    "ether_batch_metropolis": (C.c_int, [P, C.c_int32]),
+    "ether_batch_set_config": (C.c_int, [P, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
+    "ether_batch_autotune": (C.c_int, [P, PI32, C.POINTER(C.c_float)]),
+    "ether_batch_get_info": (C.c_int, [P, C.POINTER(BatchInfo)]),
+    "ether_batch_get_stream": (C.c_int, [P, C.POINTER(P)]),
     "ether_sc_energy_noalloc": (C.c_int, [C.c_int32, P, PI32, C.c_int32, PD, PD, PD, PD, P]),
     "ether_build_lattice": (C.c_int, [C.c_int32, PD, PI32, PD, PI32, C.c_char_p, C.c_int32,
                                       C.c_int32, PD, C.c_double, C.c_int32, PD, PD, PI32]),

@@ -18,10 +18,6 @@
 
 using namespace ether;
 
-struct ether_ctx {
-    Ctx c;
-};
-
 static thread_local std::string g_err;
 
 static int fail(int code, const std::string &msg) {
@@ -392,6 +388,7 @@ extern "C" int ether_create(const ether_desc *d, ether_ctx **out) {
     CUDA_TRY(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
     int rc = ETHER_OK;
 #define TRY(x) do { rc = (x); if (rc) return bail(rc); } while (0)
+    c.nnz = (long)nbr.size();
     TRY(dev_upload(c, &c.t.row_ptr, row_ptr));
     TRY(dev_upload(c, &c.t.nbr, nbr));
     TRY(dev_upload(c, &c.t.jidx, jidx));

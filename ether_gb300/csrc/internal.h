@@ -53,6 +53,7 @@ struct Ctx {
     // colouring
     int ncol = 0;
     int col_off[kMaxColours + 1] = {0};
+    long nnz = 0;  // neighbour-list entries (CSR)
     std::vector<int32_t> colour, rank, storage;  // per site (0-based index)
     std::vector<int32_t> site_of_storage;
     // fast simple-cubic path
@@ -119,6 +120,11 @@ int structure_factor_launch(Ctx &c, const double *frac, const int nq[3], const d
                             const double dq[3], float *sq_host, float *comp_host, std::string &msg);
 
 }  // namespace ether
+
+// The opaque handle of the C-ABI.
+struct ether_ctx {
+    ether::Ctx c;
+};
 
 namespace ether {
 // Division by a loop-invariant divisor d >= 1 for 0 <= n < 2^31, by multiply and shift

@@ -1,0 +1,668 @@
+// k_batch.cu -- batched Metropolis sweeps over many contexts (ether_batch_* in the C-ABI).
+//
+// The reference advances one lattice at one temperature per MPI rank (src/ether.f90:112-118,
+// one Metropolis sweep at a time: src/Metropolis.f90:34-68).  A batch advances every replica
+// of every member context -- mixed lattice sizes, Ising and XYZ, each member with its own
+// temperature ladder -- with one persistent kernel per colour phase: a grid of (resident
+// blocks per SM x SMs) walks a table of segments (member, replica, first unit, units), each
+// segment a block-sized tile of one replica's colour class.  A unit is what one thread
+// updates at a time: a W-byte vector (simple-cubic Ising), a group of eight sites (general
+// Ising) or one site (XYZ).  The per-site arithmetic is the member kernels' own
+// (sweep_ising.cuh, sweep_xyz.cuh) with the same random-number counters, so a batch sweep
+// reproduces the members' own sweeps bit for bit.  One sweep (the phases and the sweep
+// counter advance) is captured once as a CUDA graph and replayed.
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "sweep_ising.cuh"
+#include "sweep_xyz.cuh"
+
+namespace ether {
+
+enum BatchKind : int32_t { kBIsing16 = 0, kBIsing8 = 1, kBIsingCsr = 2, kBXyzSc = 3, kBXyzCsr = 4 };
+
+// Everything a segment needs from its member; copied into shared memory when a block moves
+// to another member.  Plain data (no initialisers): it lives in __shared__.
+struct BatchMember {
+    int32_t kind, N, L1, L2, L3, H;
+    FastDiv fH, fL2;
+    uint8_t *spins;
+    float4 *spins4;
+    const uint32_t *thr;
+    int32_t table_entries, pad0;
+    const int32_t *row_ptr, *nbr, *wstride, *type_base, *type_half;
+    const uint16_t *itype, *jidx;
+    const float *J;
+    XyzParams P;
+    float jx, jy, jz;
+    uint32_t seed;
+    RoundKeys K;
+    const float *beta_slot_f;
+    const int32_t *slot_of_rep;
+    const uint32_t *stream_id, *step;
+    unsigned long long *acc_count;
+    int32_t col_off[kMaxColours + 1];
+};
+static_assert(sizeof(BatchMember) % 4 == 0, "word copy");
+
+struct BatchSeg {
+    uint32_t member, rep, first, count;
+};
+
+// Two walks over the segments.  Strided (block_first == nullptr): block b takes segments
+// b, b + gridDim.x, ...; the resident blocks sweep through memory together, so the
+// neighbour planes one tile reads are the planes its neighbours' tiles read at the same time
+// (L2 hits).  Contiguous: block b takes [block_first[b], block_first[b+1]), runs balanced by
+// an estimated cost per unit, so member and replica change rarely.  No block barriers: the
+// Ising thresholds live in a per-warp slot of shared memory.
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB)
+batch_phase_kernel(const BatchMember *__restrict__ members, const BatchSeg *__restrict__ segs,
+                   const int32_t *__restrict__ block_first, int n_seg, uint32_t colour, int upt) {
+    // Per-warp copies of the current member's parameters and Ising thresholds: a warp moves
+    // to another member or replica without waiting for the rest of the block, and the
+    // parameters cost no registers.
+    __shared__ BatchMember s_m[8];
+    __shared__ uint32_t s_th[8][16], s_tl[8][16];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    BatchMember &m = s_m[warp];
+    uint32_t cur_member = 0xFFFFFFFFu, cur_rep = 0xFFFFFFFFu;
+    const uint32_t c3 = kMetro | (colour << 8);
+    const bool strided = block_first == nullptr;
+    const int s_end = strided ? n_seg : block_first[blockIdx.x + 1];
+    const int s_step = strided ? (int)gridDim.x : 1;
+    for (int sg = strided ? (int)blockIdx.x : block_first[blockIdx.x]; sg < s_end; sg += s_step) {
+        const BatchSeg S = segs[sg];
+        const uint32_t r = S.rep;
+        if (S.member != cur_member) {  // warp-uniform
+            __syncwarp();
+            const uint32_t *src = reinterpret_cast<const uint32_t *>(members + S.member);
+            uint32_t *dst = reinterpret_cast<uint32_t *>(&m);
+            for (int i = lane; i < (int)(sizeof(BatchMember) / 4); i += 32) dst[i] = src[i];
+            __syncwarp();
+        }
+        const int kind = m.kind;
+        if ((kind == kBIsing16 || kind == kBIsing8) && (S.member != cur_member || r != cur_rep)) {
+            if (lane < 14) {
+                const uint32_t T = m.thr[(size_t)m.slot_of_rep[r] * m.table_entries + lane];
+                s_th[warp][lane] = T >> 16;
+                s_tl[warp][lane] = T & 0xFFFFu;
+            }
+            __syncwarp();
+        }
+        cur_member = S.member;
+        cur_rep = r;
+        const uint32_t t = m.step[r], stream = m.stream_id[r];
+        const int end = (int)(S.first + S.count);
+        unsigned acc = 0;
+        if (kind == kBIsing16 || kind == kBIsing8) {
+            const int half = m.H * m.L2 * m.L3;
+            uint8_t *base = m.spins + (size_t)r * 2 * half;
+            const IsingSc A{base + (size_t)colour * half, base + (size_t)(colour ^ 1u) * half,
+                            m.L1, m.L2, m.L3, m.H, m.fH, m.fL2, colour};
+            for (int j = 0; j < upt; ++j) {
+                const int v = (int)S.first + (int)threadIdx.x + j * (int)blockDim.x;
+                if (kind == kBIsing16)
+                    acc += ising_sc_vectors<16, 1>(A, v, 0, end, s_th[warp], s_tl[warp], t, stream, c3, m.seed, m.K);
+                else
+                    acc += ising_sc_vectors<8, 1>(A, v, 0, end, s_th[warp], s_tl[warp], t, stream, c3, m.seed, m.K);
+            }
+        } else if (kind == kBIsingCsr) {
+            const int off = m.col_off[colour];
+            const IsingCsr A{m.spins + (size_t)r * m.N, off, m.col_off[colour + 1] - off, m.row_ptr,
+                             m.nbr, m.wstride, m.itype, m.type_base, m.type_half,
+                             m.thr + (size_t)m.slot_of_rep[r] * m.table_entries};
+            for (int g = (int)S.first + (int)threadIdx.x; g < end; g += blockDim.x)
+                acc += ising_csr_group(A, g, t, stream, c3, m.seed);
+        } else if (kind == kBXyzSc) {
+            const int half = m.H * m.L2 * m.L3;
+            float4 *base = m.spins4 + (size_t)r * 2 * half;
+            const XyzSc A{base + (size_t)colour * half, base + (size_t)(colour ^ 1u) * half,
+                          m.L1, m.L2, m.L3, m.H, m.fH, m.fL2, colour, m.jx, m.jy, m.jz};
+            const float beta_f = m.beta_slot_f[m.slot_of_rep[r]];
+            if (!m.P.zeeman && !m.P.sia && !m.P.angle) {
+                // exchange only, Marsaglia proposals: the options fold away at compile time
+                const XyzParams P0{0, 0, 0, 0.f, nullptr, nullptr, nullptr};
+                for (int rho = (int)S.first + (int)threadIdx.x; rho < end; rho += blockDim.x)
+                    acc += xyz_sc_site(A, P0, rho, beta_f, t, c3, m.seed, stream) ? 1u : 0u;
+            } else {
+                for (int rho = (int)S.first + (int)threadIdx.x; rho < end; rho += blockDim.x)
+                    acc += xyz_sc_site(A, m.P, rho, beta_f, t, c3, m.seed, stream) ? 1u : 0u;
+            }
+        } else {  // kBXyzCsr
+            float4 *sp = m.spins4 + (size_t)r * m.N;
+            const float beta_f = m.beta_slot_f[m.slot_of_rep[r]];
+            for (int rho = (int)S.first + (int)threadIdx.x; rho < end; rho += blockDim.x)
+                acc += xyz_csr_site(m.P, sp, m.col_off[colour], rho, m.row_ptr, m.nbr, m.jidx, m.J,
+                                    beta_f, t, c3, m.seed, stream) ? 1u : 0u;
+        }
+        warp_add_count(m.acc_count + r, acc);
+    }
+}
+
+// Ends a batch sweep: every replica's Metropolis sweep counter advances by one.
+__global__ void batch_advance_kernel(uint32_t *const *__restrict__ step_of, int total) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < total) *step_of[i] += 1u;
+}
+
+}  // namespace ether
+
+using namespace ether;
+
+struct ether_batch {
+    std::vector<ether_ctx *> members;
+    cudaStream_t stream = nullptr;
+    std::vector<cudaEvent_t> ev_member;
+    cudaEvent_t ev_done = nullptr, ev_t0 = nullptr, ev_t1 = nullptr;
+    std::vector<BatchMember> h_members;
+    BatchMember *d_members = nullptr;
+    BatchSeg *d_segs = nullptr;
+    size_t seg_capacity = 0;
+    std::vector<int> seg_off, seg_cnt;  // per colour phase
+    std::vector<int> bf_off, bf_grid;   // per colour phase: block ranges in d_block_first
+    int32_t *d_block_first = nullptr;
+    size_t bf_capacity = 0;
+    float xyz_cost = 20.f;              // estimated cost of an XYZ site, Ising site = 1
+    int minb = 1;                       // register cap: 1 = none, 4 = four 256-thread blocks
+    bool contiguous = false;            // segment walk (see batch_phase_kernel)
+    uint32_t **d_step_of = nullptr;
+    int total_R = 0, max_col = 0;
+    int threads = 256, upt = 2, bps = 0;  // bps 0: as many as fit
+    int grid = 0, sm_count = 0;
+    long long updates_per_sweep = 0;
+    cudaGraphExec_t graph = nullptr;
+    bool dirty = true;
+    uint64_t launches = 0;
+    float last_ms = 0.f;
+    int timed_sweeps = 0;  // sweeps between ev_t0 and ev_t1 not yet read
+};
+
+namespace {
+
+int bfail(int code, const std::string &msg) {
+    set_error(msg);
+    return code;
+}
+
+#define BCUDA(expr)                                                                          \
+    do {                                                                                     \
+        cudaError_t _e = (expr);                                                             \
+        if (_e != cudaSuccess)                                                               \
+            return bfail(_e == cudaErrorMemoryAllocation ? ETHER_ERR_NOMEM : ETHER_ERR_CUDA,  \
+                         std::string(#expr) + ": " + cudaGetErrorString(_e));                \
+    } while (0)
+
+BatchMember describe(const Ctx &c) {
+    BatchMember m;
+    std::memset(&m, 0, sizeof(m));
+    if (c.model == ETHER_MODEL_ISING)
+        m.kind = !c.fast ? kBIsingCsr : (c.vec_bytes == 16 ? kBIsing16 : kBIsing8);
+    else
+        m.kind = c.fast ? kBXyzSc : kBXyzCsr;
+    m.N = c.N;
+    m.L1 = c.L[0];
+    m.L2 = c.L[1];
+    m.L3 = c.L[2];
+    m.H = c.L[0] / 2;
+    if (c.fast) {
+        m.fH = make_fastdiv((uint32_t)m.H);
+        m.fL2 = make_fastdiv((uint32_t)m.L2);
+    }
+    m.spins = c.spins;
+    m.spins4 = c.spins4;
+    m.thr = c.thr;
+    m.table_entries = c.table_entries;
+    m.row_ptr = c.t.row_ptr;
+    m.nbr = c.t.nbr;
+    m.wstride = c.t.wstride;
+    m.type_base = c.t.type_base;
+    m.type_half = c.t.type_half;
+    m.itype = c.t.itype;
+    m.jidx = c.t.jidx;
+    m.J = c.t.J;
+    m.P.zeeman = c.zeeman;
+    m.P.sia = c.sia;
+    m.P.angle = c.angle;
+    m.P.dphi = (float)c.dphi;
+    m.P.species = c.t.species;
+    m.P.zee = c.t.zee;
+    m.P.D = c.t.D;
+    if (!c.h_Jf.empty()) {
+        m.jx = c.h_Jf[0];
+        m.jy = c.h_Jf[1];
+        m.jz = c.h_Jf[2];
+    }
+    m.seed = c.seed;
+    m.K = round_keys(c.seed);
+    m.beta_slot_f = c.beta_slot_f;
+    m.slot_of_rep = c.slot_of_rep;
+    m.stream_id = c.stream_id;
+    m.step = c.step;
+    m.acc_count = c.acc_count;
+    for (int k = 0; k <= c.ncol && k <= kMaxColours; ++k) m.col_off[k] = c.col_off[k];
+    return m;
+}
+
+// Units of one replica's colour class: vectors, groups of eight or sites.
+long units_of(const BatchMember &m, const Ctx &c, int colour) {
+    if (colour >= c.ncol) return 0;
+    const long n_c = c.col_off[colour + 1] - c.col_off[colour];
+    switch (m.kind) {
+        case kBIsing16: return n_c / 16;
+        case kBIsing8: return n_c / 8;
+        case kBIsingCsr: return (n_c + 7) / 8;
+        default: return n_c;
+    }
+}
+
+int rebuild(ether_batch &b) {
+    std::vector<BatchMember> hm;
+    hm.reserve(b.members.size());
+    for (ether_ctx *h : b.members) {
+        if (!h->c.beta_set) return bfail(ETHER_ERR_STATE, "batch member without beta (ether_set_beta / ether_set_ladder)");
+        hm.push_back(describe(h->c));
+    }
+    const bool same = hm.size() == b.h_members.size() &&
+                      std::memcmp(hm.data(), b.h_members.data(), hm.size() * sizeof(BatchMember)) == 0;
+    if (same && !b.dirty) return ETHER_OK;
+    if (b.graph) {
+        cudaGraphExecDestroy(b.graph);
+        b.graph = nullptr;
+    }
+    b.h_members = hm;
+    if (!b.d_members) BCUDA(cudaMalloc((void **)&b.d_members, hm.size() * sizeof(BatchMember)));
+    BCUDA(cudaMemcpyAsync(b.d_members, hm.data(), hm.size() * sizeof(BatchMember), cudaMemcpyHostToDevice, b.stream));
+    // segments: phase-major, member-major, replica, tile
+    b.max_col = 0;
+    for (ether_ctx *h : b.members) b.max_col = std::max(b.max_col, h->c.ncol);
+    std::vector<BatchSeg> segs;
+    b.seg_off.assign(b.max_col, 0);
+    b.seg_cnt.assign(b.max_col, 0);
+    b.updates_per_sweep = 0;
+    const long tile_units = (long)b.threads * b.upt;
+    for (int p = 0; p < b.max_col; ++p) {
+        b.seg_off[p] = (int)segs.size();
+        for (size_t k = 0; k < b.members.size(); ++k) {
+            const Ctx &c = b.members[k]->c;
+            const long u = units_of(hm[k], c, p);
+            if (u == 0) continue;
+            for (int r = 0; r < c.R; ++r)
+                for (long f = 0; f < u; f += tile_units)
+                    segs.push_back(BatchSeg{(uint32_t)k, (uint32_t)r, (uint32_t)f,
+                                            (uint32_t)std::min(tile_units, u - f)});
+            if (p < c.ncol) b.updates_per_sweep += (long long)(c.col_off[p + 1] - c.col_off[p]) * c.R;
+        }
+        b.seg_cnt[p] = (int)segs.size() - b.seg_off[p];
+    }
+    if (segs.size() > b.seg_capacity) {
+        if (b.d_segs) cudaFree(b.d_segs);
+        b.d_segs = nullptr;
+        BCUDA(cudaMalloc((void **)&b.d_segs, std::max<size_t>(1, segs.size()) * sizeof(BatchSeg)));
+        b.seg_capacity = segs.size();
+    }
+    if (!segs.empty())
+        BCUDA(cudaMemcpyAsync(b.d_segs, segs.data(), segs.size() * sizeof(BatchSeg), cudaMemcpyHostToDevice, b.stream));
+    // grid: resident blocks per SM x SMs
+    int occ = 0;
+    BCUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &occ, b.minb == 4 ? batch_phase_kernel<4> : batch_phase_kernel<1>, b.threads, 0));
+    if (occ < 1) occ = 1;
+    const int bps = b.bps > 0 ? std::min(b.bps, occ) : occ;
+    b.grid = bps * b.sm_count;
+    // per phase: contiguous segment runs of about equal estimated cost, one per block
+    std::vector<double> unit_cost(b.members.size());
+    for (size_t k = 0; k < b.members.size(); ++k) {
+        const Ctx &c = b.members[k]->c;
+        const double deg = c.N > 0 ? (double)c.nnz / c.N / 6.0 : 1.0;
+        switch (hm[k].kind) {
+            case kBIsing16: unit_cost[k] = 16.0; break;
+            case kBIsing8: unit_cost[k] = 9.0; break;
+            case kBIsingCsr: unit_cost[k] = 20.0 * deg; break;
+            case kBXyzSc: unit_cost[k] = b.xyz_cost; break;
+            default: unit_cost[k] = 1.3 * b.xyz_cost * deg; break;
+        }
+    }
+    std::vector<int32_t> bf;
+    b.bf_off.assign(b.max_col, 0);
+    b.bf_grid.assign(b.max_col, 0);
+    for (int p = 0; p < b.max_col; ++p) {
+        const int n = b.seg_cnt[p];
+        const int G = std::max(1, std::min(b.grid, n));
+        b.bf_off[p] = (int)bf.size();
+        b.bf_grid[p] = n > 0 ? G : 0;
+        std::vector<double> cum(n + 1, 0.0);
+        for (int i = 0; i < n; ++i) {
+            const BatchSeg &S = segs[b.seg_off[p] + i];
+            cum[i + 1] = cum[i] + unit_cost[S.member] * S.count;
+        }
+        int i = 0;
+        for (int blk = 0; blk <= G; ++blk) {
+            const double target = cum[n] * blk / G;
+            while (i < n && cum[i] < target) ++i;
+            bf.push_back(blk == G ? n : i);
+        }
+    }
+    if (bf.size() > b.bf_capacity) {
+        if (b.d_block_first) cudaFree(b.d_block_first);
+        b.d_block_first = nullptr;
+        BCUDA(cudaMalloc((void **)&b.d_block_first, bf.size() * sizeof(int32_t)));
+        b.bf_capacity = bf.size();
+    }
+    if (!bf.empty())
+        BCUDA(cudaMemcpyAsync(b.d_block_first, bf.data(), bf.size() * sizeof(int32_t), cudaMemcpyHostToDevice, b.stream));
+    BCUDA(cudaStreamSynchronize(b.stream));  // host vectors above go out of scope
+    b.dirty = false;
+    return ETHER_OK;
+}
+
+int issue_sweep(ether_batch &b) {
+    for (int p = 0; p < b.max_col; ++p) {
+        if (b.seg_cnt[p] == 0) continue;
+        const int32_t *bf = b.contiguous ? b.d_block_first + b.bf_off[p] : nullptr;
+        if (b.minb == 4)
+            batch_phase_kernel<4><<<b.bf_grid[p], b.threads, 0, b.stream>>>(
+                b.d_members, b.d_segs + b.seg_off[p], bf, b.seg_cnt[p], (uint32_t)p, b.upt);
+        else
+            batch_phase_kernel<1><<<b.bf_grid[p], b.threads, 0, b.stream>>>(
+                b.d_members, b.d_segs + b.seg_off[p], bf, b.seg_cnt[p], (uint32_t)p, b.upt);
+        BCUDA(cudaGetLastError());
+    }
+    batch_advance_kernel<<<(b.total_R + 255) / 256, 256, 0, b.stream>>>(b.d_step_of, b.total_R);
+    BCUDA(cudaGetLastError());
+    return ETHER_OK;
+}
+
+int kernels_per_sweep(const ether_batch &b) {
+    int n = 1;
+    for (int p = 0; p < b.max_col; ++p) n += b.seg_cnt[p] > 0 ? 1 : 0;
+    return n;
+}
+
+int capture(ether_batch &b) {
+    if (b.graph) return ETHER_OK;
+    cudaGraph_t g = nullptr;
+    BCUDA(cudaStreamBeginCapture(b.stream, cudaStreamCaptureModeThreadLocal));
+    int rc = issue_sweep(b);
+    cudaError_t e = cudaStreamEndCapture(b.stream, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return bfail(ETHER_ERR_CUDA, std::string("batch graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&b.graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return bfail(ETHER_ERR_CUDA, std::string("batch graph instantiate: ") + cudaGetErrorString(e));
+    return ETHER_OK;
+}
+
+// The batch stream waits for everything queued on the members' streams.
+int join_members(ether_batch &b) {
+    for (size_t k = 0; k < b.members.size(); ++k) {
+        BCUDA(cudaEventRecord(b.ev_member[k], b.members[k]->c.stream));
+        BCUDA(cudaStreamWaitEvent(b.stream, b.ev_member[k], 0));
+    }
+    return ETHER_OK;
+}
+// ... and later work on the members' streams waits for the batch.
+int release_members(ether_batch &b) {
+    BCUDA(cudaEventRecord(b.ev_done, b.stream));
+    for (ether_ctx *h : b.members) BCUDA(cudaStreamWaitEvent(h->c.stream, b.ev_done, 0));
+    return ETHER_OK;
+}
+
+int run_sweeps(ether_batch &b, int nsweeps, bool timed) {
+    int rc = rebuild(b);
+    if (rc) return rc;
+    rc = capture(b);
+    if (rc) return rc;
+    if (timed) BCUDA(cudaEventRecord(b.ev_t0, b.stream));
+    for (int s = 0; s < nsweeps; ++s) BCUDA(cudaGraphLaunch(b.graph, b.stream));
+    if (timed) BCUDA(cudaEventRecord(b.ev_t1, b.stream));
+    b.launches += (uint64_t)nsweeps * kernels_per_sweep(b);
+    return ETHER_OK;
+}
+
+}  // namespace
+
+extern "C" int ether_batch_create(ether_ctx *const *members, int32_t n_members, ether_batch **out) {
+    if (!out) return bfail(ETHER_ERR_ARG, "null output handle");
+    *out = nullptr;
+    if (!members || n_members < 1) return bfail(ETHER_ERR_ARG, "a batch needs at least one member");
+    std::vector<ether_ctx *> mem(members, members + n_members);
+    for (int i = 0; i < n_members; ++i) {
+        if (!mem[i]) return bfail(ETHER_ERR_ARG, "null member context");
+        for (int j = 0; j < i; ++j)
+            if (mem[j] == mem[i]) return bfail(ETHER_ERR_ARG, "a context appears twice in the batch");
+    }
+    ether_batch *b = new ether_batch();
+    b->members = mem;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    b->ev_member.assign(mem.size(), nullptr);
+    for (size_t k = 0; e == cudaSuccess && k < mem.size(); ++k)
+        e = cudaEventCreateWithFlags(&b->ev_member[k], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev_t0);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev_t1);
+    std::vector<uint32_t *> step_of;
+    for (ether_ctx *h : mem)
+        for (int r = 0; r < h->c.R; ++r) step_of.push_back(h->c.step + r);
+    b->total_R = (int)step_of.size();
+    if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_step_of, step_of.size() * sizeof(uint32_t *));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b->d_step_of, step_of.data(), step_of.size() * sizeof(uint32_t *), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        ether_batch_destroy(b);
+        return bfail(ETHER_ERR_CUDA, std::string("batch set-up: ") + cudaGetErrorString(e));
+    }
+    *out = b;
+    return ETHER_OK;
+}
+
+extern "C" int ether_batch_destroy(ether_batch *b) {
+    if (!b) return ETHER_OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    for (cudaEvent_t ev : b->ev_member)
+        if (ev) cudaEventDestroy(ev);
+    if (b->ev_done) cudaEventDestroy(b->ev_done);
+    if (b->ev_t0) cudaEventDestroy(b->ev_t0);
+    if (b->ev_t1) cudaEventDestroy(b->ev_t1);
+    if (b->d_members) cudaFree(b->d_members);
+    if (b->d_segs) cudaFree(b->d_segs);
+    if (b->d_step_of) cudaFree(b->d_step_of);
+    if (b->d_block_first) cudaFree(b->d_block_first);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return ETHER_OK;
+}
+
+extern "C" int ether_batch_metropolis(ether_batch *b, int32_t nsweeps) {
+    if (!b) return bfail(ETHER_ERR_ARG, "null batch");
+    if (nsweeps < 0) return bfail(ETHER_ERR_ARG, "negative sweep count");
+    if (nsweeps == 0) return ETHER_OK;
+    int rc = join_members(*b);
+    if (rc) return rc;
+    rc = run_sweeps(*b, nsweeps, true);
+    if (rc) return rc;
+    b->timed_sweeps = nsweeps;
+    return release_members(*b);
+}
+
+extern "C" int ether_batch_set_config(ether_batch *b, int32_t threads, int32_t units_per_thread,
+                                      int32_t blocks_per_sm, int32_t walk) {
+    if (!b) return bfail(ETHER_ERR_ARG, "null batch");
+    if (!(threads == 64 || threads == 128 || threads == 256))
+        return bfail(ETHER_ERR_ARG, "threads per block must be 64, 128 or 256");
+    if (units_per_thread < 1 || units_per_thread > 64) return bfail(ETHER_ERR_ARG, "units per thread out of [1, 64]");
+    if (blocks_per_sm < 0 || blocks_per_sm > 32) return bfail(ETHER_ERR_ARG, "blocks per SM out of [0, 32]");
+    if (walk != 0 && walk != 1) return bfail(ETHER_ERR_ARG, "walk must be 0 (strided) or 1 (contiguous)");
+    b->contiguous = walk == 1;
+    b->threads = threads;
+    b->upt = units_per_thread;
+    b->bps = blocks_per_sm;
+    b->dirty = true;
+    return ETHER_OK;
+}
+
+extern "C" int ether_batch_autotune(ether_batch *b, int32_t *config, float *best_ms) {
+    if (!b) return bfail(ETHER_ERR_ARG, "null batch");
+    int rc = join_members(*b);
+    if (rc) return rc;
+    // back up every member's spins, sweep counters and acceptance counters
+    struct Saved {
+        void *src;
+        size_t bytes;
+        size_t off;
+    };
+    std::vector<Saved> sv;
+    size_t total = 0;
+    for (ether_ctx *h : b->members) {
+        const Ctx &c = h->c;
+        const size_t sb = c.model == ETHER_MODEL_ISING ? (size_t)c.R * c.N : (size_t)c.R * c.N * sizeof(float4);
+        void *sp = c.model == ETHER_MODEL_ISING ? (void *)c.spins : (void *)c.spins4;
+        for (auto [p, n] : {std::pair<void *, size_t>{sp, sb}, {(void *)c.step, c.R * sizeof(uint32_t)},
+                            {(void *)c.acc_count, c.R * sizeof(unsigned long long)}}) {
+            sv.push_back(Saved{p, n, total});
+            total += (n + 255) / 256 * 256;
+        }
+    }
+    char *backup = nullptr;
+    BCUDA(cudaMalloc((void **)&backup, std::max<size_t>(total, 1)));
+    for (const Saved &s : sv) BCUDA(cudaMemcpyAsync(backup + s.off, s.src, s.bytes, cudaMemcpyDeviceToDevice, b->stream));
+    const int old_t = b->threads, old_u = b->upt, old_b = b->bps;
+    b->timed_sweeps = 0;
+    int occ_max = 1;
+    float best = 1e30f;
+    int bt = old_t, bu = old_u, bb = old_b;
+    rc = ETHER_OK;
+    const int old_minb = b->minb;
+    int bm = old_minb;
+    for (int cand = 0; cand < 4 && !rc; ++cand) {
+        const int minb = cand < 2 ? 1 : 4, threads = (cand & 1) ? 256 : 128;
+        int occ = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &occ, minb == 4 ? batch_phase_kernel<4> : batch_phase_kernel<1>, threads, 0) != cudaSuccess)
+            occ = 1;
+        occ_max = std::max(occ, 1);
+        for (int upt : {1, 2, 4, 8, 16}) {
+            for (int bps : {occ_max, std::max(1, occ_max / 2)}) {
+                b->minb = minb;
+                b->contiguous = false;
+                b->threads = threads;
+                b->upt = upt;
+                b->bps = bps;
+                b->dirty = true;
+                rc = run_sweeps(*b, 1, false);  // warm-up (also builds and captures)
+                if (!rc) rc = run_sweeps(*b, 2, true);
+                if (rc) break;
+                float ms = 0.f;
+                if (cudaEventSynchronize(b->ev_t1) != cudaSuccess ||
+                    cudaEventElapsedTime(&ms, b->ev_t0, b->ev_t1) != cudaSuccess) {
+                    rc = bfail(ETHER_ERR_CUDA, "batch autotune timing");
+                    break;
+                }
+                ms *= 0.5f;
+                if (ms < best) {
+                    best = ms;
+                    bt = threads;
+                    bu = upt;
+                    bb = bps;
+                    bm = minb;
+                }
+                if (occ_max == 1) break;
+            }
+            if (rc) break;
+        }
+        if (rc) break;
+    }
+    // then the cost model that splits the segment runs between blocks
+    const float old_cost = b->xyz_cost;
+    float bc = old_cost;
+    const bool old_contig = b->contiguous;
+    bool bcontig = false;
+    for (float cost : {8.f, 14.f, 20.f, 32.f, 48.f}) {
+        if (rc) break;
+        b->threads = bt;
+        b->upt = bu;
+        b->bps = bb;
+        b->minb = bm;
+        b->xyz_cost = cost;
+        b->contiguous = true;
+        b->dirty = true;
+        rc = run_sweeps(*b, 1, false);
+        if (!rc) rc = run_sweeps(*b, 2, true);
+        if (rc) break;
+        float ms = 0.f;
+        if (cudaEventSynchronize(b->ev_t1) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, b->ev_t0, b->ev_t1) != cudaSuccess) {
+            rc = bfail(ETHER_ERR_CUDA, "batch autotune timing");
+            break;
+        }
+        ms *= 0.5f;
+        if (ms < best) {
+            best = ms;
+            bc = cost;
+            bcontig = true;
+        }
+    }
+    for (const Saved &s : sv) cudaMemcpyAsync(s.src, backup + s.off, s.bytes, cudaMemcpyDeviceToDevice, b->stream);
+    cudaStreamSynchronize(b->stream);
+    cudaFree(backup);
+    b->threads = rc ? old_t : bt;
+    b->upt = rc ? old_u : bu;
+    b->bps = rc ? old_b : bb;
+    b->xyz_cost = rc ? old_cost : bc;
+    b->minb = rc ? old_minb : bm;
+    b->contiguous = rc ? old_contig : bcontig;
+    b->dirty = true;
+    if (rc) return rc;
+    int rr = release_members(*b);
+    if (rr) return rr;
+    if (config) {
+        config[0] = b->threads;
+        config[1] = b->upt;
+        config[2] = b->bps;
+        config[3] = b->contiguous ? 1 : 0;
+    }
+    if (best_ms) *best_ms = best;
+    return ETHER_OK;
+}
+
+extern "C" int ether_batch_get_info(ether_batch *b, ether_batch_info *info) {
+    if (!b || !info) return bfail(ETHER_ERR_ARG, "null argument");
+    int rc = rebuild(*b);
+    if (rc) return rc;
+    if (b->timed_sweeps > 0) {
+        float ms = 0.f;
+        BCUDA(cudaEventSynchronize(b->ev_t1));
+        BCUDA(cudaEventElapsedTime(&ms, b->ev_t0, b->ev_t1));
+        b->last_ms = ms / b->timed_sweeps;
+        b->timed_sweeps = 0;
+    }
+    info->n_members = (int32_t)b->members.size();
+    info->n_replicas = b->total_R;
+    info->threads = b->threads;
+    info->units_per_thread = b->upt;
+    info->blocks_per_sm = b->grid / std::max(1, b->sm_count);
+    info->grid = b->grid;
+    info->walk = b->contiguous ? 1 : 0;
+    info->n_segments = 0;
+    for (int n : b->seg_cnt) info->n_segments += n;
+    info->kernels_per_sweep = kernels_per_sweep(*b);
+    info->site_updates_per_sweep = b->updates_per_sweep;
+    info->kernel_launches = b->launches;
+    info->last_sweep_ms = b->last_ms;
+    return ETHER_OK;
+}
+
+extern "C" int ether_batch_get_stream(ether_batch *b, void **stream) {
+    if (!b || !stream) return bfail(ETHER_ERR_ARG, "null argument");
+    *stream = (void *)b->stream;
+    return ETHER_OK;
+}

@@ -1,74 +1,9 @@
-// k_xyz.cu -- Heisenberg (XYZ) colour phases: Metropolis (src/Metropolis.f90:39-62) with
-// update_spin_details (src/update_spin_details.f90:30-51) and Hamiltonian
-// (src/Hamiltonian.f90:34-143); overrelaxation (src/overrelaxation.f90:30-61 with
+// k_xyz.cu -- per-context launches of the Heisenberg (XYZ) colour phases (Metropolis bodies
+// in sweep_xyz.cuh); overrelaxation (src/overrelaxation.f90:30-61 with
 // get_ovrr_vec.f90:41-85); fresh_spins (src/fresh_spins.f90:31-38).
-//
-// FP32 throughout, compiled with --fmad=false; the local exchange field is one fmaf chain
-// per component over the neighbours in the reference's nn order (shells in order,
-// neighbours by increasing site number), so every kernel variant and the oracle's FP32
-// mirror round identically.
-#include "internal.h"
-#include "rng_math.cuh"
+#include "sweep_xyz.cuh"
 
 namespace ether {
-
-__device__ __forceinline__ void warp_add_count_x(unsigned long long *dst, unsigned v) {
-    unsigned s = __reduce_add_sync(0xffffffffu, v);
-    if ((threadIdx.x & 31) == 0 && s) atomicAdd(dst, (unsigned long long)s);
-}
-
-struct XyzParams {
-    int zeeman, sia, angle;
-    float dphi;
-    const uint8_t *species;
-    const float *zee;
-    const float *D;
-};
-
-// ΔE of src/Hamiltonian.f90 for S -> n given the exchange field h.
-__device__ __forceinline__ float delta_e(const XyzParams &P, int s, const float4 &S,
-                                         const Spin4 &n, float hx, float hy, float hz) {
-    float dx = n.x - S.x, dy = n.y - S.y, dz = n.z - S.z;
-    float e = dx * hx;
-    e = fmaf(dy, hy, e);
-    e = fmaf(dz, hz, e);
-    if (P.zeeman || P.sia) {
-        int si = P.species[s] - 1;
-        if (P.zeeman) {
-            const float *z = P.zee + 3 * si;
-            e = fmaf(dx, z[0], e);
-            e = fmaf(dy, z[1], e);
-            e = fmaf(dz, z[2], e);
-        }
-        if (P.sia) {
-            const float *D = P.D + 3 * si;
-            float qx = n.x * n.x - S.x * S.x;
-            float qy = n.y * n.y - S.y * S.y;
-            float qz = n.z * n.z - S.z * S.z;
-            e = fmaf(D[0], qx, e);
-            e = fmaf(D[1], qy, e);
-            e = fmaf(D[2], qz, e);
-        }
-    }
-    return e;
-}
-
-__device__ __forceinline__ bool metro_site(const XyzParams &P, float4 *sp, int s, uint32_t rho,
-                                           float hx, float hy, float hz, float beta_f,
-                                           uint32_t t, uint32_t c3, uint32_t seed, uint32_t stream) {
-    const float4 S = sp[s];
-    U4 b0 = draw(rho, t, stream, c3, seed);
-    float eta = u01(b0.x);
-    Spin4 n;
-    Spin4 So{S.x, S.y, S.z, S.w};
-    if (!propose(P.angle != 0, P.dphi, So, rho, t, stream, c3, seed, b0, &n)) return false;
-    float e = delta_e(P, s, S, n, hx, hy, hz);
-    // exp evaluated on every lane (no divergent short-circuit); e <= 0 accepts regardless
-    const float p = expf_neg(-(beta_f * fmaxf(e, 0.0f)));
-    bool acc = (e <= 0.0f) || (eta < p);
-    if (acc) sp[s] = make_float4(n.x, n.y, n.z, n.w);
-    return acc;
-}
 
 // ------------------------------------------------------------------ general lattice ----
 __global__ void __launch_bounds__(256)
@@ -84,69 +19,9 @@ xyz_csr_kernel(float4 *__restrict__ spins4, int N, int col_off, int n_c, uint32_
     const uint32_t k1 = stream_id[r], t = step[r];
     const uint32_t c3 = kMetro | (colour << 8);
     unsigned acc = 0;
-    for (int rho = blockIdx.x * blockDim.x + threadIdx.x; rho < n_c; rho += gridDim.x * blockDim.x) {
-        const int s = col_off + rho;
-        float hx = 0.f, hy = 0.f, hz = 0.f;
-        for (int k = row_ptr[s]; k < row_ptr[s + 1]; ++k) {
-            float4 Sj = sp[nbr[k]];
-            const float *Jp = J + 3 * jidx[k];
-            hx = fmaf(Jp[0], Sj.x, hx);
-            hy = fmaf(Jp[1], Sj.y, hy);
-            hz = fmaf(Jp[2], Sj.z, hz);
-        }
-        acc += metro_site(P, sp, s, (uint32_t)rho, hx, hy, hz, beta_f, t, c3, seed, k1) ? 1u : 0u;
-    }
+    for (int rho = blockIdx.x * blockDim.x + threadIdx.x; rho < n_c; rho += gridDim.x * blockDim.x)
+        acc += xyz_csr_site(P, sp, col_off, rho, row_ptr, nbr, jidx, J, beta_f, t, c3, seed, k1) ? 1u : 0u;
     warp_add_count_x(acc_count + r, acc);
-}
-
-// ------------------------------------------------------- simple cubic, colour-split ----
-// Neighbours are summed in increasing site-number order, which is the reference's nn
-// order: below-plane z neighbours, below-row y neighbours, the x pair, above-row y,
-// above-plane z.  At a periodic boundary a pair changes side (u=0: both above, in
-// order u+1, u-1; u=L-1: both below, in order u+1, u-1).
-struct Acc3 {
-    float x, y, z;
-};
-__device__ __forceinline__ void fma3(Acc3 &h, float jx, float jy, float jz, const float4 &S) {
-    h.x = fmaf(jx, S.x, h.x);
-    h.y = fmaf(jy, S.y, h.y);
-    h.z = fmaf(jz, S.z, h.z);
-}
-
-__device__ __forceinline__ Acc3 sc_field(const float4 *__restrict__ opp, int L1, int L2, int L3,
-                                         int H, int xh, int y, int z, int p, float jx, float jy,
-                                         float jz) {
-    const int row = z * L2 + y;
-    const int x = 2 * xh + p;
-    const int ym = (y == 0 ? L2 - 1 : y - 1), yp = (y == L2 - 1 ? 0 : y + 1);
-    const int zm = (z == 0 ? L3 - 1 : z - 1), zp = (z == L3 - 1 ? 0 : z + 1);
-    int xh_m, xh_p;
-    if (p == 0) { xh_m = (xh == 0 ? H - 1 : xh - 1); xh_p = xh; }
-    else { xh_m = xh; xh_p = (xh == H - 1 ? 0 : xh + 1); }
-    const float4 Sxm = opp[row * H + xh_m];
-    const float4 Sxp = opp[row * H + xh_p];
-    const float4 Sym = opp[(z * L2 + ym) * H + xh];
-    const float4 Syp = opp[(z * L2 + yp) * H + xh];
-    const float4 Szm = opp[(zm * L2 + y) * H + xh];
-    const float4 Szp = opp[(zp * L2 + y) * H + xh];
-    Acc3 h{0.f, 0.f, 0.f};
-    // below
-    if (z == L3 - 1) { fma3(h, jx, jy, jz, Szp); fma3(h, jx, jy, jz, Szm); }
-    else if (z != 0) fma3(h, jx, jy, jz, Szm);
-    if (y == L2 - 1) { fma3(h, jx, jy, jz, Syp); fma3(h, jx, jy, jz, Sym); }
-    else if (y != 0) fma3(h, jx, jy, jz, Sym);
-    // x pair in index order
-    const bool interior = (x != 0) && (x != L1 - 1);
-    const float4 xa = interior ? Sxm : Sxp;
-    const float4 xb = interior ? Sxp : Sxm;
-    fma3(h, jx, jy, jz, xa);
-    fma3(h, jx, jy, jz, xb);
-    // above
-    if (y == 0) { fma3(h, jx, jy, jz, Syp); fma3(h, jx, jy, jz, Sym); }
-    else if (y != L2 - 1) fma3(h, jx, jy, jz, Syp);
-    if (z == 0) { fma3(h, jx, jy, jz, Szp); fma3(h, jx, jy, jz, Szm); }
-    else if (z != L3 - 1) fma3(h, jx, jy, jz, Szp);
-    return h;
 }
 
 __global__ void __launch_bounds__(256)
@@ -159,20 +34,14 @@ xyz_sc_kernel(float4 *__restrict__ spins4, int L1, int L2, int L3, FastDiv fH, F
     const int H = L1 >> 1;
     const int half = H * L2 * L3;
     float4 *base = spins4 + (size_t)r * 2 * half;
-    float4 *own = base + (size_t)colour * half;
-    const float4 *opp = base + (size_t)(colour ^ 1u) * half;
+    const XyzSc A{base + (size_t)colour * half, base + (size_t)(colour ^ 1u) * half, L1, L2, L3, H,
+                  fH, fL2, colour, jx, jy, jz};
     const float beta_f = beta_slot_f[slot_of_rep[r]];
     const uint32_t k1 = stream_id[r], t = step[r];
     const uint32_t c3 = kMetro | (colour << 8);
     unsigned acc = 0;
-    for (int rho = blockIdx.x * blockDim.x + threadIdx.x; rho < half; rho += gridDim.x * blockDim.x) {
-        const int row = (int)fdiv((uint32_t)rho, fH);
-        const int xh = rho - row * H;
-        const int z = (int)fdiv((uint32_t)row, fL2), y = row - z * L2;
-        const int p = (y + z + (int)colour) & 1;
-        Acc3 h = sc_field(opp, L1, L2, L3, H, xh, y, z, p, jx, jy, jz);
-        acc += metro_site(P, own, rho, (uint32_t)rho, h.x, h.y, h.z, beta_f, t, c3, seed, k1) ? 1u : 0u;
-    }
+    for (int rho = blockIdx.x * blockDim.x + threadIdx.x; rho < half; rho += gridDim.x * blockDim.x)
+        acc += xyz_sc_site(A, P, rho, beta_f, t, c3, seed, k1) ? 1u : 0u;
     warp_add_count_x(acc_count + r, acc);
 }
 

@@ -61,7 +61,7 @@ ETHER_HD U4 draw(uint32_t c0, uint32_t t, uint32_t stream, uint32_t tag, uint32_
 struct RoundKeys {
     uint32_t k[10];
 };
-inline RoundKeys round_keys(uint32_t seed) {
+ETHER_HD RoundKeys round_keys(uint32_t seed) {
     RoundKeys K;
     for (int r = 0; r < 10; ++r) K.k[r] = seed + (uint32_t)r * 0x9E3779B9u;
     return K;

@@ -1,0 +1,163 @@
+// sweep_xyz.cuh -- device bodies of the Heisenberg (XYZ) Metropolis colour phase
+// (src/Metropolis.f90:39-62 with update_spin_details.f90:30-51 and Hamiltonian.f90:34-143),
+// shared by the per-context kernels (k_xyz.cu) and the persistent batch kernel (k_batch.cu).
+//
+// FP32 throughout, compiled with --fmad=false; the local exchange field is one fmaf chain
+// per component over the neighbours in the reference's nn order (shells in order,
+// neighbours by increasing site number), so every kernel variant and the oracle's FP32
+// mirror round identically.
+#pragma once
+#include "internal.h"
+#include "rng_math.cuh"
+
+namespace ether {
+
+__device__ __forceinline__ void warp_add_count_x(unsigned long long *dst, unsigned v) {
+    unsigned s = __reduce_add_sync(0xffffffffu, v);
+    if ((threadIdx.x & 31) == 0 && s) atomicAdd(dst, (unsigned long long)s);
+}
+
+struct XyzParams {
+    int zeeman, sia, angle;
+    float dphi;
+    const uint8_t *species;
+    const float *zee;
+    const float *D;
+};
+
+// ΔE of src/Hamiltonian.f90 for S -> n given the exchange field h.
+__device__ __forceinline__ float delta_e(const XyzParams &P, int s, const float4 &S,
+                                         const Spin4 &n, float hx, float hy, float hz) {
+    float dx = n.x - S.x, dy = n.y - S.y, dz = n.z - S.z;
+    float e = dx * hx;
+    e = fmaf(dy, hy, e);
+    e = fmaf(dz, hz, e);
+    if (P.zeeman || P.sia) {
+        int si = P.species[s] - 1;
+        if (P.zeeman) {
+            const float *z = P.zee + 3 * si;
+            e = fmaf(dx, z[0], e);
+            e = fmaf(dy, z[1], e);
+            e = fmaf(dz, z[2], e);
+        }
+        if (P.sia) {
+            const float *D = P.D + 3 * si;
+            float qx = n.x * n.x - S.x * S.x;
+            float qy = n.y * n.y - S.y * S.y;
+            float qz = n.z * n.z - S.z * S.z;
+            e = fmaf(D[0], qx, e);
+            e = fmaf(D[1], qy, e);
+            e = fmaf(D[2], qz, e);
+        }
+    }
+    return e;
+}
+
+__device__ __forceinline__ bool metro_site(const XyzParams &P, float4 *sp, int s, uint32_t rho,
+                                           float hx, float hy, float hz, float beta_f,
+                                           uint32_t t, uint32_t c3, uint32_t seed, uint32_t stream) {
+    const float4 S = sp[s];
+    U4 b0 = draw(rho, t, stream, c3, seed);
+    float eta = u01(b0.x);
+    Spin4 n;
+    Spin4 So{S.x, S.y, S.z, S.w};
+    if (!propose(P.angle != 0, P.dphi, So, rho, t, stream, c3, seed, b0, &n)) return false;
+    float e = delta_e(P, s, S, n, hx, hy, hz);
+    // exp evaluated on every lane (no divergent short-circuit); e <= 0 accepts regardless
+    const float p = expf_neg(-(beta_f * fmaxf(e, 0.0f)));
+    bool acc = (e <= 0.0f) || (eta < p);
+    if (acc) sp[s] = make_float4(n.x, n.y, n.z, n.w);
+    return acc;
+}
+
+// ------------------------------------------------------- simple cubic, colour-split ----
+// Neighbours are summed in increasing site-number order, which is the reference's nn
+// order: below-plane z neighbours, below-row y neighbours, the x pair, above-row y,
+// above-plane z.  At a periodic boundary a pair changes side (u=0: both above, in
+// order u+1, u-1; u=L-1: both below, in order u+1, u-1).
+struct Acc3 {
+    float x, y, z;
+};
+__device__ __forceinline__ void fma3(Acc3 &h, float jx, float jy, float jz, const float4 &S) {
+    h.x = fmaf(jx, S.x, h.x);
+    h.y = fmaf(jy, S.y, h.y);
+    h.z = fmaf(jz, S.z, h.z);
+}
+
+__device__ __forceinline__ Acc3 sc_field(const float4 *__restrict__ opp, int L1, int L2, int L3,
+                                         int H, int xh, int y, int z, int p, float jx, float jy,
+                                         float jz) {
+    const int row = z * L2 + y;
+    const int x = 2 * xh + p;
+    const int ym = (y == 0 ? L2 - 1 : y - 1), yp = (y == L2 - 1 ? 0 : y + 1);
+    const int zm = (z == 0 ? L3 - 1 : z - 1), zp = (z == L3 - 1 ? 0 : z + 1);
+    int xh_m, xh_p;
+    if (p == 0) { xh_m = (xh == 0 ? H - 1 : xh - 1); xh_p = xh; }
+    else { xh_m = xh; xh_p = (xh == H - 1 ? 0 : xh + 1); }
+    const float4 Sxm = opp[row * H + xh_m];
+    const float4 Sxp = opp[row * H + xh_p];
+    const float4 Sym = opp[(z * L2 + ym) * H + xh];
+    const float4 Syp = opp[(z * L2 + yp) * H + xh];
+    const float4 Szm = opp[(zm * L2 + y) * H + xh];
+    const float4 Szp = opp[(zp * L2 + y) * H + xh];
+    Acc3 h{0.f, 0.f, 0.f};
+    // below
+    if (z == L3 - 1) { fma3(h, jx, jy, jz, Szp); fma3(h, jx, jy, jz, Szm); }
+    else if (z != 0) fma3(h, jx, jy, jz, Szm);
+    if (y == L2 - 1) { fma3(h, jx, jy, jz, Syp); fma3(h, jx, jy, jz, Sym); }
+    else if (y != 0) fma3(h, jx, jy, jz, Sym);
+    // x pair in index order
+    const bool interior = (x != 0) && (x != L1 - 1);
+    const float4 xa = interior ? Sxm : Sxp;
+    const float4 xb = interior ? Sxp : Sxm;
+    fma3(h, jx, jy, jz, xa);
+    fma3(h, jx, jy, jz, xb);
+    // above
+    if (y == 0) { fma3(h, jx, jy, jz, Syp); fma3(h, jx, jy, jz, Sym); }
+    else if (y != L2 - 1) fma3(h, jx, jy, jz, Syp);
+    if (z == 0) { fma3(h, jx, jy, jz, Szp); fma3(h, jx, jy, jz, Szm); }
+    else if (z != L3 - 1) fma3(h, jx, jy, jz, Szp);
+    return h;
+}
+
+// One Metropolis update of rank rho of colour class `colour` on a general lattice.
+__device__ __forceinline__ bool xyz_csr_site(const XyzParams &P, float4 *sp, int col_off, int rho,
+                                             const int32_t *__restrict__ row_ptr,
+                                             const int32_t *__restrict__ nbr,
+                                             const uint16_t *__restrict__ jidx,
+                                             const float *__restrict__ J, float beta_f, uint32_t t,
+                                             uint32_t c3, uint32_t seed, uint32_t stream) {
+    const int s = col_off + rho;
+    float hx = 0.f, hy = 0.f, hz = 0.f;
+    for (int k = row_ptr[s]; k < row_ptr[s + 1]; ++k) {
+        float4 Sj = sp[nbr[k]];
+        const float *Jp = J + 3 * jidx[k];
+        hx = fmaf(Jp[0], Sj.x, hx);
+        hy = fmaf(Jp[1], Sj.y, hy);
+        hz = fmaf(Jp[2], Sj.z, hz);
+    }
+    return metro_site(P, sp, s, (uint32_t)rho, hx, hy, hz, beta_f, t, c3, seed, stream);
+}
+
+// One Metropolis update of rank rho of the simple-cubic colour array `own` (the other
+// colour's array is `opp`).
+struct XyzSc {
+    float4 *own;
+    const float4 *opp;
+    int L1, L2, L3, H;
+    FastDiv fH, fL2;
+    uint32_t colour;
+    float jx, jy, jz;
+};
+__device__ __forceinline__ bool xyz_sc_site(const XyzSc &A, const XyzParams &P, int rho,
+                                            float beta_f, uint32_t t, uint32_t c3, uint32_t seed,
+                                            uint32_t stream) {
+    const int row = (int)fdiv((uint32_t)rho, A.fH);
+    const int xh = rho - row * A.H;
+    const int z = (int)fdiv((uint32_t)row, A.fL2), y = row - z * A.L2;
+    const int p = (y + z + (int)A.colour) & 1;
+    Acc3 h = sc_field(A.opp, A.L1, A.L2, A.L3, A.H, xh, y, z, p, A.jx, A.jy, A.jz);
+    return metro_site(P, A.own, rho, (uint32_t)rho, h.x, h.y, h.z, beta_f, t, c3, seed, stream);
+}
+
+}  // namespace ether

@@ -306,3 +306,51 @@ class Sweep:
 
     def set_variant(self, variant):
         abi.check(self.lib.ether_set_variant(self.h, variant))
+
+
+class Batch:
+    """ether_batch: one persistent kernel per colour phase advances the Metropolis sweeps of
+    every member Sweep (mixed sizes and models), leaving each member exactly as its own
+    metropolis() would.  The members must outlive the batch."""
+
+    def __init__(self, members):
+        self.lib = abi.load()
+        self.members = list(members)
+        arr = (C.c_void_p * len(self.members))(*[m.h.value for m in self.members])
+        h_ = C.c_void_p()
+        abi.check(self.lib.ether_batch_create(arr, len(self.members), C.byref(h_)))
+        self.h = h_
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ether_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def metropolis(self, nsweeps=1):
+        abi.check(self.lib.ether_batch_metropolis(self.h, nsweeps))
+
+    def set_config(self, threads=256, units_per_thread=2, blocks_per_sm=0, walk=0):
+        abi.check(self.lib.ether_batch_set_config(self.h, threads, units_per_thread,
+                                                  blocks_per_sm, walk))
+
+    def autotune(self):
+        cfg = np.zeros(4, dtype=np.int32)
+        ms = C.c_float(0.0)
+        abi.check(self.lib.ether_batch_autotune(self.h, abi.iptr(cfg), C.byref(ms)))
+        return tuple(int(x) for x in cfg), ms.value
+
+    def info(self):
+        i = abi.BatchInfo()
+        abi.check(self.lib.ether_batch_get_info(self.h, C.byref(i)))
+        return i
+
+    def stream(self):
+        s = C.c_void_p()
+        abi.check(self.lib.ether_batch_get_stream(self.h, C.byref(s)))
+        return s.value or 0

@@ -234,6 +234,46 @@ int ether_set_variant(ether_ctx *ctx, int32_t variant);
 int ether_structure_factor(ether_ctx *ctx, const double *abc, const int32_t nq[3],
                            const double q0[3], const double dq[3], float *sq, float *comp);
 
+/* ------------------------------------------------------------------- batched sweeps ---- */
+/* The reference advances one lattice at one temperature per MPI rank (src/ether.f90:112-118,
+ * src/Metropolis.f90:34-68).  A batch advances the Metropolis sweeps of many contexts --
+ * different lattice sizes, Ising and XYZ, each with its own ladder and replicas -- with one
+ * persistent kernel per colour phase (grid = resident blocks per SM x SMs) over a table of
+ * block-sized tiles, one CUDA graph per sweep.  Spins, sweep counters, random streams and
+ * acceptance counters are the members' own: a batch sweep leaves every member exactly as
+ * ether_metropolis(member, 1) would.  Members are distinct contexts on the current device,
+ * each with beta set; they stay owned by the caller and must outlive the batch.  Batch work
+ * runs on the batch's stream, after all work already queued on the members' streams and
+ * before any work queued on them later. */
+typedef struct ether_batch ether_batch;
+int ether_batch_create(ether_ctx *const *members, int32_t n_members, ether_batch **batch);
+int ether_batch_destroy(ether_batch *batch);
+/* nsweeps Metropolis sweeps of every member (no overrelaxation, no PT: those stay per
+ * member).  Asynchronous; ether_batch_get_info reads the time it took. */
+int ether_batch_metropolis(ether_batch *batch, int32_t nsweeps);
+/* Tile shape: threads per block (64/128/256), units per thread (1..64; a unit is a 16- or
+ * 8-byte vector of simple-cubic Ising sites, a group of 8 general Ising sites, or one XYZ
+ * site), resident blocks per SM (0 = as many as fit) and the walk over the tiles (0: block
+ * b takes tiles b, b + grid, ...; 1: contiguous runs of equal estimated cost). */
+int ether_batch_set_config(ether_batch *batch, int32_t threads, int32_t units_per_thread,
+                           int32_t blocks_per_sm, int32_t walk);
+/* Autotuner: times the tile shapes, register caps and walks on the members' data (spins
+ * and counters are restored) and keeps the fastest.  config(4) = threads, units per thread,
+ * blocks per SM, walk; best_ms = one sweep.  Either output may be NULL. */
+int ether_batch_autotune(ether_batch *batch, int32_t *config, float *best_ms);
+typedef struct ether_batch_info {
+    int32_t n_members, n_replicas;
+    int32_t threads, units_per_thread, blocks_per_sm, grid, walk;
+    int32_t n_segments;        /* tiles per sweep, all colour phases                        */
+    int32_t kernels_per_sweep; /* colour phases + the counter advance                       */
+    int64_t site_updates_per_sweep;
+    uint64_t kernel_launches;  /* kernels launched by this batch so far                     */
+    float last_sweep_ms;       /* CUDA-event time per sweep of the last ether_batch_metropolis */
+} ether_batch_info;
+int ether_batch_get_info(ether_batch *batch, ether_batch_info *info);
+/* The cudaStream_t the batch launches on. */
+int ether_batch_get_stream(ether_batch *batch, void **stream);
+
 /* ------------------------------------------------------------- no-allocation energy ---- */
 /* No counterpart in the reference.  Energy and magnetisation of n_replicas simple-cubic
  * configurations already in device memory, for callers that cannot allocate device memory

@@ -1,0 +1,144 @@
+"""Batched sweeps (ether_batch_*): one persistent kernel per colour phase over many contexts
+leaves every member exactly as its own ether_metropolis would -- spins bit for bit and the
+acceptance counters -- for mixed sizes and models (simple-cubic Ising with 16- and 8-byte
+vectors, general Ising, simple-cubic XYZ, general XYZ and Ising on the pyrochlore lattice,
+whose colourings have more than two classes), for every tile shape and after the
+autotuner."""
+import numpy as np
+import pytest
+
+import ether_gb300 as eg
+from tests.helpers import beta_of, random_ising, random_xyz
+
+pytestmark = pytest.mark.gpu
+
+FM = [[(1, 1, (-1.0, -1.0, -1.0))]]
+AFM = [[(1, 1, (1.0, 1.0, 1.0))]]
+
+# (lattice, model, couplings, replicas, flags)
+SPECS = [
+    (lambda: eg.simple_cubic((32, 8, 6)), eg.MODEL_ISING, FM, 3, 0),       # 16-byte vectors
+    (lambda: eg.simple_cubic(16), eg.MODEL_ISING, AFM, 2, 0),              # 8-byte vectors
+    (lambda: eg.simple_cubic(12), eg.MODEL_ISING, FM, 2, 0),               # H = 6: general path
+    (lambda: eg.simple_cubic(8), eg.MODEL_ISING, FM, 2, eg.FLAG_FORCE_GENERAL),
+    (lambda: eg.pyrochlore(2), eg.MODEL_ISING, AFM, 2, 0),
+    (lambda: eg.simple_cubic(12), eg.MODEL_XYZ, FM, 2, 0),
+    (lambda: eg.simple_cubic((6, 8, 10)), eg.MODEL_XYZ, AFM, 3, 0),
+    (lambda: eg.pyrochlore(2), eg.MODEL_XYZ, AFM, 2, 0),
+]
+
+
+def build_members(specs=SPECS, seed0=11):
+    out = []
+    for k, (mk, model, shells, R, flags) in enumerate(specs):
+        lat = mk()
+        j = eg.couplings(lat.n_species, shells, [1.0])
+        sw = eg.Sweep.from_lattice(lat, j, np.asarray([1.0]), model, replicas=R,
+                                   seed=1992 + 7 * k, flags=flags)
+        sw.set_ladder([beta_of(3.0 + 1.5 * i) for i in range(R)])
+        ion = random_ising(lat, seed0 + k) if model == eg.MODEL_ISING else random_xyz(lat, seed0 + k)
+        sw.set_spins(ion)
+        sw.set_streams(stream=[100 * k + r for r in range(R)], step=[3 * r for r in range(R)])
+        out.append((lat, sw))
+    return out
+
+
+def states(members):
+    res = []
+    for lat, sw in members:
+        for r in range(sw.R):
+            g = sw.get_spins(lat.ion, r)
+            res.append(g[:, [1, 2, 3, 5]].copy())
+        res.append(sw.accept_counts().astype(np.float64))
+    return res
+
+
+def assert_same(a, b):
+    assert len(a) == len(b)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+
+
+@pytest.mark.parametrize("config", [(256, 2, 0, 0), (128, 1, 1, 1), (64, 8, 2, 0), (256, 64, 0, 1),
+                                    (128, 4, 0, 1)])
+def test_batch_equals_member_sweeps(config):
+    A = build_members()
+    B = build_members()
+    batch = eg.Batch([sw for _, sw in A])
+    batch.set_config(*config)
+    batch.metropolis(4)
+    for _, sw in B:
+        sw.metropolis(4)
+    assert_same(states(A), states(B))
+    info = batch.info()
+    assert info.n_members == len(SPECS)
+    assert info.n_replicas == sum(s[3] for s in SPECS)
+    max_col = max(sw.info().n_colours for _, sw in A)
+    assert info.kernels_per_sweep == max_col + 1
+    assert info.site_updates_per_sweep == sum(sw.N * sw.R for _, sw in A)
+    assert info.kernel_launches == 4 * info.kernels_per_sweep
+    assert info.last_sweep_ms > 0.0
+    batch.close()
+
+
+def test_batch_interleaves_with_member_calls():
+    """Stream ordering: batch sweeps, a member's own sweep, more batch sweeps."""
+    A = build_members()
+    B = build_members()
+    batch = eg.Batch([sw for _, sw in A])
+    batch.metropolis(2)
+    A[0][1].metropolis(1)
+    A[5][1].metropolis(1)
+    batch.metropolis(1)
+    for k, (_, sw) in enumerate(B):
+        sw.metropolis(2)
+        if k in (0, 5):
+            sw.metropolis(1)
+        sw.metropolis(1)
+    assert_same(states(A), states(B))
+    batch.close()
+
+
+def test_batch_autotune_restores_state_and_keeps_parity():
+    A = build_members()
+    B = build_members()
+    batch = eg.Batch([sw for _, sw in A])
+    before = states(A)
+    cfg, ms = batch.autotune()
+    assert cfg[0] in (128, 256) and cfg[1] in (1, 2, 4, 8) and cfg[2] >= 1 and cfg[3] in (0, 1)
+    assert ms > 0.0
+    assert_same(states(A), before)
+    batch.metropolis(3)
+    for _, sw in B:
+        sw.metropolis(3)
+    assert_same(states(A), states(B))
+    batch.close()
+
+
+def test_batch_members_with_variants():
+    """Members on other Ising kernel variants (8-byte vectors, several per thread)."""
+    specs = [SPECS[0], SPECS[1], SPECS[5]]
+    A = build_members(specs)
+    B = build_members(specs)
+    A[0][1].set_variant(84)
+    B[0][1].set_variant(161)
+    batch = eg.Batch([sw for _, sw in A])
+    batch.metropolis(3)
+    for _, sw in B:
+        sw.metropolis(3)
+    assert_same(states(A), states(B))
+    batch.close()
+
+
+def test_batch_rejects_bad_input():
+    A = build_members(SPECS[:2])
+    with pytest.raises(eg.EtherError):
+        eg.Batch([A[0][1], A[0][1]])
+    batch = eg.Batch([sw for _, sw in A])
+    with pytest.raises(eg.EtherError):
+        batch.set_config(96, 1, 0)
+    with pytest.raises(eg.EtherError):
+        batch.set_config(128, 1, 0, walk=2)
+    with pytest.raises(eg.EtherError):
+        batch.metropolis(-1)
+    batch.close()
