@@ -72,6 +72,20 @@ class BatchInfo(C.Structure):
     ]
 
 
+class LearnDesc(C.Structure):
+    _fields_ = [("patch", C.c_int32), ("hidden", C.c_int32), ("seed", C.c_uint32),
+                ("capacity", C.c_int64)]
+
+
+class LearnInfo(C.Structure):
+    _fields_ = [
+        ("n_params", C.c_int32), ("train_steps", C.c_int32), ("patches_per_class", C.c_int64),
+        ("n_samples", C.c_int64), ("capacity", C.c_int64), ("proposed", C.c_uint64),
+        ("kernel_launches", C.c_uint64), ("last_sweep_ms", C.c_float),
+        ("last_train_ms", C.c_float),
+    ]
+
+
 P = C.c_void_p
 PD = C.POINTER(C.c_double)
 PI32 = C.POINTER(C.c_int32)
@@ -121,6 +135,20 @@ SIGNATURES = {
     "ether_batch_autotune": (C.c_int, [P, PI32, C.POINTER(C.c_float)]),
     "ether_batch_get_info": (C.c_int, [P, C.POINTER(BatchInfo)]),
     "ether_batch_get_stream": (C.c_int, [P, C.POINTER(P)]),
+    "ether_learn_create": (C.c_int, [P, C.POINTER(LearnDesc), C.POINTER(P)]),
+    "ether_learn_destroy": (C.c_int, [P]),
+    "ether_learn_collect": (C.c_int, [P, C.c_int32]),
+    "ether_learn_train": (C.c_int, [P, C.c_int32, C.c_int32, C.c_float, PD]),
+    "ether_learn_sweep": (C.c_int, [P, C.c_int32]),
+    "ether_learn_get_accepts": (C.c_int, [P, PU64]),
+    "ether_learn_get_params": (C.c_int, [P, C.POINTER(C.c_float)]),
+    "ether_learn_set_params": (C.c_int, [P, C.POINTER(C.c_float)]),
+    "ether_learn_loss_grad": (C.c_int, [P, C.POINTER(C.c_float), PU32, C.c_int32, PD,
+                                        C.POINTER(C.c_float)]),
+    "ether_learn_forward": (C.c_int, [P, C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_float)]),
+    "ether_learn_set_dump": (C.c_int, [P, C.c_int32]),
+    "ether_learn_get_dump": (C.c_int, [P, C.POINTER(C.c_float)]),
+    "ether_learn_get_info": (C.c_int, [P, C.POINTER(LearnInfo)]),
     "ether_sc_energy_noalloc": (C.c_int, [C.c_int32, P, PI32, C.c_int32, PD, PD, PD, PD, P]),
     "ether_build_lattice": (C.c_int, [C.c_int32, PD, PI32, PD, PI32, C.c_char_p, C.c_int32,
                                       C.c_int32, PD, C.c_double, C.c_int32, PD, PD, PI32]),

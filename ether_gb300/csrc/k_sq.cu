@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "tc_util.cuh"
 
 namespace ether {
 namespace sq {
@@ -41,7 +42,6 @@ constexpr int kBK = 64;         // sites per k-block (128 bytes of BF16)
 constexpr int kStages = 2;
 constexpr int kProducers = 256; // warps 0-7
 constexpr int kThreads = 288;   // + warp 8 (TMA + MMA issue)
-constexpr uint64_t kWaitNs = 2000000000ull;
 
 struct Smem {
     // stage s: A_hi, A_lo (kBM x kBK bf16 each), B_hi, B_lo (BN x kBK bf16 each)
@@ -49,80 +49,10 @@ struct Smem {
     static constexpr int a_bytes = kBM * kBK * 2;  // 16 KB
 };
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ uint64_t gtime() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
-}
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive_tx(uint32_t bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        " selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
-    return ok != 0;
-}
-// Bounded wait: false (and *err set) if the phase did not complete within kWaitNs.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *err, int code) {
-    if (mbar_try(bar, parity)) return true;
-    const uint64_t t0 = gtime();
-    while (!mbar_try(bar, parity)) {
-        if (gtime() - t0 > kWaitNs) {
-            atomicCAS(err, 0, code);
-            return false;
-        }
-    }
-    return true;
-}
+using namespace tc;
 
-// Byte offset of element (row, k) in a K-major, 128-byte-swizzled tile of 64 BF16 columns:
-// 8-row atoms of 1024 bytes, 16-byte chunk index XORed with the row within the atom.
-__device__ __forceinline__ uint32_t swz(int row, int k) {
-    return (uint32_t)((row >> 3) * 1024 + (row & 7) * 128 + ((((k >> 3) ^ (row & 7))) << 4) + (k & 7) * 2);
-}
-
-// UMMA shared-memory descriptor: K-major, SWIZZLE_128B, 8-row stride 1024 bytes.
-__device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
-    uint64_t d = 0;
-    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);        // start address
-    d |= (uint64_t)1u << 16;                         // leading byte offset (unused for swizzled K-major)
-    d |= (uint64_t)(1024u >> 4) << 32;               // stride byte offset
-    d |= (uint64_t)1u << 46;                         // descriptor version
-    d |= (uint64_t)2u << 61;                         // SWIZZLE_128B
-    return d;
-}
-
-// Instruction descriptor, kind::f16: BF16 x BF16 -> FP32, both K-major, M = 128, N = n.
-__host__ __device__ constexpr uint32_t make_idesc(int n) {
-    return (1u << 4)                       // D format F32
-           | (1u << 7)                     // A format BF16
-           | (1u << 10)                    // B format BF16
-           | ((uint32_t)(n >> 3) << 17)    // N / 8
-           | ((uint32_t)(kBM >> 4) << 24); // M / 16
-}
-
-__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                     uint32_t accumulate) {
-    asm volatile(
-        "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
-        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
-        ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
-}
-__device__ __forceinline__ void umma_commit(uint32_t bar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
-}
+// Instruction descriptor for this kernel's M = 128 tiles.
+__host__ __device__ constexpr uint32_t make_idesc(int n) { return tc::make_idesc(kBM, n); }
 
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int c0, int c1, uint32_t bar) {
     asm volatile(

@@ -354,3 +354,90 @@ class Batch:
         s = C.c_void_p()
         abi.check(self.lib.ether_batch_get_stream(self.h, C.byref(s)))
         return s.value or 0
+
+
+N_LEARN_PARAMS = 128 * 128 + 128 + 128 * 128 + 128 + 32 * 128 + 32
+
+
+class Learned:
+    """ether_learn: the learned 4^3-patch proposal of a simple-cubic Ising Sweep, accepted by
+    exact Metropolis-Hastings (the plain sweep stays the fallback; interleave the two)."""
+
+    def __init__(self, sweep, seed=7, capacity=1 << 20):
+        self.lib = abi.load()
+        self.sweep = sweep
+        d = abi.LearnDesc()
+        d.patch = 4
+        d.hidden = 128
+        d.seed = seed & 0xFFFFFFFF
+        d.capacity = int(capacity)
+        h_ = C.c_void_p()
+        abi.check(self.lib.ether_learn_create(sweep.h, C.byref(d), C.byref(h_)))
+        self.h = h_
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ether_learn_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def collect(self, per_replica):
+        abi.check(self.lib.ether_learn_collect(self.h, per_replica))
+
+    def train(self, steps, batch=1024, lr=1e-3):
+        loss = C.c_double(0.0)
+        abi.check(self.lib.ether_learn_train(self.h, steps, batch, lr, C.byref(loss)))
+        return loss.value
+
+    def sweep_(self, nsweeps=1):
+        abi.check(self.lib.ether_learn_sweep(self.h, nsweeps))
+
+    def accepts(self):
+        out = np.zeros(self.sweep.R, dtype=np.uint64)
+        abi.check(self.lib.ether_learn_get_accepts(self.h, out.ctypes.data_as(abi.PU64)))
+        return out
+
+    def params(self):
+        p = np.zeros(N_LEARN_PARAMS, dtype=np.float32)
+        abi.check(self.lib.ether_learn_get_params(self.h, p.ctypes.data_as(C.POINTER(C.c_float))))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        abi.check(self.lib.ether_learn_set_params(self.h, p.ctypes.data_as(C.POINTER(C.c_float))))
+
+    def loss_grad(self, x, y):
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 128)
+        y = np.ascontiguousarray(y, dtype=np.uint32)
+        g = np.zeros(N_LEARN_PARAMS, dtype=np.float32)
+        loss = C.c_double(0.0)
+        abi.check(self.lib.ether_learn_loss_grad(
+            self.h, x.ctypes.data_as(C.POINTER(C.c_float)), y.ctypes.data_as(abi.PU32), x.shape[0],
+            C.byref(loss), g.ctypes.data_as(C.POINTER(C.c_float))))
+        return loss.value, g
+
+    def forward(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 128)
+        z = np.zeros((x.shape[0], 32), dtype=np.float32)
+        abi.check(self.lib.ether_learn_forward(self.h, x.ctypes.data_as(C.POINTER(C.c_float)),
+                                               x.shape[0], z.ctypes.data_as(C.POINTER(C.c_float))))
+        return z
+
+    def set_dump(self, on=True):
+        abi.check(self.lib.ether_learn_set_dump(self.h, int(bool(on))))
+
+    def dump(self):
+        i = self.info()
+        z = np.zeros((2, self.sweep.R, i.patches_per_class, 32), dtype=np.float32)
+        abi.check(self.lib.ether_learn_get_dump(self.h, z.ctypes.data_as(C.POINTER(C.c_float))))
+        return z
+
+    def info(self):
+        i = abi.LearnInfo()
+        abi.check(self.lib.ether_learn_get_info(self.h, C.byref(i)))
+        return i

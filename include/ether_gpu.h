@@ -274,6 +274,63 @@ int ether_batch_get_info(ether_batch *batch, ether_batch_info *info);
 /* The cudaStream_t the batch launches on. */
 int ether_batch_get_stream(ether_batch *batch, void **stream);
 
+/* ------------------------------------------------------- learned patch proposal ---- */
+/* No counterpart in the reference (which only has single-site moves, src/Metropolis.f90);
+ * its target distribution is kept exactly: every learned move is accepted or rejected by
+ * Metropolis-Hastings against the reference's Ising energy.  Simple-cubic Ising contexts with
+ * one species, one shell, no Zeeman term and extents that are multiples of 8.
+ * A learned sweep tiles each replica with 4^3 patches (a fresh random offset per sweep) and
+ * updates the two patch classes in turn: the network (96 boundary spins + 4 beta J -> 128 ->
+ * 128 -> 32, BF16 weights, tensor cores) proposes the patch's 32 colour-0 spins, the 32
+ * colour-1 spins are drawn from their exact heat-bath conditionals, and the whole patch is
+ * accepted with probability min(1, pi(new) q(old) / (pi(old) q(new))).  The plain
+ * ether_metropolis sweep stays the fallback; interleave the two. */
+typedef struct ether_learn ether_learn;
+typedef struct ether_learn_desc {
+    int32_t patch;     /* patch edge: 4                                                    */
+    int32_t hidden;    /* hidden width: 128                                                */
+    uint32_t seed;     /* weight initialisation and training minibatches                   */
+    int64_t capacity;  /* training samples kept on the device (ring buffer), >= 1024        */
+} ether_learn_desc;
+int ether_learn_create(ether_ctx *ctx, const ether_learn_desc *desc, ether_learn **learn);
+int ether_learn_destroy(ether_learn *learn);
+/* Training data: per_replica random patches (boundary, colour-0 spins, 4 beta J) of every
+ * replica's current configuration -- configurations the plain sweep produced, at every
+ * temperature of the context's ladder. */
+int ether_learn_collect(ether_learn *learn, int32_t per_replica);
+/* steps of Adam (learning rate lr) on minibatches of `batch` samples, maximum likelihood of
+ * the colour-0 spins given the boundary; loss (may be NULL) = last minibatch's mean loss. */
+int ether_learn_train(ether_learn *learn, int32_t steps, int32_t batch, float lr, double *loss);
+/* nsweeps learned sweeps of every replica (asynchronous, on the context's stream). */
+int ether_learn_sweep(ether_learn *learn, int32_t nsweeps);
+/* Accepted patches per replica since creation (accepted(R)). */
+int ether_learn_get_accepts(ether_learn *learn, uint64_t *accepted);
+/* Parameters: W1(128,128), b1(128), W2(128,128), b2(128), W3(32,128), b3(32), FP32, row =
+ * output unit; n = 37152.  Setting them resets the optimiser. */
+int ether_learn_get_params(ether_learn *learn, float *params);
+int ether_learn_set_params(ether_learn *learn, const float *params);
+/* The training kernels on a given batch: x(128, B) inputs, y(B) colour-0 spins as bits;
+ * loss = mean BCE, grad(37152) = its gradient (no update). */
+int ether_learn_loss_grad(ether_learn *learn, const float *x, const uint32_t *y, int32_t B,
+                          double *loss, float *grad);
+/* The inference network (tensor cores) on x(128, B): logits(32, B). */
+int ether_learn_forward(ether_learn *learn, const float *x, int32_t B, float *logits);
+/* Record the logits of the last sweep of the next ether_learn_sweep; get_dump returns them
+ * as logits(32, Pc, R, 2) (class, replica, patch of the class). */
+int ether_learn_set_dump(ether_learn *learn, int32_t on);
+int ether_learn_get_dump(ether_learn *learn, float *logits);
+typedef struct ether_learn_info {
+    int32_t n_params;
+    int32_t train_steps;
+    int64_t patches_per_class;  /* Pc per replica                                          */
+    int64_t n_samples, capacity;
+    uint64_t proposed;          /* patch proposals so far, all replicas                    */
+    uint64_t kernel_launches;
+    float last_sweep_ms;        /* CUDA-event time per learned sweep of the last call      */
+    float last_train_ms;        /* CUDA-event time of the last ether_learn_train          */
+} ether_learn_info;
+int ether_learn_get_info(ether_learn *learn, ether_learn_info *info);
+
 /* ------------------------------------------------------------- no-allocation energy ---- */
 /* No counterpart in the reference.  Energy and magnetisation of n_replicas simple-cubic
  * configurations already in device memory, for callers that cannot allocate device memory

@@ -6,4 +6,4 @@ set -e
 here=$(cd "$(dirname "$0")" && pwd)
 mkdir -p "$here/_build"
 ${CC:-cc} -O2 -std=c11 -D_GNU_SOURCE -fopenmp -ffp-contract=off -fno-fast-math -fPIC -shared \
-    -Wall -Wno-unused-function -o "$here/_build/libether_oracle.so" "$here/ether_oracle.c" -lm
+    -Wall -Wno-unused-function -o "$here/_build/libether_oracle.so" "$here/ether_oracle.c" "$here/learn_oracle.c" -lm

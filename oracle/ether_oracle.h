@@ -188,6 +188,24 @@ void orc_run_temperatures(const orc_sys *sy, const double *ion0, int nT, const d
 float orc_expf_neg(float x);
 void orc_sincosf(float x, float *s, float *c);
 
+
+/* ---- learned patch proposal (learn_oracle.c) ---- */
+float orc_bf16_round(float f);
+float orc_logf_own(float x);
+int orc_mlp_n_params(void);
+void orc_mlp_forward(const float *params, const float *x, int B, int quant, float *logits);
+double orc_mlp_loss_grad(const float *params, const float *x, const uint32_t *y, int B, int quant,
+                         double *grad);
+void orc_patch_tables(int32_t *A, int32_t *B, int32_t *Bn, int32_t *Ab);
+void orc_patch_gather(const uint8_t *sp, const int L[3], const int off[3], int pi, int pj, int pk,
+                      float k4, float *x, uint32_t bnd[3], uint32_t *abits, uint32_t *bbits);
+void orc_patch_btables(double betaJ, uint32_t TB[7], float LBup[7], float LBdn[7]);
+void orc_patch_offsets(uint32_t seed, uint32_t stream, uint32_t t, int off[3]);
+long orc_patch_sweep(uint8_t *sp, const int L[3], double betaJ, const float *logits,
+                     uint32_t seed, uint32_t stream, uint32_t t);
+void orc_patch_chain(const int L[3], double betaJ, long nsteps, long nequil, int use_patch,
+                     float zscale, float zbias, uint32_t seed, double out[5]);
+
 #ifdef __cplusplus
 }
 #endif

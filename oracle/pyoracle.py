@@ -97,6 +97,24 @@ def lib():
         L.orc_expf_neg.restype = C.c_float
         L.orc_expf_neg.argtypes = [C.c_float]
         L.orc_sincosf.argtypes = [C.c_float, PF, PF]
+        PU8 = C.POINTER(C.c_uint8)
+        L.orc_bf16_round.restype = C.c_float
+        L.orc_bf16_round.argtypes = [C.c_float]
+        L.orc_logf_own.restype = C.c_float
+        L.orc_logf_own.argtypes = [C.c_float]
+        L.orc_mlp_n_params.restype = C.c_int
+        L.orc_mlp_forward.argtypes = [PF, PF, C.c_int, C.c_int, PF]
+        L.orc_mlp_loss_grad.restype = C.c_double
+        L.orc_mlp_loss_grad.argtypes = [PF, PF, PU, C.c_int, C.c_int, PD]
+        L.orc_patch_tables.argtypes = [PI, PI, PI, PI]
+        L.orc_patch_gather.argtypes = [PU8, PI, PI, C.c_int, C.c_int, C.c_int, C.c_float, PF, PU,
+                                       PU, PU]
+        L.orc_patch_btables.argtypes = [C.c_double, PU, PF, PF]
+        L.orc_patch_offsets.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, PI]
+        L.orc_patch_sweep.restype = C.c_long
+        L.orc_patch_sweep.argtypes = [PU8, PI, C.c_double, PF, C.c_uint32, C.c_uint32, C.c_uint32]
+        L.orc_patch_chain.argtypes = [PI, C.c_double, C.c_long, C.c_long, C.c_int, C.c_float,
+                                      C.c_float, C.c_uint32, PD]
         _lib = L
     return _lib
 
@@ -227,3 +245,75 @@ def neighbours_bruteforce(ion, abc, sc, bc, shells, tol, cap):
     rc = lib().orc_neighbours_bruteforce(N, _d(np.ascontiguousarray(ion)), _d(a), _i(s),
                                          bc.encode(), len(sh), _d(sh), tol, cap, _i(nn))
     return rc, nn
+
+
+# ----------------------------------------------------------- learned patch proposal ----
+PU8 = C.POINTER(C.c_uint8)
+
+
+def mlp_n_params():
+    return lib().orc_mlp_n_params()
+
+
+def mlp_forward(params, x, quant=True):
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    xx = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 128)
+    z = np.zeros((xx.shape[0], 32), dtype=np.float32)
+    lib().orc_mlp_forward(_f(p), _f(xx), xx.shape[0], int(quant), _f(z))
+    return z
+
+
+def mlp_loss_grad(params, x, y, quant=True):
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    xx = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 128)
+    yy = np.ascontiguousarray(y, dtype=np.uint32)
+    g = np.zeros(p.size, dtype=np.float64)
+    loss = lib().orc_mlp_loss_grad(_f(p), _f(xx), yy.ctypes.data_as(PU), xx.shape[0], int(quant),
+                                   _d(g))
+    return loss, g
+
+
+def patch_tables():
+    A = np.zeros((32, 3), np.int32)
+    B = np.zeros((32, 3), np.int32)
+    Bn = np.zeros((32, 6), np.int32)
+    Ab = np.zeros((32, 3), np.int32)
+    lib().orc_patch_tables(_i(A), _i(B), _i(Bn), _i(Ab))
+    return A, B, Bn, Ab
+
+
+def patch_offsets(seed, stream, t):
+    o = np.zeros(3, np.int32)
+    lib().orc_patch_offsets(seed, stream, t, _i(o))
+    return o
+
+
+def patch_gather(sp, L, off, i, j, k, k4):
+    """(x[128], boundary bits[3], A bits, B bits) of patch (i, j, k) of one replica's
+    colour-split uint8 spins."""
+    spa = np.ascontiguousarray(sp, dtype=np.uint8)
+    LL = np.ascontiguousarray(L, dtype=np.int32)
+    oo = np.ascontiguousarray(off, dtype=np.int32)
+    x = np.zeros(128, np.float32)
+    bnd = np.zeros(3, np.uint32)
+    a = np.zeros(1, np.uint32)
+    b = np.zeros(1, np.uint32)
+    lib().orc_patch_gather(spa.ctypes.data_as(PU8), _i(LL), _i(oo), i, j, k, k4, _f(x),
+                           bnd.ctypes.data_as(PU), a.ctypes.data_as(PU), b.ctypes.data_as(PU))
+    return x, bnd, int(a[0]), int(b[0])
+
+
+def patch_sweep(sp, L, betaJ, logits, seed, stream, t):
+    """One learned sweep (both classes) of one replica in place; returns accepted patches."""
+    assert sp.dtype == np.uint8 and sp.flags.c_contiguous
+    LL = np.ascontiguousarray(L, dtype=np.int32)
+    z = np.ascontiguousarray(logits, dtype=np.float32)
+    return lib().orc_patch_sweep(sp.ctypes.data_as(PU8), _i(LL), betaJ, _f(z), seed, stream, t)
+
+
+def patch_chain(L, betaJ, nsteps, nequil, use_patch, zscale=0.0, zbias=0.0, seed=1):
+    LL = np.ascontiguousarray(L, dtype=np.int32)
+    out = np.zeros(5)
+    lib().orc_patch_chain(_i(LL), betaJ, nsteps, nequil, int(use_patch), zscale, zbias, seed,
+                          _d(out))
+    return {"e": out[0], "e_err": out[1], "m": out[2], "m_err": out[3], "accept": out[4]}
