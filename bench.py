@@ -384,6 +384,64 @@ def run_batch(steps=200, warmup=5, chains=256, ladder=32, config=None, forms=(Fa
             **out}
 
 
+def run_learned(L=64, R=256, train_steps=3000, n_plain=40000, n_learn=6000):
+    """Learned 4^3-patch proposal at T_c of the L^3 Ising model: trained on plain-sweep
+    configurations of an 8-temperature ladder (0.9 .. 1.1 T_c), then tau_int(|M|) and the
+    independent samples per second of (a) plain sweeps, (b) plain + learned sweep per step,
+    (c) learned sweeps alone, all with R replicas at T_c."""
+    import ether_gb300 as eg
+    from ether_gb300.analysis import tau_int
+    lat = eg.simple_cubic(L)
+    j = eg.couplings(1, [[(1, 1, (-J_MEV, -J_MEV, -J_MEV))]], [1.0])
+    sw = eg.Sweep.from_lattice(lat, j, np.array([1.0]), eg.MODEL_ISING, replicas=R, seed=31)
+    ktc = KTC_ISING * J_MEV * 1e-3
+    sw.set_beta(1.0 / (np.repeat(ktc * np.linspace(0.9, 1.1, 8), R // 8)))
+    rng = np.random.default_rng(7)
+    ion = lat.ion.copy()
+    ion[:, 3] = rng.choice([-1.0, 1.0], size=lat.N)
+    sw.set_spins(ion)
+    sw.metropolis(2000, accept=False)
+    lr = eg.Learned(sw, seed=5, capacity=1 << 21)
+    for _ in range(40):
+        sw.metropolis(20, accept=False)
+        lr.collect((L // 4) ** 3 // 4)
+    loss = lr.train(train_steps, batch=1024, lr=1e-3)
+    train_ms = lr.info().last_train_ms
+    sw.set_beta([1.0 / ktc] * R)
+    sw.metropolis(5000, accept=False)
+    sw.sync()
+
+    def series(n, plain, learned):
+        t = time.perf_counter()
+        out = lr.record_series(n, 1 if plain else 0, 1 if learned else 0)
+        return out, time.perf_counter() - t
+
+    t = time.perf_counter()
+    m_plain = sw.record_series(n_plain, stride=1)
+    s_plain = time.perf_counter() - t
+    a0, p0 = lr.accepts().sum(), lr.info().proposed
+    m_both, s_both = series(n_learn, True, True)
+    m_learn, s_learn = series(n_learn, False, True)
+    acc = (lr.accepts().sum() - a0) / max(1, lr.info().proposed - p0)
+    lr.sweep_(20)
+    sweep_ms = lr.info().last_sweep_ms
+    res = {"workload": "learned 4^3-patch proposal, %d^3 Ising at T_c, %d replicas" % (L, R),
+           "train_steps": train_steps, "final_loss": loss, "train_ms": train_ms,
+           "acceptance_at_tc": acc, "learned_sweep_ms": sweep_ms}
+    for name, m, n, secs in (("plain", m_plain, n_plain, s_plain), ("plain_plus_learned", m_both, n_learn, s_both),
+                             ("learned_only", m_learn, n_learn, s_learn)):
+        tau, err, W = tau_int(m)
+        res[name] = {"tau_int_absM_steps": tau, "tau_err": err, "steps": n,
+                     "steps_per_s": n / secs,
+                     "independent_samples_per_s": R * n / secs / (2.0 * tau)}
+    base = res["plain"]["independent_samples_per_s"]
+    for name in ("plain_plus_learned", "learned_only"):
+        res[name]["gain_vs_plain"] = res[name]["independent_samples_per_s"] / base
+    lr.close()
+    sw.close()
+    return res
+
+
 def cpu_reference(model, L, mcs, threads, seed=1992):
     """The oracle's typewriter restatement of the reference's per-MCS work (Metropolis
     + get_tot_energy), one replica (temperature) per thread."""
@@ -443,7 +501,7 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--model", default="ising", choices=["ising", "heisenberg", "sq", "batch"])
+    ap.add_argument("--model", default="ising", choices=["ising", "heisenberg", "sq", "batch", "learned"])
     ap.add_argument("--L", type=int, default=64)
     ap.add_argument("--replicas", type=int, default=0)
     ap.add_argument("--cpu-mcs", type=int, default=0)
@@ -480,6 +538,14 @@ def main():
                           "roofline": {"bound": "tensor", "achieved": r["tensor_tflops"],
                                        "peak": bf16_peak, "unit": "TFLOP/s",
                                        "frac": r["tensor_tflops"] / bf16_peak}}))
+        return 0
+
+    if args.model == "learned":
+        if rank != 0:
+            return 0
+        r = run_learned(args.L)
+        print(json.dumps({"metric": "independent samples/s gain", "value": r["learned_only"]["gain_vs_plain"],
+                          "unit": "x plain", "higher_is_better": True, "detail": r}))
         return 0
 
     if args.model == "batch":
@@ -569,6 +635,7 @@ def main():
         bt["roofline"]["frac"] = bt["roofline"]["achieved"] / hbm_peak
         comp["batch"] = bt
         comp["tau"] = run_tau(args.L)
+        comp["learned"] = run_learned(args.L)
         line["components"] = comp
     if not args.no_cpu:
         line["cpu_baseline"] = {k: v for k, v in

@@ -556,6 +556,8 @@ static int sweep_once(Ctx &c) {
     return ETHER_OK;
 }
 
+int ether::plain_sweep(Ctx &c) { return sweep_once(c); }
+
 extern "C" int ether_metropolis(ether_ctx *h, int32_t nsweeps, double *accept) {
     if (!h) return fail(ETHER_ERR_ARG, "null context");
     Ctx &c = h->c;

@@ -115,6 +115,7 @@ cudaError_t launch_measure(Ctx &c);
 cudaError_t launch_record(Ctx &c, int t, bool want_e, double *mser, double *eser);
 cudaError_t launch_pt(Ctx &c, int set_swap_count);
 int energy_blocks(const Ctx &c);
+int plain_sweep(Ctx &c);  // one Metropolis sweep of every replica (ETHER_OK or an error code)
 void set_error(const std::string &msg);
 int structure_factor_launch(Ctx &c, const double *frac, const int nq[3], const double q0[3],
                             const double dq[3], float *sq_host, float *comp_host, std::string &msg);

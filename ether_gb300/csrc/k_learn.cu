@@ -15,7 +15,7 @@
 //   * proposal: A-site k up with probability T_k / 2^32 from the logit; every B-site then from
 //     its exact heat-bath conditional given the new A-sites and the boundary;
 //   * acceptance: log alpha = log q(old) - log q(new) - beta J (bond change), FP32 in a fixed
-//     order with own exp / log (the same operations as oracle/learn_oracle.c, which replays a
+//     order with an own exp (the same operations as oracle/learn_oracle.c, which replays a
 //     sweep bit for bit given the logits).
 // Training: maximum likelihood of the A-sites given the boundary on configurations the plain
 // sweep produced (any temperature of the context's ladder), Adam, straight-through BF16
@@ -44,17 +44,17 @@ constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + NH * NI, OFF_W2 = OFF_B1 + NH, OFF_B
 constexpr int IMG_W1 = 0, IMG_W2 = 32768, IMG_W3 = 65536, IMG_B1 = 73728, IMG_B2 = IMG_B1 + 512,
               IMG_B3 = IMG_B2 + 512, IMG_BYTES = IMG_B3 + 128;
 // Shared memory of the patch kernel (from a 1024-byte aligned base).
-constexpr int SM_A = 73728, SM_BIAS = SM_A + 32768, SM_BAR = SM_BIAS + 1152, SM_BYTES = SM_BAR + 16;
+constexpr int SM_A = 73728, SM_BIAS = SM_A + 32768, SM_PATCH = SM_BIAS + 1152,
+              SM_BAR = SM_PATCH + 128 * 28, SM_BYTES = SM_BAR + 16;
 constexpr int kThreads = 128;
 
 // ------------------------------------------------------------------ patch geometry ----
 // Local sites 0..31 = A-sites, 32..63 = B-sites, packed (a | b << 2 | c << 4); boundary
-// sites packed ((a+1) | (b+1) << 4 | (c+1) << 8); B-site neighbours: >= 0 A-site index,
-// < 0 boundary -(1 + index); A-site boundary neighbours (-1 none).
+// sites packed ((a+1) | (b+1) << 4 | (c+1) << 8).  The neighbour tables below (B-site
+// neighbours: >= 0 A-site index, < 0 boundary -(1 + index); A-site boundary neighbours) are
+// built once on the host and must agree with the closed forms the kernels use.
 __constant__ uint8_t c_site[64];
 __constant__ uint16_t c_bnd[96];
-__constant__ int8_t c_Bn[32][6];
-__constant__ int8_t c_Ab[32][3];
 
 struct Geometry {
     uint8_t site[64];
@@ -71,6 +71,8 @@ static int face_index(int a, int b, int c) {
     if (c == -1) return 64 + a + 4 * b;
     return 80 + a + 4 * b;
 }
+
+static bool closed_forms_agree(const Geometry &g);
 
 static Geometry make_geometry() {
     Geometry g;
@@ -117,45 +119,46 @@ static Geometry make_geometry() {
     return g;
 }
 
+// Closed forms of the same geometry, for fully unrolled loops (folded at compile time).
+// Row = b + 4c; the two A-sites (B-sites) of a row sit at a = p, p + 2 (a = 1 - p, 3 - p),
+// p = (b + c) & 1, and have indices 2 row + (a >> 1).
+__host__ __device__ constexpr int geo_b_a(int m) { return (1 - ((((m >> 1) & 3) + ((m >> 1) >> 2)) & 1)) + 2 * (m & 1); }
+__host__ __device__ constexpr int geo_a_a(int k) { return ((((k >> 1) & 3) + ((k >> 1) >> 2)) & 1) + 2 * (k & 1); }
+// Neighbour q (-x, +x, -y, +y, -z, +z) of B-site m: A-site index (>= 0) or -(1 + boundary index).
+__host__ __device__ constexpr int geo_bn(int m, int q) {
+    const int row = m >> 1, b = row & 3, c = row >> 2, a = geo_b_a(m);
+    return q == 0 ? (a == 0 ? -(1 + b + 4 * c) : 2 * row + ((a - 1) >> 1))
+         : q == 1 ? (a == 3 ? -(1 + 16 + b + 4 * c) : 2 * row + ((a + 1) >> 1))
+         : q == 2 ? (b == 0 ? -(1 + 32 + a + 4 * c) : 2 * (row - 1) + (a >> 1))
+         : q == 3 ? (b == 3 ? -(1 + 48 + a + 4 * c) : 2 * (row + 1) + (a >> 1))
+         : q == 4 ? (c == 0 ? -(1 + 64 + a + 4 * b) : 2 * (row - 4) + (a >> 1))
+                  : (c == 3 ? -(1 + 80 + a + 4 * b) : 2 * (row + 4) + (a >> 1));
+}
+// Boundary neighbour q of A-site k (-1 if that neighbour is inside the patch).
+__host__ __device__ constexpr int geo_ab(int k, int q) {
+    const int row = k >> 1, b = row & 3, c = row >> 2, a = geo_a_a(k);
+    return q == 0 ? (a == 0 ? b + 4 * c : -1)
+         : q == 1 ? (a == 3 ? 16 + b + 4 * c : -1)
+         : q == 2 ? (b == 0 ? 32 + a + 4 * c : -1)
+         : q == 3 ? (b == 3 ? 48 + a + 4 * c : -1)
+         : q == 4 ? (c == 0 ? 64 + a + 4 * b : -1)
+                  : (c == 3 ? 80 + a + 4 * b : -1);
+}
+
 // ------------------------------------------------------------- own FP32 functions ----
 // Same operation sequence as oracle/learn_oracle.c (compiled with --fmad=false: explicit
 // fmaf only).
-__device__ __forceinline__ float logf_own(float x) {
-    uint32_t u = __float_as_uint(x);
-    int e = (int)((u >> 23) & 0xFFu) - 127;
-    u = (u & 0x007FFFFFu) | 0x3F800000u;
-    float m = __uint_as_float(u);
-    if (m > 1.41421356f) {
-        m = m * 0.5f;
-        e += 1;
-    }
-    const float s = (m - 1.0f) / (m + 1.0f);
-    const float s2 = s * s;
-    float p = 0.111111111f;
-    p = fmaf(p, s2, 0.142857143f);
-    p = fmaf(p, s2, 0.2f);
-    p = fmaf(p, s2, 0.333333333f);
-    p = fmaf(p, s2, 1.0f);
-    const float lm = 2.0f * (s * p);
-    return fmaf((float)e, 0.693147182f, lm);
-}
+// sigmoid(z) = r or e r with e = exp(-|z|), r = 1 / (1 + e) correctly rounded.
 __device__ __forceinline__ float sigmoid_own(float z) {
-    if (z >= 0.0f) {
-        const float e = expf_neg(-z);
-        return 1.0f / (1.0f + e);
-    }
-    const float e = expf_neg(z);
-    return e / (1.0f + e);
+    const float e = expf_neg(-fabsf(z));
+    const float r = __frcp_rn(1.0f + e);
+    return z >= 0.0f ? r : e * r;
 }
 __device__ __forceinline__ uint32_t thr_of_logit(float z) {
     float t = sigmoid_own(z) * 4294967296.0f;
     t = fmaxf(t, 1.0f);
     t = fminf(t, 4294967040.0f);
     return (uint32_t)t;
-}
-__device__ __forceinline__ float lq_of(uint32_t T, bool up) {
-    if (up) return logf_own((float)T * 2.3283064365386963e-10f);
-    return logf_own(__ull2float_rn(4294967296ull - (unsigned long long)T) * 2.3283064365386963e-10f);
 }
 
 // ------------------------------------------------------------------- the patch kernel ----
@@ -194,22 +197,45 @@ __device__ __forceinline__ long long site_addr(const PatchParams &P, int o0, int
     return (long long)((x + y + z) & 1) * P.half + ((long long)z * P.L2 + y) * P.H + (x >> 1);
 }
 
+// Per tile of 128 patches:
+//   1. thread p decodes patch p (replica, origin, reflection) into shared memory;
+//   2. each warp gathers its 32 patches cooperatively: lane l loads sites l, l+32, .., l+128
+//      of the list [96 boundary | 32 A | 32 B] and five ballots give the patch's bit masks;
+//   3. thread p writes its network input row (boundary spins, 4 beta J) into the A tile;
+//   4. three tcgen05 layers, TMEM lane p = patch p;
+//   5. thread p's Metropolis-Hastings step from the masks and its 32 logits.
 template <int MODE>  // 0: lattice patches + Metropolis-Hastings, 1: network forward on X
 __global__ void __launch_bounds__(kThreads, 2) patch_kernel(PatchParams P) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     float *bias = reinterpret_cast<float *>(base + SM_BIAS);  // b1[128], b2[128], b3[32]
+    uint32_t *s_org = reinterpret_cast<uint32_t *>(base + SM_PATCH);  // origin | par << 30
+    int32_t *s_rep = reinterpret_cast<int32_t *>(s_org + 128);       // replica, -1 = none
+    uint32_t *s_bits = reinterpret_cast<uint32_t *>(s_rep + 128);    // [128][5]
     uint64_t *bar = reinterpret_cast<uint64_t *>(base + SM_BAR);
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(base + SM_BAR + 8);
-    const int tid = threadIdx.x, warp = tid >> 5;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     // weights and biases into shared memory (plain 16-byte copies; the image is pre-swizzled)
     {
         const uint4 *src = reinterpret_cast<const uint4 *>(P.img);
         uint4 *dw = reinterpret_cast<uint4 *>(base);
-        for (int i = tid; i < IMG_B1 / 16; i += kThreads) dw[i] = src[i];
+        constexpr int nw = IMG_B1 / 16;  // 4608 = 36 x 128
+        for (int i0 = 0; i0 < nw; i0 += 8 * kThreads) {
+            uint4 v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int i = i0 + u * kThreads + tid;
+                if (i < nw) v[u] = __ldg(src + i);
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int i = i0 + u * kThreads + tid;
+                if (i < nw) dw[i] = v[u];
+            }
+        }
         uint4 *db = reinterpret_cast<uint4 *>(base + SM_BIAS);
-        for (int i = tid; i < (IMG_BYTES - IMG_B1) / 16; i += kThreads) db[i] = src[IMG_B1 / 16 + i];
+        for (int i = tid; i < (IMG_BYTES - IMG_B1) / 16; i += kThreads) db[i] = src[nw + i];
     }
     if (tid == 0) {
         tc::mbar_init(tc::smem_u32(bar), 1);
@@ -232,51 +258,87 @@ __global__ void __launch_bounds__(kThreads, 2) patch_kernel(PatchParams P) {
     uint32_t phase = 0;
     bool ok = true;
 
+    // this lane's five sites of every patch: canonical (a, b, c) + 1, packed 4 bits each
+    uint32_t my_site[5];
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+        const int i = lane + 32 * c;
+        if (i < 96) {
+            my_site[c] = c_bnd[i];
+        } else {
+            const uint8_t e = c_site[i - 96];
+            my_site[c] = (uint32_t)(((e & 3) + 1) | ((((e >> 2) & 3) + 1) << 4) | (((e >> 4) + 1) << 8));
+        }
+    }
+
     const long long total = MODE == 0 ? (long long)P.R * P.Pc : (long long)P.B;
     const long long ntiles = (total + kThreads - 1) / kThreads;
     for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
         const long long w = tile * kThreads + tid;
         const bool valid = w < total;
-        // ---------------------------------------------------------------- input row ------
-        int r = 0, o0 = 0, o1 = 0, o2 = 0, par = 0;
-        uint32_t pidx = 0, t = 0, stream = 0;
+        int r = 0;
         long long q = 0;
+        uint32_t pidx = 0, t = 0, stream = 0;
         uint32_t bnd0 = 0, bnd1 = 0, bnd2 = 0, ao = 0, bo = 0;
         float k4 = 0.f;
-        if (MODE == 0 && valid) {
-            r = (int)(w / P.Pc);
-            q = w - (long long)r * P.Pc;
-            const int half1 = P.P1 >> 1;
-            const int tt = (int)(q % half1);
-            const long long row = q / half1;
-            const int pj = (int)(row % P.P2), pk = (int)(row / P.P2);
-            const int pi = 2 * tt + ((P.cls + pj + pk) & 1);
-            pidx = (uint32_t)(pi + P.P1 * (pj + P.P2 * pk));
-            t = P.lstep[r];
-            stream = P.stream_id[r];
-            const U4 ow = draw(0xFFFFFFFFu, t, stream, kLearn | (0xFFu << 8), P.seed);
-            const int ox = (int)(ow.x & 3u), oy = (int)((ow.x >> 2) & 3u), oz = (int)((ow.x >> 4) & 3u);
-            par = (ox + oy + oz) & 1;
-            o0 = 4 * pi + ox;
-            o1 = 4 * pj + oy;
-            o2 = 4 * pk + oz;
-            const uint8_t *sp = P.spins + (long long)r * 2 * P.half;
-            for (int i = 0; i < 96; ++i) {
-                const uint16_t e = c_bnd[i];
-                const int a = (int)(e & 15u) - 1, b = (int)((e >> 4) & 15u) - 1, c = (int)(e >> 8) - 1;
-                const uint32_t s = sp[site_addr(P, o0, o1, o2, par, a, b, c)];
-                if (i < 32) bnd0 |= s << i;
-                else if (i < 64) bnd1 |= s << (i - 32);
-                else bnd2 |= s << (i - 64);
+        int o0 = 0, o1 = 0, o2 = 0, par = 0;
+        if (MODE == 0) {
+            // ------------------------------------------------------- 1. decode --------
+            if (valid) {
+                r = (int)(w / P.Pc);
+                q = w - (long long)r * P.Pc;
+                const int half1 = P.P1 >> 1;
+                const int tt = (int)(q % half1);
+                const long long row = q / half1;
+                const int pj = (int)(row % P.P2), pk = (int)(row / P.P2);
+                const int pi = 2 * tt + ((P.cls + pj + pk) & 1);
+                pidx = (uint32_t)(pi + P.P1 * (pj + P.P2 * pk));
+                t = P.lstep[r];
+                stream = P.stream_id[r];
+                const U4 ow = draw(0xFFFFFFFFu, t, stream, kLearn | (0xFFu << 8), P.seed);
+                const int ox = (int)(ow.x & 3u), oy = (int)((ow.x >> 2) & 3u), oz = (int)((ow.x >> 4) & 3u);
+                par = (ox + oy + oz) & 1;
+                o0 = 4 * pi + ox;
+                o1 = 4 * pj + oy;
+                o2 = 4 * pk + oz;
+                k4 = P.k4[P.slot_of_rep[r]];
             }
-            for (int k = 0; k < 32; ++k) {
-                const uint8_t e = c_site[k], f = c_site[32 + k];
-                ao |= (uint32_t)sp[site_addr(P, o0, o1, o2, par, e & 3, (e >> 2) & 3, e >> 4)] << k;
-                bo |= (uint32_t)sp[site_addr(P, o0, o1, o2, par, f & 3, (f >> 2) & 3, f >> 4)] << k;
+            s_org[tid] = (uint32_t)o0 | ((uint32_t)o1 << 10) | ((uint32_t)o2 << 20) | ((uint32_t)par << 30);
+            s_rep[tid] = valid ? r : -1;
+            __syncthreads();
+            // ------------------------------------------------------- 2. gather --------
+#pragma unroll 4
+            for (int j = 0; j < 32; ++j) {
+                const int pp = warp * 32 + j;
+                const int rr = s_rep[pp];
+                if (rr < 0) continue;  // warp-uniform
+                const uint32_t og = s_org[pp];
+                const int g0 = (int)(og & 1023u), g1 = (int)((og >> 10) & 1023u), g2 = (int)((og >> 20) & 1023u);
+                const int gp = (int)(og >> 30);
+                const uint8_t *sp = P.spins + (long long)rr * 2 * P.half;
+                uint32_t v[5];
+#pragma unroll
+                for (int c = 0; c < 5; ++c) {
+                    const uint32_t e = my_site[c];
+                    v[c] = sp[site_addr(P, g0, g1, g2, gp, (int)(e & 15u) - 1, (int)((e >> 4) & 15u) - 1,
+                                        (int)(e >> 8) - 1)];
+                }
+#pragma unroll
+                for (int c = 0; c < 5; ++c) {
+                    const uint32_t m = __ballot_sync(0xffffffffu, v[c] != 0);
+                    if (lane == c) s_bits[pp * 5 + c] = m;
+                }
             }
-            k4 = P.k4[P.slot_of_rep[r]];
+            __syncthreads();
+            if (valid) {
+                bnd0 = s_bits[tid * 5 + 0];
+                bnd1 = s_bits[tid * 5 + 1];
+                bnd2 = s_bits[tid * 5 + 2];
+                ao = s_bits[tid * 5 + 3];
+                bo = s_bits[tid * 5 + 4];
+            }
         }
-        // write this thread's 128-element row of the A tile (swizzled, 16 chunks of 8 BF16)
+        // ------------------------------------------------------------- 3. input row ------
 #pragma unroll 1
         for (int ch = 0; ch < 16; ++ch) {
             uint32_t pk4[4];
@@ -309,7 +371,7 @@ __global__ void __launch_bounds__(kThreads, 2) patch_kernel(PatchParams P) {
             uint8_t *dst = arow + (k >> 6) * 16384 + tc::swz(tid, k & 63);
             *reinterpret_cast<uint4 *>(dst) = make_uint4(pk4[0], pk4[1], pk4[2], pk4[3]);
         }
-        // --------------------------------------------------------------- three layers ----
+        // --------------------------------------------------------------- 4. layers -------
         float z[32];
 #pragma unroll 1
         for (int layer = 0; layer < 3 && ok; ++layer) {
@@ -383,58 +445,60 @@ __global__ void __launch_bounds__(kThreads, 2) patch_kernel(PatchParams P) {
 #pragma unroll
             for (int k = 0; k < 32; ++k) zo[k] = z[k];
         }
-        // --------------------------------------------------- Metropolis-Hastings step ----
+        // ---------------------------------------------- 5. Metropolis-Hastings step ----
+        // d = log q(new) - log q(old): A-sites that changed add +-z_k (log-odds), then the
+        // B-sites' heat-bath log probabilities (tables); log alpha = (0 - d) - beta J dB.
         const int slot = P.slot_of_rep[r];
         const uint32_t *TB = P.TB + 7 * slot;
         const float *LBup = P.LBup + 7 * slot, *LBdn = P.LBdn + 7 * slot;
         uint32_t an = 0, bn = 0;
-        float lqo = 0.0f, lqn = 0.0f;
+        float d = 0.0f;
         U4 rw{0, 0, 0, 0};
 #pragma unroll
         for (int k = 0; k < 32; ++k) {
             if ((k & 3) == 0) rw = draw(pidx, t, stream, kLearn | ((uint32_t)(k >> 2) << 16), P.seed);
             const uint32_t u = (k & 3) == 0 ? rw.x : (k & 3) == 1 ? rw.y : (k & 3) == 2 ? rw.z : rw.w;
-            const uint32_t T = thr_of_logit(z[k]);
-            const bool up = u < T;
+            const bool up = u < thr_of_logit(z[k]);
             an |= (up ? 1u : 0u) << k;
-            lqn += lq_of(T, up);
-            lqo += lq_of(T, ((ao >> k) & 1u) != 0);
+            if (up != (((ao >> k) & 1u) != 0)) d += up ? z[k] : -z[k];
         }
         int bond_n = 0, bond_o = 0;
-#pragma unroll 4
+#pragma unroll
         for (int m = 0; m < 32; ++m) {
             if ((m & 3) == 0) rw = draw(pidx, t, stream, kLearn | ((uint32_t)(8 + (m >> 2)) << 16), P.seed);
             const uint32_t u = (m & 3) == 0 ? rw.x : (m & 3) == 1 ? rw.y : (m & 3) == 2 ? rw.z : rw.w;
-            int nn = 0, no = 0;
+            // up-neighbour counts (the heat-bath table index (n + 6) / 2)
+            int qn = 0, qo = 0;
 #pragma unroll
             for (int qq = 0; qq < 6; ++qq) {
-                const int cd = c_Bn[m][qq];
+                const int cd = geo_bn(m, qq);
                 if (cd >= 0) {
-                    nn += ((an >> cd) & 1u) ? 1 : -1;
-                    no += ((ao >> cd) & 1u) ? 1 : -1;
+                    qn += (int)((an >> cd) & 1u);
+                    qo += (int)((ao >> cd) & 1u);
                 } else {
                     const int bi = -cd - 1;
                     const uint32_t wd = bi < 32 ? bnd0 : (bi < 64 ? bnd1 : bnd2);
-                    const int s = ((wd >> (bi & 31)) & 1u) ? 1 : -1;
-                    nn += s;
-                    no += s;
+                    const int sb = (int)((wd >> (bi & 31)) & 1u);
+                    qn += sb;
+                    qo += sb;
                 }
             }
-            const int qn = (nn + 6) >> 1, qo = (no + 6) >> 1;
+            const int nn = 2 * qn - 6, no = 2 * qo - 6;
             const bool up = u < TB[qn];
             bn |= (up ? 1u : 0u) << m;
-            lqn += up ? LBup[qn] : LBdn[qn];
             const bool upo = ((bo >> m) & 1u) != 0;
-            lqo += upo ? LBup[qo] : LBdn[qo];
+            const float lbn = up ? LBup[qn] : LBdn[qn];
+            const float lbo = upo ? LBup[qo] : LBdn[qo];
+            d += lbn - lbo;
             bond_n += (up ? 1 : -1) * nn;
             bond_o += (upo ? 1 : -1) * no;
         }
-#pragma unroll 4
+#pragma unroll
         for (int k = 0; k < 32; ++k) {
             int sb = 0;
 #pragma unroll
-            for (int qq = 0; qq < 3; ++qq) {
-                const int bi = c_Ab[k][qq];
+            for (int qq = 0; qq < 6; ++qq) {
+                const int bi = geo_ab(k, qq);
                 if (bi < 0) continue;
                 const uint32_t wd = bi < 32 ? bnd0 : (bi < 64 ? bnd1 : bnd2);
                 sb += ((wd >> (bi & 31)) & 1u) ? 1 : -1;
@@ -443,7 +507,7 @@ __global__ void __launch_bounds__(kThreads, 2) patch_kernel(PatchParams P) {
             bond_o += (((ao >> k) & 1u) ? 1 : -1) * sb;
         }
         rw = draw(pidx, t, stream, kLearn | (16u << 16), P.seed);
-        const float la = (lqo - lqn) - P.betaJf[slot] * (float)(bond_n - bond_o);
+        const float la = (0.0f - d) - P.betaJf[slot] * (float)(bond_n - bond_o);
         bool acc = la >= 0.0f;
         if (!acc) acc = u01(rw.x) < expf_neg(la);
         if (acc) {
@@ -653,6 +717,21 @@ __global__ void advance_lstep_kernel(uint32_t *c, int R) {
     if (r < R) c[r] += 1u;
 }
 
+static bool closed_forms_agree(const Geometry &g) {
+    for (int m = 0; m < 32; ++m) {
+        for (int q = 0; q < 6; ++q)
+            if (geo_bn(m, q) != g.Bn[m][q]) return false;
+        int n = 0;
+        for (int q = 0; q < 6; ++q) {
+            const int bi = geo_ab(m, q);
+            if (bi >= 0 && (n >= 3 || g.Ab[m][n++] != bi)) return false;
+        }
+        if (n < 3 && g.Ab[m][n] != -1) return false;
+        if ((g.site[m] & 3) != geo_a_a(m) || (g.site[32 + m] & 3) != geo_b_a(m)) return false;
+    }
+    return true;
+}
+
 }  // namespace learn
 }  // namespace ether
 
@@ -716,10 +795,9 @@ bool g_geometry_uploaded = false;
 int upload_geometry() {
     if (g_geometry_uploaded) return ETHER_OK;
     const Geometry g = make_geometry();
+    if (!closed_forms_agree(g)) return lfail(ETHER_ERR_CUDA, "learned proposal: inconsistent patch geometry");
     LCUDA(cudaMemcpyToSymbol(c_site, g.site, sizeof g.site));
     LCUDA(cudaMemcpyToSymbol(c_bnd, g.bnd, sizeof g.bnd));
-    LCUDA(cudaMemcpyToSymbol(c_Bn, g.Bn, sizeof g.Bn));
-    LCUDA(cudaMemcpyToSymbol(c_Ab, g.Ab, sizeof g.Ab));
     g_geometry_uploaded = true;
     return ETHER_OK;
 }
@@ -874,8 +952,8 @@ extern "C" int ether_learn_create(ether_ctx *h, const ether_learn_desc *d, ether
     // storage is the checkerboard split the kernels address arithmetically)
     if (c.model != ETHER_MODEL_ISING || c.L[0] <= 0 || c.nsp != 1 || c.nsh != 1 || c.zeeman)
         return lfail(ETHER_ERR_UNSUPPORTED, "learned proposal: simple-cubic Ising, one species, one shell, no Zeeman term");
-    if (c.L[0] % 8 || c.L[1] % 8 || c.L[2] % 8)
-        return lfail(ETHER_ERR_UNSUPPORTED, "learned proposal: every extent a multiple of 8");
+    if (c.L[0] % 8 || c.L[1] % 8 || c.L[2] % 8 || c.L[0] > 1016 || c.L[1] > 1016 || c.L[2] > 1016)
+        return lfail(ETHER_ERR_UNSUPPORTED, "learned proposal: every extent a multiple of 8, at most 1016");
     if (d->capacity < 1024) return lfail(ETHER_ERR_ARG, "training capacity below 1024 samples");
     int rc = upload_geometry();
     if (rc) return rc;
@@ -1030,6 +1108,43 @@ extern "C" int ether_learn_sweep(ether_learn *l, int32_t nsweeps) {
     l->timed = 1;
     l->timed_n = nsweeps;
     return ETHER_OK;
+}
+
+extern "C" int ether_learn_record_series(ether_learn *l, int32_t nsteps, int32_t plain_per_step,
+                                         int32_t learned_per_step, double *absM) {
+    if (!l || !absM) return lfail(ETHER_ERR_ARG, "null argument");
+    if (nsteps < 1 || plain_per_step < 0 || learned_per_step < 0 || plain_per_step + learned_per_step < 1)
+        return lfail(ETHER_ERR_ARG, "need nsteps >= 1 and at least one sweep per step");
+    Ctx &c = l->ctx->c;
+    if (!c.beta_set) return lfail(ETHER_ERR_STATE, "beta not set");
+    int rc = refresh_tables(*l);
+    if (rc) return rc;
+    const size_t bytes = sizeof(double) * (size_t)nsteps * l->R;
+    double *mser = nullptr;
+    LCUDA(cudaMalloc((void **)&mser, bytes));
+    for (int t = 0; t < nsteps && rc == ETHER_OK; ++t) {
+        for (int k = 0; k < plain_per_step && rc == ETHER_OK; ++k) rc = plain_sweep(c);
+        for (int k = 0; k < learned_per_step && rc == ETHER_OK; ++k) {
+            for (int cls = 0; cls < 2 && rc == ETHER_OK; ++cls) rc = launch_patches(*l, cls, nullptr);
+            if (rc == ETHER_OK) {
+                advance_lstep_kernel<<<(l->R + 255) / 256, 256, 0, c.stream>>>(l->lstep, l->R);
+                l->launches++;
+                l->proposed += 2ull * (uint64_t)l->R * (uint64_t)l->Pc;
+            }
+        }
+        if (rc == ETHER_OK) {
+            const cudaError_t e = launch_record(c, t, false, mser, nullptr);
+            if (e != cudaSuccess) rc = lfail(ETHER_ERR_CUDA, std::string("record: ") + cudaGetErrorString(e));
+        }
+    }
+    if (rc == ETHER_OK) {
+        cudaError_t e = cudaMemcpyAsync(absM, mser, bytes, cudaMemcpyDeviceToHost, c.stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+        if (e != cudaSuccess) rc = lfail(ETHER_ERR_CUDA, std::string("series copy: ") + cudaGetErrorString(e));
+    }
+    cudaFree(mser);
+    if (rc) return rc;
+    return read_err(*l);
 }
 
 extern "C" int ether_learn_get_accepts(ether_learn *l, uint64_t *accepted) {

@@ -397,6 +397,13 @@ class Learned:
     def sweep_(self, nsweeps=1):
         abi.check(self.lib.ether_learn_sweep(self.h, nsweeps))
 
+    def record_series(self, nsteps, plain_per_step=1, learned_per_step=1):
+        """|M| of every replica after each step, shape (R, nsteps)."""
+        out = np.zeros((nsteps, self.sweep.R), dtype=np.float64)
+        abi.check(self.lib.ether_learn_record_series(self.h, nsteps, plain_per_step,
+                                                     learned_per_step, abi.dptr(out)))
+        return out.T.copy()
+
     def accepts(self):
         out = np.zeros(self.sweep.R, dtype=np.uint64)
         abi.check(self.lib.ether_learn_get_accepts(self.h, out.ctypes.data_as(abi.PU64)))

@@ -303,6 +303,11 @@ int ether_learn_collect(ether_learn *learn, int32_t per_replica);
 int ether_learn_train(ether_learn *learn, int32_t steps, int32_t batch, float lr, double *loss);
 /* nsweeps learned sweeps of every replica (asynchronous, on the context's stream). */
 int ether_learn_sweep(ether_learn *learn, int32_t nsweeps);
+/* Device-side series for tau_int: nsteps steps of plain_per_step Metropolis sweeps then
+ * learned_per_step learned sweeps, |M| of every replica after each step:
+ * absM(R, nsteps) host array, step-major (index = t*R + r). */
+int ether_learn_record_series(ether_learn *learn, int32_t nsteps, int32_t plain_per_step,
+                              int32_t learned_per_step, double *absM);
 /* Accepted patches per replica since creation (accepted(R)). */
 int ether_learn_get_accepts(ether_learn *learn, uint64_t *accepted);
 /* Parameters: W1(128,128), b1(128), W2(128,128), b2(128), W3(32,128), b3(32), FP32, row =

@@ -23,7 +23,10 @@
  *     neighbours (A-sites just drawn, boundary): up iff u < TB[n], TB from FP64 per
  *     temperature (table of the 7 neighbour sums);
  *   * accept with log alpha = (log q(old) - log q(new)) - beta J dB, dB the change of the
- *     patch's bond sum; log q sums A then B terms in site order in FP32.
+ *     patch's bond sum.  log q(new) - log q(old) = d, accumulated in FP32 in this order:
+ *     A-sites k = 0..31 that changed add +z_k (now up) or -z_k (now down) -- the log-odds
+ *     of the proposal, whose sampler realises sigmoid(z) to FP32 rounding and 2^-32 --, then
+ *     B-sites m = 0..31 add (log q_B(new_m) - log q_B(old_m)); log alpha = (0 - d) - beta J dB.
  */
 #include <math.h>
 #include <stdint.h>
@@ -265,13 +268,11 @@ float orc_logf_own(float x) {
     return fmaf((float)e, 0.693147182f, lm);
 }
 
+/* sigmoid(z) = r or e r with e = exp(-|z|), r = 1 / (1 + e) correctly rounded */
 static float sigmoid_own(float z) {
-    if (z >= 0.0f) {
-        const float e = orc_expf_neg(-z);
-        return 1.0f / (1.0f + e);
-    }
-    const float e = orc_expf_neg(z);
-    return e / (1.0f + e);
+    const float e = orc_expf_neg(-fabsf(z));
+    const float r = 1.0f / (1.0f + e);
+    return z >= 0.0f ? r : e * r;
 }
 
 static uint32_t thr_of_logit(float z) {
@@ -279,11 +280,6 @@ static uint32_t thr_of_logit(float z) {
     if (t < 1.0f) t = 1.0f;
     if (t > 4294967040.0f) t = 4294967040.0f;
     return (uint32_t)t;
-}
-
-static float lq_of(uint32_t T, int up) {
-    if (up) return orc_logf_own((float)T * 2.3283064365386963e-10f);
-    return orc_logf_own((float)(4294967296ull - (uint64_t)T) * 2.3283064365386963e-10f);
 }
 
 static uint32_t word_of(const uint32_t w[4], int i) { return w[i & 3]; }
@@ -327,15 +323,14 @@ static int patch_update(uint8_t *sp, const int L[3], const int off[3], int pi, i
     uint32_t bnd[3], ao, bo;
     orc_patch_gather(sp, L, off, pi, pj, pk, 0.0f, NULL, bnd, &ao, &bo);
     uint32_t an = 0, bn = 0;
-    float lqo = 0.0f, lqn = 0.0f;
+    float d = 0.0f;
     uint32_t w[4];
     for (int k = 0; k < 32; ++k) {
         if ((k & 3) == 0) draw4(pidx, t, stream, K_LEARN | ((uint32_t)(k >> 2) << 16), seed, w);
         const uint32_t T = thr_of_logit(z[k]);
         const int up = word_of(w, k) < T;
         if (up) an |= 1u << k;
-        lqn += lq_of(T, up);
-        lqo += lq_of(T, (int)((ao >> k) & 1u));
+        if (up != (int)((ao >> k) & 1u)) d += up ? z[k] : -z[k];
     }
     int bond_o = 0, bond_n = 0;
     for (int m = 0; m < 32; ++m) {
@@ -356,9 +351,10 @@ static int patch_update(uint8_t *sp, const int L[3], const int off[3], int pi, i
         const int qn = (nn + 6) >> 1, qo = (no + 6) >> 1;
         const int up = word_of(w, m) < TB[qn];
         if (up) bn |= 1u << m;
-        lqn += up ? LBup[qn] : LBdn[qn];
         const int upo = (int)((bo >> m) & 1u);
-        lqo += upo ? LBup[qo] : LBdn[qo];
+        const float lbn = up ? LBup[qn] : LBdn[qn];
+        const float lbo = upo ? LBup[qo] : LBdn[qo];
+        d += lbn - lbo;
         bond_n += (up ? 1 : -1) * nn;
         bond_o += (upo ? 1 : -1) * no;
     }
@@ -373,7 +369,7 @@ static int patch_update(uint8_t *sp, const int L[3], const int off[3], int pi, i
         bond_o += (((ao >> k) & 1u) ? 1 : -1) * sb;
     }
     draw4(pidx, t, stream, K_LEARN | (16u << 16), seed, w);
-    const float la = (lqo - lqn) - betaJf * (float)(bond_n - bond_o);
+    const float la = (0.0f - d) - betaJf * (float)(bond_n - bond_o);
     int acc = la >= 0.0f;
     if (!acc) acc = (float)(w[0] >> 8) * 5.9604644775390625e-08f < orc_expf_neg(la);
     if (acc) {

@@ -183,3 +183,16 @@ def test_training_raises_acceptance():
     assert rates[1] > 3.0 * rates[0] and rates[1] > 0.02, rates
     trained.close()
     untrained.close()
+
+
+def test_learned_series_recorder():
+    """The device-side series ends at the configuration the context holds afterwards."""
+    lat, sw, _ = ising(16, 8, KTC, seed=41)
+    lr = eg.Learned(sw, seed=3, capacity=4096)
+    m = lr.record_series(25, 1, 1)
+    assert m.shape == (8, 25)
+    np.testing.assert_allclose(m[:, -1], np.linalg.norm(sw.tot_magnetisation(), axis=1), rtol=1e-12)
+    assert lr.info().proposed == 25 * 2 * 8 * lr.info().patches_per_class
+    m2 = lr.record_series(5, 0, 2)
+    assert m2.shape == (8, 5)
+    lr.close()
