@@ -899,13 +899,27 @@ extern "C" int ether_end_sweep(ether_ctx *h) {
 #include <mutex>
 namespace {
 std::mutex g_tune_mu;
-std::map<std::vector<long>, std::pair<int, int>> g_tune_cache;
+std::map<std::vector<long>, int> g_tune_cache;  // variant per (model, L, R)
 }  // namespace
+
+static int variant_of(const Ctx &c) { return (c.ising_persist ? 1000 : 0) + c.vec_bytes * 10 + c.ising_vpt; }
+
+// variant = 1000 (persistent kernel) + 10 * bytes per vector + vectors per thread
+static bool apply_variant(Ctx &c, int variant) {
+    const bool p = variant >= 1000;
+    const int rest = variant % 1000, w = rest / 10, v = rest % 10;
+    if ((w != 8 && w != 16) || (c.L[0] / 2) % w) return false;
+    if (p ? (v != 2 && v != 4) : (v != 1 && v != 2 && v != 4)) return false;
+    c.ising_persist = p;
+    c.vec_bytes = w;
+    c.ising_vpt = v;
+    return true;
+}
 
 extern "C" int ether_autotune(ether_ctx *h, int32_t *variant, float *best_ms) {
     if (!h) return fail(ETHER_ERR_ARG, "null context");
     Ctx &c = h->c;
-    if (variant) *variant = c.vec_bytes * 10 + c.ising_vpt;
+    if (variant) *variant = variant_of(c);
     if (best_ms) *best_ms = 0.f;
     if (!c.fast || c.model != ETHER_MODEL_ISING) return ETHER_OK;
     if (!c.beta_set) return fail(ETHER_ERR_STATE, "beta not set");
@@ -914,9 +928,8 @@ extern "C" int ether_autotune(ether_ctx *h, int32_t *variant, float *best_ms) {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_tune_cache.find(key);
         if (it != g_tune_cache.end()) {
-            c.vec_bytes = it->second.first;
-            c.ising_vpt = it->second.second;
-            if (variant) *variant = c.vec_bytes * 10 + c.ising_vpt;
+            apply_variant(c, it->second);
+            if (variant) *variant = variant_of(c);
             return ETHER_OK;
         }
     }
@@ -928,39 +941,32 @@ extern "C" int ether_autotune(ether_ctx *h, int32_t *variant, float *best_ms) {
     CUDA_TRY(cudaMemcpyAsync(backup, c.spins, bytes, cudaMemcpyDeviceToDevice, c.stream));
     CUDA_TRY(cudaMemcpyAsync(acc_backup, c.acc_count, sizeof(unsigned long long) * c.R,
                              cudaMemcpyDeviceToDevice, c.stream));
-    const int H = c.L[0] / 2;
-    int best_w = c.vec_bytes, best_v = c.ising_vpt;
+    int best_var = variant_of(c);
     float best = 1e30f;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    for (int w : {16, 8}) {
-        if (H % w) continue;
-        for (int v : {1, 2, 4}) {
-            c.vec_bytes = w;
-            c.ising_vpt = v;
-            CUDA_TRY(launch_ising_sweep(c, 0));  // warm-up
-            CUDA_TRY(cudaEventRecord(e0, c.stream));
-            for (int k = 0; k < 3; ++k) {
-                CUDA_TRY(launch_ising_sweep(c, 0));
-                CUDA_TRY(launch_ising_sweep(c, 1));
-            }
-            CUDA_TRY(cudaEventRecord(e1, c.stream));
-            CUDA_TRY(cudaEventSynchronize(e1));
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, e0, e1);
-            ms /= 6.0f;
-            if (ms < best) {
-                best = ms;
-                best_w = w;
-                best_v = v;
-            }
+    for (int cand : {161, 162, 164, 81, 82, 84, 1162, 1164, 1082, 1084}) {
+        if (!apply_variant(c, cand)) continue;
+        CUDA_TRY(launch_ising_sweep(c, 0));  // warm-up
+        CUDA_TRY(cudaEventRecord(e0, c.stream));
+        for (int k = 0; k < 3; ++k) {
+            CUDA_TRY(launch_ising_sweep(c, 0));
+            CUDA_TRY(launch_ising_sweep(c, 1));
+        }
+        CUDA_TRY(cudaEventRecord(e1, c.stream));
+        CUDA_TRY(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        ms /= 6.0f;
+        if (ms < best) {
+            best = ms;
+            best_var = cand;
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    c.vec_bytes = best_w;
-    c.ising_vpt = best_v;
+    apply_variant(c, best_var);
     CUDA_TRY(cudaMemcpyAsync(c.spins, backup, bytes, cudaMemcpyDeviceToDevice, c.stream));
     CUDA_TRY(cudaMemcpyAsync(c.acc_count, acc_backup, sizeof(unsigned long long) * c.R,
                              cudaMemcpyDeviceToDevice, c.stream));
@@ -969,9 +975,9 @@ extern "C" int ether_autotune(ether_ctx *h, int32_t *variant, float *best_ms) {
     cudaFree(acc_backup);
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
-        g_tune_cache[key] = {best_w, best_v};
+        g_tune_cache[key] = best_var;
     }
-    if (variant) *variant = best_w * 10 + best_v;
+    if (variant) *variant = best_var;
     if (best_ms) *best_ms = best;
     return ETHER_OK;
 }
@@ -980,11 +986,7 @@ extern "C" int ether_set_variant(ether_ctx *h, int32_t variant) {
     if (!h) return fail(ETHER_ERR_ARG, "null context");
     Ctx &c = h->c;
     if (!c.fast || c.model != ETHER_MODEL_ISING) return ETHER_OK;
-    const int w = variant / 10, v = variant % 10;
-    if ((w != 8 && w != 16) || (v != 1 && v != 2 && v != 4) || (c.L[0] / 2) % w)
-        return fail(ETHER_ERR_ARG, "variant not available for this lattice");
-    c.vec_bytes = w;
-    c.ising_vpt = v;
+    if (!apply_variant(c, variant)) return fail(ETHER_ERR_ARG, "variant not available for this lattice");
     return ETHER_OK;
 }
 

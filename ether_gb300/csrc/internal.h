@@ -84,6 +84,7 @@ struct Ctx {
     int32_t *rep_of_slot = nullptr;  // R (group*n_slots + slot -> replica)
     uint32_t *thr = nullptr;     // n_slots * table_entries: flip iff u32 <= thr
     int ising_vpt = 1;           // vectors per thread of the simple-cubic Ising kernel
+    bool ising_persist = false;  // persistent simple-cubic Ising kernel
     uint32_t *stream_id = nullptr;  // R
     uint32_t *step = nullptr;       // R (Metropolis sweep counter)
     uint32_t *ovrr_step = nullptr;  // R

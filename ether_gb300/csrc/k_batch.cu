@@ -105,9 +105,9 @@ batch_phase_kernel(const BatchMember *__restrict__ members, const BatchSeg *__re
             for (int j = 0; j < upt; ++j) {
                 const int v = (int)S.first + (int)threadIdx.x + j * (int)blockDim.x;
                 if (kind == kBIsing16)
-                    acc += ising_sc_vectors<16, 1>(A, v, 0, end, s_th[warp], s_tl[warp], t, stream, c3, m.seed, m.K);
+                    acc += byte_sum(ising_sc_vectors<16, 1>(A, v, 0, end, s_th[warp], s_tl[warp], t, stream, c3, m.seed, m.K));
                 else
-                    acc += ising_sc_vectors<8, 1>(A, v, 0, end, s_th[warp], s_tl[warp], t, stream, c3, m.seed, m.K);
+                    acc += byte_sum(ising_sc_vectors<8, 1>(A, v, 0, end, s_th[warp], s_tl[warp], t, stream, c3, m.seed, m.K));
             }
         } else if (kind == kBIsingCsr) {
             const int off = m.col_off[colour];

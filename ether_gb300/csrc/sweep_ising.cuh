@@ -104,13 +104,21 @@ __device__ __forceinline__ void stv(uint8_t *p, const Vec<W> &v) {
     }
 }
 
-// Sites of word q whose high random halves tie with the threshold's high half: decided by
-// the low halves (block 1 of the group).  Returns the XOR mask of the extra flips.  Kept
-// out of line: it runs for about one word in 16000 and must not cost the hot loop registers.
+// Sites of word q (odd: words 1, 3 of the group's blocks) whose high random halves tie with
+// their threshold's high half: decided by the low halves (block 1 of the group).  Returns
+// the XOR mask of the extra flips.  Kept out of line: it runs for about one vector in 4000
+// and must not cost the hot loop registers.
 __device__ __noinline__ inline uint32_t resolve_ties(uint32_t grp, uint32_t t, uint32_t stream,
                                                      uint32_t c3, uint32_t seed, int odd,
-                                                     uint32_t tie, uint32_t e4s,
+                                                     uint32_t e4s, const uint32_t *s_th,
                                                      const uint32_t *s_tl) {
+    const U4 rh = draw(grp, t, stream, c3, seed);
+    const uint32_t ha = odd ? rh.z : rh.x, hb = odd ? rh.w : rh.y;
+    const uint32_t h[4] = {ha & 0xFFFFu, ha >> 16, hb & 0xFFFFu, hb >> 16};
+    uint32_t tie = 0;
+    for (int k = 0; k < 4; ++k)
+        if (h[k] == s_th[((e4s >> (8 * k)) & 0xFFu) >> 2]) tie |= 1u << k;
+    if (!tie) return 0;
     const U4 rl = draw(grp, t, stream, c3 | (1u << 16), seed);
     const uint32_t la = odd ? rl.z : rl.x, lb = odd ? rl.w : rl.y;
     const uint32_t l[4] = {la & 0xFFFFu, la >> 16, lb & 0xFFFFu, lb >> 16};
@@ -128,11 +136,34 @@ struct IsingSc {
     uint32_t colour;
 };
 
+// Word q of a vector: the four sites' threshold byte offsets (4 (n + 7 s)), given the own
+// spins s0 and the six neighbour words.
+template <int W>
+__device__ __forceinline__ uint32_t sc_e4s(const Vec<W> &o0, uint32_t edge, int par, const Vec<W> &a,
+                                           const Vec<W> &b, const Vec<W> &c, const Vec<W> &d, int q,
+                                           uint32_t s0) {
+    constexpr int NW = W / 4;
+    uint32_t sh;
+    if (par == 0) {  // neighbour x-1 -> xh-1: window shifted up by one byte
+        const uint32_t lo = (q == 0) ? (edge << 24) : o0.w[q > 0 ? q - 1 : 0];
+        sh = __funnelshift_l(lo, o0.w[q], 8);
+    } else {         // neighbour x+1 -> xh+1: window shifted down by one byte
+        const uint32_t hi = (q == NW - 1) ? edge : o0.w[q < NW - 1 ? q + 1 : q];
+        sh = __funnelshift_r(o0.w[q], hi, 8);
+    }
+    const uint32_t n = o0.w[q] + sh + a.w[q] + b.w[q] + c.w[q] + d.w[q];
+    // bytewise 4*(n + 7 s) <= 52: the byte offsets of the thresholds in s_th
+    return (n + (s0 << 3) - s0) << 2;
+}
+
 // VPT vectors of W bytes per thread, vector indices vfirst + j*vstride (j < VPT, < nvec),
 // one after another.  s_th / s_tl: the 14 thresholds' high / low halves in shared memory.
-// Returns the number of flips.
+// Returns the flips as bytewise counts (each byte <= 4 VPT; sum the bytes for the total).
+// A site whose high random half ties with its threshold's high half (probability 2^-16) is
+// decided by the low halves; whether any of a vector's sites tie is checked once per vector,
+// and the rare vector with a tie is finished by resolve_ties.
 template <int W, int VPT>
-__device__ __forceinline__ unsigned ising_sc_vectors(const IsingSc &A, int vfirst, int vstride,
+__device__ __forceinline__ uint32_t ising_sc_vectors(const IsingSc &A, int vfirst, int vstride,
                                                      int nvec, const uint32_t *s_th,
                                                      const uint32_t *s_tl, uint32_t t,
                                                      uint32_t stream, uint32_t c3, uint32_t seed,
@@ -141,7 +172,7 @@ __device__ __forceinline__ unsigned ising_sc_vectors(const IsingSc &A, int vfirs
     constexpr int NW = W / 4;
     const char *th_bytes = reinterpret_cast<const char *>(s_th);
     const int H = A.H, L2 = A.L2, L3 = A.L3;
-    unsigned flips = 0;
+    uint32_t cnt = 0;
 #pragma unroll
     for (int j = 0; j < VPT; ++j) {
         const int v = vfirst + j * vstride;
@@ -154,7 +185,7 @@ __device__ __forceinline__ unsigned ising_sc_vectors(const IsingSc &A, int vfirs
         const int par = (y + z + (int)A.colour) & 1;
         const int ym = (y == 0 ? L2 - 1 : y - 1), yp = (y == L2 - 1 ? 0 : y + 1);
         const int zm = (z == 0 ? L3 - 1 : z - 1), zp = (z == L3 - 1 ? 0 : z + 1);
-        Vec<W> me = ldv<W>(A.own_a + rho0);
+        const Vec<W> me = ldv<W>(A.own_a + rho0);
         const Vec<W> o0 = ldv<W>(A.opp + rho0);
         const Vec<W> a = ldv<W>(A.opp + (z * L2 + ym) * H + xh0);
         const Vec<W> b = ldv<W>(A.opp + (z * L2 + yp) * H + xh0);
@@ -162,43 +193,49 @@ __device__ __forceinline__ unsigned ising_sc_vectors(const IsingSc &A, int vfirs
         const Vec<W> d = ldv<W>(A.opp + (zp * L2 + y) * H + xh0);
         const uint32_t edge = par == 0 ? A.opp[row * H + (xh0 == 0 ? H - 1 : xh0 - 1)]
                                        : A.opp[row * H + (xh0 + W == H ? 0 : xh0 + W)];
+        Vec<W> out;
+        uint32_t e4[NW];
+        bool tie = false;
         U4 rh{0, 0, 0, 0};
 #pragma unroll
         for (int q = 0; q < NW; ++q) {
-            const uint32_t grp = (uint32_t)((rho0 >> 3) + (q >> 1));
-            if ((q & 1) == 0) rh = draw_rk(grp, t, stream, c3, K);
-            uint32_t sh;
-            if (par == 0) {  // neighbour x-1 -> xh-1: window shifted up by one byte
-                const uint32_t lo = (q == 0) ? (edge << 24) : o0.w[q - 1];
-                sh = __funnelshift_l(lo, o0.w[q], 8);
-            } else {         // neighbour x+1 -> xh+1: window shifted down by one byte
-                const uint32_t hi = (q == NW - 1) ? edge : o0.w[q + 1];
-                sh = __funnelshift_r(o0.w[q], hi, 8);
-            }
+            if ((q & 1) == 0) rh = draw_rk((uint32_t)((rho0 >> 3) + (q >> 1)), t, stream, c3, K);
             const uint32_t s0 = me.w[q];
-            const uint32_t n = o0.w[q] + sh + a.w[q] + b.w[q] + c.w[q] + d.w[q];
-            // bytewise 4*(n + 7 s) <= 52: the byte offsets of the thresholds in s_th
-            const uint32_t e4s = (n + (s0 << 3) - s0) << 2;
+            const uint32_t e4s = sc_e4s<W>(o0, edge, par, a, b, c, d, q, s0);
+            e4[q] = e4s;
             const uint32_t t0 = *reinterpret_cast<const uint32_t *>(th_bytes + (e4s & 0xFFu));
             const uint32_t t1 = *reinterpret_cast<const uint32_t *>(th_bytes + __byte_perm(e4s, 0, 0x4441));
             const uint32_t t2 = *reinterpret_cast<const uint32_t *>(th_bytes + __byte_perm(e4s, 0, 0x4442));
             const uint32_t t3 = *reinterpret_cast<const uint32_t *>(th_bytes + (e4s >> 24));
             const uint32_t wa = (q & 1) ? rh.z : rh.x, wb = (q & 1) ? rh.w : rh.y;
             const uint32_t u0 = wa & 0xFFFFu, u1 = wa >> 16, u2 = wb & 0xFFFFu, u3 = wb >> 16;
-            uint32_t out = s0;
-            if (u0 < t0) out ^= 0x00000001u;
-            if (u1 < t1) out ^= 0x00000100u;
-            if (u2 < t2) out ^= 0x00010000u;
-            if (u3 < t3) out ^= 0x01000000u;
-            const uint32_t tie = (u0 == t0 ? 1u : 0u) | (u1 == t1 ? 2u : 0u) |
-                                 (u2 == t2 ? 4u : 0u) | (u3 == t3 ? 8u : 0u);
-            if (tie) out ^= resolve_ties(grp, t, stream, c3, seed, q & 1, tie, e4s, s_tl);
-            flips += __popc(out ^ s0);
-            me.w[q] = out;
+            uint32_t m = 0;
+            if (u0 < t0) m |= 0x00000001u;
+            if (u1 < t1) m |= 0x00000100u;
+            if (u2 < t2) m |= 0x00010000u;
+            if (u3 < t3) m |= 0x01000000u;
+            tie |= (u0 == t0) | (u1 == t1) | (u2 == t2) | (u3 == t3);
+            out.w[q] = s0 ^ m;
+            cnt += m;
         }
-        stv<W>(A.own_a + rho0, me);
+        if (tie) {
+#pragma unroll
+            for (int q = 0; q < NW; ++q) {
+                const uint32_t m = resolve_ties((uint32_t)((rho0 >> 3) + (q >> 1)), t, stream, c3, seed,
+                                                q & 1, e4[q], s_th, s_tl);
+                out.w[q] ^= m;
+                cnt += m;
+            }
+        }
+        stv<W>(A.own_a + rho0, out);
     }
-    return flips;
+    return cnt;
+}
+
+// Sum of the four byte lanes (each <= 255).
+__device__ __forceinline__ unsigned byte_sum(uint32_t cnt) {
+    const uint32_t x = (cnt & 0x00FF00FFu) + ((cnt >> 8) & 0x00FF00FFu);
+    return (x & 0xFFFFu) + (x >> 16);
 }
 
 // Loads a replica's 14 simple-cubic thresholds into shared memory (all threads call it).

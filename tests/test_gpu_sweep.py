@@ -53,7 +53,7 @@ def test_ising_sc_bit_exact(L, flags, kT):
         assert sw.info().fast_path == 1
 
 
-@pytest.mark.parametrize("variant", [161, 162, 164, 81, 82, 84])
+@pytest.mark.parametrize("variant", [161, 162, 164, 81, 82, 84, 1162, 1164, 1082, 1084])
 def test_ising_sc_every_kernel_variant_bit_exact(variant):
     lat = eg.simple_cubic((32, 8, 6))
     sw, ion, g, ao, ag = ising_replay(lat, FM, 4.511, 8, variant=variant)
