@@ -192,7 +192,7 @@ void free_ctx(Ctx &c) {
                     c.t.mweight, c.t.site_of_storage, c.spins, c.spins4, c.beta_slot,
                     c.beta_slot_f, c.slot_of_rep, c.rep_of_slot, c.thr, c.stream_id,
                     c.step, c.ovrr_step, c.fresh_call, c.acc_count, c.E, c.M, c.sums,
-                    c.partials, c.pt_accepts, c.swap_dev, c.copy_from};
+                    c.partials, c.pt_accepts, c.swap_dev, c.copy_from, c.err};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto &kv : c.graphs) cudaGraphExecDestroy(kv.second);
@@ -426,6 +426,8 @@ extern "C" int ether_create(const ether_desc *d, ether_ctx **out) {
     TRY(dev_alloc(c, &c.partials, (size_t)c.R * c.partial_blocks * 5));
     TRY(dev_alloc(c, &c.pt_accepts, 1));
     TRY(dev_alloc(c, &c.swap_dev, 1));
+    TRY(dev_alloc(c, &c.err, 1));
+    CUDA_TRY(cudaMemset(c.err, 0, sizeof(int)));
     TRY(dev_alloc(c, &c.copy_from, c.R));
 #undef TRY
     std::vector<uint32_t> sid(c.R);
@@ -866,6 +868,12 @@ extern "C" int ether_get_colouring(ether_ctx *h, int32_t *colour, int32_t *rank_
 extern "C" int ether_sync(ether_ctx *h) {
     if (!h) return fail(ETHER_ERR_ARG, "null context");
     CUDA_TRY(cudaStreamSynchronize(h->c.stream));
+    int e = 0;
+    CUDA_TRY(cudaMemcpy(&e, h->c.err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+        CUDA_TRY(cudaMemset(h->c.err, 0, sizeof(int)));
+        return fail(ETHER_ERR_TIMEOUT, "a staged sweep kernel's bounded wait ran out (code " + std::to_string(e) + ")");
+    }
     return ETHER_OK;
 }
 
@@ -902,15 +910,34 @@ std::mutex g_tune_mu;
 std::map<std::vector<long>, int> g_tune_cache;  // variant per (model, L, R)
 }  // namespace
 
-static int variant_of(const Ctx &c) { return (c.ising_persist ? 1000 : 0) + c.vec_bytes * 10 + c.ising_vpt; }
+static int variant_of(const Ctx &c) {
+    if (c.ising_stream) return 4000 + 10 * c.ising_vpt + (c.ising_cap ? 4 : 1);
+    return (c.ising_persist ? 1000 : 0) + (c.ising_cap ? 2000 : 0) + c.vec_bytes * 10 + c.ising_vpt;
+}
 
-// variant = 1000 (persistent kernel) + 10 * bytes per vector + vectors per thread
+// variant = 1000 (persistent kernel) + 2000 (register cap: four 256-thread blocks per SM)
+//           + 10 * bytes per vector + vectors per thread
+//           or 4000 + 10 * vectors per thread and step + 1 / 4 (register cap): the
+//           shared-memory staged kernel (4011, 4014, 4021, 4041)
 static bool apply_variant(Ctx &c, int variant) {
-    const bool p = variant >= 1000;
+    if (variant == 4011 || variant == 4014 || variant == 4021 || variant == 4041) {
+        const int vs = (variant / 10) % 10;
+        if (!ising_stream_supported(c, vs)) return false;
+        c.ising_stream = true;
+        c.ising_cap = variant % 10 == 4;
+        c.vec_bytes = 16;
+        c.ising_vpt = vs;
+        return true;
+    }
+    if (variant < 0 || variant >= 4000) return false;
+    c.ising_stream = false;
+    const bool p = (variant / 1000) & 1, cap = (variant / 1000) >= 2;
     const int rest = variant % 1000, w = rest / 10, v = rest % 10;
     if ((w != 8 && w != 16) || (c.L[0] / 2) % w) return false;
     if (p ? (v != 2 && v != 4) : (v != 1 && v != 2 && v != 4)) return false;
+    if (cap && (w != 16 || v == 1)) return false;
     c.ising_persist = p;
+    c.ising_cap = cap;
     c.vec_bytes = w;
     c.ising_vpt = v;
     return true;
@@ -946,7 +973,8 @@ extern "C" int ether_autotune(ether_ctx *h, int32_t *variant, float *best_ms) {
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    for (int cand : {161, 162, 164, 81, 82, 84, 1162, 1164, 1082, 1084}) {
+    for (int cand : {161, 162, 164, 81, 82, 84, 2162, 2164, 1162, 1164, 1082, 1084, 3162, 3164, 4011,
+                     4014, 4021, 4041}) {
         if (!apply_variant(c, cand)) continue;
         CUDA_TRY(launch_ising_sweep(c, 0));  // warm-up
         CUDA_TRY(cudaEventRecord(e0, c.stream));

@@ -85,6 +85,9 @@ struct Ctx {
     uint32_t *thr = nullptr;     // n_slots * table_entries: flip iff u32 <= thr
     int ising_vpt = 1;           // vectors per thread of the simple-cubic Ising kernel
     bool ising_persist = false;  // persistent simple-cubic Ising kernel
+    bool ising_cap = false;      // register-capped (four blocks per SM) instantiation
+    bool ising_stream = false;   // shared-memory staged simple-cubic Ising kernel
+    int *err = nullptr;          // device: first bounded-wait failure of a kernel (0 = none)
     uint32_t *stream_id = nullptr;  // R
     uint32_t *step = nullptr;       // R (Metropolis sweep counter)
     uint32_t *ovrr_step = nullptr;  // R
@@ -107,6 +110,7 @@ struct Ctx {
 
 // kernel launchers (k_*.cu)
 cudaError_t launch_ising_sweep(Ctx &c, int colour);
+bool ising_stream_supported(const Ctx &c, int vectors_per_step);
 cudaError_t launch_xyz_sweep(Ctx &c, int colour);
 cudaError_t launch_overrelax(Ctx &c, int colour, int pass, float part);
 cudaError_t launch_fresh(Ctx &c);

@@ -2,6 +2,7 @@
 #include <algorithm>
 
 #include "sweep_ising.cuh"
+#include "tc_util.cuh"
 
 namespace ether {
 
@@ -27,8 +28,8 @@ ising_csr_kernel(uint8_t *__restrict__ spins, int N, int col_off, int n_c, uint3
     warp_add_count(acc_count + r, acc);
 }
 
-template <int W, int VPT>
-__global__ void __launch_bounds__(256)
+template <int W, int VPT, int MINB>
+__global__ void __launch_bounds__(256, MINB)
 ising_sc_kernel(uint8_t *__restrict__ spins, int L1, int L2, int L3, FastDiv fH, FastDiv fL2,
                 uint32_t colour, const uint32_t *__restrict__ thr, int table_entries,
                 const int32_t *__restrict__ slot_of_rep, const uint32_t *__restrict__ stream_id,
@@ -53,8 +54,8 @@ ising_sc_kernel(uint8_t *__restrict__ spins, int L1, int L2, int L3, FastDiv fH,
 // [b items / G, (b + 1) items / G), an item being VPT x 256 vectors of one replica.  The
 // thresholds sit in a per-warp slot of shared memory, reloaded when the replica changes, so
 // no block barrier is needed; flips are counted per replica and added at each change.
-template <int W, int VPT>
-__global__ void __launch_bounds__(256)
+template <int W, int VPT, int MINB>
+__global__ void __launch_bounds__(256, MINB)
 ising_sc_persist(uint8_t *__restrict__ spins, int L1, int L2, int L3, FastDiv fH, FastDiv fL2,
                  uint32_t colour, const uint32_t *__restrict__ thr, int table_entries,
                  const int32_t *__restrict__ slot_of_rep, const uint32_t *__restrict__ stream_id,
@@ -102,28 +103,213 @@ ising_sc_persist(uint8_t *__restrict__ spins, int L1, int L2, int L3, FastDiv fH
     if (cur >= 0) warp_add_count(acc_count + cur, byte_sum(cnt));
 }
 
-template <int W, int VPT>
+// ---------------------------------------------------------- shared-memory staged form ----
+// Persistent; block b owns the contiguous run of steps [b T / G, (b + 1) T / G) of the
+// replica-major step sequence (T = R x steps per replica).  A step is S = 4096 / H rows of the
+// updated colour (256 threads x 16 bytes).  The other colour's rows that a step reads -- its
+// own rows and L2 rows either side (y +- 1 in the same plane, z +- 1) -- are streamed by
+// cp.async.bulk into a ring of P stages of S rows (4 KB each) completing on one mbarrier per
+// stage, issued P stages ahead by thread 0; the own spins are loaded from global memory one
+// step ahead into registers.  All six neighbour words then come from shared memory.
+// Requires H = L1 / 2 a power of two >= 16, S dividing L2 L3, and a ring of at most 160 KB.
+struct StreamGeo {
+    int L1, L2, L3, H, S, rows, spr, h, P;  // rows = L2 L3, spr = rows / S, h = ceil(2 L2 / S)
+    FastDiv fL2;
+};
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(dst), "l"(src), "r"(bytes), "r"(bar) : "memory");
+}
+
+template <int VS, int MINB>
+__global__ void __launch_bounds__(256, MINB)
+ising_sc_stream(uint8_t *__restrict__ spins, StreamGeo G, uint32_t colour,
+                const uint32_t *__restrict__ thr, int table_entries,
+                const int32_t *__restrict__ slot_of_rep, const uint32_t *__restrict__ stream_id,
+                const uint32_t *__restrict__ step, uint32_t seed, const RoundKeys K, int R,
+                unsigned long long *__restrict__ acc_count, int *__restrict__ err) {
+    extern __shared__ __align__(128) uint8_t ring[];  // P stages of S rows, then P mbarriers
+    __shared__ uint32_t s_th[8][16], s_tl[8][16];
+    const int stage_bytes = G.S * G.H;  // VS x 4096
+    uint64_t *full = reinterpret_cast<uint64_t *>(ring + (size_t)G.P * stage_bytes);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const long long T = (long long)R * G.spr;
+    const long long g0 = T * blockIdx.x / gridDim.x, g1 = T * (blockIdx.x + 1) / gridDim.x;
+    if (g0 >= g1) return;  // block-uniform
+    if (tid == 0) {
+        for (int i = 0; i < G.P; ++i) tc::mbar_init(tc::smem_u32(&full[i]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const long long half = (long long)G.H * G.rows;
+    const uint32_t ring_rows_mask = (uint32_t)(G.P * G.S - 1);
+    const int vrow = G.H >> 4;                    // 16-byte vectors per row
+    const int dr = tid / vrow, xh0 = (tid - dr * vrow) * 16;
+    const int rows_per_pass = 256 / vrow;         // rows covered by one vector of every thread
+    const uint32_t c3 = kMetro | (colour << 8);
+    long long issued = 0, waited = 0;             // stages of this block, all segments
+    bool ok = true;
+    for (long long a = g0; a < g1 && ok;) {
+        // ------------------------------------------------------------ one segment ------
+        const int r = (int)(a / G.spr);
+        const long long e_seg = (long long)(r + 1) * G.spr < g1 ? (long long)(r + 1) * G.spr : g1;
+        const int j0 = (int)(a - (long long)r * G.spr), n = (int)(e_seg - a);
+        const int nst = n + G.h;                  // stages of this segment
+        const long long sbase = issued;           // block stage index of its stage 0
+        const int rho_a = j0 * G.S;               // first own row of the segment
+        uint8_t *own = spins + (long long)r * 2 * half + (long long)colour * half;
+        const uint8_t *opp = spins + (long long)r * 2 * half + (long long)(colour ^ 1u) * half;
+        auto issue = [&](int s) {                 // thread 0: ext rows [s S, (s + 1) S)
+            const long long gs = sbase + s;
+            const uint32_t slot = (uint32_t)(gs % G.P);
+            const uint32_t bar = tc::smem_u32(&full[slot]);
+            tc::mbar_arrive_tx(bar, (uint32_t)(G.S * G.H));
+            int row = rho_a - G.L2 + s * G.S;
+            row %= G.rows;
+            if (row < 0) row += G.rows;
+            const uint32_t dst = tc::smem_u32(ring + (size_t)slot * stage_bytes);
+            const int first = G.rows - row < G.S ? G.rows - row : G.S;
+            bulk_g2s(dst, opp + (long long)row * G.H, (uint32_t)(first * G.H), bar);
+            if (first < G.S) bulk_g2s(dst + first * G.H, opp, (uint32_t)((G.S - first) * G.H), bar);
+        };
+        if (tid == 0)
+            for (int s = 0; s < G.P && s < nst; ++s) issue(s);
+        issued += nst;
+        // thresholds of this replica in the warp's slot
+        __syncwarp();
+        if (lane < 14) {
+            const uint32_t Tv = thr[(size_t)slot_of_rep[r] * table_entries + lane];
+            s_th[warp][lane] = Tv >> 16;
+            s_tl[warp][lane] = Tv & 0xFFFFu;
+        }
+        __syncwarp();
+        const uint32_t t = step[r], stream = stream_id[r];
+        uint32_t cnt = 0;
+        Vec<16> me_next[VS];
+#pragma unroll
+        for (int u = 0; u < VS; ++u) me_next[u] = ldv<16>(own + (long long)(rho_a + dr + u * rows_per_pass) * G.H + xh0);
+        for (int j = 0; j < n; ++j) {
+            // stages j .. j + h must have landed
+            const long long need = sbase + j + G.h;
+            while (waited <= need) {
+                if (!tc::mbar_wait(tc::smem_u32(&full[waited % G.P]), (uint32_t)((waited / G.P) & 1), err, 1))
+                    ok = false;
+                ++waited;
+            }
+#pragma unroll
+            for (int u = 0; u < VS; ++u) {
+                const int rho = rho_a + j * G.S + dr + u * rows_per_pass;
+                const Vec<16> me = me_next[u];
+                if (j + 1 < n) me_next[u] = ldv<16>(own + (long long)(rho + G.S) * G.H + xh0);
+                const int z = (int)fdiv((uint32_t)rho, G.fL2), y = rho - z * G.L2;
+                const int par = (y + z + (int)colour) & 1;
+                const uint32_t e = (uint32_t)(sbase * G.S) + (uint32_t)(j * G.S + dr + u * rows_per_pass + G.L2);
+                const uint32_t e_ym = y == 0 ? e + G.L2 - 1 : e - 1;
+                const uint32_t e_yp = y == G.L2 - 1 ? e - G.L2 + 1 : e + 1;
+                const uint8_t *rowp = ring + (size_t)(e & ring_rows_mask) * G.H;
+                const Vec<16> o0 = *reinterpret_cast<const Vec<16> *>(rowp + xh0);
+                const Vec<16> va = *reinterpret_cast<const Vec<16> *>(ring + (size_t)(e_ym & ring_rows_mask) * G.H + xh0);
+                const Vec<16> vb = *reinterpret_cast<const Vec<16> *>(ring + (size_t)(e_yp & ring_rows_mask) * G.H + xh0);
+                const Vec<16> vc = *reinterpret_cast<const Vec<16> *>(ring + (size_t)((e - G.L2) & ring_rows_mask) * G.H + xh0);
+                const Vec<16> vd = *reinterpret_cast<const Vec<16> *>(ring + (size_t)((e + G.L2) & ring_rows_mask) * G.H + xh0);
+                const uint32_t edge = par == 0 ? rowp[xh0 == 0 ? G.H - 1 : xh0 - 1]
+                                               : rowp[xh0 + 16 == G.H ? 0 : xh0 + 16];
+                const Vec<16> out = ising_sc_update<16>(me, o0, va, vb, vc, vd, edge, par, rho * G.H + xh0,
+                                                        s_th[warp], s_tl[warp], t, stream, c3, seed, K, cnt);
+                stv<16>(own + (long long)rho * G.H + xh0, out);
+            }
+            // every read of stage j is done (its slot may be refilled); a failed wait anywhere
+            // stops the whole block
+            const int fail = __syncthreads_or(ok ? 0 : 1);
+            if (fail) {
+                ok = false;
+                break;
+            }
+            if (tid == 0 && j + G.P < nst) issue(j + G.P);
+            if (j % (12 / VS) == (12 / VS) - 1) {  // byte lanes stay below 4 x 12
+                warp_add_count(acc_count + r, byte_sum(cnt));
+                cnt = 0;
+            }
+        }
+        warp_add_count(acc_count + r, byte_sum(cnt));
+        a = e_seg;
+    }
+    // on a failed wait: let the copies already issued land before the block's memory goes
+    if (!ok && tid == 0) {
+        while (waited < issued) {
+            tc::mbar_wait(tc::smem_u32(&full[waited % G.P]), (uint32_t)((waited / G.P) & 1), err, 2);
+            ++waited;
+        }
+    }
+}
+
+static bool stream_geometry(const Ctx &c, int vs, StreamGeo &G) {
+    G.L1 = c.L[0];
+    G.L2 = c.L[1];
+    G.L3 = c.L[2];
+    G.H = c.L[0] / 2;
+    if (G.H < 16 || G.H > 4096 || (G.H & (G.H - 1))) return false;
+    G.S = vs * 4096 / G.H;
+    G.rows = G.L2 * G.L3;
+    if (G.S < 1 || G.rows % G.S || (256 % (G.H / 16) && G.H < 4096)) return false;
+    G.spr = G.rows / G.S;
+    G.h = (2 * G.L2 + G.S - 1) / G.S;
+    int P = 4;
+    while (P < G.h + 3) P *= 2;
+    G.P = P;
+    if ((long)P * G.S * G.H > 160 * 1024) return false;
+    G.fL2 = make_fastdiv((uint32_t)G.L2);
+    return true;
+}
+
+bool ising_stream_supported(const Ctx &c, int vs) {
+    StreamGeo G;
+    return c.fast && c.model == ETHER_MODEL_ISING && stream_geometry(c, vs, G);
+}
+
+template <int VS, int MINB>
+static cudaError_t launch_stream(Ctx &c, int colour) {
+    StreamGeo G;
+    if (!stream_geometry(c, VS, G)) return cudaErrorInvalidValue;
+    const int smem = G.P * G.S * G.H + G.P * 8;
+    static int occ = 0, occ_smem = 0;  // resident blocks per SM, for the ring size it was found for
+    if (occ_smem != smem) {
+        cudaFuncSetAttribute(ising_sc_stream<VS, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ising_sc_stream<VS, MINB>, 256, smem) != cudaSuccess || occ < 1)
+            occ = 1;
+        occ_smem = smem;
+    }
+    const long long steps = (long long)c.R * G.spr;
+    const int grid = (int)std::min<long long>(steps, (long long)occ * c.sm_count);
+    ising_sc_stream<VS, MINB><<<grid, 256, smem, c.stream>>>(c.spins, G, (uint32_t)colour, c.thr, c.table_entries,
+                                                             c.slot_of_rep, c.stream_id, c.step, c.seed,
+                                                             round_keys(c.seed), c.R, c.acc_count, c.err);
+    return cudaGetLastError();
+}
+
+template <int W, int VPT, int MINB>
 static void launch_persist(Ctx &c, int colour) {
     static int occ = 0;  // resident blocks per SM of this instantiation
     if (occ == 0) {
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ising_sc_persist<W, VPT>, 256, 0) != cudaSuccess || occ < 1)
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ising_sc_persist<W, VPT, MINB>, 256, 0) != cudaSuccess || occ < 1)
             occ = 1;
     }
     const int nvec = (c.N / 2) / W;
     const long long items = (long long)c.R * ((nvec + VPT * 256 - 1) / (VPT * 256));
     const int grid = (int)std::min<long long>(items, (long long)occ * c.sm_count);
-    ising_sc_persist<W, VPT><<<grid, 256, 0, c.stream>>>(
+    ising_sc_persist<W, VPT, MINB><<<grid, 256, 0, c.stream>>>(
         c.spins, c.L[0], c.L[1], c.L[2], make_fastdiv((uint32_t)(c.L[0] / 2)),
         make_fastdiv((uint32_t)c.L[1]), (uint32_t)colour, c.thr, c.table_entries, c.slot_of_rep,
         c.stream_id, c.step, c.seed, round_keys(c.seed), c.R, c.acc_count);
 }
 
-template <int W, int VPT>
+template <int W, int VPT, int MINB>
 static void launch_sc(Ctx &c, int colour) {
     const int bs = 256;
     const int nvec = (c.N / 2) / W;
     dim3 grid((nvec + bs * VPT - 1) / (bs * VPT), c.R);
-    ising_sc_kernel<W, VPT><<<grid, bs, 0, c.stream>>>(
+    ising_sc_kernel<W, VPT, MINB><<<grid, bs, 0, c.stream>>>(
         c.spins, c.L[0], c.L[1], c.L[2], make_fastdiv((uint32_t)(c.L[0] / 2)),
         make_fastdiv((uint32_t)c.L[1]), (uint32_t)colour, c.thr, c.table_entries, c.slot_of_rep,
         c.stream_id, c.step, c.seed, round_keys(c.seed), c.acc_count);
@@ -140,19 +326,36 @@ static int blocks_for(const Ctx &c, long work, int bs) {
 
 cudaError_t launch_ising_sweep(Ctx &c, int colour) {
     const int bs = 256;
+    if (c.fast && c.ising_stream) {
+        cudaError_t e;
+        switch (c.ising_vpt * 10 + (c.ising_cap ? 4 : 1)) {
+            case 11: e = launch_stream<1, 1>(c, colour); break;
+            case 14: e = launch_stream<1, 4>(c, colour); break;
+            case 21: e = launch_stream<2, 1>(c, colour); break;
+            default: e = launch_stream<4, 1>(c, colour); break;
+        }
+        c.launches++;
+        return e;
+    }
     if (c.fast) {
-        const int key = (c.ising_persist ? 1000 : 0) + c.vec_bytes * 10 + c.ising_vpt;
+        // variant = 1000 persistent + 2000 register cap (four 256-thread blocks per SM)
+        //           + 10 bytes per vector + vectors per thread
+        const int key = (c.ising_persist ? 1000 : 0) + (c.ising_cap ? 2000 : 0) + c.vec_bytes * 10 + c.ising_vpt;
         switch (key) {
-            case 161: launch_sc<16, 1>(c, colour); break;
-            case 162: launch_sc<16, 2>(c, colour); break;
-            case 164: launch_sc<16, 4>(c, colour); break;
-            case 81: launch_sc<8, 1>(c, colour); break;
-            case 82: launch_sc<8, 2>(c, colour); break;
-            case 84: launch_sc<8, 4>(c, colour); break;
-            case 1162: launch_persist<16, 2>(c, colour); break;
-            case 1164: launch_persist<16, 4>(c, colour); break;
-            case 1082: launch_persist<8, 2>(c, colour); break;
-            default: launch_persist<8, 4>(c, colour); break;
+            case 161: launch_sc<16, 1, 1>(c, colour); break;
+            case 162: launch_sc<16, 2, 1>(c, colour); break;
+            case 164: launch_sc<16, 4, 1>(c, colour); break;
+            case 81: launch_sc<8, 1, 1>(c, colour); break;
+            case 82: launch_sc<8, 2, 1>(c, colour); break;
+            case 84: launch_sc<8, 4, 1>(c, colour); break;
+            case 2162: launch_sc<16, 2, 4>(c, colour); break;
+            case 2164: launch_sc<16, 4, 4>(c, colour); break;
+            case 1162: launch_persist<16, 2, 1>(c, colour); break;
+            case 1164: launch_persist<16, 4, 1>(c, colour); break;
+            case 1082: launch_persist<8, 2, 1>(c, colour); break;
+            case 1084: launch_persist<8, 4, 1>(c, colour); break;
+            case 3162: launch_persist<16, 2, 4>(c, colour); break;
+            default: launch_persist<16, 4, 4>(c, colour); break;
         }
     } else {
         const int n_c = c.col_off[colour + 1] - c.col_off[colour];

@@ -156,12 +156,60 @@ __device__ __forceinline__ uint32_t sc_e4s(const Vec<W> &o0, uint32_t edge, int 
     return (n + (s0 << 3) - s0) << 2;
 }
 
+// The update of one W-byte vector (sites rho0 .. rho0+W-1 of the updated colour) from its own
+// spins `me` and the six neighbour words of the other colour; returns the new spins and adds
+// the flips to the bytewise counts.  A site whose high random half ties with its threshold's
+// high half (probability 2^-16) is decided by the low halves: whether any site of the vector
+// ties is checked once, and the rare vector with a tie is finished by resolve_ties.
+template <int W>
+__device__ __forceinline__ Vec<W> ising_sc_update(const Vec<W> &me, const Vec<W> &o0, const Vec<W> &a,
+                                                  const Vec<W> &b, const Vec<W> &c, const Vec<W> &d,
+                                                  uint32_t edge, int par, int rho0, const uint32_t *s_th,
+                                                  const uint32_t *s_tl, uint32_t t, uint32_t stream,
+                                                  uint32_t c3, uint32_t seed, const RoundKeys &K,
+                                                  uint32_t &cnt) {
+    constexpr int NW = W / 4;
+    const char *th_bytes = reinterpret_cast<const char *>(s_th);
+    Vec<W> out;
+    uint32_t e4[NW];
+    bool tie = false;
+    U4 rh{0, 0, 0, 0};
+#pragma unroll
+    for (int q = 0; q < NW; ++q) {
+        if ((q & 1) == 0) rh = draw_rk((uint32_t)((rho0 >> 3) + (q >> 1)), t, stream, c3, K);
+        const uint32_t s0 = me.w[q];
+        const uint32_t e4s = sc_e4s<W>(o0, edge, par, a, b, c, d, q, s0);
+        e4[q] = e4s;
+        const uint32_t t0 = *reinterpret_cast<const uint32_t *>(th_bytes + (e4s & 0xFFu));
+        const uint32_t t1 = *reinterpret_cast<const uint32_t *>(th_bytes + __byte_perm(e4s, 0, 0x4441));
+        const uint32_t t2 = *reinterpret_cast<const uint32_t *>(th_bytes + __byte_perm(e4s, 0, 0x4442));
+        const uint32_t t3 = *reinterpret_cast<const uint32_t *>(th_bytes + (e4s >> 24));
+        const uint32_t wa = (q & 1) ? rh.z : rh.x, wb = (q & 1) ? rh.w : rh.y;
+        const uint32_t u0 = wa & 0xFFFFu, u1 = wa >> 16, u2 = wb & 0xFFFFu, u3 = wb >> 16;
+        uint32_t m = 0;
+        if (u0 < t0) m |= 0x00000001u;
+        if (u1 < t1) m |= 0x00000100u;
+        if (u2 < t2) m |= 0x00010000u;
+        if (u3 < t3) m |= 0x01000000u;
+        tie |= (u0 == t0) | (u1 == t1) | (u2 == t2) | (u3 == t3);
+        out.w[q] = s0 ^ m;
+        cnt += m;
+    }
+    if (tie) {
+#pragma unroll
+        for (int q = 0; q < NW; ++q) {
+            const uint32_t m = resolve_ties((uint32_t)((rho0 >> 3) + (q >> 1)), t, stream, c3, seed, q & 1,
+                                            e4[q], s_th, s_tl);
+            out.w[q] ^= m;
+            cnt += m;
+        }
+    }
+    return out;
+}
+
 // VPT vectors of W bytes per thread, vector indices vfirst + j*vstride (j < VPT, < nvec),
-// one after another.  s_th / s_tl: the 14 thresholds' high / low halves in shared memory.
-// Returns the flips as bytewise counts (each byte <= 4 VPT; sum the bytes for the total).
-// A site whose high random half ties with its threshold's high half (probability 2^-16) is
-// decided by the low halves; whether any of a vector's sites tie is checked once per vector,
-// and the rare vector with a tie is finished by resolve_ties.
+// one after another, loaded from global memory.  s_th / s_tl: the 14 thresholds' high / low
+// halves in shared memory.  Returns the flips as bytewise counts (each byte <= NW VPT).
 template <int W, int VPT>
 __device__ __forceinline__ uint32_t ising_sc_vectors(const IsingSc &A, int vfirst, int vstride,
                                                      int nvec, const uint32_t *s_th,
@@ -169,8 +217,6 @@ __device__ __forceinline__ uint32_t ising_sc_vectors(const IsingSc &A, int vfirs
                                                      uint32_t stream, uint32_t c3, uint32_t seed,
                                                      const RoundKeys &K) {
     static_assert(W == 8 || W == 16, "vector of one or two random-number groups");
-    constexpr int NW = W / 4;
-    const char *th_bytes = reinterpret_cast<const char *>(s_th);
     const int H = A.H, L2 = A.L2, L3 = A.L3;
     uint32_t cnt = 0;
 #pragma unroll
@@ -193,40 +239,8 @@ __device__ __forceinline__ uint32_t ising_sc_vectors(const IsingSc &A, int vfirs
         const Vec<W> d = ldv<W>(A.opp + (zp * L2 + y) * H + xh0);
         const uint32_t edge = par == 0 ? A.opp[row * H + (xh0 == 0 ? H - 1 : xh0 - 1)]
                                        : A.opp[row * H + (xh0 + W == H ? 0 : xh0 + W)];
-        Vec<W> out;
-        uint32_t e4[NW];
-        bool tie = false;
-        U4 rh{0, 0, 0, 0};
-#pragma unroll
-        for (int q = 0; q < NW; ++q) {
-            if ((q & 1) == 0) rh = draw_rk((uint32_t)((rho0 >> 3) + (q >> 1)), t, stream, c3, K);
-            const uint32_t s0 = me.w[q];
-            const uint32_t e4s = sc_e4s<W>(o0, edge, par, a, b, c, d, q, s0);
-            e4[q] = e4s;
-            const uint32_t t0 = *reinterpret_cast<const uint32_t *>(th_bytes + (e4s & 0xFFu));
-            const uint32_t t1 = *reinterpret_cast<const uint32_t *>(th_bytes + __byte_perm(e4s, 0, 0x4441));
-            const uint32_t t2 = *reinterpret_cast<const uint32_t *>(th_bytes + __byte_perm(e4s, 0, 0x4442));
-            const uint32_t t3 = *reinterpret_cast<const uint32_t *>(th_bytes + (e4s >> 24));
-            const uint32_t wa = (q & 1) ? rh.z : rh.x, wb = (q & 1) ? rh.w : rh.y;
-            const uint32_t u0 = wa & 0xFFFFu, u1 = wa >> 16, u2 = wb & 0xFFFFu, u3 = wb >> 16;
-            uint32_t m = 0;
-            if (u0 < t0) m |= 0x00000001u;
-            if (u1 < t1) m |= 0x00000100u;
-            if (u2 < t2) m |= 0x00010000u;
-            if (u3 < t3) m |= 0x01000000u;
-            tie |= (u0 == t0) | (u1 == t1) | (u2 == t2) | (u3 == t3);
-            out.w[q] = s0 ^ m;
-            cnt += m;
-        }
-        if (tie) {
-#pragma unroll
-            for (int q = 0; q < NW; ++q) {
-                const uint32_t m = resolve_ties((uint32_t)((rho0 >> 3) + (q >> 1)), t, stream, c3, seed,
-                                                q & 1, e4[q], s_th, s_tl);
-                out.w[q] ^= m;
-                cnt += m;
-            }
-        }
+        const Vec<W> out = ising_sc_update<W>(me, o0, a, b, c, d, edge, par, rho0, s_th, s_tl, t, stream,
+                                              c3, seed, K, cnt);
         stv<W>(A.own_a + rho0, out);
     }
     return cnt;

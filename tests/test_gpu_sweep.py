@@ -53,12 +53,25 @@ def test_ising_sc_bit_exact(L, flags, kT):
         assert sw.info().fast_path == 1
 
 
-@pytest.mark.parametrize("variant", [161, 162, 164, 81, 82, 84, 1162, 1164, 1082, 1084])
+@pytest.mark.parametrize("variant", [161, 162, 164, 81, 82, 84, 2162, 2164, 1162, 1164, 1082, 1084,
+                                     3162, 3164])
 def test_ising_sc_every_kernel_variant_bit_exact(variant):
     lat = eg.simple_cubic((32, 8, 6))
     sw, ion, g, ao, ag = ising_replay(lat, FM, 4.511, 8, variant=variant)
     np.testing.assert_array_equal(g[:, 3], ion[:, 3])
     assert ao == pytest.approx(ag, abs=1e-12)
+
+
+# the shared-memory staged kernel: one halo stage (32 x 16 x 32: 2 steps per replica) and two
+# halo stages with the ring wrapping many times (128 x 64 x 16: 16 steps per replica)
+@pytest.mark.parametrize("variant", [4011, 4014, 4021, 4041])
+@pytest.mark.parametrize("L", [(32, 16, 64), (128, 64, 32)])
+def test_ising_staged_kernel_bit_exact(variant, L):
+    lat = eg.simple_cubic(L)
+    sw, ion, g, ao, ag = ising_replay(lat, FM, 4.511, 6, variant=variant)
+    np.testing.assert_array_equal(g[:, 3], ion[:, 3])
+    assert ao == pytest.approx(ag, abs=1e-12)
+    sw.sync()  # no bounded wait ran out
 
 
 def test_ising_tie_path_bit_exact():
