@@ -442,6 +442,28 @@ def run_learned(L=64, R=256, train_steps=3000, n_plain=40000, n_learn=6000):
     return res
 
 
+def run_learned_sweep(L=64, R=256, sweeps=3):
+    """Time of the learned sweep alone (untrained network, T_c): the profiling case."""
+    import ether_gb300 as eg
+    lat = eg.simple_cubic(L)
+    j = eg.couplings(1, [[(1, 1, (-J_MEV, -J_MEV, -J_MEV))]], [1.0])
+    sw = eg.Sweep.from_lattice(lat, j, np.array([1.0]), eg.MODEL_ISING, replicas=R, seed=31)
+    sw.set_beta(1.0 / (KTC_ISING * J_MEV * 1e-3))
+    rng = np.random.default_rng(7)
+    ion = lat.ion.copy()
+    ion[:, 3] = rng.choice([-1.0, 1.0], size=lat.N)
+    sw.set_spins(ion)
+    lr = eg.Learned(sw, seed=5, capacity=4096)
+    sw.metropolis(10, accept=False)
+    lr.sweep_(sweeps)
+    sw.sync()
+    res = {"L": L, "replicas": R, "learned_sweep_ms": lr.info().last_sweep_ms,
+           "acceptance": float(lr.accepts().sum() / lr.info().proposed)}
+    lr.close()
+    sw.close()
+    return res
+
+
 def cpu_reference(model, L, mcs, threads, seed=1992):
     """The oracle's typewriter restatement of the reference's per-MCS work (Metropolis
     + get_tot_energy), one replica (temperature) per thread."""
@@ -501,7 +523,8 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--model", default="ising", choices=["ising", "heisenberg", "sq", "batch", "learned"])
+    ap.add_argument("--model", default="ising",
+                    choices=["ising", "heisenberg", "sq", "batch", "learned", "learned-sweep"])
     ap.add_argument("--L", type=int, default=64)
     ap.add_argument("--replicas", type=int, default=0)
     ap.add_argument("--cpu-mcs", type=int, default=0)
@@ -538,6 +561,14 @@ def main():
                           "roofline": {"bound": "tensor", "achieved": r["tensor_tflops"],
                                        "peak": bf16_peak, "unit": "TFLOP/s",
                                        "frac": r["tensor_tflops"] / bf16_peak}}))
+        return 0
+
+    if args.model == "learned-sweep":
+        if rank != 0:
+            return 0
+        r = run_learned_sweep(args.L, args.replicas or 256)
+        print(json.dumps({"metric": "learned sweep ms", "value": r["learned_sweep_ms"], "unit": "ms",
+                          "higher_is_better": False, "detail": r}))
         return 0
 
     if args.model == "learned":
