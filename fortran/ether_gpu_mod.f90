@@ -39,6 +39,12 @@ module ether_gpu_mod
         integer(c_int32_t) :: ovrr_mcs, pt, exchange_interval
     end type ether_schedule
 
+    type, bind(C) :: ether_learn_desc
+        integer(c_int32_t) :: patch, hidden
+        integer(c_int32_t) :: seed       ! uint32_t in C
+        integer(c_int64_t) :: capacity
+    end type ether_learn_desc
+
     interface
         integer(c_int) function ether_create(desc, ctx) bind(C, name="ether_create")
             import :: c_int, c_ptr, ether_desc
@@ -148,6 +154,56 @@ module ether_gpu_mod
             real(c_double), value :: tol
             real(c_double), intent(out) :: ion(0:8, *), stgg(*)
             integer(c_int32_t), intent(out) :: nn(*)
+        end function
+        ! batched sweeps over several contexts (no counterpart in the reference)
+        integer(c_int) function ether_batch_create(members, n_members, batch) bind(C, name="ether_batch_create")
+            import :: c_int, c_ptr, c_int32_t
+            type(c_ptr), intent(in) :: members(*)
+            integer(c_int32_t), value :: n_members
+            type(c_ptr), intent(out) :: batch
+        end function
+        integer(c_int) function ether_batch_destroy(batch) bind(C, name="ether_batch_destroy")
+            import :: c_int, c_ptr
+            type(c_ptr), value :: batch
+        end function
+        integer(c_int) function ether_batch_metropolis(batch, nsweeps) bind(C, name="ether_batch_metropolis")
+            import :: c_int, c_ptr, c_int32_t
+            type(c_ptr), value :: batch
+            integer(c_int32_t), value :: nsweeps
+        end function
+        integer(c_int) function ether_batch_autotune(batch, config, best_ms) bind(C, name="ether_batch_autotune")
+            import :: c_int, c_ptr, c_int32_t, c_float
+            type(c_ptr), value :: batch
+            integer(c_int32_t), intent(out) :: config(4)
+            real(c_float), intent(out) :: best_ms
+        end function
+        ! learned patch proposal (no counterpart in the reference)
+        integer(c_int) function ether_learn_create(ctx, desc, learn) bind(C, name="ether_learn_create")
+            import :: c_int, c_ptr, ether_learn_desc
+            type(c_ptr), value :: ctx
+            type(ether_learn_desc), intent(in) :: desc
+            type(c_ptr), intent(out) :: learn
+        end function
+        integer(c_int) function ether_learn_destroy(learn) bind(C, name="ether_learn_destroy")
+            import :: c_int, c_ptr
+            type(c_ptr), value :: learn
+        end function
+        integer(c_int) function ether_learn_collect(learn, per_replica) bind(C, name="ether_learn_collect")
+            import :: c_int, c_ptr, c_int32_t
+            type(c_ptr), value :: learn
+            integer(c_int32_t), value :: per_replica
+        end function
+        integer(c_int) function ether_learn_train(learn, steps, batch, lr, loss) bind(C, name="ether_learn_train")
+            import :: c_int, c_ptr, c_int32_t, c_float, c_double
+            type(c_ptr), value :: learn
+            integer(c_int32_t), value :: steps, batch
+            real(c_float), value :: lr
+            real(c_double), intent(out) :: loss
+        end function
+        integer(c_int) function ether_learn_sweep(learn, nsweeps) bind(C, name="ether_learn_sweep")
+            import :: c_int, c_ptr, c_int32_t
+            type(c_ptr), value :: learn
+            integer(c_int32_t), value :: nsweeps
         end function
     end interface
 end module ether_gpu_mod
