@@ -128,6 +128,9 @@ SIGNATURES = {
     "ether_autotune": (C.c_int, [P, PI32, C.POINTER(C.c_float)]),
     "ether_set_variant": (C.c_int, [P, C.c_int32]),
     "ether_structure_factor": (C.c_int, [P, PD, PI32, PD, PD, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "ether_moment_vectors": (C.c_int, [P, PD]),
+    "ether_spiral_setup": (C.c_int, [P, C.c_double, PD, C.c_double, C.c_int32, C.POINTER(C.c_int64)]),
+    "ether_spiral_state": (C.c_int, [P, PD]),
     "ether_batch_create": (C.c_int, [C.POINTER(P), C.c_int32, C.POINTER(P)]),
     "ether_batch_destroy": (C.c_int, [P]),
     "ether_batch_metropolis": (C.c_int, [P, C.c_int32]),

@@ -192,7 +192,8 @@ void free_ctx(Ctx &c) {
                     c.t.mweight, c.t.site_of_storage, c.spins, c.spins4, c.beta_slot,
                     c.beta_slot_f, c.slot_of_rep, c.rep_of_slot, c.thr, c.stream_id,
                     c.step, c.ovrr_step, c.fresh_call, c.acc_count, c.E, c.M, c.sums,
-                    c.partials, c.pt_accepts, c.swap_dev, c.copy_from, c.err};
+                    c.partials, c.pt_accepts, c.swap_dev, c.copy_from, c.err, c.spiral_ptr,
+                    c.spiral_nbr};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto &kv : c.graphs) cudaGraphExecDestroy(kv.second);

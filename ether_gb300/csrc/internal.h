@@ -88,6 +88,8 @@ struct Ctx {
     bool ising_cap = false;      // register-capped (four blocks per SM) instantiation
     bool ising_stream = false;   // shared-memory staged simple-cubic Ising kernel
     int *err = nullptr;          // device: first bounded-wait failure of a kernel (0 = none)
+    int32_t *spiral_ptr = nullptr, *spiral_nbr = nullptr;  // spiral partners, CSR in storage order
+    long spiral_count = 0;
     uint32_t *stream_id = nullptr;  // R
     uint32_t *step = nullptr;       // R (Metropolis sweep counter)
     uint32_t *ovrr_step = nullptr;  // R

@@ -149,6 +149,7 @@ class Sweep:
         d.flags = flags
         self.N = d.n_sites
         self.R = replicas
+        self._nsp = n_species
         self.model = model
         h_ = C.c_void_p()
         abi.check(self.lib.ether_create(C.byref(d), C.byref(h_)))
@@ -297,6 +298,24 @@ class Sweep:
 
     def end_sweep(self):
         abi.check(self.lib.ether_end_sweep(self.h))
+
+    def moment_vectors(self):
+        """get_moment_vectors: (R, n_species, 3)."""
+        out = np.zeros((self.R, self._nsp, 3), dtype=np.float64)
+        abi.check(self.lib.ether_moment_vectors(self.h, abi.dptr(out)))
+        return out
+
+    def spiral_setup(self, ss_dis, ss_direc=(0.0, 0.0, 1.0), ss_latency=2.0, capacity=5):
+        d = np.ascontiguousarray(ss_direc, dtype=np.float64)
+        n = C.c_int64(0)
+        abi.check(self.lib.ether_spiral_setup(self.h, float(ss_dis), abi.dptr(d), float(ss_latency),
+                                              int(capacity), C.byref(n)))
+        return n.value
+
+    def spiral_state(self):
+        out = np.zeros(self.R, dtype=np.float64)
+        abi.check(self.lib.ether_spiral_state(self.h, abi.dptr(out)))
+        return out
 
     def autotune(self):
         v = C.c_int32(0)

@@ -234,6 +234,22 @@ int ether_set_variant(ether_ctx *ctx, int32_t variant);
 int ether_structure_factor(ether_ctx *ctx, const double *abc, const int32_t nq[3],
                            const double q0[3], const double dq[3], float *sq, float *comp);
 
+/* ------------------------------------------- moment vectors and the spiral state ---- */
+/* get_moment_vectors (src/get_moment_vectors.f90:20-38), called at src/ether.f90:219:
+ * mm(3, nsp, R) = sum over the sites of each species of stgg_i s(sp) S_i, per replica. */
+int ether_moment_vectors(ether_ctx *ctx, double *mm);
+/* get_spiral_state 'ions_for_spiral' (src/get_spiral_state.f90:45-77), called at
+ * src/ether.f90:69 for XYZ: every site's partners j != i with |r_j - r_i| <= ss_dis and
+ * angle(r_j - r_i, ss_direc) <= ss_latency degrees (ss_direc used as given, not normalised;
+ * no periodic images), at most `capacity` per site (spiral_capacity; ETHER_ERR_CAPACITY
+ * beyond, where the reference would write past its array).  count = spiral_count. */
+int ether_spiral_setup(ether_ctx *ctx, double ss_dis, const double ss_direc[3], double ss_latency,
+                       int32_t capacity, int64_t *count);
+/* get_spiral_state 'spiral_state' (src/get_spiral_state.f90:79-108): ss(R) =
+ * |sum_i sum_j S_i x S_j| / spiral_count per replica (the per-sample value the reference
+ * accumulates into spiral_state_avg, _2_avg, _4_avg). */
+int ether_spiral_state(ether_ctx *ctx, double *ss);
+
 /* ------------------------------------------------------------------- batched sweeps ---- */
 /* The reference advances one lattice at one temperature per MPI rank (src/ether.f90:112-118,
  * src/Metropolis.f90:34-68).  A batch advances the Metropolis sweeps of many contexts --

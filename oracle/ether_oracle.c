@@ -908,3 +908,61 @@ void orc_run_temperatures(const orc_sys *sy, const double *ion0, int nT, const d
     }
     (void)nthreads;
 }
+
+/* ------------------------------------------------------ moment vectors, spiral state ---- */
+/* get_moment_vectors (src/get_moment_vectors.f90:20-38): mm(3, nsp) = sum over sites of
+ * stgg_i * s(species_i) * S_i, sites in order. */
+void orc_moment_vectors(const orc_sys *sy, const double *ion, double *mm) {
+    for (int k = 0; k < 3 * sy->n_species; ++k) mm[k] = 0.0;
+    for (int i = 0; i < sy->n_sites; ++i) {
+        const int sp = (int)ion[9 * i + 4];
+        const double w = (sy->stgg ? sy->stgg[i] : 1.0) * sy->s[sp - 1];
+        for (int a = 0; a < 3; ++a) mm[3 * (sp - 1) + a] += w * ion[9 * i + 1 + a];
+    }
+}
+
+/* get_spiral_state 'ions_for_spiral' (src/get_spiral_state.f90:45-77): for every site i the
+ * sites j != i (increasing j) with |r_j - r_i| <= ss_dis and
+ * acos((r_j - r_i)/|r_j - r_i| . ss_direc) * 180/pi <= ss_latency; no periodic images.
+ * ifs(cap, N) receives 1-based j (0 = none).  Returns the total count, or -1 if a site has
+ * more than cap (the reference writes past its array then). */
+long orc_spiral_pairs(int N, const double *ion, double ss_dis, const double ss_direc[3],
+                      double ss_latency, int cap, int32_t *ifs) {
+    const double to_angle = 180.0 / 3.14159265358979323846;
+    long count = 0;
+    for (long k = 0; k < (long)cap * N; ++k) ifs[k] = 0;
+    for (int i = 0; i < N; ++i) {
+        int found = 0;
+        for (int j = 0; j < N; ++j) {
+            if (j == i) continue;
+            double r[3];
+            for (int a = 0; a < 3; ++a) r[a] = ion[9 * j + 6 + a] - ion[9 * i + 6 + a];
+            const double dis = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+            if (!(dis <= ss_dis)) continue;
+            const double u[3] = {r[0] / dis, r[1] / dis, r[2] / dis};
+            const double ang = acos(u[0] * ss_direc[0] + u[1] * ss_direc[1] + u[2] * ss_direc[2]) * to_angle;
+            if (!(ang <= ss_latency)) continue;
+            if (found == cap) return -1;
+            ifs[(long)i * cap + found++] = j + 1;
+            ++count;
+        }
+    }
+    return count;
+}
+
+/* get_spiral_state 'spiral_state' (:79-108): |sum_i sum_j S_i x S_j| / spiral_count. */
+double orc_spiral_state(int N, const double *ion, int cap, const int32_t *ifs, long count) {
+    double ss[3] = {0, 0, 0};
+    for (int i = 0; i < N; ++i) {
+        const double *a = ion + 9 * i + 1;
+        for (int k = 0; k < cap; ++k) {
+            const int j = ifs[(long)i * cap + k];
+            if (j == 0) break;
+            const double *b = ion + 9 * (j - 1) + 1;
+            ss[0] += a[1] * b[2] - a[2] * b[1];
+            ss[1] += a[2] * b[0] - a[0] * b[2];
+            ss[2] += a[0] * b[1] - a[1] * b[0];
+        }
+    }
+    return sqrt(ss[0] * ss[0] + ss[1] * ss[1] + ss[2] * ss[2]) / (double)count;
+}

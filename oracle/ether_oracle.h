@@ -206,6 +206,13 @@ long orc_patch_sweep(uint8_t *sp, const int L[3], double betaJ, const float *log
 void orc_patch_chain(const int L[3], double betaJ, long nsteps, long nequil, int use_patch,
                      float zscale, float zbias, uint32_t seed, double out[5]);
 
+
+/* ---- moment vectors and spiral state ---- */
+void orc_moment_vectors(const orc_sys *sy, const double *ion, double *mm);
+long orc_spiral_pairs(int N, const double *ion, double ss_dis, const double ss_direc[3],
+                      double ss_latency, int cap, int32_t *ifs);
+double orc_spiral_state(int N, const double *ion, int cap, const int32_t *ifs, long count);
+
 #ifdef __cplusplus
 }
 #endif

@@ -97,6 +97,11 @@ def lib():
         L.orc_expf_neg.restype = C.c_float
         L.orc_expf_neg.argtypes = [C.c_float]
         L.orc_sincosf.argtypes = [C.c_float, PF, PF]
+        L.orc_moment_vectors.argtypes = [C.POINTER(Sys), PD, PD]
+        L.orc_spiral_pairs.restype = C.c_long
+        L.orc_spiral_pairs.argtypes = [C.c_int, PD, C.c_double, PD, C.c_double, C.c_int, PI]
+        L.orc_spiral_state.restype = C.c_double
+        L.orc_spiral_state.argtypes = [C.c_int, PD, C.c_int, PI, C.c_long]
         PU8 = C.POINTER(C.c_uint8)
         L.orc_bf16_round.restype = C.c_float
         L.orc_bf16_round.argtypes = [C.c_float]
@@ -215,6 +220,27 @@ class System:
 
     def metropolis_typewriter(self, ion, beta, st):
         return lib().orc_metropolis_typewriter(self.p(), _d(ion), beta, C.byref(st))
+
+    def moment_vectors(self, ion):
+        mm = np.zeros((self.sys.n_species, 3))
+        lib().orc_moment_vectors(self.p(), _d(np.ascontiguousarray(ion, dtype=np.float64)), _d(mm))
+        return mm
+
+
+def spiral_pairs(ion, ss_dis, ss_direc, ss_latency, cap):
+    """(ifs(N, cap) 1-based, count) of get_spiral_state's 'ions_for_spiral' (count -1: a site
+    has more than cap)."""
+    ion = np.ascontiguousarray(ion, dtype=np.float64)
+    N = ion.shape[0]
+    ifs = np.zeros((N, cap), dtype=np.int32)
+    d = np.ascontiguousarray(ss_direc, dtype=np.float64)
+    n = lib().orc_spiral_pairs(N, _d(ion), ss_dis, _d(d), ss_latency, cap, _i(ifs))
+    return ifs, n
+
+
+def spiral_state(ion, ifs, count):
+    ion = np.ascontiguousarray(ion, dtype=np.float64)
+    return lib().orc_spiral_state(ion.shape[0], _d(ion), ifs.shape[1], _i(np.ascontiguousarray(ifs)), count)
 
 
 def stream(seed, sid):
