@@ -208,7 +208,7 @@ def run_sweeps(model, L, replicas, steps, warmup, rank, world, force_variant=0, 
         t_e2e = time.perf_counter() - t_start
         esize = 1 if model == eg.MODEL_ISING else 16
         res.update({"e2e": updates / (t_e2e * 1e9) * world,
-                    "h2d": (N * esize * R) / steps,
+                    "h2d": (N * esize) / steps,   # one configuration, replicated on the device
                     "d2h": 8.0 * R + (N * esize) / steps,
                     "accept_mean": float(np.mean(acc))})
     sw.close()

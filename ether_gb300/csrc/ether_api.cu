@@ -193,9 +193,10 @@ void free_ctx(Ctx &c) {
                     c.beta_slot_f, c.slot_of_rep, c.rep_of_slot, c.thr, c.stream_id,
                     c.step, c.ovrr_step, c.fresh_call, c.acc_count, c.E, c.M, c.sums,
                     c.partials, c.pt_accepts, c.swap_dev, c.copy_from, c.err, c.spiral_ptr,
-                    c.spiral_nbr};
+                    c.spiral_nbr, c.acc_before, c.acc_ratio};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    if (c.acc_host) cudaFreeHost(c.acc_host);
     for (auto &kv : c.graphs) cudaGraphExecDestroy(kv.second);
     if (c.stream) cudaStreamDestroy(c.stream);
     c = Ctx();
@@ -428,6 +429,9 @@ extern "C" int ether_create(const ether_desc *d, ether_ctx **out) {
     TRY(dev_alloc(c, &c.pt_accepts, 1));
     TRY(dev_alloc(c, &c.swap_dev, 1));
     TRY(dev_alloc(c, &c.err, 1));
+    TRY(dev_alloc(c, &c.acc_before, c.R));
+    TRY(dev_alloc(c, &c.acc_ratio, c.R));
+    CUDA_TRY(cudaMallocHost((void **)&c.acc_host, sizeof(double) * c.R));
     CUDA_TRY(cudaMemset(c.err, 0, sizeof(int)));
     TRY(dev_alloc(c, &c.copy_from, c.R));
 #undef TRY
@@ -502,8 +506,10 @@ extern "C" int ether_set_spins(ether_ctx *h, int32_t replica, const double *ion)
     if (c.model == ETHER_MODEL_ISING) {
         std::vector<uint8_t> v(N);
         for (int i = 0; i < N; ++i) v[c.storage[i]] = ion[3 + 9 * (size_t)i] > 0.0 ? 1 : 0;
-        for (int r = (replica < 0 ? 0 : replica); r < (replica < 0 ? c.R : replica + 1); ++r)
-            CUDA_TRY(cudaMemcpyAsync(c.spins + (size_t)r * N, v.data(), N, cudaMemcpyHostToDevice, c.stream));
+        // one upload; every replica: replicated on the device
+        CUDA_TRY(cudaMemcpyAsync(c.spins + (size_t)(replica < 0 ? 0 : replica) * N, v.data(), N,
+                                 cudaMemcpyHostToDevice, c.stream));
+        if (replica < 0) CUDA_TRY(launch_broadcast(c, c.spins, (size_t)N));
         CUDA_TRY(cudaStreamSynchronize(c.stream));
     } else {
         std::vector<float4> v(N);
@@ -511,8 +517,9 @@ extern "C" int ether_set_spins(ether_ctx *h, int32_t replica, const double *ion)
             const double *p = ion + 9 * (size_t)i;
             v[c.storage[i]] = make_float4((float)p[1], (float)p[2], (float)p[3], (float)p[5]);
         }
-        for (int r = (replica < 0 ? 0 : replica); r < (replica < 0 ? c.R : replica + 1); ++r)
-            CUDA_TRY(cudaMemcpyAsync(c.spins4 + (size_t)r * N, v.data(), sizeof(float4) * N, cudaMemcpyHostToDevice, c.stream));
+        CUDA_TRY(cudaMemcpyAsync(c.spins4 + (size_t)(replica < 0 ? 0 : replica) * N, v.data(),
+                                 sizeof(float4) * N, cudaMemcpyHostToDevice, c.stream));
+        if (replica < 0) CUDA_TRY(launch_broadcast(c, c.spins4, sizeof(float4) * (size_t)N));
         CUDA_TRY(cudaStreamSynchronize(c.stream));
     }
     return ETHER_OK;
@@ -566,20 +573,20 @@ extern "C" int ether_metropolis(ether_ctx *h, int32_t nsweeps, double *accept) {
     Ctx &c = h->c;
     if (nsweeps < 0) return fail(ETHER_ERR_ARG, "negative sweep count");
     if (!c.beta_set) return fail(ETHER_ERR_STATE, "beta not set (ether_set_beta / ether_set_ladder)");
-    std::vector<unsigned long long> before, after;
-    if (accept) {
-        before.resize(c.R);
-        CUDA_TRY(cudaMemcpyAsync(before.data(), c.acc_count, sizeof(unsigned long long) * c.R, cudaMemcpyDeviceToHost, c.stream));
-    }
+    // acceptance: a device snapshot of the counters, one kernel for the ratios and one copy
+    // into pinned memory, so a call that returns them costs a single small D2H and one sync
+    if (accept)
+        CUDA_TRY(cudaMemcpyAsync(c.acc_before, c.acc_count, sizeof(unsigned long long) * c.R,
+                                 cudaMemcpyDeviceToDevice, c.stream));
     for (int k = 0; k < nsweeps; ++k) {
         int rc = sweep_once(c);
         if (rc) return rc;
     }
     if (accept) {
-        after.resize(c.R);
-        CUDA_TRY(cudaMemcpyAsync(after.data(), c.acc_count, sizeof(unsigned long long) * c.R, cudaMemcpyDeviceToHost, c.stream));
+        CUDA_TRY(launch_accept_ratio(c, c.acc_ratio));
+        CUDA_TRY(cudaMemcpyAsync(c.acc_host, c.acc_ratio, sizeof(double) * c.R, cudaMemcpyDeviceToHost, c.stream));
         CUDA_TRY(cudaStreamSynchronize(c.stream));
-        for (int r = 0; r < c.R; ++r) accept[r] = (double)(after[r] - before[r]) / c.N;
+        std::memcpy(accept, c.acc_host, sizeof(double) * c.R);
     }
     return ETHER_OK;
 }

@@ -88,6 +88,9 @@ struct Ctx {
     bool ising_cap = false;      // register-capped (four blocks per SM) instantiation
     bool ising_stream = false;   // shared-memory staged simple-cubic Ising kernel
     int *err = nullptr;          // device: first bounded-wait failure of a kernel (0 = none)
+    unsigned long long *acc_before = nullptr;  // R: acceptance counts at the start of a call
+    double *acc_ratio = nullptr;               // R: device acceptance ratios of a call
+    double *acc_host = nullptr;                // R: pinned host copy
     int32_t *spiral_ptr = nullptr, *spiral_nbr = nullptr;  // spiral partners, CSR in storage order
     long spiral_count = 0;
     uint32_t *stream_id = nullptr;  // R
@@ -117,6 +120,8 @@ cudaError_t launch_xyz_sweep(Ctx &c, int colour);
 cudaError_t launch_overrelax(Ctx &c, int colour, int pass, float part);
 cudaError_t launch_fresh(Ctx &c);
 cudaError_t launch_advance(Ctx &c, uint32_t *counter);
+cudaError_t launch_accept_ratio(Ctx &c, double *out);
+cudaError_t launch_broadcast(Ctx &c, void *base, size_t bytes_per_replica);
 cudaError_t launch_energy_mag(Ctx &c, bool want_energy);
 cudaError_t launch_measure(Ctx &c);
 cudaError_t launch_record(Ctx &c, int t, bool want_e, double *mser, double *eser);

@@ -1,6 +1,8 @@
 // k_xyz.cu -- per-context launches of the Heisenberg (XYZ) colour phases (Metropolis bodies
 // in sweep_xyz.cuh); overrelaxation (src/overrelaxation.f90:30-61 with
 // get_ovrr_vec.f90:41-85); fresh_spins (src/fresh_spins.f90:31-38).
+#include <algorithm>
+
 #include "sweep_xyz.cuh"
 
 namespace ether {
@@ -214,6 +216,46 @@ cudaError_t launch_fresh(Ctx &c) {
     fresh_kernel<<<grid, bs, 0, c.stream>>>(c.spins, c.spins4, c.N, c.model, c.angle,
                                             (float)c.dphi, c.t.site_of_storage, c.stream_id,
                                             c.fresh_call, c.seed);
+    c.launches++;
+    return cudaGetLastError();
+}
+
+// Replica 0's bytes copied into replicas 1 .. R-1 (16-byte words when the size allows).
+__global__ void broadcast_kernel(uint8_t *__restrict__ base, long long bytes, int R) {
+    const long long total = bytes * (R - 1);
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    if ((bytes & 15) == 0) {
+        const uint4 *src = reinterpret_cast<const uint4 *>(base);
+        uint4 *dst = reinterpret_cast<uint4 *>(base + bytes);
+        const long long w = bytes >> 4;
+        for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < (total >> 4); i += stride)
+            dst[i] = src[i % w];
+    } else {
+        for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += stride)
+            base[bytes + i] = base[i % bytes];
+    }
+}
+
+cudaError_t launch_broadcast(Ctx &c, void *base, size_t bytes_per_replica) {
+    if (c.R < 2) return cudaSuccess;
+    const long long work = (long long)bytes_per_replica * (c.R - 1) / 16 + 1;
+    const int grid = (int)std::min<long long>((work + 255) / 256, (long long)c.sm_count * 8);
+    broadcast_kernel<<<grid, 256, 0, c.stream>>>(reinterpret_cast<uint8_t *>(base), (long long)bytes_per_replica, c.R);
+    c.launches++;
+    return cudaGetLastError();
+}
+
+// Acceptance ratios of the sweeps since the snapshot: out[r] = (acc[r] - before[r]) / N.
+__global__ void accept_ratio_kernel(const unsigned long long *__restrict__ acc,
+                                    const unsigned long long *__restrict__ before, int R, double invN,
+                                    double *__restrict__ out) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < R) out[r] = (double)(acc[r] - before[r]) * invN;
+}
+
+cudaError_t launch_accept_ratio(Ctx &c, double *out) {
+    accept_ratio_kernel<<<(c.R + 255) / 256, 256, 0, c.stream>>>(c.acc_count, c.acc_before, c.R,
+                                                                  1.0 / (double)c.N, out);
     c.launches++;
     return cudaGetLastError();
 }

@@ -225,3 +225,22 @@ def test_replicas_are_independent_streams():
     np.testing.assert_array_equal(s[0], s[2])
     assert not np.array_equal(s[0], s[1])
     assert not np.array_equal(s[1], s[3])
+
+
+@pytest.mark.parametrize("model", [eg.MODEL_ISING, eg.MODEL_XYZ])
+@pytest.mark.parametrize("L", [(8, 6, 4), (5, 5, 5)])
+def test_set_spins_every_replica(model, L):
+    """replica = -1: one upload, replicated on the device (sizes with and without 16-byte
+    multiples per replica)."""
+    lat = eg.simple_cubic(L)
+    sw, osys = make_pair(lat, model, FM, replicas=5)
+    ion = random_ising(lat, 3) if model == eg.MODEL_ISING else random_xyz(lat, 3)
+    sw.set_spins(ion)
+    cols = [3] if model == eg.MODEL_ISING else [1, 2, 3, 5]
+    for r in range(5):
+        g = sw.get_spins(lat.ion, r)
+        np.testing.assert_array_equal(g[:, cols], ion[:, cols].astype(np.float32).astype(np.float64))
+    other = random_ising(lat, 4) if model == eg.MODEL_ISING else random_xyz(lat, 4)
+    sw.set_spins(other, 2)
+    np.testing.assert_array_equal(sw.get_spins(lat.ion, 2)[:, cols], other[:, cols].astype(np.float32).astype(np.float64))
+    np.testing.assert_array_equal(sw.get_spins(lat.ion, 3)[:, cols], ion[:, cols].astype(np.float32).astype(np.float64))
