@@ -22,6 +22,9 @@ implies.
 --impl reference times the oracle's CPU restatement on all host cores (the Fortran reference
 cannot be built: no gfortran / MPI on this image or the GPU machine).
 --model sq times only the structure factor (for profiling).
+--model program times the whole program (ether_run) on the 16^3 Ising deck of the
+reference's simple-cubic example: deck read, lattice, 19 temperatures x 10 REPEATs x 5000 MCS
+with measurements, and every output file written.
 """
 import argparse
 import ctypes as C
@@ -30,6 +33,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import threading
 import time
 
@@ -464,6 +468,41 @@ def run_learned_sweep(L=64, R=256, sweeps=3):
     return res
 
 
+PROGRAM_DECK = ("model = ising\nmcs = 5000 3000\ntemp = 100 10 5\nspin = 1\nspecies = A\n"
+                "sc = 16 16 16\nbc = c c c\nrepeat = 10\ncoa = 10\nseed = 1992\ncb = .T.\n")
+PROGRAM_STRUCT = ("simple cubic\n1.0\n 1.0 0.0 0.0\n 0.0 1.0 0.0\n 0.0 0.0 1.0\n A\n 1\n"
+                  "Direct\n 0.0 0.0 0.0\n")
+PROGRAM_J = "1\n1.0 1\nA A -1.0 -1.0 -1.0\n"
+
+
+def run_program(repeats=2):
+    """ether_run end to end on the 16^3 Ising deck (J = 1 meV ferromagnetic, 19 temperatures
+    from 100 K to 10 K, 10 REPEATs, 5000 MCS of which 3000 equilibrate, a measurement every 10
+    MCS, Checkerboard staggered signs): wall time from the deck on disk to the last output
+    file, and the MCS loop alone."""
+    import ether_gb300 as eg
+    work = tempfile.mkdtemp(prefix="ether_run_")
+    indir = os.path.join(work, "deck")
+    os.makedirs(indir)
+    for name, text in (("in.ether", PROGRAM_DECK), ("structure.vasp", PROGRAM_STRUCT),
+                       ("j_exchange", PROGRAM_J)):
+        with open(os.path.join(indir, name), "w") as f:
+            f.write(text)
+    best = None
+    for k in range(repeats):  # the first call also pays the library's one-time set-up
+        t0 = time.perf_counter()
+        info = eg.run(indir, os.path.join(work, "out%d" % k))
+        wall = time.perf_counter() - t0
+        if best is None or wall < best[0]:
+            best = (wall, info)
+    wall, info = best
+    ups = info["site_updates"]
+    return {"workload": "ether_run: simple-cubic 16^3 Ising deck, 19 T x 10 REPEAT x 5000 MCS, "
+                        "coa 10, every output file", "site_updates": ups,
+            "wall_s": wall, "mcs_loop_s": info["seconds"],
+            "updates_per_ns_wall": ups / wall / 1e9, "updates_per_ns_loop": ups / info["seconds"] / 1e9}
+
+
 def cpu_reference(model, L, mcs, threads, seed=1992):
     """The oracle's typewriter restatement of the reference's per-MCS work (Metropolis
     + get_tot_energy), one replica (temperature) per thread."""
@@ -524,7 +563,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--model", default="ising",
-                    choices=["ising", "heisenberg", "sq", "batch", "learned", "learned-sweep"])
+                    choices=["ising", "heisenberg", "sq", "batch", "learned", "learned-sweep",
+                             "program"])
     ap.add_argument("--L", type=int, default=64)
     ap.add_argument("--replicas", type=int, default=0)
     ap.add_argument("--cpu-mcs", type=int, default=0)
@@ -561,6 +601,14 @@ def main():
                           "roofline": {"bound": "tensor", "achieved": r["tensor_tflops"],
                                        "peak": bf16_peak, "unit": "TFLOP/s",
                                        "frac": r["tensor_tflops"] / bf16_peak}}))
+        return 0
+
+    if args.model == "program":
+        if rank != 0:
+            return 0
+        r = run_program()
+        print(json.dumps({"metric": "program wall s", "value": r["wall_s"], "unit": "s",
+                          "higher_is_better": False, "detail": r}))
         return 0
 
     if args.model == "learned-sweep":
@@ -667,6 +715,7 @@ def main():
         comp["batch"] = bt
         comp["tau"] = run_tau(args.L)
         comp["learned"] = run_learned(args.L)
+        comp["program"] = run_program()
         line["components"] = comp
     if not args.no_cpu:
         line["cpu_baseline"] = {k: v for k, v in

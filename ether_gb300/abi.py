@@ -22,6 +22,9 @@ FLAG_FORCE_GENERAL = 1 << 0
 FLAG_PT_TRUE_ENERGY = 1 << 1
 FLAG_PT_REFERENCE_COPY = 1 << 2
 FLAG_NO_GRAPHS = 1 << 3
+RUN_PARSE_ONLY = 1 << 0
+RUN_QUIET = 1 << 1
+RUN_RESUME = 1 << 2
 
 
 class EtherError(RuntimeError):
@@ -86,6 +89,15 @@ class LearnInfo(C.Structure):
     ]
 
 
+class RunInfo(C.Structure):
+    _fields_ = [
+        ("ranks", C.c_int32), ("model", C.c_int32), ("n_sites", C.c_int32),
+        ("n_species", C.c_int32), ("n_shells", C.c_int32), ("n_temperatures", C.c_int32),
+        ("repeat", C.c_int32), ("n_rounds", C.c_int32), ("site_updates", C.c_uint64),
+        ("seconds", C.c_double),
+    ]
+
+
 P = C.c_void_p
 PD = C.POINTER(C.c_double)
 PI32 = C.POINTER(C.c_int32)
@@ -119,6 +131,7 @@ SIGNATURES = {
     "ether_record_series": (C.c_int, [P, C.c_int32, C.c_int32, PD, PD]),
     "ether_get_accept_counts": (C.c_int, [P, PU64]),
     "ether_reset_accept_counts": (C.c_int, [P]),
+    "ether_get_slot_accept_counts": (C.c_int, [P, PU64]),
     "ether_get_info": (C.c_int, [P, C.POINTER(Info)]),
     "ether_get_colouring": (C.c_int, [P, PI32, PI32]),
     "ether_sync": (C.c_int, [P]),
@@ -131,6 +144,7 @@ SIGNATURES = {
     "ether_moment_vectors": (C.c_int, [P, PD]),
     "ether_spiral_setup": (C.c_int, [P, C.c_double, PD, C.c_double, C.c_int32, C.POINTER(C.c_int64)]),
     "ether_spiral_state": (C.c_int, [P, PD]),
+    "ether_spiral_avg": (C.c_int, [P, PD]),
     "ether_batch_create": (C.c_int, [C.POINTER(P), C.c_int32, C.POINTER(P)]),
     "ether_batch_destroy": (C.c_int, [P]),
     "ether_batch_metropolis": (C.c_int, [P, C.c_int32]),
@@ -156,6 +170,7 @@ SIGNATURES = {
     "ether_sc_energy_noalloc": (C.c_int, [C.c_int32, P, PI32, C.c_int32, PD, PD, PD, PD, P]),
     "ether_build_lattice": (C.c_int, [C.c_int32, PD, PI32, PD, PI32, C.c_char_p, C.c_int32,
                                       C.c_int32, PD, C.c_double, C.c_int32, PD, PD, PI32]),
+    "ether_run": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int32, C.POINTER(RunInfo)]),
 }
 
 _lib = None

@@ -17,7 +17,7 @@ OUT = os.path.join(HERE, "libether_gpu.so")
 BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU = ["ether_api.cu", "k_ising.cu", "k_xyz.cu", "k_obs.cu", "noalloc.cu", "k_sq.cu", "k_batch.cu", "k_learn.cu", "k_moments.cu"]
-CXX = ["lattice.cpp"]
+CXX = ["lattice.cpp", "deck.cpp"]
 
 
 def _nvcc():

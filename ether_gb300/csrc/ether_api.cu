@@ -193,7 +193,8 @@ void free_ctx(Ctx &c) {
                     c.beta_slot_f, c.slot_of_rep, c.rep_of_slot, c.thr, c.stream_id,
                     c.step, c.ovrr_step, c.fresh_call, c.acc_count, c.E, c.M, c.sums,
                     c.partials, c.pt_accepts, c.swap_dev, c.copy_from, c.err, c.spiral_ptr,
-                    c.spiral_nbr, c.acc_before, c.acc_ratio};
+                    c.spiral_nbr, c.acc_before, c.acc_ratio, c.spiral_part, c.spiral_sums,
+                    c.acc_slot, c.acc_mark};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c.acc_host) cudaFreeHost(c.acc_host);
@@ -431,6 +432,8 @@ extern "C" int ether_create(const ether_desc *d, ether_ctx **out) {
     TRY(dev_alloc(c, &c.err, 1));
     TRY(dev_alloc(c, &c.acc_before, c.R));
     TRY(dev_alloc(c, &c.acc_ratio, c.R));
+    TRY(dev_alloc(c, &c.acc_slot, c.R));
+    TRY(dev_alloc(c, &c.acc_mark, c.R));
     CUDA_TRY(cudaMallocHost((void **)&c.acc_host, sizeof(double) * c.R));
     CUDA_TRY(cudaMemset(c.err, 0, sizeof(int)));
     TRY(dev_alloc(c, &c.copy_from, c.R));
@@ -442,6 +445,8 @@ extern "C" int ether_create(const ether_desc *d, ether_ctx **out) {
     CUDA_TRY(cudaMemset(c.ovrr_step, 0, sizeof(uint32_t) * c.R));
     CUDA_TRY(cudaMemset(c.fresh_call, 0, sizeof(uint32_t) * c.R));
     CUDA_TRY(cudaMemset(c.acc_count, 0, sizeof(unsigned long long) * c.R));
+    CUDA_TRY(cudaMemset(c.acc_slot, 0, sizeof(unsigned long long) * c.R));
+    CUDA_TRY(cudaMemset(c.acc_mark, 0, sizeof(unsigned long long) * c.R));
     CUDA_TRY(cudaMemset(c.sums, 0, sizeof(double) * 7 * c.R));
     CUDA_TRY(cudaMemset(c.E, 0, sizeof(double) * 2 * c.R));
     CUDA_TRY(cudaMemset(c.M, 0, sizeof(double) * 3 * c.R));
@@ -471,6 +476,7 @@ extern "C" int ether_set_beta(ether_ctx *h, const double *beta) {
     Ctx &c = h->c;
     for (int r = 0; r < c.R; ++r)
         if (!std::isfinite(beta[r])) return fail(ETHER_ERR_ARG, "beta is not finite for replica " + std::to_string(r));
+    if (c.beta_set) CUDA_TRY(launch_acc_bin(c));
     c.n_slots = c.R;
     c.n_groups = 1;
     c.beta_slots.assign(beta, beta + c.R);
@@ -483,6 +489,8 @@ extern "C" int ether_set_ladder(ether_ctx *h, int32_t n_slots, const double *bet
     if (n_slots <= 0 || c.R % n_slots != 0) return fail(ETHER_ERR_ARG, "n_slots must divide the replica count");
     for (int s = 0; s < n_slots; ++s)
         if (!std::isfinite(beta_slots[s])) return fail(ETHER_ERR_ARG, "beta is not finite for slot " + std::to_string(s));
+    // accepts so far belong to the positions of the old ladder
+    if (c.beta_set) CUDA_TRY(launch_acc_bin(c));
     c.n_slots = n_slots;
     c.n_groups = c.R / n_slots;
     c.beta_slots.assign(beta_slots, beta_slots + n_slots);
@@ -646,6 +654,7 @@ extern "C" int ether_zero_avg(ether_ctx *h) {
     if (!h) return fail(ETHER_ERR_ARG, "null context");
     Ctx &c = h->c;
     CUDA_TRY(cudaMemsetAsync(c.sums, 0, sizeof(double) * 7 * c.R, c.stream));
+    if (c.spiral_sums) CUDA_TRY(cudaMemsetAsync(c.spiral_sums, 0, sizeof(double) * 4 * c.R, c.stream));
     return ETHER_OK;
 }
 
@@ -687,12 +696,11 @@ extern "C" int ether_avg(ether_ctx *h, double *out) {
 extern "C" int ether_per_repeat(ether_ctx *h, double *mean, double *err) {
     if (!h || !mean || !err) return fail(ETHER_ERR_ARG, "null argument");
     Ctx &c = h->c;
-    if (c.n_groups < 2) return fail(ETHER_ERR_STATE, "per-repeat statistics need at least two REPEAT groups");
     std::vector<double> v(6 * (size_t)c.R);
     int rc = ether_avg(h, v.data());
     if (rc) return rc;
     const double rep = c.n_groups;
-    const double r1 = 1.0 / (rep * (rep - 1.0));
+    const double r1 = 1.0 / (rep * (rep - 1.0));  // +inf for one group: errors NaN, as the reference
     for (int sl = 0; sl < c.n_slots; ++sl)
         for (int q = 0; q < 6; ++q) {
             double sum = 0.0;
@@ -748,6 +756,7 @@ static int issue_step(Ctx &c, const ether_schedule *sch, bool ovrr, bool pt, boo
     if (meas) {
         CUDA_TRY(launch_energy_mag(c, true));
         CUDA_TRY(launch_measure(c));
+        if (c.spiral_ptr) CUDA_TRY(launch_spiral_measure(c));  // src/observable.f90:41
     }
     return ETHER_OK;
 }
@@ -801,7 +810,8 @@ extern "C" int ether_mcs(ether_ctx *h, const ether_schedule *sch, int32_t step0,
             }
         } else {
             std::string key(sig.begin(), sig.end());
-            key += std::to_string(c.vec_bytes * 10 + c.ising_vpt) + "/" + std::to_string(sch->ovrr_para);
+            key += std::to_string(c.vec_bytes * 10 + c.ising_vpt) + "/" + std::to_string(sch->ovrr_para) +
+                   (c.spiral_ptr ? "/s" : "");
             auto it = c.graphs.find(key);
             if (it == c.graphs.end()) {
                 if (c.graphs.size() >= 64) {
@@ -847,6 +857,20 @@ extern "C" int ether_reset_accept_counts(ether_ctx *h) {
     if (!h) return fail(ETHER_ERR_ARG, "null context");
     Ctx &c = h->c;
     CUDA_TRY(cudaMemsetAsync(c.acc_count, 0, sizeof(unsigned long long) * c.R, c.stream));
+    CUDA_TRY(cudaMemsetAsync(c.acc_slot, 0, sizeof(unsigned long long) * c.R, c.stream));
+    CUDA_TRY(cudaMemsetAsync(c.acc_mark, 0, sizeof(unsigned long long) * c.R, c.stream));
+    return ETHER_OK;
+}
+
+// Accepted Metropolis moves per temperature: the count src/ether.f90:173 accumulates on the
+// rank that owns a temperature, here per (group, slot) however PT moved the replicas.
+extern "C" int ether_get_slot_accept_counts(ether_ctx *h, uint64_t *counts) {
+    if (!h || !counts) return fail(ETHER_ERR_ARG, "null argument");
+    Ctx &c = h->c;
+    if (!c.beta_set) return fail(ETHER_ERR_STATE, "beta not set");
+    CUDA_TRY(launch_acc_bin(c));
+    CUDA_TRY(cudaMemcpyAsync(counts, c.acc_slot, sizeof(uint64_t) * c.R, cudaMemcpyDeviceToHost, c.stream));
+    CUDA_TRY(cudaStreamSynchronize(c.stream));
     return ETHER_OK;
 }
 

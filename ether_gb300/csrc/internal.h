@@ -93,6 +93,13 @@ struct Ctx {
     double *acc_host = nullptr;                // R: pinned host copy
     int32_t *spiral_ptr = nullptr, *spiral_nbr = nullptr;  // spiral partners, CSR in storage order
     long spiral_count = 0;
+    double *spiral_part = nullptr;  // R * spiral_blocks * 3: block partials of the spiral sum
+    double *spiral_sums = nullptr;  // 4R per (group, slot): samples, x, x^2, x^4
+    int spiral_blocks = 0;
+    // acceptance by temperature: acc_count is per replica; acc_slot[g * n_slots + slot]
+    // collects each replica's accepts at the slot it held, binned before every PT swap
+    unsigned long long *acc_slot = nullptr;  // R
+    unsigned long long *acc_mark = nullptr;  // R: acc_count at the last binning
     uint32_t *stream_id = nullptr;  // R
     uint32_t *step = nullptr;       // R (Metropolis sweep counter)
     uint32_t *ovrr_step = nullptr;  // R
@@ -126,6 +133,8 @@ cudaError_t launch_energy_mag(Ctx &c, bool want_energy);
 cudaError_t launch_measure(Ctx &c);
 cudaError_t launch_record(Ctx &c, int t, bool want_e, double *mser, double *eser);
 cudaError_t launch_pt(Ctx &c, int set_swap_count);
+cudaError_t launch_acc_bin(Ctx &c);
+cudaError_t launch_spiral_measure(Ctx &c);
 int energy_blocks(const Ctx &c);
 int plain_sweep(Ctx &c);  // one Metropolis sweep of every replica (ETHER_OK or an error code)
 void set_error(const std::string &msg);

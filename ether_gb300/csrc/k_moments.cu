@@ -94,6 +94,24 @@ __global__ void finish3_kernel(const double *__restrict__ part, int nblk, int R,
     for (int j = 0; j < 3; ++j) out[(size_t)r * stride + off + j] = m[j];
 }
 
+// src/get_spiral_state.f90:118-123 at one measurement step: x = |sum| / spiral_count,
+// accumulated at the (group, slot) position of each replica.
+__global__ void spiral_measure_kernel(const double *__restrict__ part, int nblk, int R, int n_slots,
+                                      const int32_t *__restrict__ slot_of_rep, double inv_count,
+                                      double *__restrict__ sums) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    double m[3] = {0, 0, 0};
+    for (int b = 0; b < nblk; ++b)
+        for (int j = 0; j < 3; ++j) m[j] += part[((size_t)r * nblk + b) * 3 + j];
+    const double x = sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]) * inv_count;
+    double *a = sums + 4 * ((size_t)(r / n_slots) * n_slots + slot_of_rep[r]);
+    a[0] += 1.0;
+    a[1] += x;
+    a[2] += x * x;
+    a[3] += (x * x) * (x * x);
+}
+
 int nblocks(const Ctx &c) {
     long need = (c.N + kBs - 1) / kBs;
     long cap = (long)c.sm_count * 4 / (c.R > 0 ? c.R : 1);
@@ -101,6 +119,16 @@ int nblocks(const Ctx &c) {
 }
 
 }  // namespace
+
+cudaError_t launch_spiral_measure(Ctx &c) {
+    spiral_kernel<<<dim3(c.spiral_blocks, c.R), kBs, 0, c.stream>>>(c.spins4, c.N, c.spiral_ptr, c.spiral_nbr,
+                                                                   c.spiral_part);
+    spiral_measure_kernel<<<(c.R + 127) / 128, 128, 0, c.stream>>>(
+        c.spiral_part, c.spiral_blocks, c.R, c.n_slots, c.slot_of_rep, 1.0 / (double)c.spiral_count, c.spiral_sums);
+    c.launches += 2;
+    return cudaGetLastError();
+}
+
 }  // namespace ether
 
 using namespace ether;
@@ -222,6 +250,18 @@ extern "C" int ether_spiral_setup(ether_ctx *h, double ss_dis, const double ss_d
     MCUDA(cudaMemcpy(c.spiral_ptr, ptr.data(), ptr.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
     MCUDA(cudaMemcpy(c.spiral_nbr, nbr.data(), nbr.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
     c.spiral_count = total;
+    // accumulators of the per-sample spiral state (src/get_spiral_state.f90:118-123), read
+    // at every measurement step of ether_mcs from now on
+    if (c.spiral_part) cudaFree(c.spiral_part);
+    if (c.spiral_sums) cudaFree(c.spiral_sums);
+    c.spiral_part = c.spiral_sums = nullptr;
+    c.spiral_blocks = nblocks(c);
+    MCUDA(cudaMalloc((void **)&c.spiral_part, (size_t)c.R * c.spiral_blocks * 3 * sizeof(double)));
+    MCUDA(cudaMalloc((void **)&c.spiral_sums, (size_t)c.R * 4 * sizeof(double)));
+    MCUDA(cudaMemset(c.spiral_sums, 0, (size_t)c.R * 4 * sizeof(double)));
+    // captured MCS chunks hold the old partner tables: capture again
+    for (auto &kv : c.graphs) cudaGraphExecDestroy(kv.second);
+    c.graphs.clear();
     if (count) *count = total;
     return ETHER_OK;
 }
@@ -250,5 +290,27 @@ extern "C" int ether_spiral_state(ether_ctx *h, double *ss) {
         const double *m = v.data() + 3 * r;
         ss[r] = std::sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]) / (double)c.spiral_count;
     }
+    return ETHER_OK;
+}
+
+// get_spiral_state 'avg_spiral_state' (src/get_spiral_state.f90:127-140) per (group, slot):
+// out(3, R) = <x>, U = 1.5 - 0.5 <x^4> / <x^2>^2, chi = beta (<x^2> - <x>^2) spiral_count.
+extern "C" int ether_spiral_avg(ether_ctx *h, double *out) {
+    if (!h || !out) return mfail(ETHER_ERR_ARG, "null argument");
+    Ctx &c = h->c;
+    if (!c.spiral_sums) return mfail(ETHER_ERR_STATE, "ether_spiral_setup first");
+    std::vector<double> s((size_t)4 * c.R);
+    MCUDA(cudaMemcpyAsync(s.data(), c.spiral_sums, s.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    MCUDA(cudaStreamSynchronize(c.stream));
+    for (int g = 0; g < c.n_groups; ++g)
+        for (int sl = 0; sl < c.n_slots; ++sl) {
+            const size_t idx = (size_t)g * c.n_slots + sl;
+            const double *a = s.data() + 4 * idx;
+            const double x = a[1] / a[0], x2 = a[2] / a[0], x4 = a[3] / a[0];
+            double *o = out + 3 * idx;
+            o[0] = x;
+            o[1] = 1.5 - 0.5 * (x4 / (x2 * x2));
+            o[2] = c.beta_slots[sl] * (x2 - x * x) * (double)c.spiral_count;
+        }
     return ETHER_OK;
 }

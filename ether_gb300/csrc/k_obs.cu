@@ -300,12 +300,37 @@ __global__ void pt_bump_kernel(int32_t *__restrict__ swap, int32_t *__restrict__
     }
 }
 
+// Accepts since the last binning go to the (group, slot) position each replica holds now;
+// positions are a permutation of the replicas within a group, so no two threads collide.
+__global__ void acc_bin_kernel(const unsigned long long *__restrict__ acc_count,
+                               unsigned long long *__restrict__ acc_mark,
+                               const int32_t *__restrict__ slot_of_rep, int n_slots, int R,
+                               unsigned long long *__restrict__ acc_slot) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    const unsigned long long now = acc_count[r];
+    const int pos = (r / n_slots) * n_slots + slot_of_rep[r];
+    acc_slot[pos] += now - acc_mark[r];
+    acc_mark[r] = now;
+}
+
+cudaError_t launch_acc_bin(Ctx &c) {
+    acc_bin_kernel<<<(c.R + 127) / 128, 128, 0, c.stream>>>(c.acc_count, c.acc_mark, c.slot_of_rep,
+                                                            c.n_slots, c.R, c.acc_slot);
+    c.launches++;
+    return cudaGetLastError();
+}
+
 // set >= 0: use swap_count = set (ether_parallel_tempering); set < 0: increment the device
 // counter first (the loop of src/ether.f90:190-192 inside ether_mcs).
 cudaError_t launch_pt(Ctx &c, int set_swap_count) {
     const int copy_mode = (c.flags & ETHER_FLAG_PT_REFERENCE_COPY) ? 1 : 0;
     const int npairs = c.n_slots / 2 + 1;
     const int nt = npairs * c.n_groups;
+    {
+        cudaError_t e = launch_acc_bin(c);  // accepts so far belong to the slots held before the swap
+        if (e != cudaSuccess) return e;
+    }
     pt_bump_kernel<<<1, 32, 0, c.stream>>>(c.swap_dev, c.pt_accepts, set_swap_count >= 0 ? 1 : 0,
                                            set_swap_count);
     c.launches++;

@@ -11,6 +11,7 @@ under their reference names.  Arrays keep the reference's Fortran layouts:
 """
 import ctypes as C
 import math
+import os
 
 import numpy as np
 
@@ -274,6 +275,15 @@ class Sweep:
         abi.check(self.lib.ether_get_accept_counts(self.h, out.ctypes.data_as(abi.PU64)))
         return out
 
+    def slot_accept_counts(self):
+        """Accepted moves per (group, slot) position, index group * n_slots + slot."""
+        out = np.zeros(self.R, dtype=np.uint64)
+        abi.check(self.lib.ether_get_slot_accept_counts(self.h, out.ctypes.data_as(abi.PU64)))
+        return out
+
+    def reset_accept_counts(self):
+        abi.check(self.lib.ether_reset_accept_counts(self.h))
+
     def info(self):
         i = abi.Info()
         abi.check(self.lib.ether_get_info(self.h, C.byref(i)))
@@ -315,6 +325,12 @@ class Sweep:
     def spiral_state(self):
         out = np.zeros(self.R, dtype=np.float64)
         abi.check(self.lib.ether_spiral_state(self.h, abi.dptr(out)))
+        return out
+
+    def spiral_avg(self):
+        """get_spiral_state 'avg_spiral_state' per (group, slot): (R, 3) = <x>, U, chi."""
+        out = np.zeros((self.R, 3), dtype=np.float64)
+        abi.check(self.lib.ether_spiral_avg(self.h, abi.dptr(out)))
         return out
 
     def autotune(self):
@@ -467,3 +483,17 @@ class Learned:
         i = abi.LearnInfo()
         abi.check(self.lib.ether_learn_get_info(self.h, C.byref(i)))
         return i
+
+
+def run(indir, outdir, parse_only=False, ranks=0, resume=False, quiet=True):
+    """src/ether.f90 for one input directory (ether_run): reads the deck in indir, runs the
+    temperature scan on the GPU and writes the reference's output files into outdir.
+    parse_only reads the deck and builds the lattice only (no GPU).  Returns the run info
+    as a dict."""
+    lib = abi.load()
+    info = abi.RunInfo()
+    info.ranks = int(ranks)
+    flags = ((abi.RUN_PARSE_ONLY if parse_only else 0) | (abi.RUN_QUIET if quiet else 0) |
+             (abi.RUN_RESUME if resume else 0))
+    abi.check(lib.ether_run(os.fsencode(indir), os.fsencode(outdir), flags, C.byref(info)))
+    return {k: getattr(info, k) for k, _ in abi.RunInfo._fields_}

@@ -33,6 +33,15 @@ module ether_gpu_mod
         integer(c_int32_t) :: sc(3), basis, flags
     end type ether_desc
 
+    integer(c_int), parameter :: ETHER_RUN_PARSE_ONLY = 1, ETHER_RUN_QUIET = 2, ETHER_RUN_RESUME = 4
+
+    type, bind(C) :: ether_run_info
+        integer(c_int32_t) :: ranks, model, n_sites, n_species, n_shells, n_temperatures, &
+                              repeat, n_rounds
+        integer(c_int64_t) :: site_updates     ! uint64_t in C
+        real(c_double)     :: seconds
+    end type ether_run_info
+
     type, bind(C) :: ether_schedule
         integer(c_int32_t) :: tmcs_eq, coa, ovrr
         real(c_double)     :: ovrr_para
@@ -204,6 +213,26 @@ module ether_gpu_mod
             import :: c_int, c_ptr, c_int32_t
             type(c_ptr), value :: learn
             integer(c_int32_t), value :: nsweeps
+        end function
+        ! per-temperature acceptance (src/ether.f90:173) and the spiral-state averages
+        ! (src/get_spiral_state.f90:127-140)
+        integer(c_int) function ether_get_slot_accept_counts(ctx, counts) bind(C, name="ether_get_slot_accept_counts")
+            import :: c_int, c_ptr, c_int64_t
+            type(c_ptr), value :: ctx
+            integer(c_int64_t), intent(out) :: counts(*)
+        end function
+        integer(c_int) function ether_spiral_avg(ctx, out) bind(C, name="ether_spiral_avg")
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(out) :: out(3, *)
+        end function
+        ! the whole program src/ether.f90 for one input directory; the directory names are
+        ! C strings: trim(dir)//c_null_char
+        integer(c_int) function ether_run(indir, outdir, flags, info) bind(C, name="ether_run")
+            import :: c_int, c_char, c_int32_t, ether_run_info
+            character(kind=c_char), intent(in) :: indir(*), outdir(*)
+            integer(c_int32_t), value :: flags
+            type(ether_run_info), intent(inout) :: info
         end function
     end interface
 end module ether_gpu_mod

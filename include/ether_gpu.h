@@ -188,6 +188,10 @@ int ether_record_series(ether_ctx *ctx, int32_t nsweeps, int32_t stride, double 
 /* Acceptance counters (accepted site updates per replica since the last reset). */
 int ether_get_accept_counts(ether_ctx *ctx, uint64_t *counts);
 int ether_reset_accept_counts(ether_ctx *ctx);
+/* The same counts per temperature: counts(R) indexed group * n_slots + slot, each replica's
+ * accepts credited to the slot it held when it made them (PT moves replicas between slots).
+ * src/ether.f90:173 accumulates this count on the rank that owns a temperature. */
+int ether_get_slot_accept_counts(ether_ctx *ctx, uint64_t *counts);
 
 /* Introspection used by tests and tools. */
 typedef struct ether_info {
@@ -249,6 +253,12 @@ int ether_spiral_setup(ether_ctx *ctx, double ss_dis, const double ss_direc[3], 
  * |sum_i sum_j S_i x S_j| / spiral_count per replica (the per-sample value the reference
  * accumulates into spiral_state_avg, _2_avg, _4_avg). */
 int ether_spiral_state(ether_ctx *ctx, double *ss);
+/* Once ether_spiral_setup has run, every measurement step of ether_mcs also accumulates the
+ * spiral state per (group, slot) (src/observable.f90:41, src/get_spiral_state.f90:118-123);
+ * ether_zero_avg clears it.  get_spiral_state 'avg_spiral_state'
+ * (src/get_spiral_state.f90:127-140) per (group, slot): out(3, R) = <x>,
+ * U = 1.5 - 0.5 <x^4>/<x^2>^2, chi = beta (<x^2> - <x>^2) spiral_count. */
+int ether_spiral_avg(ether_ctx *ctx, double *out);
 
 /* ------------------------------------------------------------------- batched sweeps ---- */
 /* The reference advances one lattice at one temperature per MPI rank (src/ether.f90:112-118,
@@ -387,6 +397,32 @@ int ether_build_lattice(int32_t nbasis, const double *basis_cart, const int32_t 
                         const double *abc, const int32_t sc[3], const char bc[3],
                         int32_t checkerboard, int32_t n_shells, const double *nbd_dis,
                         double tol, int32_t cap, double *ion, double *stgg, int32_t *nn);
+
+/* ------------------------------------------------------------------ the program ---- */
+/* src/ether.f90 for one input directory: reads in.ether, structure.vasp, j_exchange and,
+ * when asked for, single_ion_anisotropy and staggered from indir exactly as the reference's
+ * readers do, runs the temperature scan (every temperature a PT slot, every REPEAT a group
+ * of replicas, one ether_mcs loop) and writes the reference's output files into outdir:
+ * ETHER.obs, ETHER.spn, data/{magnetization,energy,moment_vectors,spiral_state_parameters,
+ * gss,nbd}.dat, data/fetched_lattice_network.xsf, data/graph.sh, spins/<T>spK.xsf, plus
+ * deck.txt (everything read, after src/parameters.f90).  A malformed deck gives
+ * ETHER_ERR_PARSE with the reference's message in ether_last_error. */
+enum {
+    ETHER_RUN_PARSE_ONLY = 1 << 0, /* read the deck, build the lattice, write deck.txt,
+                                      nbd.dat and the network file; no GPU work          */
+    ETHER_RUN_QUIET = 1 << 1,      /* nothing on stdout                                  */
+    ETHER_RUN_RESUME = 1 << 2      /* start every temperature from its record of
+                                      outdir/ETHER.spn, without fresh_spins: continue an
+                                      earlier run of the same deck                        */
+};
+typedef struct ether_run_info {
+    int32_t ranks;          /* in: temperatures per PT round, as mpirun -np (0 = all at once) */
+    int32_t model;          /* out: ETHER_MODEL_*                                             */
+    int32_t n_sites, n_species, n_shells, n_temperatures, repeat, n_rounds; /* out            */
+    uint64_t site_updates;  /* out: Metropolis attempts of the run                            */
+    double seconds;         /* out: wall time of the MCS loops                                */
+} ether_run_info;
+int ether_run(const char *indir, const char *outdir, int32_t flags, ether_run_info *info);
 
 #ifdef __cplusplus
 }
