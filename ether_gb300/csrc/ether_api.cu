@@ -943,6 +943,7 @@ std::map<std::vector<long>, int> g_tune_cache;  // variant per (model, L, R)
 }  // namespace
 
 static int variant_of(const Ctx &c) {
+    if (c.model == ETHER_MODEL_XYZ) return 5000 + c.xyz_variant;
     if (c.ising_stream) return 4000 + 10 * c.ising_vpt + (c.ising_cap ? 4 : 1);
     return (c.ising_persist ? 1000 : 0) + (c.ising_cap ? 2000 : 0) + c.vec_bytes * 10 + c.ising_vpt;
 }
@@ -951,7 +952,14 @@ static int variant_of(const Ctx &c) {
 //           + 10 * bytes per vector + vectors per thread
 //           or 4000 + 10 * vectors per thread and step + 1 / 4 (register cap): the
 //           shared-memory staged kernel (4011, 4014, 4021, 4041)
+//           or 5000 + 10 * sites per thread + register cap (blocks per SM) for the
+//           simple-cubic XYZ kernel (5011 .. 5015, 5021, 5022)
 static bool apply_variant(Ctx &c, int variant) {
+    if (c.model == ETHER_MODEL_XYZ) {
+        if (!xyz_variant_valid(variant - 5000)) return false;
+        c.xyz_variant = variant - 5000;
+        return true;
+    }
     if (variant == 4011 || variant == 4014 || variant == 4021 || variant == 4041) {
         const int vs = (variant / 10) % 10;
         if (!ising_stream_supported(c, vs)) return false;
@@ -975,13 +983,74 @@ static bool apply_variant(Ctx &c, int variant) {
     return true;
 }
 
+// The simple-cubic XYZ kernel's variants timed on both colour phases (three sweeps each);
+// the configuration and acceptance counters are restored afterwards.
+static int autotune_xyz(Ctx &c, int32_t *variant, float *best_ms) {
+    const std::vector<long> key = {c.model, c.L[0], c.L[1], c.L[2], c.R, (long)c.zeeman, (long)c.sia, (long)c.angle};
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            apply_variant(c, it->second);
+            if (variant) *variant = variant_of(c);
+            return ETHER_OK;
+        }
+    }
+    const size_t bytes = (size_t)c.R * c.N * sizeof(float4);
+    void *backup = nullptr;
+    unsigned long long *acc_backup = nullptr;
+    CUDA_TRY(cudaMalloc(&backup, bytes));
+    CUDA_TRY(cudaMalloc(&acc_backup, sizeof(unsigned long long) * c.R));
+    CUDA_TRY(cudaMemcpyAsync(backup, c.spins4, bytes, cudaMemcpyDeviceToDevice, c.stream));
+    CUDA_TRY(cudaMemcpyAsync(acc_backup, c.acc_count, sizeof(unsigned long long) * c.R, cudaMemcpyDeviceToDevice, c.stream));
+    int best_var = variant_of(c);
+    float best = 1e30f;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    for (int cand : {5011, 5012, 5013, 5014, 5015, 5021, 5022}) {
+        if (!apply_variant(c, cand)) continue;
+        CUDA_TRY(launch_xyz_sweep(c, 0));  // warm-up
+        CUDA_TRY(cudaEventRecord(e0, c.stream));
+        for (int k = 0; k < 3; ++k) {
+            CUDA_TRY(launch_xyz_sweep(c, 0));
+            CUDA_TRY(launch_xyz_sweep(c, 1));
+        }
+        CUDA_TRY(cudaEventRecord(e1, c.stream));
+        CUDA_TRY(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        ms /= 6.0f;
+        if (ms < best) {
+            best = ms;
+            best_var = cand;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    apply_variant(c, best_var);
+    CUDA_TRY(cudaMemcpyAsync(c.spins4, backup, bytes, cudaMemcpyDeviceToDevice, c.stream));
+    CUDA_TRY(cudaMemcpyAsync(c.acc_count, acc_backup, sizeof(unsigned long long) * c.R, cudaMemcpyDeviceToDevice, c.stream));
+    CUDA_TRY(cudaStreamSynchronize(c.stream));
+    cudaFree(backup);
+    cudaFree(acc_backup);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_cache[key] = best_var;
+    }
+    if (variant) *variant = best_var;
+    if (best_ms) *best_ms = best;
+    return ETHER_OK;
+}
+
 extern "C" int ether_autotune(ether_ctx *h, int32_t *variant, float *best_ms) {
     if (!h) return fail(ETHER_ERR_ARG, "null context");
     Ctx &c = h->c;
     if (variant) *variant = variant_of(c);
     if (best_ms) *best_ms = 0.f;
-    if (!c.fast || c.model != ETHER_MODEL_ISING) return ETHER_OK;
+    if (!c.fast) return ETHER_OK;
     if (!c.beta_set) return fail(ETHER_ERR_STATE, "beta not set");
+    if (c.model == ETHER_MODEL_XYZ) return autotune_xyz(c, variant, best_ms);
     const std::vector<long> key = {c.model, c.L[0], c.L[1], c.L[2], c.R};
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -1045,7 +1114,7 @@ extern "C" int ether_autotune(ether_ctx *h, int32_t *variant, float *best_ms) {
 extern "C" int ether_set_variant(ether_ctx *h, int32_t variant) {
     if (!h) return fail(ETHER_ERR_ARG, "null context");
     Ctx &c = h->c;
-    if (!c.fast || c.model != ETHER_MODEL_ISING) return ETHER_OK;
+    if (!c.fast) return ETHER_OK;
     if (!apply_variant(c, variant)) return fail(ETHER_ERR_ARG, "variant not available for this lattice");
     return ETHER_OK;
 }

@@ -87,6 +87,7 @@ struct Ctx {
     bool ising_persist = false;  // persistent simple-cubic Ising kernel
     bool ising_cap = false;      // register-capped (four blocks per SM) instantiation
     bool ising_stream = false;   // shared-memory staged simple-cubic Ising kernel
+    int xyz_variant = 11;        // simple-cubic XYZ kernel: 10 * sites per thread + blocks per SM cap
     int *err = nullptr;          // device: first bounded-wait failure of a kernel (0 = none)
     unsigned long long *acc_before = nullptr;  // R: acceptance counts at the start of a call
     double *acc_ratio = nullptr;               // R: device acceptance ratios of a call
@@ -124,6 +125,7 @@ struct Ctx {
 cudaError_t launch_ising_sweep(Ctx &c, int colour);
 bool ising_stream_supported(const Ctx &c, int vectors_per_step);
 cudaError_t launch_xyz_sweep(Ctx &c, int colour);
+bool xyz_variant_valid(int variant);
 cudaError_t launch_overrelax(Ctx &c, int colour, int pass, float part);
 cudaError_t launch_fresh(Ctx &c);
 cudaError_t launch_advance(Ctx &c, uint32_t *counter);

@@ -126,17 +126,17 @@ batch_phase_kernel(const BatchMember *__restrict__ members, const BatchSeg *__re
                 // exchange only, Marsaglia proposals: the options fold away at compile time
                 const XyzParams P0{0, 0, 0, 0.f, nullptr, nullptr, nullptr};
                 for (int rho = (int)S.first + (int)threadIdx.x; rho < end; rho += blockDim.x)
-                    acc += xyz_sc_site(A, P0, rho, beta_f, t, c3, m.seed, stream) ? 1u : 0u;
+                    acc += xyz_sc_site<kXyzExchange>(A, P0, rho, beta_f, t, c3, m.K, stream) ? 1u : 0u;
             } else {
                 for (int rho = (int)S.first + (int)threadIdx.x; rho < end; rho += blockDim.x)
-                    acc += xyz_sc_site(A, m.P, rho, beta_f, t, c3, m.seed, stream) ? 1u : 0u;
+                    acc += xyz_sc_site<kXyzGeneral>(A, m.P, rho, beta_f, t, c3, m.K, stream) ? 1u : 0u;
             }
         } else {  // kBXyzCsr
             float4 *sp = m.spins4 + (size_t)r * m.N;
             const float beta_f = m.beta_slot_f[m.slot_of_rep[r]];
             for (int rho = (int)S.first + (int)threadIdx.x; rho < end; rho += blockDim.x)
-                acc += xyz_csr_site(m.P, sp, m.col_off[colour], rho, m.row_ptr, m.nbr, m.jidx, m.J,
-                                    beta_f, t, c3, m.seed, stream) ? 1u : 0u;
+                acc += xyz_csr_site<kXyzGeneral>(m.P, sp, m.col_off[colour], rho, m.row_ptr, m.nbr, m.jidx,
+                                                 m.J, beta_f, t, c3, m.K, stream) ? 1u : 0u;
         }
         warp_add_count(m.acc_count + r, acc);
     }

@@ -8,13 +8,14 @@
 namespace ether {
 
 // ------------------------------------------------------------------ general lattice ----
+template <int OPT>
 __global__ void __launch_bounds__(256)
 xyz_csr_kernel(float4 *__restrict__ spins4, int N, int col_off, int n_c, uint32_t colour,
                const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ nbr,
                const uint16_t *__restrict__ jidx, const float *__restrict__ J, XyzParams P,
                const float *__restrict__ beta_slot_f, const int32_t *__restrict__ slot_of_rep,
                const uint32_t *__restrict__ stream_id, const uint32_t *__restrict__ step,
-               uint32_t seed, unsigned long long *__restrict__ acc_count) {
+               const RoundKeys K, unsigned long long *__restrict__ acc_count) {
     const int r = blockIdx.y;
     float4 *sp = spins4 + (size_t)r * N;
     const float beta_f = beta_slot_f[slot_of_rep[r]];
@@ -22,15 +23,19 @@ xyz_csr_kernel(float4 *__restrict__ spins4, int N, int col_off, int n_c, uint32_
     const uint32_t c3 = kMetro | (colour << 8);
     unsigned acc = 0;
     for (int rho = blockIdx.x * blockDim.x + threadIdx.x; rho < n_c; rho += gridDim.x * blockDim.x)
-        acc += xyz_csr_site(P, sp, col_off, rho, row_ptr, nbr, jidx, J, beta_f, t, c3, seed, k1) ? 1u : 0u;
+        acc += xyz_csr_site<OPT>(P, sp, col_off, rho, row_ptr, nbr, jidx, J, beta_f, t, c3, K, k1) ? 1u : 0u;
     warp_add_count_x(acc_count + r, acc);
 }
 
-__global__ void __launch_bounds__(256)
+// Simple cubic, colour-split arrays.  A block takes VPT * 256 consecutive ranks per step,
+// thread i the ranks i, i + 256, ... (coalesced), processed side by side (xyz_sc_sites);
+// MINB is the register cap (blocks per SM).
+template <int OPT, int VPT, int MINB>
+__global__ void __launch_bounds__(256, MINB)
 xyz_sc_kernel(float4 *__restrict__ spins4, int L1, int L2, int L3, FastDiv fH, FastDiv fL2, uint32_t colour, float jx,
               float jy, float jz, XyzParams P, const float *__restrict__ beta_slot_f,
               const int32_t *__restrict__ slot_of_rep, const uint32_t *__restrict__ stream_id,
-              const uint32_t *__restrict__ step, uint32_t seed,
+              const uint32_t *__restrict__ step, const RoundKeys K,
               unsigned long long *__restrict__ acc_count) {
     const int r = blockIdx.y;
     const int H = L1 >> 1;
@@ -42,8 +47,9 @@ xyz_sc_kernel(float4 *__restrict__ spins4, int L1, int L2, int L3, FastDiv fH, F
     const uint32_t k1 = stream_id[r], t = step[r];
     const uint32_t c3 = kMetro | (colour << 8);
     unsigned acc = 0;
-    for (int rho = blockIdx.x * blockDim.x + threadIdx.x; rho < half; rho += gridDim.x * blockDim.x)
-        acc += xyz_sc_site(A, P, rho, beta_f, t, c3, seed, k1) ? 1u : 0u;
+    const int tile = VPT * (int)blockDim.x;
+    for (int rho0 = blockIdx.x * tile + threadIdx.x; rho0 < half; rho0 += gridDim.x * tile)
+        acc += xyz_sc_sites<OPT, VPT>(A, P, rho0, (int)blockDim.x, half, beta_f, t, c3, K, k1);
     warp_add_count_x(acc_count + r, acc);
 }
 
@@ -171,27 +177,54 @@ static XyzParams xyz_params(const Ctx &c) {
     return P;
 }
 
+template <int OPT, int VPT, int MINB>
+static void launch_xyz_sc(Ctx &c, int colour, const XyzParams &P, const RoundKeys &K) {
+    const int bs = 256;
+    const int half = c.N / 2;
+    dim3 grid(blocks_for_x(c, (half + VPT - 1) / VPT, bs), c.R);
+    // single shell, single species: J(1,1,1,:)
+    const float jx = c.h_Jf[0], jy = c.h_Jf[1], jz = c.h_Jf[2];
+    xyz_sc_kernel<OPT, VPT, MINB><<<grid, bs, 0, c.stream>>>(
+        c.spins4, c.L[0], c.L[1], c.L[2], make_fastdiv((uint32_t)(c.L[0] / 2)), make_fastdiv((uint32_t)c.L[1]),
+        (uint32_t)colour, jx, jy, jz, P, c.beta_slot_f, c.slot_of_rep, c.stream_id, c.step, K, c.acc_count);
+}
+
+// xyz_variant = 10 * VPT + MINB (11 = one site per thread, no register cap)
+template <int OPT>
+static void launch_xyz_sc_opt(Ctx &c, int colour, const XyzParams &P, const RoundKeys &K) {
+    switch (c.xyz_variant) {
+        case 12: launch_xyz_sc<OPT, 1, 2>(c, colour, P, K); break;
+        case 13: launch_xyz_sc<OPT, 1, 3>(c, colour, P, K); break;
+        case 14: launch_xyz_sc<OPT, 1, 4>(c, colour, P, K); break;
+        case 15: launch_xyz_sc<OPT, 1, 5>(c, colour, P, K); break;
+        case 21: launch_xyz_sc<OPT, 2, 1>(c, colour, P, K); break;
+        case 22: launch_xyz_sc<OPT, 2, 2>(c, colour, P, K); break;
+        default: launch_xyz_sc<OPT, 1, 1>(c, colour, P, K); break;
+    }
+}
+
+bool xyz_variant_valid(int v) { return (v >= 11 && v <= 15) || v == 21 || v == 22; }
+
 cudaError_t launch_xyz_sweep(Ctx &c, int colour) {
     const int bs = 256;
     XyzParams P = xyz_params(c);
+    const RoundKeys K = round_keys(c.seed);
+    const bool exchange_only = !P.zeeman && !P.sia && !P.angle;
     if (c.fast) {
-        const int half = c.N / 2;
-        dim3 grid(blocks_for_x(c, half, bs), c.R);
-        // single shell, single species: J(1,1,1,:)
-        float jx = c.h_Jf[0], jy = c.h_Jf[1], jz = c.h_Jf[2];
-        xyz_sc_kernel<<<grid, bs, 0, c.stream>>>(c.spins4, c.L[0], c.L[1], c.L[2], make_fastdiv((uint32_t)(c.L[0] / 2)), make_fastdiv((uint32_t)c.L[1]),
-                                                 (uint32_t)colour, jx, jy, jz, P, c.beta_slot_f,
-                                                 c.slot_of_rep, c.stream_id, c.step, c.seed,
-                                                 c.acc_count);
+        if (exchange_only) launch_xyz_sc_opt<kXyzExchange>(c, colour, P, K);
+        else launch_xyz_sc_opt<kXyzGeneral>(c, colour, P, K);
     } else {
         const int n_c = c.col_off[colour + 1] - c.col_off[colour];
         if (n_c == 0) return cudaSuccess;
         dim3 grid(blocks_for_x(c, n_c, bs), c.R);
-        xyz_csr_kernel<<<grid, bs, 0, c.stream>>>(c.spins4, c.N, c.col_off[colour], n_c,
-                                                  (uint32_t)colour, c.t.row_ptr, c.t.nbr,
-                                                  c.t.jidx, c.t.J, P, c.beta_slot_f,
-                                                  c.slot_of_rep, c.stream_id, c.step, c.seed,
-                                                  c.acc_count);
+        if (exchange_only)
+            xyz_csr_kernel<kXyzExchange><<<grid, bs, 0, c.stream>>>(
+                c.spins4, c.N, c.col_off[colour], n_c, (uint32_t)colour, c.t.row_ptr, c.t.nbr, c.t.jidx,
+                c.t.J, P, c.beta_slot_f, c.slot_of_rep, c.stream_id, c.step, K, c.acc_count);
+        else
+            xyz_csr_kernel<kXyzGeneral><<<grid, bs, 0, c.stream>>>(
+                c.spins4, c.N, c.col_off[colour], n_c, (uint32_t)colour, c.t.row_ptr, c.t.nbr, c.t.jidx,
+                c.t.J, P, c.beta_slot_f, c.slot_of_rep, c.stream_id, c.step, K, c.acc_count);
     }
     c.launches++;
     return cudaGetLastError();

@@ -97,7 +97,8 @@ ETHER_HD float bits_f(uint32_t b) {
 // bits.  Below -87 the result is the smallest normal float: a uniform eta = 0 (log eta =
 // -inf in the reference's test) is still accepted, any larger eta is rejected.
 ETHER_HD float expf_neg(float x) {
-    if (x < -87.0f) return 0x1p-126f;
+    const bool tiny = x < -87.0f;  // a select, not an early return: no divergent exit
+    x = tiny ? 0.0f : x;
     float n = rintf(x * 1.44269502f);
     float r = x - n * 0.693359375f;
     r = r - n * -2.12194440e-4f;
@@ -109,7 +110,7 @@ ETHER_HD float expf_neg(float x) {
     p = fmaf(p, r, 0.5f);
     p = fmaf(p, r, 1.0f);
     p = fmaf(p, r, 1.0f);
-    return p * bits_f((uint32_t)((int)n + 127) << 23);
+    return tiny ? 0x1p-126f : p * bits_f((uint32_t)((int)n + 127) << 23);
 }
 
 // sin and cos for |x| <= 4: reduction by pi/2 (two-part constant), Taylor polynomials on
@@ -145,38 +146,47 @@ constexpr int kMarsagliaMaxPairs = 64;
 // (George_Marsaglia.f90:29-39) or ANGLE, then normalisation.  The Marsaglia pairs come in
 // order p = 0, 1, 2, ...: pair 0 is words 1,2 of block 0 (word 0 is eta); pair p >= 1 is
 // block (p+1)/2, words 0,1 for odd p and 2,3 for even p.  The first accepted pair wins.
-// Blocks 0 and 1 (pairs 0-2, 99% of sites) are evaluated without branches so a warp does
-// not serialise on the rejection loop; later pairs come from a loop taken by ~1% of sites.
-// Returns false if 64 pairs were all rejected (probability ~1e-43): no proposal.
+// Blocks 0 and 1 (pairs 0-2, 99% of sites) are drawn by the caller and chosen among with
+// selects, so every lane runs the same instructions; later pairs come from one loop taken
+// by ~1% of sites, after which the lanes reconverge.  Returns false if 64 pairs were all
+// rejected (probability ~1e-43): no proposal.
 struct Spin4 { float x, y, z, w; };
 
-ETHER_HD bool marsaglia(uint32_t c0, uint32_t t, uint32_t stream, uint32_t tag, uint32_t seed,
-                        const U4 &b0, float *v1o, float *v2o, float *so) {
-    const U4 b1 = draw(c0, t, stream, tag | (1u << 16), seed);
+ETHER_HD bool marsaglia(uint32_t c0, uint32_t t, uint32_t stream, uint32_t tag, const RoundKeys &K,
+                        const U4 &b0, const U4 &b1, float *v1o, float *v2o, float *so) {
     const float a0 = upm1(b0.y), a1 = upm1(b0.z);
     const float c0a = upm1(b1.x), c1a = upm1(b1.y);
     const float d0 = upm1(b1.z), d1 = upm1(b1.w);
     const float s0 = a0 * a0 + a1 * a1, s1 = c0a * c0a + c1a * c1a, s2 = d0 * d0 + d1 * d1;
-    if (s0 < 1.0f) { *v1o = a0; *v2o = a1; *so = s0; return true; }
-    if (s1 < 1.0f) { *v1o = c0a; *v2o = c1a; *so = s1; return true; }
-    if (s2 < 1.0f) { *v1o = d0; *v2o = d1; *so = s2; return true; }
-    for (int blk = 2; blk <= kMarsagliaMaxPairs / 2; ++blk) {
-        const U4 o = draw(c0, t, stream, tag | ((uint32_t)blk << 16), seed);
-        float v1 = upm1(o.x), v2 = upm1(o.y), s = v1 * v1 + v2 * v2;
-        if (s < 1.0f) { *v1o = v1; *v2o = v2; *so = s; return true; }
-        if (2 * blk == kMarsagliaMaxPairs) break;
-        v1 = upm1(o.z); v2 = upm1(o.w); s = v1 * v1 + v2 * v2;
-        if (s < 1.0f) { *v1o = v1; *v2o = v2; *so = s; return true; }
+    const bool k0 = s0 < 1.0f, k1 = s1 < 1.0f, k2 = s2 < 1.0f;
+    float v1 = k0 ? a0 : (k1 ? c0a : d0);
+    float v2 = k0 ? a1 : (k1 ? c1a : d1);
+    float s = k0 ? s0 : (k1 ? s1 : s2);
+    bool ok = k0 || k1 || k2;
+    if (!ok) {
+        for (int blk = 2; blk <= kMarsagliaMaxPairs / 2 && !ok; ++blk) {
+            const U4 o = draw_rk(c0, t, stream, tag | ((uint32_t)blk << 16), K);
+            float w1 = upm1(o.x), w2 = upm1(o.y), q = w1 * w1 + w2 * w2;
+            if (q < 1.0f) {
+                v1 = w1; v2 = w2; s = q; ok = true;
+            } else if (2 * blk != kMarsagliaMaxPairs) {
+                w1 = upm1(o.z); w2 = upm1(o.w); q = w1 * w1 + w2 * w2;
+                if (q < 1.0f) { v1 = w1; v2 = w2; s = q; ok = true; }
+            }
+        }
     }
-    return false;
+    *v1o = v1; *v2o = v2; *so = s;
+    return ok;
 }
 
+// b0, b1: blocks 0 and 1 of the site's draw (block 1 is used by Marsaglia only).
 ETHER_HD bool propose(bool angle, float dphi, const Spin4 &S, uint32_t c0, uint32_t t,
-                      uint32_t stream, uint32_t tag, uint32_t seed, const U4 &b0, Spin4 *out) {
+                      uint32_t stream, uint32_t tag, const RoundKeys &K, const U4 &b0, const U4 &b1,
+                      Spin4 *out) {
     float nx, ny, nz, nphi;
     if (!angle) {
         float v1, v2, s;
-        if (!marsaglia(c0, t, stream, tag, seed, b0, &v1, &v2, &s)) return false;
+        if (!marsaglia(c0, t, stream, tag, K, b0, b1, &v1, &v2, &s)) return false;
         float tq = sqrtf(1.0f - s);
         nx = (2.0f * v1) * tq;
         ny = (2.0f * v2) * tq;

@@ -25,14 +25,19 @@ struct XyzParams {
     const float *D;
 };
 
+// Option sets of the XYZ kernels: kXyzExchange folds the Zeeman, SIA and ANGLE branches away
+// at compile time (exchange only, Marsaglia proposals); kXyzGeneral reads them from P.
+enum : int { kXyzExchange = 0, kXyzGeneral = 1 };
+
 // ΔE of src/Hamiltonian.f90 for S -> n given the exchange field h.
+template <int OPT>
 __device__ __forceinline__ float delta_e(const XyzParams &P, int s, const float4 &S,
                                          const Spin4 &n, float hx, float hy, float hz) {
     float dx = n.x - S.x, dy = n.y - S.y, dz = n.z - S.z;
     float e = dx * hx;
     e = fmaf(dy, hy, e);
     e = fmaf(dz, hz, e);
-    if (P.zeeman || P.sia) {
+    if (OPT != kXyzExchange && (P.zeeman || P.sia)) {
         int si = P.species[s] - 1;
         if (P.zeeman) {
             const float *z = P.zee + 3 * si;
@@ -53,20 +58,44 @@ __device__ __forceinline__ float delta_e(const XyzParams &P, int s, const float4
     return e;
 }
 
-__device__ __forceinline__ bool metro_site(const XyzParams &P, float4 *sp, int s, uint32_t rho,
-                                           float hx, float hy, float hz, float beta_f,
-                                           uint32_t t, uint32_t c3, uint32_t seed, uint32_t stream) {
-    const float4 S = sp[s];
-    U4 b0 = draw(rho, t, stream, c3, seed);
-    float eta = u01(b0.x);
+// The Metropolis decision of one site from its state S, the exchange field h and blocks 0
+// and 1 of its draw (block 1 only for Marsaglia proposals): returns whether the proposal is
+// accepted and, if so, the new state in out.
+template <int OPT>
+__device__ __forceinline__ bool metro_decide(const XyzParams &P, int s, const float4 &S, const U4 &b0,
+                                             const U4 &b1, float hx, float hy, float hz, float beta_f,
+                                             uint32_t rho, uint32_t t, uint32_t c3, const RoundKeys &K,
+                                             uint32_t stream, float4 &out) {
+    const bool angle = OPT != kXyzExchange && P.angle != 0;
+    const float eta = u01(b0.x);
     Spin4 n;
-    Spin4 So{S.x, S.y, S.z, S.w};
-    if (!propose(P.angle != 0, P.dphi, So, rho, t, stream, c3, seed, b0, &n)) return false;
-    float e = delta_e(P, s, S, n, hx, hy, hz);
+    const Spin4 So{S.x, S.y, S.z, S.w};
+    if (!propose(angle, P.dphi, So, rho, t, stream, c3, K, b0, b1, &n)) return false;
+    const float e = delta_e<OPT>(P, s, S, n, hx, hy, hz);
     // exp evaluated on every lane (no divergent short-circuit); e <= 0 accepts regardless
     const float p = expf_neg(-(beta_f * fmaxf(e, 0.0f)));
-    bool acc = (e <= 0.0f) || (eta < p);
-    if (acc) sp[s] = make_float4(n.x, n.y, n.z, n.w);
+    out = make_float4(n.x, n.y, n.z, n.w);
+    return (e <= 0.0f) || (eta < p);
+}
+
+template <int OPT>
+__device__ __forceinline__ void site_draws(const XyzParams &P, uint32_t rho, uint32_t t, uint32_t c3,
+                                           const RoundKeys &K, uint32_t stream, U4 &b0, U4 &b1) {
+    b0 = draw_rk(rho, t, stream, c3, K);
+    b1 = U4{0u, 0u, 0u, 0u};
+    if (!(OPT != kXyzExchange && P.angle != 0)) b1 = draw_rk(rho, t, stream, c3 | (1u << 16), K);
+}
+
+template <int OPT>
+__device__ __forceinline__ bool metro_site(const XyzParams &P, float4 *sp, int s, uint32_t rho,
+                                           float hx, float hy, float hz, float beta_f,
+                                           uint32_t t, uint32_t c3, const RoundKeys &K, uint32_t stream) {
+    const float4 S = sp[s];
+    U4 b0, b1;
+    site_draws<OPT>(P, rho, t, c3, K, stream, b0, b1);
+    float4 n;
+    const bool acc = metro_decide<OPT>(P, s, S, b0, b1, hx, hy, hz, beta_f, rho, t, c3, K, stream, n);
+    if (acc) sp[s] = n;
     return acc;
 }
 
@@ -121,12 +150,13 @@ __device__ __forceinline__ Acc3 sc_field(const float4 *__restrict__ opp, int L1,
 }
 
 // One Metropolis update of rank rho of colour class `colour` on a general lattice.
+template <int OPT>
 __device__ __forceinline__ bool xyz_csr_site(const XyzParams &P, float4 *sp, int col_off, int rho,
                                              const int32_t *__restrict__ row_ptr,
                                              const int32_t *__restrict__ nbr,
                                              const uint16_t *__restrict__ jidx,
                                              const float *__restrict__ J, float beta_f, uint32_t t,
-                                             uint32_t c3, uint32_t seed, uint32_t stream) {
+                                             uint32_t c3, const RoundKeys &K, uint32_t stream) {
     const int s = col_off + rho;
     float hx = 0.f, hy = 0.f, hz = 0.f;
     for (int k = row_ptr[s]; k < row_ptr[s + 1]; ++k) {
@@ -136,7 +166,7 @@ __device__ __forceinline__ bool xyz_csr_site(const XyzParams &P, float4 *sp, int
         hy = fmaf(Jp[1], Sj.y, hy);
         hz = fmaf(Jp[2], Sj.z, hz);
     }
-    return metro_site(P, sp, s, (uint32_t)rho, hx, hy, hz, beta_f, t, c3, seed, stream);
+    return metro_site<OPT>(P, sp, s, (uint32_t)rho, hx, hy, hz, beta_f, t, c3, K, stream);
 }
 
 // One Metropolis update of rank rho of the simple-cubic colour array `own` (the other
@@ -149,15 +179,53 @@ struct XyzSc {
     uint32_t colour;
     float jx, jy, jz;
 };
+template <int OPT>
 __device__ __forceinline__ bool xyz_sc_site(const XyzSc &A, const XyzParams &P, int rho,
-                                            float beta_f, uint32_t t, uint32_t c3, uint32_t seed,
+                                            float beta_f, uint32_t t, uint32_t c3, const RoundKeys &K,
                                             uint32_t stream) {
     const int row = (int)fdiv((uint32_t)rho, A.fH);
     const int xh = rho - row * A.H;
     const int z = (int)fdiv((uint32_t)row, A.fL2), y = row - z * A.L2;
     const int p = (y + z + (int)A.colour) & 1;
     Acc3 h = sc_field(A.opp, A.L1, A.L2, A.L3, A.H, xh, y, z, p, A.jx, A.jy, A.jz);
-    return metro_site(P, A.own, rho, (uint32_t)rho, h.x, h.y, h.z, beta_f, t, c3, seed, stream);
+    return metro_site<OPT>(P, A.own, rho, (uint32_t)rho, h.x, h.y, h.z, beta_f, t, c3, K, stream);
+}
+
+// VPT sites rho0 + j * step (j < VPT, all < n) in three passes -- loads and exchange fields,
+// the Philox blocks, then decisions and stores -- so that the independent chains of the
+// sites interleave.  Returns the number of accepted updates.
+template <int OPT, int VPT>
+__device__ __forceinline__ unsigned xyz_sc_sites(const XyzSc &A, const XyzParams &P, int rho0, int step,
+                                                 int n, float beta_f, uint32_t t, uint32_t c3,
+                                                 const RoundKeys &K, uint32_t stream) {
+    float4 S[VPT];
+    Acc3 h[VPT];
+#pragma unroll
+    for (int j = 0; j < VPT; ++j) {
+        const int rho = min(rho0 + j * step, n - 1);  // a clamped duplicate is never stored
+        const int row = (int)fdiv((uint32_t)rho, A.fH);
+        const int xh = rho - row * A.H;
+        const int z = (int)fdiv((uint32_t)row, A.fL2), y = row - z * A.L2;
+        const int p = (y + z + (int)A.colour) & 1;
+        h[j] = sc_field(A.opp, A.L1, A.L2, A.L3, A.H, xh, y, z, p, A.jx, A.jy, A.jz);
+        S[j] = A.own[rho];
+    }
+    U4 b0[VPT], b1[VPT];
+#pragma unroll
+    for (int j = 0; j < VPT; ++j) site_draws<OPT>(P, (uint32_t)(rho0 + j * step), t, c3, K, stream, b0[j], b1[j]);
+    unsigned acc = 0;
+#pragma unroll
+    for (int j = 0; j < VPT; ++j) {
+        const int rho = rho0 + j * step;
+        float4 nv;
+        const bool a = metro_decide<OPT>(P, min(rho, n - 1), S[j], b0[j], b1[j], h[j].x, h[j].y, h[j].z,
+                                         beta_f, (uint32_t)rho, t, c3, K, stream, nv);
+        if (a && rho < n) {
+            A.own[rho] = nv;
+            ++acc;
+        }
+    }
+    return acc;
 }
 
 }  // namespace ether

@@ -221,8 +221,11 @@ int ether_end_sweep(ether_ctx *ctx);
 
 /* Autotuner: times the kernel variants of this context's fast path on its own data
  * (spins and counters are restored) and keeps the fastest; the choice is cached per size
- * class for the process.  variant = bytes per thread * 10 + vectors per thread (Ising
- * simple cubic); best_ms = one colour phase.  Either output may be NULL. */
+ * class for the process.  Ising simple cubic: variant = 1000 (persistent) + 2000 (register
+ * cap) + bytes per vector * 10 + vectors per thread, or 4000 + 10 * vectors per step + 1 / 4
+ * (shared-memory staged kernel).  XYZ simple cubic: variant = 5000 + 10 * sites per thread +
+ * blocks per SM of the register cap (5011 .. 5015, 5021, 5022).  best_ms = one colour phase.  Either
+ * output may be NULL. */
 int ether_autotune(ether_ctx *ctx, int32_t *variant, float *best_ms);
 /* Force a kernel variant (same encoding as ether_autotune). */
 int ether_set_variant(ether_ctx *ctx, int32_t variant);

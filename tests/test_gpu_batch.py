@@ -105,7 +105,7 @@ def test_batch_autotune_restores_state_and_keeps_parity():
     batch = eg.Batch([sw for _, sw in A])
     before = states(A)
     cfg, ms = batch.autotune()
-    assert cfg[0] in (128, 256) and cfg[1] in (1, 2, 4, 8) and cfg[2] >= 1 and cfg[3] in (0, 1)
+    assert cfg[0] in (128, 256) and cfg[1] in (1, 2, 4, 8, 16) and cfg[2] >= 1 and cfg[3] in (0, 1)
     assert ms > 0.0
     assert_same(states(A), before)
     batch.metropolis(3)

@@ -146,7 +146,7 @@ def _ladder_sweep(model, L, temps, groups, seed=5):
 def test_slot_accept_counts_follow_the_slots():
     """Per-(group, slot) acceptance equals each replica's accepts credited, step by step, to
     the slot it held during that step; without PT it equals the per-replica count."""
-    lat, sw = _ladder_sweep(eg.MODEL_ISING, 8, [30.0, 45.0, 55.0, 70.0], 2)
+    lat, sw = _ladder_sweep(eg.MODEL_ISING, 8, [46.0, 50.0, 54.0, 58.0], 2)
     sw.metropolis(5, accept=False)
     np.testing.assert_array_equal(sw.slot_accept_counts(), sw.accept_counts())
     sw.reset_accept_counts()

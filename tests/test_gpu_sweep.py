@@ -107,14 +107,19 @@ def test_ising_pyrochlore_two_shells_bit_exact():
     assert sw.info().n_colours > 2
 
 
-def xyz_replay(lat, shells, kT, sweeps, flags=0, seed=1992, stream=3, **kw):
+def xyz_replay(lat, shells, kT, sweeps, flags=0, seed=1992, stream=3, variant=None, autotune=False,
+               **kw):
     sw, osys = make_pair(lat, eg.MODEL_XYZ, shells, flags=flags, seed=seed, **kw)
     beta = beta_of(kT)
     sw.set_beta(beta)
+    if variant is not None:
+        sw.set_variant(variant)
     sw.set_streams(stream=[stream], step=[0])
     ncol, col, rank = osys.colouring()
     ion = random_xyz(lat, 11)
     sw.set_spins(ion)
+    if autotune:
+        sw.autotune()
     sp4 = osys.spin4(ion)
     ion64 = ion.copy()
     for t in range(sweeps):
@@ -135,6 +140,28 @@ def test_xyz_sc_matches_fp32_mirror(L, flags, angle):
     np.testing.assert_array_equal(g[:, 2].astype(np.float32), sp4[:, 1])
     np.testing.assert_array_equal(g[:, 3].astype(np.float32), sp4[:, 2])
     np.testing.assert_array_equal(g[:, 5].astype(np.float32), sp4[:, 3])
+
+
+# every simple-cubic XYZ kernel variant (sites per thread, register cap), for both option
+# sets (exchange only with Marsaglia proposals, and ANGLE with a Zeeman field); (20, 6, 6)
+# has 360 sites per colour, so the two-site variants meet a ragged last tile
+@pytest.mark.parametrize("variant", [5011, 5012, 5013, 5014, 5015, 5021, 5022])
+@pytest.mark.parametrize("opts", [{}, {"angle": True, "dphi": 0.7, "zeeman": True, "h": (0.0, 0.5, 1.0)}])
+def test_xyz_sc_every_kernel_variant_matches_fp32_mirror(variant, opts):
+    lat = eg.simple_cubic((20, 6, 6))
+    sw, osys, sp4, ion64, g = xyz_replay(lat, FM, 1.443, 12, variant=variant, **opts)
+    assert sw.info().fast_path == 1
+    for k, col in ((1, 0), (2, 1), (3, 2), (5, 3)):
+        np.testing.assert_array_equal(g[:, k].astype(np.float32), sp4[:, col])
+
+
+def test_xyz_autotuner_restores_state_and_matches_fp32_mirror():
+    lat = eg.simple_cubic(16)
+    sw, osys, sp4, ion64, g = xyz_replay(lat, FM, 1.443, 10, autotune=True)
+    v, _ = sw.autotune()
+    assert 5011 <= v <= 5022
+    for k, col in ((1, 0), (2, 1), (3, 2), (5, 3)):
+        np.testing.assert_array_equal(g[:, k].astype(np.float32), sp4[:, col])
 
 
 def test_xyz_zeeman_sia_pyrochlore_matches_fp32_mirror():
