@@ -22,9 +22,10 @@ implies.
 --impl reference times the oracle's CPU restatement on all host cores (the Fortran reference
 cannot be built: no gfortran / MPI on this image or the GPU machine).
 --model sq times only the structure factor (for profiling).
---model program times the whole program (ether_run) on the 16^3 Ising deck of the
-reference's simple-cubic example: deck read, lattice, 19 temperatures x 10 REPEATs x 5000 MCS
-with measurements, and every output file written.
+--model program times the whole program (ether_run) on a deck (--deck): the 16^3 Ising deck
+(19 temperatures x 10 REPEATs x 5000 MCS) or the 32^3 Heisenberg + overrelaxation deck (29
+temperatures x 10 REPEATs x 20000 MCS): deck read, lattice, MCS loop with measurements, and
+every output file written.
 """
 import argparse
 import ctypes as C
@@ -468,28 +469,38 @@ def run_learned_sweep(L=64, R=256, sweeps=3):
     return res
 
 
-PROGRAM_DECK = ("model = ising\nmcs = 5000 3000\ntemp = 100 10 5\nspin = 1\nspecies = A\n"
-                "sc = 16 16 16\nbc = c c c\nrepeat = 10\ncoa = 10\nseed = 1992\ncb = .T.\n")
 PROGRAM_STRUCT = ("simple cubic\n1.0\n 1.0 0.0 0.0\n 0.0 1.0 0.0\n 0.0 0.0 1.0\n A\n 1\n"
                   "Direct\n 0.0 0.0 0.0\n")
 PROGRAM_J = "1\n1.0 1\nA A -1.0 -1.0 -1.0\n"
+# the simple-cubic decks of the benchmark's configurations (J = 1 meV ferromagnetic)
+PROGRAM_DECKS = {
+    "c1_ising_16": ("simple-cubic 16^3 Ising, 19 T (100..10 K) x 10 REPEAT x 5000 MCS (3000 "
+                    "equilibration), coa 10, Checkerboard staggered signs",
+                    "model = ising\nmcs = 5000 3000\ntemp = 100 10 5\nspin = 1\nspecies = A\n"
+                    "sc = 16 16 16\nbc = c c c\nrepeat = 10\ncoa = 10\nseed = 1992\ncb = .T.\n"),
+    "c2_heisenberg_32": ("simple-cubic 32^3 Heisenberg + overrelaxation every 5 MCS (one pass), "
+                         "29 T (150..10 K) x 10 REPEAT x 20000 MCS (10000 equilibration), coa 10",
+                         "model = xyz\nmcs = 20000 10000\ntemp = 150 10 5\nspin = 1\nspecies = A\n"
+                         "sc = 32 32 32\nbc = c c c\nrepeat = 10\ncoa = 10\nseed = 1992\n"
+                         "ovrr = .T. 1.0 5\n"),
+}
 
 
-def run_program(repeats=2):
-    """ether_run end to end on the 16^3 Ising deck (J = 1 meV ferromagnetic, 19 temperatures
-    from 100 K to 10 K, 10 REPEATs, 5000 MCS of which 3000 equilibrate, a measurement every 10
-    MCS, Checkerboard staggered signs): wall time from the deck on disk to the last output
-    file, and the MCS loop alone."""
+def run_program(deck="c1_ising_16", repeats=2):
+    """ether_run end to end on one of PROGRAM_DECKS: wall time from the deck on disk to the
+    last output file, and the MCS loop alone (best of `repeats` runs; the first also pays
+    the library's one-time set-up)."""
     import ether_gb300 as eg
+    what, text = PROGRAM_DECKS[deck]
     work = tempfile.mkdtemp(prefix="ether_run_")
     indir = os.path.join(work, "deck")
     os.makedirs(indir)
-    for name, text in (("in.ether", PROGRAM_DECK), ("structure.vasp", PROGRAM_STRUCT),
+    for name, body in (("in.ether", text), ("structure.vasp", PROGRAM_STRUCT),
                        ("j_exchange", PROGRAM_J)):
         with open(os.path.join(indir, name), "w") as f:
-            f.write(text)
+            f.write(body)
     best = None
-    for k in range(repeats):  # the first call also pays the library's one-time set-up
+    for k in range(repeats):
         t0 = time.perf_counter()
         info = eg.run(indir, os.path.join(work, "out%d" % k))
         wall = time.perf_counter() - t0
@@ -497,10 +508,44 @@ def run_program(repeats=2):
             best = (wall, info)
     wall, info = best
     ups = info["site_updates"]
-    return {"workload": "ether_run: simple-cubic 16^3 Ising deck, 19 T x 10 REPEAT x 5000 MCS, "
-                        "coa 10, every output file", "site_updates": ups,
+    return {"workload": "ether_run: " + what + ", every output file", "site_updates": ups,
             "wall_s": wall, "mcs_loop_s": info["seconds"],
             "updates_per_ns_wall": ups / wall / 1e9, "updates_per_ns_loop": ups / info["seconds"] / 1e9}
+
+
+def run_pyrochlore_pt(cells=12, replicas=64, mcs=2000, warmup=50):
+    """The frustrated Heisenberg configuration: pyrochlore 16-site cell x 12^3 (27648 sites),
+    J1 = +1 meV (antiferromagnetic in ETHER's sign) and J2 = -0.1 meV, single-ion anisotropy
+    D = (0, 0, -0.2) meV on every site (the reference's per-species diagonal form), Zeeman
+    H = (0, 0, 1) T with g = 2, 64 replicas on a geometric 1-50 K ladder, PT every 11 MCS,
+    measured every 10 MCS: ether_mcs timed with CUDA events."""
+    import ether_gb300 as eg
+    lat = eg.pyrochlore(cells, shells=(2.97243, 5.1484), tol=1e-3)
+    j = eg.couplings(1, [[(1, 1, (1.0, 1.0, 1.0))], [(1, 1, (-0.1, -0.1, -0.1))]], [1.0])
+    sia = np.array([[0.0, 0.0, -0.2e-3]])
+    sw = eg.Sweep.from_lattice(lat, j, np.array([1.0]), eg.MODEL_XYZ, replicas=replicas, seed=1992,
+                               zeeman=True, h=(0.0, 0.0, 1.0), g_factor=2.0, sia=True, sia_vec=sia)
+    temps = np.geomspace(1.0, 50.0, replicas)
+    sw.set_ladder(1.0 / (eg.KB_EV * temps))
+    sw.set_spins(lat.ion)
+    sw.fresh_spins()
+    sw.zero_avg()
+    swaps = sw.mcs(0, warmup, 10 ** 9, 10, pt=True, exchange_interval=11)
+    sw.sync()
+    ev = Events(sw.stream())
+    t0 = ev.record()
+    sw.mcs(warmup, mcs, warmup, 10, pt=True, exchange_interval=11, swap_count=swaps)
+    t1 = ev.record()
+    sw.sync()
+    ms = ev.ms(t0, t1)
+    ev.free([t0, t1])
+    ups = float(lat.N) * replicas * mcs
+    info = sw.info()
+    sw.close()
+    return {"workload": "pyrochlore 16 x %d^3 = %d sites, J1/J2, SIA, Zeeman, 64-replica geometric "
+                        "ladder 1-50 K, PT every 11 MCS, ether_mcs" % (cells, lat.N),
+            "mcs": mcs, "ms": ms, "value": ups / (ms * 1e6), "unit": "spin updates/ns",
+            "n_colours": info.n_colours}
 
 
 def cpu_reference(model, L, mcs, threads, seed=1992):
@@ -573,6 +618,7 @@ def main():
     ap.add_argument("--variant", type=int, default=0)
     ap.add_argument("--sq-cells", type=int, default=12)
     ap.add_argument("--chains", type=int, default=256)
+    ap.add_argument("--deck", default="c1_ising_16", choices=sorted(PROGRAM_DECKS))
     ap.add_argument("--batch-config", default="",
                     help="threads,units_per_thread,blocks_per_sm,walk (default: autotune)")
     args = ap.parse_args()
@@ -606,7 +652,7 @@ def main():
     if args.model == "program":
         if rank != 0:
             return 0
-        r = run_program()
+        r = run_program(args.deck)
         print(json.dumps({"metric": "program wall s", "value": r["wall_s"], "unit": "s",
                           "higher_is_better": False, "detail": r}))
         return 0
@@ -715,7 +761,9 @@ def main():
         comp["batch"] = bt
         comp["tau"] = run_tau(args.L)
         comp["learned"] = run_learned(args.L)
-        comp["program"] = run_program()
+        comp["program_c1"] = run_program("c1_ising_16")
+        comp["program_c2"] = run_program("c2_heisenberg_32", repeats=1)
+        comp["pyrochlore_pt"] = run_pyrochlore_pt()
         line["components"] = comp
     if not args.no_cpu:
         line["cpu_baseline"] = {k: v for k, v in

@@ -198,3 +198,40 @@ def test_per_repeat_with_one_group_gives_nan_errors():
     sw.mcs(0, 20, 5, 5)
     mean, err = sw.per_repeat()
     assert np.all(np.isfinite(mean)) and np.all(np.isnan(err))
+
+
+AFM_STRUCT = ("two species\n1.0\n 2.0 0 0\n 0 2.0 0\n 0 0 2.0\n A B\n 4 4\nDirect\n"
+              " 0 0 0\n 0 0.5 0.5\n 0.5 0 0.5\n 0.5 0.5 0\n 0 0 0.5\n 0 0.5 0\n 0.5 0 0\n 0.5 0.5 0.5\n")
+
+
+def test_run_two_species_staggered_spiral_deck(tmp_path):
+    """An XYZ deck with two species on the rock-salt split of a simple-cubic lattice,
+    antiferromagnetic A-B bonds, staggered signs from the 'staggered' file, overrelaxation and
+    the spiral-state observable: the general-lattice kernels, OVRR, the spiral accumulators
+    and every writer, through ether_run."""
+    deck_text = ("model = xyz\nmcs = 600 200\ntemp = 20 5 5\nspin = 1 1\nspecies = A B\nsc = 3 3 3\n"
+                 "repeat = 3\ncoa = 5\nstg = .T.\novrr = .T. 0.5 4\nssp = .T.\nss_dis = 1.01\n"
+                 "ss_lat = 5\nss_direc = 0 0 1\nspiral_capacity = 4\n")
+    indir = write_deck(str(tmp_path / "in"), deck_text, AFM_STRUCT, "1\n1.0 1\nA B 3.0 3.0 3.0\n",
+                       staggered="-1 B\n")
+    out = str(tmp_path / "out")
+    info = eg.run(indir, out)
+    deck = do.read_deck(indir)
+    n = 8 * 27
+    assert info["n_sites"] == n and info["n_temperatures"] == 4
+    obs = do.read_obs(os.path.join(out, "ETHER.obs"), 2)
+    spn = do.read_spn(os.path.join(out, "ETHER.spn"), n)
+    ion0, _, _ = _oracle_lattice(deck)
+    for name, text in do.output_files(deck, obs, spn, ion0).items():
+        assert open(os.path.join(out, "data", name), encoding="utf-8").read() == text, name
+    assert np.all(np.isfinite(obs[:, 1:20]))
+    assert np.all(obs[:, 14] > 0.0)                     # spiral state <|psi|>
+    # staggered |M| orders on cooling (A-B antiferromagnet, B counted with sign -1)
+    assert obs[-1, 1] > 0.6 and obs[-1, 1] > obs[0, 1]
+    # get_moment_vectors includes the staggered sign: B's moment, counted with -1, points
+    # along A's at the lowest temperature
+    mA, mB = obs[-1, 20:23], obs[-1, 23:26]
+    assert np.dot(mA, mB) > 0.0
+    for t in range(4):
+        nrm = np.linalg.norm(spn[t][:, 1:4], axis=1)
+        np.testing.assert_allclose(nrm, 1.0, atol=1e-6)
