@@ -188,6 +188,7 @@ int upload_ladder(Ctx &c) {
 
 void free_ctx(Ctx &c) {
     void *ptrs[] = {c.t.row_ptr, c.t.nbr, c.t.jidx, c.t.wstride, c.t.species, c.t.itype,
+                    c.t.ell_nbr, c.t.ell_j, c.t.ell_deg, c.t.J4, c.t.ell_ws,
                     c.t.type_base, c.t.type_half, c.t.J, c.t.Jd, c.t.zee, c.t.zeed, c.t.D,
                     c.t.mweight, c.t.site_of_storage, c.spins, c.spins4, c.beta_slot,
                     c.beta_slot_f, c.slot_of_rep, c.rep_of_slot, c.thr, c.stream_id,
@@ -407,6 +408,53 @@ extern "C" int ether_create(const ether_desc *d, ether_ctx **out) {
     TRY(dev_upload(c, &c.t.D, D));
     TRY(dev_upload(c, &c.t.mweight, mw));
     TRY(dev_upload(c, &c.t.site_of_storage, c.site_of_storage));
+    {
+        // ELL blocks per colour class: coalesced neighbour reads for the general-lattice
+        // kernels (XYZ: coupling index per entry; Ising: threshold-table stride per entry)
+        std::vector<uint16_t> deg(N);
+        c.ell_off.assign(c.ncol + 1, 0);
+        c.ell_width.assign(c.ncol, 0);
+        for (int col = 0; col < c.ncol; ++col) {
+            int w = 0;
+            for (int s = c.col_off[col]; s < c.col_off[col + 1]; ++s) {
+                const int dg = row_ptr[s + 1] - row_ptr[s];
+                if (dg > 65535) return bail(fail(ETHER_ERR_CAPACITY, "more than 65535 neighbours of one site"));
+                deg[s] = (uint16_t)dg;
+                w = std::max(w, dg);
+            }
+            c.ell_width[col] = w;
+            c.ell_off[col + 1] = c.ell_off[col] + (long)w * (c.col_off[col + 1] - c.col_off[col]);
+        }
+        const bool xyz = c.model == ETHER_MODEL_XYZ;
+        std::vector<int32_t> enb((size_t)c.ell_off[c.ncol], 0);
+        std::vector<uint16_t> ej(xyz ? (size_t)c.ell_off[c.ncol] : 0, 0);
+        std::vector<int32_t> ews(xyz ? 0 : (size_t)c.ell_off[c.ncol], 0);
+        for (int col = 0; col < c.ncol; ++col) {
+            const long n_c = c.col_off[col + 1] - c.col_off[col];
+            for (long rho = 0; rho < n_c; ++rho) {
+                const int s = c.col_off[col] + (int)rho;
+                for (int k = 0; k < deg[s]; ++k) {
+                    const size_t e = (size_t)c.ell_off[col] + (size_t)k * n_c + rho;
+                    enb[e] = nbr[row_ptr[s] + k];
+                    if (xyz) ej[e] = jidx[row_ptr[s] + k];
+                    else ews[e] = wstr[row_ptr[s] + k];
+                }
+                for (int k = deg[s]; k < c.ell_width[col]; ++k)  // padding: never read
+                    enb[(size_t)c.ell_off[col] + (size_t)k * n_c + rho] = s;
+            }
+        }
+        TRY(dev_upload(c, &c.t.ell_nbr, enb));
+        TRY(dev_upload(c, &c.t.ell_deg, deg));
+        if (xyz) {
+            std::vector<float4> j4(c.h_Jf.size() / 3);
+            for (size_t q = 0; q < j4.size(); ++q)
+                j4[q] = make_float4(c.h_Jf[3 * q], c.h_Jf[3 * q + 1], c.h_Jf[3 * q + 2], 0.f);
+            TRY(dev_upload(c, &c.t.ell_j, ej));
+            TRY(dev_upload(c, &c.t.J4, j4));
+        } else {
+            TRY(dev_upload(c, &c.t.ell_ws, ews));
+        }
+    }
     const size_t RN = (size_t)c.R * N;
     if (c.model == ETHER_MODEL_ISING) TRY(dev_alloc(c, &c.spins, RN));
     else TRY(dev_alloc(c, &c.spins4, RN));

@@ -41,6 +41,13 @@ struct DevTables {
     float *D = nullptr;           // nsp * 3 (SIA)
     double *mweight = nullptr;    // N: stgg * s(species)
     int32_t *site_of_storage = nullptr;  // N: 0-based site number of a storage index
+    // neighbour lists per colour class in ELL form: entry k of rank rho of colour c at
+    // ell_off[c] + k * n_c + rho (same order as the CSR), padded to the class's widest site
+    int32_t *ell_nbr = nullptr;   // storage indices
+    uint16_t *ell_j = nullptr;    // XYZ: coupling index (into J4)
+    int32_t *ell_ws = nullptr;    // Ising: stride of the threshold-table index
+    uint16_t *ell_deg = nullptr;  // N: neighbours of a storage index
+    float4 *J4 = nullptr;         // nJ: (Jxx, Jyy, Jzz, 0) in FP32
 };
 
 struct Ctx {
@@ -54,6 +61,8 @@ struct Ctx {
     int ncol = 0;
     int col_off[kMaxColours + 1] = {0};
     long nnz = 0;  // neighbour-list entries (CSR)
+    std::vector<long> ell_off;    // per colour: offset of its ELL block
+    std::vector<int> ell_width;   // per colour: entries per rank
     std::vector<int32_t> colour, rank, storage;  // per site (0-based index)
     std::vector<int32_t> site_of_storage;
     // fast simple-cubic path

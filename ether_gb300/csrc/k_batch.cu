@@ -124,7 +124,7 @@ batch_phase_kernel(const BatchMember *__restrict__ members, const BatchSeg *__re
             const float beta_f = m.beta_slot_f[m.slot_of_rep[r]];
             if (!m.P.zeeman && !m.P.sia && !m.P.angle) {
                 // exchange only, Marsaglia proposals: the options fold away at compile time
-                const XyzParams P0{0, 0, 0, 0.f, nullptr, nullptr, nullptr};
+                const XyzParams P0{0, 0, 0, 0.f, nullptr, nullptr, nullptr, 1};
                 for (int rho = (int)S.first + (int)threadIdx.x; rho < end; rho += blockDim.x)
                     acc += xyz_sc_site<kXyzExchange>(A, P0, rho, beta_f, t, c3, m.K, stream) ? 1u : 0u;
             } else {
@@ -230,6 +230,7 @@ BatchMember describe(const Ctx &c) {
     m.P.species = c.t.species;
     m.P.zee = c.t.zee;
     m.P.D = c.t.D;
+    m.P.nsp = c.nsp;
     if (!c.h_Jf.empty()) {
         m.jx = c.h_Jf[0];
         m.jy = c.h_Jf[1];

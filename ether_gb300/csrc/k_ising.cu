@@ -6,25 +6,122 @@
 
 namespace ether {
 
-// One thread = one group of eight consecutive sites of the colour class.
+// General lattice.  One thread = one group of eight consecutive ranks of the colour class
+// (one random-number group).  Neighbours come from the class's ELL block, entry k of rank rho
+// at k * n_c + rho: the eight ranks' entries are adjacent and a warp's are contiguous.  The
+// neighbour loads are unconditional (padding entries point at valid memory); the threshold
+// index idx = sum of stride * up-spin over the site's own entries.  The decision is
+// ising_csr_group's: same draws, same thresholds.
 __global__ void __launch_bounds__(256)
-ising_csr_kernel(uint8_t *__restrict__ spins, int N, int col_off, int n_c, uint32_t colour,
-                 const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ nbr,
-                 const int32_t *__restrict__ wstride, const uint16_t *__restrict__ itype,
+ising_ell_kernel(uint8_t *__restrict__ spins, int N, int col_off, int n_c, uint32_t colour,
+                 const int32_t *__restrict__ ell, const int32_t *__restrict__ ews,
+                 const uint16_t *__restrict__ deg, int width, const uint16_t *__restrict__ itype,
                  const int32_t *__restrict__ type_base, const int32_t *__restrict__ type_half,
                  const uint32_t *__restrict__ thr, int table_entries,
                  const int32_t *__restrict__ slot_of_rep, const uint32_t *__restrict__ stream_id,
                  const uint32_t *__restrict__ step, uint32_t seed,
                  unsigned long long *__restrict__ acc_count) {
     const int r = blockIdx.y;
-    IsingCsr A{spins + (size_t)r * N, col_off, n_c, row_ptr, nbr, wstride, itype, type_base,
-               type_half, thr + (size_t)slot_of_rep[r] * table_entries};
+    uint8_t *sp = spins + (size_t)r * N;
+    const uint32_t *tb = thr + (size_t)slot_of_rep[r] * table_entries;
     const uint32_t stream = stream_id[r], t = step[r];
     const uint32_t c3 = kMetro | (colour << 8);
     const int ng = (n_c + 7) >> 3;
     unsigned acc = 0;
-    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x)
-        acc += ising_csr_group(A, g, t, stream, c3, seed);
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
+        const int rho0 = 8 * g;
+        int idx[8], dg[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            idx[j] = 0;
+            dg[j] = rho0 + j < n_c ? (int)deg[col_off + rho0 + j] : 0;
+        }
+#pragma unroll 2
+        for (int k = 0; k < width; ++k) {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int rho = min(rho0 + j, n_c - 1);
+                const size_t e = (size_t)k * n_c + rho;
+                const int up = sp[ell[e]];
+                const int w = ews[e];
+                if (k < dg[j]) idx[j] += w * up;
+            }
+        }
+        const U4 hi = draw((uint32_t)g, t, stream, c3, seed);
+        bool have_lo = false;
+        U4 lo{0, 0, 0, 0};
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int rho = rho0 + j;
+            if (rho >= n_c) break;
+            const int s = col_off + rho;
+            const int own = sp[s];
+            const int ty = itype[s];
+            const uint32_t T = tb[type_base[ty] + own * type_half[ty] + idx[j]];
+            const uint32_t uh = half_of(hi, j), th = T >> 16;
+            bool flip = uh < th;
+            if (uh == th) {
+                if (!have_lo) {
+                    lo = draw((uint32_t)g, t, stream, c3 | (1u << 16), seed);
+                    have_lo = true;
+                }
+                flip = half_of(lo, j) <= (T & 0xFFFFu);
+            }
+            if (flip) {
+                sp[s] = (uint8_t)(own ^ 1);
+                ++acc;
+            }
+        }
+    }
+    warp_add_count(acc_count + r, acc);
+}
+
+// The same update with one site per thread, for colour classes too small to fill the GPU
+// with groups of eight: every lane draws its group's Philox block itself (the draws, and so
+// the decisions, are those of ising_ell_kernel).
+__global__ void __launch_bounds__(256)
+ising_ell_site_kernel(uint8_t *__restrict__ spins, int N, int col_off, int n_c, uint32_t colour,
+                      const int32_t *__restrict__ ell, const int32_t *__restrict__ ews,
+                      const uint16_t *__restrict__ deg, int width, const uint16_t *__restrict__ itype,
+                      const int32_t *__restrict__ type_base, const int32_t *__restrict__ type_half,
+                      const uint32_t *__restrict__ thr, int table_entries,
+                      const int32_t *__restrict__ slot_of_rep, const uint32_t *__restrict__ stream_id,
+                      const uint32_t *__restrict__ step, uint32_t seed,
+                      unsigned long long *__restrict__ acc_count) {
+    const int r = blockIdx.y;
+    uint8_t *sp = spins + (size_t)r * N;
+    const uint32_t *tb = thr + (size_t)slot_of_rep[r] * table_entries;
+    const uint32_t stream = stream_id[r], t = step[r];
+    const uint32_t c3 = kMetro | (colour << 8);
+    unsigned acc = 0;
+    for (int rho = blockIdx.x * blockDim.x + threadIdx.x; rho < n_c; rho += gridDim.x * blockDim.x) {
+        const int s = col_off + rho;
+        const int dg = deg[s];
+        int idx = 0;
+#pragma unroll 6
+        for (int k = 0; k < width; ++k) {
+            const size_t e = (size_t)k * n_c + rho;
+            const int up = sp[ell[e]];
+            const int w = ews[e];
+            if (k < dg) idx += w * up;
+        }
+        const int own = sp[s];
+        const int ty = itype[s];
+        const uint32_t T = tb[type_base[ty] + own * type_half[ty] + idx];
+        const uint32_t g = (uint32_t)rho >> 3;
+        const int j = rho & 7;
+        const U4 hi = draw(g, t, stream, c3, seed);
+        const uint32_t uh = half_of(hi, j), th = T >> 16;
+        bool flip = uh < th;
+        if (uh == th) {
+            const U4 lo = draw(g, t, stream, c3 | (1u << 16), seed);
+            flip = half_of(lo, j) <= (T & 0xFFFFu);
+        }
+        if (flip) {
+            sp[s] = (uint8_t)(own ^ 1);
+            ++acc;
+        }
+    }
     warp_add_count(acc_count + r, acc);
 }
 
@@ -360,11 +457,22 @@ cudaError_t launch_ising_sweep(Ctx &c, int colour) {
     } else {
         const int n_c = c.col_off[colour + 1] - c.col_off[colour];
         if (n_c == 0) return cudaSuccess;
-        dim3 grid(blocks_for(c, (n_c + 7) / 8, bs), c.R);
-        ising_csr_kernel<<<grid, bs, 0, c.stream>>>(
-            c.spins, c.N, c.col_off[colour], n_c, (uint32_t)colour, c.t.row_ptr, c.t.nbr,
-            c.t.wstride, c.t.itype, c.t.type_base, c.t.type_half, c.thr, c.table_entries,
-            c.slot_of_rep, c.stream_id, c.step, c.seed, c.acc_count);
+        const int32_t *ell = c.t.ell_nbr + c.ell_off[colour];
+        const int32_t *ews = c.t.ell_ws + c.ell_off[colour];
+        const long groups = (long)c.R * ((n_c + 7) / 8);
+        if (groups < 2L * c.sm_count * bs) {  // too few groups of eight to fill the GPU
+            dim3 grid(blocks_for(c, n_c, bs), c.R);
+            ising_ell_site_kernel<<<grid, bs, 0, c.stream>>>(
+                c.spins, c.N, c.col_off[colour], n_c, (uint32_t)colour, ell, ews, c.t.ell_deg,
+                c.ell_width[colour], c.t.itype, c.t.type_base, c.t.type_half, c.thr, c.table_entries,
+                c.slot_of_rep, c.stream_id, c.step, c.seed, c.acc_count);
+        } else {
+            dim3 grid(blocks_for(c, (n_c + 7) / 8, bs), c.R);
+            ising_ell_kernel<<<grid, bs, 0, c.stream>>>(
+                c.spins, c.N, c.col_off[colour], n_c, (uint32_t)colour, ell, ews, c.t.ell_deg,
+                c.ell_width[colour], c.t.itype, c.t.type_base, c.t.type_half, c.thr, c.table_entries,
+                c.slot_of_rep, c.stream_id, c.step, c.seed, c.acc_count);
+        }
     }
     c.launches++;
     return cudaGetLastError();

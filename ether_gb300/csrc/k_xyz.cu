@@ -8,11 +8,34 @@
 namespace ether {
 
 // ------------------------------------------------------------------ general lattice ----
+// Exchange field of rank rho of a colour class from its ELL block (ell: entries k * n_c + rho,
+// coalesced across a warp), in the CSR's order -- the reference's nn order -- so the fmaf
+// chain rounds as the oracle's.
+__device__ __forceinline__ Acc3 ell_field(const float4 *__restrict__ sp, const int32_t *__restrict__ ell,
+                                          const uint16_t *__restrict__ ej, const float4 *__restrict__ J4,
+                                          int n_c, int width, int rho, int deg) {
+    // The padding entries point at valid memory (the site itself, coupling 0), so the loads
+    // are unconditional and can all be in flight at once; only the fmaf is predicated.
+    Acc3 h{0.f, 0.f, 0.f};
+#pragma unroll 6
+    for (int k = 0; k < width; ++k) {
+        const size_t e = (size_t)k * n_c + rho;
+        const float4 Jv = J4[ej[e]];
+        const float4 Sj = sp[ell[e]];
+        if (k < deg) {
+            h.x = fmaf(Jv.x, Sj.x, h.x);
+            h.y = fmaf(Jv.y, Sj.y, h.y);
+            h.z = fmaf(Jv.z, Sj.z, h.z);
+        }
+    }
+    return h;
+}
+
 template <int OPT>
 __global__ void __launch_bounds__(256)
-xyz_csr_kernel(float4 *__restrict__ spins4, int N, int col_off, int n_c, uint32_t colour,
-               const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ nbr,
-               const uint16_t *__restrict__ jidx, const float *__restrict__ J, XyzParams P,
+xyz_ell_kernel(float4 *__restrict__ spins4, int N, int col_off, int n_c, uint32_t colour,
+               const int32_t *__restrict__ ell, const uint16_t *__restrict__ ej,
+               const uint16_t *__restrict__ deg, int width, const float4 *__restrict__ J4, XyzParams P,
                const float *__restrict__ beta_slot_f, const int32_t *__restrict__ slot_of_rep,
                const uint32_t *__restrict__ stream_id, const uint32_t *__restrict__ step,
                const RoundKeys K, unsigned long long *__restrict__ acc_count) {
@@ -22,8 +45,11 @@ xyz_csr_kernel(float4 *__restrict__ spins4, int N, int col_off, int n_c, uint32_
     const uint32_t k1 = stream_id[r], t = step[r];
     const uint32_t c3 = kMetro | (colour << 8);
     unsigned acc = 0;
-    for (int rho = blockIdx.x * blockDim.x + threadIdx.x; rho < n_c; rho += gridDim.x * blockDim.x)
-        acc += xyz_csr_site<OPT>(P, sp, col_off, rho, row_ptr, nbr, jidx, J, beta_f, t, c3, K, k1) ? 1u : 0u;
+    for (int rho = blockIdx.x * blockDim.x + threadIdx.x; rho < n_c; rho += gridDim.x * blockDim.x) {
+        const int s = col_off + rho;
+        const Acc3 h = ell_field(sp, ell, ej, J4, n_c, width, rho, deg[s]);
+        acc += metro_site<OPT>(P, sp, s, (uint32_t)rho, h.x, h.y, h.z, beta_f, t, c3, K, k1) ? 1u : 0u;
+    }
     warp_add_count_x(acc_count + r, acc);
 }
 
@@ -57,13 +83,13 @@ xyz_sc_kernel(float4 *__restrict__ spins4, int L1, int L2, int L3, FastDiv fH, F
 // Reflection of overrelaxation.f90:44-47 about the exchange field A (get_ovrr_vec),
 // then normalisation.  A site with A = 0 is left unchanged (the reference would divide
 // by zero).  Pass `pass` < floor(ovrr_para) reflects every site; the last pass reflects a
-// site iff its uniform < part.
+// site iff its uniform < part.  Neighbours from the colour class's ELL block.
 __global__ void __launch_bounds__(256)
-ovrr_csr_kernel(float4 *__restrict__ spins4, int N, int col_off, int n_c, uint32_t colour,
-                int pass, float part, const int32_t *__restrict__ row_ptr,
-                const int32_t *__restrict__ nbr, const uint16_t *__restrict__ jidx,
-                const float *__restrict__ J, const uint32_t *__restrict__ stream_id,
-                const uint32_t *__restrict__ ovrr_step, uint32_t seed) {
+ovrr_ell_kernel(float4 *__restrict__ spins4, int N, int col_off, int n_c, uint32_t colour,
+                int pass, float part, const int32_t *__restrict__ ell, const uint16_t *__restrict__ ej,
+                const uint16_t *__restrict__ deg, int width, const float4 *__restrict__ J4,
+                const uint32_t *__restrict__ stream_id, const uint32_t *__restrict__ ovrr_step,
+                uint32_t seed) {
     const int r = blockIdx.y;
     float4 *sp = spins4 + (size_t)r * N;
     const uint32_t k1 = stream_id[r], t = ovrr_step[r];
@@ -74,14 +100,8 @@ ovrr_csr_kernel(float4 *__restrict__ spins4, int N, int col_off, int n_c, uint32
             U4 o = draw((uint32_t)rho, t, k1, c3 | ((uint32_t)pass << 16), seed);
             if (!(u01(o.x) < part)) continue;
         }
-        float hx = 0.f, hy = 0.f, hz = 0.f;
-        for (int k = row_ptr[s]; k < row_ptr[s + 1]; ++k) {
-            float4 Sj = sp[nbr[k]];
-            const float *Jp = J + 3 * jidx[k];
-            hx = fmaf(Jp[0], Sj.x, hx);
-            hy = fmaf(Jp[1], Sj.y, hy);
-            hz = fmaf(Jp[2], Sj.z, hz);
-        }
+        const Acc3 h = ell_field(sp, ell, ej, J4, n_c, width, rho, deg[s]);
+        const float hx = h.x, hy = h.y, hz = h.z;
         float4 S = sp[s];
         float d = hx * S.x;
         d = fmaf(hy, S.y, d);
@@ -174,6 +194,7 @@ static XyzParams xyz_params(const Ctx &c) {
     P.species = c.t.species;
     P.zee = c.t.zee;
     P.D = c.t.D;
+    P.nsp = c.nsp;
     return P;
 }
 
@@ -217,14 +238,18 @@ cudaError_t launch_xyz_sweep(Ctx &c, int colour) {
         const int n_c = c.col_off[colour + 1] - c.col_off[colour];
         if (n_c == 0) return cudaSuccess;
         dim3 grid(blocks_for_x(c, n_c, bs), c.R);
+        const int32_t *ell = c.t.ell_nbr + c.ell_off[colour];
+        const uint16_t *ej = c.t.ell_j + c.ell_off[colour];
         if (exchange_only)
-            xyz_csr_kernel<kXyzExchange><<<grid, bs, 0, c.stream>>>(
-                c.spins4, c.N, c.col_off[colour], n_c, (uint32_t)colour, c.t.row_ptr, c.t.nbr, c.t.jidx,
-                c.t.J, P, c.beta_slot_f, c.slot_of_rep, c.stream_id, c.step, K, c.acc_count);
+            xyz_ell_kernel<kXyzExchange><<<grid, bs, 0, c.stream>>>(
+                c.spins4, c.N, c.col_off[colour], n_c, (uint32_t)colour, ell, ej, c.t.ell_deg,
+                c.ell_width[colour], c.t.J4, P, c.beta_slot_f, c.slot_of_rep, c.stream_id, c.step, K,
+                c.acc_count);
         else
-            xyz_csr_kernel<kXyzGeneral><<<grid, bs, 0, c.stream>>>(
-                c.spins4, c.N, c.col_off[colour], n_c, (uint32_t)colour, c.t.row_ptr, c.t.nbr, c.t.jidx,
-                c.t.J, P, c.beta_slot_f, c.slot_of_rep, c.stream_id, c.step, K, c.acc_count);
+            xyz_ell_kernel<kXyzGeneral><<<grid, bs, 0, c.stream>>>(
+                c.spins4, c.N, c.col_off[colour], n_c, (uint32_t)colour, ell, ej, c.t.ell_deg,
+                c.ell_width[colour], c.t.J4, P, c.beta_slot_f, c.slot_of_rep, c.stream_id, c.step, K,
+                c.acc_count);
     }
     c.launches++;
     return cudaGetLastError();
@@ -235,10 +260,11 @@ cudaError_t launch_overrelax(Ctx &c, int colour, int pass, float part) {
     const int n_c = c.col_off[colour + 1] - c.col_off[colour];
     if (n_c == 0) return cudaSuccess;
     dim3 grid(blocks_for_x(c, n_c, bs), c.R);
-    ovrr_csr_kernel<<<grid, bs, 0, c.stream>>>(c.spins4, c.N, c.col_off[colour], n_c,
-                                               (uint32_t)colour, pass, part, c.t.row_ptr,
-                                               c.t.nbr, c.t.jidx, c.t.J, c.stream_id,
-                                               c.ovrr_step, c.seed);
+    ovrr_ell_kernel<<<grid, bs, 0, c.stream>>>(c.spins4, c.N, c.col_off[colour], n_c, (uint32_t)colour, pass,
+                                               part, c.t.ell_nbr + c.ell_off[colour],
+                                               c.t.ell_j + c.ell_off[colour], c.t.ell_deg,
+                                               c.ell_width[colour], c.t.J4, c.stream_id, c.ovrr_step,
+                                               c.seed);
     c.launches++;
     return cudaGetLastError();
 }

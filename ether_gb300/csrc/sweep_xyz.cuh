@@ -23,6 +23,7 @@ struct XyzParams {
     const uint8_t *species;
     const float *zee;
     const float *D;
+    int nsp;  // species count: with one, the per-site species is not read
 };
 
 // Option sets of the XYZ kernels: kXyzExchange folds the Zeeman, SIA and ANGLE branches away
@@ -38,7 +39,7 @@ __device__ __forceinline__ float delta_e(const XyzParams &P, int s, const float4
     e = fmaf(dy, hy, e);
     e = fmaf(dz, hz, e);
     if (OPT != kXyzExchange && (P.zeeman || P.sia)) {
-        int si = P.species[s] - 1;
+        const int si = P.nsp == 1 ? 0 : P.species[s] - 1;
         if (P.zeeman) {
             const float *z = P.zee + 3 * si;
             e = fmaf(dx, z[0], e);

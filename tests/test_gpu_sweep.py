@@ -74,6 +74,28 @@ def test_ising_staged_kernel_bit_exact(variant, L):
     sw.sync()  # no bounded wait ran out
 
 
+def test_ising_general_lattice_both_kernel_forms_bit_exact():
+    """The general-lattice Ising phase has two forms: a group of eight sites per thread when
+    the colour classes of all replicas hold enough groups to fill the GPU, one site per thread
+    otherwise.  32^3 through the general path with 48 replicas takes the group form; replicas
+    0 and 47 are replayed by the oracle."""
+    lat = eg.simple_cubic(32)
+    sw, osys = make_pair(lat, eg.MODEL_ISING, FM, replicas=48, flags=eg.FLAG_FORCE_GENERAL)
+    beta = beta_of(4.511)
+    sw.set_beta(beta)
+    assert sw.info().fast_path == 0
+    ncol, col, rank = osys.colouring()
+    ions = [random_ising(lat, 100 + r) for r in range(48)]
+    for r in range(48):
+        sw.set_spins(ions[r], r)
+    sw.metropolis(3)
+    for r in (0, 47):
+        ion = ions[r].copy()
+        for t in range(3):
+            osys.metropolis_colour(ion, None, 64, beta, 1992, r, t, col, rank, ncol)
+        np.testing.assert_array_equal(sw.get_spins(lat.ion, r)[:, 3], ion[:, 3])
+
+
 def test_ising_tie_path_bit_exact():
     """1.3M updates: about 20 sites whose high 16 random bits tie with the threshold's and
     are decided by the low halves (the rarely taken branch of both kernels)."""
