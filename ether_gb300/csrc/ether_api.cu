@@ -425,6 +425,8 @@ extern "C" int ether_create(const ether_desc *d, ether_ctx **out) {
             c.ell_width[col] = w;
             c.ell_off[col + 1] = c.ell_off[col] + (long)w * (c.col_off[col + 1] - c.col_off[col]);
         }
+        if (c.ell_off[c.ncol] >= (1L << 31))  // the kernels index a block with 32-bit ints
+            return bail(fail(ETHER_ERR_CAPACITY, "neighbour lists of more than 2^31 entries"));
         const bool xyz = c.model == ETHER_MODEL_XYZ;
         std::vector<int32_t> enb((size_t)c.ell_off[c.ncol], 0);
         std::vector<uint16_t> ej(xyz ? (size_t)c.ell_off[c.ncol] : 0, 0);

@@ -41,7 +41,7 @@ ising_ell_kernel(uint8_t *__restrict__ spins, int N, int col_off, int n_c, uint3
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
                 const int rho = min(rho0 + j, n_c - 1);
-                const size_t e = (size_t)k * n_c + rho;
+                const int e = k * n_c + rho;  // ELL blocks hold < 2^31 entries (checked at creation)
                 const int up = sp[ell[e]];
                 const int w = ews[e];
                 if (k < dg[j]) idx[j] += w * up;
@@ -100,7 +100,7 @@ ising_ell_site_kernel(uint8_t *__restrict__ spins, int N, int col_off, int n_c, 
         int idx = 0;
 #pragma unroll 6
         for (int k = 0; k < width; ++k) {
-            const size_t e = (size_t)k * n_c + rho;
+            const int e = k * n_c + rho;  // ELL blocks hold < 2^31 entries (checked at creation)
             const int up = sp[ell[e]];
             const int w = ews[e];
             if (k < dg) idx += w * up;

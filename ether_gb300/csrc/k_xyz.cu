@@ -19,7 +19,7 @@ __device__ __forceinline__ Acc3 ell_field(const float4 *__restrict__ sp, const i
     Acc3 h{0.f, 0.f, 0.f};
 #pragma unroll 6
     for (int k = 0; k < width; ++k) {
-        const size_t e = (size_t)k * n_c + rho;
+        const int e = k * n_c + rho;  // ELL blocks hold < 2^31 entries (checked at creation)
         const float4 Jv = J4[ej[e]];
         const float4 Sj = sp[ell[e]];
         if (k < deg) {
