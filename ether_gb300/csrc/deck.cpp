@@ -645,6 +645,33 @@ void make_dir(const std::string &path) {
     if (mkdir(path.c_str(), 0755) != 0) throw DeckError{ETHER_ERR_ARG, "cannot create directory " + path};
 }
 
+// An open output file, closed on every exit path.
+struct OutFile {
+    std::FILE *f = nullptr;
+    std::string path;
+    OutFile(const std::string &p, const char *mode) : path(p) {
+        f = std::fopen(p.c_str(), mode);
+        if (!f) throw DeckError{ETHER_ERR_ARG, "cannot open " + p};
+    }
+    ~OutFile() {
+        if (f) std::fclose(f);
+    }
+    OutFile(const OutFile &) = delete;
+    OutFile &operator=(const OutFile &) = delete;
+    void put(const std::string &s) {
+        if (std::fwrite(s.data(), 1, s.size(), f) != s.size()) throw DeckError{ETHER_ERR_ARG, "cannot write " + path};
+    }
+    // record `rec` of `bytes` bytes (direct access, no record markers)
+    void put_record(long rec, const void *data, size_t bytes) {
+        if (std::fseek(f, (long)((size_t)rec * bytes), SEEK_SET) != 0 || std::fwrite(data, 1, bytes, f) != bytes)
+            throw DeckError{ETHER_ERR_ARG, "cannot write " + path};
+    }
+    void get_record(long rec, void *data, size_t bytes) {
+        if (std::fseek(f, (long)((size_t)rec * bytes), SEEK_SET) != 0 || std::fread(data, 1, bytes, f) != bytes)
+            throw DeckError{ETHER_ERR_PARSE, "resume: ETHER.spn does not hold one record of this lattice per temperature"};
+    }
+};
+
 bool file_exists(const std::string &p) {
     struct stat st;
     return stat(p.c_str(), &st) == 0;
@@ -920,16 +947,36 @@ extern "C" int ether_run(const char *indir, const char *outdir, int32_t flags, e
         const int rep = (int)d.repeat;
         const int nobs = 20 + 3 * nsp;
         std::vector<double> obs((size_t)nobs * nscan, 0.0);
-        std::vector<double> spn((size_t)9 * N * nscan, 0.0);
         const bool ssp = d.ssp && d.xyz;
-        std::vector<double> resume;
-        if (flags & ETHER_RUN_RESUME) {
-            std::ifstream f(out + "/ETHER.spn", std::ios::binary);
-            if (!f) perr("resume: ETHER.spn not found in the output directory");
-            resume.resize(spn.size());
-            f.read(reinterpret_cast<char *>(resume.data()), (std::streamsize)(resume.size() * sizeof(double)));
-            if ((size_t)f.gcount() != resume.size() * sizeof(double))
+        const bool resume = (flags & ETHER_RUN_RESUME) != 0;
+        const size_t rec_bytes = (size_t)9 * N * sizeof(double);  // one ETHER.spn record: ion(0:8, N)
+        if (resume) {
+            struct stat st;
+            if (stat((out + "/ETHER.spn").c_str(), &st) != 0) perr("resume: ETHER.spn not found in the output directory");
+            if ((size_t)st.st_size != rec_bytes * (size_t)nscan)
                 perr("resume: ETHER.spn does not hold one record of this lattice per temperature");
+        }
+        // Written as the rounds finish, temperature by temperature: ETHER.spn (src/rw_file.f90),
+        // the gss.dat blocks (src/write_gss.f90) and the spK files; the rest from ETHER.obs at the end.
+        OutFile spn_f(out + "/ETHER.spn", resume ? "r+b" : "wb");
+        OutFile gss_f(out + "/data/gss.dat", "wb");
+        {  // gss.dat header (src/write_gss.f90:41-63)
+            std::string g = fI(nscan, 5) + " " + fI(d.sc[0], 5) + " " + fI(d.sc[1], 5) + " " + fI(d.sc[2], 5) + "\n";
+            g += fI(1, 5) + " " + fI(1, 5) + " " + fI(1, 5) + " " + fI(d.sc[0], 5) + " " + fI(d.sc[1], 5) + " " +
+                 fI(d.sc[2], 5) + "\n";
+            g += fI(nbasis, 5) + " " + fI(nsp, 5) + fF(d.ht, 11, 5) + " " + fF(d.lt, 11, 5) + " " + fF(d.tint, 11, 5) + "\n";
+            g += fA(d.para ? " KbT/J" : " K", 30, 20) + "\n";
+            for (int k = 0; k < nsp; k += 5) {  // (I8,1x,I8,1x,I8,1x,I8,1x,I8), reverting after five
+                for (int j = k; j < std::min(nsp, k + 5); ++j) g += (j > k ? " " : "") + fI(tions[j], 8);
+                g += "\n";
+            }
+            for (int i = 0; i < 3; ++i)
+                g += fF(d.abc[3 * i], 10, 5) + " " + fF(d.abc[3 * i + 1], 10, 5) + " " + fF(d.abc[3 * i + 2], 10, 5) + "\n";
+            g += " # lattice points\n";
+            for (long i = 0; i < N; ++i)
+                g += fF(ion[9 * i + 6], 11, 6) + " " + fF(ion[9 * i + 7], 11, 6) + " " + fF(ion[9 * i + 8], 11, 6) + " " +
+                     fI((long)ion[9 * i], 8) + "\n";
+            gss_f.put(g);
         }
         ether_schedule sch;
         std::memset(&sch, 0, sizeof(sch));
@@ -986,14 +1033,16 @@ extern "C" int ether_run(const char *indir, const char *outdir, int32_t flags, e
             RTRY(ether_set_streams(ctx, sid.data(), st.data()));
             // start states: the lattice's, a slot's state carried from the last round, or
             // the temperature's record of ETHER.spn
-            if (!resume.empty() || !carry.empty()) {
+            if (resume || !carry.empty()) {
+                std::vector<double> rec((size_t)9 * N);
                 for (int s = 0; s < np; ++s) {
-                    const double *src = !resume.empty() ? resume.data() + (size_t)9 * N * (t0 + s)
-                                                        : carry.data() + (size_t)9 * N * s;
+                    const double *src = rec.data();
+                    if (resume) spn_f.get_record(t0 + s, rec.data(), rec_bytes);
+                    else src = carry.data() + (size_t)9 * N * s;
                     for (int g = 0; g < rep; ++g) RTRY(ether_set_spins(ctx, g * np + s, src));
                 }
             }
-            if (resume.empty()) RTRY(ether_fresh_spins(ctx));  // src/ether.f90:155
+            if (!resume) RTRY(ether_fresh_spins(ctx));  // src/ether.f90:155
             RTRY(ether_zero_avg(ctx));
             RTRY(ether_reset_accept_counts(ctx));
             if (ssp) {
@@ -1047,8 +1096,23 @@ extern "C" int ether_run(const char *indir, const char *outdir, int32_t flags, e
                 if (r_last < 0) throw RunError{ETHER_ERR_STATE};
                 std::vector<double> cfg(ion);
                 RTRY(ether_get_spins(ctx, r_last, cfg.data()));
-                std::copy(cfg.begin(), cfg.end(), spn.begin() + (size_t)9 * N * t);
                 std::copy(cfg.begin(), cfg.end(), carry.begin() + (size_t)9 * N * s);
+                spn_f.put_record(t, cfg.data(), rec_bytes);
+                {  // gss.dat block (src/write_gss.f90:65-77) and <T>spK.xsf (src/write_spins_at_K.f90)
+                    std::string g = fF(temperature[t], 11, 5) + "\n";
+                    for (long i = 0; i < N; ++i)
+                        g += fF(cfg[9 * i + 1], 11, 6) + " " + fF(cfg[9 * i + 2], 11, 6) + " " +
+                             fF(cfg[9 * i + 3], 11, 6) + " " + fI((long)cfg[9 * i + 4], 8) + "\n";
+                    gss_f.put(g);
+                    std::string xs = xsf_header(d, N);
+                    for (long i = 0; i < N; ++i) {  // format 101: (A5, 1x, six f13.7 separated by 1x)
+                        xs += fA(d.species[(int)cfg[9 * i + 4] - 1], 2, 5);
+                        for (int k : {6, 7, 8, 1, 2, 3}) xs += " " + fF(cfg[9 * i + k], 13, 7);
+                        xs += "\n";
+                    }
+                    // name: format(f9.4, 'spK.xsf'), adjustl
+                    write_file(out + "/spins/" + trim(fF(temperature[t], 9, 4) + "spK.xsf"), xs);
+                }
                 double acc = 0.0;  // acceptance_counting / (repeat tmcs), src/ether.f90:212
                 for (int g = 0; g < rep; ++g) acc += (double)accepts[(size_t)g * np + s] / (double)N;
                 acc /= (double)rep * (double)d.tmcs;
@@ -1070,7 +1134,6 @@ extern "C" int ether_run(const char *indir, const char *outdir, int32_t flags, e
         ctx = nullptr;
         // ------------------------------------------------------------------ output files ----
         write_file(out + "/ETHER.obs", std::string(reinterpret_cast<const char *>(obs.data()), obs.size() * sizeof(double)));
-        write_file(out + "/ETHER.spn", std::string(reinterpret_cast<const char *>(spn.data()), spn.size() * sizeof(double)));
         static const char *m_head[7] = {"# 1 Temp.", "2 |M|", "3 \xcf\x87", "4 \xce\x94|M|", "5 \xce\x94\xcf\x87",
                                         "6 U(|M|)", "7 \xce\x94U(|M|)"};
         static const char *ss_head[7] = {"# 1 Temp.", "2 |\xcf\x88|", "3 \xcf\x88", "4 \xce\x94|\xcf\x88|",
@@ -1101,22 +1164,6 @@ extern "C" int ether_run(const char *indir, const char *outdir, int32_t flags, e
             } while (i < n);
         }
         mom += " # Temp, sp1(Mx,My,Mz), sp1(Mx,My,Mz),..spN(Mx,My,Mz), sp1|M|, sp2|M|,..spN|M|\n";
-        // gss.dat header (src/write_gss.f90:41-63)
-        std::string gss = fI(nscan, 5) + " " + fI(d.sc[0], 5) + " " + fI(d.sc[1], 5) + " " + fI(d.sc[2], 5) + "\n";
-        gss += fI(1, 5) + " " + fI(1, 5) + " " + fI(1, 5) + " " + fI(d.sc[0], 5) + " " + fI(d.sc[1], 5) + " " +
-               fI(d.sc[2], 5) + "\n";
-        gss += fI(nbasis, 5) + " " + fI(nsp, 5) + fF(d.ht, 11, 5) + " " + fF(d.lt, 11, 5) + " " + fF(d.tint, 11, 5) + "\n";
-        gss += fA(d.para ? " KbT/J" : " K", 30, 20) + "\n";
-        for (int k = 0; k < nsp; k += 5) {  // (I8,1x,I8,1x,I8,1x,I8,1x,I8), reverting after five
-            for (int j = k; j < std::min(nsp, k + 5); ++j) gss += (j > k ? " " : "") + fI(tions[j], 8);
-            gss += "\n";
-        }
-        for (int i = 0; i < 3; ++i)
-            gss += fF(d.abc[3 * i], 10, 5) + " " + fF(d.abc[3 * i + 1], 10, 5) + " " + fF(d.abc[3 * i + 2], 10, 5) + "\n";
-        gss += " # lattice points\n";
-        for (long i = 0; i < N; ++i)
-            gss += fF(ion[9 * i + 6], 11, 6) + " " + fF(ion[9 * i + 7], 11, 6) + " " + fF(ion[9 * i + 8], 11, 6) + " " +
-                   fI((long)ion[9 * i], 8) + "\n";
         for (long t = 0; t < nscan; ++t) {
             const double *o = obs.data() + (size_t)nobs * t;
             // format 102: (f11.5, 1x, es12.5 x6, 1x, f7.2)
@@ -1142,26 +1189,11 @@ extern "C" int ether_run(const char *indir, const char *outdir, int32_t flags, e
                     mom += fF(std::sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]) / (double)tions[id - 1], 9, 3);
                 }
             mom += "\n";
-            // gss.dat block per temperature (src/write_gss.f90:65-77)
-            gss += fF(o[0], 11, 5) + "\n";
-            const double *cfg = spn.data() + (size_t)9 * N * t;
-            for (long i = 0; i < N; ++i)
-                gss += fF(cfg[9 * i + 1], 11, 6) + " " + fF(cfg[9 * i + 2], 11, 6) + " " + fF(cfg[9 * i + 3], 11, 6) +
-                       " " + fI((long)cfg[9 * i + 4], 8) + "\n";
-            // <T>spK.xsf (src/write_spins_at_K.f90): name format(f9.4,'spK.xsf'), adjustl
-            std::string xs = xsf_header(d, N);
-            for (long i = 0; i < N; ++i) {  // format 101: (A5, 1x, six f13.7 separated by 1x)
-                xs += fA(d.species[(int)cfg[9 * i + 4] - 1], 2, 5);
-                for (int k : {6, 7, 8, 1, 2, 3}) xs += " " + fF(cfg[9 * i + k], 13, 7);
-                xs += "\n";
-            }
-            write_file(out + "/spins/" + trim(fF(o[0], 9, 4) + "spK.xsf"), xs);
         }
         write_file(out + "/data/magnetization.dat", mag);
         write_file(out + "/data/energy.dat", eng);
         write_file(out + "/data/moment_vectors.dat", mom);
         write_file(out + "/data/spiral_state_parameters.dat", sss);
-        write_file(out + "/data/gss.dat", gss);
         write_file(out + "/data/graph.sh", graph_text(d));
         if (info) {
             info->n_rounds = (int32_t)rounds;
