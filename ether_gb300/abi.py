@@ -22,6 +22,7 @@ FLAG_FORCE_GENERAL = 1 << 0
 FLAG_PT_TRUE_ENERGY = 1 << 1
 FLAG_PT_REFERENCE_COPY = 1 << 2
 FLAG_NO_GRAPHS = 1 << 3
+FLAG_NO_RESIDENT = 1 << 4
 RUN_PARSE_ONLY = 1 << 0
 RUN_QUIET = 1 << 1
 RUN_RESUME = 1 << 2

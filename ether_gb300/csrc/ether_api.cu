@@ -476,6 +476,17 @@ extern "C" int ether_create(const ether_desc *d, ether_ctx **out) {
     TRY(dev_alloc(c, &c.M, 3 * (size_t)c.R));
     TRY(dev_alloc(c, &c.sums, 7 * (size_t)c.R));
     c.partial_blocks = energy_blocks(c);
+    {
+        // small simple-cubic Ising lattices: ether_mcs keeps each replica in shared memory for
+        // the sweeps between two PT or measurement steps, when the replicas alone fill the GPU
+        int dev = 0, optin = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        const size_t room = optin > 1024 ? (size_t)optin - 1024 : 0;  // leave the static shared memory
+        c.resident = !(c.flags & ETHER_FLAG_NO_RESIDENT) && ising_resident_possible(c, room) &&
+                     (long)c.R * c.N <= (16L << 20) && 2 * c.R >= c.sm_count;
+        if (c.resident) CUDA_TRY(prepare_ising_resident(c));
+    }
     TRY(dev_alloc(c, &c.partials, (size_t)c.R * c.partial_blocks * 5));
     TRY(dev_alloc(c, &c.pt_accepts, 1));
     TRY(dev_alloc(c, &c.swap_dev, 1));
@@ -811,6 +822,42 @@ static int issue_step(Ctx &c, const ether_schedule *sch, bool ovrr, bool pt, boo
     return ETHER_OK;
 }
 
+// Steps sig[0 .. n): with a resident context the sweeps that no OVRR, PT or measurement
+// separates run as one ising_sc_resident launch; otherwise step by step.
+static int issue_steps(Ctx &c, const ether_schedule *sch, const int8_t *sig, int n) {
+    if (!c.resident) {
+        for (int k = 0; k < n; ++k) {
+            int rc = issue_step(c, sch, sig[k] & 1, sig[k] & 2, sig[k] & 4);
+            if (rc) return rc;
+        }
+        return ETHER_OK;
+    }
+    int pending = 0;
+    for (int k = 0; k < n; ++k) {
+        if (sig[k] & 1) {  // not reached for Ising (no OVRR), kept for the order of operations
+            if (pending) CUDA_TRY(launch_ising_resident(c, pending));
+            pending = 0;
+            int rc = overrelax_once(c, sch->ovrr_para);
+            if (rc) return rc;
+        }
+        ++pending;
+        if (sig[k] & 6) {
+            CUDA_TRY(launch_ising_resident(c, pending));
+            pending = 0;
+            if (sig[k] & 2) {
+                CUDA_TRY(launch_energy_mag(c, true));
+                CUDA_TRY(launch_pt(c, -1));
+            }
+            if (sig[k] & 4) {
+                CUDA_TRY(launch_energy_mag(c, true));
+                CUDA_TRY(launch_measure(c));
+            }
+        }
+    }
+    if (pending) CUDA_TRY(launch_ising_resident(c, pending));
+    return ETHER_OK;
+}
+
 // The loop body for steps step0+1 .. step0+nsteps.  Steps are issued in chunks; a chunk's
 // launches depend only on its gate pattern (everything that changes from step to step --
 // sweep counters, PT swap count, slot permutation -- is read from device memory), so each
@@ -841,6 +888,9 @@ extern "C" int ether_mcs(ether_ctx *h, const ether_schedule *sch, int32_t step0,
     if (pt_on) period = lcm(period, sch->exchange_interval);
     int chunk = (int)(period <= 256 ? period : 64);
     while (chunk < 8 && chunk * 2 <= 256) chunk *= 2;
+    // resident contexts: the longest multiple of the period up to 256 steps, so that the
+    // eventless stretches (equilibration) run as few long resident launches
+    if (c.resident && period <= 256) chunk = (int)(256 / period * period);
     const bool use_graphs = !(c.flags & ETHER_FLAG_NO_GRAPHS);
     int step = step0 + 1;
     const int last = step0 + nsteps;
@@ -854,10 +904,8 @@ extern "C" int ether_mcs(ether_ctx *h, const ether_schedule *sch, int32_t step0,
             sig.push_back((int8_t)((ov ? 1 : 0) | (pt ? 2 : 0) | (me ? 4 : 0)));
         }
         if (!use_graphs || n < 4) {
-            for (int k = 0; k < n; ++k) {
-                int rc = issue_step(c, sch, sig[k] & 1, sig[k] & 2, sig[k] & 4);
-                if (rc) return rc;
-            }
+            int rc = issue_steps(c, sch, sig.data(), n);
+            if (rc) return rc;
         } else {
             std::string key(sig.begin(), sig.end());
             key += std::to_string(c.vec_bytes * 10 + c.ising_vpt) + "/" + std::to_string(sch->ovrr_para) +
@@ -871,7 +919,7 @@ extern "C" int ether_mcs(ether_ctx *h, const ether_schedule *sch, int32_t step0,
                 cudaGraph_t g = nullptr;
                 CUDA_TRY(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
                 int rc = ETHER_OK;
-                for (int k = 0; k < n && rc == ETHER_OK; ++k) rc = issue_step(c, sch, sig[k] & 1, sig[k] & 2, sig[k] & 4);
+                rc = issue_steps(c, sch, sig.data(), n);
                 cudaError_t ce = cudaStreamEndCapture(c.stream, &g);
                 if (rc) {
                     if (g) cudaGraphDestroy(g);

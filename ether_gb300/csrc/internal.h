@@ -97,6 +97,7 @@ struct Ctx {
     bool ising_cap = false;      // register-capped (four blocks per SM) instantiation
     bool ising_stream = false;   // shared-memory staged simple-cubic Ising kernel
     int xyz_variant = 11;        // simple-cubic XYZ kernel: 10 * sites per thread + blocks per SM cap
+    bool resident = false;       // ether_mcs runs runs of sweeps with ising_sc_resident
     int *err = nullptr;          // device: first bounded-wait failure of a kernel (0 = none)
     unsigned long long *acc_before = nullptr;  // R: acceptance counts at the start of a call
     double *acc_ratio = nullptr;               // R: device acceptance ratios of a call
@@ -132,6 +133,9 @@ struct Ctx {
 
 // kernel launchers (k_*.cu)
 cudaError_t launch_ising_sweep(Ctx &c, int colour);
+bool ising_resident_possible(const Ctx &c, size_t smem_max);
+cudaError_t prepare_ising_resident(const Ctx &c);
+cudaError_t launch_ising_resident(Ctx &c, int nsweeps);
 bool ising_stream_supported(const Ctx &c, int vectors_per_step);
 cudaError_t launch_xyz_sweep(Ctx &c, int colour);
 bool xyz_variant_valid(int variant);

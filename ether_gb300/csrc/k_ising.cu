@@ -421,6 +421,86 @@ static int blocks_for(const Ctx &c, long work, int bs) {
     return (int)need;
 }
 
+// Resident form for small simple-cubic lattices: one block per replica holds both colour
+// arrays in shared memory and runs nsweeps whole sweeps (colour 0, colour 1, counter + 1)
+// between two visits to global memory.  The draws, thresholds and vector update are the
+// phase kernels' (ising_sc_vectors), so every decision is the same; the sweep counter is
+// advanced here instead of by advance_kernel.
+template <int W>
+__global__ void __launch_bounds__(256)
+ising_sc_resident(uint8_t *__restrict__ spins, int L1, int L2, int L3, FastDiv fH, FastDiv fL2,
+                  const uint32_t *__restrict__ thr, int table_entries,
+                  const int32_t *__restrict__ slot_of_rep, const uint32_t *__restrict__ stream_id,
+                  uint32_t *__restrict__ step, uint32_t seed, const RoundKeys K, int nsweeps,
+                  unsigned long long *__restrict__ acc_count) {
+    extern __shared__ __align__(16) uint8_t s_sp[];  // colour 0 array, then colour 1
+    __shared__ uint32_t s_th[16], s_tl[16];
+    const int r = blockIdx.x;
+    const int H = L1 >> 1;
+    const int half = H * L2 * L3;
+    const int nvec = half / W;
+    uint4 *g = reinterpret_cast<uint4 *>(spins + (size_t)r * 2 * half);
+    uint4 *sv = reinterpret_cast<uint4 *>(s_sp);
+    const int n16 = (2 * half) >> 4;  // 2 half is a multiple of 16 (W | H)
+    for (int i = threadIdx.x; i < n16; i += blockDim.x) sv[i] = g[i];
+    load_sc_thresholds(thr + (size_t)slot_of_rep[r] * table_entries, s_th, s_tl);
+    const uint32_t stream = stream_id[r];
+    const uint32_t t0 = step[r];
+    __syncthreads();
+    unsigned flips = 0;
+    for (int k = 0; k < nsweeps; ++k) {
+        const uint32_t t = t0 + (uint32_t)k;
+        for (int colour = 0; colour < 2; ++colour) {
+            const IsingSc A{s_sp + (size_t)colour * half, s_sp + (size_t)(colour ^ 1) * half,
+                            L1, L2, L3, H, fH, fL2, (uint32_t)colour};
+            uint32_t cnt = 0;
+            for (int v = threadIdx.x; v < nvec; v += blockDim.x)
+                cnt += ising_sc_vectors<W, 1>(A, v, 0, nvec, s_th, s_tl, t, stream, kMetro | ((uint32_t)colour << 8),
+                                              seed, K);
+            flips += byte_sum(cnt);  // each byte <= (W / 4) * ceil(nvec / blockDim) per colour
+            __syncthreads();
+        }
+    }
+    for (int i = threadIdx.x; i < n16; i += blockDim.x) g[i] = sv[i];
+    if (threadIdx.x == 0) step[r] = t0 + (uint32_t)nsweeps;
+    warp_add_count(acc_count + r, flips);
+}
+
+bool ising_resident_possible(const Ctx &c, size_t smem_max) {
+    if (!c.fast || c.model != ETHER_MODEL_ISING || c.vec_bytes == 0) return false;
+    const size_t bytes = (size_t)c.L[0] * c.L[1] * c.L[2];  // both colours
+    // (W/4) ceil(nvec/256) flips per byte of a vector count must stay below 256
+    const size_t nvec = bytes / 2 / (size_t)c.vec_bytes;
+    return bytes <= smem_max && (c.vec_bytes / 4) * ((nvec + 255) / 256) < 256;
+}
+
+// Opts the resident kernel into the shared memory a replica needs (once, at creation: not
+// during a stream capture).
+cudaError_t prepare_ising_resident(const Ctx &c) {
+    const int smem = c.L[0] * c.L[1] * c.L[2];
+    return c.vec_bytes == 16
+               ? cudaFuncSetAttribute(ising_sc_resident<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
+               : cudaFuncSetAttribute(ising_sc_resident<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+}
+
+cudaError_t launch_ising_resident(Ctx &c, int nsweeps) {
+    const int smem = c.L[0] * c.L[1] * c.L[2];
+    const int bs = 256;
+    if (c.vec_bytes == 16) {
+        ising_sc_resident<16><<<c.R, bs, smem, c.stream>>>(
+            c.spins, c.L[0], c.L[1], c.L[2], make_fastdiv((uint32_t)(c.L[0] / 2)), make_fastdiv((uint32_t)c.L[1]),
+            c.thr, c.table_entries, c.slot_of_rep, c.stream_id, c.step, c.seed, round_keys(c.seed), nsweeps,
+            c.acc_count);
+    } else {
+        ising_sc_resident<8><<<c.R, bs, smem, c.stream>>>(
+            c.spins, c.L[0], c.L[1], c.L[2], make_fastdiv((uint32_t)(c.L[0] / 2)), make_fastdiv((uint32_t)c.L[1]),
+            c.thr, c.table_entries, c.slot_of_rep, c.stream_id, c.step, c.seed, round_keys(c.seed), nsweeps,
+            c.acc_count);
+    }
+    c.launches++;
+    return cudaGetLastError();
+}
+
 cudaError_t launch_ising_sweep(Ctx &c, int colour) {
     const int bs = 256;
     if (c.fast && c.ising_stream) {

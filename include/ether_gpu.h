@@ -59,8 +59,11 @@ enum {
                                           configuration into the higher slot (what
                                           parallel_tempering.f90:92-106 effectively does)
                                           instead of exchanging the two                     */
-    ETHER_FLAG_NO_GRAPHS = 1 << 3         /* ether_mcs launches kernels one by one instead of
+    ETHER_FLAG_NO_GRAPHS = 1 << 3,        /* ether_mcs launches kernels one by one instead of
                                           replaying captured CUDA graphs                    */
+    ETHER_FLAG_NO_RESIDENT = 1 << 4       /* ether_mcs never runs a small simple-cubic Ising
+                                          lattice's sweeps in the shared-memory resident
+                                          kernel (same results, one launch per phase)        */
 };
 
 typedef struct ether_ctx ether_ctx;

@@ -191,3 +191,35 @@ def test_record_series_equals_step_by_step(model):
     np.testing.assert_allclose(a, x, rtol=1e-12)
     np.testing.assert_allclose(b, y, rtol=1e-12)
     np.testing.assert_allclose(c, z, rtol=1e-12)
+
+
+def test_resident_sweeps_equal_phase_launches():
+    """A small simple-cubic Ising lattice with enough replicas runs the sweeps between PT and
+    measurement steps in the shared-memory resident kernel: same draws, so the configurations,
+    observable sums, PT slots and acceptance counts equal those of the phase-by-phase launches
+    (ETHER_FLAG_NO_RESIDENT), with far fewer launches."""
+    lat = eg.simple_cubic(16)
+    j = eg.couplings(1, FM, [1.0])
+    temps = np.linspace(3.5, 6.0, 48)
+    runs = []
+    for flags in (0, eg.FLAG_NO_RESIDENT):
+        sw = eg.Sweep.from_lattice(lat, j, np.array([1.0]), eg.MODEL_ISING, replicas=96, seed=5,
+                                   flags=flags)
+        sw.set_ladder([beta_of(k) for k in temps])
+        sw.set_spins(lat.ion)
+        sw.fresh_spins()
+        sw.zero_avg()
+        n0 = sw.info().kernel_launches
+        swaps = sw.mcs(0, 150, 40, 10, pt=True, exchange_interval=11)
+        swaps = sw.mcs(150, 63, 40, 10, pt=True, exchange_interval=11, swap_count=swaps)
+        runs.append(dict(launches=sw.info().kernel_launches - n0, sums=sw.sums(), slots=sw.slots(),
+                         acc=sw.accept_counts(), swaps=swaps,
+                         spins=np.stack([sw.get_spins(lat.ion, r)[:, 3] for r in (0, 37, 95)])))
+        sw.close()
+    a, b = runs
+    np.testing.assert_array_equal(a["spins"], b["spins"])
+    np.testing.assert_array_equal(a["sums"], b["sums"])
+    np.testing.assert_array_equal(a["slots"], b["slots"])
+    np.testing.assert_array_equal(a["acc"], b["acc"])
+    assert a["swaps"] == b["swaps"] and (a["slots"] != np.arange(96) % 48).any()
+    assert a["launches"] * 2 < b["launches"]
