@@ -188,7 +188,7 @@ int upload_ladder(Ctx &c) {
 
 void free_ctx(Ctx &c) {
     void *ptrs[] = {c.t.row_ptr, c.t.nbr, c.t.jidx, c.t.wstride, c.t.species, c.t.itype,
-                    c.t.ell_nbr, c.t.ell_j, c.t.ell_deg, c.t.J4, c.t.ell_ws,
+                    c.t.ell_nbr, c.t.ell_j, c.t.ell_deg, c.t.J4, c.t.ell_ws, c.t.ell_desc,
                     c.t.type_base, c.t.type_half, c.t.J, c.t.Jd, c.t.zee, c.t.zeed, c.t.D,
                     c.t.mweight, c.t.site_of_storage, c.spins, c.spins4, c.beta_slot,
                     c.beta_slot_f, c.slot_of_rep, c.rep_of_slot, c.thr, c.stream_id,
@@ -447,6 +447,9 @@ extern "C" int ether_create(const ether_desc *d, ether_ctx **out) {
         }
         TRY(dev_upload(c, &c.t.ell_nbr, enb));
         TRY(dev_upload(c, &c.t.ell_deg, deg));
+        std::vector<int2> desc(c.ncol);
+        for (int col = 0; col < c.ncol; ++col) desc[col] = make_int2((int)c.ell_off[col], c.ell_width[col]);
+        TRY(dev_upload(c, &c.t.ell_desc, desc));
         if (xyz) {
             std::vector<float4> j4(c.h_Jf.size() / 3);
             for (size_t q = 0; q < j4.size(); ++q)

@@ -47,6 +47,7 @@ struct DevTables {
     uint16_t *ell_j = nullptr;    // XYZ: coupling index (into J4)
     int32_t *ell_ws = nullptr;    // Ising: stride of the threshold-table index
     uint16_t *ell_deg = nullptr;  // N: neighbours of a storage index
+    int2 *ell_desc = nullptr;     // per colour: (offset of its ELL block, entries per rank)
     float4 *J4 = nullptr;         // nJ: (Jxx, Jyy, Jzz, 0) in FP32
 };
 

@@ -3,11 +3,12 @@
 // The reference advances one lattice at one temperature per MPI rank (src/ether.f90:112-118,
 // one Metropolis sweep at a time: src/Metropolis.f90:34-68).  A batch advances every replica
 // of every member context -- mixed lattice sizes, Ising and XYZ, each member with its own
-// temperature ladder -- with one persistent kernel per colour phase: a grid of (resident
-// blocks per SM x SMs) walks a table of segments (member, replica, first unit, units), each
-// segment a block-sized tile of one replica's colour class.  A unit is what one thread
-// updates at a time: a W-byte vector (simple-cubic Ising), a group of eight sites (general
-// Ising) or one site (XYZ).  The per-site arithmetic is the member kernels' own
+// temperature ladder -- with one persistent kernel per colour phase and member class (the
+// kernel specialised for that class): a grid of (resident blocks per SM x SMs) walks a table
+// of segments (member, replica, first unit, units), each segment a block-sized tile of one
+// replica's colour class.  A unit is what one thread updates at a time: a W-byte vector
+// (simple-cubic Ising) or one site (general Ising, XYZ; general lattices from the colour
+// classes' ELL neighbour blocks).  The per-site arithmetic is the member kernels' own
 // (sweep_ising.cuh, sweep_xyz.cuh) with the same random-number counters, so a batch sweep
 // reproduces the members' own sweeps bit for bit.  One sweep (the phases and the sweep
 // counter advance) is captured once as a CUDA graph and replayed.
@@ -21,7 +22,20 @@
 
 namespace ether {
 
-enum BatchKind : int32_t { kBIsing16 = 0, kBIsing8 = 1, kBIsingCsr = 2, kBXyzSc = 3, kBXyzCsr = 4 };
+enum BatchKind : int32_t { kBIsing16 = 0, kBIsing8 = 1, kBIsingEll = 2, kBXyzSc = 3, kBXyzEll = 4 };
+
+// Each colour phase launches one kernel per member class present, specialised for that class
+// alone, so that every class gets the registers and occupancy of its own arithmetic.
+enum BatchClass : int {
+    kCIsing16 = 0,  // simple-cubic Ising, 16-byte vectors
+    kCIsing8 = 1,   // simple-cubic Ising, 8-byte vectors
+    kCIsingEll = 2, // general Ising, one site per thread from the ELL blocks
+    kCXyzScX = 3,   // simple-cubic XYZ, exchange only with Marsaglia proposals
+    kCXyzScG = 4,   // simple-cubic XYZ with Zeeman, SIA or ANGLE proposals
+    kCXyzEllX = 5,  // general XYZ, exchange only with Marsaglia proposals
+    kCXyzEllG = 6,  // general XYZ with Zeeman, SIA or ANGLE proposals
+    kNumClasses = 7
+};
 
 // Everything a segment needs from its member; copied into shared memory when a block moves
 // to another member.  Plain data (no initialisers): it lives in __shared__.
@@ -32,9 +46,10 @@ struct BatchMember {
     float4 *spins4;
     const uint32_t *thr;
     int32_t table_entries, pad0;
-    const int32_t *row_ptr, *nbr, *wstride, *type_base, *type_half;
-    const uint16_t *itype, *jidx;
-    const float *J;
+    const int32_t *ell_nbr, *ell_ws, *type_base, *type_half;
+    const uint16_t *itype, *ell_j, *ell_deg;
+    const int2 *ell_desc;  // per colour: (offset of its ELL block, entries per rank)
+    const float4 *J4;
     XyzParams P;
     float jx, jy, jz;
     uint32_t seed;
@@ -51,25 +66,92 @@ struct BatchSeg {
     uint32_t member, rep, first, count;
 };
 
+// One segment of a member of each class.  m lives in shared memory.
+template <int W>
+__device__ __forceinline__ unsigned batch_ising_sc(const BatchMember &m, uint32_t r, int first, int end,
+                                                   uint32_t colour, const uint32_t *s_th, const uint32_t *s_tl,
+                                                   uint32_t t, uint32_t stream, int upt) {
+    const uint32_t c3 = kMetro | (colour << 8);
+    const int half = m.H * m.L2 * m.L3;
+    uint8_t *base = m.spins + (size_t)r * 2 * half;
+    const IsingSc A{base + (size_t)colour * half, base + (size_t)(colour ^ 1u) * half,
+                    m.L1, m.L2, m.L3, m.H, m.fH, m.fL2, colour};
+    unsigned acc = 0;
+    for (int j = 0; j < upt; ++j) {
+        const int v = first + (int)threadIdx.x + j * (int)blockDim.x;
+        acc += byte_sum(ising_sc_vectors<W, 1>(A, v, 0, end, s_th, s_tl, t, stream, c3, m.seed, m.K));
+    }
+    return acc;
+}
+
+__device__ __forceinline__ unsigned batch_ising_ell(const BatchMember &m, uint32_t r, int first, int end,
+                                                    uint32_t colour, uint32_t t, uint32_t stream) {
+    const uint32_t c3 = kMetro | (colour << 8);
+    const int off = m.col_off[colour];
+    const int2 d = m.ell_desc[colour];
+    const IsingEll A{m.spins + (size_t)r * m.N, off, m.col_off[colour + 1] - off, d.y,
+                     m.ell_nbr + d.x, m.ell_ws + d.x, m.ell_deg, m.itype, m.type_base, m.type_half,
+                     m.thr + (size_t)m.slot_of_rep[r] * m.table_entries};
+    unsigned acc = 0;
+    for (int rho = first + (int)threadIdx.x; rho < end; rho += blockDim.x)
+        acc += ising_ell_site(A, rho, t, stream, c3, m.seed) ? 1u : 0u;
+    return acc;
+}
+
+template <int OPT>
+__device__ __forceinline__ unsigned batch_xyz_sc(const BatchMember &m, uint32_t r, int first, int end,
+                                                 uint32_t colour, uint32_t t, uint32_t stream) {
+    const uint32_t c3 = kMetro | (colour << 8);
+    const int half = m.H * m.L2 * m.L3;
+    float4 *base = m.spins4 + (size_t)r * 2 * half;
+    const XyzSc A{base + (size_t)colour * half, base + (size_t)(colour ^ 1u) * half,
+                  m.L1, m.L2, m.L3, m.H, m.fH, m.fL2, colour, m.jx, m.jy, m.jz};
+    const float beta_f = m.beta_slot_f[m.slot_of_rep[r]];
+    const RoundKeys K = m.K;
+    // exchange only, Marsaglia proposals: the options fold away at compile time
+    const XyzParams P = OPT == kXyzExchange ? XyzParams{0, 0, 0, 0.f, nullptr, nullptr, nullptr, 1} : m.P;
+    unsigned acc = 0;
+    for (int rho = first + (int)threadIdx.x; rho < end; rho += blockDim.x)
+        acc += xyz_sc_site<OPT>(A, P, rho, beta_f, t, c3, K, stream) ? 1u : 0u;
+    return acc;
+}
+
+template <int OPT>
+__device__ __forceinline__ unsigned batch_xyz_ell(const BatchMember &m, uint32_t r, int first, int end,
+                                                  uint32_t colour, uint32_t t, uint32_t stream) {
+    const uint32_t c3 = kMetro | (colour << 8);
+    const int off = m.col_off[colour], n_c = m.col_off[colour + 1] - off;
+    const int2 d = m.ell_desc[colour];
+    float4 *sp = m.spins4 + (size_t)r * m.N;
+    const float beta_f = m.beta_slot_f[m.slot_of_rep[r]];
+    const XyzParams P = m.P;
+    const RoundKeys K = m.K;
+    unsigned acc = 0;
+    for (int rho = first + (int)threadIdx.x; rho < end; rho += blockDim.x)
+        acc += xyz_ell_site<OPT>(P, sp, off, n_c, rho, m.ell_nbr + d.x, m.ell_j + d.x, m.ell_deg, d.y, m.J4,
+                                 beta_f, t, c3, K, stream) ? 1u : 0u;
+    return acc;
+}
+
 // Two walks over the segments.  Strided (block_first == nullptr): block b takes segments
 // b, b + gridDim.x, ...; the resident blocks sweep through memory together, so the
 // neighbour planes one tile reads are the planes its neighbours' tiles read at the same time
 // (L2 hits).  Contiguous: block b takes [block_first[b], block_first[b+1]), runs balanced by
 // an estimated cost per unit, so member and replica change rarely.  No block barriers: the
 // Ising thresholds live in a per-warp slot of shared memory.
-template <int MINB>
+template <int CLS, int MINB>
 __global__ void __launch_bounds__(256, MINB)
 batch_phase_kernel(const BatchMember *__restrict__ members, const BatchSeg *__restrict__ segs,
                    const int32_t *__restrict__ block_first, int n_seg, uint32_t colour, int upt) {
     // Per-warp copies of the current member's parameters and Ising thresholds: a warp moves
     // to another member or replica without waiting for the rest of the block, and the
     // parameters cost no registers.
+    constexpr bool kIsingSc = CLS == kCIsing16 || CLS == kCIsing8;
     __shared__ BatchMember s_m[8];
-    __shared__ uint32_t s_th[8][16], s_tl[8][16];
+    __shared__ uint32_t s_th[8][kIsingSc ? 16 : 1], s_tl[8][kIsingSc ? 16 : 1];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     BatchMember &m = s_m[warp];
     uint32_t cur_member = 0xFFFFFFFFu, cur_rep = 0xFFFFFFFFu;
-    const uint32_t c3 = kMetro | (colour << 8);
     const bool strided = block_first == nullptr;
     const int s_end = strided ? n_seg : block_first[blockIdx.x + 1];
     const int s_step = strided ? (int)gridDim.x : 1;
@@ -83,63 +165,84 @@ batch_phase_kernel(const BatchMember *__restrict__ members, const BatchSeg *__re
             for (int i = lane; i < (int)(sizeof(BatchMember) / 4); i += 32) dst[i] = src[i];
             __syncwarp();
         }
-        const int kind = m.kind;
-        if ((kind == kBIsing16 || kind == kBIsing8) && (S.member != cur_member || r != cur_rep)) {
-            if (lane < 14) {
-                const uint32_t T = m.thr[(size_t)m.slot_of_rep[r] * m.table_entries + lane];
-                s_th[warp][lane] = T >> 16;
-                s_tl[warp][lane] = T & 0xFFFFu;
+        if constexpr (kIsingSc) {
+            if (S.member != cur_member || r != cur_rep) {
+                if (lane < 14) {
+                    const uint32_t T = m.thr[(size_t)m.slot_of_rep[r] * m.table_entries + lane];
+                    s_th[warp][lane] = T >> 16;
+                    s_tl[warp][lane] = T & 0xFFFFu;
+                }
+                __syncwarp();
             }
-            __syncwarp();
         }
         cur_member = S.member;
         cur_rep = r;
         const uint32_t t = m.step[r], stream = m.stream_id[r];
-        const int end = (int)(S.first + S.count);
-        unsigned acc = 0;
-        if (kind == kBIsing16 || kind == kBIsing8) {
-            const int half = m.H * m.L2 * m.L3;
-            uint8_t *base = m.spins + (size_t)r * 2 * half;
-            const IsingSc A{base + (size_t)colour * half, base + (size_t)(colour ^ 1u) * half,
-                            m.L1, m.L2, m.L3, m.H, m.fH, m.fL2, colour};
-            for (int j = 0; j < upt; ++j) {
-                const int v = (int)S.first + (int)threadIdx.x + j * (int)blockDim.x;
-                if (kind == kBIsing16)
-                    acc += byte_sum(ising_sc_vectors<16, 1>(A, v, 0, end, s_th[warp], s_tl[warp], t, stream, c3, m.seed, m.K));
-                else
-                    acc += byte_sum(ising_sc_vectors<8, 1>(A, v, 0, end, s_th[warp], s_tl[warp], t, stream, c3, m.seed, m.K));
-            }
-        } else if (kind == kBIsingCsr) {
-            const int off = m.col_off[colour];
-            const IsingCsr A{m.spins + (size_t)r * m.N, off, m.col_off[colour + 1] - off, m.row_ptr,
-                             m.nbr, m.wstride, m.itype, m.type_base, m.type_half,
-                             m.thr + (size_t)m.slot_of_rep[r] * m.table_entries};
-            for (int g = (int)S.first + (int)threadIdx.x; g < end; g += blockDim.x)
-                acc += ising_csr_group(A, g, t, stream, c3, m.seed);
-        } else if (kind == kBXyzSc) {
-            const int half = m.H * m.L2 * m.L3;
-            float4 *base = m.spins4 + (size_t)r * 2 * half;
-            const XyzSc A{base + (size_t)colour * half, base + (size_t)(colour ^ 1u) * half,
-                          m.L1, m.L2, m.L3, m.H, m.fH, m.fL2, colour, m.jx, m.jy, m.jz};
-            const float beta_f = m.beta_slot_f[m.slot_of_rep[r]];
-            if (!m.P.zeeman && !m.P.sia && !m.P.angle) {
-                // exchange only, Marsaglia proposals: the options fold away at compile time
-                const XyzParams P0{0, 0, 0, 0.f, nullptr, nullptr, nullptr, 1};
-                for (int rho = (int)S.first + (int)threadIdx.x; rho < end; rho += blockDim.x)
-                    acc += xyz_sc_site<kXyzExchange>(A, P0, rho, beta_f, t, c3, m.K, stream) ? 1u : 0u;
-            } else {
-                for (int rho = (int)S.first + (int)threadIdx.x; rho < end; rho += blockDim.x)
-                    acc += xyz_sc_site<kXyzGeneral>(A, m.P, rho, beta_f, t, c3, m.K, stream) ? 1u : 0u;
-            }
-        } else {  // kBXyzCsr
-            float4 *sp = m.spins4 + (size_t)r * m.N;
-            const float beta_f = m.beta_slot_f[m.slot_of_rep[r]];
-            for (int rho = (int)S.first + (int)threadIdx.x; rho < end; rho += blockDim.x)
-                acc += xyz_csr_site<kXyzGeneral>(m.P, sp, m.col_off[colour], rho, m.row_ptr, m.nbr, m.jidx,
-                                                 m.J, beta_f, t, c3, m.K, stream) ? 1u : 0u;
-        }
+        const int first = (int)S.first, end = (int)(S.first + S.count);
+        unsigned acc;
+        if constexpr (CLS == kCIsing16)
+            acc = batch_ising_sc<16>(m, r, first, end, colour, s_th[warp], s_tl[warp], t, stream, upt);
+        else if constexpr (CLS == kCIsing8)
+            acc = batch_ising_sc<8>(m, r, first, end, colour, s_th[warp], s_tl[warp], t, stream, upt);
+        else if constexpr (CLS == kCIsingEll)
+            acc = batch_ising_ell(m, r, first, end, colour, t, stream);
+        else if constexpr (CLS == kCXyzScX)
+            acc = batch_xyz_sc<kXyzExchange>(m, r, first, end, colour, t, stream);
+        else if constexpr (CLS == kCXyzScG)
+            acc = batch_xyz_sc<kXyzGeneral>(m, r, first, end, colour, t, stream);
+        else if constexpr (CLS == kCXyzEllX)
+            acc = batch_xyz_ell<kXyzExchange>(m, r, first, end, colour, t, stream);
+        else
+            acc = batch_xyz_ell<kXyzGeneral>(m, r, first, end, colour, t, stream);
         warp_add_count(m.acc_count + r, acc);
     }
+}
+
+template <int CLS>
+void launch_class(int minb, int grid, int threads, cudaStream_t st, const BatchMember *mem, const BatchSeg *segs,
+                  const int32_t *bf, int n_seg, uint32_t colour, int upt) {
+    if (minb == 4)
+        batch_phase_kernel<CLS, 4><<<grid, threads, 0, st>>>(mem, segs, bf, n_seg, colour, upt);
+    else if (minb == 3)
+        batch_phase_kernel<CLS, 3><<<grid, threads, 0, st>>>(mem, segs, bf, n_seg, colour, upt);
+    else
+        batch_phase_kernel<CLS, 1><<<grid, threads, 0, st>>>(mem, segs, bf, n_seg, colour, upt);
+}
+
+void launch_phase_class(int cls, int minb, int grid, int threads, cudaStream_t st, const BatchMember *mem,
+                        const BatchSeg *segs, const int32_t *bf, int n_seg, uint32_t colour, int upt) {
+    switch (cls) {
+        case kCIsing16: launch_class<kCIsing16>(minb, grid, threads, st, mem, segs, bf, n_seg, colour, upt); break;
+        case kCIsing8: launch_class<kCIsing8>(minb, grid, threads, st, mem, segs, bf, n_seg, colour, upt); break;
+        case kCIsingEll: launch_class<kCIsingEll>(minb, grid, threads, st, mem, segs, bf, n_seg, colour, upt); break;
+        case kCXyzScX: launch_class<kCXyzScX>(minb, grid, threads, st, mem, segs, bf, n_seg, colour, upt); break;
+        case kCXyzScG: launch_class<kCXyzScG>(minb, grid, threads, st, mem, segs, bf, n_seg, colour, upt); break;
+        case kCXyzEllX: launch_class<kCXyzEllX>(minb, grid, threads, st, mem, segs, bf, n_seg, colour, upt); break;
+        default: launch_class<kCXyzEllG>(minb, grid, threads, st, mem, segs, bf, n_seg, colour, upt); break;
+    }
+}
+
+template <int CLS>
+cudaError_t occupancy_class(int *occ, int minb, int threads) {
+    return minb == 4   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, batch_phase_kernel<CLS, 4>, threads, 0)
+           : minb == 3 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, batch_phase_kernel<CLS, 3>, threads, 0)
+                       : cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, batch_phase_kernel<CLS, 1>, threads, 0);
+}
+
+// Resident blocks per SM of a class kernel (at least 1).
+int class_occupancy(int cls, int minb, int threads) {
+    int occ = 0;
+    cudaError_t e;
+    switch (cls) {
+        case kCIsing16: e = occupancy_class<kCIsing16>(&occ, minb, threads); break;
+        case kCIsing8: e = occupancy_class<kCIsing8>(&occ, minb, threads); break;
+        case kCIsingEll: e = occupancy_class<kCIsingEll>(&occ, minb, threads); break;
+        case kCXyzScX: e = occupancy_class<kCXyzScX>(&occ, minb, threads); break;
+        case kCXyzScG: e = occupancy_class<kCXyzScG>(&occ, minb, threads); break;
+        case kCXyzEllX: e = occupancy_class<kCXyzEllX>(&occ, minb, threads); break;
+        default: e = occupancy_class<kCXyzEllG>(&occ, minb, threads); break;
+    }
+    return e == cudaSuccess && occ > 0 ? occ : 1;
 }
 
 // Ends a batch sweep: every replica's Metropolis sweep counter advances by one.
@@ -161,17 +264,30 @@ struct ether_batch {
     BatchMember *d_members = nullptr;
     BatchSeg *d_segs = nullptr;
     size_t seg_capacity = 0;
-    std::vector<int> seg_off, seg_cnt;  // per colour phase
-    std::vector<int> bf_off, bf_grid;   // per colour phase: block ranges in d_block_first
+    // runs of segments per (group, colour phase, class): index (g * max_col + p) * kNumClasses + class
+    std::vector<int> seg_off, seg_cnt;
+    std::vector<int> bf_off, bf_grid;   // per run: block ranges in d_block_first
+    // L2-sized groups of members: a group's colour phases run back to back, so that a phase
+    // finds in L2 the other colour's spins that the group's previous phase wrote.  Groups are
+    // independent and run on n_branch parallel branches of the sweep graph.
+    std::vector<int> group_of;          // per member
+    int n_groups = 1;
+    long long group_bytes = 0;          // spin bytes per group; 0: half the L2
+    long long l2_bytes = 0;
+    int n_branch = 2;
+    std::vector<cudaStream_t> branch;
+    std::vector<cudaEvent_t> ev_join;
+    cudaEvent_t ev_fork = nullptr;
     int32_t *d_block_first = nullptr;
     size_t bf_capacity = 0;
     float xyz_cost = 20.f;              // estimated cost of an XYZ site, Ising site = 1
-    int minb = 1;                       // register cap: 1 = none, 4 = four 256-thread blocks
+    int minb = 1;                       // register cap: 1 = none, 3 or 4 = that many 256-thread blocks
     bool contiguous = false;            // segment walk (see batch_phase_kernel)
     uint32_t **d_step_of = nullptr;
     int total_R = 0, max_col = 0;
     int threads = 256, upt = 2, bps = 0;  // bps 0: as many as fit
-    int grid = 0, sm_count = 0;
+    int grid = 0, sm_count = 0;         // grid: the largest class grid
+    int cls_grid[kNumClasses] = {};     // resident blocks per SM x SMs, per class
     long long updates_per_sweep = 0;
     cudaGraphExec_t graph = nullptr;
     bool dirty = true;
@@ -199,9 +315,9 @@ BatchMember describe(const Ctx &c) {
     BatchMember m;
     std::memset(&m, 0, sizeof(m));
     if (c.model == ETHER_MODEL_ISING)
-        m.kind = !c.fast ? kBIsingCsr : (c.vec_bytes == 16 ? kBIsing16 : kBIsing8);
+        m.kind = !c.fast ? kBIsingEll : (c.vec_bytes == 16 ? kBIsing16 : kBIsing8);
     else
-        m.kind = c.fast ? kBXyzSc : kBXyzCsr;
+        m.kind = c.fast ? kBXyzSc : kBXyzEll;
     m.N = c.N;
     m.L1 = c.L[0];
     m.L2 = c.L[1];
@@ -215,14 +331,15 @@ BatchMember describe(const Ctx &c) {
     m.spins4 = c.spins4;
     m.thr = c.thr;
     m.table_entries = c.table_entries;
-    m.row_ptr = c.t.row_ptr;
-    m.nbr = c.t.nbr;
-    m.wstride = c.t.wstride;
+    m.ell_nbr = c.t.ell_nbr;
+    m.ell_ws = c.t.ell_ws;
     m.type_base = c.t.type_base;
     m.type_half = c.t.type_half;
     m.itype = c.t.itype;
-    m.jidx = c.t.jidx;
-    m.J = c.t.J;
+    m.ell_j = c.t.ell_j;
+    m.ell_deg = c.t.ell_deg;
+    m.ell_desc = c.t.ell_desc;
+    m.J4 = c.t.J4;
     m.P.zeeman = c.zeeman;
     m.P.sia = c.sia;
     m.P.angle = c.angle;
@@ -247,15 +364,24 @@ BatchMember describe(const Ctx &c) {
     return m;
 }
 
-// Units of one replica's colour class: vectors, groups of eight or sites.
+// Units of one replica's colour class: vectors (simple-cubic Ising) or sites.
 long units_of(const BatchMember &m, const Ctx &c, int colour) {
     if (colour >= c.ncol) return 0;
     const long n_c = c.col_off[colour + 1] - c.col_off[colour];
     switch (m.kind) {
         case kBIsing16: return n_c / 16;
         case kBIsing8: return n_c / 8;
-        case kBIsingCsr: return (n_c + 7) / 8;
         default: return n_c;
+    }
+}
+
+int class_of(const BatchMember &m) {
+    switch (m.kind) {
+        case kBIsing16: return kCIsing16;
+        case kBIsing8: return kCIsing8;
+        case kBIsingEll: return kCIsingEll;
+        case kBXyzSc: return m.P.zeeman || m.P.sia || m.P.angle ? kCXyzScG : kCXyzScX;
+        default: return m.P.zeeman || m.P.sia || m.P.angle ? kCXyzEllG : kCXyzEllX;
     }
 }
 
@@ -276,17 +402,38 @@ int rebuild(ether_batch &b) {
     b.h_members = hm;
     if (!b.d_members) BCUDA(cudaMalloc((void **)&b.d_members, hm.size() * sizeof(BatchMember)));
     BCUDA(cudaMemcpyAsync(b.d_members, hm.data(), hm.size() * sizeof(BatchMember), cudaMemcpyHostToDevice, b.stream));
-    // segments: phase-major, member-major, replica, tile
     b.max_col = 0;
     for (ether_ctx *h : b.members) b.max_col = std::max(b.max_col, h->c.ncol);
+    // groups: consecutive members up to the byte budget (a larger member is a group alone)
+    const long long budget = b.group_bytes > 0 ? b.group_bytes : std::max(1LL, b.l2_bytes / 2);
+    b.group_of.assign(b.members.size(), 0);
+    {
+        int g = 0;
+        long long used = 0;
+        for (size_t k = 0; k < b.members.size(); ++k) {
+            const Ctx &c = b.members[k]->c;
+            const long long bytes = (long long)c.R * c.N * (c.model == ETHER_MODEL_ISING ? 1 : (long long)sizeof(float4));
+            if (used > 0 && used + bytes > budget) {
+                ++g;
+                used = 0;
+            }
+            b.group_of[k] = g;
+            used += bytes;
+        }
+        b.n_groups = g + 1;
+    }
+    // segments: group, phase, class, member, replica, tile
     std::vector<BatchSeg> segs;
-    b.seg_off.assign(b.max_col, 0);
-    b.seg_cnt.assign(b.max_col, 0);
+    const int n_runs = b.n_groups * b.max_col * kNumClasses;
+    b.seg_off.assign(n_runs, 0);
+    b.seg_cnt.assign(n_runs, 0);
     b.updates_per_sweep = 0;
     const long tile_units = (long)b.threads * b.upt;
-    for (int p = 0; p < b.max_col; ++p) {
-        b.seg_off[p] = (int)segs.size();
+    for (int q = 0; q < n_runs; ++q) {
+        const int g = q / (b.max_col * kNumClasses), p = (q / kNumClasses) % b.max_col, cls = q % kNumClasses;
+        b.seg_off[q] = (int)segs.size();
         for (size_t k = 0; k < b.members.size(); ++k) {
+            if (b.group_of[k] != g || class_of(hm[k]) != cls) continue;
             const Ctx &c = b.members[k]->c;
             const long u = units_of(hm[k], c, p);
             if (u == 0) continue;
@@ -296,7 +443,7 @@ int rebuild(ether_batch &b) {
                                             (uint32_t)std::min(tile_units, u - f)});
             if (p < c.ncol) b.updates_per_sweep += (long long)(c.col_off[p + 1] - c.col_off[p]) * c.R;
         }
-        b.seg_cnt[p] = (int)segs.size() - b.seg_off[p];
+        b.seg_cnt[q] = (int)segs.size() - b.seg_off[q];
     }
     if (segs.size() > b.seg_capacity) {
         if (b.d_segs) cudaFree(b.d_segs);
@@ -306,13 +453,14 @@ int rebuild(ether_batch &b) {
     }
     if (!segs.empty())
         BCUDA(cudaMemcpyAsync(b.d_segs, segs.data(), segs.size() * sizeof(BatchSeg), cudaMemcpyHostToDevice, b.stream));
-    // grid: resident blocks per SM x SMs
-    int occ = 0;
-    BCUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &occ, b.minb == 4 ? batch_phase_kernel<4> : batch_phase_kernel<1>, b.threads, 0));
-    if (occ < 1) occ = 1;
-    const int bps = b.bps > 0 ? std::min(b.bps, occ) : occ;
-    b.grid = bps * b.sm_count;
+    // grid of each class kernel: its resident blocks per SM x SMs
+    b.grid = 0;
+    for (int cls = 0; cls < kNumClasses; ++cls) {
+        const int occ = class_occupancy(cls, b.minb, b.threads);
+        b.cls_grid[cls] = (b.bps > 0 ? std::min(b.bps, occ) : occ) * b.sm_count;
+    }
+    for (int q = 0; q < n_runs; ++q)
+        if (b.seg_cnt[q] > 0) b.grid = std::max(b.grid, b.cls_grid[q % kNumClasses]);
     // per phase: contiguous segment runs of about equal estimated cost, one per block
     std::vector<double> unit_cost(b.members.size());
     for (size_t k = 0; k < b.members.size(); ++k) {
@@ -321,22 +469,22 @@ int rebuild(ether_batch &b) {
         switch (hm[k].kind) {
             case kBIsing16: unit_cost[k] = 16.0; break;
             case kBIsing8: unit_cost[k] = 9.0; break;
-            case kBIsingCsr: unit_cost[k] = 20.0 * deg; break;
+            case kBIsingEll: unit_cost[k] = 3.0 * deg; break;
             case kBXyzSc: unit_cost[k] = b.xyz_cost; break;
             default: unit_cost[k] = 1.3 * b.xyz_cost * deg; break;
         }
     }
     std::vector<int32_t> bf;
-    b.bf_off.assign(b.max_col, 0);
-    b.bf_grid.assign(b.max_col, 0);
-    for (int p = 0; p < b.max_col; ++p) {
-        const int n = b.seg_cnt[p];
-        const int G = std::max(1, std::min(b.grid, n));
-        b.bf_off[p] = (int)bf.size();
-        b.bf_grid[p] = n > 0 ? G : 0;
+    b.bf_off.assign(n_runs, 0);
+    b.bf_grid.assign(n_runs, 0);
+    for (int q = 0; q < n_runs; ++q) {
+        const int n = b.seg_cnt[q];
+        const int G = std::max(1, std::min(b.cls_grid[q % kNumClasses], n));
+        b.bf_off[q] = (int)bf.size();
+        b.bf_grid[q] = n > 0 ? G : 0;
         std::vector<double> cum(n + 1, 0.0);
         for (int i = 0; i < n; ++i) {
-            const BatchSeg &S = segs[b.seg_off[p] + i];
+            const BatchSeg &S = segs[b.seg_off[q] + i];
             cum[i + 1] = cum[i] + unit_cost[S.member] * S.count;
         }
         int i = 0;
@@ -360,17 +508,35 @@ int rebuild(ether_batch &b) {
 }
 
 int issue_sweep(ether_batch &b) {
-    for (int p = 0; p < b.max_col; ++p) {
-        if (b.seg_cnt[p] == 0) continue;
-        const int32_t *bf = b.contiguous ? b.d_block_first + b.bf_off[p] : nullptr;
-        if (b.minb == 4)
-            batch_phase_kernel<4><<<b.bf_grid[p], b.threads, 0, b.stream>>>(
-                b.d_members, b.d_segs + b.seg_off[p], bf, b.seg_cnt[p], (uint32_t)p, b.upt);
-        else
-            batch_phase_kernel<1><<<b.bf_grid[p], b.threads, 0, b.stream>>>(
-                b.d_members, b.d_segs + b.seg_off[p], bf, b.seg_cnt[p], (uint32_t)p, b.upt);
+    const int nbr = std::min(b.n_branch, b.n_groups);
+    if (nbr > 1) {
+        while ((int)b.branch.size() < nbr) {
+            cudaStream_t st = nullptr;
+            cudaEvent_t ev = nullptr;
+            BCUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+            b.branch.push_back(st);
+            BCUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            b.ev_join.push_back(ev);
+        }
+        BCUDA(cudaEventRecord(b.ev_fork, b.stream));
+        for (int k = 0; k < nbr; ++k) BCUDA(cudaStreamWaitEvent(b.branch[k], b.ev_fork, 0));
+    }
+    const int per_group = b.max_col * kNumClasses;
+    for (int q = 0; q < (int)b.seg_cnt.size(); ++q) {
+        if (b.seg_cnt[q] == 0) continue;
+        const int g = q / per_group;
+        cudaStream_t st = nbr > 1 ? b.branch[g % nbr] : b.stream;
+        const int32_t *bf = b.contiguous ? b.d_block_first + b.bf_off[q] : nullptr;
+        launch_phase_class(q % kNumClasses, b.minb, b.bf_grid[q], b.threads, st, b.d_members,
+                           b.d_segs + b.seg_off[q], bf, b.seg_cnt[q], (uint32_t)((q / kNumClasses) % b.max_col),
+                           b.upt);
         BCUDA(cudaGetLastError());
     }
+    if (nbr > 1)
+        for (int k = 0; k < nbr; ++k) {
+            BCUDA(cudaEventRecord(b.ev_join[k], b.branch[k]));
+            BCUDA(cudaStreamWaitEvent(b.stream, b.ev_join[k], 0));
+        }
     batch_advance_kernel<<<(b.total_R + 255) / 256, 256, 0, b.stream>>>(b.d_step_of, b.total_R);
     BCUDA(cudaGetLastError());
     return ETHER_OK;
@@ -378,7 +544,7 @@ int issue_sweep(ether_batch &b) {
 
 int kernels_per_sweep(const ether_batch &b) {
     int n = 1;
-    for (int p = 0; p < b.max_col; ++p) n += b.seg_cnt[p] > 0 ? 1 : 0;
+    for (int cnt : b.seg_cnt) n += cnt > 0 ? 1 : 0;
     return n;
 }
 
@@ -443,6 +609,10 @@ extern "C" int ether_batch_create(ether_ctx *const *members, int32_t n_members, 
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    int l2 = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
+    b->l2_bytes = l2;
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
     b->ev_member.assign(mem.size(), nullptr);
     for (size_t k = 0; e == cudaSuccess && k < mem.size(); ++k)
@@ -472,6 +642,9 @@ extern "C" int ether_batch_destroy(ether_batch *b) {
     for (cudaEvent_t ev : b->ev_member)
         if (ev) cudaEventDestroy(ev);
     if (b->ev_done) cudaEventDestroy(b->ev_done);
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    for (cudaEvent_t ev : b->ev_join) cudaEventDestroy(ev);
+    for (cudaStream_t st : b->branch) cudaStreamDestroy(st);
     if (b->ev_t0) cudaEventDestroy(b->ev_t0);
     if (b->ev_t1) cudaEventDestroy(b->ev_t1);
     if (b->d_members) cudaFree(b->d_members);
@@ -544,14 +717,12 @@ extern "C" int ether_batch_autotune(ether_batch *b, int32_t *config, float *best
     rc = ETHER_OK;
     const int old_minb = b->minb;
     int bm = old_minb;
-    for (int cand = 0; cand < 4 && !rc; ++cand) {
-        const int minb = cand < 2 ? 1 : 4, threads = (cand & 1) ? 256 : 128;
-        int occ = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                &occ, minb == 4 ? batch_phase_kernel<4> : batch_phase_kernel<1>, threads, 0) != cudaSuccess)
-            occ = 1;
-        occ_max = std::max(occ, 1);
-        for (int upt : {1, 2, 4, 8, 16}) {
+    for (int cand = 0; cand < 6 && !rc; ++cand) {
+        const int minb = cand < 2 ? 1 : cand < 4 ? 3 : 4, threads = (cand & 1) ? 256 : 128;
+        occ_max = 1;  // the largest occupancy among the classes present
+        for (ether_ctx *h : b->members)
+            occ_max = std::max(occ_max, class_occupancy(class_of(describe(h->c)), minb, threads));
+        for (int upt : {1, 2, 4, 8, 16, 32}) {
             for (int bps : {occ_max, std::max(1, occ_max / 2)}) {
                 b->minb = minb;
                 b->contiguous = false;

@@ -11,7 +11,7 @@ namespace ether {
 // at k * n_c + rho: the eight ranks' entries are adjacent and a warp's are contiguous.  The
 // neighbour loads are unconditional (padding entries point at valid memory); the threshold
 // index idx = sum of stride * up-spin over the site's own entries.  The decision is
-// ising_csr_group's: same draws, same thresholds.
+// ising_ell_site's: same draws, same thresholds.
 __global__ void __launch_bounds__(256)
 ising_ell_kernel(uint8_t *__restrict__ spins, int N, int col_off, int n_c, uint32_t colour,
                  const int32_t *__restrict__ ell, const int32_t *__restrict__ ews,
@@ -94,34 +94,9 @@ ising_ell_site_kernel(uint8_t *__restrict__ spins, int N, int col_off, int n_c, 
     const uint32_t stream = stream_id[r], t = step[r];
     const uint32_t c3 = kMetro | (colour << 8);
     unsigned acc = 0;
-    for (int rho = blockIdx.x * blockDim.x + threadIdx.x; rho < n_c; rho += gridDim.x * blockDim.x) {
-        const int s = col_off + rho;
-        const int dg = deg[s];
-        int idx = 0;
-#pragma unroll 6
-        for (int k = 0; k < width; ++k) {
-            const int e = k * n_c + rho;  // ELL blocks hold < 2^31 entries (checked at creation)
-            const int up = sp[ell[e]];
-            const int w = ews[e];
-            if (k < dg) idx += w * up;
-        }
-        const int own = sp[s];
-        const int ty = itype[s];
-        const uint32_t T = tb[type_base[ty] + own * type_half[ty] + idx];
-        const uint32_t g = (uint32_t)rho >> 3;
-        const int j = rho & 7;
-        const U4 hi = draw(g, t, stream, c3, seed);
-        const uint32_t uh = half_of(hi, j), th = T >> 16;
-        bool flip = uh < th;
-        if (uh == th) {
-            const U4 lo = draw(g, t, stream, c3 | (1u << 16), seed);
-            flip = half_of(lo, j) <= (T & 0xFFFFu);
-        }
-        if (flip) {
-            sp[s] = (uint8_t)(own ^ 1);
-            ++acc;
-        }
-    }
+    const IsingEll A{sp, col_off, n_c, width, ell, ews, deg, itype, type_base, type_half, tb};
+    for (int rho = blockIdx.x * blockDim.x + threadIdx.x; rho < n_c; rho += gridDim.x * blockDim.x)
+        acc += ising_ell_site(A, rho, t, stream, c3, seed) ? 1u : 0u;
     warp_add_count(acc_count + r, acc);
 }
 

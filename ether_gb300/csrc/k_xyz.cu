@@ -8,29 +8,7 @@
 namespace ether {
 
 // ------------------------------------------------------------------ general lattice ----
-// Exchange field of rank rho of a colour class from its ELL block (ell: entries k * n_c + rho,
-// coalesced across a warp), in the CSR's order -- the reference's nn order -- so the fmaf
-// chain rounds as the oracle's.
-__device__ __forceinline__ Acc3 ell_field(const float4 *__restrict__ sp, const int32_t *__restrict__ ell,
-                                          const uint16_t *__restrict__ ej, const float4 *__restrict__ J4,
-                                          int n_c, int width, int rho, int deg) {
-    // The padding entries point at valid memory (the site itself, coupling 0), so the loads
-    // are unconditional and can all be in flight at once; only the fmaf is predicated.
-    Acc3 h{0.f, 0.f, 0.f};
-#pragma unroll 6
-    for (int k = 0; k < width; ++k) {
-        const int e = k * n_c + rho;  // ELL blocks hold < 2^31 entries (checked at creation)
-        const float4 Jv = J4[ej[e]];
-        const float4 Sj = sp[ell[e]];
-        if (k < deg) {
-            h.x = fmaf(Jv.x, Sj.x, h.x);
-            h.y = fmaf(Jv.y, Sj.y, h.y);
-            h.z = fmaf(Jv.z, Sj.z, h.z);
-        }
-    }
-    return h;
-}
-
+// One thread per rank of the colour class (xyz_ell_site).
 template <int OPT>
 __global__ void __launch_bounds__(256)
 xyz_ell_kernel(float4 *__restrict__ spins4, int N, int col_off, int n_c, uint32_t colour,
@@ -46,9 +24,7 @@ xyz_ell_kernel(float4 *__restrict__ spins4, int N, int col_off, int n_c, uint32_
     const uint32_t c3 = kMetro | (colour << 8);
     unsigned acc = 0;
     for (int rho = blockIdx.x * blockDim.x + threadIdx.x; rho < n_c; rho += gridDim.x * blockDim.x) {
-        const int s = col_off + rho;
-        const Acc3 h = ell_field(sp, ell, ej, J4, n_c, width, rho, deg[s]);
-        acc += metro_site<OPT>(P, sp, s, (uint32_t)rho, h.x, h.y, h.z, beta_f, t, c3, K, k1) ? 1u : 0u;
+        acc += xyz_ell_site<OPT>(P, sp, col_off, n_c, rho, ell, ej, deg, width, J4, beta_f, t, c3, K, k1) ? 1u : 0u;
     }
     warp_add_count_x(acc_count + r, acc);
 }

@@ -30,45 +30,48 @@ __device__ __forceinline__ uint32_t half_of(const U4 &b, int k) {  // halfword k
 }
 
 // ------------------------------------------------------------------ general lattice ----
-// One group of eight consecutive sites (ranks 8g .. 8g+7) of colour class `colour`.
-struct IsingCsr {
+// Neighbours of a colour class in ELL form: entry k of rank rho at k * n_c + rho (coalesced
+// across a warp), in the CSR's order, padded to the class's widest site with entries that
+// point at the site itself, so the loads are unconditional and only the sum is predicated.
+struct IsingEll {
     uint8_t *sp;  // this replica's spins
-    int col_off, n_c;
-    const int32_t *row_ptr, *nbr, *wstride;
+    int col_off, n_c, width;
+    const int32_t *ell, *ews;  // this class's block: neighbour storage index, table stride
+    const uint16_t *deg;       // neighbours per storage index
     const uint16_t *itype;
     const int32_t *type_base, *type_half;
     const uint32_t *tb;  // this replica's temperature slot's thresholds
 };
-__device__ __forceinline__ unsigned ising_csr_group(const IsingCsr &A, int g, uint32_t t,
-                                                    uint32_t stream, uint32_t c3, uint32_t seed) {
-    unsigned acc = 0;
-    const U4 hi = draw((uint32_t)g, t, stream, c3, seed);
-    bool have_lo = false;
-    U4 lo{0, 0, 0, 0};
-    for (int k = 0; k < 8; ++k) {
-        const int rho = 8 * g + k;
-        if (rho >= A.n_c) break;
-        const int s = A.col_off + rho;
-        int idx = 0;
-        for (int q = A.row_ptr[s]; q < A.row_ptr[s + 1]; ++q) idx += A.wstride[q] * (int)A.sp[A.nbr[q]];
-        const int own = A.sp[s];
-        const int ty = A.itype[s];
-        const uint32_t T = A.tb[A.type_base[ty] + own * A.type_half[ty] + idx];
-        const uint32_t uh = half_of(hi, k), th = T >> 16;
-        bool flip = uh < th;
-        if (uh == th) {
-            if (!have_lo) {
-                lo = draw((uint32_t)g, t, stream, c3 | (1u << 16), seed);
-                have_lo = true;
-            }
-            flip = half_of(lo, k) <= (T & 0xFFFFu);
-        }
-        if (flip) {
-            A.sp[s] = (uint8_t)(own ^ 1);
-            ++acc;
-        }
+
+// One site: rank rho.  Threshold-table index = sum of stride * up-spin over the neighbours;
+// the draw is halfword rho & 7 of the Philox block of group rho >> 3, and on a tie the
+// same halfword of the group's second block.
+__device__ __forceinline__ bool ising_ell_site(const IsingEll &A, int rho, uint32_t t, uint32_t stream,
+                                               uint32_t c3, uint32_t seed) {
+    const int s = A.col_off + rho;
+    const int dg = A.deg[s];
+    int idx = 0;
+#pragma unroll 6
+    for (int k = 0; k < A.width; ++k) {
+        const int e = k * A.n_c + rho;  // ELL blocks hold < 2^31 entries (checked at creation)
+        const int up = A.sp[A.ell[e]];
+        const int w = A.ews[e];
+        if (k < dg) idx += w * up;
     }
-    return acc;
+    const int own = A.sp[s];
+    const int ty = A.itype[s];
+    const uint32_t T = A.tb[A.type_base[ty] + own * A.type_half[ty] + idx];
+    const uint32_t g = (uint32_t)rho >> 3;
+    const int j = rho & 7;
+    const U4 hi = draw(g, t, stream, c3, seed);
+    const uint32_t uh = half_of(hi, j), th = T >> 16;
+    bool flip = uh < th;
+    if (uh == th) {
+        const U4 lo = draw(g, t, stream, c3 | (1u << 16), seed);
+        flip = half_of(lo, j) <= (T & 0xFFFFu);
+    }
+    if (flip) A.sp[s] = (uint8_t)(own ^ 1);
+    return flip;
 }
 
 // ------------------------------------------------------- simple cubic, colour-split ----

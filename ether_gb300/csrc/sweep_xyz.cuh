@@ -150,24 +150,40 @@ __device__ __forceinline__ Acc3 sc_field(const float4 *__restrict__ opp, int L1,
     return h;
 }
 
-// One Metropolis update of rank rho of colour class `colour` on a general lattice.
+// Exchange field of rank rho of a colour class from its ELL block (ell: entries k * n_c + rho,
+// coalesced across a warp), in the CSR's order -- the reference's nn order -- so the fmaf
+// chain rounds as the oracle's.
+__device__ __forceinline__ Acc3 ell_field(const float4 *__restrict__ sp, const int32_t *__restrict__ ell,
+                                          const uint16_t *__restrict__ ej, const float4 *__restrict__ J4,
+                                          int n_c, int width, int rho, int deg) {
+    // The padding entries point at valid memory (the site itself, coupling 0), so the loads
+    // are unconditional and can all be in flight at once; only the fmaf is predicated.
+    Acc3 h{0.f, 0.f, 0.f};
+#pragma unroll 6
+    for (int k = 0; k < width; ++k) {
+        const int e = k * n_c + rho;  // ELL blocks hold < 2^31 entries (checked at creation)
+        const float4 Jv = J4[ej[e]];
+        const float4 Sj = sp[ell[e]];
+        if (k < deg) {
+            h.x = fmaf(Jv.x, Sj.x, h.x);
+            h.y = fmaf(Jv.y, Sj.y, h.y);
+            h.z = fmaf(Jv.z, Sj.z, h.z);
+        }
+    }
+    return h;
+}
+
+// One Metropolis update of rank rho of a colour class of a general lattice (ELL block of the
+// class: ell, ej; deg per storage index).
 template <int OPT>
-__device__ __forceinline__ bool xyz_csr_site(const XyzParams &P, float4 *sp, int col_off, int rho,
-                                             const int32_t *__restrict__ row_ptr,
-                                             const int32_t *__restrict__ nbr,
-                                             const uint16_t *__restrict__ jidx,
-                                             const float *__restrict__ J, float beta_f, uint32_t t,
+__device__ __forceinline__ bool xyz_ell_site(const XyzParams &P, float4 *sp, int col_off, int n_c, int rho,
+                                             const int32_t *__restrict__ ell, const uint16_t *__restrict__ ej,
+                                             const uint16_t *__restrict__ deg, int width,
+                                             const float4 *__restrict__ J4, float beta_f, uint32_t t,
                                              uint32_t c3, const RoundKeys &K, uint32_t stream) {
     const int s = col_off + rho;
-    float hx = 0.f, hy = 0.f, hz = 0.f;
-    for (int k = row_ptr[s]; k < row_ptr[s + 1]; ++k) {
-        float4 Sj = sp[nbr[k]];
-        const float *Jp = J + 3 * jidx[k];
-        hx = fmaf(Jp[0], Sj.x, hx);
-        hy = fmaf(Jp[1], Sj.y, hy);
-        hz = fmaf(Jp[2], Sj.z, hz);
-    }
-    return metro_site<OPT>(P, sp, s, (uint32_t)rho, hx, hy, hz, beta_f, t, c3, K, stream);
+    const Acc3 h = ell_field(sp, ell, ej, J4, n_c, width, rho, deg[s]);
+    return metro_site<OPT>(P, sp, s, (uint32_t)rho, h.x, h.y, h.z, beta_f, t, c3, K, stream);
 }
 
 // One Metropolis update of rank rho of the simple-cubic colour array `own` (the other

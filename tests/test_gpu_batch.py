@@ -43,6 +43,15 @@ def build_members(specs=SPECS, seed0=11):
     return out
 
 
+def member_class(lat, sw):
+    """The batch kernel class of a member: model, fast path and, for simple-cubic Ising, the
+    vector width (16 bytes when L1/2 is a multiple of 16).  The members here have no Zeeman,
+    SIA or ANGLE options."""
+    info = sw.info()
+    vec = 16 if info.fast_path and sw.model == eg.MODEL_ISING and (int(lat.sc[0]) // 2) % 16 == 0 else 8
+    return (sw.model, info.fast_path, vec)
+
+
 def states(members):
     res = []
     for lat, sw in members:
@@ -73,8 +82,10 @@ def test_batch_equals_member_sweeps(config):
     info = batch.info()
     assert info.n_members == len(SPECS)
     assert info.n_replicas == sum(s[3] for s in SPECS)
-    max_col = max(sw.info().n_colours for _, sw in A)
-    assert info.kernels_per_sweep == max_col + 1
+    # one kernel per (colour phase, member class) with work, and the sweep-counter advance
+    assert info.kernels_per_sweep == 1 + sum(
+        len({member_class(lat, sw) for lat, sw in A if sw.info().n_colours > p})
+        for p in range(max(sw.info().n_colours for _, sw in A)))
     assert info.site_updates_per_sweep == sum(sw.N * sw.R for _, sw in A)
     assert info.kernel_launches == 4 * info.kernels_per_sweep
     assert info.last_sweep_ms > 0.0
