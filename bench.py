@@ -279,18 +279,20 @@ def run_tau(L=64, replicas=128, equil=20000, sweeps=100000, stride=10):
 BATCH_SIZES = (8, 12, 16, 24, 32, 48)
 
 
-def make_batch_members(chains=256, ladder=32, seed=1992, grouped=True):
+def make_batch_members(chains=256, ladder=32, seed=1992, grouped=True, mix="mixed", sizes=None):
     """Mixed batch: `chains` chains with L drawn uniformly from BATCH_SIZES, half Ising and
-    half Heisenberg, J = +-1 meV per chain, a `ladder`-temperature geometric ladder each
-    (0.6 .. 1.6 T_c).  grouped: chains with the same (model, L, J) share one context, one
-    ladder group per chain; else one context per chain."""
+    half Heisenberg (mix "mixed"; "ising" or "heisenberg": all of one model), J = +-1 meV per
+    chain, a `ladder`-temperature geometric ladder each (0.6 .. 1.6 T_c); `sizes` replaces
+    BATCH_SIZES.  grouped: chains with the same (model, L, J) share one context, one ladder
+    group per chain; else one context per chain."""
     import ether_gb300 as eg
     rng = np.random.default_rng(seed)
     groups = {}
     keys = []
     for c in range(chains):
-        model = eg.MODEL_ISING if c < chains // 2 else eg.MODEL_XYZ
-        key = (model, int(rng.choice(BATCH_SIZES)), int(rng.choice([-1, 1])))
+        ising = c < chains // 2 if mix == "mixed" else mix == "ising"
+        model = eg.MODEL_ISING if ising else eg.MODEL_XYZ
+        key = (model, int(rng.choice(sizes or BATCH_SIZES)), int(rng.choice([-1, 1])))
         groups[key] = groups.get(key, 0) + 1
         keys.append(key)
     items = sorted(groups.items()) if grouped else [(k, 1) for k in keys]
@@ -349,7 +351,7 @@ def _time_plain(members, steps, warmup):
 
 
 def run_batch(steps=200, warmup=5, chains=256, ladder=32, config=None, forms=(False, True),
-              plain=True):
+              plain=True, mix="mixed", sizes=None):
     """The mixed batch advanced by ether_batch (one persistent kernel per colour phase, one
     graph per sweep, autotuned tiles) and by each member's own sweeps (per-context kernels
     on the members' streams), with one context per chain and with chains grouped by
@@ -358,7 +360,7 @@ def run_batch(steps=200, warmup=5, chains=256, ladder=32, config=None, forms=(Fa
     out = {}
     for grouped in forms:
         t = time.perf_counter()
-        members, groups = make_batch_members(chains, ladder, grouped=grouped)
+        members, groups = make_batch_members(chains, ladder, grouped=grouped, mix=mix, sizes=sizes)
         setup_s = time.perf_counter() - t
         ms, info, cfg = _time_batch(members, steps, warmup, config)
         updates = float(info.site_updates_per_sweep) * steps
@@ -379,9 +381,10 @@ def run_batch(steps=200, warmup=5, chains=256, ladder=32, config=None, forms=(Fa
         for m in members:
             m.close()
     pc = out["per_chain"] if "per_chain" in out else out["grouped"]
+    n_ising = {"mixed": chains // 2, "ising": chains, "heisenberg": 0}[mix]
     return {"workload": "%d chains, L ~ U%s, %d Ising + %d Heisenberg, J = +-1 meV, %d-T "
                         "geometric ladder (0.6-1.6 T_c) each: %d replicas, %.3g spins"
-                        % (chains, list(BATCH_SIZES), chains // 2, chains - chains // 2, ladder,
+                        % (chains, list(sizes or BATCH_SIZES), n_ising, chains - n_ising, ladder,
                            info.n_replicas, info.site_updates_per_sweep),
             "value": pc["value"], "unit": "spin updates/ns", "achieved_gbs": pc["achieved_gbs"],
             "plain_note": "plain = each context's own ether_metropolis per sweep on its own "
@@ -627,6 +630,10 @@ def main():
     ap.add_argument("--sq-cells", type=int, default=12)
     ap.add_argument("--chains", type=int, default=256)
     ap.add_argument("--deck", default="c1_ising_16", choices=sorted(PROGRAM_DECKS))
+    ap.add_argument("--batch-mix", default="mixed", choices=["mixed", "ising", "heisenberg"],
+                    help="--model batch: half Ising and half Heisenberg chains, or one model only")
+    ap.add_argument("--batch-L", default="",
+                    help="--model batch: comma-separated lattice sizes to draw L from (default 8..48)")
     ap.add_argument("--batch-config", default="",
                     help="threads,units_per_thread,blocks_per_sm,walk (default: autotune)")
     args = ap.parse_args()
@@ -694,7 +701,9 @@ def main():
             return 0
         cfg = [int(x) for x in args.batch_config.split(",")] if args.batch_config else None
         r = run_batch(steps=min(args.steps, 500), warmup=args.warmup, chains=args.chains,
-                      config=cfg, forms=(False,) if cfg else (False, True), plain=not cfg)
+                      config=cfg, forms=(False,) if cfg else (False, True), plain=not cfg,
+                      mix=args.batch_mix,
+                      sizes=[int(x) for x in args.batch_L.split(",")] if args.batch_L else None)
         print(json.dumps({"metric": "spin updates/ns", "value": r["value"],
                           "unit": "spin updates/ns", "higher_is_better": True, "detail": r}))
         return 0

@@ -107,7 +107,7 @@ __device__ __forceinline__ unsigned batch_xyz_sc(const BatchMember &m, uint32_t 
     const XyzSc A{base + (size_t)colour * half, base + (size_t)(colour ^ 1u) * half,
                   m.L1, m.L2, m.L3, m.H, m.fH, m.fL2, colour, m.jx, m.jy, m.jz};
     const float beta_f = m.beta_slot_f[m.slot_of_rep[r]];
-    const RoundKeys K = m.K;
+    const RoundKeys &K = m.K;  // read in place from shared memory: no registers held
     // exchange only, Marsaglia proposals: the options fold away at compile time
     const XyzParams P = OPT == kXyzExchange ? XyzParams{0, 0, 0, 0.f, nullptr, nullptr, nullptr, 1} : m.P;
     unsigned acc = 0;
@@ -125,7 +125,7 @@ __device__ __forceinline__ unsigned batch_xyz_ell(const BatchMember &m, uint32_t
     float4 *sp = m.spins4 + (size_t)r * m.N;
     const float beta_f = m.beta_slot_f[m.slot_of_rep[r]];
     const XyzParams P = m.P;
-    const RoundKeys K = m.K;
+    const RoundKeys &K = m.K;  // read in place from shared memory: no registers held
     unsigned acc = 0;
     for (int rho = first + (int)threadIdx.x; rho < end; rho += blockDim.x)
         acc += xyz_ell_site<OPT>(P, sp, off, n_c, rho, m.ell_nbr + d.x, m.ell_j + d.x, m.ell_deg, d.y, m.J4,
