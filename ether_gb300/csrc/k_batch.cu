@@ -282,7 +282,7 @@ struct ether_batch {
     size_t bf_capacity = 0;
     float xyz_cost = 20.f;              // estimated cost of an XYZ site, Ising site = 1
     int minb = 1;                       // register cap: 1 = none, 3 or 4 = that many 256-thread blocks
-    bool contiguous = false;            // segment walk (see batch_phase_kernel)
+    int walk = 0;                       // 0 strided, 1 contiguous (see batch_phase_kernel), 2 one block per segment
     uint32_t **d_step_of = nullptr;
     int total_R = 0, max_col = 0;
     int threads = 256, upt = 2, bps = 0;  // bps 0: as many as fit
@@ -481,7 +481,8 @@ int rebuild(ether_batch &b) {
         const int n = b.seg_cnt[q];
         const int G = std::max(1, std::min(b.cls_grid[q % kNumClasses], n));
         b.bf_off[q] = (int)bf.size();
-        b.bf_grid[q] = n > 0 ? G : 0;
+        // walk 2: one block per segment, balanced by the hardware's block scheduler
+        b.bf_grid[q] = n > 0 ? (b.walk == 2 ? n : G) : 0;
         std::vector<double> cum(n + 1, 0.0);
         for (int i = 0; i < n; ++i) {
             const BatchSeg &S = segs[b.seg_off[q] + i];
@@ -526,7 +527,7 @@ int issue_sweep(ether_batch &b) {
         if (b.seg_cnt[q] == 0) continue;
         const int g = q / per_group;
         cudaStream_t st = nbr > 1 ? b.branch[g % nbr] : b.stream;
-        const int32_t *bf = b.contiguous ? b.d_block_first + b.bf_off[q] : nullptr;
+        const int32_t *bf = b.walk == 1 ? b.d_block_first + b.bf_off[q] : nullptr;
         launch_phase_class(q % kNumClasses, b.minb, b.bf_grid[q], b.threads, st, b.d_members,
                            b.d_segs + b.seg_off[q], bf, b.seg_cnt[q], (uint32_t)((q / kNumClasses) % b.max_col),
                            b.upt);
@@ -675,8 +676,9 @@ extern "C" int ether_batch_set_config(ether_batch *b, int32_t threads, int32_t u
         return bfail(ETHER_ERR_ARG, "threads per block must be 64, 128 or 256");
     if (units_per_thread < 1 || units_per_thread > 64) return bfail(ETHER_ERR_ARG, "units per thread out of [1, 64]");
     if (blocks_per_sm < 0 || blocks_per_sm > 32) return bfail(ETHER_ERR_ARG, "blocks per SM out of [0, 32]");
-    if (walk != 0 && walk != 1) return bfail(ETHER_ERR_ARG, "walk must be 0 (strided) or 1 (contiguous)");
-    b->contiguous = walk == 1;
+    if (walk < 0 || walk > 2)
+        return bfail(ETHER_ERR_ARG, "walk must be 0 (strided), 1 (contiguous) or 2 (one block per tile)");
+    b->walk = walk;
     b->threads = threads;
     b->upt = units_per_thread;
     b->bps = blocks_per_sm;
@@ -715,17 +717,22 @@ extern "C" int ether_batch_autotune(ether_batch *b, int32_t *config, float *best
     float best = 1e30f;
     int bt = old_t, bu = old_u, bb = old_b;
     rc = ETHER_OK;
-    const int old_minb = b->minb;
-    int bm = old_minb;
+    const int old_minb = b->minb, old_walk = b->walk;
+    int bm = old_minb, bw = old_walk;
     for (int cand = 0; cand < 6 && !rc; ++cand) {
         const int minb = cand < 2 ? 1 : cand < 4 ? 3 : 4, threads = (cand & 1) ? 256 : 128;
         occ_max = 1;  // the largest occupancy among the classes present
         for (ether_ctx *h : b->members)
             occ_max = std::max(occ_max, class_occupancy(class_of(describe(h->c)), minb, threads));
         for (int upt : {1, 2, 4, 8, 16, 32}) {
-            for (int bps : {occ_max, std::max(1, occ_max / 2)}) {
+            // persistent grids of all resident blocks or half of them (strided walk), and
+            // one block per tile
+            for (int v = 0; v < 3; ++v) {
+                if (v == 1 && occ_max == 1) continue;
+                const int walk = v == 2 ? 2 : 0;
+                const int bps = v == 0 ? occ_max : v == 1 ? occ_max / 2 : 0;
                 b->minb = minb;
-                b->contiguous = false;
+                b->walk = walk;
                 b->threads = threads;
                 b->upt = upt;
                 b->bps = bps;
@@ -746,18 +753,16 @@ extern "C" int ether_batch_autotune(ether_batch *b, int32_t *config, float *best
                     bu = upt;
                     bb = bps;
                     bm = minb;
+                    bw = walk;
                 }
-                if (occ_max == 1) break;
             }
             if (rc) break;
         }
         if (rc) break;
     }
-    // then the cost model that splits the segment runs between blocks
+    // then the contiguous walk with the cost model that splits the segment runs between blocks
     const float old_cost = b->xyz_cost;
     float bc = old_cost;
-    const bool old_contig = b->contiguous;
-    bool bcontig = false;
     for (float cost : {8.f, 14.f, 20.f, 32.f, 48.f}) {
         if (rc) break;
         b->threads = bt;
@@ -765,7 +770,7 @@ extern "C" int ether_batch_autotune(ether_batch *b, int32_t *config, float *best
         b->bps = bb;
         b->minb = bm;
         b->xyz_cost = cost;
-        b->contiguous = true;
+        b->walk = 1;
         b->dirty = true;
         rc = run_sweeps(*b, 1, false);
         if (!rc) rc = run_sweeps(*b, 2, true);
@@ -780,7 +785,7 @@ extern "C" int ether_batch_autotune(ether_batch *b, int32_t *config, float *best
         if (ms < best) {
             best = ms;
             bc = cost;
-            bcontig = true;
+            bw = 1;
         }
     }
     for (const Saved &s : sv) cudaMemcpyAsync(s.src, backup + s.off, s.bytes, cudaMemcpyDeviceToDevice, b->stream);
@@ -791,7 +796,7 @@ extern "C" int ether_batch_autotune(ether_batch *b, int32_t *config, float *best
     b->bps = rc ? old_b : bb;
     b->xyz_cost = rc ? old_cost : bc;
     b->minb = rc ? old_minb : bm;
-    b->contiguous = rc ? old_contig : bcontig;
+    b->walk = rc ? old_walk : bw;
     b->dirty = true;
     if (rc) return rc;
     int rr = release_members(*b);
@@ -800,7 +805,7 @@ extern "C" int ether_batch_autotune(ether_batch *b, int32_t *config, float *best
         config[0] = b->threads;
         config[1] = b->upt;
         config[2] = b->bps;
-        config[3] = b->contiguous ? 1 : 0;
+        config[3] = b->walk;
     }
     if (best_ms) *best_ms = best;
     return ETHER_OK;
@@ -823,7 +828,7 @@ extern "C" int ether_batch_get_info(ether_batch *b, ether_batch_info *info) {
     info->units_per_thread = b->upt;
     info->blocks_per_sm = b->grid / std::max(1, b->sm_count);
     info->grid = b->grid;
-    info->walk = b->contiguous ? 1 : 0;
+    info->walk = b->walk;
     info->n_segments = 0;
     for (int n : b->seg_cnt) info->n_segments += n;
     info->kernels_per_sweep = kernels_per_sweep(*b);

@@ -284,9 +284,10 @@ int ether_batch_destroy(ether_batch *batch);
  * member).  Asynchronous; ether_batch_get_info reads the time it took. */
 int ether_batch_metropolis(ether_batch *batch, int32_t nsweeps);
 /* Tile shape: threads per block (64/128/256), units per thread (1..64; a unit is a 16- or
- * 8-byte vector of simple-cubic Ising sites, a group of 8 general Ising sites, or one XYZ
- * site), resident blocks per SM (0 = as many as fit) and the walk over the tiles (0: block
- * b takes tiles b, b + grid, ...; 1: contiguous runs of equal estimated cost). */
+ * 8-byte vector of simple-cubic Ising sites, or one site of a general Ising lattice or of
+ * XYZ), resident blocks per SM (0 = as many as fit) and the walk over the tiles (0: block b
+ * of a persistent grid takes tiles b, b + grid, ...; 1: contiguous runs of equal estimated
+ * cost; 2: one block per tile, blocks per SM ignored). */
 int ether_batch_set_config(ether_batch *batch, int32_t threads, int32_t units_per_thread,
                            int32_t blocks_per_sm, int32_t walk);
 /* Autotuner: times the tile shapes, register caps and walks on the members' data (spins

@@ -2,7 +2,7 @@
 leaves every member exactly as its own ether_metropolis would -- spins bit for bit and the
 acceptance counters -- for mixed sizes and models (simple-cubic Ising with 16- and 8-byte
 vectors, general Ising, simple-cubic XYZ, general XYZ and Ising on the pyrochlore lattice,
-whose colourings have more than two classes), for every tile shape and after the
+whose colourings have more than two classes), for every tile shape and walk and after the
 autotuner."""
 import numpy as np
 import pytest
@@ -69,7 +69,7 @@ def assert_same(a, b):
 
 
 @pytest.mark.parametrize("config", [(256, 2, 0, 0), (128, 1, 1, 1), (64, 8, 2, 0), (256, 64, 0, 1),
-                                    (128, 4, 0, 1)])
+                                    (128, 4, 0, 1), (128, 2, 0, 2), (64, 1, 0, 2)])
 def test_batch_equals_member_sweeps(config):
     A = build_members()
     B = build_members()
@@ -149,7 +149,7 @@ def test_batch_rejects_bad_input():
     with pytest.raises(eg.EtherError):
         batch.set_config(96, 1, 0)
     with pytest.raises(eg.EtherError):
-        batch.set_config(128, 1, 0, walk=2)
+        batch.set_config(128, 1, 0, walk=3)
     with pytest.raises(eg.EtherError):
         batch.metropolis(-1)
     batch.close()
