@@ -331,7 +331,7 @@ extern "C" int ether_create(const ether_desc *d, ether_ctx **out) {
         if (ok) {
             c.L[0] = L1; c.L[1] = L2; c.L[2] = L3;
             const int H = L1 / 2;
-            c.vec_bytes = (H % 16 == 0) ? 16 : (H % 8 == 0) ? 8 : 0;
+            c.vec_bytes = (H % 16 == 0) ? 16 : (H % 8 == 0) ? 8 : (H % 4 == 0) ? 4 : 0;
             c.fast = (c.model == ETHER_MODEL_XYZ) || c.vec_bytes > 0;
         }
     }
@@ -1074,7 +1074,7 @@ static bool apply_variant(Ctx &c, int variant) {
     c.ising_stream = false;
     const bool p = (variant / 1000) & 1, cap = (variant / 1000) >= 2;
     const int rest = variant % 1000, w = rest / 10, v = rest % 10;
-    if ((w != 8 && w != 16) || (c.L[0] / 2) % w) return false;
+    if ((w != 4 && w != 8 && w != 16) || (c.L[0] / 2) % w) return false;
     if (p ? (v != 2 && v != 4) : (v != 1 && v != 2 && v != 4)) return false;
     if (cap && (w != 16 || v == 1)) return false;
     c.ising_persist = p;
@@ -1175,8 +1175,8 @@ extern "C" int ether_autotune(ether_ctx *h, int32_t *variant, float *best_ms) {
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    for (int cand : {161, 162, 164, 81, 82, 84, 2162, 2164, 1162, 1164, 1082, 1084, 3162, 3164, 4011,
-                     4014, 4021, 4041}) {
+    for (int cand : {161, 162, 164, 81, 82, 84, 41, 42, 44, 2162, 2164, 1162, 1164, 1082, 1084, 1042, 1044,
+                     3162, 3164, 4011, 4014, 4021, 4041}) {
         if (!apply_variant(c, cand)) continue;
         CUDA_TRY(launch_ising_sweep(c, 0));  // warm-up
         CUDA_TRY(cudaEventRecord(e0, c.stream));

@@ -22,7 +22,7 @@
 
 namespace ether {
 
-enum BatchKind : int32_t { kBIsing16 = 0, kBIsing8 = 1, kBIsingEll = 2, kBXyzSc = 3, kBXyzEll = 4 };
+enum BatchKind : int32_t { kBIsing16 = 0, kBIsing8 = 1, kBIsingEll = 2, kBXyzSc = 3, kBXyzEll = 4, kBIsing4 = 5 };
 
 // Each colour phase launches one kernel per member class present, specialised for that class
 // alone, so that every class gets the registers and occupancy of its own arithmetic.
@@ -34,7 +34,8 @@ enum BatchClass : int {
     kCXyzScG = 4,   // simple-cubic XYZ with Zeeman, SIA or ANGLE proposals
     kCXyzEllX = 5,  // general XYZ, exchange only with Marsaglia proposals
     kCXyzEllG = 6,  // general XYZ with Zeeman, SIA or ANGLE proposals
-    kNumClasses = 7
+    kCIsing4 = 7,   // simple-cubic Ising, 4-byte vectors
+    kNumClasses = 8
 };
 
 // Everything a segment needs from its member; copied into shared memory when a block moves
@@ -146,7 +147,7 @@ batch_phase_kernel(const BatchMember *__restrict__ members, const BatchSeg *__re
     // Per-warp copies of the current member's parameters and Ising thresholds: a warp moves
     // to another member or replica without waiting for the rest of the block, and the
     // parameters cost no registers.
-    constexpr bool kIsingSc = CLS == kCIsing16 || CLS == kCIsing8;
+    constexpr bool kIsingSc = CLS == kCIsing16 || CLS == kCIsing8 || CLS == kCIsing4;
     __shared__ BatchMember s_m[8];
     __shared__ uint32_t s_th[8][kIsingSc ? 16 : 1], s_tl[8][kIsingSc ? 16 : 1];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -184,6 +185,8 @@ batch_phase_kernel(const BatchMember *__restrict__ members, const BatchSeg *__re
             acc = batch_ising_sc<16>(m, r, first, end, colour, s_th[warp], s_tl[warp], t, stream, upt);
         else if constexpr (CLS == kCIsing8)
             acc = batch_ising_sc<8>(m, r, first, end, colour, s_th[warp], s_tl[warp], t, stream, upt);
+        else if constexpr (CLS == kCIsing4)
+            acc = batch_ising_sc<4>(m, r, first, end, colour, s_th[warp], s_tl[warp], t, stream, upt);
         else if constexpr (CLS == kCIsingEll)
             acc = batch_ising_ell(m, r, first, end, colour, t, stream);
         else if constexpr (CLS == kCXyzScX)
@@ -218,6 +221,7 @@ void launch_phase_class(int cls, int minb, int grid, int threads, cudaStream_t s
         case kCXyzScX: launch_class<kCXyzScX>(minb, grid, threads, st, mem, segs, bf, n_seg, colour, upt); break;
         case kCXyzScG: launch_class<kCXyzScG>(minb, grid, threads, st, mem, segs, bf, n_seg, colour, upt); break;
         case kCXyzEllX: launch_class<kCXyzEllX>(minb, grid, threads, st, mem, segs, bf, n_seg, colour, upt); break;
+        case kCIsing4: launch_class<kCIsing4>(minb, grid, threads, st, mem, segs, bf, n_seg, colour, upt); break;
         default: launch_class<kCXyzEllG>(minb, grid, threads, st, mem, segs, bf, n_seg, colour, upt); break;
     }
 }
@@ -240,6 +244,7 @@ int class_occupancy(int cls, int minb, int threads) {
         case kCXyzScX: e = occupancy_class<kCXyzScX>(&occ, minb, threads); break;
         case kCXyzScG: e = occupancy_class<kCXyzScG>(&occ, minb, threads); break;
         case kCXyzEllX: e = occupancy_class<kCXyzEllX>(&occ, minb, threads); break;
+        case kCIsing4: e = occupancy_class<kCIsing4>(&occ, minb, threads); break;
         default: e = occupancy_class<kCXyzEllG>(&occ, minb, threads); break;
     }
     return e == cudaSuccess && occ > 0 ? occ : 1;
@@ -315,7 +320,7 @@ BatchMember describe(const Ctx &c) {
     BatchMember m;
     std::memset(&m, 0, sizeof(m));
     if (c.model == ETHER_MODEL_ISING)
-        m.kind = !c.fast ? kBIsingEll : (c.vec_bytes == 16 ? kBIsing16 : kBIsing8);
+        m.kind = !c.fast ? kBIsingEll : c.vec_bytes == 16 ? kBIsing16 : c.vec_bytes == 8 ? kBIsing8 : kBIsing4;
     else
         m.kind = c.fast ? kBXyzSc : kBXyzEll;
     m.N = c.N;
@@ -371,6 +376,7 @@ long units_of(const BatchMember &m, const Ctx &c, int colour) {
     switch (m.kind) {
         case kBIsing16: return n_c / 16;
         case kBIsing8: return n_c / 8;
+        case kBIsing4: return n_c / 4;
         default: return n_c;
     }
 }
@@ -379,6 +385,7 @@ int class_of(const BatchMember &m) {
     switch (m.kind) {
         case kBIsing16: return kCIsing16;
         case kBIsing8: return kCIsing8;
+        case kBIsing4: return kCIsing4;
         case kBIsingEll: return kCIsingEll;
         case kBXyzSc: return m.P.zeeman || m.P.sia || m.P.angle ? kCXyzScG : kCXyzScX;
         default: return m.P.zeeman || m.P.sia || m.P.angle ? kCXyzEllG : kCXyzEllX;
@@ -469,6 +476,7 @@ int rebuild(ether_batch &b) {
         switch (hm[k].kind) {
             case kBIsing16: unit_cost[k] = 16.0; break;
             case kBIsing8: unit_cost[k] = 9.0; break;
+            case kBIsing4: unit_cost[k] = 5.5; break;
             case kBIsingEll: unit_cost[k] = 3.0 * deg; break;
             case kBXyzSc: unit_cost[k] = b.xyz_cost; break;
             default: unit_cost[k] = 1.3 * b.xyz_cost * deg; break;

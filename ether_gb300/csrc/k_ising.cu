@@ -453,9 +453,9 @@ bool ising_resident_possible(const Ctx &c, size_t smem_max) {
 // during a stream capture).
 cudaError_t prepare_ising_resident(const Ctx &c) {
     const int smem = c.L[0] * c.L[1] * c.L[2];
-    return c.vec_bytes == 16
-               ? cudaFuncSetAttribute(ising_sc_resident<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
-               : cudaFuncSetAttribute(ising_sc_resident<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    return c.vec_bytes == 16  ? cudaFuncSetAttribute(ising_sc_resident<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
+           : c.vec_bytes == 8 ? cudaFuncSetAttribute(ising_sc_resident<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
+                              : cudaFuncSetAttribute(ising_sc_resident<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
 }
 
 cudaError_t launch_ising_resident(Ctx &c, int nsweeps) {
@@ -466,8 +466,13 @@ cudaError_t launch_ising_resident(Ctx &c, int nsweeps) {
             c.spins, c.L[0], c.L[1], c.L[2], make_fastdiv((uint32_t)(c.L[0] / 2)), make_fastdiv((uint32_t)c.L[1]),
             c.thr, c.table_entries, c.slot_of_rep, c.stream_id, c.step, c.seed, round_keys(c.seed), nsweeps,
             c.acc_count);
-    } else {
+    } else if (c.vec_bytes == 8) {
         ising_sc_resident<8><<<c.R, bs, smem, c.stream>>>(
+            c.spins, c.L[0], c.L[1], c.L[2], make_fastdiv((uint32_t)(c.L[0] / 2)), make_fastdiv((uint32_t)c.L[1]),
+            c.thr, c.table_entries, c.slot_of_rep, c.stream_id, c.step, c.seed, round_keys(c.seed), nsweeps,
+            c.acc_count);
+    } else {
+        ising_sc_resident<4><<<c.R, bs, smem, c.stream>>>(
             c.spins, c.L[0], c.L[1], c.L[2], make_fastdiv((uint32_t)(c.L[0] / 2)), make_fastdiv((uint32_t)c.L[1]),
             c.thr, c.table_entries, c.slot_of_rep, c.stream_id, c.step, c.seed, round_keys(c.seed), nsweeps,
             c.acc_count);
@@ -500,12 +505,17 @@ cudaError_t launch_ising_sweep(Ctx &c, int colour) {
             case 81: launch_sc<8, 1, 1>(c, colour); break;
             case 82: launch_sc<8, 2, 1>(c, colour); break;
             case 84: launch_sc<8, 4, 1>(c, colour); break;
+            case 41: launch_sc<4, 1, 1>(c, colour); break;
+            case 42: launch_sc<4, 2, 1>(c, colour); break;
+            case 44: launch_sc<4, 4, 1>(c, colour); break;
             case 2162: launch_sc<16, 2, 4>(c, colour); break;
             case 2164: launch_sc<16, 4, 4>(c, colour); break;
             case 1162: launch_persist<16, 2, 1>(c, colour); break;
             case 1164: launch_persist<16, 4, 1>(c, colour); break;
             case 1082: launch_persist<8, 2, 1>(c, colour); break;
             case 1084: launch_persist<8, 4, 1>(c, colour); break;
+            case 1042: launch_persist<4, 2, 1>(c, colour); break;
+            case 1044: launch_persist<4, 4, 1>(c, colour); break;
             case 3162: launch_persist<16, 2, 4>(c, colour); break;
             default: launch_persist<16, 4, 4>(c, colour); break;
         }

@@ -77,8 +77,8 @@ __device__ __forceinline__ bool ising_ell_site(const IsingEll &A, int rho, uint3
 // ------------------------------------------------------- simple cubic, colour-split ----
 // Colour c array: rho = (z*L2 + y)*H + xh, H = L1/2, site x = 2*xh + ((y+z+c)&1).
 // All six neighbours live in the other colour's array: same xh in rows (y±1,z), (y,z±1),
-// and xh, xh∓1 in row (y,z).  A thread takes W (8 or 16) consecutive bytes of one row
-// (W | H), i.e. one or two random-number groups.  Byte sums of 0/1 spins never carry
+// and xh, xh∓1 in row (y,z).  A thread takes W (4, 8 or 16) consecutive bytes of one row
+// (W | H): half of a random-number group, one or two.  Byte sums of 0/1 spins never carry
 // (max 6); e = n + 7 s (<= 13) is formed for four sites at once; flips are one predicated
 // XOR per site and are counted with popc.
 template <int W>
@@ -89,7 +89,9 @@ struct Vec {
 template <int W>
 __device__ __forceinline__ Vec<W> ldv(const uint8_t *p) {
     Vec<W> v;
-    if constexpr (W == 8) {
+    if constexpr (W == 4) {
+        v.w[0] = *reinterpret_cast<const uint32_t *>(p);
+    } else if constexpr (W == 8) {
         uint2 q = *reinterpret_cast<const uint2 *>(p);
         v.w[0] = q.x; v.w[1] = q.y;
     } else {
@@ -100,7 +102,9 @@ __device__ __forceinline__ Vec<W> ldv(const uint8_t *p) {
 }
 template <int W>
 __device__ __forceinline__ void stv(uint8_t *p, const Vec<W> &v) {
-    if constexpr (W == 8) {
+    if constexpr (W == 4) {
+        *reinterpret_cast<uint32_t *>(p) = v.w[0];
+    } else if constexpr (W == 8) {
         *reinterpret_cast<uint2 *>(p) = make_uint2(v.w[0], v.w[1]);
     } else {
         *reinterpret_cast<uint4 *>(p) = make_uint4(v.w[0], v.w[1], v.w[2], v.w[3]);
@@ -179,7 +183,9 @@ __device__ __forceinline__ Vec<W> ising_sc_update(const Vec<W> &me, const Vec<W>
     U4 rh{0, 0, 0, 0};
 #pragma unroll
     for (int q = 0; q < NW; ++q) {
-        if ((q & 1) == 0) rh = draw_rk((uint32_t)((rho0 >> 3) + (q >> 1)), t, stream, c3, K);
+        // word q's half of its group's block: q & 1, or for W = 4 the vector's own half
+        const int odd = W == 4 ? (rho0 >> 2) & 1 : q & 1;
+        if (W == 4 || (q & 1) == 0) rh = draw_rk((uint32_t)((rho0 >> 3) + (q >> 1)), t, stream, c3, K);
         const uint32_t s0 = me.w[q];
         const uint32_t e4s = sc_e4s<W>(o0, edge, par, a, b, c, d, q, s0);
         e4[q] = e4s;
@@ -187,7 +193,7 @@ __device__ __forceinline__ Vec<W> ising_sc_update(const Vec<W> &me, const Vec<W>
         const uint32_t t1 = *reinterpret_cast<const uint32_t *>(th_bytes + __byte_perm(e4s, 0, 0x4441));
         const uint32_t t2 = *reinterpret_cast<const uint32_t *>(th_bytes + __byte_perm(e4s, 0, 0x4442));
         const uint32_t t3 = *reinterpret_cast<const uint32_t *>(th_bytes + (e4s >> 24));
-        const uint32_t wa = (q & 1) ? rh.z : rh.x, wb = (q & 1) ? rh.w : rh.y;
+        const uint32_t wa = odd ? rh.z : rh.x, wb = odd ? rh.w : rh.y;
         const uint32_t u0 = wa & 0xFFFFu, u1 = wa >> 16, u2 = wb & 0xFFFFu, u3 = wb >> 16;
         uint32_t m = 0;
         if (u0 < t0) m |= 0x00000001u;
@@ -201,8 +207,8 @@ __device__ __forceinline__ Vec<W> ising_sc_update(const Vec<W> &me, const Vec<W>
     if (tie) {
 #pragma unroll
         for (int q = 0; q < NW; ++q) {
-            const uint32_t m = resolve_ties((uint32_t)((rho0 >> 3) + (q >> 1)), t, stream, c3, seed, q & 1,
-                                            e4[q], s_th, s_tl);
+            const uint32_t m = resolve_ties((uint32_t)((rho0 >> 3) + (q >> 1)), t, stream, c3, seed,
+                                            W == 4 ? (rho0 >> 2) & 1 : q & 1, e4[q], s_th, s_tl);
             out.w[q] ^= m;
             cnt += m;
         }
@@ -219,7 +225,7 @@ __device__ __forceinline__ uint32_t ising_sc_vectors(const IsingSc &A, int vfirs
                                                      const uint32_t *s_tl, uint32_t t,
                                                      uint32_t stream, uint32_t c3, uint32_t seed,
                                                      const RoundKeys &K) {
-    static_assert(W == 8 || W == 16, "vector of one or two random-number groups");
+    static_assert(W == 4 || W == 8 || W == 16, "vector of half, one or two random-number groups");
     const int H = A.H, L2 = A.L2, L3 = A.L3;
     uint32_t cnt = 0;
 #pragma unroll

@@ -225,7 +225,7 @@ int ether_end_sweep(ether_ctx *ctx);
 /* Autotuner: times the kernel variants of this context's fast path on its own data
  * (spins and counters are restored) and keeps the fastest; the choice is cached per size
  * class for the process.  Ising simple cubic: variant = 1000 (persistent) + 2000 (register
- * cap) + bytes per vector * 10 + vectors per thread, or 4000 + 10 * vectors per step + 1 / 4
+ * cap) + bytes per vector (4, 8, 16) * 10 + vectors per thread, or 4000 + 10 * vectors per step + 1 / 4
  * (shared-memory staged kernel).  XYZ simple cubic: variant = 5000 + 10 * sites per thread +
  * blocks per SM of the register cap (5011 .. 5015, 5021, 5022).  best_ms = one colour phase.  Either
  * output may be NULL. */
@@ -283,8 +283,8 @@ int ether_batch_destroy(ether_batch *batch);
 /* nsweeps Metropolis sweeps of every member (no overrelaxation, no PT: those stay per
  * member).  Asynchronous; ether_batch_get_info reads the time it took. */
 int ether_batch_metropolis(ether_batch *batch, int32_t nsweeps);
-/* Tile shape: threads per block (64/128/256), units per thread (1..64; a unit is a 16- or
- * 8-byte vector of simple-cubic Ising sites, or one site of a general Ising lattice or of
+/* Tile shape: threads per block (64/128/256), units per thread (1..64; a unit is a 16-, 8-
+ * or 4-byte vector of simple-cubic Ising sites, or one site of a general Ising lattice or of
  * XYZ), resident blocks per SM (0 = as many as fit) and the walk over the tiles (0: block b
  * of a persistent grid takes tiles b, b + grid, ...; 1: contiguous runs of equal estimated
  * cost; 2: one block per tile, blocks per SM ignored). */

@@ -1,6 +1,6 @@
 """Batched sweeps (ether_batch_*): one persistent kernel per colour phase over many contexts
 leaves every member exactly as its own ether_metropolis would -- spins bit for bit and the
-acceptance counters -- for mixed sizes and models (simple-cubic Ising with 16- and 8-byte
+acceptance counters -- for mixed sizes and models (simple-cubic Ising with 16-, 8- and 4-byte
 vectors, general Ising, simple-cubic XYZ, general XYZ and Ising on the pyrochlore lattice,
 whose colourings have more than two classes), for every tile shape and walk and after the
 autotuner."""
@@ -19,6 +19,7 @@ AFM = [[(1, 1, (1.0, 1.0, 1.0))]]
 SPECS = [
     (lambda: eg.simple_cubic((32, 8, 6)), eg.MODEL_ISING, FM, 3, 0),       # 16-byte vectors
     (lambda: eg.simple_cubic(16), eg.MODEL_ISING, AFM, 2, 0),              # 8-byte vectors
+    (lambda: eg.simple_cubic((8, 6, 4)), eg.MODEL_ISING, FM, 3, 0),        # 4-byte vectors
     (lambda: eg.simple_cubic(12), eg.MODEL_ISING, FM, 2, 0),               # H = 6: general path
     (lambda: eg.simple_cubic(8), eg.MODEL_ISING, FM, 2, eg.FLAG_FORCE_GENERAL),
     (lambda: eg.pyrochlore(2), eg.MODEL_ISING, AFM, 2, 0),
@@ -45,10 +46,13 @@ def build_members(specs=SPECS, seed0=11):
 
 def member_class(lat, sw):
     """The batch kernel class of a member: model, fast path and, for simple-cubic Ising, the
-    vector width (16 bytes when L1/2 is a multiple of 16).  The members here have no Zeeman,
-    SIA or ANGLE options."""
+    vector width (the largest of 16, 8 and 4 bytes that divides L1/2).  The members here have
+    no Zeeman, SIA or ANGLE options."""
     info = sw.info()
-    vec = 16 if info.fast_path and sw.model == eg.MODEL_ISING and (int(lat.sc[0]) // 2) % 16 == 0 else 8
+    vec = 0
+    if info.fast_path and sw.model == eg.MODEL_ISING:
+        H = int(lat.sc[0]) // 2
+        vec = 16 if H % 16 == 0 else 8 if H % 8 == 0 else 4
     return (sw.model, info.fast_path, vec)
 
 
@@ -128,7 +132,7 @@ def test_batch_autotune_restores_state_and_keeps_parity():
 
 def test_batch_members_with_variants():
     """Members on other Ising kernel variants (8-byte vectors, several per thread)."""
-    specs = [SPECS[0], SPECS[1], SPECS[5]]
+    specs = [SPECS[0], SPECS[1], SPECS[6]]
     A = build_members(specs)
     B = build_members(specs)
     A[0][1].set_variant(84)

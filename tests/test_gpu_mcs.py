@@ -193,12 +193,14 @@ def test_record_series_equals_step_by_step(model):
     np.testing.assert_allclose(c, z, rtol=1e-12)
 
 
-def test_resident_sweeps_equal_phase_launches():
+@pytest.mark.parametrize("L", [16, 8, 24])
+def test_resident_sweeps_equal_phase_launches(L):
     """A small simple-cubic Ising lattice with enough replicas runs the sweeps between PT and
     measurement steps in the shared-memory resident kernel: same draws, so the configurations,
     observable sums, PT slots and acceptance counts equal those of the phase-by-phase launches
-    (ETHER_FLAG_NO_RESIDENT), with far fewer launches."""
-    lat = eg.simple_cubic(16)
+    (ETHER_FLAG_NO_RESIDENT), with far fewer launches.  L = 16: 8-byte vectors; 8 and 24:
+    4-byte vectors."""
+    lat = eg.simple_cubic(L)
     j = eg.couplings(1, FM, [1.0])
     temps = np.linspace(3.5, 6.0, 48)
     runs = []

@@ -41,20 +41,22 @@ def ising_replay(lat, shells, kT, sweeps, flags=0, seed=1992, stream=0, variant=
     return sw, ion, g, sum(acc_o), acc_g[0]
 
 
+# L = 8 and (24, 6, 4) take the 4-byte vectors (L1/2 = 4, 12), 16 the 8-byte ones, 6 and 5
+# the general path
 @pytest.mark.parametrize("L,flags", [(8, 0), (16, 0), (8, eg.FLAG_FORCE_GENERAL), (6, 0), (5, 0),
-                                     ((16, 8, 12), 0)])
+                                     ((16, 8, 12), 0), ((24, 6, 4), 0)])
 @pytest.mark.parametrize("kT", [4.511, 2.0, 10.0])
 def test_ising_sc_bit_exact(L, flags, kT):
     lat = eg.simple_cubic(L)
     sw, ion, g, ao, ag = ising_replay(lat, FM, kT, 20, flags=flags)
     np.testing.assert_array_equal(g[:, 3], ion[:, 3])
     assert ao == pytest.approx(ag, abs=1e-12)
-    if L == 16 and flags == 0:
+    if flags == 0 and L in (8, 16, (24, 6, 4)):
         assert sw.info().fast_path == 1
 
 
-@pytest.mark.parametrize("variant", [161, 162, 164, 81, 82, 84, 2162, 2164, 1162, 1164, 1082, 1084,
-                                     3162, 3164])
+@pytest.mark.parametrize("variant", [161, 162, 164, 81, 82, 84, 41, 42, 44, 2162, 2164, 1162, 1164,
+                                     1082, 1084, 1042, 1044, 3162, 3164])
 def test_ising_sc_every_kernel_variant_bit_exact(variant):
     lat = eg.simple_cubic((32, 8, 6))
     sw, ion, g, ao, ag = ising_replay(lat, FM, 4.511, 8, variant=variant)
