@@ -825,6 +825,8 @@ static int issue_step(Ctx &c, const ether_schedule *sch, bool ovrr, bool pt, boo
     return ETHER_OK;
 }
 
+static int variant_of(const Ctx &c);
+
 // Steps sig[0 .. n): with a resident context the sweeps that no OVRR, PT or measurement
 // separates run as one ising_sc_resident launch; otherwise step by step.
 static int issue_steps(Ctx &c, const ether_schedule *sch, const int8_t *sig, int n) {
@@ -910,8 +912,9 @@ extern "C" int ether_mcs(ether_ctx *h, const ether_schedule *sch, int32_t step0,
             int rc = issue_steps(c, sch, sig.data(), n);
             if (rc) return rc;
         } else {
+            // the kernel variant is part of the key: a graph keeps the kernels it was captured with
             std::string key(sig.begin(), sig.end());
-            key += std::to_string(c.vec_bytes * 10 + c.ising_vpt) + "/" + std::to_string(sch->ovrr_para) +
+            key += std::to_string(variant_of(c)) + "/" + std::to_string(sch->ovrr_para) +
                    (c.spiral_ptr ? "/s" : "");
             auto it = c.graphs.find(key);
             if (it == c.graphs.end()) {
