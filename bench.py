@@ -392,21 +392,26 @@ def run_batch(steps=200, warmup=5, chains=256, ladder=32, config=None, forms=(Fa
             **out}
 
 
-def run_learned(L=64, R=256, train_steps=3000, n_plain=40000, n_learn=6000):
-    """Learned 4^3-patch proposal at T_c of the L^3 Ising model: trained on plain-sweep
-    configurations of an 8-temperature ladder (0.9 .. 1.1 T_c), then tau_int(|M|) and the
-    independent samples per second of (a) plain sweeps, (b) plain + learned sweep per step,
-    (c) learned sweeps alone, all with R replicas at T_c."""
+def run_learned(L=64, R=256, train_steps=3000, n_plain=40000, n_learn=6000, heisenberg=False):
+    """Learned 4^3-patch proposal at T_c of the L^3 Ising (or Heisenberg) model: trained on
+    plain-sweep configurations of an 8-temperature ladder (0.9 .. 1.1 T_c), then tau_int(|M|)
+    and the independent samples per second of (a) plain sweeps, (b) plain + learned sweep per
+    step, (c) learned sweeps alone, all with R replicas at T_c."""
     import ether_gb300 as eg
     from ether_gb300.analysis import tau_int
     lat = eg.simple_cubic(L)
     j = eg.couplings(1, [[(1, 1, (-J_MEV, -J_MEV, -J_MEV))]], [1.0])
-    sw = eg.Sweep.from_lattice(lat, j, np.array([1.0]), eg.MODEL_ISING, replicas=R, seed=31)
-    ktc = KTC_ISING * J_MEV * 1e-3
+    model = eg.MODEL_XYZ if heisenberg else eg.MODEL_ISING
+    sw = eg.Sweep.from_lattice(lat, j, np.array([1.0]), model, replicas=R, seed=31)
+    ktc = (KTC_HEIS if heisenberg else KTC_ISING) * J_MEV * 1e-3
     sw.set_beta(1.0 / (np.repeat(ktc * np.linspace(0.9, 1.1, 8), R // 8)))
     rng = np.random.default_rng(7)
     ion = lat.ion.copy()
-    ion[:, 3] = rng.choice([-1.0, 1.0], size=lat.N)
+    if heisenberg:
+        v = rng.normal(size=(lat.N, 3))
+        ion[:, 1:4] = v / np.linalg.norm(v, axis=1, keepdims=True)
+    else:
+        ion[:, 3] = rng.choice([-1.0, 1.0], size=lat.N)
     sw.set_spins(ion)
     sw.metropolis(2000, accept=False)
     lr = eg.Learned(sw, seed=5, capacity=1 << 21)
@@ -433,7 +438,8 @@ def run_learned(L=64, R=256, train_steps=3000, n_plain=40000, n_learn=6000):
     acc = (lr.accepts().sum() - a0) / max(1, lr.info().proposed - p0)
     lr.sweep_(20)
     sweep_ms = lr.info().last_sweep_ms
-    res = {"workload": "learned 4^3-patch proposal, %d^3 Ising at T_c, %d replicas" % (L, R),
+    res = {"workload": "learned 4^3-patch proposal, %d^3 %s at T_c, %d replicas"
+                       % (L, "Heisenberg" if heisenberg else "Ising", R),
            "train_steps": train_steps, "final_loss": loss, "train_ms": train_ms,
            "acceptance_at_tc": acc, "learned_sweep_ms": sweep_ms}
     for name, m, n, secs in (("plain", m_plain, n_plain, s_plain), ("plain_plus_learned", m_both, n_learn, s_both),
@@ -450,19 +456,26 @@ def run_learned(L=64, R=256, train_steps=3000, n_plain=40000, n_learn=6000):
     return res
 
 
-def run_learned_sweep(L=64, R=256, sweeps=3):
+def run_learned_sweep(L=64, R=256, sweeps=3, heisenberg=False):
     """Time of the learned sweep alone (untrained network, T_c): the profiling case."""
     import ether_gb300 as eg
     lat = eg.simple_cubic(L)
     j = eg.couplings(1, [[(1, 1, (-J_MEV, -J_MEV, -J_MEV))]], [1.0])
-    sw = eg.Sweep.from_lattice(lat, j, np.array([1.0]), eg.MODEL_ISING, replicas=R, seed=31)
-    sw.set_beta(1.0 / (KTC_ISING * J_MEV * 1e-3))
+    model = eg.MODEL_XYZ if heisenberg else eg.MODEL_ISING
+    sw = eg.Sweep.from_lattice(lat, j, np.array([1.0]), model, replicas=R, seed=31)
+    sw.set_beta(1.0 / ((KTC_HEIS if heisenberg else KTC_ISING) * J_MEV * 1e-3))
     rng = np.random.default_rng(7)
     ion = lat.ion.copy()
-    ion[:, 3] = rng.choice([-1.0, 1.0], size=lat.N)
+    if heisenberg:
+        v = rng.normal(size=(lat.N, 3))
+        ion[:, 1:4] = v / np.linalg.norm(v, axis=1, keepdims=True)
+    else:
+        ion[:, 3] = rng.choice([-1.0, 1.0], size=lat.N)
     sw.set_spins(ion)
     lr = eg.Learned(sw, seed=5, capacity=4096)
     sw.metropolis(10, accept=False)
+    lr.sweep_(1)  # warm-up: first launches and library loading stay out of the timed sweeps
+    sw.sync()
     lr.sweep_(sweeps)
     sw.sync()
     res = {"L": L, "replicas": R, "learned_sweep_ms": lr.info().last_sweep_ms,
@@ -619,7 +632,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--model", default="ising",
-                    choices=["ising", "heisenberg", "sq", "batch", "learned", "learned-sweep",
+                    choices=["ising", "heisenberg", "sq", "batch", "learned", "learned-heisenberg", "learned-sweep",
+                             "learned-sweep-heisenberg",
                              "program", "pyrochlore", "pyrochlore-ising"])
     ap.add_argument("--L", type=int, default=64)
     ap.add_argument("--replicas", type=int, default=0)
@@ -680,10 +694,18 @@ def main():
                           "higher_is_better": True, "detail": r}))
         return 0
 
-    if args.model == "learned-sweep":
+    if args.model == "learned-heisenberg":
         if rank != 0:
             return 0
-        r = run_learned_sweep(args.L, args.replicas or 256)
+        r = run_learned(args.L, R=64, train_steps=2000, n_plain=60000, n_learn=6000, heisenberg=True)
+        print(json.dumps({"metric": "independent samples/s gain", "value": r["learned_only"]["gain_vs_plain"],
+                          "unit": "x plain", "higher_is_better": True, "detail": r}))
+        return 0
+
+    if args.model in ("learned-sweep", "learned-sweep-heisenberg"):
+        if rank != 0:
+            return 0
+        r = run_learned_sweep(args.L, args.replicas or 256, heisenberg=args.model == "learned-sweep-heisenberg")
         print(json.dumps({"metric": "learned sweep ms", "value": r["learned_sweep_ms"], "unit": "ms",
                           "higher_is_better": False, "detail": r}))
         return 0

@@ -165,6 +165,9 @@ SIGNATURES = {
     "ether_learn_loss_grad": (C.c_int, [P, C.POINTER(C.c_float), PU32, C.c_int32, PD,
                                         C.POINTER(C.c_float)]),
     "ether_learn_forward": (C.c_int, [P, C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_float)]),
+    "ether_learn_loss_grad_f": (C.c_int, [P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int32, PD,
+                                          C.POINTER(C.c_float)]),
+    "ether_learn_get_shape": (C.c_int, [P, PI32, PI32, PI32]),
     "ether_learn_set_dump": (C.c_int, [P, C.c_int32]),
     "ether_learn_get_dump": (C.c_int, [P, C.POINTER(C.c_float)]),
     "ether_learn_get_info": (C.c_int, [P, C.POINTER(LearnInfo)]),

@@ -28,14 +28,14 @@
 #include <vector>
 
 #include "internal.h"
+#include "learn_common.cuh"
 #include "rng_math.cuh"
 #include "tc_util.cuh"
 
 namespace ether {
 namespace learn {
 
-constexpr uint32_t kLearn = 4;  // Philox purpose
-constexpr int NI = 128, NH = 128, NO = 32;
+constexpr int NI = 128, NO = 32;  // network input and output widths (hidden: NH)
 constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + NH * NI, OFF_W2 = OFF_B1 + NH, OFF_B2 = OFF_W2 + NH * NH,
               OFF_W3 = OFF_B2 + NH, OFF_B3 = OFF_W3 + NO * NH, NPARAM = OFF_B3 + NO;
 
@@ -119,31 +119,7 @@ static Geometry make_geometry() {
     return g;
 }
 
-// Closed forms of the same geometry, for fully unrolled loops (folded at compile time).
-// Row = b + 4c; the two A-sites (B-sites) of a row sit at a = p, p + 2 (a = 1 - p, 3 - p),
-// p = (b + c) & 1, and have indices 2 row + (a >> 1).
-__host__ __device__ constexpr int geo_b_a(int m) { return (1 - ((((m >> 1) & 3) + ((m >> 1) >> 2)) & 1)) + 2 * (m & 1); }
-__host__ __device__ constexpr int geo_a_a(int k) { return ((((k >> 1) & 3) + ((k >> 1) >> 2)) & 1) + 2 * (k & 1); }
-// Neighbour q (-x, +x, -y, +y, -z, +z) of B-site m: A-site index (>= 0) or -(1 + boundary index).
-__host__ __device__ constexpr int geo_bn(int m, int q) {
-    const int row = m >> 1, b = row & 3, c = row >> 2, a = geo_b_a(m);
-    return q == 0 ? (a == 0 ? -(1 + b + 4 * c) : 2 * row + ((a - 1) >> 1))
-         : q == 1 ? (a == 3 ? -(1 + 16 + b + 4 * c) : 2 * row + ((a + 1) >> 1))
-         : q == 2 ? (b == 0 ? -(1 + 32 + a + 4 * c) : 2 * (row - 1) + (a >> 1))
-         : q == 3 ? (b == 3 ? -(1 + 48 + a + 4 * c) : 2 * (row + 1) + (a >> 1))
-         : q == 4 ? (c == 0 ? -(1 + 64 + a + 4 * b) : 2 * (row - 4) + (a >> 1))
-                  : (c == 3 ? -(1 + 80 + a + 4 * b) : 2 * (row + 4) + (a >> 1));
-}
-// Boundary neighbour q of A-site k (-1 if that neighbour is inside the patch).
-__host__ __device__ constexpr int geo_ab(int k, int q) {
-    const int row = k >> 1, b = row & 3, c = row >> 2, a = geo_a_a(k);
-    return q == 0 ? (a == 0 ? b + 4 * c : -1)
-         : q == 1 ? (a == 3 ? 16 + b + 4 * c : -1)
-         : q == 2 ? (b == 0 ? 32 + a + 4 * c : -1)
-         : q == 3 ? (b == 3 ? 48 + a + 4 * c : -1)
-         : q == 4 ? (c == 0 ? 64 + a + 4 * b : -1)
-                  : (c == 3 ? 80 + a + 4 * b : -1);
-}
+// Closed forms of the same geometry (geo_*) are in learn_common.cuh.
 
 // ------------------------------------------------------------- own FP32 functions ----
 // Same operation sequence as oracle/learn_oracle.c (compiled with --fmad=false: explicit
@@ -740,6 +716,7 @@ using namespace ether::learn;
 
 struct ether_learn {
     ether_ctx *ctx = nullptr;
+    learn::XyzLearn *xyz = nullptr;  // an XYZ context's learner (k_learn_xyz.cu); the rest unused
     uint32_t seed = 0;
     int R = 0, L[3] = {0, 0, 0}, P[3] = {0, 0, 0};
     long long Pc = 0, half = 0;
@@ -948,6 +925,16 @@ extern "C" int ether_learn_create(ether_ctx *h, const ether_learn_desc *d, ether
     Ctx &c = h->c;
     if (d->patch != 4 || d->hidden != 128)
         return lfail(ETHER_ERR_UNSUPPORTED, "learned proposal: patch 4 and hidden width 128 only");
+    if (c.model == ETHER_MODEL_XYZ) {
+        learn::XyzLearn *x = nullptr;
+        const int rc = learn::xyz_create(h, d, &x);
+        if (rc) return rc;
+        ether_learn *l = new ether_learn();
+        l->ctx = h;
+        l->xyz = x;
+        *out = l;
+        return ETHER_OK;
+    }
     // c.L is set once the lattice is verified to be the periodic simple-cubic one (whose
     // storage is the checkerboard split the kernels address arithmetically)
     if (c.model != ETHER_MODEL_ISING || c.L[0] <= 0 || c.nsp != 1 || c.nsh != 1 || c.zeeman)
@@ -1020,6 +1007,11 @@ extern "C" int ether_learn_create(ether_ctx *h, const ether_learn_desc *d, ether
 
 extern "C" int ether_learn_destroy(ether_learn *l) {
     if (!l) return ETHER_OK;
+    if (l->xyz) {
+        learn::xyz_destroy(l->xyz);
+        delete l;
+        return ETHER_OK;
+    }
     if (l->ctx) cudaStreamSynchronize(l->ctx->c.stream);
     void *ptrs[] = {l->p, l->pq, l->g, l->m, l->v, l->img, l->X, l->Y, l->Xb, l->Yb, l->H1, l->H2,
                     l->Z, l->dZ, l->dH1, l->dH2, l->loss, l->lstep, l->k4, l->betaJf, l->TB,
@@ -1037,6 +1029,7 @@ extern "C" int ether_learn_collect(ether_learn *l, int32_t per_replica) {
     if (per_replica < 1) return lfail(ETHER_ERR_ARG, "samples per replica must be positive");
     Ctx &c = l->ctx->c;
     if (!c.beta_set) return lfail(ETHER_ERR_STATE, "beta not set");
+    if (l->xyz) return learn::xyz_collect(l->xyz, per_replica);
     int rc = refresh_tables(*l);
     if (rc) return rc;
     const long long total = (long long)l->R * per_replica;
@@ -1055,6 +1048,7 @@ extern "C" int ether_learn_collect(ether_learn *l, int32_t per_replica) {
 extern "C" int ether_learn_train(ether_learn *l, int32_t steps, int32_t batch, float lr, double *loss_out) {
     if (!l) return lfail(ETHER_ERR_ARG, "null handle");
     if (steps < 0 || batch < 1 || batch > 65536 || !(lr > 0.f)) return lfail(ETHER_ERR_ARG, "bad training arguments");
+    if (l->xyz) return learn::xyz_train(l->xyz, steps, batch, lr, loss_out);
     if (l->n == 0) return lfail(ETHER_ERR_STATE, "no training samples (ether_learn_collect)");
     int rc = ensure_batch(*l, batch);
     if (rc) return rc;
@@ -1088,6 +1082,7 @@ extern "C" int ether_learn_sweep(ether_learn *l, int32_t nsweeps) {
     if (nsweeps < 0) return lfail(ETHER_ERR_ARG, "negative sweep count");
     Ctx &c = l->ctx->c;
     if (!c.beta_set) return lfail(ETHER_ERR_STATE, "beta not set");
+    if (l->xyz) return learn::xyz_sweep(l->xyz, nsweeps);
     int rc = refresh_tables(*l);
     if (rc) return rc;
     if (l->dump_on && !l->dump)
@@ -1117,6 +1112,7 @@ extern "C" int ether_learn_record_series(ether_learn *l, int32_t nsteps, int32_t
         return lfail(ETHER_ERR_ARG, "need nsteps >= 1 and at least one sweep per step");
     Ctx &c = l->ctx->c;
     if (!c.beta_set) return lfail(ETHER_ERR_STATE, "beta not set");
+    if (l->xyz) return learn::xyz_record_series(l->xyz, nsteps, plain_per_step, learned_per_step, absM);
     int rc = refresh_tables(*l);
     if (rc) return rc;
     const size_t bytes = sizeof(double) * (size_t)nsteps * l->R;
@@ -1149,6 +1145,7 @@ extern "C" int ether_learn_record_series(ether_learn *l, int32_t nsteps, int32_t
 
 extern "C" int ether_learn_get_accepts(ether_learn *l, uint64_t *accepted) {
     if (!l || !accepted) return lfail(ETHER_ERR_ARG, "null argument");
+    if (l->xyz) return learn::xyz_get_accepts(l->xyz, accepted);
     LCUDA(cudaMemcpyAsync(accepted, l->acc, l->R * sizeof(uint64_t), cudaMemcpyDeviceToHost, l->ctx->c.stream));
     LCUDA(cudaStreamSynchronize(l->ctx->c.stream));
     return read_err(*l);
@@ -1156,12 +1153,14 @@ extern "C" int ether_learn_get_accepts(ether_learn *l, uint64_t *accepted) {
 
 extern "C" int ether_learn_set_dump(ether_learn *l, int32_t on) {
     if (!l) return lfail(ETHER_ERR_ARG, "null handle");
+    if (l->xyz) learn::xyz_set_dump(l->xyz, on != 0);
     l->dump_on = on != 0;
     return ETHER_OK;
 }
 
 extern "C" int ether_learn_get_dump(ether_learn *l, float *logits) {
     if (!l || !logits) return lfail(ETHER_ERR_ARG, "null argument");
+    if (l->xyz) return learn::xyz_get_dump(l->xyz, logits);
     if (!l->dump) return lfail(ETHER_ERR_STATE, "no logits recorded (ether_learn_set_dump, then a sweep)");
     LCUDA(cudaMemcpyAsync(logits, l->dump, 2 * (size_t)l->R * l->Pc * NO * sizeof(float),
                           cudaMemcpyDeviceToHost, l->ctx->c.stream));
@@ -1171,6 +1170,7 @@ extern "C" int ether_learn_get_dump(ether_learn *l, float *logits) {
 
 extern "C" int ether_learn_get_params(ether_learn *l, float *params) {
     if (!l || !params) return lfail(ETHER_ERR_ARG, "null argument");
+    if (l->xyz) return learn::xyz_get_params(l->xyz, params);
     LCUDA(cudaMemcpyAsync(params, l->p, NPARAM * sizeof(float), cudaMemcpyDeviceToHost, l->ctx->c.stream));
     LCUDA(cudaStreamSynchronize(l->ctx->c.stream));
     return ETHER_OK;
@@ -1178,6 +1178,7 @@ extern "C" int ether_learn_get_params(ether_learn *l, float *params) {
 
 extern "C" int ether_learn_set_params(ether_learn *l, const float *params) {
     if (!l || !params) return lfail(ETHER_ERR_ARG, "null argument");
+    if (l->xyz) return learn::xyz_set_params(l->xyz, params);
     for (int i = 0; i < NPARAM; ++i)
         if (!std::isfinite(params[i])) return lfail(ETHER_ERR_ARG, "non-finite parameter " + std::to_string(i));
     cudaStream_t st = l->ctx->c.stream;
@@ -1195,6 +1196,7 @@ extern "C" int ether_learn_loss_grad(ether_learn *l, const float *x, const uint3
                                      double *loss, float *grad) {
     if (!l || !x || !y || !grad) return lfail(ETHER_ERR_ARG, "null argument");
     if (B < 1 || B > 65536) return lfail(ETHER_ERR_ARG, "batch out of range");
+    if (l->xyz) return lfail(ETHER_ERR_UNSUPPORTED, "XYZ learner: targets are spin components (ether_learn_loss_grad_f)");
     int rc = ensure_batch(*l, B);
     if (rc) return rc;
     cudaStream_t st = l->ctx->c.stream;
@@ -1217,6 +1219,7 @@ extern "C" int ether_learn_loss_grad(ether_learn *l, const float *x, const uint3
 extern "C" int ether_learn_forward(ether_learn *l, const float *x, int32_t B, float *logits) {
     if (!l || !x || !logits) return lfail(ETHER_ERR_ARG, "null argument");
     if (B < 1 || B > (1 << 22)) return lfail(ETHER_ERR_ARG, "batch out of range");
+    if (l->xyz) return learn::xyz_forward(l->xyz, x, B, logits);
     cudaStream_t st = l->ctx->c.stream;
     std::vector<__nv_bfloat16> xb((size_t)B * NI);
     for (size_t i = 0; i < xb.size(); ++i) xb[i] = __float2bfloat16_rn(x[i]);
@@ -1248,6 +1251,7 @@ extern "C" int ether_learn_forward(ether_learn *l, const float *x, int32_t B, fl
 
 extern "C" int ether_learn_get_info(ether_learn *l, ether_learn_info *info) {
     if (!l || !info) return lfail(ETHER_ERR_ARG, "null argument");
+    if (l->xyz) return learn::xyz_info(l->xyz, info);
     if (l->timed) {
         float ms = 0.f;
         LCUDA(cudaEventSynchronize(l->e1));
@@ -1267,5 +1271,28 @@ extern "C" int ether_learn_get_info(ether_learn *l, ether_learn_info *info) {
     info->kernel_launches = l->launches;
     info->last_sweep_ms = l->sweep_ms;
     info->last_train_ms = l->train_ms;
+    return ETHER_OK;
+}
+
+extern "C" int ether_learn_loss_grad_f(ether_learn *l, const float *x, const float *y, int32_t B, double *loss,
+                                       float *grad) {
+    if (!l || !x || !y || !grad) return lfail(ETHER_ERR_ARG, "null argument");
+    if (B < 1 || B > 65536) return lfail(ETHER_ERR_ARG, "batch out of range");
+    if (l->xyz) return learn::xyz_loss_grad(l->xyz, x, y, B, loss, grad);
+    // Ising: targets 0 / 1 per output, packed as the A-site bits
+    std::vector<uint32_t> bits((size_t)B, 0u);
+    for (int b = 0; b < B; ++b)
+        for (int o = 0; o < NO; ++o)
+            if (y[(size_t)b * NO + o] > 0.5f) bits[b] |= 1u << o;
+    return ether_learn_loss_grad(l, x, bits.data(), B, loss, grad);
+}
+
+extern "C" int ether_learn_get_shape(ether_learn *l, int32_t *n_inputs, int32_t *n_outputs, int32_t *n_params) {
+    if (!l || !n_inputs || !n_outputs || !n_params) return lfail(ETHER_ERR_ARG, "null argument");
+    int ni = NI, no = NO, np = NPARAM;
+    if (l->xyz) learn::xyz_shape(&ni, &no, &np);
+    *n_inputs = ni;
+    *n_outputs = no;
+    *n_params = np;
     return ETHER_OK;
 }

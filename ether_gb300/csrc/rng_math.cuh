@@ -113,6 +113,50 @@ ETHER_HD float expf_neg(float x) {
     return tiny ? 0x1p-126f : p * bits_f((uint32_t)((int)n + 127) << 23);
 }
 
+// log x for a positive normal x: x = m 2^e with m in [sqrt(1/2), sqrt(2)), log m = 2 atanh(s),
+// s = (m - 1)/(m + 1), series through s^9 (|s| < 0.172: truncation < 1e-9).
+ETHER_HD float logf_own(float x) {
+#if defined(__CUDA_ARCH__)
+    uint32_t u = __float_as_uint(x);
+#else
+    uint32_t u;
+    __builtin_memcpy(&u, &x, 4);
+#endif
+    int e = (int)((u >> 23) & 0xFFu) - 127;
+    float m = bits_f((u & 0x007FFFFFu) | 0x3F800000u);
+    if (m > 1.41421356f) {
+        m = m * 0.5f;
+        e += 1;
+    }
+    const float s = (m - 1.0f) / (m + 1.0f);
+    const float s2 = s * s;
+    float p = 0.111111111f;
+    p = fmaf(p, s2, 0.142857143f);
+    p = fmaf(p, s2, 0.2f);
+    p = fmaf(p, s2, 0.333333333f);
+    p = fmaf(p, s2, 1.0f);
+    const float lm = 2.0f * (s * p);
+    return fmaf((float)e, 0.693147182f, lm);
+}
+
+// log(1 - y) for y in [0, 1) without cancellation: for y < 1/2, 2 atanh(s) with
+// s = -y / (2 - y) (|s| <= 1/3, series through s^15: truncation < 1e-9); else the log of
+// 1 - y, which is exact there.
+ETHER_HD float log1m_own(float y) {
+    if (y >= 0.5f) return logf_own(1.0f - y);
+    const float s = -y / (2.0f - y);
+    const float s2 = s * s;
+    float p = 0.0666666667f;
+    p = fmaf(p, s2, 0.0769230769f);
+    p = fmaf(p, s2, 0.0909090909f);
+    p = fmaf(p, s2, 0.111111111f);
+    p = fmaf(p, s2, 0.142857143f);
+    p = fmaf(p, s2, 0.2f);
+    p = fmaf(p, s2, 0.333333333f);
+    p = fmaf(p, s2, 1.0f);
+    return 2.0f * (s * p);
+}
+
 // sin and cos for |x| <= 4: reduction by pi/2 (two-part constant), Taylor polynomials on
 // |r| <= pi/4 (sine through r^9, cosine through r^8), quadrant swap.
 ETHER_HD void sincos_own(float x, float *s, float *c) {

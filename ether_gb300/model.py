@@ -395,8 +395,10 @@ N_LEARN_PARAMS = 128 * 128 + 128 + 128 * 128 + 128 + 32 * 128 + 32
 
 
 class Learned:
-    """ether_learn: the learned 4^3-patch proposal of a simple-cubic Ising Sweep, accepted by
-    exact Metropolis-Hastings (the plain sweep stays the fallback; interleave the two)."""
+    """ether_learn: the learned 4^3-patch proposal of a simple-cubic Ising or Heisenberg (XYZ)
+    Sweep, accepted by exact Metropolis-Hastings (the plain sweep stays the fallback;
+    interleave the two).  n_in, n_out, n_params: the network's widths (Ising 128, 32, 37152;
+    XYZ 304, 96 von Mises-Fisher parameters, 67936)."""
 
     def __init__(self, sweep, seed=7, capacity=1 << 20):
         self.lib = abi.load()
@@ -409,6 +411,9 @@ class Learned:
         h_ = C.c_void_p()
         abi.check(self.lib.ether_learn_create(sweep.h, C.byref(d), C.byref(h_)))
         self.h = h_
+        ni, no, npar = C.c_int32(0), C.c_int32(0), C.c_int32(0)
+        abi.check(self.lib.ether_learn_get_shape(self.h, C.byref(ni), C.byref(no), C.byref(npar)))
+        self.n_in, self.n_out, self.n_params = ni.value, no.value, npar.value
 
     def close(self):
         if getattr(self, "h", None):
@@ -445,7 +450,7 @@ class Learned:
         return out
 
     def params(self):
-        p = np.zeros(N_LEARN_PARAMS, dtype=np.float32)
+        p = np.zeros(self.n_params, dtype=np.float32)
         abi.check(self.lib.ether_learn_get_params(self.h, p.ctypes.data_as(C.POINTER(C.c_float))))
         return p
 
@@ -454,18 +459,27 @@ class Learned:
         abi.check(self.lib.ether_learn_set_params(self.h, p.ctypes.data_as(C.POINTER(C.c_float))))
 
     def loss_grad(self, x, y):
-        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 128)
-        y = np.ascontiguousarray(y, dtype=np.uint32)
-        g = np.zeros(N_LEARN_PARAMS, dtype=np.float32)
+        """Mean training loss and its gradient on inputs x (B, n_in); y: Ising colour-0 bits
+        (B,) as unsigned integers, or float targets (B, n_out) (XYZ: spin components)."""
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, self.n_in)
+        g = np.zeros(self.n_params, dtype=np.float32)
         loss = C.c_double(0.0)
-        abi.check(self.lib.ether_learn_loss_grad(
-            self.h, x.ctypes.data_as(C.POINTER(C.c_float)), y.ctypes.data_as(abi.PU32), x.shape[0],
-            C.byref(loss), g.ctypes.data_as(C.POINTER(C.c_float))))
+        y = np.asarray(y)
+        if np.issubdtype(y.dtype, np.floating):
+            y = np.ascontiguousarray(y, dtype=np.float32).reshape(-1, self.n_out)
+            abi.check(self.lib.ether_learn_loss_grad_f(
+                self.h, x.ctypes.data_as(C.POINTER(C.c_float)), y.ctypes.data_as(C.POINTER(C.c_float)),
+                x.shape[0], C.byref(loss), g.ctypes.data_as(C.POINTER(C.c_float))))
+        else:
+            y = np.ascontiguousarray(y, dtype=np.uint32)
+            abi.check(self.lib.ether_learn_loss_grad(
+                self.h, x.ctypes.data_as(C.POINTER(C.c_float)), y.ctypes.data_as(abi.PU32), x.shape[0],
+                C.byref(loss), g.ctypes.data_as(C.POINTER(C.c_float))))
         return loss.value, g
 
     def forward(self, x):
-        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 128)
-        z = np.zeros((x.shape[0], 32), dtype=np.float32)
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, self.n_in)
+        z = np.zeros((x.shape[0], self.n_out), dtype=np.float32)
         abi.check(self.lib.ether_learn_forward(self.h, x.ctypes.data_as(C.POINTER(C.c_float)),
                                                x.shape[0], z.ctypes.data_as(C.POINTER(C.c_float))))
         return z
@@ -475,7 +489,7 @@ class Learned:
 
     def dump(self):
         i = self.info()
-        z = np.zeros((2, self.sweep.R, i.patches_per_class, 32), dtype=np.float32)
+        z = np.zeros((2, self.sweep.R, i.patches_per_class, self.n_out), dtype=np.float32)
         abi.check(self.lib.ether_learn_get_dump(self.h, z.ctypes.data_as(C.POINTER(C.c_float))))
         return z
 

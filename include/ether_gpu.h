@@ -310,8 +310,14 @@ int ether_batch_get_stream(ether_batch *batch, void **stream);
 /* ------------------------------------------------------- learned patch proposal ---- */
 /* No counterpart in the reference (which only has single-site moves, src/Metropolis.f90);
  * its target distribution is kept exactly: every learned move is accepted or rejected by
- * Metropolis-Hastings against the reference's Ising energy.  Simple-cubic Ising contexts with
- * one species, one shell, no Zeeman term and extents that are multiples of 8.
+ * Metropolis-Hastings against the reference's energy.  Simple-cubic Ising contexts with one
+ * species, one shell, no Zeeman term, or simple-cubic XYZ contexts with one species, one
+ * shell, Marsaglia proposals and no Zeeman or SIA term; extents multiples of 8.
+ * XYZ: the network (96 boundary spins x 3 components + beta (Jxx, Jyy, Jzz), padded to 304
+ * -> 128 -> 128 -> 96, BF16 weights, CUDA cores) gives each colour-0 site a von Mises-Fisher
+ * parameter m (3 outputs); the colour-1 spins are drawn from their exact heat-bath vMF
+ * conditionals; params, forward outputs and dumps have the widths ether_learn_get_shape
+ * returns.  Ising:
  * A learned sweep tiles each replica with 4^3 patches (a fresh random offset per sweep) and
  * updates the two patch classes in turn: the network (96 boundary spins + 4 beta J -> 128 ->
  * 128 -> 32, BF16 weights, tensor cores) proposes the patch's 32 colour-0 spins, the 32
@@ -351,8 +357,15 @@ int ether_learn_set_params(ether_learn *learn, const float *params);
  * loss = mean BCE, grad(37152) = its gradient (no update). */
 int ether_learn_loss_grad(ether_learn *learn, const float *x, const uint32_t *y, int32_t B,
                           double *loss, float *grad);
-/* The inference network (tensor cores) on x(128, B): logits(32, B). */
+/* The same with targets as floats y(n_outputs, B): Ising 0 / 1 per colour-0 site, XYZ the
+ * colour-0 spins' components (loss = mean von Mises-Fisher negative log density). */
+int ether_learn_loss_grad_f(ether_learn *learn, const float *x, const float *y, int32_t B,
+                            double *loss, float *grad);
+/* The inference network on x(n_inputs, B): outputs(n_outputs, B) (Ising: logits, tensor
+ * cores; XYZ: the vMF parameters with the output bias). */
 int ether_learn_forward(ether_learn *learn, const float *x, int32_t B, float *logits);
+/* Widths of the network: inputs, outputs, parameters (Ising 128, 32, 37152). */
+int ether_learn_get_shape(ether_learn *learn, int32_t *n_inputs, int32_t *n_outputs, int32_t *n_params);
 /* Record the logits of the last sweep of the next ether_learn_sweep; get_dump returns them
  * as logits(32, Pc, R, 2) (class, replica, patch of the class). */
 int ether_learn_set_dump(ether_learn *learn, int32_t on);

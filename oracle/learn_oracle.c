@@ -514,3 +514,346 @@ void orc_patch_chain(const int L[3], double betaJ, long nsteps, long nequil, int
     out[4] = prop > 0 ? (double)acc / prop : 0.0;
     free(sp);
 }
+
+/* ============================================== the Heisenberg (XYZ) learned proposal ==== */
+/* Restatement of the XYZ learner (the product's k_learn_xyz.cu).  Target: exp(-beta E),
+ * E = sum over bonds of S_i . (J o S_j), J = (Jxx, Jyy, Jzz) (src/Hamiltonian.f90:57-105).
+ * Patch tiling, offsets, canonical frame and A/B numbering as the Ising learner above.
+ *   * network input x[304]: boundary site i (face order) at 3i .. 3i+2 (BF16-rounded
+ *     components), x[288..290] = bf16(beta Jxx), bf16(beta Jyy), bf16(beta Jzz), rest 0;
+ *     MLP 304 -> 128 -> 128 -> 96 (ReLU, BF16 weights and hidden activations);
+ *     m_k = outputs 3k .. 3k+2 + bias: the von Mises-Fisher parameter of A-site k;
+ *   * A-site k ~ vMF(m_k) from draw(pidx, t, stream, 4 | (32 + k) << 16): u01(.x), upm1(.y);
+ *     B-site k ~ vMF(-beta J o g_k), g_k = sum of its six neighbours (q order), from .z, .w;
+ *     |m| < 1e-3 is the uniform distribution (sampler and density);
+ *   * log alpha = sum_k [(s_A,new + s_B,new) - (s_A,old + s_B,old)], summed over k = 0..31 by
+ *     the xor butterfly (offsets 16, 8, 4, 2, 1), with s_A = (-beta) (x_A . (J o b_A)) -
+ *     log q_A(x_A), b_A the sum of A-site k's boundary neighbours, and s_B = m_B . y_B -
+ *     log q_B(y_B); accept if log alpha >= 0 or u01(draw(pidx, t, stream, 4 | 16 << 16).x) <
+ *     exp(log alpha).  FP32 throughout, the operations in the product's order. */
+enum { XNI = 304, XNO = 96 };
+#define XOFF_W1 0
+#define XOFF_B1 (XOFF_W1 + NH * XNI)
+#define XOFF_W2 (XOFF_B1 + NH)
+#define XOFF_B2 (XOFF_W2 + NH * NH)
+#define XOFF_W3 (XOFF_B2 + NH)
+#define XOFF_B3 (XOFF_W3 + XNO * NH)
+#define XNPARAM (XOFF_B3 + XNO)
+
+int orc_xmlp_n_params(void) { return XNPARAM; }
+
+static void xforward1(const float *p, const float *x, int quant, double *h1, double *h2, double *z) {
+    for (int o = 0; o < NH; ++o) {
+        double s = 0.0;
+        for (int i = 0; i < XNI; ++i) s += wq(p, XOFF_W1 + o * XNI + i, quant) * (double)x[i];
+        s += p[XOFF_B1 + o];
+        s = s > 0.0 ? s : 0.0;
+        h1[o] = quant ? (double)bf16r((float)s) : s;
+    }
+    for (int o = 0; o < NH; ++o) {
+        double s = 0.0;
+        for (int i = 0; i < NH; ++i) s += wq(p, XOFF_W2 + o * NH + i, quant) * h1[i];
+        s += p[XOFF_B2 + o];
+        s = s > 0.0 ? s : 0.0;
+        h2[o] = quant ? (double)bf16r((float)s) : s;
+    }
+    for (int o = 0; o < XNO; ++o) {
+        double s = 0.0;
+        for (int i = 0; i < NH; ++i) s += wq(p, XOFF_W3 + o * NH + i, quant) * h2[i];
+        z[o] = s + p[XOFF_B3 + o];
+    }
+}
+
+void orc_xmlp_forward(const float *params, const float *x, int B, int quant, float *out) {
+    double h1[NH], h2[NH], z[XNO];
+    for (int b = 0; b < B; ++b) {
+        xforward1(params, x + (size_t)b * XNI, quant, h1, h2, z);
+        for (int o = 0; o < XNO; ++o) out[(size_t)b * XNO + o] = (float)z[o];
+    }
+}
+
+/* log C(kappa) = log(kappa / (4 pi sinh kappa)) and A(kappa) = (1/kappa - coth kappa) / kappa */
+static void vmf_terms(double kap, double *logc, double *A) {
+    if (kap < 1e-4) {
+        *logc = -log(4.0 * M_PI) - kap * kap / 6.0;
+        *A = -1.0 / 3.0 + kap * kap / 45.0;
+    } else {
+        *logc = log(kap) - kap - log(-expm1(-2.0 * kap)) - log(2.0 * M_PI);
+        *A = (1.0 / kap - 1.0 / tanh(kap)) / kap;
+    }
+}
+
+/* Mean over the batch of sum_k -log vMF(y_k; m_k) (y: 96 spin components per row); grad =
+ * d loss / d params (straight-through for the BF16 rounding). */
+double orc_xmlp_loss_grad(const float *p, const float *x, const float *y, int B, int quant, double *grad) {
+    double h1[NH], h2[NH], z[XNO], dz[XNO], dh2[NH], dh1[NH];
+    double loss = 0.0;
+    memset(grad, 0, sizeof(double) * XNPARAM);
+    for (int b = 0; b < B; ++b) {
+        const float *xb = x + (size_t)b * XNI;
+        const float *yb = y + (size_t)b * XNO;
+        xforward1(p, xb, quant, h1, h2, z);
+        for (int k = 0; k < 32; ++k) {
+            const double mx = z[3 * k], my = z[3 * k + 1], mz = z[3 * k + 2];
+            const double kap = sqrt(mx * mx + my * my + mz * mz);
+            double logc, A;
+            vmf_terms(kap, &logc, &A);
+            loss += -(logc + mx * yb[3 * k] + my * yb[3 * k + 1] + mz * yb[3 * k + 2]);
+            dz[3 * k] = -(yb[3 * k] + A * mx) / B;
+            dz[3 * k + 1] = -(yb[3 * k + 1] + A * my) / B;
+            dz[3 * k + 2] = -(yb[3 * k + 2] + A * mz) / B;
+        }
+        for (int i = 0; i < NH; ++i) dh2[i] = 0.0;
+        for (int o = 0; o < XNO; ++o) {
+            grad[XOFF_B3 + o] += dz[o];
+            for (int i = 0; i < NH; ++i) {
+                grad[XOFF_W3 + o * NH + i] += dz[o] * h2[i];
+                dh2[i] += dz[o] * wq(p, XOFF_W3 + o * NH + i, quant);
+            }
+        }
+        for (int i = 0; i < NH; ++i) dh2[i] = h2[i] > 0.0 ? dh2[i] : 0.0;
+        for (int i = 0; i < NH; ++i) dh1[i] = 0.0;
+        for (int o = 0; o < NH; ++o) {
+            grad[XOFF_B2 + o] += dh2[o];
+            for (int i = 0; i < NH; ++i) {
+                grad[XOFF_W2 + o * NH + i] += dh2[o] * h1[i];
+                dh1[i] += dh2[o] * wq(p, XOFF_W2 + o * NH + i, quant);
+            }
+        }
+        for (int i = 0; i < NH; ++i) dh1[i] = h1[i] > 0.0 ? dh1[i] : 0.0;
+        for (int o = 0; o < NH; ++o) {
+            grad[XOFF_B1 + o] += dh1[o];
+            for (int i = 0; i < XNI; ++i) grad[XOFF_W1 + o * XNI + i] += dh1[o] * (double)xb[i];
+        }
+    }
+    return loss / B;
+}
+
+static float xu01(uint32_t u) { return (float)(u >> 8) * 0x1p-24f; }
+static float xupm1(uint32_t u) { return (float)(u >> 8) * 0x1p-23f - 1.0f; }
+
+static float xdot3(float ax, float ay, float az, float bx, float by, float bz) {
+    float d = ax * bx;
+    d = fmaf(ay, by, d);
+    return fmaf(az, bz, d);
+}
+
+/* log(1 - y), y in [0, 1): 2 atanh(-y / (2 - y)) through s^15 below 1/2, else log(1 - y) */
+static float xlog1m(float y) {
+    if (y >= 0.5f) return orc_logf_own(1.0f - y);
+    const float s = -y / (2.0f - y);
+    const float s2 = s * s;
+    float p = 0.0666666667f;
+    p = fmaf(p, s2, 0.0769230769f);
+    p = fmaf(p, s2, 0.0909090909f);
+    p = fmaf(p, s2, 0.111111111f);
+    p = fmaf(p, s2, 0.142857143f);
+    p = fmaf(p, s2, 0.2f);
+    p = fmaf(p, s2, 0.333333333f);
+    p = fmaf(p, s2, 1.0f);
+    return 2.0f * (s * p);
+}
+
+/* 1 - e^{-2 kappa}: series of 1 - e^{-y} through y^8 for y = 2 kappa < 1/2 */
+static float xoneminus(float kappa) {
+    const float y = 2.0f * kappa;
+    if (y >= 0.5f) return 1.0f - orc_expf_neg(-y);
+    float p = 2.48015873e-5f;
+    p = fmaf(p, y, -1.98412698e-4f);
+    p = fmaf(p, y, 1.38888889e-3f);
+    p = fmaf(p, y, -8.33333333e-3f);
+    p = fmaf(p, y, 4.16666667e-2f);
+    p = fmaf(p, y, -1.66666667e-1f);
+    p = fmaf(p, y, 0.5f);
+    p = fmaf(p, y, -1.0f);
+    return -(y * p);
+}
+
+#define XKAPPA_MIN 1e-3f
+#define XLOG4PI 2.53102425f
+#define XLOG2PI 1.83787707f
+
+/* vMF(m): kappa = |m|, rk = 1 / kappa, c = log(kappa / (1 - e^{-2 kappa})) - log 2 pi; the
+ * uniform distribution below XKAPPA_MIN.  log density at x = c + (m . x - kappa). */
+typedef struct {
+    float mx, my, mz, kappa, rk, c;
+    int uni;
+} Vmf;
+
+static Vmf vmf_prep(float mx, float my, float mz) {
+    Vmf V;
+    V.mx = mx;
+    V.my = my;
+    V.mz = mz;
+    V.kappa = sqrtf(xdot3(mx, my, mz, mx, my, mz));
+    V.uni = V.kappa < XKAPPA_MIN;
+    V.rk = V.uni ? 0.0f : 1.0f / V.kappa;
+    V.c = V.uni ? -XLOG4PI : orc_logf_own(V.kappa * (1.0f / xoneminus(V.kappa))) - XLOG2PI;
+    return V;
+}
+
+static float vmf_lp(const Vmf *V, float x, float y, float z) {
+    return V->uni ? -XLOG4PI : V->c + (xdot3(V->mx, V->my, V->mz, x, y, z) - V->kappa);
+}
+
+float orc_vmf_logpdf(float mx, float my, float mz, float x, float y, float z) {
+    const Vmf V = vmf_prep(mx, my, mz);
+    return vmf_lp(&V, x, y, z);
+}
+
+/* Wood's sampler: 1 - w = -log(1 - (1 - u)(1 - e^{-2 kappa})) / kappa, azimuth pi v */
+static void vmf_draw(const Vmf *V, float u, float v, float out[3]) {
+    float ux = 0.0f, uy = 0.0f, uz = 1.0f, om;
+    if (V->uni) {
+        om = 2.0f * (1.0f - u);
+    } else {
+        ux = V->mx * V->rk;
+        uy = V->my * V->rk;
+        uz = V->mz * V->rk;
+        om = -xlog1m((1.0f - u) * xoneminus(V->kappa)) * V->rk;
+    }
+    om = fminf(fmaxf(om, 0.0f), 2.0f);
+    const float w = 1.0f - om;
+    const float r = sqrtf(om * (2.0f - om));
+    float e1x, e1y, e1z;
+    if (fabsf(uz) < 0.9f) {
+        const float rn = 1.0f / sqrtf(xdot3(uy, ux, 0.0f, uy, ux, 0.0f));
+        e1x = -uy * rn;
+        e1y = ux * rn;
+        e1z = 0.0f;
+    } else {
+        const float rn = 1.0f / sqrtf(xdot3(0.0f, uz, uy, 0.0f, uz, uy));
+        e1x = 0.0f;
+        e1y = uz * rn;
+        e1z = -uy * rn;
+    }
+    const float e2x = uy * e1z - uz * e1y, e2y = uz * e1x - ux * e1z, e2z = ux * e1y - uy * e1x;
+    float sn, cs;
+    orc_sincosf(3.14159265f * v, &sn, &cs);
+    const float px = cs * e1x + sn * e2x, py = cs * e1y + sn * e2y, pz = cs * e1z + sn * e2z;
+    const float x = w * ux + r * px, y = w * uy + r * py, z = w * uz + r * pz;
+    const float rnn = 1.0f / sqrtf(xdot3(x, y, z, x, y, z));
+    out[0] = x * rnn;
+    out[1] = y * rnn;
+    out[2] = z * rnn;
+}
+
+void orc_vmf_sample(float mx, float my, float mz, float u, float v, float out[3]) {
+    const Vmf V = vmf_prep(mx, my, mz);
+    vmf_draw(&V, u, v, out);
+}
+
+static void bnd_coords(int i, int *a, int *b, int *c) {
+    const int f = i >> 4, u = i & 3, v = (i >> 2) & 3, e = (f & 1) ? 4 : -1;
+    if (f < 2) { *a = e; *b = u; *c = v; }
+    else if (f < 4) { *a = u; *b = e; *c = v; }
+    else { *a = u; *b = v; *c = e; }
+}
+
+/* One XYZ patch update; sp4: one replica's spins, 4 floats per storage index (x, y, z, phi). */
+static int xpatch_update(float *sp4, const int L[3], const int off[3], int pi, int pj, int pk, uint32_t pidx,
+                         const float *m96, float beta, const float J[3], uint32_t seed, uint32_t stream,
+                         uint32_t t) {
+    const int o[3] = {4 * pi + off[0], 4 * pj + off[1], 4 * pk + off[2]};
+    const int par = (off[0] + off[1] + off[2]) & 1;
+    const float nbeta = -beta;
+    float nA[32][3], oA[32][3], nB[32][3], d[32];
+    long ia[32], ib[32];
+    float sa_new[32], sa_old[32];
+    for (int k = 0; k < 32; ++k) {
+        ia[k] = site_of(L, o, par, g_A[k][0], g_A[k][1], g_A[k][2]);
+        for (int c = 0; c < 3; ++c) oA[k][c] = sp4[4 * ia[k] + c];
+        const float mx = m96[3 * k], my = m96[3 * k + 1], mz = m96[3 * k + 2];
+        float bx = 0.0f, by = 0.0f, bz = 0.0f;
+        for (int n = 0; n < 3; ++n) {
+            const int bi = g_Ab[k][n];
+            if (bi < 0) continue;
+            int a, b, c;
+            bnd_coords(bi, &a, &b, &c);
+            const long s = site_of(L, o, par, a, b, c);
+            bx += sp4[4 * s];
+            by += sp4[4 * s + 1];
+            bz += sp4[4 * s + 2];
+        }
+        const float hx = J[0] * bx, hy = J[1] * by, hz = J[2] * bz;
+        uint32_t w[4];
+        draw4(pidx, t, stream, K_LEARN | ((32u + (uint32_t)k) << 16), seed, w);
+        const Vmf VA = vmf_prep(mx, my, mz);
+        vmf_draw(&VA, xu01(w[0]), xupm1(w[1]), nA[k]);
+        sa_new[k] = nbeta * xdot3(nA[k][0], nA[k][1], nA[k][2], hx, hy, hz) - vmf_lp(&VA, nA[k][0], nA[k][1], nA[k][2]);
+        sa_old[k] = nbeta * xdot3(oA[k][0], oA[k][1], oA[k][2], hx, hy, hz) - vmf_lp(&VA, oA[k][0], oA[k][1], oA[k][2]);
+    }
+    for (int k = 0; k < 32; ++k) {
+        ib[k] = site_of(L, o, par, g_B[k][0], g_B[k][1], g_B[k][2]);
+        const float yo[3] = {sp4[4 * ib[k]], sp4[4 * ib[k] + 1], sp4[4 * ib[k] + 2]};
+        float gn[3] = {0.0f, 0.0f, 0.0f}, go[3] = {0.0f, 0.0f, 0.0f};
+        for (int q = 0; q < 6; ++q) {
+            const int cd = g_Bn[k][q];
+            float sn[3], so[3];
+            if (cd >= 0) {
+                for (int c = 0; c < 3; ++c) {
+                    sn[c] = nA[cd][c];
+                    so[c] = oA[cd][c];
+                }
+            } else {
+                int a, b, c;
+                bnd_coords(-cd - 1, &a, &b, &c);
+                const long s = site_of(L, o, par, a, b, c);
+                for (int e = 0; e < 3; ++e) sn[e] = so[e] = sp4[4 * s + e];
+            }
+            for (int c = 0; c < 3; ++c) {
+                gn[c] += sn[c];
+                go[c] += so[c];
+            }
+        }
+        const float mbn[3] = {nbeta * (J[0] * gn[0]), nbeta * (J[1] * gn[1]), nbeta * (J[2] * gn[2])};
+        const float mbo[3] = {nbeta * (J[0] * go[0]), nbeta * (J[1] * go[1]), nbeta * (J[2] * go[2])};
+        uint32_t w[4];
+        draw4(pidx, t, stream, K_LEARN | ((32u + (uint32_t)k) << 16), seed, w);
+        const Vmf VBn = vmf_prep(mbn[0], mbn[1], mbn[2]), VBo = vmf_prep(mbo[0], mbo[1], mbo[2]);
+        vmf_draw(&VBn, xu01(w[2]), xupm1(w[3]), nB[k]);
+        const float sb_new = xdot3(mbn[0], mbn[1], mbn[2], nB[k][0], nB[k][1], nB[k][2]) -
+                             vmf_lp(&VBn, nB[k][0], nB[k][1], nB[k][2]);
+        const float sb_old = xdot3(mbo[0], mbo[1], mbo[2], yo[0], yo[1], yo[2]) - vmf_lp(&VBo, yo[0], yo[1], yo[2]);
+        d[k] = (sa_new[k] + sb_new) - (sa_old[k] + sb_old);
+    }
+    for (int off2 = 16; off2 >= 1; off2 >>= 1) {
+        float nd[32];
+        for (int l = 0; l < 32; ++l) nd[l] = d[l] + d[l ^ off2];
+        memcpy(d, nd, sizeof(nd));
+    }
+    const float la = d[0];
+    uint32_t w[4];
+    draw4(pidx, t, stream, K_LEARN | (16u << 16), seed, w);
+    const int acc = la >= 0.0f || xu01(w[0]) < orc_expf_neg(la);
+    if (acc)
+        for (int k = 0; k < 32; ++k)
+            for (int c = 0; c < 3; ++c) {
+                sp4[4 * ia[k] + c] = nA[k][c];
+                sp4[4 * ib[k] + c] = nB[k][c];
+            }
+    return acc;
+}
+
+/* One XYZ learned sweep of one replica (class 0 then class 1); mdump: [2][Pc][96] vMF
+ * parameters in the GPU's patch order.  Returns the number of accepted patches. */
+long orc_xpatch_sweep(float *sp4, const int L[3], float beta, const float J[3], const float *mdump,
+                      uint32_t seed, uint32_t stream, uint32_t t) {
+    geometry();
+    int off[3];
+    orc_patch_offsets(seed, stream, t, off);
+    const int P1 = L[0] / 4, P2 = L[1] / 4, P3 = L[2] / 4;
+    const long Pc = (long)P1 * P2 * P3 / 2;
+    long acc = 0;
+    for (int cls = 0; cls < 2; ++cls)
+        for (long q = 0; q < Pc; ++q) {
+            const int tt = (int)(q % (P1 / 2));
+            const long row = q / (P1 / 2);
+            const int j = (int)(row % P2), k = (int)(row / P2);
+            const int i = 2 * tt + ((cls + j + k) & 1);
+            const uint32_t pidx = (uint32_t)(i + P1 * (j + P2 * k));
+            acc += xpatch_update(sp4, L, off, i, j, k, pidx, mdump + ((size_t)cls * Pc + q) * XNO, beta, J, seed,
+                                 stream, t);
+        }
+    return acc;
+}

@@ -120,6 +120,15 @@ def lib():
         L.orc_patch_sweep.argtypes = [PU8, PI, C.c_double, PF, C.c_uint32, C.c_uint32, C.c_uint32]
         L.orc_patch_chain.argtypes = [PI, C.c_double, C.c_long, C.c_long, C.c_int, C.c_float,
                                       C.c_float, C.c_uint32, PD]
+        L.orc_xmlp_n_params.restype = C.c_int
+        L.orc_xmlp_forward.argtypes = [PF, PF, C.c_int, C.c_int, PF]
+        L.orc_xmlp_loss_grad.restype = C.c_double
+        L.orc_xmlp_loss_grad.argtypes = [PF, PF, PF, C.c_int, C.c_int, PD]
+        L.orc_vmf_logpdf.restype = C.c_float
+        L.orc_vmf_logpdf.argtypes = [C.c_float] * 6
+        L.orc_vmf_sample.argtypes = [C.c_float] * 5 + [PF]
+        L.orc_xpatch_sweep.restype = C.c_long
+        L.orc_xpatch_sweep.argtypes = [PF, PI, C.c_float, PF, PF, C.c_uint32, C.c_uint32, C.c_uint32]
         _lib = L
     return _lib
 
@@ -343,3 +352,48 @@ def patch_chain(L, betaJ, nsteps, nequil, use_patch, zscale=0.0, zbias=0.0, seed
     lib().orc_patch_chain(_i(LL), betaJ, nsteps, nequil, int(use_patch), zscale, zbias, seed,
                           _d(out))
     return {"e": out[0], "e_err": out[1], "m": out[2], "m_err": out[3], "accept": out[4]}
+
+
+# ----------------------------------------------------- the XYZ learned proposal ----
+def xmlp_n_params():
+    return lib().orc_xmlp_n_params()
+
+
+def xmlp_forward(params, x, quant=True):
+    """vMF parameters m (B, 96) of the XYZ network on inputs x (B, 304), output bias included."""
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    xx = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 304)
+    z = np.zeros((xx.shape[0], 96), dtype=np.float32)
+    lib().orc_xmlp_forward(_f(p), _f(xx), xx.shape[0], int(quant), _f(z))
+    return z
+
+
+def xmlp_loss_grad(params, x, y, quant=True):
+    """Mean vMF negative log density of the targets y (B, 96) and its FP64 gradient."""
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    xx = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 304)
+    yy = np.ascontiguousarray(y, dtype=np.float32).reshape(-1, 96)
+    g = np.zeros(p.size, dtype=np.float64)
+    loss = lib().orc_xmlp_loss_grad(_f(p), _f(xx), _f(yy), xx.shape[0], int(quant), _d(g))
+    return loss, g
+
+
+def vmf_logpdf(m, x):
+    return lib().orc_vmf_logpdf(*[float(v) for v in m], *[float(v) for v in x])
+
+
+def vmf_sample(m, u, v):
+    out = np.zeros(3, np.float32)
+    lib().orc_vmf_sample(*[float(c) for c in m], float(u), float(v), _f(out))
+    return out
+
+
+def xpatch_sweep(sp4, L, beta, J, mdump, seed, stream, t):
+    """One XYZ learned sweep (both classes) of one replica in place: sp4 (N, 4) float32 spins
+    in storage order; mdump (2, Pc, 96) the vMF parameters the GPU used.  Returns the
+    accepted patches."""
+    assert sp4.dtype == np.float32 and sp4.flags.c_contiguous
+    LL = np.ascontiguousarray(L, dtype=np.int32)
+    JJ = np.ascontiguousarray(J, dtype=np.float32)
+    m = np.ascontiguousarray(mdump, dtype=np.float32)
+    return lib().orc_xpatch_sweep(_f(sp4), _i(LL), float(beta), _f(JJ), _f(m), seed, stream, t)

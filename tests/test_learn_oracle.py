@@ -5,7 +5,10 @@
 * the patch geometry covers every boundary site exactly once;
 * exact Metropolis-Hastings: a chain that interleaves learned-patch sweeps (driven by
   stand-in proposals, good and bad) with Metropolis sweeps has the same <e> and <|m|> as
-  Metropolis alone -- the stationary distribution is unchanged whatever the proposal.
+  Metropolis alone -- the stationary distribution is unchanged whatever the proposal;
+* the XYZ learner: its MLP gradient (von Mises-Fisher loss) equals central finite
+  differences, and its vMF sampler and density agree (normalised density, the sampler's
+  mean cosine coth(kappa) - 1/kappa, unit vectors).
 """
 import numpy as np
 import pytest
@@ -117,3 +120,66 @@ def test_patch_chain_is_unbiased(zscale, zbias, kT):
     for key in ("e", "m"):
         err = np.hypot(a[key + "_err"], b[key + "_err"])
         assert abs(a[key] - b[key]) < 4.0 * err + 1e-9, (key, a, b)
+
+
+def _xyz_batch(rng, B):
+    """Boundary spins (unit vectors, BF16-rounded), beta J features, unit-vector targets."""
+    v = rng.normal(size=(B, 96, 3))
+    v /= np.linalg.norm(v, axis=2, keepdims=True)
+    x = np.zeros((B, 304), np.float32)
+    x[:, :288] = [[po.lib().orc_bf16_round(float(c)) for c in row] for row in v.reshape(B, 288)]
+    x[:, 288:291] = rng.uniform(-2.0, 2.0, size=(B, 1))
+    y = rng.normal(size=(B, 32, 3))
+    y /= np.linalg.norm(y, axis=2, keepdims=True)
+    return x, y.reshape(B, 96).astype(np.float32)
+
+
+def test_xyz_mlp_gradient_matches_finite_differences():
+    rng = np.random.default_rng(8)
+    n = po.xmlp_n_params()
+    assert n == 128 * 304 + 128 + 128 * 128 + 128 + 96 * 128 + 96
+    p = (rng.normal(size=n) * 0.1).astype(np.float32)
+    x, y = _xyz_batch(rng, 5)
+    loss, g = po.xmlp_loss_grad(p, x, y, quant=False)
+    assert np.isfinite(loss)
+    o = [0, 38912, 39040, 55424, 55552, 67840, 67936]
+    idx = []
+    for a, b in zip(o[:-1], o[1:]):
+        idx += list(a + np.argsort(np.abs(g[a:b]))[-4:])
+    h = 1e-3
+    for i in idx:
+        pp = p.copy()
+        pp[i] = p[i] + h
+        lp, _ = po.xmlp_loss_grad(pp, x, y, quant=False)
+        pp[i] = p[i] - h
+        lm, _ = po.xmlp_loss_grad(pp, x, y, quant=False)
+        fd = (lp - lm) / (float(np.float32(p[i] + h)) - float(np.float32(p[i] - h)))
+        assert fd == pytest.approx(g[i], rel=2e-3, abs=1e-7), i
+
+
+@pytest.mark.parametrize("kappa", [5e-4, 0.05, 0.7, 3.0, 40.0])
+def test_vmf_sampler_and_density_agree(kappa):
+    rng = np.random.default_rng(int(kappa * 1000) + 1)
+    mu = np.array([0.2, -0.6, 0.77])
+    mu /= np.linalg.norm(mu)
+    m = (mu * kappa).astype(np.float32)
+    n = 20000
+    u = rng.integers(0, 2 ** 24, n) / 2 ** 24
+    v = rng.integers(0, 2 ** 24, n) / 2 ** 23 - 1.0
+    xs = np.array([po.vmf_sample(m, a, b) for a, b in zip(u, v)], dtype=np.float64)
+    assert np.abs(np.linalg.norm(xs, axis=1) - 1.0).max() < 3e-7
+    c = xs @ mu
+    want = 0.0 if kappa < 1e-3 else 1.0 / np.tanh(kappa) - 1.0 / kappa
+    assert abs(c.mean() - want) < 5.0 * c.std() / np.sqrt(n) + 1e-6
+    # the FP32 density equals the FP64 formula, and (where uniform points see its mass)
+    # integrates to one
+    for x in xs[:200]:
+        dot = float(np.float32(m) @ x)
+        ref = -np.log(4 * np.pi) if kappa < 1e-3 else (
+            np.log(kappa) - np.log(2 * np.pi) - np.log(-np.expm1(-2 * kappa)) + dot - kappa)
+        assert po.vmf_logpdf(m, x) == pytest.approx(ref, abs=2e-5 * max(1.0, kappa))
+    if kappa <= 3.0:
+        g = rng.normal(size=(20000, 3))
+        g /= np.linalg.norm(g, axis=1, keepdims=True)
+        pdf = np.exp([po.vmf_logpdf(m, x) for x in g])
+        assert abs(4 * np.pi * pdf.mean() - 1.0) < 5.0 * 4 * np.pi * pdf.std() / np.sqrt(len(g)) + 1e-6
