@@ -697,7 +697,7 @@ def main():
     if args.model == "learned-heisenberg":
         if rank != 0:
             return 0
-        r = run_learned(args.L, R=64, train_steps=2000, n_plain=60000, n_learn=6000, heisenberg=True)
+        r = run_learned(args.L, R=64, train_steps=4000, n_plain=60000, n_learn=6000, heisenberg=True)
         print(json.dumps({"metric": "independent samples/s gain", "value": r["learned_only"]["gain_vs_plain"],
                           "unit": "x plain", "higher_is_better": True, "detail": r}))
         return 0

@@ -153,6 +153,7 @@ struct XPatchParams {
     const float *beta_slot_f;
     float jx, jy, jz;
     uint32_t seed;
+    RoundKeys K;         // Philox round keys of seed
 };
 
 __device__ __forceinline__ int xwrap(int x, int L) { return x >= L ? x - L : (x < 0 ? x + L : x); }
@@ -168,24 +169,27 @@ __device__ __forceinline__ long long xsite(const XPatchParams &P, int o0, int o1
 
 // Patch w of this pass: replica, patch number pidx, sweep counter t, origin and reflection
 // (the Ising learner's decoding: class cls of the offset tiling of replica r's sweep t).
+// A pass holds fewer than 2^31 patches and a class fewer than 2^31 per replica (32-bit
+// arithmetic).
 struct XPatch {
-    int r, o0, o1, o2, par;
-    long long q;
+    int r, o0, o1, o2, par, q;
     uint32_t pidx, t, stream;
 };
-__device__ __forceinline__ XPatch xdecode(const XPatchParams &P, long long w) {
+__device__ __forceinline__ XPatch xdecode(const XPatchParams &P, int w) {
     XPatch D;
-    D.r = P.r0 + (int)(w / P.Pc);
-    D.q = w - (long long)(D.r - P.r0) * P.Pc;
+    const int Pc = (int)P.Pc;
+    const int rr = w / Pc;
+    D.r = P.r0 + rr;
+    D.q = w - rr * Pc;
     const int half1 = P.P1 >> 1;
-    const int tt = (int)(D.q % half1);
-    const long long row = D.q / half1;
-    const int pj = (int)(row % P.P2), pk = (int)(row / P.P2);
+    const int row = D.q / half1;
+    const int tt = D.q - row * half1;
+    const int pk = row / P.P2, pj = row - pk * P.P2;
     const int pi = 2 * tt + ((P.cls + pj + pk) & 1);
     D.pidx = (uint32_t)(pi + P.P1 * (pj + P.P2 * pk));
     D.t = P.lstep[D.r];
     D.stream = P.stream_id[D.r];
-    const U4 ow = draw(0xFFFFFFFFu, D.t, D.stream, kLearn | (0xFFu << 8), P.seed);
+    const U4 ow = draw_rk(0xFFFFFFFFu, D.t, D.stream, kLearn | (0xFFu << 8), P.K);
     const int ox = (int)(ow.x & 3u), oy = (int)((ow.x >> 2) & 3u), oz = (int)((ow.x >> 4) & 3u);
     D.par = (ox + oy + oz) & 1;
     D.o0 = 4 * pi + ox;
@@ -220,9 +224,9 @@ __device__ __forceinline__ void xinput_row(const XPatchParams &P, const float4 *
 // Network inputs of the patches of one pass (one warp per patch).
 __global__ void __launch_bounds__(256) xinputs_kernel(XPatchParams P, __nv_bfloat16 *__restrict__ X) {
     const int lane = threadIdx.x & 31;
-    const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
-    const long long total = (long long)P.nrep * P.Pc;
-    for (long long w = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5); w < total; w += nwarps) {
+    const int nwarps = (int)gridDim.x * (int)(blockDim.x >> 5);
+    const int total = P.nrep * (int)P.Pc;
+    for (int w = (int)blockIdx.x * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5); w < total; w += nwarps) {
         const XPatch D = xdecode(P, w);
         const float4 *sp = P.spins4 + (long long)D.r * 2 * P.half;
         const float beta = P.beta_slot_f[P.slot_of_rep[D.r]];
@@ -351,9 +355,9 @@ __global__ void __launch_bounds__(256, 3) xpatch_kernel(XPatchParams P, const fl
                                                      const float *__restrict__ b3, float *__restrict__ dump,
                                                      unsigned long long *__restrict__ acc) {
     const int k = threadIdx.x & 31;
-    const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
-    const long long total = (long long)P.nrep * P.Pc;
-    for (long long w = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5); w < total; w += nwarps) {
+    const int nwarps = (int)gridDim.x * (int)(blockDim.x >> 5);
+    const int total = P.nrep * (int)P.Pc;
+    for (int w = (int)blockIdx.x * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5); w < total; w += nwarps) {
         const XPatch D = xdecode(P, w);
         float4 *sp = P.spins4 + (long long)D.r * 2 * P.half;
         const float beta = P.beta_slot_f[P.slot_of_rep[D.r]];
@@ -383,7 +387,7 @@ __global__ void __launch_bounds__(256, 3) xpatch_kernel(XPatchParams P, const fl
             bz += S.z;
         }
         const float hx = P.jx * bx, hy = P.jy * by, hz = P.jz * bz;
-        const U4 rw = draw(D.pidx, D.t, D.stream, kLearn | ((uint32_t)(32 + k) << 16), P.seed);
+        const U4 rw = draw_rk(D.pidx, D.t, D.stream, kLearn | ((uint32_t)(32 + k) << 16), P.K);
         const Vmf VA = vmf_prep(mx, my, mz);
         float nx, ny, nz;
         vmf_sample(VA, u01(rw.x), upm1(rw.y), &nx, &ny, &nz);
@@ -424,7 +428,7 @@ __global__ void __launch_bounds__(256, 3) xpatch_kernel(XPatchParams P, const fl
         float la = (sa_new + sb_new) - (sa_old + sb_old);
 #pragma unroll
         for (int o = 16; o >= 1; o >>= 1) la += __shfl_xor_sync(0xffffffffu, la, o);
-        const U4 ra = draw(D.pidx, D.t, D.stream, kLearn | (16u << 16), P.seed);
+        const U4 ra = draw_rk(D.pidx, D.t, D.stream, kLearn | (16u << 16), P.K);
         const bool accept = la >= 0.0f || u01(ra.x) < expf_neg(la);
         if (accept) {
             sp[ia] = make_float4(nx, ny, nz, xo.w);
@@ -506,6 +510,7 @@ XPatchParams patch_params(const XyzLearn &x, int cls, int r0, int nrep) {
     P.beta_slot_f = c.beta_slot_f;
     P.jx = x.jx; P.jy = x.jy; P.jz = x.jz;
     P.seed = c.seed;
+    P.K = round_keys(c.seed);
     return P;
 }
 
