@@ -808,6 +808,8 @@ def main():
         comp["batch"] = bt
         comp["tau"] = run_tau(args.L)
         comp["learned"] = run_learned(args.L)
+        comp["learned_heisenberg"] = run_learned(args.L, R=64, train_steps=4000, n_plain=60000, n_learn=6000,
+                                                 heisenberg=True)
         comp["program_c1"] = run_program("c1_ising_16")
         comp["program_c2"] = run_program("c2_heisenberg_32", repeats=1)
         comp["pyrochlore_pt"] = run_pyrochlore_pt()
