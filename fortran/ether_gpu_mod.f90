@@ -215,6 +215,13 @@ module ether_gpu_mod
             type(c_ptr), value :: learn
             integer(c_int32_t), value :: nsweeps
         end function
+        ! network widths (Ising 128, 32, 37152; Heisenberg 304, 96, 67936)
+        integer(c_int) function ether_learn_get_shape(learn, n_inputs, n_outputs, n_params) &
+                bind(C, name="ether_learn_get_shape")
+            import :: c_int, c_ptr, c_int32_t
+            type(c_ptr), value :: learn
+            integer(c_int32_t), intent(out) :: n_inputs, n_outputs, n_params
+        end function
         ! per-temperature acceptance (src/ether.f90:173) and the spiral-state averages
         ! (src/get_spiral_state.f90:127-140)
         integer(c_int) function ether_get_slot_accept_counts(ctx, counts) bind(C, name="ether_get_slot_accept_counts")
