@@ -351,7 +351,7 @@ __global__ void vmf_loss_kernel(float *__restrict__ Zm, const float *__restrict_
 // The Metropolis-Hastings step of the patches of one pass (one warp per patch; lane k owns
 // A-site k and B-site k).  Z: the pass's network outputs (bias b3 added here); dump: optional
 // [R][Pc][96] parameters m of this class.
-__global__ void __launch_bounds__(256, 3) xpatch_kernel(XPatchParams P, const float *__restrict__ Z,
+__global__ void __launch_bounds__(256, 4) xpatch_kernel(XPatchParams P, const float *__restrict__ Z,
                                                      const float *__restrict__ b3, float *__restrict__ dump,
                                                      unsigned long long *__restrict__ acc) {
     const int k = threadIdx.x & 31;
