@@ -78,7 +78,9 @@ ising_ell_kernel(uint8_t *__restrict__ spins, int N, int col_off, int n_c, uint3
 
 // The same update with one site per thread, for colour classes too small to fill the GPU
 // with groups of eight: every lane draws its group's Philox block itself (the draws, and so
-// the decisions, are those of ising_ell_kernel).
+// the decisions, are those of ising_ell_kernel).  W: the class's ELL width at compile time
+// (0: at run time).
+template <int W>
 __global__ void __launch_bounds__(256)
 ising_ell_site_kernel(uint8_t *__restrict__ spins, int N, int col_off, int n_c, uint32_t colour,
                       const int32_t *__restrict__ ell, const int32_t *__restrict__ ews,
@@ -96,7 +98,7 @@ ising_ell_site_kernel(uint8_t *__restrict__ spins, int N, int col_off, int n_c, 
     unsigned acc = 0;
     const IsingEll A{sp, col_off, n_c, width, ell, ews, deg, itype, type_base, type_half, tb};
     for (int rho = blockIdx.x * blockDim.x + threadIdx.x; rho < n_c; rho += gridDim.x * blockDim.x)
-        acc += ising_ell_site(A, rho, t, stream, c3, seed) ? 1u : 0u;
+        acc += ising_ell_site<W>(A, rho, t, stream, c3, seed) ? 1u : 0u;
     warp_add_count(acc_count + r, acc);
 }
 
@@ -527,7 +529,18 @@ cudaError_t launch_ising_sweep(Ctx &c, int colour) {
         const long groups = (long)c.R * ((n_c + 7) / 8);
         if (groups < 2L * c.sm_count * bs) {  // too few groups of eight to fill the GPU
             dim3 grid(blocks_for(c, n_c, bs), c.R);
-            ising_ell_site_kernel<<<grid, bs, 0, c.stream>>>(
+            auto k = ising_ell_site_kernel<0>;
+            switch (c.ell_width[colour]) {  // common widths at compile time
+                case 4: k = ising_ell_site_kernel<4>; break;
+                case 6: k = ising_ell_site_kernel<6>; break;
+                case 8: k = ising_ell_site_kernel<8>; break;
+                case 12: k = ising_ell_site_kernel<12>; break;
+                case 14: k = ising_ell_site_kernel<14>; break;
+                case 18: k = ising_ell_site_kernel<18>; break;
+                case 24: k = ising_ell_site_kernel<24>; break;
+                default: break;
+            }
+            k<<<grid, bs, 0, c.stream>>>(
                 c.spins, c.N, c.col_off[colour], n_c, (uint32_t)colour, ell, ews, c.t.ell_deg,
                 c.ell_width[colour], c.t.itype, c.t.type_base, c.t.type_half, c.thr, c.table_entries,
                 c.slot_of_rep, c.stream_id, c.step, c.seed, c.acc_count);

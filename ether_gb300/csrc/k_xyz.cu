@@ -8,8 +8,9 @@
 namespace ether {
 
 // ------------------------------------------------------------------ general lattice ----
-// One thread per rank of the colour class (xyz_ell_site).
-template <int OPT>
+// One thread per rank of the colour class (xyz_ell_site); W: the class's ELL width at compile
+// time (0: at run time).
+template <int OPT, int W>
 __global__ void __launch_bounds__(256)
 xyz_ell_kernel(float4 *__restrict__ spins4, int N, int col_off, int n_c, uint32_t colour,
                const int32_t *__restrict__ ell, const uint16_t *__restrict__ ej,
@@ -24,7 +25,7 @@ xyz_ell_kernel(float4 *__restrict__ spins4, int N, int col_off, int n_c, uint32_
     const uint32_t c3 = kMetro | (colour << 8);
     unsigned acc = 0;
     for (int rho = blockIdx.x * blockDim.x + threadIdx.x; rho < n_c; rho += gridDim.x * blockDim.x) {
-        acc += xyz_ell_site<OPT>(P, sp, col_off, n_c, rho, ell, ej, deg, width, J4, beta_f, t, c3, K, k1) ? 1u : 0u;
+        acc += xyz_ell_site<OPT, W>(P, sp, col_off, n_c, rho, ell, ej, deg, width, J4, beta_f, t, c3, K, k1) ? 1u : 0u;
     }
     warp_add_count_x(acc_count + r, acc);
 }
@@ -200,6 +201,21 @@ static void launch_xyz_sc_opt(Ctx &c, int colour, const XyzParams &P, const Roun
     }
 }
 
+// The general-lattice kernel for a class's ELL width: common widths at compile time.
+template <int OPT>
+static auto ell_kernel_for(int width) {
+    switch (width) {
+        case 4: return xyz_ell_kernel<OPT, 4>;
+        case 6: return xyz_ell_kernel<OPT, 6>;
+        case 8: return xyz_ell_kernel<OPT, 8>;
+        case 12: return xyz_ell_kernel<OPT, 12>;
+        case 14: return xyz_ell_kernel<OPT, 14>;
+        case 18: return xyz_ell_kernel<OPT, 18>;
+        case 24: return xyz_ell_kernel<OPT, 24>;
+        default: return xyz_ell_kernel<OPT, 0>;
+    }
+}
+
 bool xyz_variant_valid(int v) { return (v >= 11 && v <= 15) || v == 21 || v == 22; }
 
 cudaError_t launch_xyz_sweep(Ctx &c, int colour) {
@@ -216,16 +232,11 @@ cudaError_t launch_xyz_sweep(Ctx &c, int colour) {
         dim3 grid(blocks_for_x(c, n_c, bs), c.R);
         const int32_t *ell = c.t.ell_nbr + c.ell_off[colour];
         const uint16_t *ej = c.t.ell_j + c.ell_off[colour];
-        if (exchange_only)
-            xyz_ell_kernel<kXyzExchange><<<grid, bs, 0, c.stream>>>(
-                c.spins4, c.N, c.col_off[colour], n_c, (uint32_t)colour, ell, ej, c.t.ell_deg,
-                c.ell_width[colour], c.t.J4, P, c.beta_slot_f, c.slot_of_rep, c.stream_id, c.step, K,
-                c.acc_count);
-        else
-            xyz_ell_kernel<kXyzGeneral><<<grid, bs, 0, c.stream>>>(
-                c.spins4, c.N, c.col_off[colour], n_c, (uint32_t)colour, ell, ej, c.t.ell_deg,
-                c.ell_width[colour], c.t.J4, P, c.beta_slot_f, c.slot_of_rep, c.stream_id, c.step, K,
-                c.acc_count);
+        auto k = exchange_only ? ell_kernel_for<kXyzExchange>(c.ell_width[colour])
+                               : ell_kernel_for<kXyzGeneral>(c.ell_width[colour]);
+        k<<<grid, bs, 0, c.stream>>>(c.spins4, c.N, c.col_off[colour], n_c, (uint32_t)colour, ell, ej, c.t.ell_deg,
+                                     c.ell_width[colour], c.t.J4, P, c.beta_slot_f, c.slot_of_rep, c.stream_id,
+                                     c.step, K, c.acc_count);
     }
     c.launches++;
     return cudaGetLastError();

@@ -45,18 +45,30 @@ struct IsingEll {
 
 // One site: rank rho.  Threshold-table index = sum of stride * up-spin over the neighbours;
 // the draw is halfword rho & 7 of the Philox block of group rho >> 3, and on a tie the
-// same halfword of the group's second block.
+// same halfword of the group's second block.  W > 0: the class's ELL width, known at compile
+// time (every load of the site issued at once); W = 0: A.width at run time.
+template <int W = 0>
 __device__ __forceinline__ bool ising_ell_site(const IsingEll &A, int rho, uint32_t t, uint32_t stream,
                                                uint32_t c3, uint32_t seed) {
     const int s = A.col_off + rho;
     const int dg = A.deg[s];
     int idx = 0;
+    if constexpr (W > 0) {
+#pragma unroll
+        for (int k = 0; k < W; ++k) {
+            const int e = k * A.n_c + rho;  // ELL blocks hold < 2^31 entries (checked at creation)
+            const int up = A.sp[A.ell[e]];
+            const int w = A.ews[e];
+            if (k < dg) idx += w * up;
+        }
+    } else {
 #pragma unroll 6
-    for (int k = 0; k < A.width; ++k) {
-        const int e = k * A.n_c + rho;  // ELL blocks hold < 2^31 entries (checked at creation)
-        const int up = A.sp[A.ell[e]];
-        const int w = A.ews[e];
-        if (k < dg) idx += w * up;
+        for (int k = 0; k < A.width; ++k) {
+            const int e = k * A.n_c + rho;
+            const int up = A.sp[A.ell[e]];
+            const int w = A.ews[e];
+            if (k < dg) idx += w * up;
+        }
     }
     const int own = A.sp[s];
     const int ty = A.itype[s];

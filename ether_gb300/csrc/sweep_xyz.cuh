@@ -153,36 +153,53 @@ __device__ __forceinline__ Acc3 sc_field(const float4 *__restrict__ opp, int L1,
 // Exchange field of rank rho of a colour class from its ELL block (ell: entries k * n_c + rho,
 // coalesced across a warp), in the CSR's order -- the reference's nn order -- so the fmaf
 // chain rounds as the oracle's.
+// W > 0: the class's ELL width, known at compile time (every load of the site issued at
+// once); W = 0: width at run time.
+template <int W = 0>
 __device__ __forceinline__ Acc3 ell_field(const float4 *__restrict__ sp, const int32_t *__restrict__ ell,
                                           const uint16_t *__restrict__ ej, const float4 *__restrict__ J4,
                                           int n_c, int width, int rho, int deg) {
     // The padding entries point at valid memory (the site itself, coupling 0), so the loads
     // are unconditional and can all be in flight at once; only the fmaf is predicated.
     Acc3 h{0.f, 0.f, 0.f};
+    if constexpr (W > 0) {
+#pragma unroll
+        for (int k = 0; k < W; ++k) {
+            const int e = k * n_c + rho;  // ELL blocks hold < 2^31 entries (checked at creation)
+            const float4 Jv = J4[ej[e]];
+            const float4 Sj = sp[ell[e]];
+            if (k < deg) {
+                h.x = fmaf(Jv.x, Sj.x, h.x);
+                h.y = fmaf(Jv.y, Sj.y, h.y);
+                h.z = fmaf(Jv.z, Sj.z, h.z);
+            }
+        }
+    } else {
 #pragma unroll 6
-    for (int k = 0; k < width; ++k) {
-        const int e = k * n_c + rho;  // ELL blocks hold < 2^31 entries (checked at creation)
-        const float4 Jv = J4[ej[e]];
-        const float4 Sj = sp[ell[e]];
-        if (k < deg) {
-            h.x = fmaf(Jv.x, Sj.x, h.x);
-            h.y = fmaf(Jv.y, Sj.y, h.y);
-            h.z = fmaf(Jv.z, Sj.z, h.z);
+        for (int k = 0; k < width; ++k) {
+            const int e = k * n_c + rho;
+            const float4 Jv = J4[ej[e]];
+            const float4 Sj = sp[ell[e]];
+            if (k < deg) {
+                h.x = fmaf(Jv.x, Sj.x, h.x);
+                h.y = fmaf(Jv.y, Sj.y, h.y);
+                h.z = fmaf(Jv.z, Sj.z, h.z);
+            }
         }
     }
     return h;
 }
 
 // One Metropolis update of rank rho of a colour class of a general lattice (ELL block of the
-// class: ell, ej; deg per storage index).
-template <int OPT>
+// class: ell, ej; deg per storage index; W as ell_field's).
+template <int OPT, int W = 0>
 __device__ __forceinline__ bool xyz_ell_site(const XyzParams &P, float4 *sp, int col_off, int n_c, int rho,
                                              const int32_t *__restrict__ ell, const uint16_t *__restrict__ ej,
                                              const uint16_t *__restrict__ deg, int width,
                                              const float4 *__restrict__ J4, float beta_f, uint32_t t,
                                              uint32_t c3, const RoundKeys &K, uint32_t stream) {
     const int s = col_off + rho;
-    const Acc3 h = ell_field(sp, ell, ej, J4, n_c, width, rho, deg[s]);
+    const Acc3 h = ell_field<W>(sp, ell, ej, J4, n_c, width, rho, deg[s]);
     return metro_site<OPT>(P, sp, s, (uint32_t)rho, h.x, h.y, h.z, beta_f, t, c3, K, stream);
 }
 
