@@ -54,12 +54,17 @@ __device__ __forceinline__ bool ising_ell_site(const IsingEll &A, int rho, uint3
     const int dg = A.deg[s];
     int idx = 0;
     if constexpr (W > 0) {
+        // the neighbours' storage indices, then all their spins, then the index sum
+        int nb[W];
+#pragma unroll
+        for (int k = 0; k < W; ++k) nb[k] = A.ell[k * A.n_c + rho];  // ELL blocks hold < 2^31 entries
+        int up[W];
+#pragma unroll
+        for (int k = 0; k < W; ++k) up[k] = A.sp[nb[k]];
 #pragma unroll
         for (int k = 0; k < W; ++k) {
-            const int e = k * A.n_c + rho;  // ELL blocks hold < 2^31 entries (checked at creation)
-            const int up = A.sp[A.ell[e]];
-            const int w = A.ews[e];
-            if (k < dg) idx += w * up;
+            const int w = A.ews[k * A.n_c + rho];
+            if (k < dg) idx += w * up[k];
         }
     } else {
 #pragma unroll 6

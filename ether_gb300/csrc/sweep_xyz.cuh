@@ -163,15 +163,20 @@ __device__ __forceinline__ Acc3 ell_field(const float4 *__restrict__ sp, const i
     // are unconditional and can all be in flight at once; only the fmaf is predicated.
     Acc3 h{0.f, 0.f, 0.f};
     if constexpr (W > 0) {
+        // the neighbours' storage indices, then all their spins, then the field
+        int nb[W];
+#pragma unroll
+        for (int k = 0; k < W; ++k) nb[k] = ell[k * n_c + rho];  // ELL blocks hold < 2^31 entries
+        float4 Sj[W];
+#pragma unroll
+        for (int k = 0; k < W; ++k) Sj[k] = sp[nb[k]];
 #pragma unroll
         for (int k = 0; k < W; ++k) {
-            const int e = k * n_c + rho;  // ELL blocks hold < 2^31 entries (checked at creation)
-            const float4 Jv = J4[ej[e]];
-            const float4 Sj = sp[ell[e]];
+            const float4 Jv = J4[ej[k * n_c + rho]];
             if (k < deg) {
-                h.x = fmaf(Jv.x, Sj.x, h.x);
-                h.y = fmaf(Jv.y, Sj.y, h.y);
-                h.z = fmaf(Jv.z, Sj.z, h.z);
+                h.x = fmaf(Jv.x, Sj[k].x, h.x);
+                h.y = fmaf(Jv.y, Sj[k].y, h.y);
+                h.z = fmaf(Jv.z, Sj[k].z, h.z);
             }
         }
     } else {
