@@ -61,6 +61,21 @@ xyz_sc_kernel(float4 *__restrict__ spins4, int L1, int L2, int L3, FastDiv fH, F
 // then normalisation.  A site with A = 0 is left unchanged (the reference would divide
 // by zero).  Pass `pass` < floor(ovrr_para) reflects every site; the last pass reflects a
 // site iff its uniform < part.  Neighbours from the colour class's ELL block.
+__device__ __forceinline__ void ovrr_reflect(float4 *site, float hx, float hy, float hz) {
+    const float4 S = *site;
+    float d = hx * S.x;
+    d = fmaf(hy, S.y, d);
+    d = fmaf(hz, S.z, d);
+    float a2 = hx * hx;
+    a2 = fmaf(hy, hy, a2);
+    a2 = fmaf(hz, hz, a2);
+    if (!(a2 > 0.0f)) return;
+    const float f = 2.0f * (d / a2);
+    const float nx = f * hx - S.x, ny = f * hy - S.y, nz = f * hz - S.z;
+    const float inv = 1.0f / sqrtf(nx * nx + ny * ny + nz * nz);
+    *site = make_float4(nx * inv, ny * inv, nz * inv, S.w);
+}
+
 __global__ void __launch_bounds__(256)
 ovrr_ell_kernel(float4 *__restrict__ spins4, int N, int col_off, int n_c, uint32_t colour,
                 int pass, float part, const int32_t *__restrict__ ell, const uint16_t *__restrict__ ej,
@@ -78,19 +93,35 @@ ovrr_ell_kernel(float4 *__restrict__ spins4, int N, int col_off, int n_c, uint32
             if (!(u01(o.x) < part)) continue;
         }
         const Acc3 h = ell_field(sp, ell, ej, J4, n_c, width, rho, deg[s]);
-        const float hx = h.x, hy = h.y, hz = h.z;
-        float4 S = sp[s];
-        float d = hx * S.x;
-        d = fmaf(hy, S.y, d);
-        d = fmaf(hz, S.z, d);
-        float a2 = hx * hx;
-        a2 = fmaf(hy, hy, a2);
-        a2 = fmaf(hz, hz, a2);
-        if (!(a2 > 0.0f)) continue;
-        float f = 2.0f * (d / a2);
-        float nx = f * hx - S.x, ny = f * hy - S.y, nz = f * hz - S.z;
-        float inv = 1.0f / sqrtf(nx * nx + ny * ny + nz * nz);
-        sp[s] = make_float4(nx * inv, ny * inv, nz * inv, S.w);
+        ovrr_reflect(sp + s, h.x, h.y, h.z);
+    }
+}
+
+// The same on a simple-cubic lattice: neighbours from the other colour's array in closed
+// form (sc_field sums them in the order of the ELL block, so the results are the same).
+__global__ void __launch_bounds__(256)
+ovrr_sc_kernel(float4 *__restrict__ spins4, int L1, int L2, int L3, FastDiv fH, FastDiv fL2, uint32_t colour,
+               int pass, float part, float jx, float jy, float jz, const uint32_t *__restrict__ stream_id,
+               const uint32_t *__restrict__ ovrr_step, uint32_t seed) {
+    const int r = blockIdx.y;
+    const int H = L1 >> 1;
+    const int half = H * L2 * L3;
+    float4 *base = spins4 + (size_t)r * 2 * half;
+    float4 *own = base + (size_t)colour * half;
+    const float4 *opp = base + (size_t)(colour ^ 1u) * half;
+    const uint32_t k1 = stream_id[r], t = ovrr_step[r];
+    const uint32_t c3 = kOvrr | (colour << 8);
+    for (int rho = blockIdx.x * blockDim.x + threadIdx.x; rho < half; rho += gridDim.x * blockDim.x) {
+        if (part < 1.0f) {
+            U4 o = draw((uint32_t)rho, t, k1, c3 | ((uint32_t)pass << 16), seed);
+            if (!(u01(o.x) < part)) continue;
+        }
+        const int row = (int)fdiv((uint32_t)rho, fH);
+        const int xh = rho - row * H;
+        const int z = (int)fdiv((uint32_t)row, fL2), y = row - z * L2;
+        const int p = (y + z + (int)colour) & 1;
+        const Acc3 h = sc_field(opp, L1, L2, L3, H, xh, y, z, p, jx, jy, jz);
+        ovrr_reflect(own + rho, h.x, h.y, h.z);
     }
 }
 
@@ -247,6 +278,13 @@ cudaError_t launch_overrelax(Ctx &c, int colour, int pass, float part) {
     const int n_c = c.col_off[colour + 1] - c.col_off[colour];
     if (n_c == 0) return cudaSuccess;
     dim3 grid(blocks_for_x(c, n_c, bs), c.R);
+    if (c.fast) {
+        ovrr_sc_kernel<<<grid, bs, 0, c.stream>>>(c.spins4, c.L[0], c.L[1], c.L[2], make_fastdiv((uint32_t)(c.L[0] / 2)),
+                                                  make_fastdiv((uint32_t)c.L[1]), (uint32_t)colour, pass, part,
+                                                  c.h_Jf[0], c.h_Jf[1], c.h_Jf[2], c.stream_id, c.ovrr_step, c.seed);
+        c.launches++;
+        return cudaGetLastError();
+    }
     ovrr_ell_kernel<<<grid, bs, 0, c.stream>>>(c.spins4, c.N, c.col_off[colour], n_c, (uint32_t)colour, pass,
                                                part, c.t.ell_nbr + c.ell_off[colour],
                                                c.t.ell_j + c.ell_off[colour], c.t.ell_deg,

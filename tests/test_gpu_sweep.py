@@ -227,10 +227,13 @@ def test_energy_magnetisation_match_oracle():
             np.testing.assert_allclose(M, osys.tot_magnetisation_f32(ion, sp4), rtol=1e-12, atol=1e-9)
 
 
+# flags 0: the simple-cubic kernel (closed-form neighbours); FORCE_GENERAL: the ELL kernel
+@pytest.mark.parametrize("flags", [0, eg.FLAG_FORCE_GENERAL])
 @pytest.mark.parametrize("para", [0.4, 1.0, 1.7])
-def test_overrelaxation_matches_oracle_and_conserves_energy(para):
+def test_overrelaxation_matches_oracle_and_conserves_energy(para, flags):
     lat = eg.simple_cubic(8)
-    sw, osys = make_pair(lat, eg.MODEL_XYZ, FM)
+    sw, osys = make_pair(lat, eg.MODEL_XYZ, FM, flags=flags)
+    assert sw.info().fast_path == (0 if flags else 1)
     sw.set_beta(1.0)
     sw.set_streams(stream=[5], step=[0])
     ion = random_xyz(lat, 5)
