@@ -352,8 +352,8 @@ def _time_plain(members, steps, warmup):
 
 def run_batch(steps=200, warmup=5, chains=256, ladder=32, config=None, forms=(False, True),
               plain=True, mix="mixed", sizes=None):
-    """The mixed batch advanced by ether_batch (one persistent kernel per colour phase, one
-    graph per sweep, autotuned tiles) and by each member's own sweeps (per-context kernels
+    """The mixed batch advanced by ether_batch (one kernel per member group, colour phase and
+    member class, one graph per sweep, autotuned tiles) and by each member's own sweeps (per-context kernels
     on the members' streams), with one context per chain and with chains grouped by
     (model, L, J)."""
     import ether_gb300 as eg

@@ -3,8 +3,8 @@
 // The reference advances one lattice at one temperature per MPI rank (src/ether.f90:112-118,
 // one Metropolis sweep at a time: src/Metropolis.f90:34-68).  A batch advances every replica
 // of every member context -- mixed lattice sizes, Ising and XYZ, each member with its own
-// temperature ladder -- with one persistent kernel per colour phase and member class (the
-// kernel specialised for that class): a grid of (resident blocks per SM x SMs) walks a table
+// temperature ladder -- with one kernel per colour phase, member class (the kernel
+// specialised for that class) and L2-sized group of members: a grid of blocks walks a table
 // of segments (member, replica, first unit, units), each segment a block-sized tile of one
 // replica's colour class.  A unit is what one thread updates at a time: a W-byte vector
 // (simple-cubic Ising) or one site (general Ising, XYZ; general lattices from the colour

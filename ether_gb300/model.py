@@ -344,9 +344,10 @@ class Sweep:
 
 
 class Batch:
-    """ether_batch: one persistent kernel per colour phase advances the Metropolis sweeps of
-    every member Sweep (mixed sizes and models), leaving each member exactly as its own
-    metropolis() would.  The members must outlive the batch."""
+    """ether_batch: kernels per member group, colour phase and member class, captured in one
+    graph per sweep, advance the Metropolis sweeps of every member Sweep (mixed sizes and
+    models), leaving each member exactly as its own metropolis() would.  The members must
+    outlive the batch."""
 
     def __init__(self, members):
         self.lib = abi.load()

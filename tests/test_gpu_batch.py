@@ -1,5 +1,5 @@
-"""Batched sweeps (ether_batch_*): one persistent kernel per colour phase over many contexts
-leaves every member exactly as its own ether_metropolis would -- spins bit for bit and the
+"""Batched sweeps (ether_batch_*): kernels per member group, colour phase and member class over
+many contexts leave every member exactly as its own ether_metropolis would -- spins bit for bit and the
 acceptance counters -- for mixed sizes and models (simple-cubic Ising with 16-, 8- and 4-byte
 vectors, general Ising, simple-cubic XYZ, general XYZ and Ising on the pyrochlore lattice,
 whose colourings have more than two classes), for every tile shape and walk and after the
