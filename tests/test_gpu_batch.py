@@ -30,12 +30,15 @@ SPECS = [
 
 
 def build_members(specs=SPECS, seed0=11):
+    """Member contexts of the specs (lattice, model, couplings, replicas, flags[, options])."""
     out = []
-    for k, (mk, model, shells, R, flags) in enumerate(specs):
+    for k, spec in enumerate(specs):
+        mk, model, shells, R, flags = spec[:5]
+        opts = spec[5] if len(spec) > 5 else {}
         lat = mk()
         j = eg.couplings(lat.n_species, shells, [1.0])
         sw = eg.Sweep.from_lattice(lat, j, np.asarray([1.0]), model, replicas=R,
-                                   seed=1992 + 7 * k, flags=flags)
+                                   seed=1992 + 7 * k, flags=flags, **opts)
         sw.set_ladder([beta_of(3.0 + 1.5 * i) for i in range(R)])
         ion = random_ising(lat, seed0 + k) if model == eg.MODEL_ISING else random_xyz(lat, seed0 + k)
         sw.set_spins(ion)
@@ -120,7 +123,9 @@ def test_batch_autotune_restores_state_and_keeps_parity():
     batch = eg.Batch([sw for _, sw in A])
     before = states(A)
     cfg, ms = batch.autotune()
-    assert cfg[0] in (128, 256) and cfg[1] in (1, 2, 4, 8, 16) and cfg[2] >= 1 and cfg[3] in (0, 1)
+    # walk 2 (one block per tile) ignores the blocks per SM, reported as 0
+    assert cfg[0] in (128, 256) and cfg[1] in (1, 2, 4, 8, 16, 32) and cfg[3] in (0, 1, 2)
+    assert cfg[2] >= 1 or cfg[3] == 2
     assert ms > 0.0
     assert_same(states(A), before)
     batch.metropolis(3)
@@ -156,4 +161,26 @@ def test_batch_rejects_bad_input():
         batch.set_config(128, 1, 0, walk=3)
     with pytest.raises(eg.EtherError):
         batch.metropolis(-1)
+    batch.close()
+
+
+def test_batch_members_with_field_anisotropy_and_angle_proposals():
+    """The XYZ classes with options (Zeeman, SIA, ANGLE proposals) on simple-cubic and general
+    lattices, beside exchange-only members: spins and counters as the members' own sweeps."""
+    zs = {"zeeman": True, "h": (0.0, 0.3, 1.0), "g_factor": 2.0, "sia": True,
+          "sia_vec": np.array([[0.0, 0.0, -0.3e-3]])}
+    specs = [
+        (lambda: eg.simple_cubic(12), eg.MODEL_XYZ, FM, 2, 0, zs),
+        (lambda: eg.simple_cubic((6, 8, 10)), eg.MODEL_XYZ, AFM, 2, 0, {"angle": True, "dphi": 0.6}),
+        (lambda: eg.pyrochlore(2), eg.MODEL_XYZ, AFM, 2, 0, zs),
+        (lambda: eg.simple_cubic(8), eg.MODEL_XYZ, FM, 2, 0),
+        (lambda: eg.simple_cubic(16), eg.MODEL_ISING, AFM, 2, 0),
+    ]
+    A = build_members(specs)
+    B = build_members(specs)
+    batch = eg.Batch([sw for _, sw in A])
+    batch.metropolis(4)
+    for _, sw in B:
+        sw.metropolis(4)
+    assert_same(states(A), states(B))
     batch.close()
