@@ -298,3 +298,27 @@ def test_set_spins_every_replica(model, L):
     sw.set_spins(other, 2)
     np.testing.assert_array_equal(sw.get_spins(lat.ion, 2)[:, cols], other[:, cols].astype(np.float32).astype(np.float64))
     np.testing.assert_array_equal(sw.get_spins(lat.ion, 3)[:, cols], ion[:, cols].astype(np.float32).astype(np.float64))
+
+
+# The general-lattice kernels are instantiated for common ELL widths: bcc (8 nearest
+# neighbours), fcc (12), and the simple-cubic first + second shells (6 + 12 = 18); every form
+# must reproduce the oracle bit for bit.
+def _lattice(kind):
+    if kind == "bcc":
+        return eg.Lattice([[0.0, 0.0, 0.0], [0.5, 0.5, 0.5]], [1, 1], np.eye(3), (4, 4, 4), [0.8660254]), FM
+    if kind == "fcc":
+        return eg.Lattice([[0.0, 0.0, 0.0], [0.0, 0.5, 0.5], [0.5, 0.0, 0.5], [0.5, 0.5, 0.0]], [1, 1, 1, 1],
+                          np.eye(3), (3, 3, 3), [0.70710678]), FM
+    return eg.Lattice([[0.0, 0.0, 0.0]], [1], np.eye(3), (6, 6, 6), [1.0, 1.41421356]), AFM_J1_J2
+
+
+@pytest.mark.parametrize("kind,width", [("bcc", 8), ("fcc", 12), ("sc2", 18)])
+def test_general_lattice_widths_bit_exact(kind, width):
+    lat, shells = _lattice(kind)
+    sw, ion, g, ao, ag = ising_replay(lat, shells, 4.0, 12)
+    assert sw.info().fast_path == 0
+    np.testing.assert_array_equal(g[:, 3], ion[:, 3])
+    assert ao == pytest.approx(ag, abs=1e-12)
+    sw, osys, sp4, ion64, g = xyz_replay(lat, shells, 1.5, 12)
+    for k, col in ((1, 0), (2, 1), (3, 2), (5, 3)):
+        np.testing.assert_array_equal(g[:, k].astype(np.float32), sp4[:, col])
