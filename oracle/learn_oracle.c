@@ -1,7 +1,8 @@
 /*
- * learn_oracle.c -- TEST INFRASTRUCTURE: CPU restatement of the learned patch proposal
- * (the product's ether_learn_* in ether_gb300/csrc/k_learn.cu).  Only tests/, smoke() and
- * bench.py's CPU legs call it.  The reference has no learned proposal; what must match the
+ * learn_oracle.c -- TEST INFRASTRUCTURE: CPU restatement of the learned patch proposals
+ * (the product's ether_learn_* in ether_gb300/csrc/k_learn.cu for Ising and
+ * ether_gb300/csrc/k_learn_xyz.cu for Heisenberg; the Heisenberg part is at the end of this
+ * file).  Only tests/, smoke() and bench.py's CPU legs call it.  The reference has no learned proposal; what must match the
  * reference is the stationary distribution, which exact Metropolis-Hastings preserves: the
  * acceptance below uses the reference's Ising energy (src/Hamiltonian.f90:57-105, pair
  * energy J s_i s_j with s = +-1, J the z component of j_exc) and its Boltzmann weight
