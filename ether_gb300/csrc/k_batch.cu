@@ -276,6 +276,8 @@ struct ether_batch {
     // finds in L2 the other colour's spins that the group's previous phase wrote.  Groups are
     // independent and run on n_branch parallel branches of the sweep graph.
     std::vector<int> group_of;          // per member
+    std::vector<int> solo;              // per group: a member above the byte budget alone in its group
+                                        // (it runs its own phase kernels), else -1
     int n_groups = 1;
     long long group_bytes = 0;          // spin bytes per group; 0: half the L2
     long long l2_bytes = 0;
@@ -414,18 +416,22 @@ int rebuild(ether_batch &b) {
     // groups: consecutive members up to the byte budget (a larger member is a group alone)
     const long long budget = b.group_bytes > 0 ? b.group_bytes : std::max(1LL, b.l2_bytes / 2);
     b.group_of.assign(b.members.size(), 0);
+    b.solo.clear();
     {
         int g = 0;
         long long used = 0;
+        b.solo.push_back(-1);
         for (size_t k = 0; k < b.members.size(); ++k) {
             const Ctx &c = b.members[k]->c;
             const long long bytes = (long long)c.R * c.N * (c.model == ETHER_MODEL_ISING ? 1 : (long long)sizeof(float4));
-            if (used > 0 && used + bytes > budget) {
+            if (used > 0 && (used + bytes > budget || bytes > budget)) {
                 ++g;
                 used = 0;
+                b.solo.push_back(-1);
             }
             b.group_of[k] = g;
             used += bytes;
+            if (bytes > budget) b.solo[g] = (int)k;  // a large member: its own kernels, no segments
         }
         b.n_groups = g + 1;
     }
@@ -442,6 +448,11 @@ int rebuild(ether_batch &b) {
         for (size_t k = 0; k < b.members.size(); ++k) {
             if (b.group_of[k] != g || class_of(hm[k]) != cls) continue;
             const Ctx &c = b.members[k]->c;
+            if (b.solo[g] == (int)k) {
+                if (p < c.ncol && cls == class_of(hm[k]))
+                    b.updates_per_sweep += (long long)(c.col_off[p + 1] - c.col_off[p]) * c.R;
+                continue;
+            }
             const long u = units_of(hm[k], c, p);
             if (u == 0) continue;
             for (int r = 0; r < c.R; ++r)
@@ -531,15 +542,29 @@ int issue_sweep(ether_batch &b) {
         for (int k = 0; k < nbr; ++k) BCUDA(cudaStreamWaitEvent(b.branch[k], b.ev_fork, 0));
     }
     const int per_group = b.max_col * kNumClasses;
-    for (int q = 0; q < (int)b.seg_cnt.size(); ++q) {
-        if (b.seg_cnt[q] == 0) continue;
-        const int g = q / per_group;
+    for (int g = 0; g < b.n_groups; ++g) {
         cudaStream_t st = nbr > 1 ? b.branch[g % nbr] : b.stream;
-        const int32_t *bf = b.walk == 1 ? b.d_block_first + b.bf_off[q] : nullptr;
-        launch_phase_class(q % kNumClasses, b.minb, b.bf_grid[q], b.threads, st, b.d_members,
-                           b.d_segs + b.seg_off[q], bf, b.seg_cnt[q], (uint32_t)((q / kNumClasses) % b.max_col),
-                           b.upt);
-        BCUDA(cudaGetLastError());
+        for (int p = 0; p < b.max_col; ++p) {
+            if (b.solo[g] >= 0) {
+                // the member's own phase kernel (its autotuned variant), on this branch
+                Ctx &c = b.members[b.solo[g]]->c;
+                if (p >= c.ncol) continue;
+                cudaStream_t own = c.stream;
+                c.stream = st;
+                const cudaError_t e = c.model == ETHER_MODEL_ISING ? launch_ising_sweep(c, p) : launch_xyz_sweep(c, p);
+                c.stream = own;
+                if (e != cudaSuccess) return bfail(ETHER_ERR_CUDA, std::string("batch member phase: ") + cudaGetErrorString(e));
+                continue;
+            }
+            for (int cls = 0; cls < kNumClasses; ++cls) {
+                const int q = g * per_group + p * kNumClasses + cls;
+                if (b.seg_cnt[q] == 0) continue;
+                const int32_t *bf = b.walk == 1 ? b.d_block_first + b.bf_off[q] : nullptr;
+                launch_phase_class(cls, b.minb, b.bf_grid[q], b.threads, st, b.d_members, b.d_segs + b.seg_off[q], bf,
+                                   b.seg_cnt[q], (uint32_t)p, b.upt);
+                BCUDA(cudaGetLastError());
+            }
+        }
     }
     if (nbr > 1)
         for (int k = 0; k < nbr; ++k) {
@@ -554,6 +579,8 @@ int issue_sweep(ether_batch &b) {
 int kernels_per_sweep(const ether_batch &b) {
     int n = 1;
     for (int cnt : b.seg_cnt) n += cnt > 0 ? 1 : 0;
+    for (int k : b.solo)
+        if (k >= 0) n += b.members[k]->c.ncol;
     return n;
 }
 
@@ -796,6 +823,35 @@ extern "C" int ether_batch_autotune(ether_batch *b, int32_t *config, float *best
             bw = 1;
         }
     }
+    // then the number of parallel graph branches the member groups are spread over
+    const int old_nb = b->n_branch;
+    int bnb = old_nb;
+    for (int nb : {1, 2, 4, 8}) {
+        if (rc) break;
+        b->threads = bt;
+        b->upt = bu;
+        b->bps = bb;
+        b->minb = bm;
+        b->xyz_cost = bc;
+        b->walk = bw;
+        b->n_branch = nb;
+        b->dirty = true;
+        rc = run_sweeps(*b, 1, false);
+        if (!rc) rc = run_sweeps(*b, 2, true);
+        if (rc) break;
+        float ms = 0.f;
+        if (cudaEventSynchronize(b->ev_t1) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, b->ev_t0, b->ev_t1) != cudaSuccess) {
+            rc = bfail(ETHER_ERR_CUDA, "batch autotune timing");
+            break;
+        }
+        ms *= 0.5f;
+        if (ms < best) {
+            best = ms;
+            bnb = nb;
+        }
+    }
+    b->n_branch = rc ? old_nb : bnb;
     for (const Saved &s : sv) cudaMemcpyAsync(s.src, backup + s.off, s.bytes, cudaMemcpyDeviceToDevice, b->stream);
     cudaStreamSynchronize(b->stream);
     cudaFree(backup);

@@ -184,3 +184,28 @@ def test_batch_members_with_field_anisotropy_and_angle_proposals():
         sw.metropolis(4)
     assert_same(states(A), states(B))
     batch.close()
+
+
+def test_batch_large_member_runs_its_own_kernels():
+    """A member above the L2 group budget of half the L2 (64^3 x 48 XYZ replicas = 201 MB,
+    beside smaller members) runs its own phase kernels inside the batch graph: the same spins
+    and counters as the members' own sweeps."""
+    specs = [
+        (lambda: eg.simple_cubic(16), eg.MODEL_ISING, AFM, 2, 0),
+        (lambda: eg.simple_cubic(64), eg.MODEL_XYZ, FM, 48, 0),
+        (lambda: eg.simple_cubic(12), eg.MODEL_XYZ, FM, 2, 0),
+    ]
+    A = build_members(specs)
+    B = build_members(specs)
+    batch = eg.Batch([sw for _, sw in A])
+    batch.metropolis(3)
+    for _, sw in B:
+        sw.metropolis(3)
+    assert_same(states(A), states(B))
+    info = batch.info()
+    assert info.site_updates_per_sweep == sum(sw.N * sw.R for _, sw in A)
+    # groups: the Ising member, the large member alone, the small XYZ member; per sweep the
+    # large member's two phase kernels, one class kernel per phase for each small member's
+    # group, and the counter advance
+    assert info.kernels_per_sweep == 2 + 2 * 2 + 1
+    batch.close()
