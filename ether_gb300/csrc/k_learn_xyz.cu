@@ -8,9 +8,10 @@
 //   * network: input = the 96 boundary spins (3 components each, BF16-rounded) and
 //     beta (Jxx, Jyy, Jzz), zero-padded to 304; 128 -> 128 (ReLU, BF16 activations) -> 96;
 //     outputs 3k .. 3k+2 (+ bias) are the von Mises-Fisher parameter m_k of A-site k;
-//     inference: the three layers as cuBLAS BF16 x BF16 -> FP32 tensor-core GEMMs (plain
-//     library GEMMs) with this file's bias / ReLU / BF16 kernels between them; training on
-//     the FP32 GEMM of k_learn.cu;
+//     inference: the three layers as cuBLAS BF16 x BF16 tensor-core GEMMs (plain library
+//     GEMMs; layers 1 and 2 with cuBLASLt's bias + ReLU epilogue writing BF16, else this
+//     file's bias / ReLU / BF16 kernel; hidden biases in BF16 there); training on the FP32
+//     GEMM of k_learn.cu;
 //   * proposal: A-site k ~ vMF(m_k) (Wood's exact sampler on the sphere, own log / exp /
 //     sincos); then every B-site from its exact heat-bath conditional vMF(-beta g), g = J o
 //     (sum of its six neighbours: new A-sites and the boundary); a vMF with |m| < 1e-3 is
@@ -28,6 +29,7 @@
 #include <string>
 #include <vector>
 
+#include <cublasLt.h>
 #include <cublas_v2.h>
 
 #include "internal.h"
@@ -278,9 +280,9 @@ __global__ void xbatch_kernel(const __nv_bfloat16 *__restrict__ X, const float *
     for (int i = threadIdx.x; i < XNO; i += blockDim.x) Yb[(size_t)b * XNO + i] = Y[(size_t)row * XNO + i];
 }
 
-// H16 = bf16(max(H + b, 0)) (the value the FP32 path stores), rows x NH, eight columns per
-// thread (two 16-byte loads, one 16-byte store)
-__global__ void bias_relu_bf16_kernel(const float *__restrict__ Hm, const float *__restrict__ b,
+// H16 = bf16(max(H + b, 0)), b in BF16 (the cuBLASLt epilogue's operands), rows x NH, eight
+// columns per thread (two 16-byte loads, one 16-byte store)
+__global__ void bias_relu_bf16_kernel(const float *__restrict__ Hm, const __nv_bfloat16 *__restrict__ b16,
                                       __nv_bfloat16 *__restrict__ H16, long long rows) {
     const long long nv = rows * (NH / 8);
     for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv; v += (long long)gridDim.x * blockDim.x) {
@@ -290,8 +292,9 @@ __global__ void bias_relu_bf16_kernel(const float *__restrict__ Hm, const float 
         uint32_t w[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const __nv_bfloat162 pr = __floats2bfloat162_rn(fmaxf(h[2 * j] + b[c0 + 2 * j], 0.0f),
-                                                            fmaxf(h[2 * j + 1] + b[c0 + 2 * j + 1], 0.0f));
+            const __nv_bfloat162 pr =
+                __floats2bfloat162_rn(fmaxf(h[2 * j] + __bfloat162float(b16[c0 + 2 * j]), 0.0f),
+                                      fmaxf(h[2 * j + 1] + __bfloat162float(b16[c0 + 2 * j + 1]), 0.0f));
             w[j] = *reinterpret_cast<const uint32_t *>(&pr);
         }
         reinterpret_cast<uint4 *>(H16)[v] = make_uint4(w[0], w[1], w[2], w[3]);
@@ -460,6 +463,16 @@ struct XyzLearn {
     double *loss = nullptr;
     // inference: BF16 weights, one pass of up to `rows` patches
     cublasHandle_t blas = nullptr;
+    cublasLtHandle_t lt = nullptr;
+    void *lt_ws = nullptr;         // cuBLASLt workspace
+    struct LtPlan {                // a fused layer (bias + ReLU epilogue, BF16 out) for M rows
+        int M = 0, K = 0;
+        cublasLtMatmulDesc_t op = nullptr;
+        cublasLtMatrixLayout_t a = nullptr, b = nullptr, d = nullptr;
+        cublasLtMatmulAlgo_t algo;
+        bool ok = false;
+    };
+    std::vector<LtPlan> plans;
     __nv_bfloat16 *W16 = nullptr;  // W1, W2, W3 at their parameter offsets
     long long rows = 0;
     __nv_bfloat16 *Xh = nullptr, *H1h = nullptr, *H2h = nullptr;
@@ -548,16 +561,74 @@ int tc_gemm(XyzLearn &x, cudaStream_t st, int M, int N, int K, const __nv_bfloat
     return ETHER_OK;
 }
 
+constexpr size_t kLtWorkspace = 32u << 20;
+
+// A cuBLASLt plan for H (row-major M x NH, BF16) = bf16(relu(A . W^T + b)), A row-major M x K
+// (BF16), W row-major NH x K; in column-major terms H^T = op_T(W^T) . A^T.  ok = false when
+// cuBLASLt offers no algorithm for the shape.
+XyzLearn::LtPlan &lt_plan(XyzLearn &x, int M, int K) {
+    for (XyzLearn::LtPlan &p : x.plans)
+        if (p.M == M && p.K == K) return p;
+    x.plans.emplace_back();
+    XyzLearn::LtPlan &p = x.plans.back();
+    p.M = M;
+    p.K = K;
+    const cublasOperation_t ta = CUBLAS_OP_T, tb = CUBLAS_OP_N;
+    const cublasLtEpilogue_t epi = CUBLASLT_EPILOGUE_RELU_BIAS;  // bias in D's type (BF16)
+    bool ok = cublasLtMatmulDescCreate(&p.op, CUBLAS_COMPUTE_32F, CUDA_R_32F) == CUBLAS_STATUS_SUCCESS;
+    ok = ok && cublasLtMatmulDescSetAttribute(p.op, CUBLASLT_MATMUL_DESC_TRANSA, &ta, sizeof(ta)) == CUBLAS_STATUS_SUCCESS;
+    ok = ok && cublasLtMatmulDescSetAttribute(p.op, CUBLASLT_MATMUL_DESC_TRANSB, &tb, sizeof(tb)) == CUBLAS_STATUS_SUCCESS;
+    ok = ok && cublasLtMatmulDescSetAttribute(p.op, CUBLASLT_MATMUL_DESC_EPILOGUE, &epi, sizeof(epi)) == CUBLAS_STATUS_SUCCESS;
+    ok = ok && cublasLtMatrixLayoutCreate(&p.a, CUDA_R_16BF, K, NH, K) == CUBLAS_STATUS_SUCCESS;
+    ok = ok && cublasLtMatrixLayoutCreate(&p.b, CUDA_R_16BF, K, M, K) == CUBLAS_STATUS_SUCCESS;
+    ok = ok && cublasLtMatrixLayoutCreate(&p.d, CUDA_R_16BF, NH, M, NH) == CUBLAS_STATUS_SUCCESS;
+    if (ok) {
+        cublasLtMatmulPreference_t pref = nullptr;
+        ok = cublasLtMatmulPreferenceCreate(&pref) == CUBLAS_STATUS_SUCCESS;
+        const size_t ws = kLtWorkspace;
+        ok = ok && cublasLtMatmulPreferenceSetAttribute(pref, CUBLASLT_MATMUL_PREF_MAX_WORKSPACE_BYTES, &ws,
+                                                        sizeof(ws)) == CUBLAS_STATUS_SUCCESS;
+        cublasLtMatmulHeuristicResult_t res;
+        int n = 0;
+        ok = ok && cublasLtMatmulAlgoGetHeuristic(x.lt, p.op, p.a, p.b, p.d, p.d, pref, 1, &res, &n) ==
+                       CUBLAS_STATUS_SUCCESS && n > 0;
+        if (ok) p.algo = res.algo;
+        if (pref) cublasLtMatmulPreferenceDestroy(pref);
+    }
+    p.ok = ok;
+    return p;
+}
+
+// One hidden layer: H16 = bf16(relu(A . W^T + b)), b in BF16 (cuBLASLt epilogue, or GEMM +
+// this file's kernel).
+int hidden_layer(XyzLearn &x, cudaStream_t st, int M, int K, const __nv_bfloat16 *A, const __nv_bfloat16 *W,
+                 const __nv_bfloat16 *bias, __nv_bfloat16 *H16) {
+    XyzLearn::LtPlan &p = lt_plan(x, M, K);
+    if (p.ok && cublasLtMatmulDescSetAttribute(p.op, CUBLASLT_MATMUL_DESC_BIAS_POINTER, &bias, sizeof(bias)) ==
+                    CUBLAS_STATUS_SUCCESS) {
+        const float one = 1.0f, zero = 0.0f;
+        if (cublasLtMatmul(x.lt, p.op, &one, W, p.a, A, p.b, &zero, H16, p.d, H16, p.d, &p.algo, x.lt_ws, kLtWorkspace,
+                           st) == CUBLAS_STATUS_SUCCESS) {
+            x.launches++;
+            return ETHER_OK;
+        }
+        p.ok = false;  // not again for this shape
+    }
+    int rc = tc_gemm(x, st, M, NH, K, A, W, x.Hf);
+    if (rc) return rc;
+    bias_relu_bf16_kernel<<<4 * x.sm_count, 256, 0, st>>>(x.Hf, bias, H16, M);
+    x.launches++;
+    XCUDA(cudaGetLastError());
+    return ETHER_OK;
+}
+
 // The inference network on M rows of Xh (BF16): Zi (no output bias).
 int infer_rows(XyzLearn &x, cudaStream_t st, int M, const __nv_bfloat16 *Xh, float *Z) {
-    int rc = tc_gemm(x, st, M, NH, XNI, Xh, x.W16 + XOFF_W1, x.Hf);
+    int rc = hidden_layer(x, st, M, XNI, Xh, x.W16 + XOFF_W1, x.W16 + XOFF_B1, x.H1h);
     if (rc) return rc;
-    bias_relu_bf16_kernel<<<4 * x.sm_count, 256, 0, st>>>(x.Hf, x.pq + XOFF_B1, x.H1h, M);
-    rc = tc_gemm(x, st, M, NH, NH, x.H1h, x.W16 + XOFF_W2, x.Hf);
+    rc = hidden_layer(x, st, M, NH, x.H1h, x.W16 + XOFF_W2, x.W16 + XOFF_B2, x.H2h);
     if (rc) return rc;
-    bias_relu_bf16_kernel<<<4 * x.sm_count, 256, 0, st>>>(x.Hf, x.pq + XOFF_B2, x.H2h, M);
     rc = tc_gemm(x, st, M, XNO, NH, x.H2h, x.W16 + XOFF_W3, Z);
-    x.launches += 2;
     if (rc) return rc;
     XCUDA(cudaGetLastError());
     return ETHER_OK;
@@ -710,6 +781,16 @@ int xyz_create(ether_ctx *h, const ether_learn_desc *d, XyzLearn **out) {
         xyz_destroy(x);
         return xfail(ETHER_ERR_CUDA, "learned proposal set-up: cublasCreate failed");
     }
+    if (cublasLtCreate(&x->lt) != CUBLAS_STATUS_SUCCESS) {
+        x->lt = nullptr;
+        xyz_destroy(x);
+        return xfail(ETHER_ERR_CUDA, "learned proposal set-up: cublasLtCreate failed");
+    }
+    e = cudaMalloc(&x->lt_ws, kLtWorkspace);
+    if (e != cudaSuccess) {
+        xyz_destroy(x);
+        return xfail(ETHER_ERR_NOMEM, "learned proposal set-up: cuBLASLt workspace");
+    }
     int rc = quantise(*x, c.stream);
     if (rc) {
         xyz_destroy(x);
@@ -723,6 +804,14 @@ void xyz_destroy(XyzLearn *x) {
     if (!x) return;
     if (x->ctx) cudaStreamSynchronize(x->ctx->c.stream);
     if (x->blas) cublasDestroy(x->blas);
+    for (XyzLearn::LtPlan &p : x->plans) {
+        if (p.a) cublasLtMatrixLayoutDestroy(p.a);
+        if (p.b) cublasLtMatrixLayoutDestroy(p.b);
+        if (p.d) cublasLtMatrixLayoutDestroy(p.d);
+        if (p.op) cublasLtMatmulDescDestroy(p.op);
+    }
+    if (x->lt) cublasLtDestroy(x->lt);
+    if (x->lt_ws) cudaFree(x->lt_ws);
     void *ptrs[] = {x->p, x->pq, x->g, x->m, x->v, x->X, x->Y, x->Xb, x->Yb, x->H1, x->H2, x->Z, x->dZ, x->dH1,
                     x->dH2, x->loss, x->W16, x->Xh, x->H1h, x->H2h, x->Hf, x->Zi, x->lstep, x->acc, x->dump};
     for (void *q : ptrs)

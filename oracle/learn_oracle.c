@@ -543,18 +543,20 @@ enum { XNI = 304, XNO = 96 };
 
 int orc_xmlp_n_params(void) { return XNPARAM; }
 
+/* quant 1: BF16 weights and hidden activations (the training kernels); quant 2: also BF16
+ * hidden-layer biases (the inference path, cuBLASLt's bias epilogue in BF16). */
 static void xforward1(const float *p, const float *x, int quant, double *h1, double *h2, double *z) {
     for (int o = 0; o < NH; ++o) {
         double s = 0.0;
         for (int i = 0; i < XNI; ++i) s += wq(p, XOFF_W1 + o * XNI + i, quant) * (double)x[i];
-        s += p[XOFF_B1 + o];
+        s += quant == 2 ? (double)bf16r(p[XOFF_B1 + o]) : (double)p[XOFF_B1 + o];
         s = s > 0.0 ? s : 0.0;
         h1[o] = quant ? (double)bf16r((float)s) : s;
     }
     for (int o = 0; o < NH; ++o) {
         double s = 0.0;
         for (int i = 0; i < NH; ++i) s += wq(p, XOFF_W2 + o * NH + i, quant) * h1[i];
-        s += p[XOFF_B2 + o];
+        s += quant == 2 ? (double)bf16r(p[XOFF_B2 + o]) : (double)p[XOFF_B2 + o];
         s = s > 0.0 ? s : 0.0;
         h2[o] = quant ? (double)bf16r((float)s) : s;
     }

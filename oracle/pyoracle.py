@@ -360,7 +360,9 @@ def xmlp_n_params():
 
 
 def xmlp_forward(params, x, quant=True):
-    """vMF parameters m (B, 96) of the XYZ network on inputs x (B, 304), output bias included."""
+    """vMF parameters m (B, 96) of the XYZ network on inputs x (B, 304), output bias included.
+    quant: False FP64; True BF16 weights and hidden activations; 2 also BF16 hidden biases
+    (the GPU inference path)."""
     p = np.ascontiguousarray(params, dtype=np.float32)
     xx = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 304)
     z = np.zeros((xx.shape[0], 96), dtype=np.float32)
