@@ -796,6 +796,30 @@ int xyz_create(ether_ctx *h, const ether_learn_desc *d, XyzLearn **out) {
         xyz_destroy(x);
         return rc;
     }
+    // one inference pass of every size a sweep uses, on zero inputs: the GEMM libraries load
+    // their kernels and choose their algorithms here, not inside the first learned sweep
+    e = cudaMemsetAsync(x->Xh, 0, (size_t)x->rows * XNI * sizeof(__nv_bfloat16), c.stream);
+    if (e != cudaSuccess) {
+        xyz_destroy(x);
+        return xfail(ETHER_ERR_CUDA, std::string("learned proposal set-up: ") + cudaGetErrorString(e));
+    }
+    {
+        const int per = (int)std::max<long long>(1, std::min<long long>(x->R, x->rows / x->Pc));
+        std::vector<int> sizes = {per * (int)x->Pc};
+        if (x->R % per) sizes.push_back((x->R % per) * (int)x->Pc);
+        for (int M : sizes) {
+            rc = infer_rows(*x, c.stream, M, x->Xh, x->Zi);
+            if (rc) {
+                xyz_destroy(x);
+                return rc;
+            }
+        }
+    }
+    e = cudaStreamSynchronize(c.stream);
+    if (e != cudaSuccess) {
+        xyz_destroy(x);
+        return xfail(ETHER_ERR_CUDA, std::string("learned proposal set-up: ") + cudaGetErrorString(e));
+    }
     *out = x;
     return ETHER_OK;
 }
