@@ -349,12 +349,13 @@ int ether_learn_record_series(ether_learn *learn, int32_t nsteps, int32_t plain_
                               int32_t learned_per_step, double *absM);
 /* Accepted patches per replica since creation (accepted(R)). */
 int ether_learn_get_accepts(ether_learn *learn, uint64_t *accepted);
-/* Parameters: W1(128,128), b1(128), W2(128,128), b2(128), W3(32,128), b3(32), FP32, row =
- * output unit; n = 37152.  Setting them resets the optimiser. */
+/* Parameters: W1(n_inputs,128), b1(128), W2(128,128), b2(128), W3(128,n_outputs),
+ * b3(n_outputs), FP32, row = output unit; n = n_params (Ising 37152, XYZ 67936).  Setting them
+ * resets the optimiser. */
 int ether_learn_get_params(ether_learn *learn, float *params);
 int ether_learn_set_params(ether_learn *learn, const float *params);
-/* The training kernels on a given batch: x(128, B) inputs, y(B) colour-0 spins as bits;
- * loss = mean BCE, grad(37152) = its gradient (no update). */
+/* The training kernels on a given batch (Ising): x(128, B) inputs, y(B) colour-0 spins as
+ * bits; loss = mean BCE, grad(37152) = its gradient (no update). */
 int ether_learn_loss_grad(ether_learn *learn, const float *x, const uint32_t *y, int32_t B,
                           double *loss, float *grad);
 /* The same with targets as floats y(n_outputs, B): Ising 0 / 1 per colour-0 site, XYZ the
@@ -366,8 +367,9 @@ int ether_learn_loss_grad_f(ether_learn *learn, const float *x, const float *y, 
 int ether_learn_forward(ether_learn *learn, const float *x, int32_t B, float *logits);
 /* Widths of the network: inputs, outputs, parameters (Ising 128, 32, 37152). */
 int ether_learn_get_shape(ether_learn *learn, int32_t *n_inputs, int32_t *n_outputs, int32_t *n_params);
-/* Record the logits of the last sweep of the next ether_learn_sweep; get_dump returns them
- * as logits(32, Pc, R, 2) (class, replica, patch of the class). */
+/* Record the network outputs of the last sweep of the next ether_learn_sweep (Ising: the 32
+ * logits; XYZ: the 96 vMF parameters with the output bias); get_dump returns them as
+ * out(n_outputs, Pc, R, 2) (class, replica, patch of the class). */
 int ether_learn_set_dump(ether_learn *learn, int32_t on);
 int ether_learn_get_dump(ether_learn *learn, float *logits);
 typedef struct ether_learn_info {
