@@ -640,11 +640,44 @@ static int sweep_once(Ctx &c) {
 
 int ether::plain_sweep(Ctx &c) { return sweep_once(c); }
 
+static int variant_of(const Ctx &c);
+
 extern "C" int ether_metropolis(ether_ctx *h, int32_t nsweeps, double *accept) {
     if (!h) return fail(ETHER_ERR_ARG, "null context");
     Ctx &c = h->c;
     if (nsweeps < 0) return fail(ETHER_ERR_ARG, "negative sweep count");
     if (!c.beta_set) return fail(ETHER_ERR_STATE, "beta not set (ether_set_beta / ether_set_ladder)");
+    if (accept && nsweeps == 1 && !(c.flags & ETHER_FLAG_NO_GRAPHS)) {
+        // the reference's per-MCS call (Metropolis, then its acceptance): snapshot, sweep,
+        // ratios and the copy to pinned memory captured once per kernel variant and replayed
+        const std::string key = "metropolis1/" + std::to_string(variant_of(c));
+        auto it = c.graphs.find(key);
+        if (it == c.graphs.end()) {
+            cudaGraph_t g = nullptr;
+            CUDA_TRY(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+            cudaError_t ce = cudaMemcpyAsync(c.acc_before, c.acc_count, sizeof(unsigned long long) * c.R,
+                                             cudaMemcpyDeviceToDevice, c.stream);
+            int rc = ce == cudaSuccess ? sweep_once(c) : ETHER_ERR_CUDA;
+            if (rc == ETHER_OK) ce = launch_accept_ratio(c, c.acc_ratio);
+            if (rc == ETHER_OK && ce == cudaSuccess)
+                ce = cudaMemcpyAsync(c.acc_host, c.acc_ratio, sizeof(double) * c.R, cudaMemcpyDeviceToHost, c.stream);
+            const cudaError_t ee = cudaStreamEndCapture(c.stream, &g);
+            if (rc != ETHER_OK || ce != cudaSuccess || ee != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                if (rc != ETHER_OK) return rc;
+                CUDA_TRY(ce != cudaSuccess ? ce : ee);
+            }
+            cudaGraphExec_t ex = nullptr;
+            ce = cudaGraphInstantiate(&ex, g, 0);
+            cudaGraphDestroy(g);
+            CUDA_TRY(ce);
+            it = c.graphs.emplace(key, ex).first;
+        }
+        CUDA_TRY(cudaGraphLaunch(it->second, c.stream));
+        CUDA_TRY(cudaStreamSynchronize(c.stream));
+        std::memcpy(accept, c.acc_host, sizeof(double) * c.R);
+        return ETHER_OK;
+    }
     // acceptance: a device snapshot of the counters, one kernel for the ratios and one copy
     // into pinned memory, so a call that returns them costs a single small D2H and one sync
     if (accept)

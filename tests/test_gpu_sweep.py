@@ -322,3 +322,25 @@ def test_general_lattice_widths_bit_exact(kind, width):
     sw, osys, sp4, ion64, g = xyz_replay(lat, shells, 1.5, 12)
     for k, col in ((1, 0), (2, 1), (3, 2), (5, 3)):
         np.testing.assert_array_equal(g[:, k].astype(np.float32), sp4[:, col])
+
+
+@pytest.mark.parametrize("model", [eg.MODEL_ISING, eg.MODEL_XYZ])
+def test_single_sweep_with_acceptance_graph_equals_direct_launches(model):
+    """ether_metropolis(ctx, 1, accept) replays a captured graph (one per kernel variant);
+    with ETHER_FLAG_NO_GRAPHS it launches directly: same spins and acceptance ratios, also
+    across a change of kernel variant."""
+    lat = eg.simple_cubic((32, 8, 6))
+    runs = []
+    for flags in (0, eg.FLAG_NO_GRAPHS):
+        j = eg.couplings(1, FM, [1.0])
+        sw = eg.Sweep.from_lattice(lat, j, np.array([1.0]), model, replicas=3, seed=17, flags=flags)
+        sw.set_beta([beta_of(k) for k in (3.0, 4.5, 6.0)] if model == eg.MODEL_ISING else
+                    [beta_of(k) for k in (1.0, 1.4, 2.0)])
+        sw.set_spins(random_ising(lat, 3) if model == eg.MODEL_ISING else random_xyz(lat, 3))
+        accs = [sw.metropolis(1) for _ in range(4)]
+        sw.set_variant(81 if model == eg.MODEL_ISING else 5021)
+        accs += [sw.metropolis(1) for _ in range(4)]
+        runs.append((np.array(accs), sw.get_spins(lat.ion, 2)[:, [1, 2, 3]].copy()))
+        sw.close()
+    np.testing.assert_array_equal(runs[0][0], runs[1][0])
+    np.testing.assert_array_equal(runs[0][1], runs[1][1])
