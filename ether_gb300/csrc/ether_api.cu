@@ -1085,6 +1085,10 @@ static int variant_of(const Ctx &c) {
     return (c.ising_persist ? 1000 : 0) + (c.ising_cap ? 2000 : 0) + c.vec_bytes * 10 + c.ising_vpt;
 }
 
+namespace ether {
+int ctx_variant(const Ctx &c) { return variant_of(c); }
+}  // namespace ether
+
 // variant = 1000 (persistent kernel) + 2000 (register cap: four 256-thread blocks per SM)
 //           + 10 * bytes per vector + vectors per thread
 //           or 4000 + 10 * vectors per thread and step + 1 / 4 (register cap): the

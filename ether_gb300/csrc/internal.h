@@ -153,6 +153,7 @@ cudaError_t launch_acc_bin(Ctx &c);
 cudaError_t launch_spiral_measure(Ctx &c);
 int energy_blocks(const Ctx &c);
 int plain_sweep(Ctx &c);  // one Metropolis sweep of every replica (ETHER_OK or an error code)
+int ctx_variant(const Ctx &c);  // the context's kernel variant code (ether_set_variant's numbering)
 void set_error(const std::string &msg);
 int structure_factor_launch(Ctx &c, const double *frac, const int nq[3], const double q0[3],
                             const double dq[3], float *sq_host, float *comp_host, std::string &msg);

@@ -266,6 +266,7 @@ struct ether_batch {
     std::vector<cudaEvent_t> ev_member;
     cudaEvent_t ev_done = nullptr, ev_t0 = nullptr, ev_t1 = nullptr;
     std::vector<BatchMember> h_members;
+    std::vector<int> h_variants;       // members' kernel variants when the graph was built
     BatchMember *d_members = nullptr;
     BatchSeg *d_segs = nullptr;
     size_t seg_capacity = 0;
@@ -401,9 +402,15 @@ int rebuild(ether_batch &b) {
         if (!h->c.beta_set) return bfail(ETHER_ERR_STATE, "batch member without beta (ether_set_beta / ether_set_ladder)");
         hm.push_back(describe(h->c));
     }
-    const bool same = hm.size() == b.h_members.size() &&
+    // a member that runs its own phase kernels is captured with its variant of the moment:
+    // a later ether_set_variant / ether_autotune of that member rebuilds the graph
+    std::vector<int> hv;
+    hv.reserve(b.members.size());
+    for (ether_ctx *h : b.members) hv.push_back(ctx_variant(h->c));
+    const bool same = hm.size() == b.h_members.size() && hv == b.h_variants &&
                       std::memcmp(hm.data(), b.h_members.data(), hm.size() * sizeof(BatchMember)) == 0;
     if (same && !b.dirty) return ETHER_OK;
+    b.h_variants = hv;
     if (b.graph) {
         cudaGraphExecDestroy(b.graph);
         b.graph = nullptr;

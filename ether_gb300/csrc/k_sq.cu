@@ -22,7 +22,9 @@
 // pair cos/sin rows with a lane shuffle and write |S(q)|^2 / N^2 and |S_a(q)| / N.
 //
 // Every mbarrier wait is bounded (%globaltimer, 2 s): on expiry the kernel records an error
-// code, stops issuing work, waits (bounded) for the MMAs it issued, frees its TMEM and exits.
+// code and stops issuing work; the issuing thread waits (bounded) for the TMA copies it
+// started, every thread waits for the MMAs issued so far (the `done` commit), and the TMEM is
+// freed only once those have completed.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -94,7 +96,8 @@ sq_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CU
     uint64_t *full = reinterpret_cast<uint64_t *>(bar_area);
     uint64_t *empty = full + kStages;
     uint64_t *done = empty + kStages;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+    uint64_t *tmab = done + 1;  // per stage: the two B-tile copies have landed
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tmab + kStages);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int tile = blockIdx.x;
@@ -104,8 +107,9 @@ sq_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CU
 
     if (tid == 0) {
         for (int s = 0; s < kStages; ++s) {
-            mbar_init(smem_u32(&full[s]), kProducers + 1);
+            mbar_init(smem_u32(&full[s]), kProducers);
             mbar_init(smem_u32(&empty[s]), 1);
+            mbar_init(smem_u32(&tmab[s]), 1);
         }
         mbar_init(smem_u32(done), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -175,16 +179,26 @@ sq_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CU
             if (f >= 1 && !mbar_wait(smem_u32(&empty[s]), (f - 1) & 1, P.err, 2)) return false;
             uint8_t *b_hi = base + s * stage_bytes + 2 * Smem::a_bytes;
             uint8_t *b_lo = b_hi + b_bytes;
-            mbar_arrive_tx(smem_u32(&full[s]), tx);
-            tma_load_2d(smem_u32(b_hi), &map_hi, kb * kBK, 0, smem_u32(&full[s]));
-            tma_load_2d(smem_u32(b_lo), &map_lo, kb * kBK, 0, smem_u32(&full[s]));
+            mbar_arrive_tx(smem_u32(&tmab[s]), tx);
+            tma_load_2d(smem_u32(b_hi), &map_hi, kb * kBK, 0, smem_u32(&tmab[s]));
+            tma_load_2d(smem_u32(b_lo), &map_lo, kb * kBK, 0, smem_u32(&tmab[s]));
             return true;
         };
         int issued = 0;
-        if (P.nk > 0) ok = issue_tma(0);
+        int tma_next = 0;    // k-blocks whose copies were started: 0 .. tma_next - 1
+        int tma_waited = 0;  // k-blocks whose copies were seen complete: 0 .. tma_waited - 1
+        if (P.nk > 0) {
+            ok = issue_tma(0);
+            tma_next = ok ? 1 : 0;
+        }
         for (int kb = 0; kb < P.nk && ok; ++kb) {
-            if (kb + 1 < P.nk && !issue_tma(kb + 1)) { ok = false; break; }
+            if (kb + 1 < P.nk) {
+                if (!issue_tma(kb + 1)) { ok = false; break; }
+                tma_next = kb + 2;
+            }
             const int s = kb & 1, f = kb >> 1;
+            if (!mbar_wait(smem_u32(&tmab[s]), f & 1, P.err, 3)) { ok = false; break; }
+            tma_waited = kb + 1;
             if (!mbar_wait(smem_u32(&full[s]), f & 1, P.err, 3)) { ok = false; break; }
             asm volatile("tcgen05.fence::after_thread_sync;");
             const uint32_t a_hi = smem_u32(base + s * stage_bytes);
@@ -201,6 +215,10 @@ sq_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CU
             umma_commit(smem_u32(&empty[s]));
             ++issued;
         }
+        // after a failed wait: the copies already started still write into this block's
+        // shared memory, so wait for them (bounded) before the block can exit
+        for (int kb = tma_waited; kb < tma_next; ++kb)
+            mbar_wait(smem_u32(&tmab[kb & 1]), (kb >> 1) & 1, P.err, 5);
         umma_commit(smem_u32(done));  // arrives once everything issued above has completed
     }
 
@@ -246,8 +264,11 @@ sq_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CU
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     if (warp == kProducers / 32) {
+        // the MMAs write the TMEM until `done` arrives: free it only after that (one more
+        // bounded wait if the first one ran out)
+        const bool drained = __all_sync(0xffffffffu, fin || mbar_wait(smem_u32(done), 0, P.err, 6));
         asm volatile("tcgen05.fence::after_thread_sync;");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
+        if (drained) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
     }
 }
 

@@ -22,7 +22,17 @@
 //
 // Set-up.  Host code cannot use the array's name as a device address (it names a host-side
 // stand-in).  The first call on each device, with that device current, looks the address up
-// with cudaGetSymbolAddress and caches it; make that first call before any stream capture.
+// with cudaGetSymbolAddress and caches it.
+//
+// Streams.  Every call ends with cudaStreamSynchronize on the caller's stream, so no call may
+// be made while that stream is being captured into a CUDA graph (the synchronisation would
+// break the caller's capture).
+//
+// Input memory.  `spins` must be memory the current device can address: a device allocation
+// of this device, managed memory, or page-locked host memory mapped for the device.  Anything
+// else (pageable host memory, another device's memory, a pointer the runtime does not know)
+// is rejected with ETHER_ERR_ARG before any kernel is launched, since a kernel given it would
+// fault or read unrelated memory.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -149,6 +159,28 @@ extern "C" int ether_sc_energy_noalloc(int32_t model, const void *spins, const i
     if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
         set_error(std::string("ether_sc_energy_noalloc: cudaGetDevice: ") + cudaGetErrorString(e));
         return ETHER_ERR_NODEV;
+    }
+    {
+        cudaPointerAttributes pa{};
+        e = cudaPointerGetAttributes(&pa, spins);
+        if (e != cudaSuccess) {
+            cudaGetLastError();  // the failed query is not a lasting error: clear it
+            set_error(std::string("ether_sc_energy_noalloc: spins is not a pointer the CUDA "
+                                  "runtime knows: ") + cudaGetErrorString(e));
+            return ETHER_ERR_ARG;
+        }
+        const bool ok = (pa.type == cudaMemoryTypeDevice && pa.device == dev) ||
+                        pa.type == cudaMemoryTypeManaged ||
+                        (pa.type == cudaMemoryTypeHost && pa.devicePointer == spins);
+        if (!ok) {
+            set_error("ether_sc_energy_noalloc: spins must be memory this device can address "
+                      "(its own device memory, managed memory or mapped page-locked host "
+                      "memory); got " +
+                      std::string(pa.type == cudaMemoryTypeUnregistered ? "pageable host memory"
+                                  : pa.type == cudaMemoryTypeDevice ? "another device's memory"
+                                                                    : "unmapped host memory"));
+            return ETHER_ERR_ARG;
+        }
     }
     double *scr;
     {

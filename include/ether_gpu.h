@@ -398,9 +398,11 @@ int ether_learn_get_info(ether_learn *learn, ether_learn_info *info);
  *   get_tot_magnetisation (unit stagger and spin length).  stream: cudaStream_t or NULL.
  * Scratch is 1 MiB of the library's static device memory, shared by all calls: at most 992
  * replicas per call (ETHER_ERR_CAPACITY beyond, before any memory is touched), and calls
- * that overlap on the GPU race.  The
- * first call on a device looks up the scratch address (cudaGetSymbolAddress) and must come
- * before any stream capture.  Returns after the results are in E and M. */
+ * that overlap on the GPU race.  The first call on a device looks up the scratch address
+ * (cudaGetSymbolAddress).  Every call synchronizes `stream` before it returns (the results
+ * are then in E and M), so it must not be made while that stream is being captured into a
+ * CUDA graph.  `spins` that the current device cannot address (pageable host memory,
+ * another device's memory, an unknown pointer) give ETHER_ERR_ARG before any launch. */
 int ether_sc_energy_noalloc(int32_t model, const void *spins, const int32_t L[3],
                             int32_t n_replicas, const double J[3], const double zee[3],
                             double *E, double *M, void *stream);

@@ -73,3 +73,80 @@ def test_noalloc_rejects_more_replicas_than_its_scratch():
                                      R, abi.dptr(J), abi.dptr(J), abi.dptr(E), abi.dptr(M), None)
     assert rc == -5
     assert b"at most 992" in lib.ether_last_error()
+
+
+def _numpy_energy(spins, L, J, zee, model):
+    """get_tot_energy / get_tot_magnetisation of periodic simple-cubic configurations in the
+    reference's site order (x fastest), computed by array rolls: E = sum_i S_i . (J o h_i + z)
+    with h_i the sum of the six neighbours."""
+    R = spins.shape[0]
+    L1, L2, L3 = L
+    if model == eg.MODEL_ISING:
+        s = spins.reshape(R, L3, L2, L1)
+        nb = np.zeros_like(s)
+        for ax in (1, 2, 3):
+            nb += np.roll(s, 1, axis=ax)
+            nb += np.roll(s, -1, axis=ax)
+        bonds = (s.astype(np.int32) * nb).reshape(R, -1).sum(axis=1, dtype=np.int64)
+        tot = s.reshape(R, -1).sum(axis=1, dtype=np.int64)
+        E = J[2] * bonds.astype(np.float64) + zee[2] * tot.astype(np.float64)
+        M = np.zeros((R, 3))
+        M[:, 2] = tot
+        return E, M
+    s = spins[..., :3].astype(np.float64).reshape(R, L3, L2, L1, 3)
+    h = np.zeros_like(s)
+    for ax in (1, 2, 3):
+        h += np.roll(s, 1, axis=ax) + np.roll(s, -1, axis=ax)
+    E = (s * (h * np.asarray(J) + np.asarray(zee))).reshape(R, -1).sum(axis=1)
+    return E, s.reshape(R, -1, 3).sum(axis=1)
+
+
+@pytest.mark.parametrize("model,R", [(eg.MODEL_ISING, 992), (eg.MODEL_XYZ, 5)])
+def test_noalloc_unequal_sides_at_the_block_clamp(model, R):
+    """(40, 36, 50) = 72000 sites: more than 32 blocks of 2048 sites, so the partials use the
+    32-block clamp; for Ising the 992 replicas fill the scratch array to its limit."""
+    lib = abi.load()
+    L = (40, 36, 50)
+    N = int(np.prod(L))
+    rng = np.random.default_rng(5)
+    if model == eg.MODEL_ISING:
+        # biased towards +1 so that E and M are far from zero
+        host = np.where(rng.random((R, N)) < 0.7, 1, -1).astype(np.int8)
+    else:
+        v = rng.normal(size=(R, N, 3)) + np.array([0.0, 0.0, 1.5])
+        v /= np.linalg.norm(v, axis=2, keepdims=True)
+        host = np.concatenate([v, np.zeros((R, N, 1))], axis=2).astype(np.float32)
+    J = np.array([-1e-3, -0.8e-3, -1.2e-3])
+    zee = np.array([0.1e-3, -0.2e-3, 0.3e-3])
+    E_ref, M_ref = _numpy_energy(host, L, J, zee, model)
+    dev = _device_copy(host)
+    Lv = np.array(L, dtype=np.int32)
+    for call in range(2):
+        E = np.full(R, np.nan)
+        M = np.full((R, 3), np.nan)
+        rc = lib.ether_sc_energy_noalloc(model, C.c_void_p(dev.data_ptr()), abi.iptr(Lv), R,
+                                         abi.dptr(J), abi.dptr(zee), abi.dptr(E), abi.dptr(M), None)
+        assert rc == 0, lib.ether_last_error()
+        np.testing.assert_allclose(E, E_ref, rtol=1e-9, atol=1e-8)
+        np.testing.assert_allclose(M, M_ref, rtol=1e-9, atol=1e-6)
+
+
+def test_noalloc_rejects_pageable_host_memory_without_launching():
+    """A host array that was never registered with CUDA is refused by the pointer check that
+    runs before any launch; the call returns ETHER_ERR_ARG and the device stays usable."""
+    lib = abi.load()
+    host = np.ones(4 * 4 * 4, dtype=np.int8)
+    Lv = np.array([4, 4, 4], dtype=np.int32)
+    J = np.zeros(3)
+    E = np.zeros(1)
+    M = np.zeros(3)
+    rc = lib.ether_sc_energy_noalloc(eg.MODEL_ISING, C.c_void_p(host.ctypes.data), abi.iptr(Lv),
+                                     1, abi.dptr(J), abi.dptr(J), abi.dptr(E), abi.dptr(M), None)
+    assert rc == -1
+    assert b"pageable host memory" in lib.ether_last_error()
+    # the library keeps working after the refusal
+    dev = _device_copy(host)
+    rc = lib.ether_sc_energy_noalloc(eg.MODEL_ISING, C.c_void_p(dev.data_ptr()), abi.iptr(Lv),
+                                     1, abi.dptr(J), abi.dptr(J), abi.dptr(E), abi.dptr(M), None)
+    assert rc == 0, lib.ether_last_error()
+    assert M[2] == 64.0
