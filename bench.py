@@ -7,12 +7,15 @@ R = 1024 independent replicas (each its own Philox stream) so the int8 state (26
 larger than the 129 MB L2.  A step is one full sweep (both colour phases) of every replica.
 
   value        spin updates / ns over the timed steps (state resident in HBM, CUDA events)
-  e2e          the same sweeps through the C-ABI from host memory: configuration uploaded at
-               the start, acceptance ratios returned to the host every step (the reference's
-               Metropolis(beta, accept) boundary), replica 0 read back at the end
+  e2e          the same sweeps through the C-ABI with host buffers: every replica's
+               configuration in the reference's ion(0:8, N) layout uploaded before the sweeps
+               (ether_set_spins_batch), the acceptance ratios of all replicas returned to the
+               host every step (the reference's Metropolis(beta, accept) boundary), every
+               replica read back after the last sweep (ether_get_spins_batch)
   roofline     the dominant kernel (one colour phase) at 3 algorithmic bytes per update
   cpu_baseline the oracle's typewriter restatement of src/Metropolis.f90 + get_tot_energy per
-               MCS (what src/ether.f90:172-177 does), one replica per host core
+               MCS (what src/ether.f90:172-177 does), one replica per host core, built with
+               the reference's optimisation flags
 
 components (same JSON line): the 64^3 Heisenberg sweep (48 B per update), the structure
 factor on the tensor cores at the pyrochlore size (16-site cell x 12^3 = 27648 sites, 64
@@ -20,7 +23,8 @@ replicas, 64^3 q-grid), and tau_int(|M|) at T_c with the independent samples per
 implies.
 
 --impl reference times the oracle's CPU restatement on all host cores (the Fortran reference
-cannot be built: no gfortran / MPI on this image or the GPU machine).
+cannot be built: no gfortran / MPI on this image or the GPU machine); that arm never loads the
+product library.
 --model sq times only the structure factor (for profiling).
 --model program times the whole program (ether_run) on a deck (--deck): the 16^3 Ising deck
 (19 temperatures x 10 REPEATs x 5000 MCS) or the 32^3 Heisenberg + overrelaxation deck (29
@@ -48,6 +52,7 @@ KTC_ISING = 4.511      # k_B T_c / J, 3D simple-cubic Ising
 KTC_HEIS = 1.443       # k_B T_c / J, 3D simple-cubic classical Heisenberg
 BYTES_ISING = 3.0      # algorithmic bytes per int8 site update (read own, write own, read neighbours)
 BYTES_HEIS = 48.0      # float4: 16 read own + 16 write own + 16 neighbours
+MODEL_ISING, MODEL_XYZ = 0, 1   # ETHER_MODEL_ISING / ETHER_MODEL_XYZ
 
 
 def _cudart():
@@ -204,18 +209,33 @@ def run_sweeps(model, L, replicas, steps, warmup, rank, world, force_variant=0, 
            "achieved_gbs": achieved_gbs, "bytes_per_update": bpu, "launches": int(launches),
            "clocks": clk, "variant": variant}
     if e2e:
+        # every replica's configuration as the reference holds it, ion(0:8, N) per replica
+        # (72 B per site), uploaded before the sweeps and read back after them through the
+        # C-ABI; the acceptance ratios of all replicas come back to the host every sweep
+        ions = np.empty((R, N, 9))
+        ions[:] = ion
+        sw.set_spins_batch(ions)   # first call: allocates the pinned staging area
+        sw.get_spins_batch(ions)
+        sw.sync()
         acc = None
         t_start = time.perf_counter()
-        sw.set_spins(ion)
+        sw.set_spins_batch(ions)
+        t_set = time.perf_counter()
         for _ in range(steps):
             acc = sw.metropolis(1, accept=True)   # D2H of R doubles every step
-        sw.get_spins(lat.ion, 0)
-        t_e2e = time.perf_counter() - t_start
+        t_run = time.perf_counter()
+        sw.get_spins_batch(ions)
+        t_end = time.perf_counter()
+        t_e2e = t_end - t_start
         esize = 1 if model == eg.MODEL_ISING else 16
         res.update({"e2e": updates / (t_e2e * 1e9) * world,
-                    "h2d": (N * esize) / steps,   # one configuration, replicated on the device
-                    "d2h": 8.0 * R + (N * esize) / steps,
+                    "h2d": (R * N * esize) / steps,   # every replica, once per timed run
+                    "d2h": 8.0 * R + (R * N * esize) / steps,
+                    "e2e_detail": {"steps": steps, "set_spins_batch_s": t_set - t_start,
+                                   "sweeps_s": t_run - t_set, "get_spins_batch_s": t_end - t_run,
+                                   "host_ion_bytes": R * N * 72},
                     "accept_mean": float(np.mean(acc))})
+        del ions
     sw.close()
     return res
 
@@ -572,15 +592,17 @@ def run_pyrochlore_pt(cells=12, replicas=64, mcs=2000, warmup=50, ising=False):
             "n_colours": info.n_colours}
 
 
-def cpu_reference(model, L, mcs, threads, seed=1992):
+def cpu_reference(model, L, mcs, threads, seed=1992, steps=1, warmup=0):
     """The oracle's typewriter restatement of the reference's per-MCS work (Metropolis
-    + get_tot_energy), one replica (temperature) per thread."""
-    import ether_gb300 as eg
+    + get_tot_energy), one replica (temperature) per thread, built with the reference's
+    optimisation flags.  Lattice and couplings come from the oracle's own builders: this arm
+    does not load the product library.  Each step is one bounded sample (`threads` replicas x
+    `mcs` MCS from the initial state); `warmup` untimed steps, then `steps` timed ones."""
     from oracle import pyoracle as po
-    lat = eg.simple_cubic(L)
-    j = eg.couplings(1, [[(1, 1, (-J_MEV, -J_MEV, -J_MEV))]], [1.0])
+    lat = po.ScLattice(L)
+    j = po.sc_couplings((-J_MEV, -J_MEV, -J_MEV))
     osys = po.System.from_lattice(lat, j, np.array([1.0]), model)
-    ktc = KTC_ISING if model == eg.MODEL_ISING else KTC_HEIS
+    ktc = KTC_ISING if model == MODEL_ISING else KTC_HEIS
     beta = 1.0 / (ktc * J_MEV * 1e-3)
     cfg = po.RunCfg(tmcs=mcs, tmcs_eq=mcs, coa=1 << 30, repeat=1, ovrr=0, ovrr_para=0.0,
                     ovrr_mcs=0, seed=seed, itemp=1, rank=0)
@@ -588,17 +610,22 @@ def cpu_reference(model, L, mcs, threads, seed=1992):
     vals = np.zeros(6 * nT)
     acc = np.zeros(nT)
     b = np.full(nT, beta)
-    t = time.perf_counter()
-    po.lib().orc_run_temperatures(osys.p(), osys.ion0.ctypes.data_as(po.PD), nT,
-                                  b.ctypes.data_as(po.PD), C.byref(cfg), threads,
-                                  vals.ctypes.data_as(po.PD), acc.ctypes.data_as(po.PD))
-    dt = time.perf_counter() - t
-    updates = float(lat.N) * mcs * nT
+    times = []
+    for k in range(warmup + steps):
+        t = time.perf_counter()
+        po.timed_lib().orc_run_temperatures(osys.p(), osys.ion0.ctypes.data_as(po.PD), nT,
+                                            b.ctypes.data_as(po.PD), C.byref(cfg), threads,
+                                            vals.ctypes.data_as(po.PD), acc.ctypes.data_as(po.PD))
+        if k >= warmup:
+            times.append(time.perf_counter() - t)
+    dt = float(np.sum(times))
+    updates = float(lat.N) * mcs * nT * steps
     return {"value": updates / (dt * 1e9), "unit": "spin updates/ns", "cores": threads,
-            "kind": "port",
-            "sample": "%d replicas x %d MCS of %d^3 %s, typewriter order, FP64, per-MCS "
-                      "get_tot_energy as src/ether.f90:177 (%.1f s wall)" %
-                      (nT, mcs, L, "Ising" if model == 0 else "Heisenberg", dt),
+            "kind": "port", "ms_per_step": 1e3 * dt / steps,
+            "sample": "%d step(s) of %d replicas x %d MCS of %d^3 %s, typewriter order, FP64, per-MCS "
+                      "get_tot_energy as src/ether.f90:177, built -O3 -fopenmp -funroll-loops "
+                      "-finline-functions -fno-math-errno -fno-trapping-math (%.1f s timed)" %
+                      (steps, nT, mcs, L, "Ising" if model == 0 else "Heisenberg", dt),
             "seconds": dt}
 
 
@@ -660,12 +687,47 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("gloo")
 
-    import ether_gb300 as eg
     peaks = _peaks()
     hbm_peak = peaks.get("hbm_gbs") or 6800.0
     peak_src = "measured" if peaks.get("hbm_gbs") else "fallback"
     bf16_peak = peaks.get("bf16_tflops") or 1900.0
     cores = os.cpu_count() or 1
+
+    model = MODEL_ISING if args.model == "ising" else MODEL_XYZ
+    replicas = args.replicas or (1024 if model == MODEL_ISING else 64)
+    workload = ("plain checkerboard Metropolis, simple-cubic %d^3 %s at kT_c=%.3f J "
+                "(J=1 meV FM, periodic), %d independent replicas per GPU" %
+                (args.L, "Ising int8" if model == 0 else "Heisenberg float4",
+                 KTC_ISING if model == 0 else KTC_HEIS, replicas))
+    state_mb = args.L ** 3 * replicas * (1 if model == 0 else 16) / 1e6
+    config = {"workload": workload, "L": args.L, "replicas": replicas,
+              "sites_per_replica": args.L ** 3, "state_MB": round(state_mb, 1),
+              "l2_policy": "inputs larger than L2 (%.0f MB > 129 MB)" % state_mb,
+              "parallelism": "replicas only (independent chains per GPU)"}
+
+    if args.impl == "reference":
+        # the reference's path on the host cores: the product library is never loaded here
+        if rank != 0:
+            return 0
+        # each step a bounded sample: cores replicas x m MCS, m sized so that the whole
+        # warm-up + timed run stays within a few minutes of host time
+        m = args.cpu_mcs or max(2, min(40, 4000 // (args.steps + args.warmup)))
+        ref = cpu_reference(model, args.L, m, cores, steps=args.steps, warmup=args.warmup)
+        line = {"metric": "spin updates/ns", "value": ref["value"], "unit": "spin updates/ns",
+                "impl": "reference", "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ref["ms_per_step"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": config,
+                "cpu_baseline": {k: ref[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "e2e": {"value": ref["value"], "unit": "spin updates/ns",
+                        "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "note": "Fortran reference not buildable (no gfortran/MPI): its path restated "
+                        "in C (oracle/) and timed on all host cores; a step is one bounded "
+                        "sample of the workload (see cpu_baseline.sample)"}
+        print(json.dumps(line))
+        return 0
+
+    import ether_gb300 as eg
 
     if args.model == "sq":
         if rank != 0:
@@ -730,35 +792,6 @@ def main():
                           "unit": "spin updates/ns", "higher_is_better": True, "detail": r}))
         return 0
 
-    model = eg.MODEL_ISING if args.model == "ising" else eg.MODEL_XYZ
-    replicas = args.replicas or (1024 if model == eg.MODEL_ISING else 64)
-    workload = ("plain checkerboard Metropolis, simple-cubic %d^3 %s at kT_c=%.3f J "
-                "(J=1 meV FM, periodic), %d independent replicas per GPU" %
-                (args.L, "Ising int8" if model == 0 else "Heisenberg float4",
-                 KTC_ISING if model == 0 else KTC_HEIS, replicas))
-    state_mb = args.L ** 3 * replicas * (1 if model == 0 else 16) / 1e6
-    config = {"workload": workload, "L": args.L, "replicas": replicas,
-              "sites_per_replica": args.L ** 3, "state_MB": round(state_mb, 1),
-              "l2_policy": "inputs larger than L2 (%.0f MB > 129 MB)" % state_mb,
-              "parallelism": "replicas only (independent chains per GPU)"}
-
-    if args.impl == "reference":
-        if rank != 0:
-            return 0
-        ref = cpu_reference(model, args.L, args.cpu_mcs or 300, cores)
-        line = {"metric": "spin updates/ns", "value": ref["value"], "unit": "spin updates/ns",
-                "impl": "reference", "n_gpus": args.gpus, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": config,
-                "cpu_baseline": {k: ref[k] for k in ("value", "unit", "cores", "kind", "sample")},
-                "e2e": {"value": ref["value"], "unit": "spin updates/ns",
-                        "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-                "note": "Fortran reference not buildable (no gfortran/MPI): its path restated "
-                        "in C (oracle/) and timed on all host cores"}
-        print(json.dumps(line))
-        return 0
-
     res = run_sweeps(model, args.L, replicas, args.steps, args.warmup, rank, world, args.variant)
     if rank != 0:
         return 0
@@ -782,7 +815,8 @@ def main():
                      "bytes_per_update": res["bytes_per_update"], "phase_ms": res["phase_ms"],
                      "autotuned_variant": res["variant"]},
         "e2e": {"value": res["e2e"], "unit": "spin updates/ns",
-                "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"]},
+                "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"],
+                "detail": res["e2e_detail"]},
         "gpu_launches": res["launches"],
         "clocks": res["clocks"],
         "accept_ratio": res["accept_mean"],
@@ -817,7 +851,7 @@ def main():
         line["components"] = comp
     if not args.no_cpu:
         line["cpu_baseline"] = {k: v for k, v in
-                                cpu_reference(model, args.L, args.cpu_mcs or 300, cores).items()
+                                cpu_reference(model, args.L, args.cpu_mcs or 600, cores).items()
                                 if k in ("value", "unit", "cores", "kind", "sample")}
     print(json.dumps(line))
     return 0

@@ -116,6 +116,8 @@ SIGNATURES = {
     "ether_set_streams": (C.c_int, [P, PU32, PU32]),
     "ether_set_spins": (C.c_int, [P, C.c_int32, PD]),
     "ether_get_spins": (C.c_int, [P, C.c_int32, PD]),
+    "ether_set_spins_batch": (C.c_int, [P, C.c_int32, C.c_int32, PD]),
+    "ether_get_spins_batch": (C.c_int, [P, C.c_int32, C.c_int32, PD]),
     "ether_fresh_spins": (C.c_int, [P]),
     "ether_metropolis": (C.c_int, [P, C.c_int32, PD]),
     "ether_overrelaxation": (C.c_int, [P, C.c_double]),

@@ -10,8 +10,10 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <atomic>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "internal.h"
@@ -199,6 +201,7 @@ void free_ctx(Ctx &c) {
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c.acc_host) cudaFreeHost(c.acc_host);
+    if (c.stage) cudaFreeHost(c.stage);
     for (auto &kv : c.graphs) cudaGraphExecDestroy(kv.second);
     if (c.stream) cudaStreamDestroy(c.stream);
     c = Ctx();
@@ -619,6 +622,155 @@ extern "C" int ether_get_spins(ether_ctx *h, int32_t replica, double *ion) {
         }
     }
     return ETHER_OK;
+}
+
+// ----------------------------------------------------------------------------------------
+// Every replica's ion(0:8, N) at once.  A driver that replaces the reference's MPI ranks by
+// the replica batch holds one ion array per replica: n of them back to back, ion(0:8, N, n).
+// The conversion to and from the device layout (a strided read or write of ion(3) or
+// ion(1:3,5) per 72-byte record, and the colour-major permutation) is the cost of this
+// boundary, so it runs on the host's cores into a pinned staging area, in chunks of whole
+// replicas whose copies start as soon as a chunk is converted.
+namespace {
+constexpr size_t kStageMax = size_t(512) << 20;  // pinned staging, per context
+constexpr size_t kChunkBytes = size_t(4) << 20;  // a copy per ~4 MB of spins
+
+int host_threads() {
+    const unsigned t = std::thread::hardware_concurrency();
+    return (int)std::max(1u, std::min(t, 32u));
+}
+
+int ensure_stage(Ctx &c, size_t bytes) {
+    if (c.stage_bytes >= bytes) return ETHER_OK;
+    if (c.stage) cudaFreeHost(c.stage);
+    c.stage = nullptr;
+    c.stage_bytes = 0;
+    CUDA_TRY(cudaHostAlloc(&c.stage, bytes, cudaHostAllocDefault));
+    c.stage_bytes = bytes;
+    return ETHER_OK;
+}
+
+// Runs f(k) for k in [0, n) on up to host_threads() threads (f must not throw).
+template <class F>
+void parallel_for(int n, F f) {
+    const int T = std::min(n, host_threads());
+    if (T <= 1) {
+        for (int k = 0; k < n; ++k) f(k);
+        return;
+    }
+    std::atomic<int> next{0};
+    std::vector<std::thread> pool;
+    pool.reserve(T);
+    for (int t = 0; t < T; ++t)
+        pool.emplace_back([&]() {
+            for (int k = next.fetch_add(1); k < n; k = next.fetch_add(1)) f(k);
+        });
+    for (auto &th : pool) th.join();
+}
+
+void ion_to_device_layout(const Ctx &c, const double *ion, void *dst) {
+    const int N = c.N;
+    if (c.model == ETHER_MODEL_ISING) {
+        uint8_t *v = static_cast<uint8_t *>(dst);
+        for (int i = 0; i < N; ++i) v[c.storage[i]] = ion[3 + 9 * (size_t)i] > 0.0 ? 1 : 0;
+    } else {
+        float4 *v = static_cast<float4 *>(dst);
+        for (int i = 0; i < N; ++i) {
+            const double *p = ion + 9 * (size_t)i;
+            v[c.storage[i]] = make_float4((float)p[1], (float)p[2], (float)p[3], (float)p[5]);
+        }
+    }
+}
+
+void device_layout_to_ion(const Ctx &c, const void *src, double *ion) {
+    const int N = c.N;
+    if (c.model == ETHER_MODEL_ISING) {
+        const uint8_t *v = static_cast<const uint8_t *>(src);
+        for (int i = 0; i < N; ++i) ion[3 + 9 * (size_t)i] = v[c.storage[i]] ? 1.0 : -1.0;
+    } else {
+        const float4 *v = static_cast<const float4 *>(src);
+        for (int i = 0; i < N; ++i) {
+            double *p = ion + 9 * (size_t)i;
+            const float4 q = v[c.storage[i]];
+            p[1] = q.x; p[2] = q.y; p[3] = q.z; p[5] = q.w;
+        }
+    }
+}
+}  // namespace
+
+static int spins_batch(Ctx &c, int32_t r0, int32_t n, double *ion, bool to_device) {
+    const size_t per_rep = c.model == ETHER_MODEL_ISING ? (size_t)c.N : sizeof(float4) * c.N;
+    const size_t ion_rep = (size_t)9 * c.N;
+    uint8_t *dev = c.model == ETHER_MODEL_ISING ? c.spins : reinterpret_cast<uint8_t *>(c.spins4);
+    const int per_chunk = (int)std::max<size_t>(1, kChunkBytes / per_rep);
+    const int per_pass = (int)std::max<size_t>((size_t)per_chunk, kStageMax / per_rep / per_chunk * per_chunk);
+    {
+        const int rc = ensure_stage(c, per_rep * (size_t)std::min(n, per_pass));
+        if (rc) return rc;
+    }
+    uint8_t *stage = static_cast<uint8_t *>(c.stage);
+    for (int p0 = 0; p0 < n; p0 += per_pass) {
+        const int np = std::min(per_pass, n - p0);
+        const int nchunk = (np + per_chunk - 1) / per_chunk;
+        std::vector<cudaEvent_t> ev(nchunk, nullptr);
+        std::atomic<int> cuda_err{0};
+        if (!to_device) {
+            // device -> staging, one event per chunk; the host converts each as it lands
+            for (int k = 0; k < nchunk; ++k) {
+                const int a = k * per_chunk, b = std::min(np, a + per_chunk);
+                cudaError_t e = cudaMemcpyAsync(stage + per_rep * a, dev + per_rep * (size_t)(r0 + p0 + a),
+                                                per_rep * (b - a), cudaMemcpyDeviceToHost, c.stream);
+                if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming);
+                if (e == cudaSuccess) e = cudaEventRecord(ev[k], c.stream);
+                if (e != cudaSuccess) {
+                    for (cudaEvent_t x : ev)
+                        if (x) cudaEventDestroy(x);
+                    return fail(ETHER_ERR_CUDA, std::string("ether_get_spins_batch: ") + cudaGetErrorString(e));
+                }
+            }
+        }
+        parallel_for(nchunk, [&](int k) {
+            const int a = k * per_chunk, b = std::min(np, a + per_chunk);
+            if (to_device) {
+                for (int r = a; r < b; ++r)
+                    ion_to_device_layout(c, ion + ion_rep * (size_t)(p0 + r), stage + per_rep * r);
+                const cudaError_t e = cudaMemcpyAsync(dev + per_rep * (size_t)(r0 + p0 + a), stage + per_rep * a,
+                                                      per_rep * (b - a), cudaMemcpyHostToDevice, c.stream);
+                if (e != cudaSuccess) cuda_err.store((int)e);
+            } else {
+                const cudaError_t e = cudaEventSynchronize(ev[k]);
+                if (e != cudaSuccess) {
+                    cuda_err.store((int)e);
+                    return;
+                }
+                for (int r = a; r < b; ++r)
+                    device_layout_to_ion(c, stage + per_rep * r, ion + ion_rep * (size_t)(p0 + r));
+            }
+        });
+        for (cudaEvent_t x : ev)
+            if (x) cudaEventDestroy(x);
+        // the staging area is reused by the next pass (and the next call)
+        cudaError_t e = cudaStreamSynchronize(c.stream);
+        if (e == cudaSuccess && cuda_err.load()) e = (cudaError_t)cuda_err.load();
+        if (e != cudaSuccess)
+            return fail(ETHER_ERR_CUDA, std::string(to_device ? "ether_set_spins_batch: " : "ether_get_spins_batch: ") +
+                                            cudaGetErrorString(e));
+    }
+    return ETHER_OK;
+}
+
+extern "C" int ether_set_spins_batch(ether_ctx *h, int32_t r0, int32_t n, const double *ion) {
+    if (!h || !ion) return fail(ETHER_ERR_ARG, "null argument");
+    Ctx &c = h->c;
+    if (r0 < 0 || n <= 0 || (long)r0 + n > c.R) return fail(ETHER_ERR_ARG, "replica range out of bounds");
+    return spins_batch(c, r0, n, const_cast<double *>(ion), true);
+}
+
+extern "C" int ether_get_spins_batch(ether_ctx *h, int32_t r0, int32_t n, double *ion) {
+    if (!h || !ion) return fail(ETHER_ERR_ARG, "null argument");
+    Ctx &c = h->c;
+    if (r0 < 0 || n <= 0 || (long)r0 + n > c.R) return fail(ETHER_ERR_ARG, "replica range out of bounds");
+    return spins_batch(c, r0, n, ion, false);
 }
 
 extern "C" int ether_fresh_spins(ether_ctx *h) {

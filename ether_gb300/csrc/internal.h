@@ -103,6 +103,8 @@ struct Ctx {
     unsigned long long *acc_before = nullptr;  // R: acceptance counts at the start of a call
     double *acc_ratio = nullptr;               // R: device acceptance ratios of a call
     double *acc_host = nullptr;                // R: pinned host copy
+    void *stage = nullptr;                     // pinned staging of ether_{set,get}_spins_batch
+    size_t stage_bytes = 0;
     int32_t *spiral_ptr = nullptr, *spiral_nbr = nullptr;  // spiral partners, CSR in storage order
     long spiral_count = 0;
     double *spiral_part = nullptr;  // R * spiral_blocks * 3: block partials of the spiral sum

@@ -198,6 +198,18 @@ class Sweep:
         abi.check(self.lib.ether_get_spins(self.h, replica, abi.dptr(out)))
         return out
 
+    def set_spins_batch(self, ions, r0=0):
+        """ions: (n, N, 9) -- ion(0:8, N) of replicas r0 .. r0+n-1 back to back."""
+        ions = np.ascontiguousarray(ions, dtype=np.float64)
+        abi.check(self.lib.ether_set_spins_batch(self.h, r0, ions.shape[0], abi.dptr(ions)))
+
+    def get_spins_batch(self, ions, r0=0):
+        """Fills ions (n, N, 9), C-contiguous float64, in place: ion(1:3, :) and ion(5, :) of
+        replicas r0 .. r0+n-1; the other columns keep their values."""
+        assert ions.dtype == np.float64 and ions.flags.c_contiguous
+        abi.check(self.lib.ether_get_spins_batch(self.h, r0, ions.shape[0], abi.dptr(ions)))
+        return ions
+
     # -- reference routines
     def fresh_spins(self):
         abi.check(self.lib.ether_fresh_spins(self.h))

@@ -96,6 +96,18 @@ module ether_gpu_mod
             integer(c_int32_t), value :: replica
             real(c_double), intent(inout) :: ion(0:8, *)
         end function
+        integer(c_int) function ether_set_spins_batch(ctx, r0, n, ion) bind(C, name="ether_set_spins_batch")
+            import :: c_int, c_ptr, c_double, c_int32_t
+            type(c_ptr), value :: ctx
+            integer(c_int32_t), value :: r0, n
+            real(c_double), intent(in) :: ion(0:8, *)
+        end function
+        integer(c_int) function ether_get_spins_batch(ctx, r0, n, ion) bind(C, name="ether_get_spins_batch")
+            import :: c_int, c_ptr, c_double, c_int32_t
+            type(c_ptr), value :: ctx
+            integer(c_int32_t), value :: r0, n
+            real(c_double), intent(inout) :: ion(0:8, *)
+        end function
         integer(c_int) function ether_fresh_spins(ctx) bind(C, name="ether_fresh_spins")
             import :: c_int, c_ptr
             type(c_ptr), value :: ctx

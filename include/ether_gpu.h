@@ -119,6 +119,13 @@ int ether_set_streams(ether_ctx *ctx, const uint32_t *stream, const uint32_t *st
  * (get).  Only ion(1:3,:) and ion(5,:) are read or written. */
 int ether_set_spins(ether_ctx *ctx, int32_t replica, const double *ion);
 int ether_get_spins(ether_ctx *ctx, int32_t replica, double *ion);
+/* The same for replicas r0 .. r0+n-1 at once: ion(0:8, N, n), one reference ion array per
+ * replica back to back (what a driver holds when the replica batch replaces the MPI ranks
+ * of src/ether.f90:112-118, each of which owned one ion).  The layout conversion runs on
+ * the host's cores into pinned staging memory (up to 512 MB, allocated on the first call
+ * and kept by the context), overlapped with the copies.  Returns when the data is in place. */
+int ether_set_spins_batch(ether_ctx *ctx, int32_t r0, int32_t n, const double *ion);
+int ether_get_spins_batch(ether_ctx *ctx, int32_t r0, int32_t n, double *ion);
 
 /* fresh_spins (src/fresh_spins.f90:31-38), called at src/ether.f90:155: Ising flips every
  * spin, XYZ draws a new Marsaglia / ANGLE state, on every replica. */

@@ -909,6 +909,80 @@ void orc_run_temperatures(const orc_sys *sy, const double *ion0, int nT, const d
     (void)nthreads;
 }
 
+/* One round of temperatures with parallel tempering: src/ether.f90:150-214 as the nT MPI
+ * ranks of comm_ei execute it in lockstep (rank k holds temperature slot k, itemp = k + 1),
+ * with src/parallel_tempering.f90:39-108 every `ex` MCS except at measurement steps
+ * (ether.f90:189-198) and swap_count reset every REPEAT (:158).  Per MCS and slot: the OVRR
+ * gate (:163-168), Metropolis in typewriter order, get_tot_energy (:177); then the swap
+ * attempts over the ladder with those raw energies; then observable (:201) on each slot's
+ * configuration.  On an accepted swap the two configurations change slots and each slot
+ * keeps its own random stream (seeded as :154).  Slots are updated on `nthreads` OpenMP
+ * threads between the swap steps.  vals(6, repeat, nT) as orc_run_temperatures; acc[nT]
+ * the acceptance ratio per slot; the number of accepted swaps goes to *n_accepted. */
+void orc_run_ladder(const orc_sys *sy, const double *ion0, int nT, const double *beta,
+                    const orc_run_cfg *cfg, int ex, int nthreads, double *vals, double *acc,
+                    long *n_accepted) {
+    const int N = sy->n_sites;
+    const size_t nb = sizeof(double) * 9 * (size_t)N;
+    const int ovrr_steps = (int)lround(N * cfg->ovrr_para);
+    const int ovrr_on = cfg->ovrr && sy->model == 1 && !sy->zeeman && !sy->sia && cfg->ovrr_mcs > 0;
+    double **cfgs = (double **)malloc(sizeof(double *) * nT);
+    double *E = (double *)malloc(sizeof(double) * nT);
+    int32_t *conf_of_slot = (int32_t *)malloc(sizeof(int32_t) * nT);
+    orc_stream *st = (orc_stream *)malloc(sizeof(orc_stream) * nT);
+    orc_acc *a = (orc_acc *)malloc(sizeof(orc_acc) * nT);
+    for (int k = 0; k < nT; ++k) {
+        cfgs[k] = (double *)malloc(nb);
+        memcpy(cfgs[k], ion0, nb);
+        conf_of_slot[k] = k;
+        acc[k] = 0.0;
+    }
+    long nacc = 0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+    for (int r = 1; r <= cfg->repeat; ++r) {
+        int swap_count = 0;
+        for (int k = 0; k < nT; ++k) {
+            orc_stream_init(&st[k], cfg->seed, (uint32_t)((k + 1) + 175 * cfg->rank + 666 * r));
+            orc_fresh_spins_typewriter(sy, cfgs[conf_of_slot[k]], &st[k]);
+            memset(&a[k], 0, sizeof(orc_acc));
+        }
+        for (int step = 1; step <= cfg->tmcs; ++step) {
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static, 1)
+#endif
+            for (int k = 0; k < nT; ++k) {
+                double *ion = cfgs[conf_of_slot[k]];
+                if (ovrr_on && step % cfg->ovrr_mcs == 0 && step % cfg->coa != 0)
+                    orc_overrelaxation_typewriter(sy, ion, ovrr_steps, &st[k]);
+                acc[k] += orc_metropolis_typewriter(sy, ion, beta[k], &st[k]);
+                E[conf_of_slot[k]] = orc_tot_energy(sy, ion);
+            }
+            if (ex > 0 && step % ex == 0 && step % cfg->coa != 0) {
+                ++swap_count;
+                nacc += orc_parallel_tempering(nT, beta, E, conf_of_slot, swap_count, cfg->seed,
+                                               (uint32_t)r, 0, NULL);
+            }
+            if (step > cfg->tmcs_eq && step % cfg->coa == 0)
+                for (int k = 0; k < nT; ++k) {
+                    double M[3];
+                    orc_tot_magnetisation(sy, cfgs[conf_of_slot[k]], M);
+                    orc_acc_sample(&a[k], E[conf_of_slot[k]], M, N);
+                }
+        }
+        for (int k = 0; k < nT; ++k)
+            orc_acc_average(&a[k], beta[k], N, vals + 6 * ((size_t)cfg->repeat * k + (r - 1)));
+    }
+    for (int k = 0; k < nT; ++k) {
+        acc[k] /= (double)cfg->repeat * cfg->tmcs;
+        free(cfgs[k]);
+    }
+    free(cfgs); free(E); free(conf_of_slot); free(st); free(a);
+    if (n_accepted) *n_accepted = nacc;
+    (void)nthreads;
+}
+
 /* ------------------------------------------------------ moment vectors, spiral state ---- */
 /* get_moment_vectors (src/get_moment_vectors.f90:20-38): mm(3, nsp) = sum over sites of
  * stgg_i * s(species_i) * S_i, sites in order. */

@@ -181,6 +181,12 @@ double orc_run_temperature(const orc_sys *sy, double *ion, double beta, const or
  * initial state shared by all temperatures; vals[6*repeat*nT]; acc[nT]. */
 void orc_run_temperatures(const orc_sys *sy, const double *ion0, int nT, const double *beta,
                           const orc_run_cfg *cfg, int nthreads, double *vals, double *acc);
+/* One round of nT temperatures with parallel tempering every `ex` MCS (0: none), the ranks
+ * of src/ether.f90 in lockstep; configurations move between slots on an accepted swap.
+ * vals[6*repeat*nT], acc[nT], *n_accepted = accepted swaps of the run. */
+void orc_run_ladder(const orc_sys *sy, const double *ion0, int nT, const double *beta,
+                    const orc_run_cfg *cfg, int ex, int nthreads, double *vals, double *acc,
+                    long *n_accepted);
 
 /* ---------------------------------------------------------- own float math ---------- */
 /* exp / sincos used by the FP32 mirror (same algorithm as the GPU kernels: Cody-Waite

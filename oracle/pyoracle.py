@@ -12,6 +12,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SO = os.path.join(HERE, "_build", "libether_oracle.so")
+SO_TIMED = os.path.join(HERE, "_build", "libether_oracle_timed.so")
 
 PD = C.POINTER(C.c_double)
 PF = C.POINTER(C.c_float)
@@ -42,6 +43,7 @@ class RunCfg(C.Structure):
 
 
 _lib = None
+_timed = None
 
 
 def build():
@@ -49,88 +51,149 @@ def build():
 
 
 def lib():
+    """The checker build (every FP32 operation rounded separately)."""
     global _lib
     if _lib is None:
         if not os.path.exists(SO):
             build()
-        L = C.CDLL(SO)
-        L.orc_philox4x32_10.argtypes = [PU, PU, PU]
-        L.orc_supercell.restype = C.c_int
-        L.orc_supercell.argtypes = [C.c_int, PD, PI, PD, PI, C.c_int, PD, PD]
-        L.orc_neighbours_bruteforce.restype = C.c_int
-        L.orc_neighbours_bruteforce.argtypes = [C.c_int, PD, PD, PI, C.c_char_p, C.c_int, PD,
-                                                C.c_double, C.c_int, PI]
-        L.orc_greedy_colouring.restype = C.c_int
-        L.orc_greedy_colouring.argtypes = [C.c_int, C.c_int, C.c_int, PI, PI, PI]
-        L.orc_hamiltonian.restype = C.c_double
-        L.orc_tot_energy.restype = C.c_double
-        L.orc_tot_energy.argtypes = [C.POINTER(Sys), PD]
-        L.orc_tot_magnetisation.argtypes = [C.POINTER(Sys), PD, PD]
-        L.orc_tot_energy_f32.restype = C.c_double
-        L.orc_tot_energy_f32.argtypes = [C.POINTER(Sys), PD, PF]
-        L.orc_tot_magnetisation_f32.argtypes = [C.POINTER(Sys), PD, PF, PD]
-        L.orc_stream_init.argtypes = [C.POINTER(Stream), C.c_uint32, C.c_uint32]
-        L.orc_stream_uniform.restype = C.c_double
-        L.orc_stream_uniform.argtypes = [C.POINTER(Stream)]
-        L.orc_metropolis_typewriter.restype = C.c_double
-        L.orc_metropolis_typewriter.argtypes = [C.POINTER(Sys), PD, C.c_double, C.POINTER(Stream)]
-        L.orc_fresh_spins_typewriter.argtypes = [C.POINTER(Sys), PD, C.POINTER(Stream)]
-        L.orc_overrelaxation_typewriter.argtypes = [C.POINTER(Sys), PD, C.c_int, C.POINTER(Stream)]
-        L.orc_metropolis_colour.restype = C.c_double
-        L.orc_metropolis_colour.argtypes = [C.POINTER(Sys), PD, PF, C.c_int, C.c_double,
-                                            C.c_uint32, C.c_uint32, C.c_uint32, PI, PI, C.c_int]
-        L.orc_overrelax_colour.argtypes = [C.POINTER(Sys), PD, PF, C.c_double, C.c_uint32,
-                                           C.c_uint32, C.c_uint32, PI, PI, C.c_int]
-        L.orc_fresh_spins_colour.argtypes = [C.POINTER(Sys), PD, PF, C.c_uint32, C.c_uint32,
-                                             C.c_uint32]
-        L.orc_parallel_tempering.restype = C.c_int
-        L.orc_parallel_tempering.argtypes = [C.c_int, PD, PD, PI, C.c_int, C.c_uint32,
-                                             C.c_uint32, C.c_int, PI]
-        L.orc_acc_sample.argtypes = [C.POINTER(Acc), C.c_double, PD, C.c_int]
-        L.orc_acc_average.argtypes = [C.POINTER(Acc), C.c_double, C.c_int, PD]
-        L.orc_per_repeat.argtypes = [C.c_int, PD, PD, PD]
-        L.orc_structure_factor.argtypes = [C.c_int, PD, PD, C.c_int, PD, PD]
-        L.orc_run_temperature.restype = C.c_double
-        L.orc_run_temperature.argtypes = [C.POINTER(Sys), PD, C.c_double, C.POINTER(RunCfg), PD]
-        L.orc_run_temperatures.argtypes = [C.POINTER(Sys), PD, C.c_int, PD, C.POINTER(RunCfg),
-                                           C.c_int, PD, PD]
-        L.orc_expf_neg.restype = C.c_float
-        L.orc_expf_neg.argtypes = [C.c_float]
-        L.orc_sincosf.argtypes = [C.c_float, PF, PF]
-        L.orc_moment_vectors.argtypes = [C.POINTER(Sys), PD, PD]
-        L.orc_spiral_pairs.restype = C.c_long
-        L.orc_spiral_pairs.argtypes = [C.c_int, PD, C.c_double, PD, C.c_double, C.c_int, PI]
-        L.orc_spiral_state.restype = C.c_double
-        L.orc_spiral_state.argtypes = [C.c_int, PD, C.c_int, PI, C.c_long]
-        PU8 = C.POINTER(C.c_uint8)
-        L.orc_bf16_round.restype = C.c_float
-        L.orc_bf16_round.argtypes = [C.c_float]
-        L.orc_logf_own.restype = C.c_float
-        L.orc_logf_own.argtypes = [C.c_float]
-        L.orc_mlp_n_params.restype = C.c_int
-        L.orc_mlp_forward.argtypes = [PF, PF, C.c_int, C.c_int, PF]
-        L.orc_mlp_loss_grad.restype = C.c_double
-        L.orc_mlp_loss_grad.argtypes = [PF, PF, PU, C.c_int, C.c_int, PD]
-        L.orc_patch_tables.argtypes = [PI, PI, PI, PI]
-        L.orc_patch_gather.argtypes = [PU8, PI, PI, C.c_int, C.c_int, C.c_int, C.c_float, PF, PU,
-                                       PU, PU]
-        L.orc_patch_btables.argtypes = [C.c_double, PU, PF, PF]
-        L.orc_patch_offsets.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, PI]
-        L.orc_patch_sweep.restype = C.c_long
-        L.orc_patch_sweep.argtypes = [PU8, PI, C.c_double, PF, C.c_uint32, C.c_uint32, C.c_uint32]
-        L.orc_patch_chain.argtypes = [PI, C.c_double, C.c_long, C.c_long, C.c_int, C.c_float,
-                                      C.c_float, C.c_uint32, PD]
-        L.orc_xmlp_n_params.restype = C.c_int
-        L.orc_xmlp_forward.argtypes = [PF, PF, C.c_int, C.c_int, PF]
-        L.orc_xmlp_loss_grad.restype = C.c_double
-        L.orc_xmlp_loss_grad.argtypes = [PF, PF, PF, C.c_int, C.c_int, PD]
-        L.orc_vmf_logpdf.restype = C.c_float
-        L.orc_vmf_logpdf.argtypes = [C.c_float] * 6
-        L.orc_vmf_sample.argtypes = [C.c_float] * 5 + [PF]
-        L.orc_xpatch_sweep.restype = C.c_long
-        L.orc_xpatch_sweep.argtypes = [PF, PI, C.c_float, PF, PF, C.c_uint32, C.c_uint32, C.c_uint32]
-        _lib = L
+        _lib = _bind(C.CDLL(SO), learn=True)
     return _lib
+
+
+def timed_lib():
+    """The same restatement built with the reference's optimisation flags: the CPU baseline
+    that bench.py times (its arithmetic may contract a*b+c; it is never the checker)."""
+    global _timed
+    if _timed is None:
+        if not os.path.exists(SO_TIMED):
+            build()
+        _timed = _bind(C.CDLL(SO_TIMED), learn=False)
+    return _timed
+
+
+def _bind(L, learn):
+    """Declares the argument and result types of the oracle's entry points on L."""
+    L.orc_philox4x32_10.argtypes = [PU, PU, PU]
+    L.orc_supercell.restype = C.c_int
+    L.orc_supercell.argtypes = [C.c_int, PD, PI, PD, PI, C.c_int, PD, PD]
+    L.orc_neighbours_bruteforce.restype = C.c_int
+    L.orc_neighbours_bruteforce.argtypes = [C.c_int, PD, PD, PI, C.c_char_p, C.c_int, PD,
+                                            C.c_double, C.c_int, PI]
+    L.orc_greedy_colouring.restype = C.c_int
+    L.orc_greedy_colouring.argtypes = [C.c_int, C.c_int, C.c_int, PI, PI, PI]
+    L.orc_hamiltonian.restype = C.c_double
+    L.orc_tot_energy.restype = C.c_double
+    L.orc_tot_energy.argtypes = [C.POINTER(Sys), PD]
+    L.orc_tot_magnetisation.argtypes = [C.POINTER(Sys), PD, PD]
+    L.orc_tot_energy_f32.restype = C.c_double
+    L.orc_tot_energy_f32.argtypes = [C.POINTER(Sys), PD, PF]
+    L.orc_tot_magnetisation_f32.argtypes = [C.POINTER(Sys), PD, PF, PD]
+    L.orc_stream_init.argtypes = [C.POINTER(Stream), C.c_uint32, C.c_uint32]
+    L.orc_stream_uniform.restype = C.c_double
+    L.orc_stream_uniform.argtypes = [C.POINTER(Stream)]
+    L.orc_metropolis_typewriter.restype = C.c_double
+    L.orc_metropolis_typewriter.argtypes = [C.POINTER(Sys), PD, C.c_double, C.POINTER(Stream)]
+    L.orc_fresh_spins_typewriter.argtypes = [C.POINTER(Sys), PD, C.POINTER(Stream)]
+    L.orc_overrelaxation_typewriter.argtypes = [C.POINTER(Sys), PD, C.c_int, C.POINTER(Stream)]
+    L.orc_metropolis_colour.restype = C.c_double
+    L.orc_metropolis_colour.argtypes = [C.POINTER(Sys), PD, PF, C.c_int, C.c_double,
+                                        C.c_uint32, C.c_uint32, C.c_uint32, PI, PI, C.c_int]
+    L.orc_overrelax_colour.argtypes = [C.POINTER(Sys), PD, PF, C.c_double, C.c_uint32,
+                                       C.c_uint32, C.c_uint32, PI, PI, C.c_int]
+    L.orc_fresh_spins_colour.argtypes = [C.POINTER(Sys), PD, PF, C.c_uint32, C.c_uint32,
+                                         C.c_uint32]
+    L.orc_parallel_tempering.restype = C.c_int
+    L.orc_parallel_tempering.argtypes = [C.c_int, PD, PD, PI, C.c_int, C.c_uint32,
+                                         C.c_uint32, C.c_int, PI]
+    L.orc_acc_sample.argtypes = [C.POINTER(Acc), C.c_double, PD, C.c_int]
+    L.orc_acc_average.argtypes = [C.POINTER(Acc), C.c_double, C.c_int, PD]
+    L.orc_per_repeat.argtypes = [C.c_int, PD, PD, PD]
+    L.orc_structure_factor.argtypes = [C.c_int, PD, PD, C.c_int, PD, PD]
+    L.orc_run_temperature.restype = C.c_double
+    L.orc_run_temperature.argtypes = [C.POINTER(Sys), PD, C.c_double, C.POINTER(RunCfg), PD]
+    L.orc_run_temperatures.argtypes = [C.POINTER(Sys), PD, C.c_int, PD, C.POINTER(RunCfg),
+                                       C.c_int, PD, PD]
+    L.orc_run_ladder.argtypes = [C.POINTER(Sys), PD, C.c_int, PD, C.POINTER(RunCfg), C.c_int,
+                                 C.c_int, PD, PD, C.POINTER(C.c_long)]
+    L.orc_expf_neg.restype = C.c_float
+    L.orc_expf_neg.argtypes = [C.c_float]
+    L.orc_sincosf.argtypes = [C.c_float, PF, PF]
+    L.orc_moment_vectors.argtypes = [C.POINTER(Sys), PD, PD]
+    L.orc_spiral_pairs.restype = C.c_long
+    L.orc_spiral_pairs.argtypes = [C.c_int, PD, C.c_double, PD, C.c_double, C.c_int, PI]
+    L.orc_spiral_state.restype = C.c_double
+    L.orc_spiral_state.argtypes = [C.c_int, PD, C.c_int, PI, C.c_long]
+    if not learn:
+        return L
+    PU8 = C.POINTER(C.c_uint8)
+    L.orc_bf16_round.restype = C.c_float
+    L.orc_bf16_round.argtypes = [C.c_float]
+    L.orc_logf_own.restype = C.c_float
+    L.orc_logf_own.argtypes = [C.c_float]
+    L.orc_mlp_n_params.restype = C.c_int
+    L.orc_mlp_forward.argtypes = [PF, PF, C.c_int, C.c_int, PF]
+    L.orc_mlp_loss_grad.restype = C.c_double
+    L.orc_mlp_loss_grad.argtypes = [PF, PF, PU, C.c_int, C.c_int, PD]
+    L.orc_patch_tables.argtypes = [PI, PI, PI, PI]
+    L.orc_patch_gather.argtypes = [PU8, PI, PI, C.c_int, C.c_int, C.c_int, C.c_float, PF, PU,
+                                   PU, PU]
+    L.orc_patch_btables.argtypes = [C.c_double, PU, PF, PF]
+    L.orc_patch_offsets.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, PI]
+    L.orc_patch_sweep.restype = C.c_long
+    L.orc_patch_sweep.argtypes = [PU8, PI, C.c_double, PF, C.c_uint32, C.c_uint32, C.c_uint32]
+    L.orc_patch_chain.argtypes = [PI, C.c_double, C.c_long, C.c_long, C.c_int, C.c_float,
+                                  C.c_float, C.c_uint32, PD]
+    L.orc_xmlp_n_params.restype = C.c_int
+    L.orc_xmlp_forward.argtypes = [PF, PF, C.c_int, C.c_int, PF]
+    L.orc_xmlp_loss_grad.restype = C.c_double
+    L.orc_xmlp_loss_grad.argtypes = [PF, PF, PF, C.c_int, C.c_int, PD]
+    L.orc_vmf_logpdf.restype = C.c_float
+    L.orc_vmf_logpdf.argtypes = [C.c_float] * 6
+    L.orc_vmf_sample.argtypes = [C.c_float] * 5 + [PF]
+    L.orc_xpatch_sweep.restype = C.c_long
+    L.orc_xpatch_sweep.argtypes = [PF, PI, C.c_float, PF, PF, C.c_uint32, C.c_uint32, C.c_uint32]
+    return L
+
+
+class ScLattice:
+    """The periodic L1 x L2 x L3 simple-cubic lattice (lattice constant 1, one species, one
+    neighbour shell at distance 1) in the reference's layouts, built without the product
+    library: sites by orc_supercell (generate_supercell, src/generate_supercell.f90:104-132)
+    and the neighbour table nn(1, N, 0:cap, 0:1) in closed form.  getting_nbd
+    (src/getting_nbd.f90:34-78) lists a site's neighbours by increasing site number, each
+    once; with every extent >= 3 the six are distinct (at 2 the search finds one site for two
+    periodic images).  Attributes as the product's Lattice: ion (N, 9), nn (2, cap+1, N, 1),
+    stgg, N, nsh, cap."""
+
+    def __init__(self, L, cap=20):
+        L1, L2, L3 = (L, L, L) if np.isscalar(L) else tuple(L)
+        if min(L1, L2, L3) < 3:
+            raise ValueError("every extent must be >= 3")
+        self.N = N = L1 * L2 * L3
+        self.nsh, self.cap = 1, int(cap)
+        self.ion = np.zeros((N, 9))
+        self.stgg = np.zeros(N)
+        sc = np.array([L1, L2, L3], dtype=np.int32)
+        lib().orc_supercell(1, _d(np.zeros(3)), _i(np.ones(1, dtype=np.int32)), _d(np.eye(3)),
+                            _i(sc), 0, _d(self.ion), _d(self.stgg))
+        i = np.arange(N)
+        x, y, z = i % L1, (i // L1) % L2, i // (L1 * L2)
+        nb = np.stack([(x + 1) % L1 + L1 * (y + L2 * z), (x - 1) % L1 + L1 * (y + L2 * z),
+                       x + L1 * ((y + 1) % L2 + L2 * z), x + L1 * ((y - 1) % L2 + L2 * z),
+                       x + L1 * (y + L2 * ((z + 1) % L3)), x + L1 * (y + L2 * ((z - 1) % L3))], axis=1)
+        nb.sort(axis=1)
+        self.nn = np.zeros((2, self.cap + 1, N, 1), dtype=np.int32)
+        self.nn[0, 0, :, 0] = 6
+        self.nn[0, 1:7, :, 0] = (nb + 1).T
+        self.nn[1, 1:7, :, 0] = (nb + 1).T
+
+
+def sc_couplings(J_mev):
+    """j_exc(1, 1, 1, 3) of one species with spin length 1 and a diagonal J (meV) on the one
+    shell, after parameters.f90 (meV -> eV): layout (3, nsp, nsp, nsh)."""
+    j = np.zeros((3, 1, 1, 1))
+    j[:, 0, 0, 0] = np.asarray(J_mev, dtype=np.float64) / 1000.0
+    return j
 
 
 def _d(a):

@@ -40,3 +40,31 @@ def make_pair(lat, model, shells_J, s=(1.0,), replicas=1, seed=1992, flags=0, pa
                                seed=seed, flags=flags, **kw)
     osys = po.System.from_lattice(lat, j, np.asarray(s, float), model, **kw)
     return sw, osys
+
+
+def assert_same_ensemble(mean, err, ref_mean, ref_err, family_p=0.01):
+    """Statistical parity of two runs' per-temperature observables (E, U_E, C_v, |M|, U_M,
+    chi: src/observables_per_repeat.f90:29-69), each given as the mean over REPEATs and its
+    REPEAT error bar sqrt(sum (x - mean)^2 / (m (m - 1))).
+
+    z = (mean - ref_mean) / sqrt(err^2 + ref_err^2) for each of the K comparisons.  The rule,
+    at a family-wise false-alarm rate of `family_p` (1%):
+      * every |z| <= z*, the two-sided Bonferroni bound Phi^-1(1 - family_p / (2K)), which
+        holds whatever the correlation between the comparisons (the six observables of one
+        temperature share their samples);
+      * sum z^2 <= the (1 - family_p) quantile of chi^2 with K degrees of freedom: a check
+        that no small systematic offset is spread over many comparisons (exact for
+        independent comparisons).
+    Asking every z to lie within 2 sigma would fail about K/20 comparisons by chance alone."""
+    from scipy import stats
+    z = (np.asarray(mean) - np.asarray(ref_mean)) / np.sqrt(np.asarray(err) ** 2 + np.asarray(ref_err) ** 2)
+    assert np.all(np.isfinite(z)), z
+    K = z.size
+    zmax = stats.norm.isf(family_p / (2 * K))
+    chi2 = float((z ** 2).sum())
+    chi2_max = stats.chi2.isf(family_p, K)
+    print("ENSEMBLE K=%d max|z|=%.2f (bound %.2f) chi2=%.1f (bound %.1f)" %
+          (K, np.abs(z).max(), zmax, chi2, chi2_max))
+    assert np.abs(z).max() <= zmax, z
+    assert chi2 <= chi2_max, (chi2, chi2_max, z)
+    return z

@@ -344,3 +344,38 @@ def test_single_sweep_with_acceptance_graph_equals_direct_launches(model):
         sw.close()
     np.testing.assert_array_equal(runs[0][0], runs[1][0])
     np.testing.assert_array_equal(runs[0][1], runs[1][1])
+
+
+@pytest.mark.parametrize("model,L,R", [(eg.MODEL_ISING, (64, 32, 32), 70), (eg.MODEL_XYZ, (32, 16, 20), 60)])
+def test_spins_batch_equals_per_replica_calls(model, L, R):
+    """ether_set_spins_batch / ether_get_spins_batch move ion(0:8, N, n) of many replicas at
+    once (the conversion in chunks of whole replicas on several host threads): the same device
+    state and the same ion records as one ether_set_spins / ether_get_spins per replica.
+    The sizes give two (Ising) and three (XYZ) chunks, the last one partial."""
+    lat = eg.simple_cubic(L)
+    sw, _ = make_pair(lat, model, FM, replicas=R)
+    sw.set_beta(beta_of(4.511 if model == eg.MODEL_ISING else 1.443))
+    mk = random_ising if model == eg.MODEL_ISING else random_xyz
+    ions = np.stack([mk(lat, 500 + r) for r in range(R)])
+    sw.set_spins_batch(ions)
+    cols = [3] if model == eg.MODEL_ISING else [1, 2, 3, 5]
+    for r in (0, 1, R // 2, R - 1):
+        np.testing.assert_array_equal(sw.get_spins(lat.ion, r)[:, cols],
+                                      ions[r][:, cols].astype(np.float32).astype(np.float64))
+    sw.metropolis(2, accept=False)
+    got = np.stack([lat.ion] * R).copy()
+    got[:, :, 0] = -7.0  # columns the call must not touch
+    sw.get_spins_batch(got)
+    assert np.all(got[:, :, 0] == -7.0)
+    for r in range(R):
+        np.testing.assert_array_equal(got[r][:, cols], sw.get_spins(lat.ion, r)[:, cols])
+    # a sub-range: replicas 5 .. 5+k-1
+    k = R - 9
+    sub = ions[:k].copy()
+    sub[:, :, 3] *= -1.0 if model == eg.MODEL_ISING else 1.0
+    sw.set_spins_batch(sub, r0=5)
+    back = np.stack([lat.ion] * k).copy()
+    sw.get_spins_batch(back, r0=5)
+    np.testing.assert_array_equal(back[:, :, cols], sub[:, :, cols].astype(np.float32).astype(np.float64))
+    np.testing.assert_array_equal(sw.get_spins(lat.ion, 4)[:, cols], got[4][:, cols])
+    sw.close()

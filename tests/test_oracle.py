@@ -186,3 +186,40 @@ def test_per_repeat_matches_formula():
                             mean.ctypes.data_as(po.PD), err.ctypes.data_as(po.PD))
     np.testing.assert_allclose(mean, vals.mean(0))
     np.testing.assert_allclose(err, vals.std(0, ddof=1) / math.sqrt(5))
+
+
+@pytest.mark.parametrize("L", [3, 4, (5, 3, 4), (3, 6, 5)])
+def test_closed_form_simple_cubic_equals_bruteforce_getting_nbd(L):
+    """The oracle's own simple-cubic builder (used by the CPU baseline, which must not load the
+    product library) gives the same ion and nn arrays as the brute-force restatement of
+    getting_nbd / search_nbd."""
+    lat = po.ScLattice(L)
+    sc = np.array([L] * 3 if np.isscalar(L) else L, dtype=np.int32)
+    N = int(np.prod(sc))
+    ion = np.zeros((N, 9))
+    po.lib().orc_supercell(1, po._d(np.zeros(3)), po._i(np.ones(1, dtype=np.int32)),
+                           po._d(np.eye(3)), po._i(sc), 0, po._d(ion), None)
+    nn = np.zeros((2, 21, N, 1), dtype=np.int32)
+    rc = po.lib().orc_neighbours_bruteforce(N, po._d(ion), po._d(np.eye(3)), po._i(sc), b"ccc", 1,
+                                            po._d(np.array([1.0])), 1e-5, 20, po._i(nn))
+    assert rc == 0
+    np.testing.assert_array_equal(lat.ion, ion)
+    np.testing.assert_array_equal(lat.nn, nn)
+
+
+def test_timed_build_computes_the_same_energies():
+    """The CPU baseline's build (the reference's optimisation flags) and the checker build
+    agree on get_tot_energy to rounding."""
+    lat = po.ScLattice(6)
+    j = po.sc_couplings((-1.0, -1.0, -1.0))
+    for model in (0, 1):
+        osys = po.System.from_lattice(lat, j, np.array([1.0]), model)
+        rng = np.random.default_rng(model)
+        ion = lat.ion.copy()
+        v = rng.normal(size=(lat.N, 3))
+        ion[:, 1:4] = v / np.linalg.norm(v, axis=1, keepdims=True) if model else 0.0
+        if not model:
+            ion[:, 3] = rng.choice([-1.0, 1.0], size=lat.N)
+        a = po.lib().orc_tot_energy(osys.p(), po._d(ion))
+        b = po.timed_lib().orc_tot_energy(osys.p(), po._d(ion))
+        assert b == pytest.approx(a, rel=1e-12)
