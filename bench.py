@@ -551,9 +551,10 @@ def run_program(deck="c1_ising_16", repeats=2):
 
 def run_pyrochlore_pt(cells=12, replicas=64, mcs=2000, warmup=50, ising=False):
     """The frustrated Heisenberg configuration: pyrochlore 16-site cell x 12^3 (27648 sites),
-    J1 = +1 meV (antiferromagnetic in ETHER's sign) and J2 = -0.1 meV, single-ion anisotropy
-    D = (0, 0, -0.2) meV on every site (the reference's per-species diagonal form), Zeeman
-    H = (0, 0, 1) T with g = 2, 64 replicas on a geometric 1-50 K ladder, PT every 11 MCS,
+    J1 = +1 meV (antiferromagnetic in ETHER's sign) and J2 = -0.1 meV, easy-axis single-ion
+    anisotropy D = -0.2 meV along each site's local <111> axis (sia_local; the reference's
+    anisotropy is diagonal per species and cannot express it), Zeeman H = (0, 0, 1) T with
+    g = 2, 64 replicas on a geometric 1-50 K ladder, PT every 11 MCS,
     measured every 10 MCS: ether_mcs timed with CUDA events.  ising: the same lattice, ladder
     and schedule for the Ising model (J1 = -1 meV, ferromagnetic as the reference's pyrochlore
     example, and J2; Zeeman field, no anisotropy)."""
@@ -565,9 +566,9 @@ def run_pyrochlore_pt(cells=12, replicas=64, mcs=2000, warmup=50, ising=False):
                                    seed=1992, zeeman=True, h=(0.0, 0.0, 1.0), g_factor=2.0)
     else:
         j = eg.couplings(1, [[(1, 1, (1.0, 1.0, 1.0))], [(1, 1, (-0.1, -0.1, -0.1))]], [1.0])
-        sia = np.array([[0.0, 0.0, -0.2e-3]])
+        sia_local = np.concatenate([eg.local_111_axes(lat), np.full((lat.N, 1), -0.2e-3)], axis=1)
         sw = eg.Sweep.from_lattice(lat, j, np.array([1.0]), eg.MODEL_XYZ, replicas=replicas, seed=1992,
-                                   zeeman=True, h=(0.0, 0.0, 1.0), g_factor=2.0, sia=True, sia_vec=sia)
+                                   zeeman=True, h=(0.0, 0.0, 1.0), g_factor=2.0, sia_local=sia_local)
     temps = np.geomspace(1.0, 50.0, replicas)
     sw.set_ladder(1.0 / (eg.KB_EV * temps))
     sw.set_spins(lat.ion)
@@ -587,7 +588,7 @@ def run_pyrochlore_pt(cells=12, replicas=64, mcs=2000, warmup=50, ising=False):
     sw.close()
     return {"workload": "pyrochlore 16 x %d^3 = %d sites, %s, 64-replica geometric ladder 1-50 K, "
                         "PT every 11 MCS, ether_mcs" % (cells, lat.N, "Ising, J1/J2, Zeeman" if ising
-                                                         else "Heisenberg, J1/J2, SIA, Zeeman"),
+                                                         else "Heisenberg, J1/J2, local <111> SIA, Zeeman"),
             "mcs": mcs, "ms": ms, "value": ups / (ms * 1e6), "unit": "spin updates/ns",
             "n_colours": info.n_colours}
 

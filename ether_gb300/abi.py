@@ -44,7 +44,7 @@ class Desc(C.Structure):
         ("j_exc", C.POINTER(C.c_double)), ("sia_vec", C.POINTER(C.c_double)),
         ("s", C.POINTER(C.c_double)), ("stgg", C.POINTER(C.c_double)),
         ("n_replicas", C.c_int32), ("seed", C.c_uint32), ("sc", C.c_int32 * 3),
-        ("basis", C.c_int32), ("flags", C.c_int32),
+        ("basis", C.c_int32), ("flags", C.c_int32), ("sia_local", C.POINTER(C.c_double)),
     ]
 
 

@@ -52,7 +52,7 @@ def build(verbose=False):
         logs = list(ex.map(_run, jobs))
     objs = [os.path.join(BUILD, f + ".o") for f in CU + CXX]
     tmp = OUT + ".tmp"
-    _run([nvcc, *ARCH, "-shared", "-cudart", "shared", "-o", tmp, *objs, "-lcublasLt", "-lcublas", "-Xlinker", "--no-undefined"])
+    _run([nvcc, *ARCH, "-shared", "-cudart", "shared", "-o", tmp, *objs, "-Xlinker", "--no-undefined"])
     os.replace(tmp, OUT)
     if verbose:
         for l in logs:

@@ -197,7 +197,7 @@ void free_ctx(Ctx &c) {
                     c.step, c.ovrr_step, c.fresh_call, c.acc_count, c.E, c.M, c.sums,
                     c.partials, c.pt_accepts, c.swap_dev, c.copy_from, c.err, c.spiral_ptr,
                     c.spiral_nbr, c.acc_before, c.acc_ratio, c.spiral_part, c.spiral_sums,
-                    c.acc_slot, c.acc_mark};
+                    c.acc_slot, c.acc_mark, c.t.sia_cls, c.t.sia_ax};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c.acc_host) cudaFreeHost(c.acc_host);
@@ -240,6 +240,7 @@ extern "C" int ether_create(const ether_desc *d, ether_ctx **out) {
     c.dphi = d->dphi;
     c.zeeman = d->zeeman ? 1 : 0;
     c.sia = (d->sia && d->model == ETHER_MODEL_XYZ) ? 1 : 0;
+    c.sia_local = (d->sia_local && d->model == ETHER_MODEL_XYZ) ? 1 : 0;
     for (int k = 0; k < 3; ++k) c.h[k] = d->h[k];
     c.g = d->g_factor;
     c.mb = d->mb;
@@ -363,6 +364,28 @@ extern "C" int ether_create(const ether_desc *d, ether_ctx **out) {
         }
     }
 
+    // ----- local-axis anisotropy: distinct (a, D) in FP32 as classes, one byte per site
+    std::vector<float4> sia_ax;
+    std::vector<uint8_t> sia_site;
+    if (c.sia_local) {
+        std::map<std::vector<float>, int> cls;
+        sia_site.assign(N, 0);
+        for (int i = 0; i < N; ++i) {
+            const double *a = d->sia_local + 4 * (size_t)i;
+            for (int k = 0; k < 4; ++k)
+                if (!std::isfinite(a[k])) return bail(fail(ETHER_ERR_ARG, "sia_local is not finite at site " + std::to_string(i + 1)));
+            const std::vector<float> key = {(float)a[0], (float)a[1], (float)a[2], (float)a[3]};
+            auto it = cls.find(key);
+            if (it == cls.end()) {
+                if (cls.size() == 256)
+                    return bail(fail(ETHER_ERR_CAPACITY, "sia_local: more than 256 distinct (axis, D) pairs"));
+                it = cls.emplace(key, (int)cls.size()).first;
+                sia_ax.push_back(make_float4(key[0], key[1], key[2], key[3]));
+            }
+            sia_site[i] = (uint8_t)it->second;
+        }
+    }
+
     // ----- CSR in storage order
     std::vector<int32_t> row_ptr(N + 1, 0), nbr, wstr;
     std::vector<uint16_t> jidx;
@@ -409,6 +432,12 @@ extern "C" int ether_create(const ether_desc *d, ether_ctx **out) {
     TRY(dev_upload(c, &c.t.zee, zee));
     TRY(dev_upload(c, &c.t.zeed, zeed));
     TRY(dev_upload(c, &c.t.D, D));
+    if (c.sia_local) {
+        std::vector<uint8_t> scls(N);
+        for (int s = 0; s < N; ++s) scls[s] = sia_site[c.site_of_storage[s]];
+        TRY(dev_upload(c, &c.t.sia_cls, scls));
+        TRY(dev_upload(c, &c.t.sia_ax, sia_ax));
+    }
     TRY(dev_upload(c, &c.t.mweight, mw));
     TRY(dev_upload(c, &c.t.site_of_storage, c.site_of_storage));
     {
@@ -1060,7 +1089,8 @@ extern "C" int ether_mcs(ether_ctx *h, const ether_schedule *sch, int32_t step0,
     if (!c.beta_set) return fail(ETHER_ERR_STATE, "beta not set");
     if (sch->coa <= 0 || nsteps < 0 || step0 < 0)
         return fail(ETHER_ERR_ARG, "coa must be positive, step0 and nsteps >= 0");
-    const bool ovrr_on = sch->ovrr && c.model == ETHER_MODEL_XYZ && !c.zeeman && !c.sia && sch->ovrr_mcs > 0;
+    const bool ovrr_on = sch->ovrr && c.model == ETHER_MODEL_XYZ && !c.zeeman && !c.sia && !c.sia_local &&
+                         sch->ovrr_mcs > 0;
     const bool pt_on = sch->pt && sch->exchange_interval > 0;
     if (pt_on && !(c.flags & ETHER_FLAG_PT_REFERENCE_COPY) && c.n_slots < 2)
         return fail(ETHER_ERR_STATE, "PT needs a ladder of at least two slots");
@@ -1279,7 +1309,8 @@ static bool apply_variant(Ctx &c, int variant) {
 // The simple-cubic XYZ kernel's variants timed on both colour phases (three sweeps each);
 // the configuration and acceptance counters are restored afterwards.
 static int autotune_xyz(Ctx &c, int32_t *variant, float *best_ms) {
-    const std::vector<long> key = {c.model, c.L[0], c.L[1], c.L[2], c.R, (long)c.zeeman, (long)c.sia, (long)c.angle};
+    const std::vector<long> key = {c.model, c.L[0], c.L[1], c.L[2], c.R, (long)c.zeeman, (long)(c.sia || c.sia_local),
+                                   (long)c.angle};
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_tune_cache.find(key);

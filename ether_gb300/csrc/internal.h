@@ -49,11 +49,14 @@ struct DevTables {
     uint16_t *ell_deg = nullptr;  // N: neighbours of a storage index
     int2 *ell_desc = nullptr;     // per colour: (offset of its ELL block, entries per rank)
     float4 *J4 = nullptr;         // nJ: (Jxx, Jyy, Jzz, 0) in FP32
+    uint8_t *sia_cls = nullptr;   // N: local-axis anisotropy class of a storage index
+    float4 *sia_ax = nullptr;     // classes: (a_x, a_y, a_z, D) in FP32
 };
 
 struct Ctx {
     // configuration
     int N = 0, nsp = 0, nsh = 0, cap = 0, model = 0, angle = 0, zeeman = 0, sia = 0;
+    int sia_local = 0;  // per-site local-axis anisotropy classes present (XYZ)
     double dphi = 0, h[3] = {0, 0, 0}, g = 0, mb = 0;
     int R = 0;
     uint32_t seed = 0;
@@ -156,6 +159,7 @@ cudaError_t launch_spiral_measure(Ctx &c);
 int energy_blocks(const Ctx &c);
 int plain_sweep(Ctx &c);  // one Metropolis sweep of every replica (ETHER_OK or an error code)
 int ctx_variant(const Ctx &c);  // the context's kernel variant code (ether_set_variant's numbering)
+void *tma_encode_tiled_fn();    // cuTensorMapEncodeTiled (PFN_cuTensorMapEncodeTiled_v12000), or null
 void set_error(const std::string &msg);
 int structure_factor_launch(Ctx &c, const double *frac, const int nq[3], const double q0[3],
                             const double dq[3], float *sq_host, float *comp_host, std::string &msg);

@@ -350,6 +350,9 @@ BatchMember describe(const Ctx &c) {
     m.J4 = c.t.J4;
     m.P.zeeman = c.zeeman;
     m.P.sia = c.sia;
+    m.P.sia_local = c.sia_local;
+    m.P.sia_cls = c.t.sia_cls;
+    m.P.sia_ax = c.t.sia_ax;
     m.P.angle = c.angle;
     m.P.dphi = (float)c.dphi;
     m.P.species = c.t.species;
@@ -390,8 +393,8 @@ int class_of(const BatchMember &m) {
         case kBIsing8: return kCIsing8;
         case kBIsing4: return kCIsing4;
         case kBIsingEll: return kCIsingEll;
-        case kBXyzSc: return m.P.zeeman || m.P.sia || m.P.angle ? kCXyzScG : kCXyzScX;
-        default: return m.P.zeeman || m.P.sia || m.P.angle ? kCXyzEllG : kCXyzEllX;
+        case kBXyzSc: return m.P.zeeman || m.P.sia || m.P.sia_local || m.P.angle ? kCXyzScG : kCXyzScX;
+        default: return m.P.zeeman || m.P.sia || m.P.sia_local || m.P.angle ? kCXyzEllG : kCXyzEllX;
     }
 }
 

@@ -8,9 +8,9 @@
 //   * network: input = the 96 boundary spins (3 components each, BF16-rounded) and
 //     beta (Jxx, Jyy, Jzz), zero-padded to 304; 128 -> 128 (ReLU, BF16 activations) -> 96;
 //     outputs 3k .. 3k+2 (+ bias) are the von Mises-Fisher parameter m_k of A-site k;
-//     inference: the three layers as cuBLAS BF16 x BF16 tensor-core GEMMs (plain library
-//     GEMMs; layers 1 and 2 with cuBLASLt's bias + ReLU epilogue writing BF16, else this
-//     file's bias / ReLU / BF16 kernel; hidden biases in BF16 there); training on the FP32
+//     inference: xmlp_kernel, the three layers on the tensor cores (tcgen05, TMA-loaded
+//     inputs, weights resident in shared memory, FP32 accumulators in tensor memory; the
+//     hidden layers' bias (BF16) + ReLU + BF16 rounding in the epilogue); training on the FP32
 //     GEMM of k_learn.cu;
 //   * proposal: A-site k ~ vMF(m_k) (Wood's exact sampler on the sphere, own log / exp /
 //     sincos); then every B-site from its exact heat-bath conditional vMF(-beta g), g = J o
@@ -29,12 +29,13 @@
 #include <string>
 #include <vector>
 
-#include <cublasLt.h>
-#include <cublas_v2.h>
+#include <cuda.h>
+#include <cudaTypedefs.h>
 
 #include "internal.h"
 #include "learn_common.cuh"
 #include "rng_math.cuh"
+#include "tc_util.cuh"
 
 namespace ether {
 namespace learn {
@@ -280,27 +281,6 @@ __global__ void xbatch_kernel(const __nv_bfloat16 *__restrict__ X, const float *
     for (int i = threadIdx.x; i < XNO; i += blockDim.x) Yb[(size_t)b * XNO + i] = Y[(size_t)row * XNO + i];
 }
 
-// H16 = bf16(max(H + b, 0)), b in BF16 (the cuBLASLt epilogue's operands), rows x NH, eight
-// columns per thread (two 16-byte loads, one 16-byte store)
-__global__ void bias_relu_bf16_kernel(const float *__restrict__ Hm, const __nv_bfloat16 *__restrict__ b16,
-                                      __nv_bfloat16 *__restrict__ H16, long long rows) {
-    const long long nv = rows * (NH / 8);
-    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv; v += (long long)gridDim.x * blockDim.x) {
-        const int c0 = (int)(v % (NH / 8)) * 8;
-        const float4 a0 = reinterpret_cast<const float4 *>(Hm)[2 * v], a1 = reinterpret_cast<const float4 *>(Hm)[2 * v + 1];
-        const float h[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-        uint32_t w[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const __nv_bfloat162 pr =
-                __floats2bfloat162_rn(fmaxf(h[2 * j] + __bfloat162float(b16[c0 + 2 * j]), 0.0f),
-                                      fmaxf(h[2 * j + 1] + __bfloat162float(b16[c0 + 2 * j + 1]), 0.0f));
-            w[j] = *reinterpret_cast<const uint32_t *>(&pr);
-        }
-        reinterpret_cast<uint4 *>(H16)[v] = make_uint4(w[0], w[1], w[2], w[3]);
-    }
-}
-
 __global__ void to_bf16_kernel(const float *__restrict__ q, __nv_bfloat16 *__restrict__ o, int n) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) o[i] = __float2bfloat16_rn(q[i]);
 }
@@ -441,6 +421,222 @@ __global__ void __launch_bounds__(256, 4) xpatch_kernel(XPatchParams P, const fl
     }
 }
 
+// ------------------------------------------------------------ inference network ----
+// xmlp_kernel: Z = W3 . h2, h2 = bf16(relu(W2 . h1 + b2)), h1 = bf16(relu(W1 . x + b1)) for
+// 128-row tiles of X (M x 304, BF16) on the fifth-generation tensor cores.  A persistent CTA of
+// four warps keeps the three weight matrices in shared memory (the image packed by
+// xpack_kernel: BF16, K-major, 128-byte swizzle, W1's K zero-padded to 320) and per tile:
+//   * thread 0 loads the X tile with five TMA copies (64 columns each; the columns past 304
+//     and the rows past M read as zeros), then issues each layer's tcgen05.mma chain (K = 16
+//     per instruction, FP32 accumulators in tensor memory: layer 1 in columns 0-127, layer 2
+//     in 128-255, layer 3 in 0-95) and commits it to an mbarrier;
+//   * thread p owns row p = TMEM lane p: after layers 1 and 2 it reads its 128 accumulators
+//     (tcgen05.ld), adds the BF16 bias, applies ReLU, rounds to BF16 and writes the next
+//     layer's A operand over the X tile; after layer 3 it writes its 96 outputs to Z;
+//   * once layer 3 has read its operand, the next tile's X copies start, under the last
+//     epilogue.
+// Every wait is bounded (2 s of %globaltimer): on expiry the kernel records an error code,
+// stops, waits (bounded) for the copies and MMAs it started, and frees its tensor memory.
+constexpr int XKT1 = 5;  // 64-column K-tiles of layer 1
+constexpr int XIMG_W1 = 0, XIMG_W2 = XIMG_W1 + XKT1 * 16384, XIMG_W3 = XIMG_W2 + 2 * 16384,
+              XIMG_B = XIMG_W3 + 2 * XNO * 128, XIMG_BYTES = XIMG_B + 2 * NH * 4;
+constexpr int XSM_A = (XIMG_BYTES + 1023) / 1024 * 1024;  // X tile, then h1 / h2
+constexpr int XSM_BAR = XSM_A + XKT1 * 16384;
+constexpr int XSM_BYTES = XSM_BAR + 64 + 1024;            // + barriers, + alignment slack
+constexpr uint32_t kXTileBytes = XKT1 * 16384;
+static_assert(XSM_BYTES <= 232448, "xmlp_kernel shared memory above the 227 KB opt-in limit");
+
+// the inference image from the BF16 parameters: W1, W2, W3 swizzled, b1, b2 as FP32
+__global__ void xpack_kernel(const __nv_bfloat16 *__restrict__ W16, uint8_t *__restrict__ img) {
+    const int total = NH * XNI + NH * NH + XNO * NH;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        int base, rows, off, K, idx = e;
+        if (idx < NH * XNI) { base = XIMG_W1; rows = NH; off = XOFF_W1; K = XNI; }
+        else if ((idx -= NH * XNI) < NH * NH) { base = XIMG_W2; rows = NH; off = XOFF_W2; K = NH; }
+        else { idx -= NH * NH; base = XIMG_W3; rows = XNO; off = XOFF_W3; K = NH; }
+        const int n = idx / K, k = idx % K;
+        const uint32_t o = (uint32_t)base + (uint32_t)(k >> 6) * (uint32_t)(rows * 128) + tc::swz(n, k & 63);
+        *reinterpret_cast<__nv_bfloat16 *>(img + o) = W16[off + idx];
+    }
+    float *bf = reinterpret_cast<float *>(img + XIMG_B);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 2 * NH; i += gridDim.x * blockDim.x)
+        bf[i] = __bfloat162float(W16[(i < NH ? XOFF_B1 : XOFF_B2 - NH) + i]);
+}
+
+__device__ __forceinline__ void xtma_load(uint32_t dst, const CUtensorMap *map, int c0, int c1, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(dst), "l"(map), "r"(c0), "r"(c1), "r"(bar) : "memory");
+}
+
+__global__ void __launch_bounds__(128, 1)
+xmlp_kernel(const __grid_constant__ CUtensorMap xmap, const uint8_t *__restrict__ img, float *__restrict__ Z, int M,
+            int *__restrict__ err) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t *bar_x = reinterpret_cast<uint64_t *>(base + XSM_BAR);  // the X tile has landed
+    uint64_t *bar_m = bar_x + 1;                                     // a layer's MMAs are done
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_m + 1);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int ntiles = (M + 127) / 128;
+
+    {  // weights and biases into shared memory (plain 16-byte copies of the swizzled image)
+        const uint4 *src = reinterpret_cast<const uint4 *>(img);
+        uint4 *dst = reinterpret_cast<uint4 *>(base);
+        for (int i = tid; i < XIMG_BYTES / 16; i += 128) dst[i] = __ldg(src + i);
+    }
+    if (tid == 0) {
+        tc::mbar_init(tc::smem_u32(bar_x), 1);
+        tc::mbar_init(tc::smem_u32(bar_m), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(tc::smem_u32(tmem_slot)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    tc::fence_proxy_async();
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    const uint32_t sA = tc::smem_u32(base + XSM_A);
+    const uint32_t sW1 = tc::smem_u32(base + XIMG_W1), sW2 = tc::smem_u32(base + XIMG_W2),
+                   sW3 = tc::smem_u32(base + XIMG_W3);
+    const float *bias = reinterpret_cast<const float *>(base + XIMG_B);
+    uint8_t *arow = base + XSM_A;
+
+    auto load_x = [&](int tile) {  // thread 0
+        tc::mbar_arrive_tx(tc::smem_u32(bar_x), kXTileBytes);
+#pragma unroll
+        for (int kt = 0; kt < XKT1; ++kt)
+            xtma_load(sA + (uint32_t)kt * 16384u, &xmap, 64 * kt, 128 * tile, tc::smem_u32(bar_x));
+    };
+    // one layer: K-steps of 16 over nkt 64-column tiles of A and B (B tiles of n rows), into
+    // TMEM column dcol, committed to bar_m
+    auto layer = [&](uint32_t sB, int n, int ksteps, uint32_t dcol) {  // thread 0
+        tc::fence_after();
+        const uint32_t idesc = tc::make_idesc(128, n);
+        for (int ks = 0; ks < ksteps; ++ks) {
+            const uint32_t ao = (uint32_t)(ks >> 2) * 16384u + (uint32_t)(ks & 3) * 32u;
+            const uint32_t bo = (uint32_t)(ks >> 2) * (uint32_t)(n * 128) + (uint32_t)(ks & 3) * 32u;
+            tc::umma(tmem + dcol, tc::make_desc(sA + ao), tc::make_desc(sB + bo), idesc, ks > 0 ? 1u : 0u);
+        }
+        tc::umma_commit(tc::smem_u32(bar_m));
+    };
+    // this thread's 128 accumulators at dcol -> bf16(relu(acc + b)) -> A tiles 0, 1 of row tid
+    auto hidden = [&](uint32_t dcol, const float *b) {
+#pragma unroll 1
+        for (int cc = 0; cc < 4; ++cc) {
+            uint32_t v[32];
+            tc::tmem_ld32(lane_base + dcol + 32u * cc, v);
+            tc::tmem_wait_ld();
+#pragma unroll
+            for (int g = 0; g < 4; ++g) {
+                uint32_t pk4[4];
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    const int c0 = 8 * g + 2 * h;
+                    const float a0 = fmaxf(__uint_as_float(v[c0]) + b[32 * cc + c0], 0.0f);
+                    const float a1 = fmaxf(__uint_as_float(v[c0 + 1]) + b[32 * cc + c0 + 1], 0.0f);
+                    const __nv_bfloat162 bv = __floats2bfloat162_rn(a0, a1);
+                    pk4[h] = *reinterpret_cast<const uint32_t *>(&bv);
+                }
+                const int k = 32 * cc + 8 * g;
+                *reinterpret_cast<uint4 *>(arow + (k >> 6) * 16384 + tc::swz(tid, k & 63)) =
+                    make_uint4(pk4[0], pk4[1], pk4[2], pk4[3]);
+            }
+        }
+    };
+
+    bool ok = true, x_pending = false, m_pending = false;
+    uint32_t ph_x = 0, ph_m = 0;
+    auto wait_m = [&](int code) -> bool {  // every thread: the committed MMAs are done
+        const bool got = tc::mbar_wait(tc::smem_u32(bar_m), ph_m, err, code);
+        if (got) {
+            ph_m ^= 1u;
+            m_pending = false;
+        }
+        const bool all = __syncthreads_and(got ? 1 : 0) != 0;
+        tc::fence_after();
+        return all;
+    };
+    if (tid == 0 && (int)blockIdx.x < ntiles) {
+        load_x(blockIdx.x);
+        x_pending = true;
+    }
+    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        // ---- layer 1 on the X tile, once every thread has read the previous tile's layer-3
+        // accumulators (the barrier) and the copies have landed
+        bool got = true;
+        if (tid == 0) {
+            got = tc::mbar_wait(tc::smem_u32(bar_x), ph_x, err, 1);
+            if (got) {
+                ph_x ^= 1u;
+                x_pending = false;
+            }
+        }
+        if (!(ok = __syncthreads_and(got ? 1 : 0) != 0)) break;
+        if (tid == 0) {
+            layer(sW1, NH, XNI / 16, 0u);
+            m_pending = true;
+        }
+        if (!(ok = wait_m(2))) break;
+        hidden(0u, bias);
+        tc::fence_proxy_async();
+        tc::fence_before();
+        __syncthreads();
+        // ---- layer 2 on h1
+        if (tid == 0) {
+            layer(sW2, NH, NH / 16, 128u);
+            m_pending = true;
+        }
+        if (!(ok = wait_m(3))) break;
+        hidden(128u, bias + NH);
+        tc::fence_proxy_async();
+        tc::fence_before();
+        __syncthreads();
+        // ---- layer 3 on h2
+        if (tid == 0) {
+            layer(sW3, XNO, NH / 16, 0u);
+            m_pending = true;
+        }
+        if (!(ok = wait_m(4))) break;
+        // the A tile is free again: the next tile's copies run under this epilogue
+        const int next = tile + gridDim.x;
+        if (tid == 0 && next < ntiles) {
+            load_x(next);
+            x_pending = true;
+        }
+        // tcgen05.ld is warp-collective: every lane reads, lanes past M store nothing
+        const int row = tile * 128 + tid;
+        float4 *z4 = reinterpret_cast<float4 *>(Z + (size_t)(row < M ? row : 0) * XNO);
+#pragma unroll 1
+        for (int cc = 0; cc < 3; ++cc) {
+            uint32_t v[32];
+            tc::tmem_ld32(lane_base + 32u * cc, v);
+            tc::tmem_wait_ld();
+            if (row < M) {
+#pragma unroll
+                for (int g = 0; g < 8; ++g)
+                    z4[8 * cc + g] = make_float4(__uint_as_float(v[4 * g]), __uint_as_float(v[4 * g + 1]),
+                                                 __uint_as_float(v[4 * g + 2]), __uint_as_float(v[4 * g + 3]));
+            }
+        }
+        tc::fence_before();  // these TMEM reads precede the next tile's MMAs
+    }
+    // after a failed wait: the copies and MMAs already started still write this block's
+    // shared and tensor memory; wait for them (bounded) before freeing and exiting
+    if (tid == 0 && x_pending) tc::mbar_wait(tc::smem_u32(bar_x), ph_x, err, 5);
+    bool drained = true;
+    if (tid == 0 && m_pending) drained = tc::mbar_wait(tc::smem_u32(bar_m), ph_m, err, 6);
+    drained = __syncthreads_and(drained ? 1 : 0) != 0;
+    if (warp == 0) {
+        tc::fence_after();
+        if (drained) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
+    }
+}
+
 // ------------------------------------------------------------------------ host side ----
 struct XyzLearn {
     ether_ctx *ctx = nullptr;
@@ -461,22 +657,13 @@ struct XyzLearn {
     float *Xb = nullptr, *Yb = nullptr, *H1 = nullptr, *H2 = nullptr, *Z = nullptr, *dZ = nullptr,
           *dH1 = nullptr, *dH2 = nullptr;
     double *loss = nullptr;
-    // inference: BF16 weights, one pass of up to `rows` patches
-    cublasHandle_t blas = nullptr;
-    cublasLtHandle_t lt = nullptr;
-    void *lt_ws = nullptr;         // cuBLASLt workspace
-    struct LtPlan {                // a fused layer (bias + ReLU epilogue, BF16 out) for M rows
-        int M = 0, K = 0;
-        cublasLtMatmulDesc_t op = nullptr;
-        cublasLtMatrixLayout_t a = nullptr, b = nullptr, d = nullptr;
-        cublasLtMatmulAlgo_t algo;
-        bool ok = false;
-    };
-    std::vector<LtPlan> plans;
-    __nv_bfloat16 *W16 = nullptr;  // W1, W2, W3 at their parameter offsets
+    // inference: BF16 weights and their swizzled image, one pass of up to `rows` patches
+    __nv_bfloat16 *W16 = nullptr;  // W1, W2, W3 (and b1, b2) at their parameter offsets
+    uint8_t *ximg = nullptr;       // XIMG_BYTES: xmlp_kernel's shared-memory image
     long long rows = 0;
-    __nv_bfloat16 *Xh = nullptr, *H1h = nullptr, *H2h = nullptr;
-    float *Hf = nullptr, *Zi = nullptr;
+    __nv_bfloat16 *Xh = nullptr;
+    float *Zi = nullptr;
+    int *err = nullptr;            // device: first bounded-wait failure of xmlp_kernel
     // sweeps
     uint32_t *lstep = nullptr;
     unsigned long long *acc = nullptr;
@@ -540,97 +727,45 @@ void xgemm(cudaStream_t st, int M, int N, int K, const float *A, int lda, int ta
 int quantise(XyzLearn &x, cudaStream_t st) {
     xquantise_kernel<<<64, 256, 0, st>>>(x.p, x.pq, XNPARAM);
     to_bf16_kernel<<<64, 256, 0, st>>>(x.pq, x.W16, XNPARAM);
-    x.launches += 2;
+    xpack_kernel<<<64, 256, 0, st>>>(x.W16, x.ximg);
+    x.launches += 3;
     XCUDA(cudaGetLastError());
     return ETHER_OK;
 }
 
-// C (row-major M x N, FP32) = A (row-major M x K, BF16) . W^T, W row-major N x K (BF16):
-// in cuBLAS's column-major terms C^T = W^T(op T of the K x N matrix) . A^T.
-int tc_gemm(XyzLearn &x, cudaStream_t st, int M, int N, int K, const __nv_bfloat16 *A, const __nv_bfloat16 *W,
-            float *C) {
-    const float one = 1.0f, zero = 0.0f;
-    cublasStatus_t b = cublasSetStream(x.blas, st);
-    if (b == CUBLAS_STATUS_SUCCESS)
-        b = cublasGemmEx(x.blas, CUBLAS_OP_T, CUBLAS_OP_N, N, M, K, &one, W, CUDA_R_16BF, K, A, CUDA_R_16BF, K, &zero,
-                         C, CUDA_R_32F, N, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
-    if (b != CUBLAS_STATUS_SUCCESS)
-        return xfail(ETHER_ERR_CUDA, std::string("learned proposal: cuBLAS GEMM failed (status ") +
-                                         std::to_string((int)b) + ")");
-    x.launches++;
-    return ETHER_OK;
-}
-
-constexpr size_t kLtWorkspace = 32u << 20;
-
-// A cuBLASLt plan for H (row-major M x NH, BF16) = bf16(relu(A . W^T + b)), A row-major M x K
-// (BF16), W row-major NH x K; in column-major terms H^T = op_T(W^T) . A^T.  ok = false when
-// cuBLASLt offers no algorithm for the shape.
-XyzLearn::LtPlan &lt_plan(XyzLearn &x, int M, int K) {
-    for (XyzLearn::LtPlan &p : x.plans)
-        if (p.M == M && p.K == K) return p;
-    x.plans.emplace_back();
-    XyzLearn::LtPlan &p = x.plans.back();
-    p.M = M;
-    p.K = K;
-    const cublasOperation_t ta = CUBLAS_OP_T, tb = CUBLAS_OP_N;
-    const cublasLtEpilogue_t epi = CUBLASLT_EPILOGUE_RELU_BIAS;  // bias in D's type (BF16)
-    bool ok = cublasLtMatmulDescCreate(&p.op, CUBLAS_COMPUTE_32F, CUDA_R_32F) == CUBLAS_STATUS_SUCCESS;
-    ok = ok && cublasLtMatmulDescSetAttribute(p.op, CUBLASLT_MATMUL_DESC_TRANSA, &ta, sizeof(ta)) == CUBLAS_STATUS_SUCCESS;
-    ok = ok && cublasLtMatmulDescSetAttribute(p.op, CUBLASLT_MATMUL_DESC_TRANSB, &tb, sizeof(tb)) == CUBLAS_STATUS_SUCCESS;
-    ok = ok && cublasLtMatmulDescSetAttribute(p.op, CUBLASLT_MATMUL_DESC_EPILOGUE, &epi, sizeof(epi)) == CUBLAS_STATUS_SUCCESS;
-    ok = ok && cublasLtMatrixLayoutCreate(&p.a, CUDA_R_16BF, K, NH, K) == CUBLAS_STATUS_SUCCESS;
-    ok = ok && cublasLtMatrixLayoutCreate(&p.b, CUDA_R_16BF, K, M, K) == CUBLAS_STATUS_SUCCESS;
-    ok = ok && cublasLtMatrixLayoutCreate(&p.d, CUDA_R_16BF, NH, M, NH) == CUBLAS_STATUS_SUCCESS;
-    if (ok) {
-        cublasLtMatmulPreference_t pref = nullptr;
-        ok = cublasLtMatmulPreferenceCreate(&pref) == CUBLAS_STATUS_SUCCESS;
-        const size_t ws = kLtWorkspace;
-        ok = ok && cublasLtMatmulPreferenceSetAttribute(pref, CUBLASLT_MATMUL_PREF_MAX_WORKSPACE_BYTES, &ws,
-                                                        sizeof(ws)) == CUBLAS_STATUS_SUCCESS;
-        cublasLtMatmulHeuristicResult_t res;
-        int n = 0;
-        ok = ok && cublasLtMatmulAlgoGetHeuristic(x.lt, p.op, p.a, p.b, p.d, p.d, pref, 1, &res, &n) ==
-                       CUBLAS_STATUS_SUCCESS && n > 0;
-        if (ok) p.algo = res.algo;
-        if (pref) cublasLtMatmulPreferenceDestroy(pref);
-    }
-    p.ok = ok;
-    return p;
-}
-
-// One hidden layer: H16 = bf16(relu(A . W^T + b)), b in BF16 (cuBLASLt epilogue, or GEMM +
-// this file's kernel).
-int hidden_layer(XyzLearn &x, cudaStream_t st, int M, int K, const __nv_bfloat16 *A, const __nv_bfloat16 *W,
-                 const __nv_bfloat16 *bias, __nv_bfloat16 *H16) {
-    XyzLearn::LtPlan &p = lt_plan(x, M, K);
-    if (p.ok && cublasLtMatmulDescSetAttribute(p.op, CUBLASLT_MATMUL_DESC_BIAS_POINTER, &bias, sizeof(bias)) ==
-                    CUBLAS_STATUS_SUCCESS) {
-        const float one = 1.0f, zero = 0.0f;
-        if (cublasLtMatmul(x.lt, p.op, &one, W, p.a, A, p.b, &zero, H16, p.d, H16, p.d, &p.algo, x.lt_ws, kLtWorkspace,
-                           st) == CUBLAS_STATUS_SUCCESS) {
-            x.launches++;
-            return ETHER_OK;
-        }
-        p.ok = false;  // not again for this shape
-    }
-    int rc = tc_gemm(x, st, M, NH, K, A, W, x.Hf);
-    if (rc) return rc;
-    bias_relu_bf16_kernel<<<4 * x.sm_count, 256, 0, st>>>(x.Hf, bias, H16, M);
-    x.launches++;
-    XCUDA(cudaGetLastError());
-    return ETHER_OK;
-}
-
-// The inference network on M rows of Xh (BF16): Zi (no output bias).
+// The inference network on M rows of Xh (BF16, M <= rows): Zi (no output bias), by
+// xmlp_kernel: one persistent CTA per SM at most, the X tiles read by TMA.
 int infer_rows(XyzLearn &x, cudaStream_t st, int M, const __nv_bfloat16 *Xh, float *Z) {
-    int rc = hidden_layer(x, st, M, XNI, Xh, x.W16 + XOFF_W1, x.W16 + XOFF_B1, x.H1h);
-    if (rc) return rc;
-    rc = hidden_layer(x, st, M, NH, x.H1h, x.W16 + XOFF_W2, x.W16 + XOFF_B2, x.H2h);
-    if (rc) return rc;
-    rc = tc_gemm(x, st, M, XNO, NH, x.H2h, x.W16 + XOFF_W3, Z);
-    if (rc) return rc;
+    auto encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(tma_encode_tiled_fn());
+    if (!encode) return xfail(ETHER_ERR_CUDA, "learned proposal: cuTensorMapEncodeTiled not available");
+    CUtensorMap map;
+    cuuint64_t gdim[2] = {(cuuint64_t)XNI, (cuuint64_t)M};
+    cuuint64_t gstride[1] = {(cuuint64_t)XNI * sizeof(__nv_bfloat16)};
+    cuuint32_t box[2] = {64, 128};
+    cuuint32_t estride[2] = {1, 1};
+    if (encode(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16 *>(Xh), gdim, gstride, box,
+               estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return xfail(ETHER_ERR_CUDA, "learned proposal: cuTensorMapEncodeTiled failed");
+    XCUDA(cudaFuncSetAttribute(xmlp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, XSM_BYTES));
+    const int ntiles = (M + 127) / 128;
+    xmlp_kernel<<<std::min(ntiles, x.sm_count), 128, XSM_BYTES, st>>>(map, x.ximg, Z, M, x.err);
+    x.launches++;
     XCUDA(cudaGetLastError());
+    return ETHER_OK;
+}
+
+// The device error flag of xmlp_kernel (synchronises the stream): ETHER_ERR_TIMEOUT once
+// after a bounded wait ran out, then cleared.
+int xread_err(XyzLearn &x) {
+    int e = 0;
+    XCUDA(cudaMemcpyAsync(&e, x.err, sizeof(int), cudaMemcpyDeviceToHost, x.ctx->c.stream));
+    XCUDA(cudaStreamSynchronize(x.ctx->c.stream));
+    if (e) {
+        cudaMemsetAsync(x.err, 0, sizeof(int), x.ctx->c.stream);
+        return xfail(ETHER_ERR_TIMEOUT, "learned proposal: an inference pipeline wait timed out (stage " +
+                                            std::to_string(e) + ")");
+    }
     return ETHER_OK;
 }
 
@@ -716,7 +851,8 @@ int xyz_create(ether_ctx *h, const ether_learn_desc *d, XyzLearn **out) {
     *out = nullptr;
     Ctx &c = h->c;
     // c.L is set once the lattice is verified to be the periodic simple-cubic one
-    if (c.model != ETHER_MODEL_XYZ || c.L[0] <= 0 || c.nsp != 1 || c.nsh != 1 || c.zeeman || c.sia || c.angle)
+    if (c.model != ETHER_MODEL_XYZ || c.L[0] <= 0 || c.nsp != 1 || c.nsh != 1 || c.zeeman || c.sia || c.sia_local ||
+        c.angle)
         return xfail(ETHER_ERR_UNSUPPORTED,
                      "learned proposal (XYZ): simple cubic, one species, one shell, Marsaglia proposals, no Zeeman or SIA term");
     if (c.L[0] % 8 || c.L[1] % 8 || c.L[2] % 8 || c.L[0] > 1016 || c.L[1] > 1016 || c.L[2] > 1016)
@@ -748,9 +884,10 @@ int xyz_create(ether_ctx *h, const ether_learn_desc *d, XyzLearn **out) {
     if (e == cudaSuccess) e = cudaMalloc((void **)&x->Y, (size_t)x->cap * XNO * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc((void **)&x->W16, XNPARAM * sizeof(__nv_bfloat16));
     if (e == cudaSuccess) e = cudaMalloc((void **)&x->Xh, (size_t)x->rows * XNI * sizeof(__nv_bfloat16));
-    if (e == cudaSuccess) e = cudaMalloc((void **)&x->H1h, (size_t)x->rows * NH * sizeof(__nv_bfloat16));
-    if (e == cudaSuccess) e = cudaMalloc((void **)&x->H2h, (size_t)x->rows * NH * sizeof(__nv_bfloat16));
-    if (e == cudaSuccess) e = cudaMalloc((void **)&x->Hf, (size_t)x->rows * NH * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&x->ximg, XIMG_BYTES);
+    if (e == cudaSuccess) e = cudaMemset(x->ximg, 0, XIMG_BYTES);  // W1's K padding stays zero
+    if (e == cudaSuccess) e = cudaMalloc((void **)&x->err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(x->err, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc((void **)&x->Zi, (size_t)x->rows * XNO * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc((void **)&x->loss, sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc((void **)&x->lstep, x->R * sizeof(uint32_t));
@@ -776,28 +913,13 @@ int xyz_create(ether_ctx *h, const ether_learn_desc *d, XyzLearn **out) {
         return xfail(e == cudaErrorMemoryAllocation ? ETHER_ERR_NOMEM : ETHER_ERR_CUDA,
                      std::string("learned proposal set-up: ") + cudaGetErrorString(e));
     }
-    if (cublasCreate(&x->blas) != CUBLAS_STATUS_SUCCESS) {
-        x->blas = nullptr;
-        xyz_destroy(x);
-        return xfail(ETHER_ERR_CUDA, "learned proposal set-up: cublasCreate failed");
-    }
-    if (cublasLtCreate(&x->lt) != CUBLAS_STATUS_SUCCESS) {
-        x->lt = nullptr;
-        xyz_destroy(x);
-        return xfail(ETHER_ERR_CUDA, "learned proposal set-up: cublasLtCreate failed");
-    }
-    e = cudaMalloc(&x->lt_ws, kLtWorkspace);
-    if (e != cudaSuccess) {
-        xyz_destroy(x);
-        return xfail(ETHER_ERR_NOMEM, "learned proposal set-up: cuBLASLt workspace");
-    }
     int rc = quantise(*x, c.stream);
     if (rc) {
         xyz_destroy(x);
         return rc;
     }
-    // one inference pass of every size a sweep uses, on zero inputs: the GEMM libraries load
-    // their kernels and choose their algorithms here, not inside the first learned sweep
+    // one inference pass of every size a sweep uses, on zero inputs: the kernel's one-time
+    // set-up (module load, shared-memory opt-in) happens here, not inside the first sweep
     e = cudaMemsetAsync(x->Xh, 0, (size_t)x->rows * XNI * sizeof(__nv_bfloat16), c.stream);
     if (e != cudaSuccess) {
         xyz_destroy(x);
@@ -815,10 +937,10 @@ int xyz_create(ether_ctx *h, const ether_learn_desc *d, XyzLearn **out) {
             }
         }
     }
-    e = cudaStreamSynchronize(c.stream);
-    if (e != cudaSuccess) {
+    rc = xread_err(*x);
+    if (rc) {
         xyz_destroy(x);
-        return xfail(ETHER_ERR_CUDA, std::string("learned proposal set-up: ") + cudaGetErrorString(e));
+        return rc;
     }
     *out = x;
     return ETHER_OK;
@@ -827,17 +949,8 @@ int xyz_create(ether_ctx *h, const ether_learn_desc *d, XyzLearn **out) {
 void xyz_destroy(XyzLearn *x) {
     if (!x) return;
     if (x->ctx) cudaStreamSynchronize(x->ctx->c.stream);
-    if (x->blas) cublasDestroy(x->blas);
-    for (XyzLearn::LtPlan &p : x->plans) {
-        if (p.a) cublasLtMatrixLayoutDestroy(p.a);
-        if (p.b) cublasLtMatrixLayoutDestroy(p.b);
-        if (p.d) cublasLtMatrixLayoutDestroy(p.d);
-        if (p.op) cublasLtMatmulDescDestroy(p.op);
-    }
-    if (x->lt) cublasLtDestroy(x->lt);
-    if (x->lt_ws) cudaFree(x->lt_ws);
     void *ptrs[] = {x->p, x->pq, x->g, x->m, x->v, x->X, x->Y, x->Xb, x->Yb, x->H1, x->H2, x->Z, x->dZ, x->dH1,
-                    x->dH2, x->loss, x->W16, x->Xh, x->H1h, x->H2h, x->Hf, x->Zi, x->lstep, x->acc, x->dump};
+                    x->dH2, x->loss, x->W16, x->ximg, x->err, x->Xh, x->Zi, x->lstep, x->acc, x->dump};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (x->e0) cudaEventDestroy(x->e0);
@@ -922,13 +1035,14 @@ int xyz_record_series(XyzLearn *x, int nsteps, int plain_per_step, int learned_p
         if (e != cudaSuccess) rc = xfail(ETHER_ERR_CUDA, std::string("series copy: ") + cudaGetErrorString(e));
     }
     cudaFree(mser);
+    if (rc == ETHER_OK) rc = xread_err(*x);
     return rc;
 }
 
 int xyz_get_accepts(XyzLearn *x, uint64_t *accepted) {
     XCUDA(cudaMemcpyAsync(accepted, x->acc, x->R * sizeof(uint64_t), cudaMemcpyDeviceToHost, x->ctx->c.stream));
     XCUDA(cudaStreamSynchronize(x->ctx->c.stream));
-    return ETHER_OK;
+    return xread_err(*x);
 }
 
 void xyz_set_dump(XyzLearn *x, bool on) { x->dump_on = on; }
@@ -997,7 +1111,7 @@ int xyz_forward(XyzLearn *x, const float *xin, int B, float *out) {
     }
     for (int b = 0; b < B; ++b)
         for (int o = 0; o < XNO; ++o) out[(size_t)b * XNO + o] += b3[o];
-    return ETHER_OK;
+    return xread_err(*x);
 }
 
 int xyz_info(XyzLearn *x, ether_learn_info *info) {

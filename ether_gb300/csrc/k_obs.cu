@@ -27,6 +27,7 @@ energy_mag_kernel(const uint8_t *__restrict__ spins, const float4 *__restrict__ 
                   const float *__restrict__ J, const double *__restrict__ Jd,
                   const uint8_t *__restrict__ species, const float *__restrict__ zee,
                   const double *__restrict__ zeed, const float *__restrict__ D,
+                  const uint8_t *__restrict__ sia_cls, const float4 *__restrict__ sia_ax,
                   const double *__restrict__ mweight, double *__restrict__ partials) {
     const int r = blockIdx.y;
     double q[kNq] = {0, 0, 0, 0, 0};
@@ -73,6 +74,13 @@ energy_mag_kernel(const uint8_t *__restrict__ spins, const float4 *__restrict__ 
                     e = fmaf(d[1], S.y * S.y, e);
                     e = fmaf(d[2], S.z * S.z, e);
                 }
+            }
+            if (sia_cls) {  // local-axis anisotropy D (a . S)^2
+                const float4 a = sia_ax[sia_cls[s]];
+                float ps = a.x * S.x;
+                ps = fmaf(a.y, S.y, ps);
+                ps = fmaf(a.z, S.z, ps);
+                e = fmaf(a.w, ps * ps, e);
             }
             q[0] += (double)e;
             q[2] += w * (double)S.x;
@@ -205,7 +213,8 @@ cudaError_t launch_energy_mag(Ctx &c, bool) {
     dim3 grid(nblk, c.R);
     energy_mag_kernel<<<grid, kRedBs, 0, c.stream>>>(
         c.spins, c.spins4, c.N, c.model, c.zeeman, c.sia && c.model == 1, c.t.row_ptr, c.t.nbr,
-        c.t.jidx, c.t.J, c.t.Jd, c.t.species, c.t.zee, c.t.zeed, c.t.D, c.t.mweight, c.partials);
+        c.t.jidx, c.t.J, c.t.Jd, c.t.species, c.t.zee, c.t.zeed, c.t.D,
+        c.sia_local && c.model == 1 ? c.t.sia_cls : nullptr, c.t.sia_ax, c.t.mweight, c.partials);
     finish_energy_kernel<<<c.R, 128, 0, c.stream>>>(c.partials, nblk, c.R, c.E, c.M);
     c.launches += 2;
     return cudaGetLastError();

@@ -300,17 +300,24 @@ __global__ void sq_prep_b(const uint8_t *__restrict__ spins, const float4 *__res
 using namespace ether;
 using namespace ether::sq;
 
-namespace {
-PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+namespace ether {
+// The driver's cuTensorMapEncodeTiled, looked up once through the runtime (no -lcuda).
+void *tma_encode_tiled_fn() {
+    static void *fn = nullptr;
     if (!fn) {
         cudaDriverEntryPointQueryResult q;
         void *p = nullptr;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+            fn = p;
     }
     return fn;
+}
+}  // namespace ether
+
+namespace {
+PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(ether::tma_encode_tiled_fn());
 }
 }  // namespace
 

@@ -203,6 +203,9 @@ static XyzParams xyz_params(const Ctx &c) {
     P.zee = c.t.zee;
     P.D = c.t.D;
     P.nsp = c.nsp;
+    P.sia_local = c.sia_local;
+    P.sia_cls = c.t.sia_cls;
+    P.sia_ax = c.t.sia_ax;
     return P;
 }
 
@@ -253,7 +256,7 @@ cudaError_t launch_xyz_sweep(Ctx &c, int colour) {
     const int bs = 256;
     XyzParams P = xyz_params(c);
     const RoundKeys K = round_keys(c.seed);
-    const bool exchange_only = !P.zeeman && !P.sia && !P.angle;
+    const bool exchange_only = !P.zeeman && !P.sia && !P.angle && !P.sia_local;
     if (c.fast) {
         if (exchange_only) launch_xyz_sc_opt<kXyzExchange>(c, colour, P, K);
         else launch_xyz_sc_opt<kXyzGeneral>(c, colour, P, K);

@@ -24,6 +24,9 @@ struct XyzParams {
     const float *zee;
     const float *D;
     int nsp;  // species count: with one, the per-site species is not read
+    int sia_local;            // per-site local-axis anisotropy D (a . S)^2
+    const uint8_t *sia_cls;   // storage index -> class
+    const float4 *sia_ax;     // class -> (a_x, a_y, a_z, D)
 };
 
 // Option sets of the XYZ kernels: kXyzExchange folds the Zeeman, SIA and ANGLE branches away
@@ -38,7 +41,7 @@ __device__ __forceinline__ float delta_e(const XyzParams &P, int s, const float4
     float e = dx * hx;
     e = fmaf(dy, hy, e);
     e = fmaf(dz, hz, e);
-    if (OPT != kXyzExchange && (P.zeeman || P.sia)) {
+    if (OPT != kXyzExchange && (P.zeeman || P.sia || P.sia_local)) {
         const int si = P.nsp == 1 ? 0 : P.species[s] - 1;
         if (P.zeeman) {
             const float *z = P.zee + 3 * si;
@@ -54,6 +57,16 @@ __device__ __forceinline__ float delta_e(const XyzParams &P, int s, const float4
             e = fmaf(D[0], qx, e);
             e = fmaf(D[1], qy, e);
             e = fmaf(D[2], qz, e);
+        }
+        if (P.sia_local) {
+            const float4 a = P.sia_ax[P.sia_cls[s]];
+            float pn = a.x * n.x;
+            pn = fmaf(a.y, n.y, pn);
+            pn = fmaf(a.z, n.z, pn);
+            float ps = a.x * S.x;
+            ps = fmaf(a.y, S.y, ps);
+            ps = fmaf(a.z, S.z, ps);
+            e = fmaf(a.w, pn * pn - ps * ps, e);
         }
     }
     return e;

@@ -79,6 +79,38 @@ def pyrochlore(n, shells=(2.97243,), cap=20, tol=1e-5):
     return Lattice(cart, [1] * 16, abc, n, list(shells), cap=cap, tol=tol)
 
 
+def local_111_axes(lat, shell=0):
+    """Per-site local easy axes of a lattice of corner-sharing tetrahedra (pyrochlore): the
+    unit vector from a site to the centroid of one of its nearest-neighbour triangles (the
+    three other corners of a tetrahedron it belongs to), which is the site's local <111>
+    direction.  Bond vectors use the minimum image of the periodic supercell.  Returns (N, 3),
+    each axis with its first non-zero component positive ((a . S)^2 does not depend on the
+    sign)."""
+    pos = lat.ion[:, 6:9]
+    SC = lat.abc * lat.sc[:, None]          # supercell vectors as rows
+    SCinv = np.linalg.inv(SC)
+    cnt = lat.nn[0, 0, :, shell]
+    nbrs = [set((lat.nn[0, 1:cnt[i] + 1, i, shell] - 1).tolist()) for i in range(lat.N)]
+    axes = np.zeros((lat.N, 3))
+    for i in range(lat.N):
+        nb = sorted(nbrs[i])
+        a = nb[0]
+        tri = [a] + [j for j in nb[1:] if j in nbrs[a]]
+        if len(tri) != 3:
+            raise ValueError("site %d: its nearest neighbours do not form triangles" % (i + 1))
+        d = pos[tri] - pos[i]
+        d -= np.round(d @ SCinv) @ SC
+        v = d.sum(axis=0)
+        v /= np.linalg.norm(v)
+        k = int(np.argmax(np.abs(v) > 1e-9))  # the first non-zero component made positive
+        v = v if v[k] > 0 else -v
+        # rounded to 1e-9 and renormalised: sites whose axes differ only by the rounding of
+        # their bond sums get the same axis (and so share one anisotropy class)
+        v = np.round(v, 9)
+        axes[i] = v / np.linalg.norm(v)
+    return axes
+
+
 def couplings(n_species, shells, s, para=None):
     """j_values.f90:61-86 + parameters.f90:26-38.
 
@@ -110,7 +142,7 @@ class Sweep:
     def __init__(self, ion, nn, j_exc, s, *, model, n_species, n_shells, cap, replicas=1,
                  seed=1992, angle=False, dphi=0.0, zeeman=False, h=(0.0, 0.0, 0.0),
                  g_factor=2.0, mb=MB_EV, sia=False, sia_vec=None, stgg=None, sc=(0, 0, 0),
-                 basis=0, flags=0):
+                 basis=0, flags=0, sia_local=None):
         self.lib = abi.load()
         self._keep = []
 
@@ -148,6 +180,7 @@ class Sweep:
             d.sc[k] = int(sc[k])
         d.basis = basis
         d.flags = flags
+        d.sia_local = abi.dptr(keep(sia_local, np.float64))  # (N, 4): axis, D per site
         self.N = d.n_sites
         self.R = replicas
         self._nsp = n_species

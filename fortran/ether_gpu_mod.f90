@@ -32,6 +32,7 @@ module ether_gpu_mod
         integer(c_int32_t) :: n_replicas
         integer(c_int32_t) :: seed          ! uint32_t in C
         integer(c_int32_t) :: sc(3), basis, flags
+        type(c_ptr)        :: sia_local     ! sia_local(4, N) or c_null_ptr
     end type ether_desc
 
     integer(c_int), parameter :: ETHER_RUN_PARSE_ONLY = 1, ETHER_RUN_QUIET = 2, ETHER_RUN_RESUME = 4

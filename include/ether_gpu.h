@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define ETHER_ABI_VERSION 1
+#define ETHER_ABI_VERSION 2
 
 enum {
     ETHER_OK = 0,
@@ -92,6 +92,15 @@ typedef struct ether_desc {
     int32_t sc[3];        /* supercell (0 = unknown); enables the simple-cubic kernels     */
     int32_t basis;        /* lattice_per_unit_cell (0 = unknown)                           */
     int32_t flags;        /* ETHER_FLAG_*                                                  */
+    const double *sia_local; /* sia_local(4, N) or NULL: per-site single-ion anisotropy
+                             D (a . S)^2 about a local unit axis a = sia_local(1:3, i) with
+                             D = sia_local(4, i) (energy units after parameters.f90), XYZ only,
+                             added to the sia_vec term.  No counterpart in the reference, whose
+                             anisotropy is diagonal per species (src/get_sia_values.f90:57-58):
+                             it expresses easy axes along local directions such as the
+                             pyrochlore's <111>.  At most 256 distinct (a, D) per context
+                             (ETHER_ERR_CAPACITY beyond).  Turns overrelaxation off in
+                             ether_mcs, as the reference's SIA does (src/ether.f90:163-168). */
 } ether_desc;
 
 /* Library version / last error (thread-local message of the last failing call). */

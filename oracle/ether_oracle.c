@@ -244,6 +244,11 @@ int orc_greedy_colouring(int N, int nsh, int cap, const int32_t *nn, int32_t *co
     return ncol;
 }
 
+/* The local-axis anisotropy of site i in FP32 as the GPU holds it: (a_x, a_y, a_z, D). */
+static void sia_local_f32(const orc_sys *sy, int i, float a[4]) {
+    for (int c = 0; c < 4; ++c) a[c] = (float)sy->sia_local[4 * (size_t)i + c];
+}
+
 /* ------------------------------------------------------------- Hamiltonian ---------- */
 double orc_hamiltonian(const orc_sys *sy, const double *ion, int i, const double *s_trial,
                        const double *s_old, int trial) {
@@ -277,6 +282,12 @@ double orc_hamiltonian(const orc_sys *sy, const double *ion, int i, const double
     if (sy->sia && sy->model == 1) { /* siaS2, Hamiltonian.f90:137-141 */
         const double *D = sy->sia_vec + 3 * (size_t)(si - 1);
         tot += D[0] * S2d[0] + D[1] * S2d[1] + D[2] * S2d[2];
+    }
+    if (sy->sia_local && sy->model == 1) { /* D (a . S)^2 about the site's own axis */
+        const double *a = sy->sia_local + 4 * (size_t)i;
+        const double pn = a[0] * s_trial[0] + a[1] * s_trial[1] + a[2] * s_trial[2];
+        const double po = a[0] * s_old[0] + a[1] * s_old[1] + a[2] * s_old[2];
+        tot += trial ? a[3] * (pn * pn - po * po) : a[3] * (po * po);
     }
     return tot;
 }
@@ -349,6 +360,14 @@ double orc_tot_energy_f32(const orc_sys *sy, const double *ion, const float *sp4
             e = fmaf((float)D[0], S[0] * S[0], e);
             e = fmaf((float)D[1], S[1] * S[1], e);
             e = fmaf((float)D[2], S[2] * S[2], e);
+        }
+        if (sy->sia_local && sy->model == 1) {
+            float a[4];
+            sia_local_f32(sy, i, a);
+            float ps = a[0] * S[0];
+            ps = fmaf(a[1], S[1], ps);
+            ps = fmaf(a[2], S[2], ps);
+            e = fmaf(a[3], ps * ps, e);
         }
         t += (double)e;
     }
@@ -585,6 +604,17 @@ static int xyz_site_f32(const orc_sys *sy, const double *ion, float *sp4, int i,
         e = fmaf((float)D[0], qx, e);
         e = fmaf((float)D[1], qy, e);
         e = fmaf((float)D[2], qz, e);
+    }
+    if (sy->sia_local) {
+        float a[4];
+        sia_local_f32(sy, i, a);
+        float pn = a[0] * nx;
+        pn = fmaf(a[1], ny, pn);
+        pn = fmaf(a[2], nz, pn);
+        float ps = a[0] * S[0];
+        ps = fmaf(a[1], S[1], ps);
+        ps = fmaf(a[2], S[2], ps);
+        e = fmaf(a[3], pn * pn - ps * ps, e);
     }
     int acc = (e <= 0.0f) || (eta < orc_expf_neg(-(beta_f * e)));
     if (acc) { S[0] = nx; S[1] = ny; S[2] = nz; S[3] = nphi; }
@@ -867,7 +897,7 @@ double orc_run_temperature(const orc_sys *sy, double *ion, double beta, const or
                            double *vals) {
     int N = sy->n_sites;
     int ovrr_steps = (int)lround(N * cfg->ovrr_para);
-    int ovrr_on = cfg->ovrr && sy->model == 1 && !sy->zeeman && !sy->sia && cfg->ovrr_mcs > 0;
+    int ovrr_on = cfg->ovrr && sy->model == 1 && !sy->zeeman && !sy->sia && !sy->sia_local && cfg->ovrr_mcs > 0;
     double acc_total = 0.0;
     for (int r = 1; r <= cfg->repeat; ++r) {
         orc_stream st;
@@ -925,7 +955,7 @@ void orc_run_ladder(const orc_sys *sy, const double *ion0, int nT, const double 
     const int N = sy->n_sites;
     const size_t nb = sizeof(double) * 9 * (size_t)N;
     const int ovrr_steps = (int)lround(N * cfg->ovrr_para);
-    const int ovrr_on = cfg->ovrr && sy->model == 1 && !sy->zeeman && !sy->sia && cfg->ovrr_mcs > 0;
+    const int ovrr_on = cfg->ovrr && sy->model == 1 && !sy->zeeman && !sy->sia && !sy->sia_local && cfg->ovrr_mcs > 0;
     double **cfgs = (double **)malloc(sizeof(double *) * nT);
     double *E = (double *)malloc(sizeof(double) * nT);
     int32_t *conf_of_slot = (int32_t *)malloc(sizeof(int32_t) * nT);

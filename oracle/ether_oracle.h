@@ -49,6 +49,11 @@ typedef struct orc_sys {
     const double *sia_vec;/* may be NULL when !sia                                      */
     const double *s;      /* spin length per species                                   */
     const double *stgg;   /* stgg_ion(N) (src/get_tot_magnetisation.f90:37); NULL = 1  */
+    const double *sia_local; /* sia_local(4, N) or NULL: a site term D (a . S)^2 with the
+                             unit axis a = sia_local(0:2, i) and D = sia_local(3, i), XYZ only.
+                             Not expressible in the reference (its SIA is the diagonal
+                             sia_vec per species, src/get_sia_values.f90:57-58); it adds to
+                             that term like siaS2 (src/Hamiltonian.f90:127-143) adds D S^2. */
 } orc_sys;
 
 /* ------------------------------------------------------------- lattice build -------- */

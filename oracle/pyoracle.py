@@ -25,7 +25,7 @@ class Sys(C.Structure):
                 ("cap", C.c_int), ("model", C.c_int), ("angle", C.c_int), ("dphi", C.c_double),
                 ("zeeman", C.c_int), ("h", C.c_double * 3), ("g_factor", C.c_double),
                 ("mb", C.c_double), ("sia", C.c_int), ("nn", PI), ("j_exc", PD),
-                ("sia_vec", PD), ("s", PD), ("stgg", PD)]
+                ("sia_vec", PD), ("s", PD), ("stgg", PD), ("sia_local", PD)]
 
 
 class Stream(C.Structure):
@@ -221,12 +221,13 @@ class System:
 
     def __init__(self, ion, nn, j_exc, s, *, model, n_species, n_shells, cap, angle=False,
                  dphi=0.0, zeeman=False, h=(0, 0, 0), g_factor=2.0, mb=5.7883818060e-5,
-                 sia=False, sia_vec=None, stgg=None):
+                 sia=False, sia_vec=None, stgg=None, sia_local=None):
         self.ion0 = np.ascontiguousarray(ion, dtype=np.float64)
         self.nn = np.ascontiguousarray(nn, dtype=np.int32)
         self.j_exc = np.ascontiguousarray(j_exc, dtype=np.float64)
         self.s = np.ascontiguousarray(s, dtype=np.float64)
         self.sia_vec = None if sia_vec is None else np.ascontiguousarray(sia_vec, dtype=np.float64)
+        self.sia_local = None if sia_local is None else np.ascontiguousarray(sia_local, dtype=np.float64)
         self.stgg = None if stgg is None else np.ascontiguousarray(stgg, dtype=np.float64)
         self.N = self.ion0.shape[0]
         y = Sys()
@@ -238,6 +239,7 @@ class System:
         y.g_factor, y.mb, y.sia = float(g_factor), float(mb), int(bool(sia))
         y.nn, y.j_exc, y.sia_vec = _i(self.nn), _d(self.j_exc), _d(self.sia_vec)
         y.s, y.stgg = _d(self.s), _d(self.stgg)
+        y.sia_local = _d(self.sia_local)
         self.sys = y
         self.model = model
 

@@ -209,3 +209,36 @@ def test_batch_large_member_runs_its_own_kernels():
     # group, and the counter advance
     assert info.kernels_per_sweep == 2 + 2 * 2 + 1
     batch.close()
+
+
+def test_batch_members_with_local_axis_anisotropy():
+    """Members with per-site local-axis anisotropy (pyrochlore <111> axes; a simple-cubic
+    lattice with two axis classes) in the XYZ option classes: as their own sweeps."""
+    def members():
+        out = []
+        lat = eg.pyrochlore(2)
+        ax = eg.local_111_axes(lat)
+        sl = np.concatenate([ax, np.full((lat.N, 1), -0.2e-3)], axis=1)
+        sc = eg.simple_cubic(12)
+        par = (np.arange(sc.N) % 12 + (np.arange(sc.N) // 12) % 12 + np.arange(sc.N) // 144) % 2
+        sl2 = np.where(par[:, None] == 0, [[0.0, 0.0, 1.0, -0.3e-3]], [[0.6, 0.8, 0.0, 0.1e-3]])
+        for k, (l, shells, s) in enumerate(((lat, AFM, sl), (sc, FM, sl2))):
+            j = eg.couplings(1, shells, [1.0])
+            sw = eg.Sweep.from_lattice(l, j, np.asarray([1.0]), eg.MODEL_XYZ, replicas=2, seed=5 + k,
+                                       sia_local=s)
+            sw.set_ladder([beta_of(1.0), beta_of(2.5)])
+            sw.set_spins(random_xyz(l, 40 + k))
+            out.append((l, sw))
+        lat3 = eg.simple_cubic(8)
+        sw3 = eg.Sweep.from_lattice(lat3, eg.couplings(1, FM, [1.0]), np.asarray([1.0]), eg.MODEL_XYZ, replicas=2)
+        sw3.set_ladder([beta_of(1.0), beta_of(2.5)])
+        sw3.set_spins(random_xyz(lat3, 9))
+        out.append((lat3, sw3))
+        return out
+    A, B = members(), members()
+    batch = eg.Batch([sw for _, sw in A])
+    batch.metropolis(4)
+    for _, sw in B:
+        sw.metropolis(4)
+    assert_same(states(A), states(B))
+    batch.close()

@@ -134,7 +134,7 @@ def test_statistical_parity_with_reference_order_run():
     """E, |M|, C_v, chi, U_E, U_M per temperature from REPEAT = 16 independent repeats on the
     GPU (Checkerboard order, replicas) vs the oracle's reference-order (typewriter) run of
     src/ether.f90's per-temperature loop, compared in units of the combined REPEAT error bars
-    (z) by the family-wise rule of assert_same_ensemble (24 comparisons)."""
+    (per temperature, jointly over the six observables: assert_same_ensemble)."""
     L, REP, TMCS, EQ, COA = 12, 16, 1200, 400, 5
     temps = [3.6, 4.4, 4.6, 6.0]
     lat = eg.simple_cubic(L)
@@ -149,23 +149,15 @@ def test_statistical_parity_with_reference_order_run():
                                   betas.ctypes.data_as(po.PD), C.byref(cfg), 0,
                                   vals.ctypes.data_as(po.PD), accr.ctypes.data_as(po.PD))
     vals = vals.reshape(len(temps), REP, 6)
-    ref_mean, ref_err = vals.mean(1), vals.std(1, ddof=1) / np.sqrt(REP)
-    sw = eg.Sweep.from_lattice(lat, j, np.array([1.0]), eg.MODEL_ISING, replicas=REP * len(temps),
-                               seed=77)
-    sw.set_ladder(betas)
-    sw.set_spins(lat.ion)
-    sw.fresh_spins()
-    sw.zero_avg()
-    sw.mcs(0, TMCS, EQ, COA)
-    mean, err = sw.per_repeat()
-    assert_same_ensemble(mean, err, ref_mean, ref_err)
+    mine = _gpu_run(lat, j, eg.MODEL_ISING, betas, REP, TMCS, EQ, COA)
+    assert_same_ensemble(mine, vals)
 
 
 def _reference_order(osys, lat, betas, cfg, ex=0):
     """The oracle's reference-order run: per temperature the loop of src/ether.f90:150-214
     (typewriter Metropolis, random-site overrelaxation, get_tot_energy every MCS); with ex > 0
     the temperatures run in lockstep as MPI ranks with parallel_tempering every ex MCS.
-    Returns the REPEAT means and error bars per temperature."""
+    Returns the per-REPEAT values (temperatures, REPEATs, 6)."""
     nT, REP = len(betas), cfg.repeat
     vals = np.zeros(6 * REP * nT)
     accr = np.zeros(nT)
@@ -180,8 +172,7 @@ def _reference_order(osys, lat, betas, cfg, ex=0):
         po.lib().orc_run_temperatures(osys.p(), osys.ion0.ctypes.data_as(po.PD), nT,
                                       b.ctypes.data_as(po.PD), C.byref(cfg), 0,
                                       vals.ctypes.data_as(po.PD), accr.ctypes.data_as(po.PD))
-    vals = vals.reshape(nT, REP, 6)
-    return vals.mean(1), vals.std(1, ddof=1) / np.sqrt(REP)
+    return vals.reshape(nT, REP, 6)
 
 
 def _gpu_run(lat, j, model, betas, REP, TMCS, EQ, COA, seed=77, **mcs_kw):
@@ -194,8 +185,11 @@ def _gpu_run(lat, j, model, betas, REP, TMCS, EQ, COA, seed=77, **mcs_kw):
     sw.zero_avg()
     sw.mcs(0, TMCS, EQ, COA, **mcs_kw)
     mean, err = sw.per_repeat()
+    # per-REPEAT values: replica g * nT + t is REPEAT g at temperature slot t
+    vals = sw.avg().reshape(REP, len(betas), 6).transpose(1, 0, 2)
+    np.testing.assert_allclose(vals.mean(1), mean, rtol=1e-9, atol=1e-12)
     sw.close()
-    return mean, err
+    return vals
 
 
 def test_heisenberg_overrelaxation_schedule_same_ensemble_as_reference_order():
@@ -211,10 +205,10 @@ def test_heisenberg_overrelaxation_schedule_same_ensemble_as_reference_order():
     betas = np.array([beta_of(k) for k in (1.0, 1.4, 1.5, 2.5)])
     cfg = po.RunCfg(tmcs=TMCS, tmcs_eq=EQ, coa=COA, repeat=REP, ovrr=1, ovrr_para=1.0, ovrr_mcs=5,
                     seed=1992, itemp=1, rank=0)
-    ref_mean, ref_err = _reference_order(osys, lat, betas, cfg)
-    mean, err = _gpu_run(lat, j, eg.MODEL_XYZ, betas, REP, TMCS, EQ, COA, ovrr=True, ovrr_para=1.0,
-                         ovrr_mcs=5)
-    assert_same_ensemble(mean, err, ref_mean, ref_err)
+    ref = _reference_order(osys, lat, betas, cfg)
+    mine = _gpu_run(lat, j, eg.MODEL_XYZ, betas, REP, TMCS, EQ, COA, ovrr=True, ovrr_para=1.0,
+                    ovrr_mcs=5)
+    assert_same_ensemble(mine, ref)
 
 
 def test_heisenberg_pt_ladder_zeeman_sia_same_ensemble_as_reference_order():
@@ -232,10 +226,10 @@ def test_heisenberg_pt_ladder_zeeman_sia_same_ensemble_as_reference_order():
     betas = np.array([beta_of(k) for k in np.geomspace(1.2, 1.8, 6)])
     cfg = po.RunCfg(tmcs=TMCS, tmcs_eq=EQ, coa=COA, repeat=REP, ovrr=0, ovrr_para=0.0, ovrr_mcs=0,
                     seed=1992, itemp=1, rank=0)
-    ref_mean, ref_err = _reference_order(osys, lat, betas, cfg, ex=EX)
-    mean, err = _gpu_run(lat, j, eg.MODEL_XYZ, betas, REP, TMCS, EQ, COA, pt=True,
-                         exchange_interval=EX, **opts)
-    assert_same_ensemble(mean, err, ref_mean, ref_err)
+    ref = _reference_order(osys, lat, betas, cfg, ex=EX)
+    mine = _gpu_run(lat, j, eg.MODEL_XYZ, betas, REP, TMCS, EQ, COA, pt=True, exchange_interval=EX,
+                    **opts)
+    assert_same_ensemble(mine, ref)
 
 
 def test_ising_pt_ladder_same_ensemble_as_reference_order():
@@ -248,10 +242,9 @@ def test_ising_pt_ladder_same_ensemble_as_reference_order():
     betas = np.array([beta_of(k) for k in np.geomspace(4.2, 4.9, 6)])
     cfg = po.RunCfg(tmcs=TMCS, tmcs_eq=EQ, coa=COA, repeat=REP, ovrr=0, ovrr_para=0.0, ovrr_mcs=0,
                     seed=1992, itemp=1, rank=0)
-    ref_mean, ref_err = _reference_order(osys, lat, betas, cfg, ex=EX)
-    mean, err = _gpu_run(lat, j, eg.MODEL_ISING, betas, REP, TMCS, EQ, COA, pt=True,
-                         exchange_interval=EX)
-    assert_same_ensemble(mean, err, ref_mean, ref_err)
+    ref = _reference_order(osys, lat, betas, cfg, ex=EX)
+    mine = _gpu_run(lat, j, eg.MODEL_ISING, betas, REP, TMCS, EQ, COA, pt=True, exchange_interval=EX)
+    assert_same_ensemble(mine, ref)
 
 
 @pytest.mark.parametrize("model", [eg.MODEL_ISING, eg.MODEL_XYZ])

@@ -12,7 +12,7 @@ import pytest
 import ether_gb300 as eg
 from oracle import deck_oracle as do
 from oracle import pyoracle as po
-from tests.helpers import assert_same_ensemble
+from tests.helpers import assert_means_agree
 from tests.test_deck import SC_STRUCT, write_deck
 
 pytestmark = pytest.mark.gpu
@@ -73,7 +73,7 @@ def test_run_thermodynamics_match_oracle_run(tmp_path):
     """ETHER.obs of a 10^3 Ising deck vs the oracle's reference-order run of the same deck
     (typewriter Metropolis, REPEATs one after another): |M|, chi, U_M, E, C_v, U_E per
     temperature in units of the combined REPEAT error bars (the family-wise rule of
-    assert_same_ensemble), and the acceptance rate."""
+    assert_means_agree), and the acceptance rate."""
     indir = write_deck(str(tmp_path / "in"), ISING_DECK, SC_STRUCT, J_FM)
     out = str(tmp_path / "out")
     eg.run(indir, out)
@@ -98,7 +98,7 @@ def test_run_thermodynamics_match_oracle_run(tmp_path):
     # ETHER.obs order: 1 |M|, 2 chi, 3 d|M|, 4 dchi, 5 U_M, 6 dU_M, 7 E, 8 C_v, 9 dE, 10 dC_v, 11 U_E, 12 dU_E
     mine = obs[:, [7, 11, 8, 1, 5, 2]]
     mine_err = obs[:, [9, 12, 10, 3, 6, 4]]
-    assert_same_ensemble(mine, mine_err, ref, ref_err)
+    assert_means_agree(mine, mine_err, ref, ref_err, rep, rep)
     np.testing.assert_allclose(obs[:, 13], 100.0 * accr, rtol=0.05, atol=0.5)
 
 

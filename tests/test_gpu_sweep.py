@@ -379,3 +379,59 @@ def test_spins_batch_equals_per_replica_calls(model, L, R):
     np.testing.assert_array_equal(back[:, :, cols], sub[:, :, cols].astype(np.float32).astype(np.float64))
     np.testing.assert_array_equal(sw.get_spins(lat.ion, 4)[:, cols], got[4][:, cols])
     sw.close()
+
+
+def _sia_local(axes, D):
+    return np.ascontiguousarray(np.concatenate([axes, np.broadcast_to(np.asarray(D, float), (len(axes),))[:, None]],
+                                               axis=1))
+
+
+def test_xyz_local_axis_sia_pyrochlore_matches_fp32_mirror():
+    """Single-ion anisotropy D (a_i . S)^2 about each site's local <111> axis (D = -0.2 meV,
+    easy axis), beside the reference's diagonal term and a Zeeman field, on the pyrochlore
+    lattice with two shells: the GPU state equals the oracle's FP32 mirror bit for bit; E
+    equals the mirror's to rounding and the FP64 replay's to 1e-5."""
+    lat = eg.Lattice(eg.pyrochlore(2).basis_cart, [1] * 16, np.eye(3) * eg.model.PYROCHLORE_A,
+                     (2, 2, 2), [2.97243, 5.1484], tol=1e-3)
+    sia_local = _sia_local(eg.local_111_axes(lat), -0.2e-3)
+    sw, osys, sp4, ion64, g = xyz_replay(lat, AFM_J1_J2, 2.0, 20, zeeman=True, h=(0.0, 0.0, 1.0),
+                                         g_factor=2.0, sia=True, sia_vec=np.array([[0.0, 0.05e-3, 0.0]]),
+                                         sia_local=sia_local)
+    assert sw.info().fast_path == 0
+    np.testing.assert_array_equal(g[:, 1:4].astype(np.float32), sp4[:, 0:3])
+    E = sw.tot_energy()[0]
+    ion = lat.ion.copy()
+    assert E == pytest.approx(osys.tot_energy_f32(ion, sp4), rel=1e-12)
+    assert E == pytest.approx(osys.tot_energy(ion64), rel=1e-5)
+
+
+def test_xyz_local_axis_sia_simple_cubic_fast_path():
+    """Two anisotropy classes (axis and D per checkerboard sublattice) on the simple-cubic fast
+    kernel: bit-exact against the FP32 mirror; energy as the oracle's."""
+    lat = eg.simple_cubic(8)
+    rng = np.random.default_rng(4)
+    two = rng.normal(size=(2, 3))
+    two /= np.linalg.norm(two, axis=1, keepdims=True)
+    par = (np.arange(lat.N) % 8 + (np.arange(lat.N) // 8) % 8 + np.arange(lat.N) // 64) % 2
+    sia_local = _sia_local(two[par], np.where(par == 0, -0.3e-3, 0.2e-3))
+    sw, osys, sp4, ion64, g = xyz_replay(lat, FM, 1.443, 15, sia_local=sia_local)
+    assert sw.info().fast_path == 1
+    for k, col in ((1, 0), (2, 1), (3, 2)):
+        np.testing.assert_array_equal(g[:, k].astype(np.float32), sp4[:, col])
+    assert sw.tot_energy()[0] == pytest.approx(osys.tot_energy_f32(lat.ion.copy(), sp4), rel=1e-12)
+
+
+def test_local_axis_sia_turns_overrelaxation_off_in_mcs():
+    """As the reference's SIA does (src/ether.f90:163-168): ether_mcs with ovrr on leaves a
+    context with local-axis anisotropy exactly as without ovrr."""
+    lat = eg.simple_cubic(8)
+    axes = np.tile([[0.0, 0.6, 0.8]], (lat.N, 1))
+    runs = []
+    for ovrr in (False, True):
+        sw, _ = make_pair(lat, eg.MODEL_XYZ, FM, replicas=2, sia_local=_sia_local(axes, -0.1e-3))
+        sw.set_beta([beta_of(1.2), beta_of(2.0)])
+        sw.set_spins(random_xyz(lat, 8))
+        sw.mcs(0, 30, 10, 5, ovrr=ovrr, ovrr_para=1.0, ovrr_mcs=3)
+        runs.append(np.stack([sw.get_spins(lat.ion, r)[:, 1:4] for r in range(2)]))
+        sw.close()
+    np.testing.assert_array_equal(runs[0], runs[1])

@@ -68,7 +68,7 @@ def test_library_exports_every_declared_symbol():
     for name in declared:
         assert hasattr(lib, name), name
     assert declared == set(abi.SIGNATURES), declared ^ set(abi.SIGNATURES)
-    assert lib.ether_abi_version() == 1
+    assert lib.ether_abi_version() == 2
 
 
 def test_create_without_gpu_or_bad_input_fails_cleanly():

@@ -223,3 +223,25 @@ def test_timed_build_computes_the_same_energies():
         a = po.lib().orc_tot_energy(osys.p(), po._d(ion))
         b = po.timed_lib().orc_tot_energy(osys.p(), po._d(ion))
         assert b == pytest.approx(a, rel=1e-12)
+
+
+def test_oracle_local_axis_anisotropy_energy():
+    """The oracle's local-axis anisotropy: with the exchange switched off, get_tot_energy of
+    spins along their own axes is N D, and a trial move's Hamiltonian(.TRUE.) equals the
+    difference of the two site energies."""
+    lat = po.ScLattice(4)
+    rng = np.random.default_rng(3)
+    ax = rng.normal(size=(lat.N, 3))
+    ax /= np.linalg.norm(ax, axis=1, keepdims=True)
+    D = -0.2e-3
+    sl = np.concatenate([ax, np.full((lat.N, 1), D)], axis=1)
+    osys = po.System.from_lattice(lat, po.sc_couplings((0.0, 0.0, 0.0)), np.array([1.0]), 1, sia_local=sl)
+    ion = lat.ion.copy()
+    ion[:, 1:4] = ax
+    assert osys.tot_energy(ion) == pytest.approx(lat.N * D, rel=1e-12)
+    i = 5
+    new = rng.normal(size=3)
+    new /= np.linalg.norm(new)
+    old = ion[i, 1:4].copy()
+    dE = po.lib().orc_hamiltonian(osys.p(), po._d(ion), i, po._d(new), po._d(old), 1)
+    assert dE == pytest.approx(D * ((ax[i] @ new) ** 2 - (ax[i] @ old) ** 2), rel=1e-12)
