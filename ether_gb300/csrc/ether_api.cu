@@ -1264,6 +1264,7 @@ std::map<std::vector<long>, int> g_tune_cache;  // variant per (model, L, R)
 static int variant_of(const Ctx &c) {
     if (c.model == ETHER_MODEL_XYZ) return 5000 + c.xyz_variant;
     if (c.ising_stream) return 4000 + 10 * c.ising_vpt + (c.ising_cap ? 4 : 1);
+    if (c.ising_cap5) return 6000 + c.vec_bytes * 10 + c.ising_vpt;
     return (c.ising_persist ? 1000 : 0) + (c.ising_cap ? 2000 : 0) + c.vec_bytes * 10 + c.ising_vpt;
 }
 
@@ -1273,6 +1274,8 @@ int ctx_variant(const Ctx &c) { return variant_of(c); }
 
 // variant = 1000 (persistent kernel) + 2000 (register cap: four 256-thread blocks per SM)
 //           + 10 * bytes per vector + vectors per thread
+//           or 6162: the phase kernel capped at five blocks per SM (two 16-byte vectors
+//           per thread in 48 registers)
 //           or 4000 + 10 * vectors per thread and step + 1 / 4 (register cap): the
 //           shared-memory staged kernel (4011, 4014, 4021, 4041)
 //           or 5000 + 10 * sites per thread + register cap (blocks per SM) for the
@@ -1287,13 +1290,25 @@ static bool apply_variant(Ctx &c, int variant) {
         const int vs = (variant / 10) % 10;
         if (!ising_stream_supported(c, vs)) return false;
         c.ising_stream = true;
+        c.ising_cap5 = false;
         c.ising_cap = variant % 10 == 4;
         c.vec_bytes = 16;
         c.ising_vpt = vs;
         return true;
     }
+    if (variant == 6162) {
+        if ((c.L[0] / 2) % 16) return false;
+        c.ising_stream = false;
+        c.ising_persist = false;
+        c.ising_cap = false;
+        c.ising_cap5 = true;
+        c.vec_bytes = 16;
+        c.ising_vpt = 2;
+        return true;
+    }
     if (variant < 0 || variant >= 4000) return false;
     c.ising_stream = false;
+    c.ising_cap5 = false;
     const bool p = (variant / 1000) & 1, cap = (variant / 1000) >= 2;
     const int rest = variant % 1000, w = rest / 10, v = rest % 10;
     if ((w != 4 && w != 8 && w != 16) || (c.L[0] / 2) % w) return false;
@@ -1398,8 +1413,8 @@ extern "C" int ether_autotune(ether_ctx *h, int32_t *variant, float *best_ms) {
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    for (int cand : {161, 162, 164, 81, 82, 84, 41, 42, 44, 2162, 2164, 1162, 1164, 1082, 1084, 1042, 1044,
-                     3162, 3164, 4011, 4014, 4021, 4041}) {
+    for (int cand : {161, 162, 164, 81, 82, 84, 41, 42, 44, 2162, 2164, 6162, 1162, 1164, 1082, 1084, 1042,
+                     1044, 3162, 3164, 4011, 4014, 4021, 4041}) {
         if (!apply_variant(c, cand)) continue;
         CUDA_TRY(launch_ising_sweep(c, 0));  // warm-up
         CUDA_TRY(cudaEventRecord(e0, c.stream));

@@ -99,6 +99,7 @@ struct Ctx {
     int ising_vpt = 1;           // vectors per thread of the simple-cubic Ising kernel
     bool ising_persist = false;  // persistent simple-cubic Ising kernel
     bool ising_cap = false;      // register-capped (four blocks per SM) instantiation
+    bool ising_cap5 = false;     // register-capped to five blocks per SM (48 registers)
     bool ising_stream = false;   // shared-memory staged simple-cubic Ising kernel
     int xyz_variant = 11;        // simple-cubic XYZ kernel: 10 * sites per thread + blocks per SM cap
     bool resident = false;       // ether_mcs runs runs of sweeps with ising_sc_resident

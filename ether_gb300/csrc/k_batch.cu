@@ -110,7 +110,8 @@ __device__ __forceinline__ unsigned batch_xyz_sc(const BatchMember &m, uint32_t 
     const float beta_f = m.beta_slot_f[m.slot_of_rep[r]];
     const RoundKeys &K = m.K;  // read in place from shared memory: no registers held
     // exchange only, Marsaglia proposals: the options fold away at compile time
-    const XyzParams P = OPT == kXyzExchange ? XyzParams{0, 0, 0, 0.f, nullptr, nullptr, nullptr, 1} : m.P;
+    XyzParams P = OPT == kXyzExchange ? XyzParams{0, 0, 0, 0.f, nullptr, nullptr, nullptr, 1} : m.P;
+    if (P.sia_cls) P.sia_cls += (size_t)colour * half;  // sites are ranks in the colour array
     unsigned acc = 0;
     for (int rho = first + (int)threadIdx.x; rho < end; rho += blockDim.x)
         acc += xyz_sc_site<OPT>(A, P, rho, beta_f, t, c3, K, stream) ? 1u : 0u;

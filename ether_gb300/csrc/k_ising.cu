@@ -499,8 +499,10 @@ cudaError_t launch_ising_sweep(Ctx &c, int colour) {
     if (c.fast) {
         // variant = 1000 persistent + 2000 register cap (four 256-thread blocks per SM)
         //           + 10 bytes per vector + vectors per thread
-        const int key = (c.ising_persist ? 1000 : 0) + (c.ising_cap ? 2000 : 0) + c.vec_bytes * 10 + c.ising_vpt;
+        const int key = c.ising_cap5 ? 6000 + c.vec_bytes * 10 + c.ising_vpt
+                                     : (c.ising_persist ? 1000 : 0) + (c.ising_cap ? 2000 : 0) + c.vec_bytes * 10 + c.ising_vpt;
         switch (key) {
+            case 6162: launch_sc<16, 2, 5>(c, colour); break;
             case 161: launch_sc<16, 1, 1>(c, colour); break;
             case 162: launch_sc<16, 2, 1>(c, colour); break;
             case 164: launch_sc<16, 4, 1>(c, colour); break;

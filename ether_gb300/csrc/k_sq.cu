@@ -8,6 +8,11 @@
 // D = A_hi B_hi + A_hi B_lo + A_lo B_hi is accumulated in FP32 in tensor memory: about 16
 // significant bits per product instead of BF16's 8.
 //
+// Ising spins are +-1 along z: B_lo is identically zero and the x, y components vanish, so
+// the Ising form (ISING = true) keeps one column per replica (S_z; up to 256 replicas per
+// pass instead of 85), loads no B_lo tile and issues two products per K-step
+// (A_hi B_hi + A_lo B_hi) instead of three.
+//
 // One CTA owns a 128-row tile of D (64 q-points: consecutive h1 at fixed h2, h3) and all
 // 3R columns (<= 256).  Per 64-site k-block:
 //   * warps 0-7 generate the A tile in shared memory: phase factors
@@ -75,7 +80,7 @@ struct SqParams {
     int N;             // sites (true count)
     int Kpad;          // sites padded to kBK
     int R;             // replicas in this launch
-    int BN;            // columns (3R padded to 16)
+    int BN;            // columns (3R, or R for Ising, padded to 16)
     const float2 *E1;  // [M1/16][Kpad]   exp(2 pi i (q0_1 + 16 m dq_1) u_i)
     const float2 *E2;  // [M2][Kpad]
     const float2 *E3;  // [M3][Kpad]
@@ -85,13 +90,15 @@ struct SqParams {
     int *err;
 };
 
+template <bool ISING>
 __global__ void __launch_bounds__(kThreads, 1)
 sq_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
           SqParams P) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int b_bytes = P.BN * kBK * 2;
-    const int stage_bytes = 2 * Smem::a_bytes + 2 * b_bytes;  // multiple of 1024 (BN % 16 == 0 -> b_bytes % 2048 == 0)
+    constexpr int nb = ISING ? 1 : 2;                          // B tiles per stage: hi (, lo)
+    const int stage_bytes = 2 * Smem::a_bytes + nb * b_bytes;  // multiple of 1024 (BN % 16 == 0 -> b_bytes % 2048 == 0)
     uint8_t *bar_area = base + kStages * stage_bytes;
     uint64_t *full = reinterpret_cast<uint64_t *>(bar_area);
     uint64_t *empty = full + kStages;
@@ -173,7 +180,7 @@ sq_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CU
     } else if (lane == 0) {
         // ------------------------------------------------------- TMA + MMA issue --------
         const uint32_t idesc = make_idesc(P.BN);
-        const uint32_t tx = 2u * (uint32_t)b_bytes;
+        const uint32_t tx = (uint32_t)nb * (uint32_t)b_bytes;
         auto issue_tma = [&](int kb) -> bool {
             const int s = kb & 1, f = kb >> 1;
             if (f >= 1 && !mbar_wait(smem_u32(&empty[s]), (f - 1) & 1, P.err, 2)) return false;
@@ -181,7 +188,7 @@ sq_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CU
             uint8_t *b_lo = b_hi + b_bytes;
             mbar_arrive_tx(smem_u32(&tmab[s]), tx);
             tma_load_2d(smem_u32(b_hi), &map_hi, kb * kBK, 0, smem_u32(&tmab[s]));
-            tma_load_2d(smem_u32(b_lo), &map_lo, kb * kBK, 0, smem_u32(&tmab[s]));
+            if (!ISING) tma_load_2d(smem_u32(b_lo), &map_lo, kb * kBK, 0, smem_u32(&tmab[s]));
             return true;
         };
         int issued = 0;
@@ -209,7 +216,7 @@ sq_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CU
             for (int kk = 0; kk < kBK / 16; ++kk) {
                 const uint32_t o = kk * 32;  // 16 BF16 along K
                 umma(tmem, make_desc(a_hi + o), make_desc(b_hi + o), idesc, (kb | kk) ? 1u : 0u);
-                umma(tmem, make_desc(a_hi + o), make_desc(b_lo + o), idesc, 1u);
+                if (!ISING) umma(tmem, make_desc(a_hi + o), make_desc(b_lo + o), idesc, 1u);
                 umma(tmem, make_desc(a_lo + o), make_desc(b_hi + o), idesc, 1u);
             }
             umma_commit(smem_u32(&empty[s]));
@@ -237,7 +244,30 @@ sq_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CU
         const int qloc = row >> 1;         // rows 2q, 2q+1 = cos, sin
         const int q = h1_0 + qloc + P.M1 * (h2 + P.M2 * h3);
         const float invN = 1.0f / (float)P.N;
-        for (int r = warp >> 2; r < P.R; r += kProducers / 128) {
+        if (ISING) {
+            // column r = S_z of replica r: four replicas per TMEM load
+            for (int r0 = 4 * (warp >> 2); r0 < P.R; r0 += 4 * (kProducers / 128)) {
+                uint32_t v[4];
+                const uint32_t taddr = tmem + ((uint32_t)(wl * 32) << 16) + (uint32_t)r0;
+                asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
+                             : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]) : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const float mine = __uint_as_float(v[j]);
+                    const float other = __shfl_xor_sync(0xffffffffu, mine, 1);
+                    const float m2 = mine * mine + other * other;
+                    if ((lane & 1) == 0 && r0 + j < P.R) {
+                        P.sq[(size_t)(r0 + j) * Q + q] = m2 * invN * invN;
+                        float *c = P.comp + ((size_t)(r0 + j) * Q + q) * 3;
+                        c[0] = 0.f;
+                        c[1] = 0.f;
+                        c[2] = sqrtf(m2) * invN;
+                    }
+                }
+            }
+        }
+        for (int r = warp >> 2; !ISING && r < P.R; r += kProducers / 128) {
             uint32_t v[4];
             const uint32_t taddr = tmem + ((uint32_t)(wl * 32) << 16) + (uint32_t)(3 * r);
             asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
@@ -279,10 +309,11 @@ __global__ void sq_prep_b(const uint8_t *__restrict__ spins, const float4 *__res
     const long total = (long)BN * Kpad;
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
         const int n = (int)(e / Kpad), k = (int)(e - (long)n * Kpad);
-        const int r = n / 3, a = n - 3 * r;
+        // Ising: one row per replica (S_z); XYZ: rows 3r + a
+        const int r = model == 0 ? n : n / 3, a = model == 0 ? 2 : n - 3 * r;
         float x = 0.f;
         if (r < R && k < N) {
-            if (model == 0) x = (a == 2) ? (spins[(size_t)(r0 + r) * N + k] ? 1.f : -1.f) : 0.f;
+            if (model == 0) x = spins[(size_t)(r0 + r) * N + k] ? 1.f : -1.f;
             else {
                 const float4 S = spins4[(size_t)(r0 + r) * N + k];
                 x = a == 0 ? S.x : a == 1 ? S.y : S.z;
@@ -357,14 +388,16 @@ int structure_factor_launch(Ctx &c, const double *frac /*3N, storage order*/, co
         const double ph = tp * dq[0] * u;
         bb[i] = make_float2((float)cos(ph), (float)sin(ph));
     }
-    const int rmax = 85;  // 3 * 85 = 255 <= 256 columns of TMEM per pass
+    const bool ising = c.model == ETHER_MODEL_ISING;
+    const int cols = ising ? 1 : 3;            // TMEM columns per replica
+    const int rmax = ising ? 256 : 85;         // 3 * 85 = 255 <= 256 columns of TMEM per pass
     float2 *dE1 = nullptr, *dE2 = nullptr, *dE3 = nullptr, *dbb = nullptr;
     __nv_bfloat16 *bhi = nullptr, *blo = nullptr;
     float *dsq = nullptr, *dcomp = nullptr;
     int *derr = nullptr;
     int rc = ETHER_OK;
     const int rpass = std::min(c.R, rmax);
-    const int BNmax = (3 * rpass + 15) / 16 * 16;
+    const int BNmax = (cols * rpass + 15) / 16 * 16;
     auto cleanup = [&]() {
         cudaFree(dE1); cudaFree(dE2); cudaFree(dE3); cudaFree(dbb); cudaFree(bhi); cudaFree(blo);
         cudaFree(dsq); cudaFree(dcomp); cudaFree(derr);
@@ -385,7 +418,7 @@ int structure_factor_launch(Ctx &c, const double *frac /*3N, storage order*/, co
     SQ_TRY(cudaMemcpyAsync(dbb, bb.data(), bb.size() * sizeof(float2), cudaMemcpyHostToDevice, c.stream));
     for (int r0 = 0; r0 < c.R && rc == ETHER_OK; r0 += rpass) {
         const int R = std::min(rpass, c.R - r0);
-        const int BN = (3 * R + 15) / 16 * 16;
+        const int BN = (cols * R + 15) / 16 * 16;
         SQ_TRY(cudaMemsetAsync(derr, 0, sizeof(int), c.stream));
         sq_prep_b<<<std::max(1, std::min(4096, (int)(((long)BN * Kpad + 255) / 256))), 256, 0, c.stream>>>(
             c.spins, c.spins4, c.model, N, Kpad, r0, R, BN, bhi, blo);
@@ -409,15 +442,16 @@ int structure_factor_launch(Ctx &c, const double *frac /*3N, storage order*/, co
         P.N = N; P.Kpad = Kpad; P.R = R; P.BN = BN;
         P.E1 = dE1; P.E2 = dE2; P.E3 = dE3; P.bb = dbb;
         P.sq = dsq; P.comp = dcomp; P.err = derr;
-        const int stage_bytes = 2 * Smem::a_bytes + 2 * BN * kBK * 2;
+        const int stage_bytes = 2 * Smem::a_bytes + (ising ? 1 : 2) * BN * kBK * 2;
         const int smem = 1024 + kStages * stage_bytes + 64;
-        SQ_TRY(cudaFuncSetAttribute(sq_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        auto kern = ising ? sq_kernel<true> : sq_kernel<false>;
+        SQ_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         const int tiles = (int)(Q / 64);
         cudaEvent_t ev0, ev1;
         SQ_TRY(cudaEventCreate(&ev0));
         SQ_TRY(cudaEventCreate(&ev1));
         SQ_TRY(cudaEventRecord(ev0, c.stream));
-        sq_kernel<<<tiles, kThreads, smem, c.stream>>>(mh, ml, P);
+        kern<<<tiles, kThreads, smem, c.stream>>>(mh, ml, P);
         c.launches++;
         SQ_TRY(cudaGetLastError());
         SQ_TRY(cudaEventRecord(ev1, c.stream));

@@ -216,9 +216,11 @@ static void launch_xyz_sc(Ctx &c, int colour, const XyzParams &P, const RoundKey
     dim3 grid(blocks_for_x(c, (half + VPT - 1) / VPT, bs), c.R);
     // single shell, single species: J(1,1,1,:)
     const float jx = c.h_Jf[0], jy = c.h_Jf[1], jz = c.h_Jf[2];
+    XyzParams Pc = P;  // the kernel indexes sites by rank in the colour array
+    if (Pc.sia_cls) Pc.sia_cls += (size_t)colour * half;
     xyz_sc_kernel<OPT, VPT, MINB><<<grid, bs, 0, c.stream>>>(
         c.spins4, c.L[0], c.L[1], c.L[2], make_fastdiv((uint32_t)(c.L[0] / 2)), make_fastdiv((uint32_t)c.L[1]),
-        (uint32_t)colour, jx, jy, jz, P, c.beta_slot_f, c.slot_of_rep, c.stream_id, c.step, K, c.acc_count);
+        (uint32_t)colour, jx, jy, jz, Pc, c.beta_slot_f, c.slot_of_rep, c.stream_id, c.step, K, c.acc_count);
 }
 
 // xyz_variant = 10 * VPT + MINB (11 = one site per thread, no register cap)

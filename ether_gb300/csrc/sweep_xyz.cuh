@@ -25,7 +25,9 @@ struct XyzParams {
     const float *D;
     int nsp;  // species count: with one, the per-site species is not read
     int sia_local;            // per-site local-axis anisotropy D (a . S)^2
-    const uint8_t *sia_cls;   // storage index -> class
+    const uint8_t *sia_cls;   // site -> class, indexed like the spin array the kernel updates:
+                              // by storage index (general lattices) or, for the simple-cubic
+                              // colour arrays, by rank (the table offset to the colour at launch)
     const float4 *sia_ax;     // class -> (a_x, a_y, a_z, D)
 };
 

@@ -55,7 +55,7 @@ def test_ising_sc_bit_exact(L, flags, kT):
         assert sw.info().fast_path == 1
 
 
-@pytest.mark.parametrize("variant", [161, 162, 164, 81, 82, 84, 41, 42, 44, 2162, 2164, 1162, 1164,
+@pytest.mark.parametrize("variant", [161, 162, 164, 81, 82, 84, 41, 42, 44, 2162, 2164, 6162, 1162, 1164,
                                      1082, 1084, 1042, 1044, 3162, 3164])
 def test_ising_sc_every_kernel_variant_bit_exact(variant):
     lat = eg.simple_cubic((32, 8, 6))
