@@ -420,11 +420,13 @@ def run_batch(steps=200, warmup=5, chains=256, ladder=32, config=None, forms=(Fa
             **out}
 
 
-def run_learned(L=64, R=256, train_steps=3000, n_plain=40000, n_learn=6000, heisenberg=False):
+def run_learned(L=64, R=256, train_steps=3000, n_plain=40000, n_learn=20000, heisenberg=False, stride=10):
     """Learned 4^3-patch proposal at T_c of the L^3 Ising (or Heisenberg) model: trained on
     plain-sweep configurations of an 8-temperature ladder (0.9 .. 1.1 T_c), then tau_int(|M|)
     and the independent samples per second of (a) plain sweeps, (b) plain + learned sweep per
-    step, (c) learned sweeps alone, all with R replicas at T_c."""
+    step, (c) learned sweeps alone, all with R replicas at T_c.  |M| is recorded every
+    `stride` steps in all three chains (as a production run measures every COA steps), so the
+    recording adds the same small cost per step to each and tau is converted to steps."""
     import ether_gb300 as eg
     from ether_gb300.analysis import tau_int
     lat = eg.simple_cubic(L)
@@ -450,15 +452,16 @@ def run_learned(L=64, R=256, train_steps=3000, n_plain=40000, n_learn=6000, heis
     train_ms = lr.info().last_train_ms
     sw.set_beta([1.0 / ktc] * R)
     sw.metropolis(5000, accept=False)
+    sw.autotune()  # the plain sweeps below run the fastest kernel variant
     sw.sync()
 
     def series(n, plain, learned):
         t = time.perf_counter()
-        out = lr.record_series(n, 1 if plain else 0, 1 if learned else 0)
+        out = lr.record_series(n, 1 if plain else 0, 1 if learned else 0, stride=stride)
         return out, time.perf_counter() - t
 
     t = time.perf_counter()
-    m_plain = sw.record_series(n_plain, stride=1)
+    m_plain = sw.record_series(n_plain, stride=stride)
     s_plain = time.perf_counter() - t
     a0, p0 = lr.accepts().sum(), lr.info().proposed
     m_both, s_both = series(n_learn, True, True)
@@ -469,10 +472,11 @@ def run_learned(L=64, R=256, train_steps=3000, n_plain=40000, n_learn=6000, heis
     res = {"workload": "learned 4^3-patch proposal, %d^3 %s at T_c, %d replicas"
                        % (L, "Heisenberg" if heisenberg else "Ising", R),
            "train_steps": train_steps, "final_loss": loss, "train_ms": train_ms,
-           "acceptance_at_tc": acc, "learned_sweep_ms": sweep_ms}
+           "acceptance_at_tc": acc, "learned_sweep_ms": sweep_ms, "record_stride_steps": stride}
     for name, m, n, secs in (("plain", m_plain, n_plain, s_plain), ("plain_plus_learned", m_both, n_learn, s_both),
                              ("learned_only", m_learn, n_learn, s_learn)):
         tau, err, W = tau_int(m)
+        tau, err = tau * stride, err * stride
         res[name] = {"tau_int_absM_steps": tau, "tau_err": err, "steps": n,
                      "steps_per_s": n / secs,
                      "independent_samples_per_s": R * n / secs / (2.0 * tau)}
@@ -677,6 +681,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-components", action="store_true")
     ap.add_argument("--variant", type=int, default=0)
+    ap.add_argument("--learn-steps", type=int, default=0,
+                    help="--model learned / learned-heisenberg: Adam steps (default 3000 / 4000)")
     ap.add_argument("--sq-cells", type=int, default=12)
     ap.add_argument("--chains", type=int, default=256)
     ap.add_argument("--deck", default="c1_ising_16", choices=sorted(PROGRAM_DECKS))
@@ -771,7 +777,8 @@ def main():
     if args.model == "learned-heisenberg":
         if rank != 0:
             return 0
-        r = run_learned(args.L, R=64, train_steps=4000, n_plain=60000, n_learn=6000, heisenberg=True)
+        r = run_learned(args.L, R=64, train_steps=args.learn_steps or 4000, n_plain=60000, n_learn=20000,
+                        heisenberg=True)
         print(json.dumps({"metric": "independent samples/s gain", "value": r["learned_only"]["gain_vs_plain"],
                           "unit": "x plain", "higher_is_better": True, "detail": r}))
         return 0
@@ -787,7 +794,7 @@ def main():
     if args.model == "learned":
         if rank != 0:
             return 0
-        r = run_learned(args.L)
+        r = run_learned(args.L, train_steps=args.learn_steps or 3000)
         print(json.dumps({"metric": "independent samples/s gain", "value": r["learned_only"]["gain_vs_plain"],
                           "unit": "x plain", "higher_is_better": True, "detail": r}))
         return 0
@@ -860,7 +867,7 @@ def main():
         comp["batch"] = bt
         comp["tau"] = run_tau(args.L)
         comp["learned"] = run_learned(args.L)
-        comp["learned_heisenberg"] = run_learned(args.L, R=64, train_steps=4000, n_plain=60000, n_learn=6000,
+        comp["learned_heisenberg"] = run_learned(args.L, R=64, train_steps=4000, n_plain=60000, n_learn=20000,
                                                  heisenberg=True)
         comp["program_c1"] = run_program("c1_ising_16")
         comp["program_c2"] = run_program("c2_heisenberg_32", repeats=1)

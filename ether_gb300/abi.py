@@ -159,8 +159,9 @@ SIGNATURES = {
     "ether_learn_destroy": (C.c_int, [P]),
     "ether_learn_collect": (C.c_int, [P, C.c_int32]),
     "ether_learn_train": (C.c_int, [P, C.c_int32, C.c_int32, C.c_float, PD]),
+    "ether_learn_batch_sweep": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.c_int32, C.c_int32]),
     "ether_learn_sweep": (C.c_int, [P, C.c_int32]),
-    "ether_learn_record_series": (C.c_int, [P, C.c_int32, C.c_int32, C.c_int32, PD]),
+    "ether_learn_record_series": (C.c_int, [P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, PD]),
     "ether_learn_get_accepts": (C.c_int, [P, PU64]),
     "ether_learn_get_params": (C.c_int, [P, C.POINTER(C.c_float)]),
     "ether_learn_set_params": (C.c_int, [P, C.POINTER(C.c_float)]),

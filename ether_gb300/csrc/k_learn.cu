@@ -1105,17 +1105,42 @@ extern "C" int ether_learn_sweep(ether_learn *l, int32_t nsweeps) {
     return ETHER_OK;
 }
 
+extern "C" int ether_learn_batch_sweep(ether_learn *const *learns, int32_t n, int32_t nsweeps,
+                                       int32_t plain_per_sweep) {
+    if (!learns || n <= 0 || nsweeps < 0 || plain_per_sweep < 0) return lfail(ETHER_ERR_ARG, "invalid argument");
+    for (int k = 0; k < n; ++k) {
+        if (!learns[k]) return lfail(ETHER_ERR_ARG, "null learner");
+        if (!learns[k]->ctx->c.beta_set) return lfail(ETHER_ERR_STATE, "beta not set");
+        for (int j = 0; j < k; ++j)
+            if (learns[j]->ctx == learns[k]->ctx) return lfail(ETHER_ERR_ARG, "two learners of one context");
+    }
+    // step s of every context before step s + 1 of any: each context's stream gets its own
+    // work in order, the contexts run side by side
+    for (int s = 0; s < nsweeps; ++s)
+        for (int k = 0; k < n; ++k) {
+            for (int p = 0; p < plain_per_sweep; ++p) {
+                const int rc = plain_sweep(learns[k]->ctx->c);
+                if (rc) return rc;
+            }
+            const int rc = ether_learn_sweep(learns[k], 1);
+            if (rc) return rc;
+        }
+    return ETHER_OK;
+}
+
 extern "C" int ether_learn_record_series(ether_learn *l, int32_t nsteps, int32_t plain_per_step,
-                                         int32_t learned_per_step, double *absM) {
+                                         int32_t learned_per_step, int32_t stride, double *absM) {
     if (!l || !absM) return lfail(ETHER_ERR_ARG, "null argument");
-    if (nsteps < 1 || plain_per_step < 0 || learned_per_step < 0 || plain_per_step + learned_per_step < 1)
-        return lfail(ETHER_ERR_ARG, "need nsteps >= 1 and at least one sweep per step");
+    if (nsteps < 1 || plain_per_step < 0 || learned_per_step < 0 || plain_per_step + learned_per_step < 1 ||
+        stride < 1 || nsteps / stride < 1)
+        return lfail(ETHER_ERR_ARG, "need nsteps >= stride >= 1 and at least one sweep per step");
     Ctx &c = l->ctx->c;
     if (!c.beta_set) return lfail(ETHER_ERR_STATE, "beta not set");
-    if (l->xyz) return learn::xyz_record_series(l->xyz, nsteps, plain_per_step, learned_per_step, absM);
+    if (l->xyz) return learn::xyz_record_series(l->xyz, nsteps, plain_per_step, learned_per_step, stride, absM);
     int rc = refresh_tables(*l);
     if (rc) return rc;
-    const size_t bytes = sizeof(double) * (size_t)nsteps * l->R;
+    const int nrec = nsteps / stride;
+    const size_t bytes = sizeof(double) * (size_t)nrec * l->R;
     double *mser = nullptr;
     LCUDA(cudaMalloc((void **)&mser, bytes));
     for (int t = 0; t < nsteps && rc == ETHER_OK; ++t) {
@@ -1128,8 +1153,8 @@ extern "C" int ether_learn_record_series(ether_learn *l, int32_t nsteps, int32_t
                 l->proposed += 2ull * (uint64_t)l->R * (uint64_t)l->Pc;
             }
         }
-        if (rc == ETHER_OK) {
-            const cudaError_t e = launch_record(c, t, false, mser, nullptr);
+        if (rc == ETHER_OK && (t + 1) % stride == 0 && (t + 1) / stride <= nrec) {
+            const cudaError_t e = launch_record(c, (t + 1) / stride - 1, false, mser, nullptr);
             if (e != cudaSuccess) rc = lfail(ETHER_ERR_CUDA, std::string("record: ") + cudaGetErrorString(e));
         }
     }

@@ -119,19 +119,15 @@ __host__ __device__ __forceinline__ void vmf_sample(const Vmf &V, float u, float
     om = fminf(fmaxf(om, 0.0f), 2.0f);
     const float w = 1.0f - om;
     const float r = sqrtf(om * (2.0f - om));
-    // e1 perpendicular to the mean direction, e2 = mean x e1
-    float e1x, e1y, e1z;
-    if (fabsf(uz) < 0.9f) {
-        const float rn = rcp_f(sqrtf(dot3(uy, ux, 0.0f, uy, ux, 0.0f)));
-        e1x = -uy * rn;
-        e1y = ux * rn;
-        e1z = 0.0f;
-    } else {
-        const float rn = rcp_f(sqrtf(dot3(0.0f, uz, uy, 0.0f, uz, uy)));
-        e1x = 0.0f;
-        e1y = uz * rn;
-        e1z = -uy * rn;
-    }
+    // e1 perpendicular to the mean direction, e2 = mean x e1: (-uy, ux, 0) / |.| when
+    // |uz| < 0.9, else (0, uz, -uy) / |.| -- one normalisation of the selected vector, so the
+    // lanes of a warp do not diverge (the same operations as the two separate branches)
+    const bool flat = fabsf(uz) < 0.9f;
+    const float pa = flat ? uy : 0.0f, pb = flat ? ux : uz, pc = flat ? 0.0f : uy;
+    const float rn = rcp_f(sqrtf(dot3(pa, pb, pc, pa, pb, pc)));
+    const float e1x = flat ? -uy * rn : 0.0f;
+    const float e1y = pb * rn;
+    const float e1z = flat ? 0.0f : -uy * rn;
     const float e2x = uy * e1z - uz * e1y, e2y = uz * e1x - ux * e1z, e2z = ux * e1y - uy * e1x;
     float sn, cs;
     sincos_own(kPi * v, &sn, &cs);
@@ -1015,17 +1011,19 @@ int xyz_sweep(XyzLearn *x, int nsweeps) {
     return ETHER_OK;
 }
 
-int xyz_record_series(XyzLearn *x, int nsteps, int plain_per_step, int learned_per_step, double *absM) {
+int xyz_record_series(XyzLearn *x, int nsteps, int plain_per_step, int learned_per_step, int stride,
+                      double *absM) {
     Ctx &c = x->ctx->c;
-    const size_t bytes = sizeof(double) * (size_t)nsteps * x->R;
+    const int nrec = nsteps / stride;
+    const size_t bytes = sizeof(double) * (size_t)nrec * x->R;
     double *mser = nullptr;
     XCUDA(cudaMalloc((void **)&mser, bytes));
     int rc = ETHER_OK;
     for (int t = 0; t < nsteps && rc == ETHER_OK; ++t) {
         for (int k = 0; k < plain_per_step && rc == ETHER_OK; ++k) rc = plain_sweep(c);
         for (int k = 0; k < learned_per_step && rc == ETHER_OK; ++k) rc = learned_sweep(*x, nullptr);
-        if (rc == ETHER_OK) {
-            const cudaError_t e = launch_record(c, t, false, mser, nullptr);
+        if (rc == ETHER_OK && (t + 1) % stride == 0 && (t + 1) / stride <= nrec) {
+            const cudaError_t e = launch_record(c, (t + 1) / stride - 1, false, mser, nullptr);
             if (e != cudaSuccess) rc = xfail(ETHER_ERR_CUDA, std::string("record: ") + cudaGetErrorString(e));
         }
     }

@@ -72,7 +72,8 @@ void xyz_destroy(XyzLearn *x);
 int xyz_collect(XyzLearn *x, int per_replica);
 int xyz_train(XyzLearn *x, int steps, int batch, float lr, double *loss);
 int xyz_sweep(XyzLearn *x, int nsweeps);
-int xyz_record_series(XyzLearn *x, int nsteps, int plain_per_step, int learned_per_step, double *absM);
+int xyz_record_series(XyzLearn *x, int nsteps, int plain_per_step, int learned_per_step, int stride,
+                      double *absM);
 int xyz_get_accepts(XyzLearn *x, uint64_t *accepted);
 void xyz_set_dump(XyzLearn *x, bool on);
 int xyz_get_dump(XyzLearn *x, float *out);

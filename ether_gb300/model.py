@@ -483,11 +483,11 @@ class Learned:
     def sweep_(self, nsweeps=1):
         abi.check(self.lib.ether_learn_sweep(self.h, nsweeps))
 
-    def record_series(self, nsteps, plain_per_step=1, learned_per_step=1):
-        """|M| of every replica after each step, shape (R, nsteps)."""
-        out = np.zeros((nsteps, self.sweep.R), dtype=np.float64)
+    def record_series(self, nsteps, plain_per_step=1, learned_per_step=1, stride=1):
+        """|M| of every replica after every stride-th step, shape (R, nsteps // stride)."""
+        out = np.zeros((nsteps // stride, self.sweep.R), dtype=np.float64)
         abi.check(self.lib.ether_learn_record_series(self.h, nsteps, plain_per_step,
-                                                     learned_per_step, abi.dptr(out)))
+                                                     learned_per_step, stride, abi.dptr(out)))
         return out.T.copy()
 
     def accepts(self):
@@ -543,6 +543,14 @@ class Learned:
         i = abi.LearnInfo()
         abi.check(self.lib.ether_learn_get_info(self.h, C.byref(i)))
         return i
+
+
+def learn_batch_sweep(learners, nsweeps=1, plain_per_sweep=1):
+    """ether_learn_batch_sweep: the learners' contexts advance together, nsweeps steps of
+    plain_per_sweep Metropolis sweeps then one learned sweep each (asynchronous)."""
+    lib = abi.load()
+    hs = (C.c_void_p * len(learners))(*[l.h.value for l in learners])
+    abi.check(lib.ether_learn_batch_sweep(hs, len(learners), nsweeps, plain_per_sweep))
 
 
 def run(indir, outdir, parse_only=False, ranks=0, resume=False, quiet=True):

@@ -229,6 +229,12 @@ module ether_gpu_mod
             integer(c_int32_t), value :: nsweeps
         end function
         ! network widths (Ising 128, 32, 37152; Heisenberg 304, 96, 67936)
+        integer(c_int) function ether_learn_batch_sweep(learns, n, nsweeps, plain_per_sweep) &
+                bind(C, name="ether_learn_batch_sweep")
+            import :: c_int, c_ptr, c_int32_t
+            type(c_ptr), intent(in) :: learns(*)
+            integer(c_int32_t), value :: n, nsweeps, plain_per_sweep
+        end function
         integer(c_int) function ether_learn_get_shape(learn, n_inputs, n_outputs, n_params) &
                 bind(C, name="ether_learn_get_shape")
             import :: c_int, c_ptr, c_int32_t

@@ -358,11 +358,19 @@ int ether_learn_collect(ether_learn *learn, int32_t per_replica);
 int ether_learn_train(ether_learn *learn, int32_t steps, int32_t batch, float lr, double *loss);
 /* nsweeps learned sweeps of every replica (asynchronous, on the context's stream). */
 int ether_learn_sweep(ether_learn *learn, int32_t nsweeps);
+/* No counterpart in the reference (its moves are single-site).  The learned form batched over
+ * contexts: n learners of n distinct contexts (any mix of models and sizes) advance together,
+ * nsweeps steps of plain_per_sweep Metropolis sweeps then one learned sweep each, the steps of
+ * all contexts issued in turn without waiting, so the contexts' work overlaps on the GPU.
+ * Leaves every context exactly as its own calls (ether_metropolis, ether_learn_sweep) would.
+ * Asynchronous. */
+int ether_learn_batch_sweep(ether_learn *const *learns, int32_t n, int32_t nsweeps,
+                            int32_t plain_per_sweep);
 /* Device-side series for tau_int: nsteps steps of plain_per_step Metropolis sweeps then
- * learned_per_step learned sweeps, |M| of every replica after each step:
- * absM(R, nsteps) host array, step-major (index = t*R + r). */
+ * learned_per_step learned sweeps, |M| of every replica after every stride-th step:
+ * absM(R, nsteps / stride) host array, record-major (index = t*R + r). */
 int ether_learn_record_series(ether_learn *learn, int32_t nsteps, int32_t plain_per_step,
-                              int32_t learned_per_step, double *absM);
+                              int32_t learned_per_step, int32_t stride, double *absM);
 /* Accepted patches per replica since creation (accepted(R)). */
 int ether_learn_get_accepts(ether_learn *learn, uint64_t *accepted);
 /* Parameters: W1(n_inputs,128), b1(128), W2(128,128), b2(128), W3(128,n_outputs),

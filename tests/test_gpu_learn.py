@@ -195,4 +195,7 @@ def test_learned_series_recorder():
     assert lr.info().proposed == 25 * 2 * 8 * lr.info().patches_per_class
     m2 = lr.record_series(5, 0, 2)
     assert m2.shape == (8, 5)
+    m3 = lr.record_series(12, 1, 1, stride=4)  # |M| after steps 4, 8, 12
+    assert m3.shape == (8, 3)
+    np.testing.assert_allclose(m3[:, -1], np.linalg.norm(sw.tot_magnetisation(), axis=1), rtol=1e-12)
     lr.close()

@@ -213,4 +213,44 @@ def test_learned_series_recorder():
     assert m.shape == (8, 10)
     np.testing.assert_allclose(m[:, -1], np.linalg.norm(sw.tot_magnetisation(), axis=1), rtol=1e-12)
     assert lr.info().proposed == 10 * 2 * 8 * lr.info().patches_per_class
+    m3 = lr.record_series(9, 0, 1, stride=3)
+    assert m3.shape == (8, 3)
+    np.testing.assert_allclose(m3[:, -1], np.linalg.norm(sw.tot_magnetisation(), axis=1), rtol=1e-12)
     lr.close()
+
+
+def test_learn_batch_sweep_equals_each_contexts_own_calls():
+    """ether_learn_batch_sweep over an Ising and a Heisenberg context (different sizes):
+    spins and accepted patches as each context's own ether_metropolis + ether_learn_sweep."""
+    def pair():
+        out = []
+        for model, L, kT, seed in ((eg.MODEL_ISING, 16, 4.511, 3), (eg.MODEL_XYZ, 8, KTC, 4)):
+            lat = eg.simple_cubic(L)
+            sw = eg.Sweep.from_lattice(lat, eg.couplings(1, FM, [1.0]), np.array([1.0]), model, replicas=3,
+                                       seed=seed)
+            sw.set_beta([beta_of(kT)] * 3)
+            ion = lat.ion.copy()
+            rng = np.random.default_rng(seed)
+            if model == eg.MODEL_ISING:
+                ion[:, 3] = rng.choice([-1.0, 1.0], size=lat.N)
+            else:
+                v = rng.normal(size=(lat.N, 3))
+                ion[:, 1:4] = v / np.linalg.norm(v, axis=1, keepdims=True)
+            sw.set_spins(ion)
+            lr = eg.Learned(sw, seed=seed, capacity=4096)
+            if model == eg.MODEL_XYZ:
+                lr.set_params(random_params(6, scale=0.1))
+            out.append((lat, sw, lr))
+        return out
+    A, B = pair(), pair()
+    eg.learn_batch_sweep([lr for _, _, lr in A], nsweeps=4, plain_per_sweep=1)
+    for _ in range(4):
+        for _, sw, lr in B:
+            sw.metropolis(1, accept=False)
+            lr.sweep_(1)
+    for (lat, sa, la), (_, sb, lb) in zip(A, B):
+        for r in range(3):
+            np.testing.assert_array_equal(sa.get_spins(lat.ion, r), sb.get_spins(lat.ion, r))
+        np.testing.assert_array_equal(la.accepts(), lb.accepts())
+    for (_, sa, la), (_, sb, lb) in zip(A, B):
+        la.close(); lb.close(); sa.close(); sb.close()
