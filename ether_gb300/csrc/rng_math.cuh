@@ -141,12 +141,9 @@ ETHER_HD float logf_own(float x) {
 
 // log(1 - y) for y in [0, 1) without cancellation: for y < 1/2, 2 atanh(s) with
 // s = -y / (2 - y) (|s| <= 1/3, series through s^15: truncation < 1e-9); else the log of
-// 1 - y, which is exact there.  Both forms are evaluated and one is selected, so the lanes
-// of a warp do not diverge (the value is the branch's).
+// 1 - y, which is exact there.
 ETHER_HD float log1m_own(float y) {
-    const bool big = y >= 0.5f;
-    const float lbig = logf_own(big ? 1.0f - y : 1.0f);
-    y = big ? 0.0f : y;
+    if (y >= 0.5f) return logf_own(1.0f - y);
     const float s = -y / (2.0f - y);
     const float s2 = s * s;
     float p = 0.0666666667f;
@@ -157,7 +154,7 @@ ETHER_HD float log1m_own(float y) {
     p = fmaf(p, s2, 0.2f);
     p = fmaf(p, s2, 0.333333333f);
     p = fmaf(p, s2, 1.0f);
-    return big ? lbig : 2.0f * (s * p);
+    return 2.0f * (s * p);
 }
 
 // sin and cos for |x| <= 4: reduction by pi/2 (two-part constant), Taylor polynomials on
