@@ -144,31 +144,19 @@ sq_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CU
         const uint32_t rowbase = (uint32_t)(rq * 4 * 1024);  // atoms 4 rq .. 4 rq + 3
         const size_t e1row = (size_t)((h1_0 + j0) >> 4) * P.Kpad;
         const size_t e2row = (size_t)h2 * P.Kpad, e3row = (size_t)h3 * P.Kpad;
-        // phase factors of the first two k-blocks, then prefetched two blocks ahead (the
-        // producers otherwise wait on these L2 reads)
+        // phase factors of the first k-block, then prefetched one block ahead
         float2 e1 = P.E1[e1row + i], e2 = P.E2[e2row + i], e3 = P.E3[e3row + i], bq = P.bb[i];
-        float2 f1 = e1, f2 = e2, f3 = e3, fq = bq;
-        if (P.nk > 1) {
-            f1 = P.E1[e1row + kBK + i];
-            f2 = P.E2[e2row + kBK + i];
-            f3 = P.E3[e3row + kBK + i];
-            fq = P.bb[kBK + i];
-        }
         for (int kb = 0; kb < P.nk && ok; ++kb) {
             const int s = kb & 1, f = kb >> 1;
             const Cplx p23 = cmul(Cplx{e2.x, e2.y}, Cplx{e3.x, e3.y});
             Cplx z = cmul(Cplx{e1.x, e1.y}, p23);
             const Cplx b{bq.x, bq.y};
-            e1 = f1;
-            e2 = f2;
-            e3 = f3;
-            bq = fq;
-            if (kb + 2 < P.nk) {
-                const int nxt = (kb + 2) * kBK + i;
-                f1 = P.E1[e1row + nxt];
-                f2 = P.E2[e2row + nxt];
-                f3 = P.E3[e3row + nxt];
-                fq = P.bb[nxt];
+            if (kb + 1 < P.nk) {
+                const int nxt = (kb + 1) * kBK + i;
+                e1 = P.E1[e1row + nxt];
+                e2 = P.E2[e2row + nxt];
+                e3 = P.E3[e3row + nxt];
+                bq = P.bb[nxt];
             }
             if (f >= 1 && !mbar_wait(smem_u32(&empty[s]), (f - 1) & 1, P.err, 1)) { ok = false; break; }
             uint8_t *a_hi = base + s * stage_bytes + rowbase;
