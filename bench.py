@@ -364,6 +364,39 @@ def _time_batch(members, steps, warmup, config=None):
     return ms, info, cfg
 
 
+# the MCS-loop comparison's schedule: overrelaxation (exchange-only Heisenberg members) and PT
+# every 5 steps, a measurement every 10
+MCS_SCHEDULE = dict(tmcs_eq=0, coa=10, ovrr=True, ovrr_para=1.0, ovrr_mcs=5, pt=True,
+                    exchange_interval=5)
+
+
+def _time_batch_mcs(members, steps, config):
+    """Wall time per MCS step of the whole loop body (OVRR, sweep, PT, measurement) for every
+    member: one ether_batch_mcs call, against each member's own ether_mcs in turn.  The
+    warm-up is one period of the schedule's gates and the timed steps whole periods, so the
+    timed calls replay graphs captured in the warm-up."""
+    import ether_gb300 as eg
+    warmup = MCS_SCHEDULE["coa"]
+    steps = max(1, steps // warmup) * warmup
+    b = eg.Batch(members)
+    b.set_config(*config)
+    sc = b.mcs(0, warmup, **MCS_SCHEDULE)
+    t = time.perf_counter()
+    b.mcs(warmup, steps, swap_counts=sc, **MCS_SCHEDULE)   # synchronous: swap counters read back
+    batch_s = time.perf_counter() - t
+    event_ms = b.info().last_sweep_ms
+    b.close()
+    n0 = warmup + steps
+    sc = [m.mcs(n0, warmup, **MCS_SCHEDULE) for m in members]
+    t = time.perf_counter()
+    for m, s0 in zip(members, sc):
+        m.mcs(n0 + warmup, steps, swap_count=int(s0), **MCS_SCHEDULE)
+    own_s = time.perf_counter() - t
+    return {"schedule": MCS_SCHEDULE, "steps": steps,
+            "batch_ms_per_step": batch_s * 1e3 / steps, "batch_event_ms_per_step": event_ms,
+            "own_ms_per_step": own_s * 1e3 / steps, "speedup": own_s / batch_s}
+
+
 def _time_plain(members, steps, warmup):
     for m in members:
         m.metropolis(warmup, accept=False)
@@ -405,6 +438,8 @@ def run_batch(steps=200, warmup=5, chains=256, ladder=32, config=None, forms=(Fa
                "plain_value": float(info.site_updates_per_sweep) * plain_steps / (plain_s * 1e9),
                "plain_kernels_per_sweep": 3 * len(members)}
         res["speedup_vs_plain"] = res["value"] / res["plain_value"]
+        if plain and not grouped:
+            res["mcs"] = _time_batch_mcs(members, max(20, steps // 4), cfg)
         out["grouped" if grouped else "per_chain"] = res
         for m in members:
             m.close()

@@ -151,6 +151,7 @@ SIGNATURES = {
     "ether_batch_create": (C.c_int, [C.POINTER(P), C.c_int32, C.POINTER(P)]),
     "ether_batch_destroy": (C.c_int, [P]),
     "ether_batch_metropolis": (C.c_int, [P, C.c_int32]),
+    "ether_batch_mcs": (C.c_int, [P, C.POINTER(Schedule), C.c_int32, C.c_int32, PI32]),
     "ether_batch_set_config": (C.c_int, [P, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "ether_batch_autotune": (C.c_int, [P, PI32, C.POINTER(C.c_float)]),
     "ether_batch_get_info": (C.c_int, [P, C.POINTER(BatchInfo)]),

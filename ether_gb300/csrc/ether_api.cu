@@ -679,7 +679,9 @@ int ensure_stage(Ctx &c, size_t bytes) {
     return ETHER_OK;
 }
 
-// Runs f(k) for k in [0, n) on up to host_threads() threads (f must not throw).
+// Runs f(k) for k in [0, n) on up to host_threads() threads (f must not throw).  The
+// workers make the caller's device current first: a new thread starts on device 0, and f
+// issues copies on streams of the caller's device.
 template <class F>
 void parallel_for(int n, F f) {
     const int T = std::min(n, host_threads());
@@ -687,11 +689,14 @@ void parallel_for(int n, F f) {
         for (int k = 0; k < n; ++k) f(k);
         return;
     }
+    int dev = 0;
+    cudaGetDevice(&dev);
     std::atomic<int> next{0};
     std::vector<std::thread> pool;
     pool.reserve(T);
     for (int t = 0; t < T; ++t)
         pool.emplace_back([&]() {
+            cudaSetDevice(dev);
             for (int k = next.fetch_add(1); k < n; k = next.fetch_add(1)) f(k);
         });
     for (auto &th : pool) th.join();
@@ -1017,26 +1022,78 @@ extern "C" int ether_get_slots(ether_ctx *h, int32_t *slot_of_replica) {
     return ETHER_OK;
 }
 
-// One MCS of src/ether.f90:163-201 given its gates: OVRR (:163-169), Metropolis (:172),
-// total energy + PT when PT runs (:177, :189-198; the swap counter lives on the device),
-// observable on measurement steps (:201).
-static int issue_step(Ctx &c, const ether_schedule *sch, bool ovrr, bool pt, bool meas) {
-    if (ovrr) {
-        int rc = overrelax_once(c, sch->ovrr_para);
-        if (rc) return rc;
-    }
-    int rc = sweep_once(c);
-    if (rc) return rc;
-    if (pt) {
+namespace ether {
+
+// Whether src/ether.f90:163-169 overrelaxes this context at all: XYZ spins with neither a
+// field nor anisotropy (overrelaxation conserves the exchange energy only).
+bool mcs_ovrr_on(const Ctx &c, const ether_schedule *sch) {
+    return sch->ovrr && c.model == ETHER_MODEL_XYZ && !c.zeeman && !c.sia && !c.sia_local && sch->ovrr_mcs > 0;
+}
+
+int mcs_check(const Ctx &c, const ether_schedule *sch) {
+    if (!c.beta_set) return fail(ETHER_ERR_STATE, "beta not set");
+    const bool pt_on = sch->pt && sch->exchange_interval > 0;
+    if (pt_on && !(c.flags & ETHER_FLAG_PT_REFERENCE_COPY) && c.n_slots < 2)
+        return fail(ETHER_ERR_STATE, "PT needs a ladder of at least two slots");
+    return ETHER_OK;
+}
+
+// The gates of MCS step `step`: bit 0 overrelaxation (:163-169), bit 1 total energy + PT
+// (:177, :189-198), bit 2 observable (:201).
+int mcs_gates(const Ctx &c, const ether_schedule *sch, int step) {
+    const bool ov = mcs_ovrr_on(c, sch) && step % sch->ovrr_mcs == 0 && step % sch->coa != 0;
+    const bool pt = sch->pt && sch->exchange_interval > 0 && step % sch->exchange_interval == 0 &&
+                    step % sch->coa != 0;
+    const bool me = step > sch->tmcs_eq && step % sch->coa == 0;
+    return (ov ? 1 : 0) | (pt ? 2 : 0) | (me ? 4 : 0);
+}
+
+// The parts of one MCS before and after the Metropolis sweep, on the context's stream.
+int mcs_before_sweep(Ctx &c, const ether_schedule *sch, int gates) {
+    if (gates & 1) return overrelax_once(c, sch->ovrr_para);
+    return ETHER_OK;
+}
+
+int mcs_after_sweep(Ctx &c, int gates) {
+    if (gates & 2) {
         CUDA_TRY(launch_energy_mag(c, true));
-        CUDA_TRY(launch_pt(c, -1));
+        CUDA_TRY(launch_pt(c, -1));  // the swap counter lives on the device
     }
-    if (meas) {
+    if (gates & 4) {
         CUDA_TRY(launch_energy_mag(c, true));
         CUDA_TRY(launch_measure(c));
         if (c.spiral_ptr) CUDA_TRY(launch_spiral_measure(c));  // src/observable.f90:41
     }
     return ETHER_OK;
+}
+
+// The period of the gates in steps.
+long mcs_period(const ether_schedule *sch, bool ovrr_on, bool pt_on) {
+    auto lcm = [](long x, long y) { long g = x, b = y; while (b) { long t = g % b; g = b; b = t; } return x / g * y; };
+    long period = sch->coa;
+    if (ovrr_on) period = lcm(period, sch->ovrr_mcs);
+    if (pt_on) period = lcm(period, sch->exchange_interval);
+    return period;
+}
+
+// Steps per captured chunk: the period of the gates, kept between 1 and 256 steps (at least 8
+// where doubling allows).
+int mcs_chunk(long period) {
+    int chunk = (int)(period <= 256 ? period : 64);
+    while (chunk < 8 && chunk * 2 <= 256) chunk *= 2;
+    return chunk;
+}
+
+}  // namespace ether
+
+// One MCS of src/ether.f90:163-201 given its gates: OVRR (:163-169), Metropolis (:172),
+// total energy + PT when PT runs (:177, :189-198), observable on measurement steps (:201).
+static int issue_step(Ctx &c, const ether_schedule *sch, int gates) {
+    int rc = mcs_before_sweep(c, sch, gates);
+    if (rc) return rc;
+    rc = sweep_once(c);
+    if (rc) return rc;
+    return mcs_after_sweep(c, gates);
 }
 
 static int variant_of(const Ctx &c);
@@ -1046,7 +1103,7 @@ static int variant_of(const Ctx &c);
 static int issue_steps(Ctx &c, const ether_schedule *sch, const int8_t *sig, int n) {
     if (!c.resident) {
         for (int k = 0; k < n; ++k) {
-            int rc = issue_step(c, sch, sig[k] & 1, sig[k] & 2, sig[k] & 4);
+            int rc = issue_step(c, sch, sig[k]);
             if (rc) return rc;
         }
         return ETHER_OK;
@@ -1086,28 +1143,18 @@ extern "C" int ether_mcs(ether_ctx *h, const ether_schedule *sch, int32_t step0,
                          int32_t *swap_count) {
     if (!h || !sch) return fail(ETHER_ERR_ARG, "null argument");
     Ctx &c = h->c;
-    if (!c.beta_set) return fail(ETHER_ERR_STATE, "beta not set");
     if (sch->coa <= 0 || nsteps < 0 || step0 < 0)
         return fail(ETHER_ERR_ARG, "coa must be positive, step0 and nsteps >= 0");
-    const bool ovrr_on = sch->ovrr && c.model == ETHER_MODEL_XYZ && !c.zeeman && !c.sia && !c.sia_local &&
-                         sch->ovrr_mcs > 0;
+    {
+        const int rc = mcs_check(c, sch);
+        if (rc) return rc;
+    }
+    const bool ovrr_on = mcs_ovrr_on(c, sch);
     const bool pt_on = sch->pt && sch->exchange_interval > 0;
-    if (pt_on && !(c.flags & ETHER_FLAG_PT_REFERENCE_COPY) && c.n_slots < 2)
-        return fail(ETHER_ERR_STATE, "PT needs a ladder of at least two slots");
     const int32_t sc0 = swap_count ? *swap_count : 0;
     CUDA_TRY(cudaMemcpyAsync(c.swap_dev, &sc0, sizeof(int32_t), cudaMemcpyHostToDevice, c.stream));
-    auto gate = [&](int step, bool &ov, bool &pt, bool &me) {
-        ov = ovrr_on && step % sch->ovrr_mcs == 0 && step % sch->coa != 0;
-        pt = pt_on && step % sch->exchange_interval == 0 && step % sch->coa != 0;
-        me = step > sch->tmcs_eq && step % sch->coa == 0;
-    };
-    // chunk length: the period of the gates, kept between 1 and 256 steps
-    long period = sch->coa;
-    auto lcm = [](long x, long y) { long g = x, b = y; while (b) { long t = g % b; g = b; b = t; } return x / g * y; };
-    if (ovrr_on) period = lcm(period, sch->ovrr_mcs);
-    if (pt_on) period = lcm(period, sch->exchange_interval);
-    int chunk = (int)(period <= 256 ? period : 64);
-    while (chunk < 8 && chunk * 2 <= 256) chunk *= 2;
+    const long period = mcs_period(sch, ovrr_on, pt_on);
+    int chunk = mcs_chunk(period);
     // resident contexts: the longest multiple of the period up to 256 steps, so that the
     // eventless stretches (equilibration) run as few long resident launches
     if (c.resident && period <= 256) chunk = (int)(256 / period * period);
@@ -1118,19 +1165,16 @@ extern "C" int ether_mcs(ether_ctx *h, const ether_schedule *sch, int32_t step0,
         const int n = std::min(chunk, last - step + 1);
         std::vector<int8_t> sig;
         sig.reserve(n + 1);
-        bool ov, pt, me;
-        for (int k = 0; k < n; ++k) {
-            gate(step + k, ov, pt, me);
-            sig.push_back((int8_t)((ov ? 1 : 0) | (pt ? 2 : 0) | (me ? 4 : 0)));
-        }
+        for (int k = 0; k < n; ++k) sig.push_back((int8_t)mcs_gates(c, sch, step + k));
         if (!use_graphs || n < 4) {
             int rc = issue_steps(c, sch, sig.data(), n);
             if (rc) return rc;
         } else {
-            // the kernel variant is part of the key: a graph keeps the kernels it was captured with
+            // the kernel variant and the ladder's shape are part of the key: a graph keeps the
+            // kernels and launch arguments it was captured with
             std::string key(sig.begin(), sig.end());
-            key += std::to_string(variant_of(c)) + "/" + std::to_string(sch->ovrr_para) +
-                   (c.spiral_ptr ? "/s" : "");
+            key += std::to_string(variant_of(c)) + "/" + std::to_string(sch->ovrr_para) + "/" +
+                   std::to_string(c.n_slots) + (c.spiral_ptr ? "/s" : "");
             auto it = c.graphs.find(key);
             if (it == c.graphs.end()) {
                 if (c.graphs.size() >= 64) {
@@ -1279,7 +1323,8 @@ int ctx_variant(const Ctx &c) { return variant_of(c); }
 //           or 4000 + 10 * vectors per thread and step + 1 / 4 (register cap): the
 //           shared-memory staged kernel (4011, 4014, 4021, 4041)
 //           or 5000 + 10 * sites per thread + register cap (blocks per SM) for the
-//           simple-cubic XYZ kernel (5011 .. 5015, 5021, 5022)
+//           simple-cubic XYZ kernel (5011 .. 5015, 5021 .. 5024, 5041, 5042; with two or
+//           more sites per thread a warp draws the second Philox block of its sites together)
 static bool apply_variant(Ctx &c, int variant) {
     if (c.model == ETHER_MODEL_XYZ) {
         if (!xyz_variant_valid(variant - 5000)) return false;
@@ -1347,7 +1392,7 @@ static int autotune_xyz(Ctx &c, int32_t *variant, float *best_ms) {
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    for (int cand : {5011, 5012, 5013, 5014, 5015, 5021, 5022}) {
+    for (int cand : {5011, 5012, 5013, 5014, 5015, 5021, 5022, 5023, 5024, 5041, 5042}) {
         if (!apply_variant(c, cand)) continue;
         CUDA_TRY(launch_xyz_sweep(c, 0));  // warm-up
         CUDA_TRY(cudaEventRecord(e0, c.stream));

@@ -161,6 +161,16 @@ int energy_blocks(const Ctx &c);
 int plain_sweep(Ctx &c);  // one Metropolis sweep of every replica (ETHER_OK or an error code)
 int ctx_variant(const Ctx &c);  // the context's kernel variant code (ether_set_variant's numbering)
 void *tma_encode_tiled_fn();    // cuTensorMapEncodeTiled (PFN_cuTensorMapEncodeTiled_v12000), or null
+
+// Pieces of one MCS of src/ether.f90:159-203, shared by ether_mcs and ether_batch_mcs.  The
+// launches go to c.stream.
+bool mcs_ovrr_on(const Ctx &c, const ether_schedule *sch);     // overrelaxes at all
+int mcs_check(const Ctx &c, const ether_schedule *sch);        // beta set, PT ladder
+int mcs_gates(const Ctx &c, const ether_schedule *sch, int step);  // 1 OVRR, 2 PT, 4 measure
+int mcs_before_sweep(Ctx &c, const ether_schedule *sch, int gates);
+int mcs_after_sweep(Ctx &c, int gates);
+long mcs_period(const ether_schedule *sch, bool ovrr_on, bool pt_on);
+int mcs_chunk(long period);
 void set_error(const std::string &msg);
 int structure_factor_launch(Ctx &c, const double *frac, const int nq[3], const double q0[3],
                             const double dq[3], float *sq_host, float *comp_host, std::string &msg);

@@ -299,6 +299,7 @@ struct ether_batch {
     int cls_grid[kNumClasses] = {};     // resident blocks per SM x SMs, per class
     long long updates_per_sweep = 0;
     cudaGraphExec_t graph = nullptr;
+    std::map<std::string, cudaGraphExec_t> mcs_graphs;  // ether_batch_mcs chunks by gate pattern
     bool dirty = true;
     uint64_t launches = 0;
     float last_ms = 0.f;
@@ -399,6 +400,11 @@ int class_of(const BatchMember &m) {
     }
 }
 
+void drop_mcs_graphs(ether_batch &b) {
+    for (auto &kv : b.mcs_graphs) cudaGraphExecDestroy(kv.second);
+    b.mcs_graphs.clear();
+}
+
 int rebuild(ether_batch &b) {
     std::vector<BatchMember> hm;
     hm.reserve(b.members.size());
@@ -419,6 +425,7 @@ int rebuild(ether_batch &b) {
         cudaGraphExecDestroy(b.graph);
         b.graph = nullptr;
     }
+    drop_mcs_graphs(b);
     b.h_members = hm;
     if (!b.d_members) BCUDA(cudaMalloc((void **)&b.d_members, hm.size() * sizeof(BatchMember)));
     BCUDA(cudaMemcpyAsync(b.d_members, hm.data(), hm.size() * sizeof(BatchMember), cudaMemcpyHostToDevice, b.stream));
@@ -538,19 +545,35 @@ int rebuild(ether_batch &b) {
     return ETHER_OK;
 }
 
+// Branches 0 .. n-1 exist and wait for the work queued so far on the batch stream.
+int fork_branches(ether_batch &b, int n) {
+    while ((int)b.branch.size() < n) {
+        cudaStream_t st = nullptr;
+        cudaEvent_t ev = nullptr;
+        BCUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        b.branch.push_back(st);
+        BCUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        b.ev_join.push_back(ev);
+    }
+    BCUDA(cudaEventRecord(b.ev_fork, b.stream));
+    for (int k = 0; k < n; ++k) BCUDA(cudaStreamWaitEvent(b.branch[k], b.ev_fork, 0));
+    return ETHER_OK;
+}
+
+// The batch stream waits for branches 0 .. n-1.
+int join_branches(ether_batch &b, int n) {
+    for (int k = 0; k < n; ++k) {
+        BCUDA(cudaEventRecord(b.ev_join[k], b.branch[k]));
+        BCUDA(cudaStreamWaitEvent(b.stream, b.ev_join[k], 0));
+    }
+    return ETHER_OK;
+}
+
 int issue_sweep(ether_batch &b) {
     const int nbr = std::min(b.n_branch, b.n_groups);
     if (nbr > 1) {
-        while ((int)b.branch.size() < nbr) {
-            cudaStream_t st = nullptr;
-            cudaEvent_t ev = nullptr;
-            BCUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-            b.branch.push_back(st);
-            BCUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-            b.ev_join.push_back(ev);
-        }
-        BCUDA(cudaEventRecord(b.ev_fork, b.stream));
-        for (int k = 0; k < nbr; ++k) BCUDA(cudaStreamWaitEvent(b.branch[k], b.ev_fork, 0));
+        const int rc = fork_branches(b, nbr);
+        if (rc) return rc;
     }
     const int per_group = b.max_col * kNumClasses;
     for (int g = 0; g < b.n_groups; ++g) {
@@ -577,11 +600,10 @@ int issue_sweep(ether_batch &b) {
             }
         }
     }
-    if (nbr > 1)
-        for (int k = 0; k < nbr; ++k) {
-            BCUDA(cudaEventRecord(b.ev_join[k], b.branch[k]));
-            BCUDA(cudaStreamWaitEvent(b.stream, b.ev_join[k], 0));
-        }
+    if (nbr > 1) {
+        const int rc = join_branches(b, nbr);
+        if (rc) return rc;
+    }
     batch_advance_kernel<<<(b.total_R + 255) / 256, 256, 0, b.stream>>>(b.d_step_of, b.total_R);
     BCUDA(cudaGetLastError());
     return ETHER_OK;
@@ -639,6 +661,55 @@ int run_sweeps(ether_batch &b, int nsweeps, bool timed) {
     return ETHER_OK;
 }
 
+// A member's kernels go to a stream of the batch (its stream or a branch) while this is in scope.
+struct OnBatchStream {
+    Ctx &c;
+    cudaStream_t own;
+    OnBatchStream(Ctx &ctx, cudaStream_t st) : c(ctx), own(ctx.stream) { c.stream = st; }
+    ~OnBatchStream() { c.stream = own; }
+};
+
+constexpr int kMemberBranches = 8;
+
+// The members' own parts of one step (gates g[m]): before the sweep their overrelaxation,
+// after it their PT and measurement.  The members' kernels are small and independent, so
+// they are spread over up to kMemberBranches parallel branches.
+int issue_member_parts(ether_batch &b, const ether_schedule *sch, const int8_t *g, bool before) {
+    const int M = (int)b.members.size();
+    const int mask = before ? 1 : 6;
+    int need = 0;
+    for (int m = 0; m < M; ++m) need += (g[m] & mask) ? 1 : 0;
+    if (need == 0) return ETHER_OK;
+    const int nbr = std::min(kMemberBranches, need);
+    if (nbr > 1) {
+        const int rc = fork_branches(b, nbr);
+        if (rc) return rc;
+    }
+    for (int m = 0, k = 0; m < M; ++m) {
+        if (!(g[m] & mask)) continue;
+        OnBatchStream on(b.members[m]->c, nbr > 1 ? b.branch[k++ % nbr] : b.stream);
+        const int rc = before ? mcs_before_sweep(on.c, sch, g[m]) : mcs_after_sweep(on.c, g[m]);
+        if (rc) return rc;
+    }
+    return nbr > 1 ? join_branches(b, nbr) : ETHER_OK;
+}
+
+// Steps of the MCS loop, gates sig[k * M + m] for step k and member m: every member's
+// overrelaxation, the batch sweep, every member's PT and measurement.
+int issue_mcs_steps(ether_batch &b, const ether_schedule *sch, const int8_t *sig, int n) {
+    const int M = (int)b.members.size();
+    for (int k = 0; k < n; ++k) {
+        int rc = issue_member_parts(b, sch, sig + (size_t)k * M, true);
+        if (rc) return rc;
+        rc = issue_sweep(b);
+        if (rc) return rc;
+        rc = issue_member_parts(b, sch, sig + (size_t)k * M, false);
+        if (rc) return rc;
+    }
+    b.launches += (uint64_t)n * kernels_per_sweep(b);
+    return ETHER_OK;
+}
+
 }  // namespace
 
 extern "C" int ether_batch_create(ether_ctx *const *members, int32_t n_members, ether_batch **out) {
@@ -686,6 +757,7 @@ extern "C" int ether_batch_destroy(ether_batch *b) {
     if (!b) return ETHER_OK;
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->graph) cudaGraphExecDestroy(b->graph);
+    drop_mcs_graphs(*b);
     for (cudaEvent_t ev : b->ev_member)
         if (ev) cudaEventDestroy(ev);
     if (b->ev_done) cudaEventDestroy(b->ev_done);
@@ -712,6 +784,82 @@ extern "C" int ether_batch_metropolis(ether_batch *b, int32_t nsweeps) {
     rc = run_sweeps(*b, nsweeps, true);
     if (rc) return rc;
     b->timed_sweeps = nsweeps;
+    return release_members(*b);
+}
+
+extern "C" int ether_batch_mcs(ether_batch *b, const ether_schedule *sch, int32_t step0, int32_t nsteps,
+                               int32_t *swap_counts) {
+    if (!b || !sch) return bfail(ETHER_ERR_ARG, "null argument");
+    if (sch->coa <= 0 || nsteps < 0 || step0 < 0)
+        return bfail(ETHER_ERR_ARG, "coa must be positive, step0 and nsteps >= 0");
+    const int M = (int)b->members.size();
+    bool ovrr_on = false;
+    for (ether_ctx *h : b->members) {
+        const int rc = mcs_check(h->c, sch);
+        if (rc) return rc;
+        ovrr_on = ovrr_on || mcs_ovrr_on(h->c, sch);
+    }
+    const bool pt_on = sch->pt && sch->exchange_interval > 0;
+    int rc = rebuild(*b);
+    if (rc) return rc;
+    rc = join_members(*b);
+    if (rc) return rc;
+    // every member's device swap counter starts from the caller's value, as ether_mcs does
+    std::vector<int32_t> sc(M, 0);
+    if (swap_counts) sc.assign(swap_counts, swap_counts + M);
+    for (int m = 0; m < M; ++m)
+        BCUDA(cudaMemcpyAsync(b->members[m]->c.swap_dev, &sc[m], sizeof(int32_t), cudaMemcpyHostToDevice, b->stream));
+    const int chunk = mcs_chunk(mcs_period(sch, ovrr_on, pt_on));
+    // the key's tail: what the captured launches take besides the gates
+    std::string tail = "/" + std::to_string(sch->ovrr_para);
+    for (ether_ctx *h : b->members)
+        tail += "/" + std::to_string(h->c.n_slots) + (h->c.spiral_ptr ? "s" : "");
+    BCUDA(cudaEventRecord(b->ev_t0, b->stream));
+    std::vector<int8_t> sig;
+    for (int step = step0 + 1, last = step0 + nsteps; step <= last;) {
+        const int n = std::min(chunk, last - step + 1);
+        sig.clear();
+        for (int k = 0; k < n; ++k)
+            for (int m = 0; m < M; ++m) sig.push_back((int8_t)mcs_gates(b->members[m]->c, sch, step + k));
+        if (n < 4) {
+            rc = issue_mcs_steps(*b, sch, sig.data(), n);
+            if (rc) return rc;
+        } else {
+            std::string key(sig.begin(), sig.end());
+            key += tail;
+            auto it = b->mcs_graphs.find(key);
+            if (it == b->mcs_graphs.end()) {
+                if (b->mcs_graphs.size() >= 64) drop_mcs_graphs(*b);
+                cudaGraph_t g = nullptr;
+                BCUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+                const uint64_t before = b->launches;
+                rc = issue_mcs_steps(*b, sch, sig.data(), n);
+                b->launches = before;
+                cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+                if (rc) {
+                    if (g) cudaGraphDestroy(g);
+                    return rc;
+                }
+                if (e != cudaSuccess) return bfail(ETHER_ERR_CUDA, std::string("batch MCS capture: ") + cudaGetErrorString(e));
+                cudaGraphExec_t ex = nullptr;
+                e = cudaGraphInstantiate(&ex, g, 0);
+                cudaGraphDestroy(g);
+                if (e != cudaSuccess) return bfail(ETHER_ERR_CUDA, std::string("batch MCS instantiate: ") + cudaGetErrorString(e));
+                it = b->mcs_graphs.emplace(key, ex).first;
+            }
+            BCUDA(cudaGraphLaunch(it->second, b->stream));
+            b->launches += (uint64_t)n * kernels_per_sweep(*b);
+        }
+        step += n;
+    }
+    BCUDA(cudaEventRecord(b->ev_t1, b->stream));
+    b->timed_sweeps = nsteps;
+    if (swap_counts) {
+        for (int m = 0; m < M; ++m)
+            BCUDA(cudaMemcpyAsync(&sc[m], b->members[m]->c.swap_dev, sizeof(int32_t), cudaMemcpyDeviceToHost, b->stream));
+        BCUDA(cudaStreamSynchronize(b->stream));
+        std::copy(sc.begin(), sc.end(), swap_counts);
+    }
     return release_members(*b);
 }
 

@@ -416,6 +416,18 @@ class Batch:
     def metropolis(self, nsweeps=1):
         abi.check(self.lib.ether_batch_metropolis(self.h, nsweeps))
 
+    def mcs(self, step0, nsteps, tmcs_eq, coa, ovrr=False, ovrr_para=0.0, ovrr_mcs=0, pt=False,
+            exchange_interval=11, swap_counts=None):
+        """The MCS loop of every member under one schedule (Sweep.mcs's arguments); returns
+        the members' PT swap counters (started from swap_counts, default all 0)."""
+        s = abi.Schedule(tmcs_eq, coa, int(ovrr), float(ovrr_para), ovrr_mcs, int(pt),
+                         exchange_interval)
+        sc = np.zeros(len(self.members), dtype=np.int32)
+        if swap_counts is not None:
+            sc[:] = swap_counts
+        abi.check(self.lib.ether_batch_mcs(self.h, C.byref(s), step0, nsteps, abi.iptr(sc)))
+        return sc
+
     def set_config(self, threads=256, units_per_thread=2, blocks_per_sm=0, walk=0):
         abi.check(self.lib.ether_batch_set_config(self.h, threads, units_per_thread,
                                                   blocks_per_sm, walk))

@@ -194,6 +194,13 @@ module ether_gpu_mod
             type(c_ptr), value :: batch
             integer(c_int32_t), value :: nsweeps
         end function
+        integer(c_int) function ether_batch_mcs(batch, sch, step0, nsteps, swap_counts) bind(C, name="ether_batch_mcs")
+            import :: c_int, c_ptr, c_int32_t, ether_schedule
+            type(c_ptr), value :: batch
+            type(ether_schedule), intent(in) :: sch
+            integer(c_int32_t), value :: step0, nsteps
+            integer(c_int32_t), intent(inout) :: swap_counts(*)
+        end function
         integer(c_int) function ether_batch_autotune(batch, config, best_ms) bind(C, name="ether_batch_autotune")
             import :: c_int, c_ptr, c_int32_t, c_float
             type(c_ptr), value :: batch

@@ -243,7 +243,8 @@ int ether_end_sweep(ether_ctx *ctx);
  * class for the process.  Ising simple cubic: variant = 1000 (persistent) + 2000 (register
  * cap) + bytes per vector (4, 8, 16) * 10 + vectors per thread, or 4000 + 10 * vectors per step + 1 / 4
  * (shared-memory staged kernel).  XYZ simple cubic: variant = 5000 + 10 * sites per thread +
- * blocks per SM of the register cap (5011 .. 5015, 5021, 5022).  best_ms = one colour phase.  Either
+ * blocks per SM of the register cap (5011 .. 5015, 5021 .. 5024, 5041, 5042).  best_ms = one colour
+ * phase.  Either
  * output may be NULL. */
 int ether_autotune(ether_ctx *ctx, int32_t *variant, float *best_ms);
 /* Force a kernel variant (same encoding as ether_autotune). */
@@ -299,6 +300,17 @@ int ether_batch_destroy(ether_batch *batch);
 /* nsweeps Metropolis sweeps of every member (no overrelaxation, no PT: those stay per
  * member).  Asynchronous; ether_batch_get_info reads the time it took. */
 int ether_batch_metropolis(ether_batch *batch, int32_t nsweeps);
+/* The MCS loop body of src/ether.f90:159-203 (as ether_mcs) for every member at once, steps
+ * step0+1 .. step0+nsteps under one schedule: each step runs every member's overrelaxation
+ * where its gate is open (:163-169), one batch sweep (:172), then every member's total energy
+ * + PT (:177, :189-198) and observable (:201) where theirs are; members that cannot
+ * overrelax (Ising, field, anisotropy) skip that part, as in ether_mcs.  Chunks of steps are
+ * captured once per gate pattern and replayed.  swap_counts(n_members), in and out, is each
+ * member's PT swap counter (NULL: all start at 0).  Leaves every member exactly as
+ * ether_mcs(member, sch, step0, nsteps, &swap_counts[m]) would.  Synchronous only when
+ * swap_counts is given.  ether_batch_get_info's last_sweep_ms gives the time per MCS step. */
+int ether_batch_mcs(ether_batch *batch, const ether_schedule *sch, int32_t step0, int32_t nsteps,
+                    int32_t *swap_counts);
 /* Tile shape: threads per block (64/128/256), units per thread (1..64; a unit is a 16-, 8-
  * or 4-byte vector of simple-cubic Ising sites, or one site of a general Ising lattice or of
  * XYZ), resident blocks per SM (0 = as many as fit) and the walk over the tiles (0: block b
@@ -317,7 +329,8 @@ typedef struct ether_batch_info {
     int32_t kernels_per_sweep; /* colour phases + the counter advance                       */
     int64_t site_updates_per_sweep;
     uint64_t kernel_launches;  /* kernels launched by this batch so far                     */
-    float last_sweep_ms;       /* CUDA-event time per sweep of the last ether_batch_metropolis */
+    float last_sweep_ms;       /* CUDA-event time per sweep of the last ether_batch_metropolis
+                                  (per MCS step of the last ether_batch_mcs)                */
 } ether_batch_info;
 int ether_batch_get_info(ether_batch *batch, ether_batch_info *info);
 /* The cudaStream_t the batch launches on. */

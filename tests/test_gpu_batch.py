@@ -242,3 +242,35 @@ def test_batch_members_with_local_axis_anisotropy():
         sw.metropolis(4)
     assert_same(states(A), states(B))
     batch.close()
+
+
+def test_batch_mcs_equals_each_members_own_mcs():
+    """ether_batch_mcs against every member's own ether_mcs under one schedule (overrelaxation
+    every 3 steps, PT every 2, measurement every 4 after 6 equilibration steps): spins,
+    acceptance counters, slot permutations, measurement sums and swap counters bit for bit,
+    over a captured chunk (24 steps) and a short direct one (3 steps).  Members: Ising and
+    XYZ on simple-cubic and pyrochlore lattices, and an XYZ member with a field, which does
+    not overrelax."""
+    zs = {"zeeman": True, "h": (0.0, 0.3, 1.0), "g_factor": 2.0}
+    specs = [SPECS[0], SPECS[2], SPECS[5], SPECS[6], SPECS[8],
+             (lambda: eg.simple_cubic(8), eg.MODEL_XYZ, FM, 2, 0, zs)]
+    sch = dict(tmcs_eq=6, coa=4, ovrr=True, ovrr_para=0.5, ovrr_mcs=3, pt=True, exchange_interval=2)
+    A = build_members(specs)
+    B = build_members(specs)
+    for _, sw in A + B:
+        sw.zero_avg()
+    batch = eg.Batch([sw for _, sw in A])
+    swaps = batch.mcs(0, 24, swap_counts=[5 * k for k in range(len(specs))], **sch)
+    swaps = batch.mcs(24, 3, swap_counts=swaps, **sch)
+    own = []
+    for k, (_, sw) in enumerate(B):
+        s = sw.mcs(0, 24, swap_count=5 * k, **sch)
+        own.append(sw.mcs(24, 3, swap_count=s, **sch))
+    np.testing.assert_array_equal(swaps, own)
+    assert_same(states(A), states(B))
+    for (_, a), (_, b) in zip(A, B):
+        np.testing.assert_array_equal(a.slots(), b.slots())
+        np.testing.assert_array_equal(a.sums(), b.sums())
+    assert all(b_.sums()[:, 0].max() > 0 for _, b_ in B)  # measurements happened
+    assert batch.info().last_sweep_ms > 0.0
+    batch.close()

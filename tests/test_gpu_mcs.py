@@ -45,6 +45,27 @@ def test_graph_replay_equals_direct_launches(model):
     np.testing.assert_array_equal(a[4], b[4])
 
 
+def test_graph_replay_after_a_ladder_change():
+    """ether_mcs, a new ladder with another slot count (4 slots x 2 groups -> 2 slots x 4
+    groups), and ether_mcs again over steps with the same gate pattern: the graphs captured
+    for the first ladder are not replayed with its launch arguments; the run equals direct
+    launches."""
+    lat = eg.simple_cubic(12)
+    sch = dict(tmcs_eq=0, coa=5, ovrr=True, ovrr_para=0.5, ovrr_mcs=3, pt=True, exchange_interval=4)
+    runs = []
+    for flags in (0, eg.FLAG_NO_GRAPHS):
+        sw, _ = make_pair(lat, eg.MODEL_XYZ, FM, replicas=8, flags=flags)
+        sw.set_ladder([beta_of(1.443 * f) for f in (0.9, 1.0, 1.1, 1.3)])
+        sw.set_spins(random_xyz(lat, 4))
+        sc = sw.mcs(0, 60, **sch)
+        sw.set_ladder([beta_of(1.443 * f) for f in (0.8, 1.2)])
+        sc = sw.mcs(60, 60, swap_count=sc, **sch)
+        runs.append((_state(sw, lat), sw.sums(), sw.slots(), sc))
+    a, b = runs
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+
+
 def test_mcs_equals_the_reference_call_sequence():
     """ether_mcs == the host loop of src/ether.f90:159-203 through the single-call entries."""
     lat = eg.simple_cubic(16)
