@@ -187,7 +187,12 @@ constexpr float kTwoPiF = 6.28318548f;
 constexpr int kMarsagliaMaxPairs = 64;
 
 // Proposal of update_spin_details (src/update_spin_details.f90:30-51) in FP32: Marsaglia
-// (George_Marsaglia.f90:29-39) or ANGLE, then normalisation.  The Marsaglia pairs come in
+// (George_Marsaglia.f90:29-39) or ANGLE.  The reference then divides by the norm
+// (update_spin_details.f90:50-51).  Both proposals are unit vectors by construction
+// (4s(1-s) + (1-2s)^2 = 1; (1-z^2)(cos^2 + sin^2) + z^2 = 1), so in FP32 that division only
+// moves the components by a few units in the last place; it is left out here and in the
+// FP32 mirror (the FP64 replay keeps it).  A proposal replaces the spin whole, so the length
+// error does not accumulate.  The Marsaglia pairs come in
 // order p = 0, 1, 2, ...: pair 0 is words 1,2 of block 0 (word 0 is eta); pair p >= 1 is
 // block (p+1)/2, words 0,1 for odd p and 2,3 for even p.  The first accepted pair wins.
 // Blocks 0 and 1 (pairs 0-2, 99% of sites) are drawn by the caller and chosen among with
@@ -247,10 +252,9 @@ ETHER_HD bool propose(bool angle, float dphi, const Spin4 &S, uint32_t c0, uint3
         nx = r * cs;
         ny = r * sn;
     }
-    float inv = 1.0f / sqrtf(nx * nx + ny * ny + nz * nz);
-    out->x = nx * inv;
-    out->y = ny * inv;
-    out->z = nz * inv;
+    out->x = nx;
+    out->y = ny;
+    out->z = nz;
     out->w = nphi;
     return true;
 }

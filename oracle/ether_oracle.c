@@ -583,8 +583,8 @@ static int xyz_site_f32(const orc_sys *sy, const double *ion, float *sp4, int i,
         nx = r * cs;
         ny = r * sn;
     }
-    float inv = 1.0f / sqrtf(nx * nx + ny * ny + nz * nz);
-    nx = nx * inv; ny = ny * inv; nz = nz * inv;
+    /* no division by the norm: the FP32 kernels leave out update_spin_details.f90:50-51,
+     * whose effect on these unit-length proposals is a few ulp (the FP64 replay keeps it) */
     float dx = nx - S[0], dy = ny - S[1], dz = nz - S[2];
     float e = dx * h[0];
     e = fmaf(dy, h[1], e);
