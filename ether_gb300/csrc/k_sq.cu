@@ -15,10 +15,13 @@
 //
 // One CTA owns a 128-row tile of D (64 q-points: consecutive h1 at fixed h2, h3) and all
 // 3R columns (<= 256).  Per 64-site k-block:
-//   * warps 0-7 generate the A tile in shared memory: phase factors
-//       exp(i q.r) = E1[h1_0 + 16m][i] * E2[h2][i] * E3[h3][i] * b_i^j,  b_i = exp(2 pi i dq_1 u_i)
-//     (complex FP32, restarted every 16 steps from FP64-built tables), split into hi/lo and
-//     stored in the K-major 128-byte-swizzled layout the MMA descriptors describe;
+//   * warps 0-7 generate the A tile in shared memory.  Warp w takes sites 8w .. 8w+7 (one
+//     16-byte chunk of every row), lane l the site 8w + l/4 and the q-points h1_0 + 4a + l%4
+//     (a = 0..15): phase factors
+//       exp(i q.r) = E1[h1_0 + l%4][i] * E2[h2][i] * E3[h3][i] * b4_i^a,  b4_i = exp(2 pi i 4 dq_1 u_i)
+//     (complex FP32 from FP64-built tables, 15 steps of the recurrence), split into hi/lo
+//     BF16 pairs (cos, sin) and written four 8x8 blocks at a time with stmatrix.trans into the
+//     K-major 128-byte-swizzled layout the MMA descriptors describe;
 //   * one thread of warp 8 loads the B_hi / B_lo tiles with TMA (same swizzle) and issues the
 //     12 tcgen05.mma (3 products x 4 K-steps of 16), then tcgen05.commit to the stage's
 //     "empty" barrier;
@@ -81,10 +84,10 @@ struct SqParams {
     int Kpad;          // sites padded to kBK
     int R;             // replicas in this launch
     int BN;            // columns (3R, or R for Ising, padded to 16)
-    const float2 *E1;  // [M1/16][Kpad]   exp(2 pi i (q0_1 + 16 m dq_1) u_i)
+    const float2 *E1;  // [M1/64][4][Kpad]  exp(2 pi i (q0_1 + (64 t + p) dq_1) u_i)
     const float2 *E2;  // [M2][Kpad]
     const float2 *E3;  // [M3][Kpad]
-    const float2 *bb;  // [Kpad]          exp(2 pi i dq_1 u_i)
+    const float2 *bb;  // [Kpad]            exp(2 pi i 4 dq_1 u_i)
     float *sq;         // [R][Q]
     float *comp;       // [R][Q][3]
     int *err;
@@ -133,16 +136,17 @@ sq_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CU
 
     if (warp < kProducers / 32) {
         // ------------------------------------------------------------- producers ----------
-        // thread = (site i of the k-block, block of 16 q-points j0 .. j0+15 = rows 32 rq ..)
-        const int i = tid & 63;
-        const int rq = tid >> 6;  // 0..3
-        const int j0 = 16 * rq;
-        // byte offsets of (row, i) for the 8 rows of a swizzle atom (row & 7 = x)
-        uint32_t cx[8];
-#pragma unroll
-        for (int x = 0; x < 8; ++x) cx[x] = (uint32_t)(x * 128 + ((((i >> 3) ^ x)) << 4) + (i & 7) * 2);
-        const uint32_t rowbase = (uint32_t)(rq * 4 * 1024);  // atoms 4 rq .. 4 rq + 3
-        const size_t e1row = (size_t)((h1_0 + j0) >> 4) * P.Kpad;
+        // lane = (site i = 8 warp + lane / 4 of the k-block, q-phase ph = lane % 4): q-points
+        // h1_0 + 4a + ph, rows 8a + 2ph (cos) and 8a + 2ph + 1 (sin) = rows 2ph, 2ph + 1 of
+        // atom a.  stmatrix.trans stores thread t's register (low, high) = (cos, sin) of site
+        // t / 4 at rows 2(t % 4), 2(t % 4) + 1 of an 8x8 block, whose row r lane 8m + r
+        // addresses (block m of the x4 = atom 4g + m); the rows are 16-byte chunks `warp` of
+        // the swizzled rows.
+        const int i = 8 * warp + (lane >> 2);
+        const int ph = lane & 3;
+        const int xr = lane & 7;
+        const uint32_t rowoff = (uint32_t)((lane >> 3) * 1024 + xr * 128 + ((warp ^ xr) << 4));
+        const size_t e1row = ((size_t)(h1_0 >> 6) * 4 + ph) * P.Kpad;
         const size_t e2row = (size_t)h2 * P.Kpad, e3row = (size_t)h3 * P.Kpad;
         // phase factors of the first k-block, then prefetched one block ahead
         float2 e1 = P.E1[e1row + i], e2 = P.E2[e2row + i], e3 = P.E3[e3row + i], bq = P.bb[i];
@@ -158,21 +162,29 @@ sq_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CU
                 e3 = P.E3[e3row + nxt];
                 bq = P.bb[nxt];
             }
-            if (f >= 1 && !mbar_wait(smem_u32(&empty[s]), (f - 1) & 1, P.err, 1)) { ok = false; break; }
-            uint8_t *a_hi = base + s * stage_bytes + rowbase;
-            uint8_t *a_lo = a_hi + Smem::a_bytes;
+            // stmatrix is warp-collective: the warp goes on only if every lane's wait succeeded
+            if (f >= 1 && !__all_sync(0xffffffffu, mbar_wait(smem_u32(&empty[s]), (f - 1) & 1, P.err, 1))) {
+                ok = false;
+                break;
+            }
+            const uint32_t a_hi = smem_u32(base + s * stage_bytes) + rowoff;
+            const uint32_t a_lo = a_hi + Smem::a_bytes;
 #pragma unroll
-            for (int jj = 0; jj < 16; ++jj) {
-                // rows 2(j0+jj) (cos) and 2(j0+jj)+1 (sin): atom jj/4, rows 2(jj%4), 2(jj%4)+1
-                const __nv_bfloat162 hi = __floats2bfloat162_rn(z.re, z.im);
-                const __nv_bfloat162 lo = __floats2bfloat162_rn(z.re - __low2float(hi), z.im - __high2float(hi));
-                const uint32_t oc = (uint32_t)((jj >> 2) * 1024) + cx[2 * (jj & 3)];
-                const uint32_t os = (uint32_t)((jj >> 2) * 1024) + cx[2 * (jj & 3) + 1];
-                *reinterpret_cast<__nv_bfloat16 *>(a_hi + oc) = __low2bfloat16(hi);
-                *reinterpret_cast<__nv_bfloat16 *>(a_hi + os) = __high2bfloat16(hi);
-                *reinterpret_cast<__nv_bfloat16 *>(a_lo + oc) = __low2bfloat16(lo);
-                *reinterpret_cast<__nv_bfloat16 *>(a_lo + os) = __high2bfloat16(lo);
-                z = cmul(z, b);
+            for (int g = 0; g < 4; ++g) {
+                uint32_t hi[4], lo[4];
+#pragma unroll
+                for (int m = 0; m < 4; ++m) {
+                    const __nv_bfloat162 h = __floats2bfloat162_rn(z.re, z.im);
+                    const __nv_bfloat162 l = __floats2bfloat162_rn(z.re - __low2float(h), z.im - __high2float(h));
+                    hi[m] = *reinterpret_cast<const uint32_t *>(&h);
+                    lo[m] = *reinterpret_cast<const uint32_t *>(&l);
+                    z = cmul(z, b);
+                }
+                const uint32_t o = (uint32_t)(g * 4 * 1024);
+                asm volatile("stmatrix.sync.aligned.m8n8.x4.trans.shared.b16 [%0], {%1, %2, %3, %4};"
+                             ::"r"(a_hi + o), "r"(hi[0]), "r"(hi[1]), "r"(hi[2]), "r"(hi[3]) : "memory");
+                asm volatile("stmatrix.sync.aligned.m8n8.x4.trans.shared.b16 [%0], {%1, %2, %3, %4};"
+                             ::"r"(a_lo + o), "r"(lo[0]), "r"(lo[1]), "r"(lo[2]), "r"(lo[3]) : "memory");
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             mbar_arrive(smem_u32(&full[s]));
@@ -368,13 +380,14 @@ int structure_factor_launch(Ctx &c, const double *frac /*3N, storage order*/, co
     if (!encode) { msg = "cuTensorMapEncodeTiled not available"; return ETHER_ERR_CUDA; }
     // phase tables in FP64 on the host
     const double tp = 2.0 * M_PI;
+    // E1 row 4t + p: the phase at h1 = 64t + p (the first q-point of q-phase p of tile t)
     std::vector<float2> E1((size_t)(M1 / 16) * Kpad, make_float2(0.f, 0.f));
     std::vector<float2> E2((size_t)M2 * Kpad, make_float2(0.f, 0.f)), E3((size_t)M3 * Kpad, make_float2(0.f, 0.f));
     std::vector<float2> bb(Kpad, make_float2(1.f, 0.f));
     for (int i = 0; i < N; ++i) {
         const double u = frac[3 * i], v = frac[3 * i + 1], w = frac[3 * i + 2];
         for (int m = 0; m < M1 / 16; ++m) {
-            const double ph = tp * (q0[0] + 16.0 * m * dq[0]) * u;
+            const double ph = tp * (q0[0] + (64.0 * (m >> 2) + (m & 3)) * dq[0]) * u;
             E1[(size_t)m * Kpad + i] = make_float2((float)cos(ph), (float)sin(ph));
         }
         for (int h = 0; h < M2; ++h) {
@@ -385,7 +398,7 @@ int structure_factor_launch(Ctx &c, const double *frac /*3N, storage order*/, co
             const double ph = tp * (q0[2] + h * dq[2]) * w;
             E3[(size_t)h * Kpad + i] = make_float2((float)cos(ph), (float)sin(ph));
         }
-        const double ph = tp * dq[0] * u;
+        const double ph = tp * 4.0 * dq[0] * u;
         bb[i] = make_float2((float)cos(ph), (float)sin(ph));
     }
     const bool ising = c.model == ETHER_MODEL_ISING;
