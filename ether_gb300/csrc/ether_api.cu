@@ -197,7 +197,7 @@ void free_ctx(Ctx &c) {
                     c.step, c.ovrr_step, c.fresh_call, c.acc_count, c.E, c.M, c.sums,
                     c.partials, c.pt_accepts, c.swap_dev, c.copy_from, c.err, c.spiral_ptr,
                     c.spiral_nbr, c.acc_before, c.acc_ratio, c.spiral_part, c.spiral_sums,
-                    c.acc_slot, c.acc_mark, c.t.sia_cls, c.t.sia_ax};
+                    c.acc_slot, c.acc_mark, c.t.sia_cls, c.t.sia_ax, c.t.mweight_f};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c.acc_host) cudaFreeHost(c.acc_host);
@@ -414,6 +414,23 @@ extern "C" int ether_create(const ether_desc *d, ether_ctx **out) {
         for (int k = 0; k < 3; ++k) c.pos.push_back(d->ion[6 + k + 9 * (size_t)i]);
     }
 
+    // exact shortcuts of the energy reduction: one z coupling on every bond, one |weight|,
+    // weights exact in FP32
+    c.juni_set = !jidx.empty();
+    if (c.juni_set) {
+        c.ising_juni = c.h_Jd[3 * (size_t)jidx[0] + 2];
+        for (uint16_t j : jidx)
+            if (c.h_Jd[3 * (size_t)j + 2] != c.ising_juni) { c.juni_set = false; break; }
+    }
+    c.mw_abs = N > 0 ? std::fabs(mw[0]) : 0.0;
+    bool mw_f32 = true;
+    std::vector<float> mwf(N);
+    for (int s = 0; s < N; ++s) {
+        if (std::fabs(mw[s]) != c.mw_abs) c.mw_abs = 0.0;
+        mwf[s] = (float)mw[s];
+        if ((double)mwf[s] != mw[s]) mw_f32 = false;
+    }
+
     // ----- device
     CUDA_TRY(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
     int rc = ETHER_OK;
@@ -439,6 +456,7 @@ extern "C" int ether_create(const ether_desc *d, ether_ctx **out) {
         TRY(dev_upload(c, &c.t.sia_ax, sia_ax));
     }
     TRY(dev_upload(c, &c.t.mweight, mw));
+    if (mw_f32) TRY(dev_upload(c, &c.t.mweight_f, mwf));
     TRY(dev_upload(c, &c.t.site_of_storage, c.site_of_storage));
     {
         // ELL blocks per colour class: coalesced neighbour reads for the general-lattice

@@ -40,6 +40,7 @@ struct DevTables {
     double *zeed = nullptr;       // nsp * 3
     float *D = nullptr;           // nsp * 3 (SIA)
     double *mweight = nullptr;    // N: stgg * s(species)
+    float *mweight_f = nullptr;   // N: the same in FP32 when every weight is exact in FP32
     int32_t *site_of_storage = nullptr;  // N: 0-based site number of a storage index
     // neighbour lists per colour class in ELL form: entry k of rank rho of colour c at
     // ell_off[c] + k * n_c + rho (same order as the CSR), padded to the class's widest site
@@ -128,6 +129,10 @@ struct Ctx {
     double *sums = nullptr;      // 7R (per group*n_slots + slot)
     double *partials = nullptr;  // scratch for reductions
     int partial_blocks = 0;
+    // exact shortcuts of the energy reduction (k_obs.cu): every bond's z coupling equal
+    // (ising_juni, Ising), every |weight| equal (mw_abs), every weight exact in FP32
+    bool juni_set = false;
+    double ising_juni = 0.0, mw_abs = 0.0;
     int32_t *pt_accepts = nullptr;  // 1
     int32_t *swap_dev = nullptr;    // 1: PT swap counter
     int32_t *copy_from = nullptr;   // R (reference-copy PT mode)
@@ -137,6 +142,53 @@ struct Ctx {
     float sq_ms = 0.f;  // last structure-factor kernel time (CUDA events)
     int sm_count = 0;
 };
+
+// One context's observables and PT state as the batched observable kernels see it
+// (obs_member, k_obs.cu): a member of a device table.
+struct ObsMember {
+    const uint8_t *spins;
+    const float4 *spins4;
+    int N, model, zeeman, sia;
+    const int32_t *row_ptr, *nbr;
+    const uint16_t *jidx;
+    const float *J;
+    const double *Jd;
+    const uint8_t *species;
+    const float *zee;
+    const double *zeed;
+    const float *D;
+    const uint8_t *sia_cls;  // null unless local-axis anisotropy
+    const float4 *sia_ax;
+    const double *mweight;
+    const float *mweight_f;  // null unless every weight is exact in FP32
+    double juni, mw_abs;     // Ising counting form: the one bond coupling, the one |weight|
+    int count_form, nsp;     // count_form: Ising sums by integer counts (juni, mw_abs, one species)
+    double *partials;
+    int nblk, R;             // energy blocks per replica, replicas
+    double *E, *M, *sums;
+    int n_slots, n_groups;
+    const double *beta_slot;
+    int32_t *rep_of_slot, *slot_of_rep, *copy_from, *swap_dev, *pt_accepts;
+    uint32_t seed;
+    int true_energy;
+    const unsigned long long *acc_count;
+    unsigned long long *acc_mark, *acc_slot;
+};
+
+// A device table of members and the prefix offsets the batched kernels index it by:
+// eoff energy blocks (R * nblk), roff replicas, poff PT pairs (n_groups * (n_slots/2 + 1)),
+// each of length M + 1.
+struct ObsTable {
+    const ObsMember *mem = nullptr;
+    const int32_t *eoff = nullptr, *roff = nullptr, *poff = nullptr;
+    int M = 0, eblocks = 0, rtotal = 0, ptotal = 0;
+};
+ObsMember obs_member(const Ctx &c);
+// The per-member sequences of launch_energy_mag, launch_pt(c, -1) (true-swap mode) and
+// launch_measure for every member of the table, one launch per kernel on stream st.
+cudaError_t launch_batch_energy(const ObsTable &t, cudaStream_t st);
+cudaError_t launch_batch_pt(const ObsTable &t, cudaStream_t st);
+cudaError_t launch_batch_measure(const ObsTable &t, cudaStream_t st);
 
 // kernel launchers (k_*.cu)
 cudaError_t launch_ising_sweep(Ctx &c, int colour);

@@ -300,6 +300,14 @@ struct ether_batch {
     long long updates_per_sweep = 0;
     cudaGraphExec_t graph = nullptr;
     std::map<std::string, cudaGraphExec_t> mcs_graphs;  // ether_batch_mcs chunks by gate pattern
+    // ether_batch_mcs: the members whose PT and measurement run as batched launches (all but
+    // those in the reference-copy PT mode), their table and its offsets
+    std::vector<int> obs_in;            // per member: 1 if in the table
+    std::vector<ObsMember> h_obs;
+    std::vector<int32_t> h_obs_off;     // eoff | roff | poff
+    ObsMember *d_obs = nullptr;
+    int32_t *d_obs_off = nullptr;
+    ObsTable obs;
     bool dirty = true;
     uint64_t launches = 0;
     float last_ms = 0.f;
@@ -671,14 +679,92 @@ struct OnBatchStream {
 
 constexpr int kMemberBranches = 8;
 
+// The table of the batched observables: every member not in the reference-copy PT mode, as
+// it is now (ladder shapes can change between calls; the graph key carries them).
+int build_obs(ether_batch &b) {
+    const int M = (int)b.members.size();
+    std::vector<ObsMember> hm;
+    std::vector<int32_t> eo{0}, ro{0}, po{0};
+    b.obs_in.assign(M, 0);
+    for (int m = 0; m < M; ++m) {
+        const Ctx &c = b.members[m]->c;
+        if (c.flags & ETHER_FLAG_PT_REFERENCE_COPY) continue;
+        b.obs_in[m] = 1;
+        const ObsMember a = obs_member(c);
+        hm.push_back(a);
+        eo.push_back(eo.back() + a.R * a.nblk);
+        ro.push_back(ro.back() + a.R);
+        po.push_back(po.back() + a.n_groups * (a.n_slots / 2 + 1));
+    }
+    const int Mt = (int)hm.size();
+    if (Mt == 0) {
+        b.obs = ObsTable();
+        return ETHER_OK;
+    }
+    if (!b.d_obs) {  // sized for every member once: captured graphs keep these addresses
+        BCUDA(cudaMalloc((void **)&b.d_obs, (size_t)M * sizeof(ObsMember)));
+        BCUDA(cudaMalloc((void **)&b.d_obs_off, (size_t)3 * (M + 1) * sizeof(int32_t)));
+    }
+    std::vector<int32_t> off(eo);
+    off.insert(off.end(), ro.begin(), ro.end());
+    off.insert(off.end(), po.begin(), po.end());
+    const bool same = hm.size() == b.h_obs.size() && off == b.h_obs_off &&
+                      std::memcmp(hm.data(), b.h_obs.data(), hm.size() * sizeof(ObsMember)) == 0;
+    if (!same) {
+        b.h_obs = hm;
+        b.h_obs_off = off;
+        BCUDA(cudaMemcpyAsync(b.d_obs, b.h_obs.data(), hm.size() * sizeof(ObsMember), cudaMemcpyHostToDevice, b.stream));
+        BCUDA(cudaMemcpyAsync(b.d_obs_off, b.h_obs_off.data(), off.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                              b.stream));
+        BCUDA(cudaStreamSynchronize(b.stream));
+    }
+    b.obs.mem = b.d_obs;
+    b.obs.eoff = b.d_obs_off;
+    b.obs.roff = b.d_obs_off + (Mt + 1);
+    b.obs.poff = b.d_obs_off + 2 * (Mt + 1);
+    b.obs.M = Mt;
+    b.obs.eblocks = eo.back();
+    b.obs.rtotal = ro.back();
+    b.obs.ptotal = po.back();
+    return ETHER_OK;
+}
+
 // The members' own parts of one step (gates g[m]): before the sweep their overrelaxation,
-// after it their PT and measurement.  The members' kernels are small and independent, so
-// they are spread over up to kMemberBranches parallel branches.
+// after it their PT and measurement.  After the sweep the members of the observable table
+// take PT and measurement in batched launches, one per kernel for all of them (their gates
+// agree: one schedule); the rest -- overrelaxation, members outside the table, spiral
+// samples -- is small and independent per member, spread over up to kMemberBranches
+// parallel branches.
 int issue_member_parts(ether_batch &b, const ether_schedule *sch, const int8_t *g, bool before) {
     const int M = (int)b.members.size();
     const int mask = before ? 1 : 6;
+    bool batched = false;
+    if (!before && b.obs.M > 0) {
+        int gb = -1;
+        batched = true;
+        for (int m = 0; m < M; ++m)
+            if (b.obs_in[m]) {
+                if (gb < 0) gb = g[m] & 6;
+                else if ((g[m] & 6) != gb) batched = false;
+            }
+        if (batched && (gb & 2)) {
+            BCUDA(launch_batch_energy(b.obs, b.stream));
+            BCUDA(launch_batch_pt(b.obs, b.stream));
+        }
+        if (batched && (gb & 4)) {
+            BCUDA(launch_batch_energy(b.obs, b.stream));
+            BCUDA(launch_batch_measure(b.obs, b.stream));
+        }
+    }
+    // per member: 1 its own parts, 2 only its spiral sample (src/observable.f90:41)
+    std::vector<int8_t> job(M, 0);
     int need = 0;
-    for (int m = 0; m < M; ++m) need += (g[m] & mask) ? 1 : 0;
+    for (int m = 0; m < M; ++m) {
+        if (!(g[m] & mask)) continue;
+        if (batched && b.obs_in[m]) job[m] = ((g[m] & 4) && b.members[m]->c.spiral_ptr) ? 2 : 0;
+        else job[m] = 1;
+        need += job[m] ? 1 : 0;
+    }
     if (need == 0) return ETHER_OK;
     const int nbr = std::min(kMemberBranches, need);
     if (nbr > 1) {
@@ -686,8 +772,12 @@ int issue_member_parts(ether_batch &b, const ether_schedule *sch, const int8_t *
         if (rc) return rc;
     }
     for (int m = 0, k = 0; m < M; ++m) {
-        if (!(g[m] & mask)) continue;
+        if (!job[m]) continue;
         OnBatchStream on(b.members[m]->c, nbr > 1 ? b.branch[k++ % nbr] : b.stream);
+        if (job[m] == 2) {
+            BCUDA(launch_spiral_measure(on.c));
+            continue;
+        }
         const int rc = before ? mcs_before_sweep(on.c, sch, g[m]) : mcs_after_sweep(on.c, g[m]);
         if (rc) return rc;
     }
@@ -770,6 +860,8 @@ extern "C" int ether_batch_destroy(ether_batch *b) {
     if (b->d_segs) cudaFree(b->d_segs);
     if (b->d_step_of) cudaFree(b->d_step_of);
     if (b->d_block_first) cudaFree(b->d_block_first);
+    if (b->d_obs) cudaFree(b->d_obs);
+    if (b->d_obs_off) cudaFree(b->d_obs_off);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return ETHER_OK;
@@ -803,6 +895,8 @@ extern "C" int ether_batch_mcs(ether_batch *b, const ether_schedule *sch, int32_
     int rc = rebuild(*b);
     if (rc) return rc;
     rc = join_members(*b);
+    if (rc) return rc;
+    rc = build_obs(*b);
     if (rc) return rc;
     // every member's device swap counter starts from the caller's value, as ether_mcs does
     std::vector<int32_t> sc(M, 0);

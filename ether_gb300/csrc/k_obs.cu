@@ -3,9 +3,16 @@
 // src/get_eng.f90:36-40, src/get_mag.f90:36-41) and parallel tempering
 // (src/parallel_tempering.f90:39-108).
 //
-// Site energies are FP32 (XYZ) or exact FP64 sums of ±J (Ising); every per-replica total
-// and every accumulator is FP64.  Reductions write per-block partials to scratch memory
-// and a second kernel adds them in a fixed order, so results do not depend on timing.
+// Site energies are FP32 (XYZ) or exact sums of ±J (Ising); every per-replica total and
+// every accumulator is FP64.  Reductions write per-block partials to scratch memory and a
+// second kernel adds them in a fixed order, so results do not depend on timing.
+//
+// GB300 issues about 2 FP64 instructions per SM and clock against 128 FP32, so a thread's
+// running sums avoid FP64 per site: Ising bond terms s_i s_j J are +-J exactly, so with one
+// coupling, one species and one |weight| a thread counts them in integers and multiplies
+// once (else it adds +-J, one FP64 add per bond); XYZ sums are kept as FP32 double-single
+// pairs (Knuth's TwoSum, products split exactly with fmaf), about 48 significant bits, and
+// turned into FP64 once per thread.
 #include "internal.h"
 #include "rng_math.cuh"
 
@@ -14,44 +21,80 @@ namespace ether {
 constexpr int kRedBs = 256;
 constexpr int kNq = 5;  // E_raw, E_exchange, Mx, My, Mz
 
+// A running sum hi + lo of FP32 terms (double-single): TwoSum keeps hi's rounding error
+// exactly, lo collects those errors.
+struct DS {
+    float hi = 0.f, lo = 0.f;
+};
+__device__ __forceinline__ void ds_add(DS &a, float x) {
+    const float s = a.hi + x;
+    const float bp = s - a.hi;
+    const float err = (a.hi - (s - bp)) + (x - bp);
+    a.hi = s;
+    a.lo += err;
+}
+// a += w x, the product split exactly (p + fmaf(w, x, -p) = w x)
+__device__ __forceinline__ void ds_add_prod(DS &a, float w, float x) {
+    const float p = w * x;
+    const float e = fmaf(w, x, -p);
+    ds_add(a, p);
+    a.lo += e;
+}
+__device__ __forceinline__ double ds_value(const DS &a) { return (double)a.hi + (double)a.lo; }
+
+// Sign flip of an FP64 value by its sign bit (no FP64 instruction).
+__device__ __forceinline__ double neg_if(double v, bool neg) {
+    return __longlong_as_double(__double_as_longlong(v) ^ (neg ? (long long)0x8000000000000000ULL : 0LL));
+}
+
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     return v;
 }
 
-__global__ void __launch_bounds__(kRedBs)
-energy_mag_kernel(const uint8_t *__restrict__ spins, const float4 *__restrict__ spins4, int N,
-                  int model, int zeeman, int sia, const int32_t *__restrict__ row_ptr,
-                  const int32_t *__restrict__ nbr, const uint16_t *__restrict__ jidx,
-                  const float *__restrict__ J, const double *__restrict__ Jd,
-                  const uint8_t *__restrict__ species, const float *__restrict__ zee,
-                  const double *__restrict__ zeed, const float *__restrict__ D,
-                  const uint8_t *__restrict__ sia_cls, const float4 *__restrict__ sia_ax,
-                  const double *__restrict__ mweight, double *__restrict__ partials) {
-    const int r = blockIdx.y;
+// Partial sums of block b (of a.nblk) of replica r into a.partials[(r * nblk + b) * kNq ..]:
+// the whole block calls it.
+__device__ __forceinline__ void energy_block(const ObsMember &a, int r, int b) {
+    const int N = a.N;
+    const int stride = a.nblk * blockDim.x;
     double q[kNq] = {0, 0, 0, 0, 0};
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += gridDim.x * blockDim.x) {
-        const double w = mweight[s];
-        if (model == 0) {
-            const uint8_t *sp = spins + (size_t)r * N;
-            const double si = sp[s] ? 1.0 : -1.0;
+    if (a.model == 0 && a.count_form) {
+        // E_ex = J sum s_i s_j, the field term z sum s_i, M = |w| sum sign(w_i) s_i
+        const uint8_t *sp = a.spins + (size_t)r * N;
+        int cb = 0, cz = 0, cm = 0;
+        for (int s = b * blockDim.x + threadIdx.x; s < N; s += stride) {
+            const uint8_t own = sp[s];
+            for (int k = a.row_ptr[s]; k < a.row_ptr[s + 1]; ++k) cb += (sp[a.nbr[k]] == own) ? 1 : -1;
+            cz += own ? 1 : -1;
+            const bool wneg = __double_as_longlong(a.mweight[s]) < 0;
+            cm += ((own != 0) != wneg) ? 1 : -1;
+        }
+        q[1] = a.juni * (double)cb;
+        q[0] = a.zeeman ? q[1] + a.zeed[2] * (double)cz : q[1];
+        q[4] = a.mw_abs * (double)cm;
+    } else if (a.model == 0) {
+        const uint8_t *sp = a.spins + (size_t)r * N;
+        for (int s = b * blockDim.x + threadIdx.x; s < N; s += stride) {
+            const uint8_t own = sp[s];
             double e = 0.0;
-            for (int k = row_ptr[s]; k < row_ptr[s + 1]; ++k) {
-                double sj = sp[nbr[k]] ? 1.0 : -1.0;
-                e += (si * sj) * Jd[3 * jidx[k] + 2];
-            }
+            for (int k = a.row_ptr[s]; k < a.row_ptr[s + 1]; ++k)
+                e += neg_if(a.Jd[3 * a.jidx[k] + 2], sp[a.nbr[k]] != own);  // (s_i s_j) J
             q[1] += e;
-            if (zeeman) e += si * zeed[3 * (species[s] - 1) + 2];
+            if (a.zeeman) e += neg_if(a.zeed[3 * (a.species[s] - 1) + 2], !own);
             q[0] += e;
-            q[4] += w * si;
-        } else {
-            const float4 *sp = spins4 + (size_t)r * N;
+            q[4] += neg_if(a.mweight[s], !own);
+        }
+    } else {
+        const float4 *sp = a.spins4 + (size_t)r * N;
+        DS e0, e1, m0, m1, m2;
+        const bool mwf = a.mweight_f != nullptr;
+        for (int s = b * blockDim.x + threadIdx.x; s < N; s += stride) {
             const float4 S = sp[s];
             float hx = 0.f, hy = 0.f, hz = 0.f;
-            for (int k = row_ptr[s]; k < row_ptr[s + 1]; ++k) {
-                float4 Sj = sp[nbr[k]];
-                const float *Jp = J + 3 * jidx[k];
+            for (int k = a.row_ptr[s]; k < a.row_ptr[s + 1]; ++k) {
+                float4 Sj = sp[a.nbr[k]];
+                const float *Jp = a.J + 3 * a.jidx[k];
                 hx = fmaf(Jp[0], Sj.x, hx);
                 hy = fmaf(Jp[1], Sj.y, hy);
                 hz = fmaf(Jp[2], Sj.z, hz);
@@ -59,33 +102,48 @@ energy_mag_kernel(const uint8_t *__restrict__ spins, const float4 *__restrict__ 
             float e = S.x * hx;
             e = fmaf(S.y, hy, e);
             e = fmaf(S.z, hz, e);
-            q[1] += (double)e;
-            if (zeeman || sia) {
-                const int si = species[s] - 1;
-                if (zeeman) {
-                    const float *z = zee + 3 * si;
+            ds_add(e1, e);
+            if (a.zeeman || a.sia) {
+                const int si = a.species[s] - 1;
+                if (a.zeeman) {
+                    const float *z = a.zee + 3 * si;
                     e = fmaf(S.x, z[0], e);
                     e = fmaf(S.y, z[1], e);
                     e = fmaf(S.z, z[2], e);
                 }
-                if (sia) {
-                    const float *d = D + 3 * si;
+                if (a.sia) {
+                    const float *d = a.D + 3 * si;
                     e = fmaf(d[0], S.x * S.x, e);
                     e = fmaf(d[1], S.y * S.y, e);
                     e = fmaf(d[2], S.z * S.z, e);
                 }
             }
-            if (sia_cls) {  // local-axis anisotropy D (a . S)^2
-                const float4 a = sia_ax[sia_cls[s]];
-                float ps = a.x * S.x;
-                ps = fmaf(a.y, S.y, ps);
-                ps = fmaf(a.z, S.z, ps);
-                e = fmaf(a.w, ps * ps, e);
+            if (a.sia_cls) {  // local-axis anisotropy D (a . S)^2
+                const float4 ax = a.sia_ax[a.sia_cls[s]];
+                float ps = ax.x * S.x;
+                ps = fmaf(ax.y, S.y, ps);
+                ps = fmaf(ax.z, S.z, ps);
+                e = fmaf(ax.w, ps * ps, e);
             }
-            q[0] += (double)e;
-            q[2] += w * (double)S.x;
-            q[3] += w * (double)S.y;
-            q[4] += w * (double)S.z;
+            ds_add(e0, e);
+            if (mwf) {
+                const float wf = a.mweight_f[s];
+                ds_add_prod(m0, wf, S.x);
+                ds_add_prod(m1, wf, S.y);
+                ds_add_prod(m2, wf, S.z);
+            } else {
+                const double w = a.mweight[s];
+                q[2] += w * (double)S.x;
+                q[3] += w * (double)S.y;
+                q[4] += w * (double)S.z;
+            }
+        }
+        q[0] = ds_value(e0);
+        q[1] = ds_value(e1);
+        if (mwf) {
+            q[2] = ds_value(m0);
+            q[3] = ds_value(m1);
+            q[4] = ds_value(m2);
         }
     }
     __shared__ double sm[kRedBs / 32][kNq];
@@ -99,14 +157,17 @@ energy_mag_kernel(const uint8_t *__restrict__ spins, const float4 *__restrict__ 
     if (threadIdx.x < kNq) {
         double v = 0.0;
         for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2) v += sm[w2][threadIdx.x];
-        partials[((size_t)r * gridDim.x + blockIdx.x) * kNq + threadIdx.x] = v;
+        a.partials[((size_t)r * a.nblk + b) * kNq + threadIdx.x] = v;
     }
 }
 
-// One block per replica: sums the partials in index order.
-__global__ void finish_energy_kernel(const double *__restrict__ partials, int nblk, int R,
-                                     double *__restrict__ E, double *__restrict__ M) {
-    const int r = blockIdx.x;
+__global__ void __launch_bounds__(kRedBs) energy_mag_kernel(const ObsMember a) {
+    energy_block(a, blockIdx.y, blockIdx.x);
+}
+
+// Replica r: sums the partials in index order (a block of 128 threads).
+__device__ __forceinline__ void finish_block(const double *__restrict__ partials, int nblk, int R, int r,
+                                             double *__restrict__ E, double *__restrict__ M) {
     __shared__ double sm[kNq][128];
     for (int j = 0; j < kNq; ++j) {
         double v = 0.0;
@@ -128,12 +189,16 @@ __global__ void finish_energy_kernel(const double *__restrict__ partials, int nb
     }
 }
 
-// get_eng('eng') / get_mag('mag') for every replica, into its (group, slot) accumulator.
-__global__ void measure_kernel(const double *__restrict__ E, const double *__restrict__ M, int N,
-                               int R, int n_slots, const int32_t *__restrict__ slot_of_rep,
-                               double *__restrict__ sums) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= R) return;
+// One block per replica.
+__global__ void finish_energy_kernel(const double *__restrict__ partials, int nblk, int R,
+                                     double *__restrict__ E, double *__restrict__ M) {
+    finish_block(partials, nblk, R, blockIdx.x, E, M);
+}
+
+// get_eng('eng') / get_mag('mag') of replica r, into its (group, slot) accumulator.
+__device__ __forceinline__ void measure_one(const double *__restrict__ E, const double *__restrict__ M,
+                                            int N, int n_slots, const int32_t *__restrict__ slot_of_rep,
+                                            double *__restrict__ sums, int r) {
     const int idx = (r / n_slots) * n_slots + slot_of_rep[r];
     const double e = E[r] / (2.0 * N);
     const double mx = M[3 * r], my = M[3 * r + 1], mz = M[3 * r + 2];
@@ -148,15 +213,21 @@ __global__ void measure_kernel(const double *__restrict__ E, const double *__res
     a[6] += (m * m) * (m * m);
 }
 
-// parallel_tempering: one thread per (group, pair).  Exponent in FP64.
-__global__ void pt_kernel(const double *__restrict__ E, int R, int n_slots, int n_groups,
-                          const double *__restrict__ beta_slot, int32_t *__restrict__ rep_of_slot,
-                          int32_t *__restrict__ slot_of_rep, int32_t *__restrict__ copy_from,
-                          const int32_t *__restrict__ swap_ptr, uint32_t seed, int true_energy, int copy_mode,
-                          int32_t *__restrict__ n_acc) {
+__global__ void measure_kernel(const double *__restrict__ E, const double *__restrict__ M, int N,
+                               int R, int n_slots, const int32_t *__restrict__ slot_of_rep,
+                               double *__restrict__ sums) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < R) measure_one(E, M, N, n_slots, slot_of_rep, sums, r);
+}
+
+// parallel_tempering: pair tid = (group, pair) of one ladder set.  Exponent in FP64.
+__device__ __forceinline__ void pt_pair(const double *__restrict__ E, int R, int n_slots, int n_groups,
+                                        const double *__restrict__ beta_slot, int32_t *__restrict__ rep_of_slot,
+                                        int32_t *__restrict__ slot_of_rep, int32_t *__restrict__ copy_from,
+                                        const int32_t *__restrict__ swap_ptr, uint32_t seed, int true_energy,
+                                        int copy_mode, int32_t *__restrict__ n_acc, int tid) {
     const int swap_count = *swap_ptr;
     const int npairs = n_slots / 2 + 1;
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     if (tid >= npairs * n_groups) return;
     const int g = tid / npairs, q = tid - g * npairs;
     const int s = ((swap_count & 1) ? 1 : 0) + 2 * q;
@@ -187,6 +258,16 @@ __global__ void pt_kernel(const double *__restrict__ E, int R, int n_slots, int 
     }
 }
 
+// One thread per (group, pair).
+__global__ void pt_kernel(const double *__restrict__ E, int R, int n_slots, int n_groups,
+                          const double *__restrict__ beta_slot, int32_t *__restrict__ rep_of_slot,
+                          int32_t *__restrict__ slot_of_rep, int32_t *__restrict__ copy_from,
+                          const int32_t *__restrict__ swap_ptr, uint32_t seed, int true_energy, int copy_mode,
+                          int32_t *__restrict__ n_acc) {
+    pt_pair(E, R, n_slots, n_groups, beta_slot, rep_of_slot, slot_of_rep, copy_from, swap_ptr, seed,
+            true_energy, copy_mode, n_acc, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 // Reference-copy PT mode: replica r takes the configuration of replica copy_from[r].
 __global__ void pt_copy_kernel(uint8_t *__restrict__ spins, float4 *__restrict__ spins4, int N,
                                int model, const int32_t *__restrict__ copy_from) {
@@ -208,31 +289,100 @@ int energy_blocks(const Ctx &c) {
     return (int)(need < 1 ? 1 : need);
 }
 
+ObsMember obs_member(const Ctx &c) {
+    ObsMember a{};
+    a.spins = c.spins;
+    a.spins4 = c.spins4;
+    a.N = c.N;
+    a.model = c.model;
+    a.zeeman = c.zeeman;
+    a.sia = c.sia && c.model == 1;
+    a.row_ptr = c.t.row_ptr;
+    a.nbr = c.t.nbr;
+    a.jidx = c.t.jidx;
+    a.J = c.t.J;
+    a.Jd = c.t.Jd;
+    a.species = c.t.species;
+    a.zee = c.t.zee;
+    a.zeed = c.t.zeed;
+    a.D = c.t.D;
+    a.sia_cls = c.sia_local && c.model == 1 ? c.t.sia_cls : nullptr;
+    a.sia_ax = c.t.sia_ax;
+    a.mweight = c.t.mweight;
+    a.mweight_f = c.t.mweight_f;
+    a.juni = c.ising_juni;
+    a.mw_abs = c.mw_abs;
+    a.nsp = c.nsp;
+    a.count_form = (c.model == 0 && c.juni_set && c.mw_abs > 0.0 && (!c.zeeman || c.nsp == 1)) ? 1 : 0;
+    a.partials = c.partials;
+    a.nblk = c.partial_blocks;
+    a.R = c.R;
+    a.E = c.E;
+    a.M = c.M;
+    a.sums = c.sums;
+    a.n_slots = c.n_slots;
+    a.n_groups = c.n_groups;
+    a.beta_slot = c.beta_slot;
+    a.rep_of_slot = c.rep_of_slot;
+    a.slot_of_rep = c.slot_of_rep;
+    a.copy_from = c.copy_from;
+    a.swap_dev = c.swap_dev;
+    a.pt_accepts = c.pt_accepts;
+    a.seed = c.seed;
+    a.true_energy = (c.flags & ETHER_FLAG_PT_TRUE_ENERGY) ? 1 : 0;
+    a.acc_count = c.acc_count;
+    a.acc_mark = c.acc_mark;
+    a.acc_slot = c.acc_slot;
+    return a;
+}
+
 cudaError_t launch_energy_mag(Ctx &c, bool) {
     const int nblk = c.partial_blocks;
     dim3 grid(nblk, c.R);
-    energy_mag_kernel<<<grid, kRedBs, 0, c.stream>>>(
-        c.spins, c.spins4, c.N, c.model, c.zeeman, c.sia && c.model == 1, c.t.row_ptr, c.t.nbr,
-        c.t.jidx, c.t.J, c.t.Jd, c.t.species, c.t.zee, c.t.zeed, c.t.D,
-        c.sia_local && c.model == 1 ? c.t.sia_cls : nullptr, c.t.sia_ax, c.t.mweight, c.partials);
+    energy_mag_kernel<<<grid, kRedBs, 0, c.stream>>>(obs_member(c));
     finish_energy_kernel<<<c.R, 128, 0, c.stream>>>(c.partials, nblk, c.R, c.E, c.M);
     c.launches += 2;
     return cudaGetLastError();
 }
 
 // Magnetisation only (src/get_tot_magnetisation.f90:32-40), no neighbour reads: per-block
-// partial sums of w_s S_s into partials[(r*nblk + b)*kNq + 2..4].
-__global__ void __launch_bounds__(kRedBs)
-mag_kernel(const uint8_t *__restrict__ spins, const float4 *__restrict__ spins4, int N, int model,
-           const double *__restrict__ mweight, double *__restrict__ partials) {
+// partial sums of w_s S_s into partials[(r*nblk + b)*kNq + 2..4], summed per thread as
+// energy_block sums them (so the two give the same M).
+__global__ void __launch_bounds__(kRedBs) mag_kernel(const ObsMember a) {
     const int r = blockIdx.y;
+    const int N = a.N;
+    const int stride = gridDim.x * blockDim.x;
     double q[3] = {0, 0, 0};
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += gridDim.x * blockDim.x) {
-        const double w = mweight[s];
-        if (model == 0) {
-            q[2] += w * (spins[(size_t)r * N + s] ? 1.0 : -1.0);
-        } else {
-            const float4 S = spins4[(size_t)r * N + s];
+    if (a.model == 0 && a.count_form) {
+        const uint8_t *sp = a.spins + (size_t)r * N;
+        int cm = 0;
+        for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += stride) {
+            const bool wneg = __double_as_longlong(a.mweight[s]) < 0;
+            cm += ((sp[s] != 0) != wneg) ? 1 : -1;
+        }
+        q[2] = a.mw_abs * (double)cm;
+    } else if (a.model == 0) {
+        const uint8_t *sp = a.spins + (size_t)r * N;
+        for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += stride)
+            q[2] += neg_if(a.mweight[s], !sp[s]);
+    } else if (a.mweight_f) {
+        const float4 *sp = a.spins4 + (size_t)r * N;
+        DS m0, m1, m2;
+        for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += stride) {
+            const float4 S = sp[s];
+            const float wf = a.mweight_f[s];
+            ds_add_prod(m0, wf, S.x);
+            ds_add_prod(m1, wf, S.y);
+            ds_add_prod(m2, wf, S.z);
+        }
+        q[0] = ds_value(m0);
+        q[1] = ds_value(m1);
+        q[2] = ds_value(m2);
+    } else {
+        const float4 *sp = a.spins4 + (size_t)r * N;
+        for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += stride) {
+            const double w = a.mweight[s];
+            const float4 S = sp[s];
             q[0] += w * (double)S.x;
             q[1] += w * (double)S.y;
             q[2] += w * (double)S.z;
@@ -249,7 +399,7 @@ mag_kernel(const uint8_t *__restrict__ spins, const float4 *__restrict__ spins4,
     if (threadIdx.x < 3) {
         double v = 0.0;
         for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2) v += sm[w2][threadIdx.x];
-        partials[((size_t)r * gridDim.x + blockIdx.x) * kNq + 2 + threadIdx.x] = v;
+        a.partials[((size_t)r * gridDim.x + blockIdx.x) * kNq + 2 + threadIdx.x] = v;
     }
 }
 
@@ -284,8 +434,7 @@ cudaError_t launch_record(Ctx &c, int t, bool want_e, double *mser, double *eser
         c.launches++;
     } else {
         dim3 grid(c.partial_blocks, c.R);
-        mag_kernel<<<grid, kRedBs, 0, c.stream>>>(c.spins, c.spins4, c.N, c.model, c.t.mweight,
-                                                  c.partials);
+        mag_kernel<<<grid, kRedBs, 0, c.stream>>>(obs_member(c));
         record_kernel<<<(c.R + 127) / 128, 128, 0, c.stream>>>(c.partials, c.partial_blocks, c.R, 1,
                                                                 c.M, c.E, mser, nullptr, t);
         c.launches += 2;
@@ -301,26 +450,35 @@ cudaError_t launch_measure(Ctx &c) {
 }
 
 // PT swap counter, kept on the device so that captured graphs replay correctly.
+__device__ __forceinline__ void pt_bump(int32_t *__restrict__ swap, int32_t *__restrict__ n_acc, int set,
+                                        int32_t value) {
+    *swap = set ? value : *swap + 1;
+    *n_acc = 0;
+}
+
 __global__ void pt_bump_kernel(int32_t *__restrict__ swap, int32_t *__restrict__ n_acc, int set,
                                int32_t value) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        *swap = set ? value : *swap + 1;
-        *n_acc = 0;
-    }
+    if (threadIdx.x == 0 && blockIdx.x == 0) pt_bump(swap, n_acc, set, value);
 }
 
 // Accepts since the last binning go to the (group, slot) position each replica holds now;
 // positions are a permutation of the replicas within a group, so no two threads collide.
+__device__ __forceinline__ void acc_bin_one(const unsigned long long *__restrict__ acc_count,
+                                            unsigned long long *__restrict__ acc_mark,
+                                            const int32_t *__restrict__ slot_of_rep, int n_slots,
+                                            unsigned long long *__restrict__ acc_slot, int r) {
+    const unsigned long long now = acc_count[r];
+    const int pos = (r / n_slots) * n_slots + slot_of_rep[r];
+    acc_slot[pos] += now - acc_mark[r];
+    acc_mark[r] = now;
+}
+
 __global__ void acc_bin_kernel(const unsigned long long *__restrict__ acc_count,
                                unsigned long long *__restrict__ acc_mark,
                                const int32_t *__restrict__ slot_of_rep, int n_slots, int R,
                                unsigned long long *__restrict__ acc_slot) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= R) return;
-    const unsigned long long now = acc_count[r];
-    const int pos = (r / n_slots) * n_slots + slot_of_rep[r];
-    acc_slot[pos] += now - acc_mark[r];
-    acc_mark[r] = now;
+    if (r < R) acc_bin_one(acc_count, acc_mark, slot_of_rep, n_slots, acc_slot, r);
 }
 
 cudaError_t launch_acc_bin(Ctx &c) {
@@ -354,6 +512,86 @@ cudaError_t launch_pt(Ctx &c, int set_swap_count) {
         pt_copy_kernel<<<grid, 256, 0, c.stream>>>(c.spins, c.spins4, c.N, c.model, c.copy_from);
         c.launches++;
     }
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------- batched forms ----
+// The same bodies over a table of members: item idx belongs to member m with
+// off[m] <= idx < off[m + 1] (members with no items are skipped).
+__device__ __forceinline__ int member_of(const int32_t *__restrict__ off, int M, int idx) {
+    int lo = 0, hi = M;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (off[mid] <= idx) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// One block per (member, replica, energy block).
+__global__ void __launch_bounds__(kRedBs)
+batch_energy_kernel(const ObsMember *__restrict__ mem, const int32_t *__restrict__ eoff, int M) {
+    const int m = member_of(eoff, M, blockIdx.x);
+    const ObsMember &a = mem[m];
+    const int local = blockIdx.x - eoff[m];
+    energy_block(a, local / a.nblk, local % a.nblk);
+}
+
+// One block of 128 per (member, replica).
+__global__ void batch_finish_kernel(const ObsMember *__restrict__ mem, const int32_t *__restrict__ roff, int M) {
+    const int m = member_of(roff, M, blockIdx.x);
+    const ObsMember &a = mem[m];
+    finish_block(a.partials, a.nblk, a.R, blockIdx.x - roff[m], a.E, a.M);
+}
+
+// One thread per (member, replica): what = 0 acceptance binning, 1 measurement.
+__global__ void batch_replica_kernel(const ObsMember *__restrict__ mem, const int32_t *__restrict__ roff,
+                                     int M, int total, int what) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    const int m = member_of(roff, M, idx);
+    const ObsMember &a = mem[m];
+    const int r = idx - roff[m];
+    if (what == 0) acc_bin_one(a.acc_count, a.acc_mark, a.slot_of_rep, a.n_slots, a.acc_slot, r);
+    else measure_one(a.E, a.M, a.N, a.n_slots, a.slot_of_rep, a.sums, r);
+}
+
+// One thread per member.
+__global__ void batch_pt_bump_kernel(const ObsMember *__restrict__ mem, int M) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m < M) pt_bump(mem[m].swap_dev, mem[m].pt_accepts, 0, 0);
+}
+
+// One thread per (member, group, pair).
+__global__ void batch_pt_kernel(const ObsMember *__restrict__ mem, const int32_t *__restrict__ poff, int M,
+                                int total) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    const int m = member_of(poff, M, idx);
+    const ObsMember &a = mem[m];
+    pt_pair(a.E, a.R, a.n_slots, a.n_groups, a.beta_slot, a.rep_of_slot, a.slot_of_rep, a.copy_from,
+            a.swap_dev, a.seed, a.true_energy, 0, a.pt_accepts, idx - poff[m]);
+}
+
+cudaError_t launch_batch_energy(const ObsTable &t, cudaStream_t st) {
+    if (t.M == 0) return cudaSuccess;
+    batch_energy_kernel<<<t.eblocks, kRedBs, 0, st>>>(t.mem, t.eoff, t.M);
+    batch_finish_kernel<<<t.rtotal, 128, 0, st>>>(t.mem, t.roff, t.M);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_pt(const ObsTable &t, cudaStream_t st) {
+    if (t.M == 0) return cudaSuccess;
+    // accepts so far belong to the slots held before the swap
+    batch_replica_kernel<<<(t.rtotal + 127) / 128, 128, 0, st>>>(t.mem, t.roff, t.M, t.rtotal, 0);
+    batch_pt_bump_kernel<<<(t.M + 127) / 128, 128, 0, st>>>(t.mem, t.M);
+    if (t.ptotal > 0) batch_pt_kernel<<<(t.ptotal + 127) / 128, 128, 0, st>>>(t.mem, t.poff, t.M, t.ptotal);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_measure(const ObsTable &t, cudaStream_t st) {
+    if (t.M == 0) return cudaSuccess;
+    batch_replica_kernel<<<(t.rtotal + 127) / 128, 128, 0, st>>>(t.mem, t.roff, t.M, t.rtotal, 1);
     return cudaGetLastError();
 }
 

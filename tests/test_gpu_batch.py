@@ -247,16 +247,21 @@ def test_batch_members_with_local_axis_anisotropy():
 def test_batch_mcs_equals_each_members_own_mcs():
     """ether_batch_mcs against every member's own ether_mcs under one schedule (overrelaxation
     every 3 steps, PT every 2, measurement every 4 after 6 equilibration steps): spins,
-    acceptance counters, slot permutations, measurement sums and swap counters bit for bit,
-    over a captured chunk (24 steps) and a short direct one (3 steps).  Members: Ising and
-    XYZ on simple-cubic and pyrochlore lattices, and an XYZ member with a field, which does
-    not overrelax."""
+    acceptance counters, per-temperature acceptance, slot permutations, measurement sums,
+    spiral sums and swap counters bit for bit, over a captured chunk (24 steps) and a short
+    direct one (3 steps).  Members: Ising and XYZ on simple-cubic and pyrochlore lattices
+    (PT and measurement in the batched launches, one of them also sampling the spiral state
+    per member), an XYZ member with a field, which does not overrelax, and a member in the
+    reference-copy PT mode, which keeps its own PT and measurement kernels."""
     zs = {"zeeman": True, "h": (0.0, 0.3, 1.0), "g_factor": 2.0}
     specs = [SPECS[0], SPECS[2], SPECS[5], SPECS[6], SPECS[8],
-             (lambda: eg.simple_cubic(8), eg.MODEL_XYZ, FM, 2, 0, zs)]
+             (lambda: eg.simple_cubic(8), eg.MODEL_XYZ, FM, 2, 0, zs),
+             (lambda: eg.simple_cubic(6), eg.MODEL_XYZ, AFM, 3, eg.FLAG_PT_REFERENCE_COPY)]
     sch = dict(tmcs_eq=6, coa=4, ovrr=True, ovrr_para=0.5, ovrr_mcs=3, pt=True, exchange_interval=2)
     A = build_members(specs)
     B = build_members(specs)
+    for X in (A, B):
+        assert X[3][1].spiral_setup(1.01) > 0
     for _, sw in A + B:
         sw.zero_avg()
     batch = eg.Batch([sw for _, sw in A])
@@ -271,6 +276,8 @@ def test_batch_mcs_equals_each_members_own_mcs():
     for (_, a), (_, b) in zip(A, B):
         np.testing.assert_array_equal(a.slots(), b.slots())
         np.testing.assert_array_equal(a.sums(), b.sums())
+        np.testing.assert_array_equal(a.slot_accept_counts(), b.slot_accept_counts())
+    np.testing.assert_array_equal(A[3][1].spiral_avg(), B[3][1].spiral_avg())
     assert all(b_.sums()[:, 0].max() > 0 for _, b_ in B)  # measurements happened
     assert batch.info().last_sweep_ms > 0.0
     batch.close()
