@@ -25,7 +25,8 @@ implies.
 --impl reference times the oracle's CPU restatement on all host cores (the Fortran reference
 cannot be built: no gfortran / MPI on this image or the GPU machine); that arm never loads the
 product library.
---model sq times only the structure factor (for profiling).
+--model sq times only the structure factor (for profiling); --model batch-mcs only the
+batched MCS loop of the 256-chain mix (ether_batch_mcs; --batch-config fixes the tiles).
 --model program times the whole program (ether_run) on a deck (--deck): the 16^3 Ising deck
 (19 temperatures x 10 REPEATs x 5000 MCS) or the 32^3 Heisenberg + overrelaxation deck (29
 temperatures x 10 REPEATs x 20000 MCS): deck read, lattice, MCS loop with measurements, and
@@ -707,7 +708,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--model", default="ising",
-                    choices=["ising", "heisenberg", "sq", "sq-ising", "batch", "learned", "learned-heisenberg", "learned-sweep",
+                    choices=["ising", "heisenberg", "sq", "sq-ising", "batch", "batch-mcs", "learned",
+                             "learned-heisenberg", "learned-sweep",
                              "learned-sweep-heisenberg",
                              "program", "pyrochlore", "pyrochlore-ising"])
     ap.add_argument("--L", type=int, default=64)
@@ -832,6 +834,38 @@ def main():
         r = run_learned(args.L, train_steps=args.learn_steps or 3000)
         print(json.dumps({"metric": "independent samples/s gain", "value": r["learned_only"]["gain_vs_plain"],
                           "unit": "x plain", "higher_is_better": True, "detail": r}))
+        return 0
+
+    if args.model == "batch-mcs":
+        # the whole MCS loop of the mixed batch (one context per chain) through
+        # ether_batch_mcs alone: --steps timed steps after --warmup, tiles autotuned or given
+        if rank != 0:
+            return 0
+        import ether_gb300 as eg
+        members, _ = make_batch_members(args.chains, 32, grouped=False, mix=args.batch_mix)
+        b = eg.Batch(members)
+        if args.batch_config:
+            b.set_config(*[int(x) for x in args.batch_config.split(",")])
+        else:
+            b.autotune()
+        period = MCS_SCHEDULE["coa"]
+        warm = max(1, args.warmup // period) * period
+        steps = max(1, args.steps // period) * period
+        sc = b.mcs(0, warm, **MCS_SCHEDULE)
+        t = time.perf_counter()
+        b.mcs(warm, steps, swap_counts=sc, **MCS_SCHEDULE)
+        wall = time.perf_counter() - t
+        info = b.info()
+        print(json.dumps({"metric": "batch MCS step", "value": wall * 1e3 / steps, "unit": "ms",
+                          "higher_is_better": False, "detail": {
+                              "contexts": len(members), "replicas": info.n_replicas,
+                              "site_updates_per_sweep": info.site_updates_per_sweep,
+                              "schedule": MCS_SCHEDULE, "steps": steps, "warmup": warm,
+                              "event_ms_per_step": info.last_sweep_ms,
+                              "tile_config": [info.threads, info.units_per_thread, info.blocks_per_sm, info.walk]}}))
+        b.close()
+        for m in members:
+            m.close()
         return 0
 
     if args.model == "batch":

@@ -24,6 +24,25 @@ namespace ether {
 
 constexpr int kMaxColours = 64;
 
+// Division by a loop-invariant divisor d >= 1 for 0 <= n < 2^31, by multiply and shift
+// (Granlund & Montgomery, "Division by invariant integers using multiplication", PLDI 1994;
+// round-up variant): l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1,
+// n / d = (umulhi(n, m) + n) >> l.  The sum cannot overflow because n < 2^31.
+struct FastDiv {
+    uint32_t d, m, l;
+};
+inline FastDiv make_fastdiv(uint32_t d) {
+    uint32_t l = 0;
+    while ((1ull << l) < d) ++l;
+    const uint64_t m = ((1ull << 32) * ((1ull << l) - d)) / d + 1;
+    return FastDiv{d, (uint32_t)m, l};
+}
+#if defined(__CUDACC__)
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) {
+    return (__umulhi(n, f.m) + n) >> f.l;
+}
+#endif
+
 struct DevTables {
     // lattice (storage order)
     int32_t *row_ptr = nullptr;   // N+1
@@ -161,6 +180,11 @@ struct ObsMember {
     const float4 *sia_ax;
     const double *mweight;
     const float *mweight_f;  // null unless every weight is exact in FP32
+    // simple-cubic XYZ contexts (sc_xyz = 1): neighbours in closed form from the colour arrays
+    int sc_xyz, sc_L1, sc_L2, sc_L3;
+    FastDiv sc_fH, sc_fL2;
+    float sc_jx, sc_jy, sc_jz;
+    int sc_pad;
     double juni, mw_abs;     // Ising counting form: the one bond coupling, the one |weight|
     int count_form, nsp;     // count_form: Ising sums by integer counts (juni, mw_abs, one species)
     double *partials;
@@ -235,22 +259,4 @@ struct ether_ctx {
 };
 
 namespace ether {
-// Division by a loop-invariant divisor d >= 1 for 0 <= n < 2^31, by multiply and shift
-// (Granlund & Montgomery, "Division by invariant integers using multiplication", PLDI 1994;
-// round-up variant): l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1,
-// n / d = (umulhi(n, m) + n) >> l.  The sum cannot overflow because n < 2^31.
-struct FastDiv {
-    uint32_t d, m, l;
-};
-inline FastDiv make_fastdiv(uint32_t d) {
-    uint32_t l = 0;
-    while ((1ull << l) < d) ++l;
-    const uint64_t m = ((1ull << 32) * ((1ull << l) - d)) / d + 1;
-    return FastDiv{d, (uint32_t)m, l};
-}
-#if defined(__CUDACC__)
-__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) {
-    return (__umulhi(n, f.m) + n) >> f.l;
-}
-#endif
 }  // namespace ether

@@ -15,6 +15,7 @@
 // turned into FP64 once per thread.
 #include "internal.h"
 #include "rng_math.cuh"
+#include "sweep_xyz.cuh"
 
 namespace ether {
 
@@ -89,15 +90,31 @@ __device__ __forceinline__ void energy_block(const ObsMember &a, int r, int b) {
         const float4 *sp = a.spins4 + (size_t)r * N;
         DS e0, e1, m0, m1, m2;
         const bool mwf = a.mweight_f != nullptr;
+        const int H = a.sc_L1 >> 1, half = N >> 1;
         for (int s = b * blockDim.x + threadIdx.x; s < N; s += stride) {
             const float4 S = sp[s];
             float hx = 0.f, hy = 0.f, hz = 0.f;
-            for (int k = a.row_ptr[s]; k < a.row_ptr[s + 1]; ++k) {
-                float4 Sj = sp[a.nbr[k]];
-                const float *Jp = a.J + 3 * a.jidx[k];
-                hx = fmaf(Jp[0], Sj.x, hx);
-                hy = fmaf(Jp[1], Sj.y, hy);
-                hz = fmaf(Jp[2], Sj.z, hz);
+            if (a.sc_xyz) {
+                // simple cubic: storage index s = colour * half + rank; the six neighbours in
+                // closed form from the other colour's array, summed in the CSR's order
+                const int colour = s >= half ? 1 : 0, rho = s - colour * half;
+                const int row = (int)fdiv((uint32_t)rho, a.sc_fH);
+                const int xh = rho - row * H;
+                const int z = (int)fdiv((uint32_t)row, a.sc_fL2), y = row - z * a.sc_L2;
+                const int p = (y + z + colour) & 1;
+                const Acc3 h = sc_field(sp + (size_t)(colour ^ 1) * half, a.sc_L1, a.sc_L2, a.sc_L3, H, xh, y, z, p,
+                                        a.sc_jx, a.sc_jy, a.sc_jz);
+                hx = h.x;
+                hy = h.y;
+                hz = h.z;
+            } else {
+                for (int k = a.row_ptr[s]; k < a.row_ptr[s + 1]; ++k) {
+                    float4 Sj = sp[a.nbr[k]];
+                    const float *Jp = a.J + 3 * a.jidx[k];
+                    hx = fmaf(Jp[0], Sj.x, hx);
+                    hy = fmaf(Jp[1], Sj.y, hy);
+                    hz = fmaf(Jp[2], Sj.z, hz);
+                }
             }
             float e = S.x * hx;
             e = fmaf(S.y, hy, e);
@@ -314,6 +331,16 @@ ObsMember obs_member(const Ctx &c) {
     a.mw_abs = c.mw_abs;
     a.nsp = c.nsp;
     a.count_form = (c.model == 0 && c.juni_set && c.mw_abs > 0.0 && (!c.zeeman || c.nsp == 1)) ? 1 : 0;
+    a.sc_xyz = (c.fast && c.model == 1) ? 1 : 0;
+    a.sc_L1 = c.L[0];
+    a.sc_L2 = c.L[1];
+    a.sc_L3 = c.L[2];
+    a.sc_fH = make_fastdiv((uint32_t)std::max(1, c.L[0] / 2));
+    a.sc_fL2 = make_fastdiv((uint32_t)std::max(1, c.L[1]));
+    a.sc_jx = a.sc_xyz ? c.h_Jf[0] : 0.f;
+    a.sc_jy = a.sc_xyz ? c.h_Jf[1] : 0.f;
+    a.sc_jz = a.sc_xyz ? c.h_Jf[2] : 0.f;
+    a.sc_pad = 0;
     a.partials = c.partials;
     a.nblk = c.partial_blocks;
     a.R = c.R;
