@@ -7,12 +7,12 @@
 // every accumulator is FP64.  Reductions write per-block partials to scratch memory and a
 // second kernel adds them in a fixed order, so results do not depend on timing.
 //
-// GB300 issues about 2 FP64 instructions per SM and clock against 128 FP32, so a thread's
-// running sums avoid FP64 per site: Ising bond terms s_i s_j J are +-J exactly, so with one
-// coupling, one species and one |weight| a thread counts them in integers and multiplies
-// once (else it adds +-J, one FP64 add per bond); XYZ sums are kept as FP32 double-single
-// pairs (Knuth's TwoSum, products split exactly with fmaf), about 48 significant bits, and
-// turned into FP64 once per thread.
+// GB300 issues about 2 FP64 instructions per SM and clock against 128 FP32, so the running
+// sums avoid FP64 per site: Ising bond terms s_i s_j J are +-J exactly, so with one coupling,
+// one species and one |weight| a thread counts them in integers and the warp adds the
+// counts (else it adds +-J, one FP64 add per bond); XYZ sums are kept as FP32 double-single
+// pairs (Knuth's TwoSum, products split exactly with fmaf), about 48 significant bits,
+// summed over the warp the same way and turned into FP64 once per warp.
 #include "internal.h"
 #include "rng_math.cuh"
 #include "sweep_xyz.cuh"
@@ -42,6 +42,17 @@ __device__ __forceinline__ void ds_add_prod(DS &a, float w, float x) {
     a.lo += e;
 }
 __device__ __forceinline__ double ds_value(const DS &a) { return (double)a.hi + (double)a.lo; }
+// Warp sum of double-single values (lane 0 holds it): FP32 shuffles and TwoSums, no FP64.
+__device__ __forceinline__ DS warp_sum_ds(DS v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float h = __shfl_down_sync(0xffffffffu, v.hi, o);
+        const float l = __shfl_down_sync(0xffffffffu, v.lo, o);
+        ds_add(v, h);
+        v.lo += l;
+    }
+    return v;
+}
 
 // Sign flip of an FP64 value by its sign bit (no FP64 instruction).
 __device__ __forceinline__ double neg_if(double v, bool neg) {
@@ -60,6 +71,7 @@ __device__ __forceinline__ void energy_block(const ObsMember &a, int r, int b) {
     const int N = a.N;
     const int stride = a.nblk * blockDim.x;
     double q[kNq] = {0, 0, 0, 0, 0};
+    bool warp_done = false;  // q already holds the warp's sums (lane 0)
     if (a.model == 0 && a.count_form) {
         // E_ex = J sum s_i s_j, the field term z sum s_i, M = |w| sum sign(w_i) s_i
         const uint8_t *sp = a.spins + (size_t)r * N;
@@ -71,9 +83,14 @@ __device__ __forceinline__ void energy_block(const ObsMember &a, int r, int b) {
             const bool wneg = __double_as_longlong(a.mweight[s]) < 0;
             cm += ((own != 0) != wneg) ? 1 : -1;
         }
+        // counts summed over the warp in integers, turned into FP64 once per warp
+        cb = __reduce_add_sync(0xffffffffu, cb);
+        cz = __reduce_add_sync(0xffffffffu, cz);
+        cm = __reduce_add_sync(0xffffffffu, cm);
         q[1] = a.juni * (double)cb;
         q[0] = a.zeeman ? q[1] + a.zeed[2] * (double)cz : q[1];
         q[4] = a.mw_abs * (double)cm;
+        warp_done = true;
     } else if (a.model == 0) {
         const uint8_t *sp = a.spins + (size_t)r * N;
         for (int s = b * blockDim.x + threadIdx.x; s < N; s += stride) {
@@ -155,19 +172,24 @@ __device__ __forceinline__ void energy_block(const ObsMember &a, int r, int b) {
                 q[4] += w * (double)S.z;
             }
         }
-        q[0] = ds_value(e0);
-        q[1] = ds_value(e1);
+        // double-single sums over the warp, turned into FP64 once per warp
+        q[0] = ds_value(warp_sum_ds(e0));
+        q[1] = ds_value(warp_sum_ds(e1));
         if (mwf) {
-            q[2] = ds_value(m0);
-            q[3] = ds_value(m1);
-            q[4] = ds_value(m2);
+            q[2] = ds_value(warp_sum_ds(m0));
+            q[3] = ds_value(warp_sum_ds(m1));
+            q[4] = ds_value(warp_sum_ds(m2));
+            warp_done = true;
+        } else {
+            for (int j = 2; j < kNq; ++j) q[j] = warp_sum_d(q[j]);
+            warp_done = true;
         }
     }
     __shared__ double sm[kRedBs / 32][kNq];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int j = 0; j < kNq; ++j) {
-        double v = warp_sum_d(q[j]);
+        const double v = warp_done ? q[j] : warp_sum_d(q[j]);
         if (lane == 0) sm[wid][j] = v;
     }
     __syncthreads();
@@ -373,13 +395,14 @@ cudaError_t launch_energy_mag(Ctx &c, bool) {
 }
 
 // Magnetisation only (src/get_tot_magnetisation.f90:32-40), no neighbour reads: per-block
-// partial sums of w_s S_s into partials[(r*nblk + b)*kNq + 2..4], summed per thread as
-// energy_block sums them (so the two give the same M).
+// partial sums of w_s S_s into partials[(r*nblk + b)*kNq + 2..4], summed per thread and
+// warp as energy_block sums them (so the two give the same M).
 __global__ void __launch_bounds__(kRedBs) mag_kernel(const ObsMember a) {
     const int r = blockIdx.y;
     const int N = a.N;
     const int stride = gridDim.x * blockDim.x;
     double q[3] = {0, 0, 0};
+    bool warp_done = false;  // q already holds the warp's sums (lane 0)
     if (a.model == 0 && a.count_form) {
         const uint8_t *sp = a.spins + (size_t)r * N;
         int cm = 0;
@@ -387,7 +410,8 @@ __global__ void __launch_bounds__(kRedBs) mag_kernel(const ObsMember a) {
             const bool wneg = __double_as_longlong(a.mweight[s]) < 0;
             cm += ((sp[s] != 0) != wneg) ? 1 : -1;
         }
-        q[2] = a.mw_abs * (double)cm;
+        q[2] = a.mw_abs * (double)__reduce_add_sync(0xffffffffu, cm);
+        warp_done = true;
     } else if (a.model == 0) {
         const uint8_t *sp = a.spins + (size_t)r * N;
         for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += stride)
@@ -402,9 +426,10 @@ __global__ void __launch_bounds__(kRedBs) mag_kernel(const ObsMember a) {
             ds_add_prod(m1, wf, S.y);
             ds_add_prod(m2, wf, S.z);
         }
-        q[0] = ds_value(m0);
-        q[1] = ds_value(m1);
-        q[2] = ds_value(m2);
+        q[0] = ds_value(warp_sum_ds(m0));
+        q[1] = ds_value(warp_sum_ds(m1));
+        q[2] = ds_value(warp_sum_ds(m2));
+        warp_done = true;
     } else {
         const float4 *sp = a.spins4 + (size_t)r * N;
         for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += stride) {
@@ -419,7 +444,7 @@ __global__ void __launch_bounds__(kRedBs) mag_kernel(const ObsMember a) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-        double v = warp_sum_d(q[j]);
+        const double v = warp_done ? q[j] : warp_sum_d(q[j]);
         if (lane == 0) sm[wid][j] = v;
     }
     __syncthreads();
