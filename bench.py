@@ -722,6 +722,8 @@ def main():
                     help="--model learned / learned-heisenberg: Adam steps (default 3000 / 4000)")
     ap.add_argument("--sq-cells", type=int, default=12)
     ap.add_argument("--chains", type=int, default=256)
+    ap.add_argument("--mcs-parts", action="store_true",
+                    help="batch-mcs: also time the loop with parts of the schedule switched off")
     ap.add_argument("--deck", default="c1_ising_16", choices=sorted(PROGRAM_DECKS))
     ap.add_argument("--batch-mix", default="mixed", choices=["mixed", "ising", "heisenberg"],
                     help="--model batch: half Ising and half Heisenberg chains, or one model only")
@@ -851,6 +853,19 @@ def main():
         period = MCS_SCHEDULE["coa"]
         warm = max(1, args.warmup // period) * period
         steps = max(1, args.steps // period) * period
+        parts = {}
+        if args.mcs_parts:
+            # the same loop with parts of the schedule switched off (time per step by parts)
+            off = dict(MCS_SCHEDULE, tmcs_eq=10 ** 9, ovrr=False, pt=False)
+            step0 = 0
+            for name, sch in (("sweeps", off), ("sweeps + measurement every 10", dict(off, tmcs_eq=0)),
+                              ("sweeps + PT every 5", dict(off, pt=True)),
+                              ("sweeps + overrelaxation every 5", dict(off, ovrr=True))):
+                sc0 = b.mcs(step0, warm, **sch)
+                t = time.perf_counter()
+                b.mcs(step0 + warm, steps, swap_counts=sc0, **sch)
+                parts[name] = (time.perf_counter() - t) * 1e3 / steps
+                step0 += warm + steps
         sc = b.mcs(0, warm, **MCS_SCHEDULE)
         t = time.perf_counter()
         b.mcs(warm, steps, swap_counts=sc, **MCS_SCHEDULE)
@@ -861,7 +876,7 @@ def main():
                               "contexts": len(members), "replicas": info.n_replicas,
                               "site_updates_per_sweep": info.site_updates_per_sweep,
                               "schedule": MCS_SCHEDULE, "steps": steps, "warmup": warm,
-                              "event_ms_per_step": info.last_sweep_ms,
+                              "event_ms_per_step": info.last_sweep_ms, "parts_ms_per_step": parts,
                               "tile_config": [info.threads, info.units_per_thread, info.blocks_per_sm, info.walk]}}))
         b.close()
         for m in members:
