@@ -423,10 +423,12 @@ extern "C" int ether_create(const ether_desc *d, ether_ctx **out) {
             if (c.h_Jd[3 * (size_t)j + 2] != c.ising_juni) { c.juni_set = false; break; }
     }
     c.mw_abs = N > 0 ? std::fabs(mw[0]) : 0.0;
+    c.mw_pos = N > 0;
     bool mw_f32 = true;
     std::vector<float> mwf(N);
     for (int s = 0; s < N; ++s) {
         if (std::fabs(mw[s]) != c.mw_abs) c.mw_abs = 0.0;
+        if (!(mw[s] > 0.0)) c.mw_pos = false;
         mwf[s] = (float)mw[s];
         if ((double)mwf[s] != mw[s]) mw_f32 = false;
     }

@@ -150,7 +150,7 @@ struct Ctx {
     int partial_blocks = 0;
     // exact shortcuts of the energy reduction (k_obs.cu): every bond's z coupling equal
     // (ising_juni, Ising), every |weight| equal (mw_abs), every weight exact in FP32
-    bool juni_set = false;
+    bool juni_set = false, mw_pos = false;
     double ising_juni = 0.0, mw_abs = 0.0;
     int32_t *pt_accepts = nullptr;  // 1
     int32_t *swap_dev = nullptr;    // 1: PT swap counter
@@ -180,11 +180,13 @@ struct ObsMember {
     const float4 *sia_ax;
     const double *mweight;
     const float *mweight_f;  // null unless every weight is exact in FP32
-    // simple-cubic XYZ contexts (sc_xyz = 1): neighbours in closed form from the colour arrays
-    int sc_xyz, sc_L1, sc_L2, sc_L3;
+    // simple-cubic contexts (sc_xyz = 1 XYZ, sc_ising = 1 Ising in the counting form):
+    // neighbours in closed form from the colour arrays; mw_pos: every weight is +mw_abs
+    int sc_xyz, sc_L1, sc_L2, sc_L3, sc_ising, mw_pos;
     FastDiv sc_fH, sc_fL2;
     float sc_jx, sc_jy, sc_jz;
-    int sc_pad;
+    float mw_abs_f;          // mw_abs in FP32 (exact when mweight_f is set)
+    int sc_pad2, sc_pad3;
     double juni, mw_abs;     // Ising counting form: the one bond coupling, the one |weight|
     int count_form, nsp;     // count_form: Ising sums by integer counts (juni, mw_abs, one species)
     double *partials;

@@ -54,6 +54,26 @@ __device__ __forceinline__ DS warp_sum_ds(DS v) {
     return v;
 }
 
+// Simple cubic, colour-split arrays: sum over the six bonds of rank rho of colour `colour`
+// of s_i s_j (+1 aligned, -1 not), neighbours in closed form from the other colour's bytes.
+__device__ __forceinline__ int sc_ising_bonds(const uint8_t *__restrict__ opp, const ObsMember &a, int H,
+                                              int colour, int rho, uint8_t own) {
+    const int row = (int)fdiv((uint32_t)rho, a.sc_fH);
+    const int xh = rho - row * H;
+    const int z = (int)fdiv((uint32_t)row, a.sc_fL2), y = row - z * a.sc_L2;
+    const int p = (y + z + colour) & 1;
+    const int L2 = a.sc_L2, L3 = a.sc_L3;
+    const int ym = (y == 0 ? L2 - 1 : y - 1), yp = (y == L2 - 1 ? 0 : y + 1);
+    const int zm = (z == 0 ? L3 - 1 : z - 1), zp = (z == L3 - 1 ? 0 : z + 1);
+    const int xh_m = p == 0 ? (xh == 0 ? H - 1 : xh - 1) : xh;
+    const int xh_p = p == 0 ? xh : (xh == H - 1 ? 0 : xh + 1);
+    const uint8_t v0 = opp[row * H + xh_m], v1 = opp[row * H + xh_p];
+    const uint8_t v2 = opp[(z * L2 + ym) * H + xh], v3 = opp[(z * L2 + yp) * H + xh];
+    const uint8_t v4 = opp[(zm * L2 + y) * H + xh], v5 = opp[(zp * L2 + y) * H + xh];
+    const int same = (v0 == own) + (v1 == own) + (v2 == own) + (v3 == own) + (v4 == own) + (v5 == own);
+    return 2 * same - 6;
+}
+
 // Sign flip of an FP64 value by its sign bit (no FP64 instruction).
 __device__ __forceinline__ double neg_if(double v, bool neg) {
     return __longlong_as_double(__double_as_longlong(v) ^ (neg ? (long long)0x8000000000000000ULL : 0LL));
@@ -76,11 +96,17 @@ __device__ __forceinline__ void energy_block(const ObsMember &a, int r, int b) {
         // E_ex = J sum s_i s_j, the field term z sum s_i, M = |w| sum sign(w_i) s_i
         const uint8_t *sp = a.spins + (size_t)r * N;
         int cb = 0, cz = 0, cm = 0;
+        const int H = a.sc_L1 >> 1, half = N >> 1;
         for (int s = b * blockDim.x + threadIdx.x; s < N; s += stride) {
             const uint8_t own = sp[s];
-            for (int k = a.row_ptr[s]; k < a.row_ptr[s + 1]; ++k) cb += (sp[a.nbr[k]] == own) ? 1 : -1;
+            if (a.sc_ising) {
+                const int colour = s >= half ? 1 : 0;
+                cb += sc_ising_bonds(sp + (size_t)(colour ^ 1) * half, a, H, colour, s - colour * half, own);
+            } else {
+                for (int k = a.row_ptr[s]; k < a.row_ptr[s + 1]; ++k) cb += (sp[a.nbr[k]] == own) ? 1 : -1;
+            }
             cz += own ? 1 : -1;
-            const bool wneg = __double_as_longlong(a.mweight[s]) < 0;
+            const bool wneg = a.mw_pos ? false : __double_as_longlong(a.mweight[s]) < 0;
             cm += ((own != 0) != wneg) ? 1 : -1;
         }
         // counts summed over the warp in integers, turned into FP64 once per warp
@@ -161,7 +187,7 @@ __device__ __forceinline__ void energy_block(const ObsMember &a, int r, int b) {
             }
             ds_add(e0, e);
             if (mwf) {
-                const float wf = a.mweight_f[s];
+                const float wf = a.mw_pos ? a.mw_abs_f : a.mweight_f[s];  // mw_pos: all weights +mw_abs
                 ds_add_prod(m0, wf, S.x);
                 ds_add_prod(m1, wf, S.y);
                 ds_add_prod(m2, wf, S.z);
@@ -354,6 +380,9 @@ ObsMember obs_member(const Ctx &c) {
     a.nsp = c.nsp;
     a.count_form = (c.model == 0 && c.juni_set && c.mw_abs > 0.0 && (!c.zeeman || c.nsp == 1)) ? 1 : 0;
     a.sc_xyz = (c.fast && c.model == 1) ? 1 : 0;
+    a.sc_ising = (c.fast && c.model == 0 && a.count_form) ? 1 : 0;
+    a.mw_pos = (c.mw_pos && c.mw_abs > 0.0) ? 1 : 0;
+    a.sc_pad2 = a.sc_pad3 = 0;
     a.sc_L1 = c.L[0];
     a.sc_L2 = c.L[1];
     a.sc_L3 = c.L[2];
@@ -362,7 +391,7 @@ ObsMember obs_member(const Ctx &c) {
     a.sc_jx = a.sc_xyz ? c.h_Jf[0] : 0.f;
     a.sc_jy = a.sc_xyz ? c.h_Jf[1] : 0.f;
     a.sc_jz = a.sc_xyz ? c.h_Jf[2] : 0.f;
-    a.sc_pad = 0;
+    a.mw_abs_f = (float)c.mw_abs;
     a.partials = c.partials;
     a.nblk = c.partial_blocks;
     a.R = c.R;
@@ -407,7 +436,7 @@ __global__ void __launch_bounds__(kRedBs) mag_kernel(const ObsMember a) {
         const uint8_t *sp = a.spins + (size_t)r * N;
         int cm = 0;
         for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += stride) {
-            const bool wneg = __double_as_longlong(a.mweight[s]) < 0;
+            const bool wneg = a.mw_pos ? false : __double_as_longlong(a.mweight[s]) < 0;
             cm += ((sp[s] != 0) != wneg) ? 1 : -1;
         }
         q[2] = a.mw_abs * (double)__reduce_add_sync(0xffffffffu, cm);
@@ -421,7 +450,7 @@ __global__ void __launch_bounds__(kRedBs) mag_kernel(const ObsMember a) {
         DS m0, m1, m2;
         for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += stride) {
             const float4 S = sp[s];
-            const float wf = a.mweight_f[s];
+            const float wf = a.mw_pos ? a.mw_abs_f : a.mweight_f[s];
             ds_add_prod(m0, wf, S.x);
             ds_add_prod(m1, wf, S.y);
             ds_add_prod(m2, wf, S.z);
