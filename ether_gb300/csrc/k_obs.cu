@@ -609,8 +609,9 @@ __device__ __forceinline__ int member_of(const int32_t *__restrict__ off, int M,
     return lo;
 }
 
-// One block per (member, replica, energy block).
-__global__ void __launch_bounds__(kRedBs)
+// One block per (member, replica, energy block); capped at four resident blocks per SM (the
+// kernel waits on neighbour gathers, so more warps hide more of it).
+__global__ void __launch_bounds__(kRedBs, 4)
 batch_energy_kernel(const ObsMember *__restrict__ mem, const int32_t *__restrict__ eoff, int M) {
     const int m = member_of(eoff, M, blockIdx.x);
     const ObsMember &a = mem[m];
