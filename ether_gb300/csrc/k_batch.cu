@@ -281,7 +281,8 @@ struct ether_batch {
     std::vector<int> solo;              // per group: a member above the byte budget alone in its group
                                         // (it runs its own phase kernels), else -1
     int n_groups = 1;
-    long long group_bytes = 0;          // spin bytes per group; 0: half the L2
+    long long group_bytes = 0;          // spin bytes per group; 0: half the L2; 1: every member
+                                        // alone, on its own phase kernels
     long long l2_bytes = 0;
     int n_branch = 2;
     std::vector<cudaStream_t> branch;
@@ -970,6 +971,7 @@ extern "C" int ether_batch_set_config(ether_batch *b, int32_t threads, int32_t u
     b->threads = threads;
     b->upt = units_per_thread;
     b->bps = blocks_per_sm;
+    b->group_bytes = 0;  // the class kernels over L2-sized groups, with this tile shape
     b->dirty = true;
     return ETHER_OK;
 }
@@ -1000,6 +1002,8 @@ extern "C" int ether_batch_autotune(ether_batch *b, int32_t *config, float *best
     BCUDA(cudaMalloc((void **)&backup, std::max<size_t>(total, 1)));
     for (const Saved &s : sv) BCUDA(cudaMemcpyAsync(backup + s.off, s.src, s.bytes, cudaMemcpyDeviceToDevice, b->stream));
     const int old_t = b->threads, old_u = b->upt, old_b = b->bps;
+    const long long old_gb = b->group_bytes;
+    b->group_bytes = 0;  // the class-kernel stages below use L2-sized groups
     b->timed_sweeps = 0;
     int occ_max = 1;
     float best = 1e30f;
@@ -1104,6 +1108,38 @@ extern "C" int ether_batch_autotune(ether_batch *b, int32_t *config, float *best
             bnb = nb;
         }
     }
+    // last, every member on its own phase kernels (each member a group of its own, on the
+    // graph's parallel branches): the batch is then never slower than the members' own launches
+    // by more than the graph's own cost
+    long long bgb = 0;
+    for (int nb : {4, 8, 16}) {
+        if (rc) break;
+        b->threads = bt;
+        b->upt = bu;
+        b->bps = bb;
+        b->minb = bm;
+        b->xyz_cost = bc;
+        b->walk = bw;
+        b->n_branch = nb;
+        b->group_bytes = 1;
+        b->dirty = true;
+        rc = run_sweeps(*b, 1, false);
+        if (!rc) rc = run_sweeps(*b, 2, true);
+        if (rc) break;
+        float ms = 0.f;
+        if (cudaEventSynchronize(b->ev_t1) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, b->ev_t0, b->ev_t1) != cudaSuccess) {
+            rc = bfail(ETHER_ERR_CUDA, "batch autotune timing");
+            break;
+        }
+        ms *= 0.5f;
+        if (ms < best) {
+            best = ms;
+            bnb = nb;
+            bgb = 1;
+        }
+    }
+    b->group_bytes = rc ? old_gb : bgb;
     b->n_branch = rc ? old_nb : bnb;
     for (const Saved &s : sv) cudaMemcpyAsync(s.src, backup + s.off, s.bytes, cudaMemcpyDeviceToDevice, b->stream);
     cudaStreamSynchronize(b->stream);
