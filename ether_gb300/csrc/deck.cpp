@@ -40,6 +40,7 @@
 #include <fstream>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/ether_gpu.h"
@@ -1087,32 +1088,51 @@ extern "C" int ether_run(const char *indir, const char *outdir, int32_t flags, e
             std::vector<double> mm((size_t)R * nsp * 3);
             RTRY(ether_moment_vectors(ctx, mm.data()));
             carry.assign((size_t)9 * N * np, 0.0);
+            // the configuration the last REPEAT left at each temperature
+            std::vector<int> last(np, -1);
+            for (int s = 0; s < np; ++s) {
+                for (int r = (rep - 1) * np; r < R; ++r)
+                    if (slots[r] == s) last[s] = r;
+                if (last[s] < 0) throw RunError{ETHER_ERR_STATE};
+                std::copy(ion.begin(), ion.end(), carry.begin() + (size_t)9 * N * s);
+                RTRY(ether_get_spins(ctx, last[s], carry.data() + (size_t)9 * N * s));
+            }
+            // gss.dat blocks (src/write_gss.f90:65-77) and <T>spK.xsf files
+            // (src/write_spins_at_K.f90): the text of every temperature is formatted on the
+            // host's cores side by side, then written in temperature order
+            std::vector<std::string> gss_txt(np), xsf_txt(np);
+            {
+                const int T = (int)std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), (unsigned)np));
+                std::vector<std::thread> pool;
+                for (int w = 0; w < T; ++w)
+                    pool.emplace_back([&, w]() {
+                        for (int s = w; s < np; s += T) {
+                            const double *cfg = carry.data() + (size_t)9 * N * s;
+                            std::string g = fF(temperature[t0 + s], 11, 5) + "\n";
+                            for (long i = 0; i < N; ++i)
+                                g += fF(cfg[9 * i + 1], 11, 6) + " " + fF(cfg[9 * i + 2], 11, 6) + " " +
+                                     fF(cfg[9 * i + 3], 11, 6) + " " + fI((long)cfg[9 * i + 4], 8) + "\n";
+                            std::string xs = xsf_header(d, N);
+                            for (long i = 0; i < N; ++i) {  // format 101: (A5, 1x, six f13.7 separated by 1x)
+                                xs += fA(d.species[(int)cfg[9 * i + 4] - 1], 2, 5);
+                                for (int k : {6, 7, 8, 1, 2, 3}) xs += " " + fF(cfg[9 * i + k], 13, 7);
+                                xs += "\n";
+                            }
+                            gss_txt[s].swap(g);
+                            xsf_txt[s].swap(xs);
+                        }
+                    });
+                for (auto &th : pool) th.join();
+            }
             for (int s = 0; s < np; ++s) {
                 const long t = t0 + s;
-                // the configuration the last REPEAT left at this temperature
-                int r_last = -1;
-                for (int r = (rep - 1) * np; r < R; ++r)
-                    if (slots[r] == s) r_last = r;
-                if (r_last < 0) throw RunError{ETHER_ERR_STATE};
-                std::vector<double> cfg(ion);
-                RTRY(ether_get_spins(ctx, r_last, cfg.data()));
-                std::copy(cfg.begin(), cfg.end(), carry.begin() + (size_t)9 * N * s);
-                spn_f.put_record(t, cfg.data(), rec_bytes);
-                {  // gss.dat block (src/write_gss.f90:65-77) and <T>spK.xsf (src/write_spins_at_K.f90)
-                    std::string g = fF(temperature[t], 11, 5) + "\n";
-                    for (long i = 0; i < N; ++i)
-                        g += fF(cfg[9 * i + 1], 11, 6) + " " + fF(cfg[9 * i + 2], 11, 6) + " " +
-                             fF(cfg[9 * i + 3], 11, 6) + " " + fI((long)cfg[9 * i + 4], 8) + "\n";
-                    gss_f.put(g);
-                    std::string xs = xsf_header(d, N);
-                    for (long i = 0; i < N; ++i) {  // format 101: (A5, 1x, six f13.7 separated by 1x)
-                        xs += fA(d.species[(int)cfg[9 * i + 4] - 1], 2, 5);
-                        for (int k : {6, 7, 8, 1, 2, 3}) xs += " " + fF(cfg[9 * i + k], 13, 7);
-                        xs += "\n";
-                    }
-                    // name: format(f9.4, 'spK.xsf'), adjustl
-                    write_file(out + "/spins/" + trim(fF(temperature[t], 9, 4) + "spK.xsf"), xs);
-                }
+                const int r_last = last[s];
+                spn_f.put_record(t, carry.data() + (size_t)9 * N * s, rec_bytes);
+                gss_f.put(gss_txt[s]);
+                // name: format(f9.4, 'spK.xsf'), adjustl
+                write_file(out + "/spins/" + trim(fF(temperature[t], 9, 4) + "spK.xsf"), xsf_txt[s]);
+                std::string().swap(gss_txt[s]);
+                std::string().swap(xsf_txt[s]);
                 double acc = 0.0;  // acceptance_counting / (repeat tmcs), src/ether.f90:212
                 for (int g = 0; g < rep; ++g) acc += (double)accepts[(size_t)g * np + s] / (double)N;
                 acc /= (double)rep * (double)d.tmcs;
