@@ -37,6 +37,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <exception>
 #include <fstream>
 #include <sstream>
 #include <string>
@@ -1104,8 +1105,10 @@ extern "C" int ether_run(const char *indir, const char *outdir, int32_t flags, e
             {
                 const int T = (int)std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), (unsigned)np));
                 std::vector<std::thread> pool;
+                std::vector<std::exception_ptr> failed(T);  // rethrown after the join
                 for (int w = 0; w < T; ++w)
                     pool.emplace_back([&, w]() {
+                      try {
                         for (int s = w; s < np; s += T) {
                             const double *cfg = carry.data() + (size_t)9 * N * s;
                             std::string g = fF(temperature[t0 + s], 11, 5) + "\n";
@@ -1121,8 +1124,13 @@ extern "C" int ether_run(const char *indir, const char *outdir, int32_t flags, e
                             gss_txt[s].swap(g);
                             xsf_txt[s].swap(xs);
                         }
+                      } catch (...) {
+                        failed[w] = std::current_exception();
+                      }
                     });
                 for (auto &th : pool) th.join();
+                for (const std::exception_ptr &e : failed)
+                    if (e) std::rethrow_exception(e);
             }
             for (int s = 0; s < np; ++s) {
                 const long t = t0 + s;
