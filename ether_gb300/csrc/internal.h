@@ -156,6 +156,14 @@ struct Ctx {
     int32_t *swap_dev = nullptr;    // 1: PT swap counter
     int32_t *copy_from = nullptr;   // R (reference-copy PT mode)
     std::map<std::string, cudaGraphExec_t> graphs;  // ether_mcs chunks by gate pattern
+    // replica window of the general-lattice sweep launchers and launch_advance: replicas
+    // rw0 .. rw0 + rwn - 1 (rwn 0: all); ether_mcs runs parts of a general lattice's replicas
+    // on c.stream and the aux streams side by side between its PT and measurement steps
+    static constexpr int kMaxParts = 4;
+    int rw0 = 0, rwn = 0;
+    int n_parts = 0;
+    cudaStream_t aux[kMaxParts - 1] = {nullptr, nullptr, nullptr};
+    cudaEvent_t ev_fork = nullptr, ev_join[kMaxParts - 1] = {nullptr, nullptr, nullptr};
     size_t device_bytes = 0;
     uint64_t launches = 0;
     float sq_ms = 0.f;  // last structure-factor kernel time (CUDA events)

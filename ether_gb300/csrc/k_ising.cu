@@ -528,9 +528,11 @@ cudaError_t launch_ising_sweep(Ctx &c, int colour) {
         if (n_c == 0) return cudaSuccess;
         const int32_t *ell = c.t.ell_nbr + c.ell_off[colour];
         const int32_t *ews = c.t.ell_ws + c.ell_off[colour];
+        const int r0 = c.rw0, nr = c.rwn ? c.rwn : c.R;  // replica window (the kernel form follows the full R)
+        uint8_t *spins = c.spins + (size_t)r0 * c.N;
         const long groups = (long)c.R * ((n_c + 7) / 8);
         if (groups < 2L * c.sm_count * bs) {  // too few groups of eight to fill the GPU
-            dim3 grid(blocks_for(c, n_c, bs), c.R);
+            dim3 grid(blocks_for(c, n_c, bs), nr);
             auto k = ising_ell_site_kernel<0>;
             switch (c.ell_width[colour]) {  // common widths at compile time
                 case 4: k = ising_ell_site_kernel<4>; break;
@@ -543,15 +545,15 @@ cudaError_t launch_ising_sweep(Ctx &c, int colour) {
                 default: break;
             }
             k<<<grid, bs, 0, c.stream>>>(
-                c.spins, c.N, c.col_off[colour], n_c, (uint32_t)colour, ell, ews, c.t.ell_deg,
+                spins, c.N, c.col_off[colour], n_c, (uint32_t)colour, ell, ews, c.t.ell_deg,
                 c.ell_width[colour], c.t.itype, c.t.type_base, c.t.type_half, c.thr, c.table_entries,
-                c.slot_of_rep, c.stream_id, c.step, c.seed, c.acc_count);
+                c.slot_of_rep + r0, c.stream_id + r0, c.step + r0, c.seed, c.acc_count + r0);
         } else {
-            dim3 grid(blocks_for(c, (n_c + 7) / 8, bs), c.R);
+            dim3 grid(blocks_for(c, (n_c + 7) / 8, bs), nr);
             ising_ell_kernel<<<grid, bs, 0, c.stream>>>(
-                c.spins, c.N, c.col_off[colour], n_c, (uint32_t)colour, ell, ews, c.t.ell_deg,
+                spins, c.N, c.col_off[colour], n_c, (uint32_t)colour, ell, ews, c.t.ell_deg,
                 c.ell_width[colour], c.t.itype, c.t.type_base, c.t.type_half, c.thr, c.table_entries,
-                c.slot_of_rep, c.stream_id, c.step, c.seed, c.acc_count);
+                c.slot_of_rep + r0, c.stream_id + r0, c.step + r0, c.seed, c.acc_count + r0);
         }
     }
     c.launches++;

@@ -265,14 +265,15 @@ cudaError_t launch_xyz_sweep(Ctx &c, int colour) {
     } else {
         const int n_c = c.col_off[colour + 1] - c.col_off[colour];
         if (n_c == 0) return cudaSuccess;
-        dim3 grid(blocks_for_x(c, n_c, bs), c.R);
+        const int r0 = c.rw0, nr = c.rwn ? c.rwn : c.R;  // replica window (the grid keeps the full R's width)
+        dim3 grid(blocks_for_x(c, n_c, bs), nr);
         const int32_t *ell = c.t.ell_nbr + c.ell_off[colour];
         const uint16_t *ej = c.t.ell_j + c.ell_off[colour];
         auto k = exchange_only ? ell_kernel_for<kXyzExchange>(c.ell_width[colour])
                                : ell_kernel_for<kXyzGeneral>(c.ell_width[colour]);
-        k<<<grid, bs, 0, c.stream>>>(c.spins4, c.N, c.col_off[colour], n_c, (uint32_t)colour, ell, ej, c.t.ell_deg,
-                                     c.ell_width[colour], c.t.J4, P, c.beta_slot_f, c.slot_of_rep, c.stream_id,
-                                     c.step, K, c.acc_count);
+        k<<<grid, bs, 0, c.stream>>>(c.spins4 + (size_t)r0 * c.N, c.N, c.col_off[colour], n_c, (uint32_t)colour, ell,
+                                     ej, c.t.ell_deg, c.ell_width[colour], c.t.J4, P, c.beta_slot_f,
+                                     c.slot_of_rep + r0, c.stream_id + r0, c.step + r0, K, c.acc_count + r0);
     }
     c.launches++;
     return cudaGetLastError();
@@ -350,7 +351,8 @@ cudaError_t launch_accept_ratio(Ctx &c, double *out) {
 }
 
 cudaError_t launch_advance(Ctx &c, uint32_t *counter) {
-    advance_kernel<<<(c.R + 255) / 256, 256, 0, c.stream>>>(counter, c.R);
+    const int r0 = c.rw0, nr = c.rwn ? c.rwn : c.R;
+    advance_kernel<<<(nr + 255) / 256, 256, 0, c.stream>>>(counter + r0, nr);
     c.launches++;
     return cudaGetLastError();
 }

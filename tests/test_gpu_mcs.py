@@ -94,6 +94,42 @@ def test_mcs_equals_the_reference_call_sequence():
     np.testing.assert_array_equal(s1.slots(), s2.slots())
 
 
+@pytest.mark.parametrize("model,R", [(eg.MODEL_XYZ, 18), (eg.MODEL_ISING, 18), (eg.MODEL_XYZ, 36),
+                                     (eg.MODEL_ISING, 36)])
+def test_mcs_in_replica_parts_equals_the_reference_call_sequence(model, R):
+    """A general lattice with 16 or more replicas: ether_mcs runs the sweeps between PT and
+    measurement steps as two (R >= 16) or four (R >= 32) replica parts on as many streams.  The
+    result equals the single-call sequence (one launch per colour phase over all replicas):
+    spins, sums, slots, swaps and acceptance counters."""
+    lat = eg.pyrochlore(2, shells=(2.97243, 5.1484), tol=1e-3)
+    shells = [[(1, 1, (1.0, 1.0, 1.0))], [(1, 1, (-0.1, -0.1, -0.1))]]
+    ladder = [beta_of(0.5 * 1.25 ** k) for k in range(6)]
+    kw = dict(zeeman=True, h=(0.0, 0.0, 1.0), g_factor=2.0)
+    s1, _ = make_pair(lat, model, shells, replicas=R, **kw)
+    s2, _ = make_pair(lat, model, shells, replicas=R, **kw)
+    assert s1.info().fast_path == 0
+    ion = random_xyz(lat, 8) if model == eg.MODEL_XYZ else random_ising(lat, 8)
+    for s in (s1, s2):
+        s.set_ladder(ladder)
+        s.set_streams(stream=list(range(R)), step=[0] * R)
+        s.set_spins(ion)
+        s.zero_avg()
+    tmcs_eq, coa, ex = 6, 5, 3
+    sc = s1.mcs(0, 40, tmcs_eq, coa, pt=True, exchange_interval=ex)
+    swap = 0
+    for step in range(1, 41):
+        s2.metropolis(1, accept=False)
+        if step % ex == 0 and step % coa != 0:
+            swap += 1
+            s2.parallel_tempering(swap)
+        s2.observable(step, tmcs_eq, coa)
+    assert sc == swap
+    np.testing.assert_array_equal(_state(s1, lat), _state(s2, lat))
+    np.testing.assert_array_equal(s1.sums(), s2.sums())
+    np.testing.assert_array_equal(s1.slots(), s2.slots())
+    np.testing.assert_array_equal(s1.accept_counts(), s2.accept_counts())
+
+
 @pytest.mark.parametrize("copy_mode", [False, True])
 def test_parallel_tempering_matches_oracle(copy_mode):
     lat = eg.simple_cubic(8)
