@@ -851,6 +851,52 @@ static int sweep_once(Ctx &c) {
 
 int ether::plain_sweep(Ctx &c) { return sweep_once(c); }
 
+// How many replica parts ether_mcs splits this context's sweeps into (general lattices:
+// their colour phases are small, dependent, latency-bound launches): 1 (no split), 2 or 4.
+static int sweep_parts(const Ctx &c) {
+    if (c.fast || c.resident) return 1;
+    return c.R >= 32 ? 4 : c.R >= 16 ? 2 : 1;
+}
+
+// m sweeps of every replica as replica parts side by side, on c.stream and the aux streams
+// (each part its own chain of colour phases, joined at the end): replicas are independent,
+// so this is the same work and the same results.
+static int sweeps_in_parts(Ctx &c, int m) {
+    const int P = c.n_parts;
+    CUDA_TRY(cudaEventRecord(c.ev_fork, c.stream));
+    for (int p = 1; p < P; ++p) CUDA_TRY(cudaStreamWaitEvent(c.aux[p - 1], c.ev_fork, 0));
+    const cudaStream_t own = c.stream;
+    int rc = ETHER_OK;
+    for (int p = 0; p < P && !rc; ++p) {
+        c.stream = p ? c.aux[p - 1] : own;
+        c.rw0 = (int)((long)c.R * p / P);
+        c.rwn = (int)((long)c.R * (p + 1) / P) - c.rw0;
+        for (int k = 0; k < m && !rc; ++k) rc = sweep_once(c);
+    }
+    c.stream = own;
+    c.rw0 = c.rwn = 0;
+    if (rc) return rc;
+    for (int p = 1; p < P; ++p) {
+        CUDA_TRY(cudaEventRecord(c.ev_join[p - 1], c.aux[p - 1]));
+        CUDA_TRY(cudaStreamWaitEvent(c.stream, c.ev_join[p - 1], 0));
+    }
+    return ETHER_OK;
+}
+
+// The streams of the replica parts, made once per context (outside any capture).
+static int ensure_parts(Ctx &c) {
+    if (c.n_parts) return ETHER_OK;
+    const int P = sweep_parts(c);
+    if (P > 1) CUDA_TRY(cudaEventCreateWithFlags(&c.ev_fork, cudaEventDisableTiming));
+    for (int p = 1; p < P; ++p) {
+        CUDA_TRY(cudaStreamCreateWithFlags(&c.aux[p - 1], cudaStreamNonBlocking));
+        CUDA_TRY(cudaEventCreateWithFlags(&c.ev_join[p - 1], cudaEventDisableTiming));
+    }
+    c.n_parts = P;
+    return ETHER_OK;
+}
+
+
 static int variant_of(const Ctx &c);
 
 extern "C" int ether_metropolis(ether_ctx *h, int32_t nsweeps, double *accept) {
@@ -894,9 +940,18 @@ extern "C" int ether_metropolis(ether_ctx *h, int32_t nsweeps, double *accept) {
     if (accept)
         CUDA_TRY(cudaMemcpyAsync(c.acc_before, c.acc_count, sizeof(unsigned long long) * c.R,
                                  cudaMemcpyDeviceToDevice, c.stream));
-    for (int k = 0; k < nsweeps; ++k) {
-        int rc = sweep_once(c);
+    if (nsweeps > 1) {
+        const int rc = ensure_parts(c);
         if (rc) return rc;
+    }
+    if (nsweeps > 1 && c.n_parts > 1) {  // general lattices: replica parts side by side, same bits
+        const int rc = sweeps_in_parts(c, nsweeps);
+        if (rc) return rc;
+    } else {
+        for (int k = 0; k < nsweeps; ++k) {
+            int rc = sweep_once(c);
+            if (rc) return rc;
+        }
     }
     if (accept) {
         CUDA_TRY(launch_accept_ratio(c, c.acc_ratio));
@@ -1125,38 +1180,6 @@ static int variant_of(const Ctx &c);
 
 // Steps sig[0 .. n): with a resident context the sweeps that no OVRR, PT or measurement
 // separates run as one ising_sc_resident launch; otherwise step by step.
-// How many replica parts ether_mcs splits this context's sweeps into (general lattices:
-// their colour phases are small, dependent, latency-bound launches): 1 (no split), 2 or 4.
-static int sweep_parts(const Ctx &c) {
-    if (c.fast || c.resident) return 1;
-    return c.R >= 32 ? 4 : c.R >= 16 ? 2 : 1;
-}
-
-// m sweeps of every replica as replica parts side by side, on c.stream and the aux streams
-// (each part its own chain of colour phases, joined at the end): replicas are independent,
-// so this is the same work and the same results.
-static int sweeps_in_parts(Ctx &c, int m) {
-    const int P = c.n_parts;
-    CUDA_TRY(cudaEventRecord(c.ev_fork, c.stream));
-    for (int p = 1; p < P; ++p) CUDA_TRY(cudaStreamWaitEvent(c.aux[p - 1], c.ev_fork, 0));
-    const cudaStream_t own = c.stream;
-    int rc = ETHER_OK;
-    for (int p = 0; p < P && !rc; ++p) {
-        c.stream = p ? c.aux[p - 1] : own;
-        c.rw0 = (int)((long)c.R * p / P);
-        c.rwn = (int)((long)c.R * (p + 1) / P) - c.rw0;
-        for (int k = 0; k < m && !rc; ++k) rc = sweep_once(c);
-    }
-    c.stream = own;
-    c.rw0 = c.rwn = 0;
-    if (rc) return rc;
-    for (int p = 1; p < P; ++p) {
-        CUDA_TRY(cudaEventRecord(c.ev_join[p - 1], c.aux[p - 1]));
-        CUDA_TRY(cudaStreamWaitEvent(c.stream, c.ev_join[p - 1], 0));
-    }
-    return ETHER_OK;
-}
-
 static int issue_steps(Ctx &c, const ether_schedule *sch, const int8_t *sig, int n) {
     if (c.n_parts > 1) {
         // runs of sweeps that no OVRR, PT or measurement separates, in replica parts
@@ -1225,14 +1248,9 @@ extern "C" int ether_mcs(ether_ctx *h, const ether_schedule *sch, int32_t step0,
     const bool pt_on = sch->pt && sch->exchange_interval > 0;
     const int32_t sc0 = swap_count ? *swap_count : 0;
     CUDA_TRY(cudaMemcpyAsync(c.swap_dev, &sc0, sizeof(int32_t), cudaMemcpyHostToDevice, c.stream));
-    if (c.n_parts == 0) {  // the streams of the replica parts, made once
-        const int P = sweep_parts(c);
-        if (P > 1) CUDA_TRY(cudaEventCreateWithFlags(&c.ev_fork, cudaEventDisableTiming));
-        for (int p = 1; p < P; ++p) {
-            CUDA_TRY(cudaStreamCreateWithFlags(&c.aux[p - 1], cudaStreamNonBlocking));
-            CUDA_TRY(cudaEventCreateWithFlags(&c.ev_join[p - 1], cudaEventDisableTiming));
-        }
-        c.n_parts = P;
+    {
+        const int rc = ensure_parts(c);
+        if (rc) return rc;
     }
     const long period = mcs_period(sch, ovrr_on, pt_on);
     int chunk = mcs_chunk(period);

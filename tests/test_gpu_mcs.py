@@ -130,6 +130,28 @@ def test_mcs_in_replica_parts_equals_the_reference_call_sequence(model, R):
     np.testing.assert_array_equal(s1.accept_counts(), s2.accept_counts())
 
 
+@pytest.mark.parametrize("model", [eg.MODEL_XYZ, eg.MODEL_ISING])
+def test_metropolis_in_replica_parts_equals_single_sweeps(model):
+    """ether_metropolis(n > 1) on a general lattice with 36 replicas runs the n sweeps as four
+    replica parts on parallel streams: the same spins and acceptance counters as n calls of one
+    sweep."""
+    lat = eg.pyrochlore(2, shells=(2.97243, 5.1484), tol=1e-3)
+    shells = [[(1, 1, (1.0, 1.0, 1.0))], [(1, 1, (-0.1, -0.1, -0.1))]]
+    R = 36
+    s1, _ = make_pair(lat, model, shells, replicas=R)
+    s2, _ = make_pair(lat, model, shells, replicas=R)
+    ion = random_xyz(lat, 4) if model == eg.MODEL_XYZ else random_ising(lat, 4)
+    for s in (s1, s2):
+        s.set_beta([beta_of(0.4 + 0.1 * r) for r in range(R)])
+        s.set_streams(stream=list(range(R)), step=[0] * R)
+        s.set_spins(ion)
+    s1.metropolis(12, accept=False)
+    for _ in range(12):
+        s2.metropolis(1, accept=False)
+    np.testing.assert_array_equal(_state(s1, lat), _state(s2, lat))
+    np.testing.assert_array_equal(s1.accept_counts(), s2.accept_counts())
+
+
 @pytest.mark.parametrize("copy_mode", [False, True])
 def test_parallel_tempering_matches_oracle(copy_mode):
     lat = eg.simple_cubic(8)
