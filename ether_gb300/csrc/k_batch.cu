@@ -283,6 +283,8 @@ struct ether_batch {
     int n_groups = 1;
     long long group_bytes = 0;          // spin bytes per group; 0: half the L2; 1: every member
                                         // alone, on its own phase kernels
+    bool xyz_solo = false;              // every XYZ member alone on its own kernels, Ising members
+                                        // in the class kernels
     long long l2_bytes = 0;
     int n_branch = 2;
     std::vector<cudaStream_t> branch;
@@ -451,14 +453,19 @@ int rebuild(ether_batch &b) {
         for (size_t k = 0; k < b.members.size(); ++k) {
             const Ctx &c = b.members[k]->c;
             const long long bytes = (long long)c.R * c.N * (c.model == ETHER_MODEL_ISING ? 1 : (long long)sizeof(float4));
-            if (used > 0 && (used + bytes > budget || bytes > budget)) {
+            // a large member, or (xyz_solo) an XYZ member: a group of its own, its own kernels
+            const bool alone = bytes > budget || (b.xyz_solo && c.model == ETHER_MODEL_XYZ);
+            if (used > 0 && (used + bytes > budget || alone)) {
                 ++g;
                 used = 0;
                 b.solo.push_back(-1);
             }
             b.group_of[k] = g;
             used += bytes;
-            if (bytes > budget) b.solo[g] = (int)k;  // a large member: its own kernels, no segments
+            if (alone) {
+                b.solo[g] = (int)k;  // no segments
+                used = budget + 1;   // the next member starts a new group
+            }
         }
         b.n_groups = g + 1;
     }
@@ -972,6 +979,7 @@ extern "C" int ether_batch_set_config(ether_batch *b, int32_t threads, int32_t u
     b->upt = units_per_thread;
     b->bps = blocks_per_sm;
     b->group_bytes = 0;  // the class kernels over L2-sized groups, with this tile shape
+    b->xyz_solo = false;
     b->dirty = true;
     return ETHER_OK;
 }
@@ -1003,7 +1011,9 @@ extern "C" int ether_batch_autotune(ether_batch *b, int32_t *config, float *best
     for (const Saved &s : sv) BCUDA(cudaMemcpyAsync(backup + s.off, s.src, s.bytes, cudaMemcpyDeviceToDevice, b->stream));
     const int old_t = b->threads, old_u = b->upt, old_b = b->bps;
     const long long old_gb = b->group_bytes;
+    const bool old_xs = b->xyz_solo;
     b->group_bytes = 0;  // the class-kernel stages below use L2-sized groups
+    b->xyz_solo = false;
     b->timed_sweeps = 0;
     int occ_max = 1;
     float best = 1e30f;
@@ -1110,10 +1120,17 @@ extern "C" int ether_batch_autotune(ether_batch *b, int32_t *config, float *best
     }
     // last, every member on its own phase kernels (each member a group of its own, on the
     // graph's parallel branches): the batch is then never slower than the members' own launches
-    // by more than the graph's own cost
+    // by more than the graph's own cost; and the hybrid of XYZ members on their own kernels
+    // with Ising members in the class kernels
     long long bgb = 0;
-    for (int nb : {4, 8, 16}) {
+    bool bxs = false;
+    bool have_xyz = false, have_ising = false;
+    for (ether_ctx *h : b->members) (h->c.model == ETHER_MODEL_XYZ ? have_xyz : have_ising) = true;
+    for (int cand = 0; cand < 6; ++cand) {
         if (rc) break;
+        const int nb = (cand % 3 == 0) ? 4 : (cand % 3 == 1) ? 8 : 16;
+        const bool hybrid = cand >= 3;
+        if (hybrid && !(have_xyz && have_ising)) continue;
         b->threads = bt;
         b->upt = bu;
         b->bps = bb;
@@ -1121,7 +1138,8 @@ extern "C" int ether_batch_autotune(ether_batch *b, int32_t *config, float *best
         b->xyz_cost = bc;
         b->walk = bw;
         b->n_branch = nb;
-        b->group_bytes = 1;
+        b->group_bytes = hybrid ? 0 : 1;
+        b->xyz_solo = hybrid;
         b->dirty = true;
         rc = run_sweeps(*b, 1, false);
         if (!rc) rc = run_sweeps(*b, 2, true);
@@ -1136,10 +1154,12 @@ extern "C" int ether_batch_autotune(ether_batch *b, int32_t *config, float *best
         if (ms < best) {
             best = ms;
             bnb = nb;
-            bgb = 1;
+            bgb = hybrid ? 0 : 1;
+            bxs = hybrid;
         }
     }
     b->group_bytes = rc ? old_gb : bgb;
+    b->xyz_solo = rc ? old_xs : bxs;
     b->n_branch = rc ? old_nb : bnb;
     for (const Saved &s : sv) cudaMemcpyAsync(s.src, backup + s.off, s.bytes, cudaMemcpyDeviceToDevice, b->stream);
     cudaStreamSynchronize(b->stream);

@@ -319,9 +319,9 @@ int ether_batch_mcs(ether_batch *batch, const ether_schedule *sch, int32_t step0
 int ether_batch_set_config(ether_batch *batch, int32_t threads, int32_t units_per_thread,
                            int32_t blocks_per_sm, int32_t walk);
 /* Autotuner: times the tile shapes, register caps and walks on the members' data (spins
- * and counters are restored) and keeps the fastest; its last candidate runs every member on
- * its own phase kernels inside the batch graph (ether_batch_set_config returns to the class
- * kernels).  config(4) = threads, units per thread,
+ * and counters are restored) and keeps the fastest; its last candidates run every member, or
+ * every XYZ member, on its own phase kernels inside the batch graph (ether_batch_set_config
+ * returns to the class kernels).  config(4) = threads, units per thread,
  * blocks per SM, walk; best_ms = one sweep.  Either output may be NULL. */
 int ether_batch_autotune(ether_batch *batch, int32_t *config, float *best_ms);
 typedef struct ether_batch_info {
