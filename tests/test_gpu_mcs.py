@@ -152,6 +152,84 @@ def test_metropolis_in_replica_parts_equals_single_sweeps(model):
     np.testing.assert_array_equal(s1.accept_counts(), s2.accept_counts())
 
 
+@pytest.mark.parametrize("model", [eg.MODEL_XYZ, eg.MODEL_ISING])
+def test_mcs_equals_the_oracles_replay_of_the_loop(model):
+    """ether_mcs (overrelaxation every 3 steps for XYZ, PT every 2, a measurement every 4 after
+    4 equilibration steps; 4 slots x 2 groups) against the oracle's replay of the same loop:
+    Checkerboard sweeps of every replica at its current slot's temperature, overrelaxation
+    passes, the total energies, PT swaps of each group (src/parallel_tempering.f90:39-108 with
+    the same draws) and the observable accumulators (src/observable.f90:30-43).  Spins, slots
+    and the swap count agree exactly; the accumulators to 1e-12 (energies are summed in another
+    order)."""
+    lat = eg.simple_cubic(8)
+    ns, R, steps = 4, 8, 24
+    ladder = np.array([beta_of(f * (1.443 if model == eg.MODEL_XYZ else 4.511)) for f in (0.8, 1.0, 1.2, 1.5)])
+    sw, osys = make_pair(lat, model, FM, replicas=R)
+    sw.set_ladder(ladder)
+    streams = [3 * r + 1 for r in range(R)]
+    sw.set_streams(stream=streams, step=[0] * R)
+    xyz = model == eg.MODEL_XYZ
+    ions = [(random_xyz if xyz else random_ising)(lat, 60 + r) for r in range(R)]
+    for r in range(R):
+        sw.set_spins(ions[r], replica=r)
+    sw.zero_avg()
+    tmcs_eq, coa, ovrr_mcs, para, ex = 4, 4, 3, 0.5, 2
+    sc = sw.mcs(0, steps, tmcs_eq, coa, ovrr=xyz, ovrr_para=para, ovrr_mcs=ovrr_mcs, pt=True,
+                exchange_interval=ex)
+
+    ncol, col, rank = osys.colouring()
+    sp4 = [osys.spin4(ion) if xyz else None for ion in ions]
+    sor = np.arange(R) % ns                      # slot of each replica
+    ros = np.arange(R, dtype=np.int32)           # per group: replica of each slot
+    sums = np.zeros((R, 7))
+    swap = 0
+    N = lat.N
+
+    def energy(r):
+        return osys.tot_energy_f32(ions[r], sp4[r]) if xyz else osys.tot_energy(ions[r])
+
+    def mag(r):
+        return osys.tot_magnetisation_f32(ions[r], sp4[r]) if xyz else osys.tot_magnetisation(ions[r])
+
+    t_ovrr = 0  # the overrelaxation counter advances once per overrelaxation step
+    for step in range(1, steps + 1):
+        if xyz and step % ovrr_mcs == 0 and step % coa != 0:
+            for r in range(R):
+                osys.overrelax_colour(ions[r], sp4[r], para, 1992, streams[r], t_ovrr, col, rank, ncol)
+            t_ovrr += 1
+        for r in range(R):
+            osys.metropolis_colour(ions[r], sp4[r], 32 if xyz else 64, float(ladder[sor[r]]), 1992, streams[r],
+                                   step - 1, col, rank, ncol)
+        if step % ex == 0 and step % coa != 0:
+            E = np.array([energy(r) for r in range(R)])
+            swap += 1
+            copy_from = np.zeros(ns, dtype=np.int32)
+            for g in range(R // ns):
+                sub = np.ascontiguousarray(ros[g * ns:(g + 1) * ns])
+                po.lib().orc_parallel_tempering(ns, ladder.ctypes.data_as(po.PD), E.ctypes.data_as(po.PD),
+                                                sub.ctypes.data_as(po.PI), swap, 1992, g, 0,
+                                                copy_from.ctypes.data_as(po.PI))
+                ros[g * ns:(g + 1) * ns] = sub
+            for g in range(R // ns):
+                for s_ in range(ns):
+                    sor[ros[g * ns + s_]] = s_
+        if step > tmcs_eq and step % coa == 0:
+            for r in range(R):
+                e = energy(r) / (2.0 * N)
+                m = np.linalg.norm(mag(r)) / N
+                a = sums[(r // ns) * ns + sor[r]]
+                a += [1.0, e, e * e, (e * e) * (e * e), m, m * m, (m * m) * (m * m)]
+    assert sc == swap
+    np.testing.assert_array_equal(sw.slots(), sor)
+    for r in range(R):
+        g = sw.get_spins(lat.ion, r)
+        if xyz:
+            np.testing.assert_array_equal(g[:, [1, 2, 3, 5]].astype(np.float32), sp4[r], err_msg="replica %d" % r)
+        else:
+            np.testing.assert_array_equal(g[:, 3], ions[r][:, 3], err_msg="replica %d" % r)
+    np.testing.assert_allclose(sw.sums(), sums, rtol=1e-12, atol=1e-15)
+
+
 @pytest.mark.parametrize("copy_mode", [False, True])
 def test_parallel_tempering_matches_oracle(copy_mode):
     lat = eg.simple_cubic(8)
