@@ -1622,11 +1622,33 @@ extern "C" int ether_record_series(ether_ctx *h, int32_t nsweeps, int32_t stride
     }
     int rc = ETHER_OK;
     int t = 0;
-    for (int k = 1; k <= nsweeps && rc == ETHER_OK; ++k) {
-        rc = sweep_once(c);
-        if (rc == ETHER_OK && k % stride == 0 && t < nrec) {
-            cudaError_t e = launch_record(c, t++, E != nullptr, mser, eser);
-            if (e != cudaSuccess) rc = fail(ETHER_ERR_CUDA, std::string("record: ") + cudaGetErrorString(e));
+    int32_t *t_dev = nullptr;
+    cudaGraphExec_t ex = nullptr;
+    if (nrec >= 4 && !(c.flags & ETHER_FLAG_NO_GRAPHS) && cudaMalloc(&t_dev, sizeof(int32_t)) == cudaSuccess) {
+        // one stride -- stride sweeps and the record of row *t_dev -- captured once, replayed
+        // for every row
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaMemsetAsync(t_dev, 0, sizeof(int32_t), c.stream);
+        if (e == cudaSuccess) e = cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            for (int k = 0; k < stride && rc == ETHER_OK; ++k) rc = sweep_once(c);
+            if (rc == ETHER_OK) e = launch_record(c, 0, E != nullptr, mser, eser, t_dev);
+            const cudaError_t ee = cudaStreamEndCapture(c.stream, &g);
+            if (e == cudaSuccess) e = ee;
+        }
+        if (rc == ETHER_OK && e == cudaSuccess) e = cudaGraphInstantiate(&ex, g, 0);
+        if (g) cudaGraphDestroy(g);
+        for (int i = 0; i < nrec && rc == ETHER_OK && e == cudaSuccess; ++i) e = cudaGraphLaunch(ex, c.stream);
+        if (rc == ETHER_OK && e != cudaSuccess) rc = fail(ETHER_ERR_CUDA, std::string("series graph: ") + cudaGetErrorString(e));
+        // the sweeps after the last recorded row
+        for (int k = nrec * stride + 1; k <= nsweeps && rc == ETHER_OK; ++k) rc = sweep_once(c);
+    } else {
+        for (int k = 1; k <= nsweeps && rc == ETHER_OK; ++k) {
+            rc = sweep_once(c);
+            if (rc == ETHER_OK && k % stride == 0 && t < nrec) {
+                cudaError_t e = launch_record(c, t++, E != nullptr, mser, eser);
+                if (e != cudaSuccess) rc = fail(ETHER_ERR_CUDA, std::string("record: ") + cudaGetErrorString(e));
+            }
         }
     }
     if (rc == ETHER_OK) {
@@ -1635,6 +1657,8 @@ extern "C" int ether_record_series(ether_ctx *h, int32_t nsweeps, int32_t stride
         if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
         if (e != cudaSuccess) rc = fail(ETHER_ERR_CUDA, std::string("series copy: ") + cudaGetErrorString(e));
     }
+    if (ex) cudaGraphExecDestroy(ex);
+    if (t_dev) cudaFree(t_dev);
     cudaFree(mser);
     if (eser) cudaFree(eser);
     return rc;

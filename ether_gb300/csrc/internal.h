@@ -239,7 +239,9 @@ cudaError_t launch_accept_ratio(Ctx &c, double *out);
 cudaError_t launch_broadcast(Ctx &c, void *base, size_t bytes_per_replica);
 cudaError_t launch_energy_mag(Ctx &c, bool want_energy);
 cudaError_t launch_measure(Ctx &c);
-cudaError_t launch_record(Ctx &c, int t, bool want_e, double *mser, double *eser);
+// Row t of the |M| (and E) series; with t_dev the row is read from device memory and
+// advanced afterwards (for captured graphs).
+cudaError_t launch_record(Ctx &c, int t, bool want_e, double *mser, double *eser, int32_t *t_dev = nullptr);
 cudaError_t launch_pt(Ctx &c, int set_swap_count);
 cudaError_t launch_acc_bin(Ctx &c);
 cudaError_t launch_spiral_measure(Ctx &c);

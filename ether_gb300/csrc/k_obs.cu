@@ -490,9 +490,10 @@ __global__ void __launch_bounds__(kRedBs) mag_kernel(const ObsMember a) {
 __global__ void record_kernel(const double *__restrict__ partials, int nblk, int R,
                               int from_partials, double *__restrict__ M,
                               const double *__restrict__ E, double *__restrict__ mser,
-                              double *__restrict__ eser, int t) {
+                              double *__restrict__ eser, int t_arg, const int32_t *__restrict__ t_dev) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= R) return;
+    const int t = t_dev ? *t_dev : t_arg;  // t_dev: the row from device memory (graph replays)
     double m[3];
     if (from_partials) {
         m[0] = m[1] = m[2] = 0.0;
@@ -506,19 +507,28 @@ __global__ void record_kernel(const double *__restrict__ partials, int nblk, int
     if (eser) eser[(size_t)t * R + r] = E[r];
 }
 
-cudaError_t launch_record(Ctx &c, int t, bool want_e, double *mser, double *eser) {
+// The next row of a series whose row index lives in device memory.
+__global__ void record_bump_kernel(int32_t *__restrict__ t_dev) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *t_dev += 1;
+}
+
+cudaError_t launch_record(Ctx &c, int t, bool want_e, double *mser, double *eser, int32_t *t_dev) {
     if (want_e) {
         cudaError_t e = launch_energy_mag(c, true);
         if (e != cudaSuccess) return e;
         record_kernel<<<(c.R + 127) / 128, 128, 0, c.stream>>>(c.partials, c.partial_blocks, c.R, 0,
-                                                                c.M, c.E, mser, eser, t);
+                                                                c.M, c.E, mser, eser, t, t_dev);
         c.launches++;
     } else {
         dim3 grid(c.partial_blocks, c.R);
         mag_kernel<<<grid, kRedBs, 0, c.stream>>>(obs_member(c));
         record_kernel<<<(c.R + 127) / 128, 128, 0, c.stream>>>(c.partials, c.partial_blocks, c.R, 1,
-                                                                c.M, c.E, mser, nullptr, t);
+                                                                c.M, c.E, mser, nullptr, t, t_dev);
         c.launches += 2;
+    }
+    if (t_dev) {
+        record_bump_kernel<<<1, 32, 0, c.stream>>>(t_dev);
+        c.launches++;
     }
     return cudaGetLastError();
 }
