@@ -228,11 +228,19 @@ def run_sweeps(model, L, replicas, steps, warmup, rank, world, force_variant=0, 
         sw.get_spins_batch(ions)
         t_end = time.perf_counter()
         t_e2e = t_end - t_start
-        esize = 1 if model == eg.MODEL_ISING else 16
+        # bytes that cross the link per site: the spin fields of the records where a kernel
+        # moves them in place (ion(3) as FP64; ion(1:3), ion(5)), else the device layout
+        direct = sw.info().ion_direct
+        if direct:
+            esize = 8 if model == eg.MODEL_ISING else 32
+        else:
+            esize = 1 if model == eg.MODEL_ISING else 16
         res.update({"e2e": updates / (t_e2e * 1e9) * world,
                     "h2d": (R * N * esize) / steps,   # every replica, once per timed run
                     "d2h": 8.0 * R + (R * N * esize) / steps,
-                    "e2e_detail": {"steps": steps, "set_spins_batch_s": t_set - t_start,
+                    "e2e_detail": {"steps": steps, "records": "moved in place by a kernel" if direct else
+                                   "converted on the host's cores through pinned staging",
+                                   "set_spins_batch_s": t_set - t_start,
                                    "sweeps_s": t_run - t_set, "get_spins_batch_s": t_end - t_run,
                                    "host_ion_bytes": R * N * 72},
                     "accept_mean": float(np.mean(acc))})

@@ -23,6 +23,7 @@ FLAG_PT_TRUE_ENERGY = 1 << 1
 FLAG_PT_REFERENCE_COPY = 1 << 2
 FLAG_NO_GRAPHS = 1 << 3
 FLAG_NO_RESIDENT = 1 << 4
+FLAG_STAGED_SPINS = 1 << 5
 RUN_PARSE_ONLY = 1 << 0
 RUN_QUIET = 1 << 1
 RUN_RESUME = 1 << 2
@@ -61,7 +62,7 @@ class Info(C.Structure):
         ("n_colours", C.c_int32), ("fast_path", C.c_int32), ("n_types", C.c_int32),
         ("table_entries", C.c_int32), ("n_slots", C.c_int32), ("n_groups", C.c_int32),
         ("device_bytes", C.c_size_t), ("kernel_launches", C.c_uint64),
-        ("sq_kernel_ms", C.c_float),
+        ("sq_kernel_ms", C.c_float), ("ion_direct", C.c_int32),
     ]
 
 

@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libether_gpu.so")
 BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU = ["ether_api.cu", "k_ising.cu", "k_xyz.cu", "k_obs.cu", "noalloc.cu", "k_sq.cu", "k_batch.cu", "k_learn.cu", "k_learn_xyz.cu", "k_moments.cu"]
+CU = ["ether_api.cu", "k_ising.cu", "k_xyz.cu", "k_obs.cu", "noalloc.cu", "k_sq.cu", "k_batch.cu", "k_learn.cu", "k_learn_xyz.cu", "k_moments.cu", "k_ion.cu"]
 CXX = ["lattice.cpp", "deck.cpp"]
 
 

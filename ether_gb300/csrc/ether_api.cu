@@ -197,7 +197,7 @@ void free_ctx(Ctx &c) {
                     c.step, c.ovrr_step, c.fresh_call, c.acc_count, c.E, c.M, c.sums,
                     c.partials, c.pt_accepts, c.swap_dev, c.copy_from, c.err, c.spiral_ptr,
                     c.spiral_nbr, c.acc_before, c.acc_ratio, c.spiral_part, c.spiral_sums,
-                    c.acc_slot, c.acc_mark, c.t.sia_cls, c.t.sia_ax, c.t.mweight_f};
+                    c.acc_slot, c.acc_mark, c.t.sia_cls, c.t.sia_ax, c.t.mweight_f, c.t.storage};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c.acc_host) cudaFreeHost(c.acc_host);
@@ -465,6 +465,8 @@ extern "C" int ether_create(const ether_desc *d, ether_ctx **out) {
     TRY(dev_upload(c, &c.t.mweight, mw));
     if (mw_f32) TRY(dev_upload(c, &c.t.mweight_f, mwf));
     TRY(dev_upload(c, &c.t.site_of_storage, c.site_of_storage));
+    TRY(dev_upload(c, &c.t.storage, c.storage));
+    c.ion_direct = !(c.flags & ETHER_FLAG_STAGED_SPINS) && ion_direct_possible(dev);
     {
         // ELL blocks per colour class: coalesced neighbour reads for the general-lattice
         // kernels (XYZ: coupling index per entry; Ising: threshold-table stride per entry)
@@ -758,6 +760,14 @@ void device_layout_to_ion(const Ctx &c, const void *src, double *ion) {
 }  // namespace
 
 static int spins_batch(Ctx &c, int32_t r0, int32_t n, double *ion, bool to_device) {
+    if (c.ion_direct) {
+        cudaError_t e = launch_ion_copy(c, r0, n, ion, to_device);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+        if (e != cudaSuccess)
+            return fail(ETHER_ERR_CUDA, std::string(to_device ? "ether_set_spins_batch: " : "ether_get_spins_batch: ") +
+                                            cudaGetErrorString(e));
+        return ETHER_OK;
+    }
     const size_t per_rep = c.model == ETHER_MODEL_ISING ? (size_t)c.N : sizeof(float4) * c.N;
     const size_t ion_rep = (size_t)9 * c.N;
     uint8_t *dev = c.model == ETHER_MODEL_ISING ? c.spins : reinterpret_cast<uint8_t *>(c.spins4);
@@ -1348,6 +1358,7 @@ extern "C" int ether_get_info(ether_ctx *h, ether_info *info) {
     info->device_bytes = c.device_bytes;
     info->kernel_launches = c.launches;
     info->sq_kernel_ms = c.sq_ms;
+    info->ion_direct = c.ion_direct ? 1 : 0;
     return ETHER_OK;
 }
 

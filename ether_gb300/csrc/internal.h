@@ -61,6 +61,7 @@ struct DevTables {
     double *mweight = nullptr;    // N: stgg * s(species)
     float *mweight_f = nullptr;   // N: the same in FP32 when every weight is exact in FP32
     int32_t *site_of_storage = nullptr;  // N: 0-based site number of a storage index
+    int32_t *storage = nullptr;          // N: storage index of a 0-based site number
     // neighbour lists per colour class in ELL form: entry k of rank rho of colour c at
     // ell_off[c] + k * n_c + rho (same order as the CSR), padded to the class's widest site
     int32_t *ell_nbr = nullptr;   // storage indices
@@ -128,6 +129,7 @@ struct Ctx {
     double *acc_ratio = nullptr;               // R: device acceptance ratios of a call
     double *acc_host = nullptr;                // R: pinned host copy
     void *stage = nullptr;                     // pinned staging of ether_{set,get}_spins_batch
+    bool ion_direct = false;                   // the device reads / writes the host records in place
     size_t stage_bytes = 0;
     int32_t *spiral_ptr = nullptr, *spiral_nbr = nullptr;  // spiral partners, CSR in storage order
     long spiral_count = 0;
@@ -237,6 +239,10 @@ cudaError_t launch_fresh(Ctx &c);
 cudaError_t launch_advance(Ctx &c, uint32_t *counter);
 cudaError_t launch_accept_ratio(Ctx &c, double *out);
 cudaError_t launch_broadcast(Ctx &c, void *base, size_t bytes_per_replica);
+// k_ion.cu: whether device dev addresses pageable host memory through the host's page tables;
+// replicas r0 .. r0+n-1 from (to_device) or into the ion(0:8, N, n) records at ion, on c.stream
+bool ion_direct_possible(int dev);
+cudaError_t launch_ion_copy(Ctx &c, int r0, int n, double *ion, bool to_device);
 cudaError_t launch_energy_mag(Ctx &c, bool want_energy);
 cudaError_t launch_measure(Ctx &c);
 // Row t of the |M| (and E) series; with t_dev the row is read from device memory and

@@ -21,6 +21,7 @@ module ether_gpu_mod
     integer(c_int), parameter :: ETHER_FLAG_PT_TRUE_ENERGY = 2
     integer(c_int), parameter :: ETHER_FLAG_PT_REFERENCE_COPY = 4
     integer(c_int), parameter :: ETHER_FLAG_NO_GRAPHS = 8, ETHER_FLAG_NO_RESIDENT = 16
+    integer(c_int), parameter :: ETHER_FLAG_STAGED_SPINS = 32
 
     type, bind(C) :: ether_desc
         integer(c_int32_t) :: n_sites, n_species, n_shells, nbd_capacity, model, angle

@@ -61,9 +61,13 @@ enum {
                                           instead of exchanging the two                     */
     ETHER_FLAG_NO_GRAPHS = 1 << 3,        /* ether_mcs launches kernels one by one instead of
                                           replaying captured CUDA graphs                    */
-    ETHER_FLAG_NO_RESIDENT = 1 << 4       /* ether_mcs never runs a small simple-cubic Ising
+    ETHER_FLAG_NO_RESIDENT = 1 << 4,      /* ether_mcs never runs a small simple-cubic Ising
                                           lattice's sweeps in the shared-memory resident
                                           kernel (same results, one launch per phase)        */
+    ETHER_FLAG_STAGED_SPINS = 1 << 5      /* ether_{set,get}_spins_batch convert on the host's
+                                          cores through pinned staging even where the device
+                                          could read and write the ion records in place
+                                          (same results)                                     */
 };
 
 typedef struct ether_ctx ether_ctx;
@@ -130,9 +134,13 @@ int ether_set_spins(ether_ctx *ctx, int32_t replica, const double *ion);
 int ether_get_spins(ether_ctx *ctx, int32_t replica, double *ion);
 /* The same for replicas r0 .. r0+n-1 at once: ion(0:8, N, n), one reference ion array per
  * replica back to back (what a driver holds when the replica batch replaces the MPI ranks
- * of src/ether.f90:112-118, each of which owned one ion).  The layout conversion runs on
- * the host's cores into pinned staging memory (up to 512 MB, allocated on the first call
- * and kept by the context), overlapped with the copies.  Returns when the data is in place. */
+ * of src/ether.f90:112-118, each of which owned one ion).  Where the device addresses
+ * pageable host memory through the host's page tables (ether_info.ion_direct: a Grace CPU's
+ * memory over NVLink-C2C), a kernel reads and writes the records' spin fields in place (an
+ * XYZ set reads whole records in tiles; only the spin fields are written);
+ * otherwise the layout conversion runs on the host's cores into pinned staging memory (up to
+ * 512 MB, allocated on the first call and kept by the context), overlapped with the copies.
+ * Returns when the data is in place; ion must stay valid for the call. */
 int ether_set_spins_batch(ether_ctx *ctx, int32_t r0, int32_t n, const double *ion);
 int ether_get_spins_batch(ether_ctx *ctx, int32_t r0, int32_t n, double *ion);
 
@@ -222,6 +230,8 @@ typedef struct ether_info {
     size_t device_bytes;     /* device memory owned by the context                         */
     uint64_t kernel_launches;/* kernels launched by this context so far                    */
     float sq_kernel_ms;      /* CUDA-event time of the last ether_structure_factor's kernels */
+    int32_t ion_direct;      /* 1 when ether_{set,get}_spins_batch move the records by a kernel
+                                in place (takes the struct's former tail padding)              */
 } ether_info;
 int ether_get_info(ether_ctx *ctx, ether_info *info);
 /* colour(N) and rank_in_colour(N) of the Checkerboard order. */

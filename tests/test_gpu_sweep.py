@@ -346,14 +346,21 @@ def test_single_sweep_with_acceptance_graph_equals_direct_launches(model):
     np.testing.assert_array_equal(runs[0][1], runs[1][1])
 
 
+@pytest.mark.parametrize("staged", [False, True])
 @pytest.mark.parametrize("model,L,R", [(eg.MODEL_ISING, (64, 32, 32), 70), (eg.MODEL_XYZ, (32, 16, 20), 60)])
-def test_spins_batch_equals_per_replica_calls(model, L, R):
+def test_spins_batch_equals_per_replica_calls(model, L, R, staged):
     """ether_set_spins_batch / ether_get_spins_batch move ion(0:8, N, n) of many replicas at
-    once (the conversion in chunks of whole replicas on several host threads): the same device
-    state and the same ion records as one ether_set_spins / ether_get_spins per replica.
-    The sizes give two (Ising) and three (XYZ) chunks, the last one partial."""
+    once: the same device state and the same ion records as one ether_set_spins /
+    ether_get_spins per replica, both where a kernel reads and writes the records in place
+    (a device that addresses pageable host memory) and with the conversion in chunks of whole
+    replicas on several host threads (ETHER_FLAG_STAGED_SPINS).  The sizes give two (Ising)
+    and three (XYZ) staging chunks, the last one partial."""
     lat = eg.simple_cubic(L)
-    sw, _ = make_pair(lat, model, FM, replicas=R)
+    sw, _ = make_pair(lat, model, FM, replicas=R, flags=eg.FLAG_STAGED_SPINS if staged else 0)
+    direct = sw.info().ion_direct
+    print("ion records moved %s" % ("in place by a kernel" if direct else "through host staging"))
+    if staged:
+        assert direct == 0
     sw.set_beta(beta_of(4.511 if model == eg.MODEL_ISING else 1.443))
     mk = random_ising if model == eg.MODEL_ISING else random_xyz
     ions = np.stack([mk(lat, 500 + r) for r in range(R)])
