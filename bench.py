@@ -229,15 +229,21 @@ def run_sweeps(model, L, replicas, steps, warmup, rank, world, force_variant=0, 
         t_end = time.perf_counter()
         t_e2e = t_end - t_start
         # bytes that cross the link per site: the spin fields of the records where a kernel
-        # moves them in place (ion(3) as FP64; ion(1:3), ion(5)), else the device layout
+        # moves them in place (ion(3) as FP64; ion(1:3), ion(5)), else the device layout; an
+        # in-place upload of 8 or more replicas leaves 3/8 of them to the host's cores (the
+        # library's split when the host has 8 or more threads)
         direct = sw.info().ion_direct
+        dsize = 1 if model == eg.MODEL_ISING else 16
+        fsize = 8 if model == eg.MODEL_ISING else 32
         if direct:
-            esize = 8 if model == eg.MODEL_ISING else 32
+            staged = R * 3 // 8 if R >= 8 and (os.cpu_count() or 1) >= 8 else 0
+            up = (R - staged) * N * fsize + staged * N * dsize
+            down = R * N * fsize
         else:
-            esize = 1 if model == eg.MODEL_ISING else 16
+            up = down = R * N * dsize
         res.update({"e2e": updates / (t_e2e * 1e9) * world,
-                    "h2d": (R * N * esize) / steps,   # every replica, once per timed run
-                    "d2h": 8.0 * R + (R * N * esize) / steps,
+                    "h2d": up / steps,   # every replica, once per timed run
+                    "d2h": 8.0 * R + down / steps,
                     "e2e_detail": {"steps": steps, "records": "moved in place by a kernel" if direct else
                                    "converted on the host's cores through pinned staging",
                                    "set_spins_batch_s": t_set - t_start,
