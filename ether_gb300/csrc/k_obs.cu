@@ -85,13 +85,73 @@ __device__ __forceinline__ double warp_sum_d(double v) {
     return v;
 }
 
+// How a block's per-thread sums are kept until the block total: integer counts (Ising
+// counting form), double-single pairs for all kNq (or only the two energies) quantities, or
+// FP64.  Integers and pairs are summed over the warp and then over the block's warps, and
+// turned into FP64 once per block: the FP64 pipe, 1/64 of the FP32 rate, then carries one
+// conversion per block instead of one per warp.
+enum { kFormDouble = 0, kFormCount = 1, kFormDS = 2, kFormDSEnergy = 3 };
+
+// Block totals of three per-warp integer sums (lane 0 of each warp holds its warp's) into
+// t[0..2] of thread 0 (the whole block calls it).
+__device__ __forceinline__ void block_sum_ints(const int (&ci)[3], int (&t)[3]) {
+    __shared__ int si[kRedBs / 32][3];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0)
+        for (int j = 0; j < 3; ++j) si[wid][j] = ci[j];
+    __syncthreads();
+    t[0] = t[1] = t[2] = 0;
+    if (threadIdx.x == 0)
+        for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2)
+            for (int j = 0; j < 3; ++j) t[j] += si[w2][j];
+}
+
+// Block totals of Q quantities into out[0..Q-1] (thread j writes quantity j; the whole block
+// calls it): quantities j < nds come as per-warp double-single sums in qd (lane 0 holds the
+// warp's), the others as per-thread FP64 values in q, summed over the warp here.
+template <int Q>
+__device__ __forceinline__ void block_sum_mixed(const double (&q)[Q], const DS (&qd)[Q], int nds,
+                                                double *__restrict__ out) {
+    __shared__ float2 sd[kRedBs / 32][Q];
+    __shared__ double sm[kRedBs / 32][Q];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < Q; ++j) {
+        if (j < nds) {
+            if (lane == 0) sd[wid][j] = make_float2(qd[j].hi, qd[j].lo);
+        } else {
+            const double v = warp_sum_d(q[j]);
+            if (lane == 0) sm[wid][j] = v;
+        }
+    }
+    __syncthreads();
+    const int j = threadIdx.x;
+    if (j < Q) {
+        const int nw = (int)(blockDim.x >> 5);
+        if (j < nds) {
+            DS acc;
+            for (int w2 = 0; w2 < nw; ++w2) {
+                ds_add(acc, sd[w2][j].x);
+                acc.lo += sd[w2][j].y;
+            }
+            out[j] = ds_value(acc);
+        } else {
+            double v = 0.0;
+            for (int w2 = 0; w2 < nw; ++w2) v += sm[w2][j];
+            out[j] = v;
+        }
+    }
+}
+
 // Partial sums of block b (of a.nblk) of replica r into a.partials[(r * nblk + b) * kNq ..]:
 // the whole block calls it.
 __device__ __forceinline__ void energy_block(const ObsMember &a, int r, int b) {
     const int N = a.N;
     const int stride = a.nblk * blockDim.x;
     double q[kNq] = {0, 0, 0, 0, 0};
-    bool warp_done = false;  // q already holds the warp's sums (lane 0)
+    int ci[3] = {0, 0, 0};
+    DS qd[kNq];
+    int form = kFormDouble;
     if (a.model == 0 && a.count_form) {
         // E_ex = J sum s_i s_j, the field term z sum s_i, M = |w| sum sign(w_i) s_i
         const uint8_t *sp = a.spins + (size_t)r * N;
@@ -109,14 +169,11 @@ __device__ __forceinline__ void energy_block(const ObsMember &a, int r, int b) {
             const bool wneg = a.mw_pos ? false : __double_as_longlong(a.mweight[s]) < 0;
             cm += ((own != 0) != wneg) ? 1 : -1;
         }
-        // counts summed over the warp in integers, turned into FP64 once per warp
-        cb = __reduce_add_sync(0xffffffffu, cb);
-        cz = __reduce_add_sync(0xffffffffu, cz);
-        cm = __reduce_add_sync(0xffffffffu, cm);
-        q[1] = a.juni * (double)cb;
-        q[0] = a.zeeman ? q[1] + a.zeed[2] * (double)cz : q[1];
-        q[4] = a.mw_abs * (double)cm;
-        warp_done = true;
+        // counts summed over the warp and the block in integers, FP64 once per block
+        ci[0] = __reduce_add_sync(0xffffffffu, cb);
+        ci[1] = __reduce_add_sync(0xffffffffu, cz);
+        ci[2] = __reduce_add_sync(0xffffffffu, cm);
+        form = kFormCount;
     } else if (a.model == 0) {
         const uint8_t *sp = a.spins + (size_t)r * N;
         for (int s = b * blockDim.x + threadIdx.x; s < N; s += stride) {
@@ -133,6 +190,8 @@ __device__ __forceinline__ void energy_block(const ObsMember &a, int r, int b) {
         const float4 *sp = a.spins4 + (size_t)r * N;
         DS e0, e1, m0, m1, m2;
         const bool mwf = a.mweight_f != nullptr;
+        // no Zeeman or anisotropy term: e0 would add the same values as e1
+        const bool fields = a.zeeman || a.sia || a.sia_cls;
         const int H = a.sc_L1 >> 1, half = N >> 1;
         for (int s = b * blockDim.x + threadIdx.x; s < N; s += stride) {
             const float4 S = sp[s];
@@ -163,29 +222,31 @@ __device__ __forceinline__ void energy_block(const ObsMember &a, int r, int b) {
             e = fmaf(S.y, hy, e);
             e = fmaf(S.z, hz, e);
             ds_add(e1, e);
-            if (a.zeeman || a.sia) {
-                const int si = a.species[s] - 1;
-                if (a.zeeman) {
-                    const float *z = a.zee + 3 * si;
-                    e = fmaf(S.x, z[0], e);
-                    e = fmaf(S.y, z[1], e);
-                    e = fmaf(S.z, z[2], e);
+            if (fields) {
+                if (a.zeeman || a.sia) {
+                    const int si = a.species[s] - 1;
+                    if (a.zeeman) {
+                        const float *z = a.zee + 3 * si;
+                        e = fmaf(S.x, z[0], e);
+                        e = fmaf(S.y, z[1], e);
+                        e = fmaf(S.z, z[2], e);
+                    }
+                    if (a.sia) {
+                        const float *d = a.D + 3 * si;
+                        e = fmaf(d[0], S.x * S.x, e);
+                        e = fmaf(d[1], S.y * S.y, e);
+                        e = fmaf(d[2], S.z * S.z, e);
+                    }
                 }
-                if (a.sia) {
-                    const float *d = a.D + 3 * si;
-                    e = fmaf(d[0], S.x * S.x, e);
-                    e = fmaf(d[1], S.y * S.y, e);
-                    e = fmaf(d[2], S.z * S.z, e);
+                if (a.sia_cls) {  // local-axis anisotropy D (a . S)^2
+                    const float4 ax = a.sia_ax[a.sia_cls[s]];
+                    float ps = ax.x * S.x;
+                    ps = fmaf(ax.y, S.y, ps);
+                    ps = fmaf(ax.z, S.z, ps);
+                    e = fmaf(ax.w, ps * ps, e);
                 }
+                ds_add(e0, e);
             }
-            if (a.sia_cls) {  // local-axis anisotropy D (a . S)^2
-                const float4 ax = a.sia_ax[a.sia_cls[s]];
-                float ps = ax.x * S.x;
-                ps = fmaf(ax.y, S.y, ps);
-                ps = fmaf(ax.z, S.z, ps);
-                e = fmaf(ax.w, ps * ps, e);
-            }
-            ds_add(e0, e);
             if (mwf) {
                 const float wf = a.mw_pos ? a.mw_abs_f : a.mweight_f[s];  // mw_pos: all weights +mw_abs
                 ds_add_prod(m0, wf, S.x);
@@ -198,31 +259,30 @@ __device__ __forceinline__ void energy_block(const ObsMember &a, int r, int b) {
                 q[4] += w * (double)S.z;
             }
         }
-        // double-single sums over the warp, turned into FP64 once per warp
-        q[0] = ds_value(warp_sum_ds(e0));
-        q[1] = ds_value(warp_sum_ds(e1));
+        // double-single sums over the warp and the block, FP64 once per block
+        qd[1] = warp_sum_ds(e1);
+        qd[0] = fields ? warp_sum_ds(e0) : qd[1];
         if (mwf) {
-            q[2] = ds_value(warp_sum_ds(m0));
-            q[3] = ds_value(warp_sum_ds(m1));
-            q[4] = ds_value(warp_sum_ds(m2));
-            warp_done = true;
-        } else {
-            for (int j = 2; j < kNq; ++j) q[j] = warp_sum_d(q[j]);
-            warp_done = true;
+            qd[2] = warp_sum_ds(m0);
+            qd[3] = warp_sum_ds(m1);
+            qd[4] = warp_sum_ds(m2);
         }
+        form = mwf ? kFormDS : kFormDSEnergy;
     }
-    __shared__ double sm[kRedBs / 32][kNq];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int j = 0; j < kNq; ++j) {
-        const double v = warp_done ? q[j] : warp_sum_d(q[j]);
-        if (lane == 0) sm[wid][j] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x < kNq) {
-        double v = 0.0;
-        for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2) v += sm[w2][threadIdx.x];
-        a.partials[((size_t)r * a.nblk + b) * kNq + threadIdx.x] = v;
+    double *out = a.partials + ((size_t)r * a.nblk + b) * kNq;
+    if (form == kFormCount) {
+        int t[3];
+        block_sum_ints(ci, t);
+        if (threadIdx.x == 0) {
+            const double e_ex = a.juni * (double)t[0];
+            out[0] = a.zeeman ? e_ex + a.zeed[2] * (double)t[1] : e_ex;
+            out[1] = e_ex;
+            out[2] = 0.0;
+            out[3] = 0.0;
+            out[4] = a.mw_abs * (double)t[2];
+        }
+    } else {
+        block_sum_mixed<kNq>(q, qd, form == kFormDS ? kNq : form == kFormDSEnergy ? 2 : 0, out);
     }
 }
 
@@ -345,8 +405,13 @@ __global__ void pt_copy_kernel(uint8_t *__restrict__ spins, float4 *__restrict__
     }
 }
 
+// Blocks per replica of the reductions: no more than four blocks per SM over all replicas
+// (the context's own launch fills the GPU once, each thread running through many sites), and
+// at least eight sites per thread, so that the per-warp and per-block sums stay a small part
+// of a thread's work also for the many small contexts of a batch.  The same number serves the
+// context's own launches and the batched ones, so the two sum in the same order.
 int energy_blocks(const Ctx &c) {
-    long need = (c.N + kRedBs - 1) / kRedBs;
+    long need = (c.N + kRedBs * 8 - 1) / (kRedBs * 8);
     long cap = (long)c.sm_count * 4 / (c.R > 0 ? c.R : 1);
     if (cap < 1) cap = 1;
     if (need > cap) need = cap;
@@ -431,7 +496,9 @@ __global__ void __launch_bounds__(kRedBs) mag_kernel(const ObsMember a) {
     const int N = a.N;
     const int stride = gridDim.x * blockDim.x;
     double q[3] = {0, 0, 0};
-    bool warp_done = false;  // q already holds the warp's sums (lane 0)
+    DS qd[3];
+    int form = kFormDouble;
+    double *out = a.partials + ((size_t)r * gridDim.x + blockIdx.x) * kNq + 2;
     if (a.model == 0 && a.count_form) {
         const uint8_t *sp = a.spins + (size_t)r * N;
         int cm = 0;
@@ -439,8 +506,15 @@ __global__ void __launch_bounds__(kRedBs) mag_kernel(const ObsMember a) {
             const bool wneg = a.mw_pos ? false : __double_as_longlong(a.mweight[s]) < 0;
             cm += ((sp[s] != 0) != wneg) ? 1 : -1;
         }
-        q[2] = a.mw_abs * (double)__reduce_add_sync(0xffffffffu, cm);
-        warp_done = true;
+        const int ci[3] = {0, 0, __reduce_add_sync(0xffffffffu, cm)};
+        int t[3];
+        block_sum_ints(ci, t);
+        if (threadIdx.x == 0) {
+            out[0] = 0.0;
+            out[1] = 0.0;
+            out[2] = a.mw_abs * (double)t[2];
+        }
+        return;
     } else if (a.model == 0) {
         const uint8_t *sp = a.spins + (size_t)r * N;
         for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += stride)
@@ -455,10 +529,10 @@ __global__ void __launch_bounds__(kRedBs) mag_kernel(const ObsMember a) {
             ds_add_prod(m1, wf, S.y);
             ds_add_prod(m2, wf, S.z);
         }
-        q[0] = ds_value(warp_sum_ds(m0));
-        q[1] = ds_value(warp_sum_ds(m1));
-        q[2] = ds_value(warp_sum_ds(m2));
-        warp_done = true;
+        qd[0] = warp_sum_ds(m0);
+        qd[1] = warp_sum_ds(m1);
+        qd[2] = warp_sum_ds(m2);
+        form = kFormDS;
     } else {
         const float4 *sp = a.spins4 + (size_t)r * N;
         for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += stride) {
@@ -469,19 +543,7 @@ __global__ void __launch_bounds__(kRedBs) mag_kernel(const ObsMember a) {
             q[2] += w * (double)S.z;
         }
     }
-    __shared__ double sm[kRedBs / 32][3];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-        const double v = warp_done ? q[j] : warp_sum_d(q[j]);
-        if (lane == 0) sm[wid][j] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x < 3) {
-        double v = 0.0;
-        for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2) v += sm[w2][threadIdx.x];
-        a.partials[((size_t)r * gridDim.x + blockIdx.x) * kNq + 2 + threadIdx.x] = v;
-    }
+    block_sum_mixed<3>(q, qd, form == kFormDS ? 3 : 0, out);
 }
 
 // One row t of the time series: |M| (and E) of every replica.  from_partials: M is summed
@@ -623,8 +685,16 @@ __device__ __forceinline__ int member_of(const int32_t *__restrict__ off, int M,
 // kernel waits on neighbour gathers, so more warps hide more of it).
 __global__ void __launch_bounds__(kRedBs, 4)
 batch_energy_kernel(const ObsMember *__restrict__ mem, const int32_t *__restrict__ eoff, int M) {
+    // the member's record in shared memory: its fields are read in every site's iteration
+    __shared__ ObsMember a;
     const int m = member_of(eoff, M, blockIdx.x);
-    const ObsMember &a = mem[m];
+    {
+        static_assert(sizeof(ObsMember) % 8 == 0, "ObsMember is copied in 8-byte words");
+        const unsigned long long *src = reinterpret_cast<const unsigned long long *>(mem + m);
+        unsigned long long *dst = reinterpret_cast<unsigned long long *>(&a);
+        for (int k = threadIdx.x; k < (int)(sizeof(ObsMember) / 8); k += blockDim.x) dst[k] = src[k];
+    }
+    __syncthreads();
     const int local = blockIdx.x - eoff[m];
     energy_block(a, local / a.nblk, local % a.nblk);
 }
