@@ -16,6 +16,9 @@
 #include <thread>
 #include <vector>
 
+#include <sys/mman.h>
+#include <unistd.h>
+
 #include "internal.h"
 
 using namespace ether;
@@ -761,6 +764,22 @@ void device_layout_to_ion(const Ctx &c, const void *src, double *ion) {
 
 static int spins_staged(Ctx &c, int32_t r0, int32_t n, double *ion, bool to_device);
 
+// Whether [p, p + bytes) is host memory mapped in this process, checked before a kernel reads
+// or writes it in place (a wrong pointer must not reach the device): device memory is refused
+// by the CUDA runtime's attributes, an unmapped page by msync (ENOMEM), which with MS_ASYNC
+// only checks the mappings.
+static bool host_range_mapped(const void *p, size_t bytes) {
+    cudaPointerAttributes pa{};
+    if (cudaPointerGetAttributes(&pa, p) != cudaSuccess) {
+        cudaGetLastError();  // an unknown pointer is not a lasting error
+    } else if (pa.type == cudaMemoryTypeDevice) {
+        return false;
+    }
+    const uintptr_t page = (uintptr_t)sysconf(_SC_PAGESIZE);
+    const uintptr_t a = (uintptr_t)p & ~(page - 1), b = (uintptr_t)p + bytes;
+    return msync(reinterpret_cast<void *>(a), (size_t)(b - a), MS_ASYNC) == 0;
+}
+
 // Where the device reads and writes host memory in place (c.ion_direct) a kernel moves the
 // records.  An upload of 8 or more replicas on a host with 8 or more threads is split: the
 // kernel reads the first 5/8 of the replicas while the host's cores convert the rest through
@@ -771,6 +790,9 @@ static int spins_staged(Ctx &c, int32_t r0, int32_t n, double *ion, bool to_devi
 // slower (111-133 against 100 ms).
 static int spins_batch(Ctx &c, int32_t r0, int32_t n, double *ion, bool to_device) {
     if (!c.ion_direct) return spins_staged(c, r0, n, ion, to_device);
+    if (!host_range_mapped(ion, sizeof(double) * 9 * (size_t)c.N * n))
+        return fail(ETHER_ERR_ARG, std::string(to_device ? "ether_set_spins_batch" : "ether_get_spins_batch") +
+                                       ": ion is not host memory mapped for n replicas' records");
     const int nk = to_device && n >= 8 && host_threads() >= 8 ? n - n * 3 / 8 : n;
     cudaError_t e = launch_ion_copy(c, r0, nk, ion, to_device);
     if (e == cudaSuccess && nk == n) e = cudaStreamSynchronize(c.stream);

@@ -140,7 +140,9 @@ int ether_get_spins(ether_ctx *ctx, int32_t replica, double *ion);
  * XYZ set reads whole records in tiles; only the spin fields are written);
  * otherwise the layout conversion runs on the host's cores into pinned staging memory (up to
  * 512 MB, allocated on the first call and kept by the context), overlapped with the copies.
- * Returns when the data is in place; ion must stay valid for the call. */
+ * Returns when the data is in place; ion must stay valid for the call.  On the in-place path
+ * ion must be host memory mapped for all n records (device memory or an unmapped page gives
+ * ETHER_ERR_ARG before any launch). */
 int ether_set_spins_batch(ether_ctx *ctx, int32_t r0, int32_t n, const double *ion);
 int ether_get_spins_batch(ether_ctx *ctx, int32_t r0, int32_t n, double *ion);
 

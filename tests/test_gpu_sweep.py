@@ -4,6 +4,8 @@ Ising: bit-exact spin trajectories (fixed-stream replay).  XYZ: the GPU's FP32 s
 the oracle's FP32 mirror bit for bit, and its observables stay within 1e-5 relative of the
 oracle's FP64 replay over the first 100 sweeps.
 """
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -385,6 +387,31 @@ def test_spins_batch_equals_per_replica_calls(model, L, R, staged):
     sw.get_spins_batch(back, r0=5)
     np.testing.assert_array_equal(back[:, :, cols], sub[:, :, cols].astype(np.float32).astype(np.float64))
     np.testing.assert_array_equal(sw.get_spins(lat.ion, 4)[:, cols], got[4][:, cols])
+    sw.close()
+
+
+def test_spins_batch_refuses_device_memory_before_any_launch():
+    """Where a kernel moves the records in place, a pointer to device memory is refused before
+    anything is launched (ETHER_ERR_ARG), in both directions, and the context keeps working."""
+    torch = pytest.importorskip("torch")
+    lat = eg.simple_cubic(8)
+    sw, _ = make_pair(lat, eg.MODEL_ISING, FM, replicas=2)
+    if not sw.info().ion_direct:
+        sw.close()
+        pytest.skip("the records are staged through the host on this system")
+    sw.set_beta(beta_of(4.5))
+    dev = torch.zeros(2 * lat.N * 9, dtype=torch.float64, device="cuda")
+    launches = sw.info().kernel_launches
+    for fn in (sw.lib.ether_set_spins_batch, sw.lib.ether_get_spins_batch):
+        rc = fn(sw.h, 0, 2, C.cast(C.c_void_p(dev.data_ptr()), C.POINTER(C.c_double)))
+        assert rc == -1  # ETHER_ERR_ARG
+        assert b"not host memory" in sw.lib.ether_last_error()
+    assert sw.info().kernel_launches == launches
+    ions = np.stack([random_ising(lat, 3)] * 2)
+    sw.set_spins_batch(ions)
+    back = np.stack([lat.ion] * 2).copy()
+    sw.get_spins_batch(back)
+    np.testing.assert_array_equal(back[:, :, 3], ions[:, :, 3])
     sw.close()
 
 
