@@ -143,11 +143,11 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_workload(model, L, replicas, seed=1992):
+def make_workload(model, L, replicas, seed=1992, flags=0):
     import ether_gb300 as eg
     lat = eg.simple_cubic(L)
     j = eg.couplings(1, [[(1, 1, (-J_MEV, -J_MEV, -J_MEV))]], [1.0])
-    sw = eg.Sweep.from_lattice(lat, j, np.array([1.0]), model, replicas=replicas, seed=seed)
+    sw = eg.Sweep.from_lattice(lat, j, np.array([1.0]), model, replicas=replicas, seed=seed, flags=flags)
     ktc = KTC_ISING if model == eg.MODEL_ISING else KTC_HEIS
     beta = 1.0 / (ktc * J_MEV * 1e-3)
     sw.set_beta(beta)
@@ -162,9 +162,9 @@ def make_workload(model, L, replicas, seed=1992):
 
 
 def run_sweeps(model, L, replicas, steps, warmup, rank, world, force_variant=0, clocks=True,
-               e2e=True):
+               e2e=True, flags=0):
     import ether_gb300 as eg
-    lat, j, sw, ion, beta = make_workload(model, L, replicas, seed=1992 + 7919 * rank)
+    lat, j, sw, ion, beta = make_workload(model, L, replicas, seed=1992 + 7919 * rank, flags=flags)
     sw.set_spins(ion)
     if force_variant:
         sw.set_variant(force_variant)
@@ -732,6 +732,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-components", action="store_true")
     ap.add_argument("--variant", type=int, default=0)
+    ap.add_argument("--staged-spins", action="store_true",
+                    help="e2e: the records converted on the host's cores through pinned staging "
+                         "(ETHER_FLAG_STAGED_SPINS) instead of moved in place by kernels")
     ap.add_argument("--learn-steps", type=int, default=0,
                     help="--model learned / learned-heisenberg: Adam steps (default 3000 / 4000)")
     ap.add_argument("--sq-cells", type=int, default=12)
@@ -909,7 +912,9 @@ def main():
                           "unit": "spin updates/ns", "higher_is_better": True, "detail": r}))
         return 0
 
-    res = run_sweeps(model, args.L, replicas, args.steps, args.warmup, rank, world, args.variant)
+    from ether_gb300.abi import FLAG_STAGED_SPINS
+    res = run_sweeps(model, args.L, replicas, args.steps, args.warmup, rank, world, args.variant,
+                     flags=FLAG_STAGED_SPINS if args.staged_spins else 0)
     if rank != 0:
         return 0
     traffic = None
