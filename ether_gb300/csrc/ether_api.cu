@@ -688,8 +688,9 @@ extern "C" int ether_get_spins(ether_ctx *h, int32_t replica, double *ion) {
 // the replica batch holds one ion array per replica: n of them back to back, ion(0:8, N, n).
 // The conversion to and from the device layout (a strided read or write of ion(3) or
 // ion(1:3,5) per 72-byte record, and the colour-major permutation) is the cost of this
-// boundary, so it runs on the host's cores into a pinned staging area, in chunks of whole
-// replicas whose copies start as soon as a chunk is converted.
+// boundary.  Where the device cannot read the records in place (spins_batch below), it runs on
+// the host's cores into a pinned staging area, in chunks of whole replicas whose copies start
+// as soon as a chunk is converted.
 namespace {
 constexpr size_t kStageMax = size_t(512) << 20;  // pinned staging, per context
 constexpr size_t kChunkBytes = size_t(4) << 20;  // a copy per ~4 MB of spins
@@ -796,9 +797,11 @@ static int spins_batch(Ctx &c, int32_t r0, int32_t n, double *ion, bool to_devic
     const int nk = to_device && n >= 8 && host_threads() >= 8 ? n - n * 3 / 8 : n;
     cudaError_t e = launch_ion_copy(c, r0, nk, ion, to_device);
     if (e == cudaSuccess && nk == n) e = cudaStreamSynchronize(c.stream);
-    if (e != cudaSuccess)
+    if (e != cudaSuccess) {
+        cudaStreamSynchronize(c.stream);  // launches before a failed one may still be reading ion
         return fail(ETHER_ERR_CUDA, std::string(to_device ? "ether_set_spins_batch: " : "ether_get_spins_batch: ") +
                                         cudaGetErrorString(e));
+    }
     if (nk == n) return ETHER_OK;
     // the staged part synchronises the stream (kernel included) before it returns; on an
     // early failure the kernel may still be reading the caller's records, so wait for it

@@ -9,10 +9,11 @@
 //
 // GB300 issues about 2 FP64 instructions per SM and clock against 128 FP32, so the running
 // sums avoid FP64 per site: Ising bond terms s_i s_j J are +-J exactly, so with one coupling,
-// one species and one |weight| a thread counts them in integers and the warp adds the
-// counts (else it adds +-J, one FP64 add per bond); XYZ sums are kept as FP32 double-single
-// pairs (Knuth's TwoSum, products split exactly with fmaf), about 48 significant bits,
-// summed over the warp the same way and turned into FP64 once per warp.
+// one species and one |weight| a thread counts them in integers and the warp and the block
+// add the counts (else it adds +-J, one FP64 add per bond); XYZ sums are kept as FP32
+// double-single pairs (Knuth's TwoSum, products split exactly with fmaf), about 48
+// significant bits, summed over the warp and the block the same way and turned into FP64 once
+// per block.
 #include "internal.h"
 #include "rng_math.cuh"
 #include "sweep_xyz.cuh"
