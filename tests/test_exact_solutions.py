@@ -1,0 +1,149 @@
+"""The Monte Carlo path against exact solutions.
+
+Ising: the nearest-neighbour ferromagnet on a finite square torus, whose partition function
+is Kaufman's closed form (tests/exact2d.py).
+
+CPU: the closed form equals the enumeration of all 2^(mn) states of small tori.
+GPU: a 16 x 16 torus (one site per cell, the third axis 8 lattice constants long, so each site
+has its four in-plane neighbours and nothing else; the general-lattice kernels) sampled by
+ether_mcs at kT = 2.0, 2.269 (near the infinite lattice's T_c) and 3.0 J, 64 independent
+chains per temperature, 20 000 measurements each after 2 000 equilibration steps.  The energy
+per site (src/get_eng.f90:36-40, E / 2N) and the heat capacity per site from its fluctuations
+agree with the exact values: each of the 6 differences, over the spread of the 64 chains'
+estimates, passes a two-sided z-test at 0.01 / 6 (Bonferroni, a family-wise 1%).
+
+Heisenberg (XYZ): the classical ferromagnetic ring of 64 unit spins (the other two axes 8
+lattice constants long: two neighbours per site).  Its transfer matrix gives the energy per
+site -J L(K) and the heat capacity per site 1 - K^2 / sinh^2 K (L the Langevin function,
+K = J / kT; M. E. Fisher, Am. J. Phys. 32, 343 (1964)), up to terms of relative order
+L(K)^64 (below 1e-17 here).  ether_mcs with Marsaglia proposals and an overrelaxation pass
+every step (src/ether.f90:163-172) at kT = 0.5, 1 and 2 J, the same rule as above.
+"""
+import numpy as np
+import pytest
+
+import ether_gb300 as eg
+from tests.helpers import beta_of, make_pair, random_ising, random_xyz
+
+FM = [[(1, 1, (-1.0, -1.0, -1.0))]]   # ETHER's sign: J < 0 is ferromagnetic, |J| = 1 meV
+
+# kT / J -> (energy per site / J, heat capacity per site / k_B) of the 16 x 16 torus, from the
+# closed form (test_exact_values_are_the_closed_forms checks them; the GPU test needs no mpmath)
+EXACT_16 = {2.0: (-1.7455306689909191, 0.7255087677365641),
+            2.269: (-1.4533425476693835, 1.4983111034990866),
+            3.0: (-0.8176893678695545, 0.4043325741653013)}
+
+
+def _exact2d():
+    pytest.importorskip("mpmath")
+    from tests import exact2d
+    return exact2d
+
+
+@pytest.mark.parametrize("m,n", [(4, 4), (2, 4), (3, 4), (4, 5)])
+def test_closed_form_equals_enumeration(m, n):
+    exact2d = _exact2d()
+    for K in (0.2, 0.4406867935, 0.6, 1.0):
+        assert abs(float(exact2d.ln_z(K, m, n) - exact2d.brute_force_ln_z(K, m, n))) < 1e-40
+
+
+def test_closed_form_approaches_onsager_at_tc():
+    """At K_c = ln(1 + sqrt 2) / 2: the energy per site of the L x L torus approaches the
+    infinite lattice's -sqrt(2) J as 1/L, and the heat capacity per site grows by Onsager's
+    (8 / pi) K_c^2 ln 2 each time L doubles (its logarithmic divergence)."""
+    exact2d = _exact2d()
+    Kc = float(np.log(1 + np.sqrt(2)) / 2)
+    res = {L: exact2d.energy_cv(Kc, L, L) for L in (16, 32, 64, 128)}
+    slope = [(res[L][0] + np.sqrt(2)) * L for L in (16, 32, 64, 128)]
+    assert max(slope) - min(slope) < 0.01 * abs(slope[-1])
+    step = 8 / np.pi * Kc * Kc * np.log(2)
+    for L in (16, 32, 64):
+        assert abs(res[2 * L][1] - res[L][1] - step) < 0.02 * step
+
+
+def test_exact_values_are_the_closed_forms():
+    exact2d = _exact2d()
+    for t, (e, cv) in EXACT_16.items():
+        assert np.allclose(exact2d.energy_cv(1.0 / t, 16, 16), (e, cv), rtol=1e-14, atol=0)
+
+
+def _square_torus(L):
+    return eg.Lattice([[0.0, 0.0, 0.0]], [1], np.diag([1.0, 1.0, 8.0]), (L, L, 1), [1.0])
+
+
+@pytest.mark.gpu
+def test_mcs_energy_and_heat_capacity_equal_the_exact_torus():
+    L, G = 16, 64
+    temps = (2.0, 2.269, 3.0)
+    lat = _square_torus(L)
+    sw, _ = make_pair(lat, eg.MODEL_ISING, FM, replicas=G * len(temps))
+    info = sw.info()
+    assert info.fast_path == 0 and info.n_colours == 2
+    sw.set_ladder([beta_of(t) for t in temps])
+    # every site has its four in-plane neighbours: the all-up state has E / 2N = -2 J
+    up = lat.ion.copy()
+    up[:, 3] = 1.0
+    sw.set_spins(up)
+    assert np.allclose(np.asarray(sw.tot_energy()) / (2 * lat.N), -2e-3)
+    sw.set_streams(stream=list(range(sw.R)), step=[0] * sw.R)
+    sw.set_spins(random_ising(lat, 11))
+    sw.zero_avg()
+    eq, meas = 2000, 20000
+    sw.mcs(0, eq + meas, eq, 1)
+    sums = sw.sums().reshape(G, len(temps), 7)
+    from scipy.special import erfcinv
+    n_cmp = 2 * len(temps)
+    zmax = float(np.sqrt(2) * erfcinv(0.01 / n_cmp))   # two-sided 0.01 / 6: |z| < 3.14
+    for k, t in enumerate(temps):
+        K = 1.0 / t
+        cnt = sums[:, k, 0]
+        assert np.all(cnt == meas)
+        e = sums[:, k, 1] / cnt / 1e-3            # per chain, units of J
+        e2 = sums[:, k, 2] / cnt / 1e-6
+        cv = lat.N * K * K * (e2 - e * e)         # per chain
+        e_ex, cv_ex = EXACT_16[t]
+        for name, x, ref in (("E/N", e, e_ex), ("C/N", cv, cv_ex)):
+            z = (x.mean() - ref) / (x.std(ddof=1) / np.sqrt(G))
+            print("kT=%.3f %s: GPU %.5f +- %.5f, exact %.5f, z = %.2f" %
+                  (t, name, x.mean(), x.std(ddof=1) / np.sqrt(G), ref, z))
+            assert abs(z) < zmax, (t, name, x.mean(), ref, z)
+    sw.close()
+
+
+@pytest.mark.gpu
+def test_mcs_heisenberg_ring_equals_the_exact_chain():
+    N, G = 64, 64
+    temps = (0.5, 1.0, 2.0)
+    lat = eg.Lattice([[0.0, 0.0, 0.0]], [1], np.diag([1.0, 8.0, 8.0]), (N, 1, 1), [1.0])
+    sw, _ = make_pair(lat, eg.MODEL_XYZ, FM, replicas=G * len(temps))
+    info = sw.info()
+    assert info.fast_path == 0 and info.n_colours == 2
+    sw.set_ladder([beta_of(t) for t in temps])
+    # two neighbours per site: the aligned state has E / 2N = -J
+    al = lat.ion.copy()
+    al[:, 1:4] = (0.0, 0.0, 1.0)
+    sw.set_spins(al)
+    assert np.allclose(np.asarray(sw.tot_energy()) / (2 * N), -1e-3)
+    sw.set_streams(stream=list(range(sw.R)), step=[0] * sw.R)
+    sw.set_spins(random_xyz(lat, 12))
+    sw.zero_avg()
+    eq, meas = 2000, 40000
+    sw.mcs(0, eq + meas, eq, 1, ovrr=True, ovrr_para=1.0, ovrr_mcs=1)
+    sums = sw.sums().reshape(G, len(temps), 7)
+    from scipy.special import erfcinv
+    zmax = float(np.sqrt(2) * erfcinv(0.01 / (2 * len(temps))))
+    for k, t in enumerate(temps):
+        K = 1.0 / t
+        cnt = sums[:, k, 0]
+        assert np.all(cnt == meas)
+        e = sums[:, k, 1] / cnt / 1e-3
+        e2 = sums[:, k, 2] / cnt / 1e-6
+        cv = N * K * K * (e2 - e * e)
+        e_ex = -(1.0 / np.tanh(K) - 1.0 / K)
+        cv_ex = 1.0 - (K / np.sinh(K)) ** 2
+        for name, x, ref in (("E/N", e, e_ex), ("C/N", cv, cv_ex)):
+            z = (x.mean() - ref) / (x.std(ddof=1) / np.sqrt(G))
+            print("Heisenberg ring kT=%.2f %s: GPU %.5f +- %.5f, exact %.5f, z = %.2f" %
+                  (t, name, x.mean(), x.std(ddof=1) / np.sqrt(G), ref, z))
+            assert abs(z) < zmax, (t, name, x.mean(), ref, z)
+    sw.close()
