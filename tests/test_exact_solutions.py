@@ -10,7 +10,10 @@ ether_mcs at kT = 2.0, 2.269 (near the infinite lattice's T_c) and 3.0 J, 64 ind
 chains per temperature, 20 000 measurements each after 2 000 equilibration steps.  The energy
 per site (src/get_eng.f90:36-40, E / 2N) and the heat capacity per site from its fluctuations
 agree with the exact values: each of the 6 differences, over the spread of the 64 chains'
-estimates, passes a two-sided z-test at 0.01 / 6 (Bonferroni, a family-wise 1%).
+estimates, passes a two-sided z-test at 0.01 / 6 (Bonferroni, a family-wise 1%).  The same
+holds on a ladder of kT = 2.0, 2.1, 2.269 and 2.5 J with parallel tempering when the swap
+exponent uses the Hamiltonian energy; the reference's raw-sum exponent (every bond counted
+twice) measurably biases the coldest slot.
 
 Heisenberg (XYZ): the classical ferromagnetic ring of 64 unit spins (the other two axes 8
 lattice constants long: two neighbours per site).  Its transfer matrix gives the energy per
@@ -30,7 +33,9 @@ FM = [[(1, 1, (-1.0, -1.0, -1.0))]]   # ETHER's sign: J < 0 is ferromagnetic, |J
 # kT / J -> (energy per site / J, heat capacity per site / k_B) of the 16 x 16 torus, from the
 # closed form (test_exact_values_are_the_closed_forms checks them; the GPU test needs no mpmath)
 EXACT_16 = {2.0: (-1.7455306689909191, 0.7255087677365641),
+            2.1: (-1.662024277054132, 0.9601262642539019),
             2.269: (-1.4533425476693835, 1.4983111034990866),
+            2.5: (-1.131317984410729, 1.0649768828534356),
             3.0: (-0.8176893678695545, 0.4043325741653013)}
 
 
@@ -71,12 +76,12 @@ def _square_torus(L):
     return eg.Lattice([[0.0, 0.0, 0.0]], [1], np.diag([1.0, 1.0, 8.0]), (L, L, 1), [1.0])
 
 
-@pytest.mark.gpu
-def test_mcs_energy_and_heat_capacity_equal_the_exact_torus():
+def _torus_run(pt, flags=0):
+    """Per (chain, temperature) energy and heat capacity per site, and the exact values."""
     L, G = 16, 64
-    temps = (2.0, 2.269, 3.0)
+    temps = (2.0, 2.1, 2.269, 2.5) if pt else (2.0, 2.269, 3.0)
     lat = _square_torus(L)
-    sw, _ = make_pair(lat, eg.MODEL_ISING, FM, replicas=G * len(temps))
+    sw, _ = make_pair(lat, eg.MODEL_ISING, FM, replicas=G * len(temps), flags=flags)
     info = sw.info()
     assert info.fast_path == 0 and info.n_colours == 2
     sw.set_ladder([beta_of(t) for t in temps])
@@ -88,16 +93,19 @@ def test_mcs_energy_and_heat_capacity_equal_the_exact_torus():
     sw.set_streams(stream=list(range(sw.R)), step=[0] * sw.R)
     sw.set_spins(random_ising(lat, 11))
     sw.zero_avg()
-    eq, meas = 2000, 20000
-    sw.mcs(0, eq + meas, eq, 1)
+    # PT runs on steps that are multiples of 5 but not measurement steps (src/ether.f90:190-191):
+    # with PT a measurement every second step, so the swaps come every 10
+    eq, meas, coa = 2000, 20000, 2 if pt else 1
+    swaps = sw.mcs(0, eq + meas, eq, coa, pt=pt, exchange_interval=5)
+    if pt:
+        assert swaps > 0 and not np.array_equal(sw.slots(), np.arange(sw.R) % len(temps))
     sums = sw.sums().reshape(G, len(temps), 7)
-    from scipy.special import erfcinv
-    n_cmp = 2 * len(temps)
-    zmax = float(np.sqrt(2) * erfcinv(0.01 / n_cmp))   # two-sided 0.01 / 6: |z| < 3.14
+    sw.close()
+    out = []
     for k, t in enumerate(temps):
         K = 1.0 / t
         cnt = sums[:, k, 0]
-        assert np.all(cnt == meas)
+        assert np.all(cnt == meas // coa)
         e = sums[:, k, 1] / cnt / 1e-3            # per chain, units of J
         e2 = sums[:, k, 2] / cnt / 1e-6
         cv = lat.N * K * K * (e2 - e * e)         # per chain
@@ -106,8 +114,35 @@ def test_mcs_energy_and_heat_capacity_equal_the_exact_torus():
             z = (x.mean() - ref) / (x.std(ddof=1) / np.sqrt(G))
             print("kT=%.3f %s: GPU %.5f +- %.5f, exact %.5f, z = %.2f" %
                   (t, name, x.mean(), x.std(ddof=1) / np.sqrt(G), ref, z))
-            assert abs(z) < zmax, (t, name, x.mean(), ref, z)
-    sw.close()
+            out.append((t, name, x.mean(), ref, z))
+    return out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("pt", [False, True])
+def test_mcs_energy_and_heat_capacity_equal_the_exact_torus(pt):
+    """pt: each chain is a ladder of kT = 2.0, 2.1, 2.269 and 2.5 J with parallel-tempering
+    swaps every 10 steps (src/parallel_tempering.f90:39-108) whose exponent uses the
+    Hamiltonian energy (ETHER_FLAG_PT_TRUE_ENERGY), which leaves every temperature's ensemble
+    exact; the statistics are per (chain, temperature slot)."""
+    from scipy.special import erfcinv
+    res = _torus_run(pt, flags=eg.FLAG_PT_TRUE_ENERGY if pt else 0)
+    zmax = float(np.sqrt(2) * erfcinv(0.01 / len(res)))   # two-sided 0.01 / 6 (or / 8): |z| < 3.14 (3.23)
+    for t, name, got, ref, z in res:
+        assert abs(z) < zmax, (t, name, got, ref, z)
+
+
+@pytest.mark.gpu
+def test_reference_pt_exponent_biases_the_cold_end():
+    """The reference's PT exponent takes get_tot_energy's raw sum, which counts every bond
+    twice (src/ether.f90:177, src/get_tot_energy.f90:33-47): the swap acceptance is
+    exp(2 dbeta dH) instead of exp(dbeta dH), which breaks detailed balance.  The default mode
+    reproduces it, and on the same ladder the coldest slot's energy is measurably below the
+    exact value (the chains are seeded, so the figure is reproducible)."""
+    res = _torus_run(True)
+    t, name, got, ref, z = res[0]
+    assert (t, name) == (2.0, "E/N")
+    assert z < -5.0, res[0]
 
 
 @pytest.mark.gpu
