@@ -21,6 +21,9 @@ site -J L(K) and the heat capacity per site 1 - K^2 / sinh^2 K (L the Langevin f
 K = J / kT; M. E. Fisher, Am. J. Phys. 32, 343 (1964)), up to terms of relative order
 L(K)^64 (below 1e-17 here).  ether_mcs with Marsaglia proposals and an overrelaxation pass
 every step (src/ether.f90:163-172) at kT = 0.5, 1 and 2 J, the same rule as above.
+
+Ising in a field: the ring of 64 spins in a Zeeman field, against its transfer matrix (the
+reported energy per site and its variance).
 """
 import numpy as np
 import pytest
@@ -180,5 +183,86 @@ def test_mcs_heisenberg_ring_equals_the_exact_chain():
             z = (x.mean() - ref) / (x.std(ddof=1) / np.sqrt(G))
             print("Heisenberg ring kT=%.2f %s: GPU %.5f +- %.5f, exact %.5f, z = %.2f" %
                   (t, name, x.mean(), x.std(ddof=1) / np.sqrt(G), ref, z))
+            assert abs(z) < zmax, (t, name, x.mean(), ref, z)
+    sw.close()
+
+
+def _chain_f(K, h):
+    """ln of the larger transfer-matrix eigenvalue of the Ising chain, weights
+    exp(K s s' + h s): the free energy per site of a long ring, in units of -kT."""
+    return np.log(np.exp(K) * np.cosh(h) + np.sqrt(np.exp(2 * K) * np.sinh(h) ** 2 + np.exp(-2 * K)))
+
+
+def _chain_derivs(K, h, d=1e-4):
+    """f_K, f_h, f_KK, f_hh, f_Kh by central differences (step 1e-4: errors ~1e-8)."""
+    f = _chain_f
+    fK = (f(K + d, h) - f(K - d, h)) / (2 * d)
+    fh = (f(K, h + d) - f(K, h - d)) / (2 * d)
+    fKK = (f(K + d, h) - 2 * f(K, h) + f(K - d, h)) / d ** 2
+    fhh = (f(K, h + d) - 2 * f(K, h) + f(K, h - d)) / d ** 2
+    fKh = (f(K + d, h + d) - f(K + d, h - d) - f(K - d, h + d) + f(K - d, h - d)) / (4 * d * d)
+    return fK, fh, fKK, fhh, fKh
+
+
+def test_chain_transfer_matrix_equals_enumeration():
+    """The eigenvalue formula against the enumeration of a 14-site ring (K = 0.7, h = 0.3):
+    <s s'> and <s> per site agree to the ring's (lambda_- / lambda_+)^14 correction."""
+    n, K, h = 14, 0.7, 0.3
+    s = 1 - 2 * ((np.arange(1 << n)[:, None] >> np.arange(n)) & 1)
+    ss = (s * np.roll(s, 1, axis=1)).sum(axis=1)
+    m = s.sum(axis=1)
+    w = np.exp(K * ss + h * m)
+    w /= w.sum()
+    fK, fh, *_ = _chain_derivs(K, h)
+    assert abs((w * ss).sum() / n - fK) < 1e-3
+    assert abs((w * m).sum() / n - fh) < 1e-3
+
+
+@pytest.mark.gpu
+def test_mcs_ising_ring_in_a_field_equals_the_transfer_matrix():
+    """A ring of 64 Ising spins (the general-lattice kernels) with exchange |J| = 1 meV and a
+    Zeeman field H = 2 T along z (g = 2, s = 1: h = g mu_B H per spin).  The reported energy
+    per site is E_raw / 2N = -|J| <s s'> - (h / 2) <s> (the half Zeeman term of
+    src/get_eng.f90:36), and N Var(e) = |J|^2 f_KK + (h / 2)^2 f_hh + |J| h f_Kh, both from
+    the transfer matrix's eigenvalue (ring corrections below 1e-12).  kT = 0.5, 1 and 2 meV;
+    64 chains each; the same family-wise rule."""
+    N, G, Hz = 64, 64, 2.0
+    temps = (0.5, 1.0, 2.0)
+    lat = eg.Lattice([[0.0, 0.0, 0.0]], [1], np.diag([1.0, 8.0, 8.0]), (N, 1, 1), [1.0])
+    sw, _ = make_pair(lat, eg.MODEL_ISING, FM, replicas=G * len(temps), zeeman=True,
+                      h=(0.0, 0.0, Hz), g_factor=2.0)
+    assert sw.info().fast_path == 0 and sw.info().n_colours == 2
+    sw.set_ladder([beta_of(t) for t in temps])
+    h_mev = 2.0 * eg.MB_EV * Hz * 1e3
+    up = lat.ion.copy()
+    up[:, 3] = 1.0
+    sw.set_spins(up)
+    e_up = np.asarray(sw.tot_energy())[0] / (2 * N) / 1e-3
+    up[:, 3] = -1.0
+    sw.set_spins(up)
+    e_dn = np.asarray(sw.tot_energy())[0] / (2 * N) / 1e-3
+    # the field lowers an up spin's energy by h; the reported energy carries half of it
+    assert np.isclose(e_up, -1.0 - h_mev / 2) and np.isclose(e_dn, -1.0 + h_mev / 2)
+    sw.set_streams(stream=list(range(sw.R)), step=[0] * sw.R)
+    sw.set_spins(random_ising(lat, 13))
+    sw.zero_avg()
+    eq, meas = 2000, 40000
+    sw.mcs(0, eq + meas, eq, 1)
+    sums = sw.sums().reshape(G, len(temps), 7)
+    from scipy.special import erfcinv
+    zmax = float(np.sqrt(2) * erfcinv(0.01 / (2 * len(temps))))
+    for k, t in enumerate(temps):
+        K, hb = 1.0 / t, h_mev / t
+        fK, fh, fKK, fhh, fKh = _chain_derivs(K, hb)
+        e_ex = -fK - (h_mev / 2) * fh
+        var_ex = fKK + (h_mev / 2) ** 2 * fhh + h_mev * fKh     # N Var(e), meV^2
+        cnt = sums[:, k, 0]
+        assert np.all(cnt == meas)
+        e = sums[:, k, 1] / cnt / 1e-3
+        var = N * (sums[:, k, 2] / cnt / 1e-6 - e * e)
+        for name, x, ref in (("E/N", e, e_ex), ("N Var(E/N)", var, var_ex)):
+            z = (x.mean() - ref) / (x.std(ddof=1) / np.sqrt(G))
+            print("Ising ring in H=%.0f T, kT=%.2f %s: GPU %.5f +- %.5f, exact %.5f, z = %.2f" %
+                  (Hz, t, name, x.mean(), x.std(ddof=1) / np.sqrt(G), ref, z))
             assert abs(z) < zmax, (t, name, x.mean(), ref, z)
     sw.close()
