@@ -32,12 +32,16 @@ static int fail(int code, const std::string &msg) {
 
 void ether::set_error(const std::string &msg) { g_err = msg; }
 
+// A failed call is reported here and its error read off the runtime (cudaGetLastError), so
+// that a later launch check does not report it again; a sticky error stays with the context.
 #define CUDA_TRY(expr)                                                                     \
     do {                                                                                   \
         cudaError_t _e = (expr);                                                           \
-        if (_e != cudaSuccess)                                                             \
+        if (_e != cudaSuccess) {                                                           \
+            cudaGetLastError();                                                            \
             return fail(_e == cudaErrorMemoryAllocation ? ETHER_ERR_NOMEM : ETHER_ERR_CUDA, \
                         std::string(#expr) + ": " + cudaGetErrorString(_e));               \
+        }                                                                                  \
     } while (0)
 
 extern "C" int ether_abi_version(void) { return ETHER_ABI_VERSION; }
@@ -49,7 +53,10 @@ template <class T>
 int dev_alloc(Ctx &c, T **p, size_t n) {
     if (n == 0) n = 1;
     cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
-    if (e != cudaSuccess) return fail(ETHER_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ETHER_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
     c.device_bytes += n * sizeof(T);
     return ETHER_OK;
 }
@@ -1671,6 +1678,7 @@ extern "C" int ether_record_series(ether_ctx *h, int32_t nsweeps, int32_t stride
     const size_t bytes = sizeof(double) * (size_t)nrec * c.R;
     CUDA_TRY(cudaMalloc(&mser, bytes));
     if (E && cudaMalloc(&eser, bytes) != cudaSuccess) {
+        cudaGetLastError();  // reported here; not left for the next launch check to find
         cudaFree(mser);
         return fail(ETHER_ERR_NOMEM, "cudaMalloc of the energy series failed");
     }
@@ -1678,7 +1686,13 @@ extern "C" int ether_record_series(ether_ctx *h, int32_t nsweeps, int32_t stride
     int t = 0;
     int32_t *t_dev = nullptr;
     cudaGraphExec_t ex = nullptr;
-    if (nrec >= 4 && !(c.flags & ETHER_FLAG_NO_GRAPHS) && cudaMalloc(&t_dev, sizeof(int32_t)) == cudaSuccess) {
+    bool use_graph = nrec >= 4 && !(c.flags & ETHER_FLAG_NO_GRAPHS);
+    if (use_graph && cudaMalloc(&t_dev, sizeof(int32_t)) != cudaSuccess) {
+        cudaGetLastError();  // direct launches instead; the failed allocation is not a lasting error
+        t_dev = nullptr;
+        use_graph = false;
+    }
+    if (use_graph) {
         // one stride -- stride sweeps and the record of row *t_dev -- captured once, replayed
         // for every row
         cudaGraph_t g = nullptr;

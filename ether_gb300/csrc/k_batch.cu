@@ -327,9 +327,11 @@ int bfail(int code, const std::string &msg) {
 #define BCUDA(expr)                                                                          \
     do {                                                                                     \
         cudaError_t _e = (expr);                                                             \
-        if (_e != cudaSuccess)                                                               \
+        if (_e != cudaSuccess) {                                                             \
+            cudaGetLastError(); /* reported here, not again by a later launch check */       \
             return bfail(_e == cudaErrorMemoryAllocation ? ETHER_ERR_NOMEM : ETHER_ERR_CUDA,  \
                          std::string(#expr) + ": " + cudaGetErrorString(_e));                \
+        }                                                                                    \
     } while (0)
 
 BatchMember describe(const Ctx &c) {
