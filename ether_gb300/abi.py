@@ -119,6 +119,7 @@ SIGNATURES = {
     "ether_get_spins": (C.c_int, [P, C.c_int32, PD]),
     "ether_set_spins_batch": (C.c_int, [P, C.c_int32, C.c_int32, PD]),
     "ether_get_spins_batch": (C.c_int, [P, C.c_int32, C.c_int32, PD]),
+    "ether_spins_batch_split": (C.c_int, [P, PI32, PI32]),
     "ether_fresh_spins": (C.c_int, [P]),
     "ether_metropolis": (C.c_int, [P, C.c_int32, PD]),
     "ether_overrelaxation": (C.c_int, [P, C.c_double]),

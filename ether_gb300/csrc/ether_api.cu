@@ -6,6 +6,7 @@
 // recognises the even periodic simple-cubic lattice (arithmetic neighbours), and builds
 // the FP64 Ising acceptance-threshold tables per temperature slot.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -212,6 +213,8 @@ void free_ctx(Ctx &c) {
         if (p) cudaFree(p);
     if (c.acc_host) cudaFreeHost(c.acc_host);
     if (c.stage) cudaFreeHost(c.stage);
+    for (cudaEvent_t e : c.ion_ev)
+        if (e) cudaEventDestroy(e);
     for (auto &kv : c.graphs) cudaGraphExecDestroy(kv.second);
     if (c.ev_fork) cudaEventDestroy(c.ev_fork);
     for (int k = 0; k < Ctx::kMaxParts - 1; ++k) {
@@ -770,7 +773,7 @@ void device_layout_to_ion(const Ctx &c, const void *src, double *ion) {
 }
 }  // namespace
 
-static int spins_staged(Ctx &c, int32_t r0, int32_t n, double *ion, bool to_device);
+static int spins_staged(Ctx &c, int32_t r0, int32_t n, double *ion, bool to_device, double *host_s = nullptr);
 
 // Whether [p, p + bytes) is host memory mapped in this process, checked before a kernel reads
 // or writes it in place (a wrong pointer must not reach the device): device memory is refused
@@ -788,36 +791,77 @@ static bool host_range_mapped(const void *p, size_t bytes) {
     return msync(reinterpret_cast<void *>(a), (size_t)(b - a), MS_ASYNC) == 0;
 }
 
-// Where the device reads and writes host memory in place (c.ion_direct) a kernel moves the
-// records.  An upload of 8 or more replicas on a host with 8 or more threads is split: the
-// kernel reads the first 5/8 of the replicas while the host's cores convert the rest through
-// the staging area, whose copies follow the kernel on the stream (64^3 x 1024 Ising records
-// on a Grace host: 77 ms by the kernel alone, 83 ms by the cores alone, 53 ms split 5/8;
-// 1/2 and 3/4 measured 67 and 59 ms).  A read-back is not split: each 8-byte write is a
-// read-modify-write of a line in host memory, whichever side makes it, and a split measured
-// slower (111-133 against 100 ms).
+// Where the device reads and writes host memory in place (c.ion_direct) a kernel can move the
+// records, and the host's cores can convert them through the staging area at the same time;
+// which does how much is measured per context and direction, because the in-place path's
+// speed depends on the host: on most Grace machines it is the faster (64^3 x 1024 Ising records:
+// upload 77 ms by the kernel alone, 83-86 by the cores alone, 53-61 split 5/8; read-back 100
+// against 148 ms), on some it was several times slower (0.23 s and 0.72 s in one process).
+// * Upload: the kernel reads the first share of the replicas while the host's cores convert
+//   the rest, the staged copies following the kernel on the stream.  The first call splits
+//   5/8 : 3/8 (8 or more replicas and host threads; 1/2 and 3/4 measured 67 and 59 ms), later
+//   calls in proportion to the two rates measured side by side in the previous one, so both
+//   parts end together.
+// * Read-back: not split (each 8-byte write is a read-modify-write of a line in host memory,
+//   whichever side makes it, and a split measured slower, 111-133 against 100 ms).  The first
+//   call runs the kernel, the second the host's cores, and later calls the faster of the two.
+// Rates come from CUDA events around the kernel and the wall time of the host's conversion.
 static int spins_batch(Ctx &c, int32_t r0, int32_t n, double *ion, bool to_device) {
     if (!c.ion_direct) return spins_staged(c, r0, n, ion, to_device);
     if (!host_range_mapped(ion, sizeof(double) * 9 * (size_t)c.N * n))
         return fail(ETHER_ERR_ARG, std::string(to_device ? "ether_set_spins_batch" : "ether_get_spins_batch") +
                                        ": ion is not host memory mapped for n replicas' records");
-    const int nk = to_device && n >= 8 && host_threads() >= 8 ? n - n * 3 / 8 : n;
-    cudaError_t e = launch_ion_copy(c, r0, nk, ion, to_device);
-    if (e == cudaSuccess && nk == n) e = cudaStreamSynchronize(c.stream);
-    if (e != cudaSuccess) {
-        cudaStreamSynchronize(c.stream);  // launches before a failed one may still be reading ion
-        return fail(ETHER_ERR_CUDA, std::string(to_device ? "ether_set_spins_batch: " : "ether_get_spins_batch: ") +
-                                        cudaGetErrorString(e));
+    const int d = to_device ? 1 : 0;
+    const double rk = c.ion_rate_k[d], rh = c.ion_rate_h[d];
+    int nk;
+    if (to_device) {
+        if (rk > 0.0 && rh > 0.0)
+            nk = (int)std::lround((double)n * rk / (rk + rh));
+        else
+            nk = n >= 8 && host_threads() >= 8 ? n - n * 3 / 8 : n;
+    } else {
+        nk = rk <= 0.0 ? n : rh <= 0.0 ? 0 : (rk >= rh ? n : 0);
     }
-    if (nk == n) return ETHER_OK;
-    // the staged part synchronises the stream (kernel included) before it returns; on an
-    // early failure the kernel may still be reading the caller's records, so wait for it
-    const int rc = spins_staged(c, r0 + nk, n - nk, ion + (size_t)9 * c.N * nk, to_device);
-    if (rc != ETHER_OK) cudaStreamSynchronize(c.stream);
-    return rc;
+    nk = std::max(0, std::min(n, nk));
+    const char *who = to_device ? "ether_set_spins_batch: " : "ether_get_spins_batch: ";
+    cudaError_t e = cudaSuccess;
+    if (nk > 0) {
+        for (int k = 0; k < 2 && e == cudaSuccess; ++k)
+            if (!c.ion_ev[k]) e = cudaEventCreate(&c.ion_ev[k]);
+        if (e == cudaSuccess) e = cudaEventRecord(c.ion_ev[0], c.stream);
+        if (e == cudaSuccess) e = launch_ion_copy(c, r0, nk, ion, to_device);
+        if (e == cudaSuccess) e = cudaEventRecord(c.ion_ev[1], c.stream);
+        if (e == cudaSuccess && nk == n) e = cudaStreamSynchronize(c.stream);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            cudaStreamSynchronize(c.stream);  // launches before a failed one may still be reading ion
+            return fail(ETHER_ERR_CUDA, std::string(who) + cudaGetErrorString(e));
+        }
+    }
+    double host_s = 0.0;
+    if (nk < n) {
+        // the staged part synchronises the stream (kernel included) before it returns; on an
+        // early failure the kernel may still be reading the caller's records, so wait for it
+        const int rc = spins_staged(c, r0 + nk, n - nk, ion + (size_t)9 * c.N * nk, to_device, &host_s);
+        if (rc != ETHER_OK) {
+            cudaStreamSynchronize(c.stream);
+            return rc;
+        }
+        if (host_s > 0.0) c.ion_rate_h[d] = (double)(n - nk) / host_s;
+    }
+    if (nk > 0) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, c.ion_ev[0], c.ion_ev[1]) == cudaSuccess && ms > 0.f)
+            c.ion_rate_k[d] = (double)nk / (1e-3 * ms);
+        else
+            cudaGetLastError();
+    }
+    c.ion_last_kernel[d] = nk;
+    return ETHER_OK;
 }
 
-static int spins_staged(Ctx &c, int32_t r0, int32_t n, double *ion, bool to_device) {
+// host_s (may be null) accumulates the wall time of the host's conversion loops.
+static int spins_staged(Ctx &c, int32_t r0, int32_t n, double *ion, bool to_device, double *host_s) {
     const size_t per_rep = c.model == ETHER_MODEL_ISING ? (size_t)c.N : sizeof(float4) * c.N;
     const size_t ion_rep = (size_t)9 * c.N;
     uint8_t *dev = c.model == ETHER_MODEL_ISING ? c.spins : reinterpret_cast<uint8_t *>(c.spins4);
@@ -848,6 +892,7 @@ static int spins_staged(Ctx &c, int32_t r0, int32_t n, double *ion, bool to_devi
                 }
             }
         }
+        const auto t0 = std::chrono::steady_clock::now();
         parallel_for(nchunk, [&](int k) {
             const int a = k * per_chunk, b = std::min(np, a + per_chunk);
             if (to_device) {
@@ -866,6 +911,7 @@ static int spins_staged(Ctx &c, int32_t r0, int32_t n, double *ion, bool to_devi
                     device_layout_to_ion(c, stage + per_rep * r, ion + ion_rep * (size_t)(p0 + r));
             }
         });
+        if (host_s) host_s[0] += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         for (cudaEvent_t x : ev)
             if (x) cudaEventDestroy(x);
         // the staging area is reused by the next pass (and the next call)
@@ -875,6 +921,14 @@ static int spins_staged(Ctx &c, int32_t r0, int32_t n, double *ion, bool to_devi
             return fail(ETHER_ERR_CUDA, std::string(to_device ? "ether_set_spins_batch: " : "ether_get_spins_batch: ") +
                                             cudaGetErrorString(e));
     }
+    return ETHER_OK;
+}
+
+extern "C" int ether_spins_batch_split(ether_ctx *h, int32_t *get_kernel, int32_t *set_kernel) {
+    if (!h || !get_kernel || !set_kernel) return fail(ETHER_ERR_ARG, "null argument");
+    Ctx &c = h->c;
+    *get_kernel = c.ion_last_kernel[0];
+    *set_kernel = c.ion_last_kernel[1];
     return ETHER_OK;
 }
 

@@ -130,6 +130,12 @@ struct Ctx {
     double *acc_host = nullptr;                // R: pinned host copy
     void *stage = nullptr;                     // pinned staging of ether_{set,get}_spins_batch
     bool ion_direct = false;                   // the device reads / writes the host records in place
+    // ether_{set,get}_spins_batch where ion_direct: measured rates (replicas per second) of the
+    // in-place kernel and of the host's staged conversion, per direction (0 read-back, 1
+    // upload), the replicas the kernel moved in the last call, and the kernel's timing events
+    double ion_rate_k[2] = {0.0, 0.0}, ion_rate_h[2] = {0.0, 0.0};
+    int ion_last_kernel[2] = {0, 0};
+    cudaEvent_t ion_ev[2] = {nullptr, nullptr};
     size_t stage_bytes = 0;
     int32_t *spiral_ptr = nullptr, *spiral_nbr = nullptr;  // spiral partners, CSR in storage order
     long spiral_count = 0;

@@ -244,6 +244,12 @@ class Sweep:
         return ions
 
     # -- reference routines
+    def spins_batch_split(self):
+        """Replicas the last get_spins_batch / set_spins_batch moved in place by a kernel."""
+        g, st = C.c_int32(0), C.c_int32(0)
+        abi.check(self.lib.ether_spins_batch_split(self.h, C.byref(g), C.byref(st)))
+        return g.value, st.value
+
     def fresh_spins(self):
         abi.check(self.lib.ether_fresh_spins(self.h))
 

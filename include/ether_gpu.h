@@ -137,7 +137,8 @@ int ether_get_spins(ether_ctx *ctx, int32_t replica, double *ion);
  * of src/ether.f90:112-118, each of which owned one ion).  Where the device addresses
  * pageable host memory through the host's page tables (ether_info.ion_direct: a Grace CPU's
  * memory over NVLink-C2C), a kernel reads and writes the records' spin fields in place (an
- * XYZ set reads whole records in tiles; only the spin fields are written);
+ * XYZ set reads whole records in tiles; only the spin fields are written), beside or instead
+ * of the host's conversion as measured (ether_spins_batch_split);
  * otherwise the layout conversion runs on the host's cores into pinned staging memory (up to
  * 512 MB, allocated on the first call and kept by the context), overlapped with the copies.
  * Returns when the data is in place; ion must stay valid for the call.  On the in-place path
@@ -145,6 +146,12 @@ int ether_get_spins(ether_ctx *ctx, int32_t replica, double *ion);
  * ETHER_ERR_ARG before any launch). */
 int ether_set_spins_batch(ether_ctx *ctx, int32_t r0, int32_t n, const double *ion);
 int ether_get_spins_batch(ether_ctx *ctx, int32_t r0, int32_t n, double *ion);
+/* How the last ether_get_spins_batch / ether_set_spins_batch divided its replicas: the number
+ * moved in place by a kernel (the rest went through the host's staging).  Where both ways are
+ * open the context measures them: an upload is split in proportion to the two rates measured
+ * in the previous upload (5/8 to the kernel the first time); a read-back uses the kernel the
+ * first time, the host's cores the second, then the faster. */
+int ether_spins_batch_split(ether_ctx *ctx, int32_t *get_kernel, int32_t *set_kernel);
 
 /* fresh_spins (src/fresh_spins.f90:31-38), called at src/ether.f90:155: Ising flips every
  * spin, XYZ draws a new Marsaglia / ANGLE state, on every replica. */

@@ -390,6 +390,35 @@ def test_spins_batch_equals_per_replica_calls(model, L, R, staged):
     sw.close()
 
 
+def test_spins_batch_measures_both_ways_and_keeps_the_records():
+    """Where the records can move in place: the first upload splits 5/8 of the replicas to the
+    kernel, later ones by the measured rates; the read-back runs the kernel, then the host's
+    cores, then the faster of the two.  Every call leaves the same device state and records."""
+    lat = eg.simple_cubic((32, 16, 16))
+    R = 40
+    sw, _ = make_pair(lat, eg.MODEL_ISING, FM, replicas=R)
+    if not sw.info().ion_direct:
+        sw.close()
+        pytest.skip("the records are staged through the host on this system")
+    sw.set_beta(beta_of(4.5))
+    ions = np.stack([random_ising(lat, 40 + r) for r in range(R)])
+    gets, sets = [], []
+    for k in range(4):
+        sw.set_spins_batch(ions)
+        sets.append(sw.spins_batch_split()[1])
+        back = np.stack([lat.ion] * R).copy()
+        back[:, :, 0] = 5.0
+        sw.get_spins_batch(back)
+        gets.append(sw.spins_batch_split()[0])
+        np.testing.assert_array_equal(back[:, :, 3], ions[:, :, 3])
+        assert np.all(back[:, :, 0] == 5.0)
+    print("kernel share of the uploads", sets, "of the read-backs", gets, "of", R)
+    assert sets[0] == R - R * 3 // 8
+    assert all(0 <= k <= R for k in sets)
+    assert gets[0] == R and gets[1] == 0 and gets[2] in (0, R) and gets[3] == gets[2]
+    sw.close()
+
+
 def test_spins_batch_refuses_device_memory_before_any_launch():
     """Where a kernel moves the records in place, a pointer to device memory is refused before
     anything is launched (ETHER_ERR_ARG), in both directions, and the context keeps working."""
