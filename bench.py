@@ -216,8 +216,8 @@ def run_sweeps(model, L, replicas, steps, warmup, rank, world, force_variant=0, 
         ions = np.empty((R, N, 9))
         ions[:] = ion
         # untimed rounds: the first allocates the pinned staging area, and where the records can
-        # also move in place the library measures both ways on its first calls (the read-back
-        # tries each once) and settles on its split
+        # also move in place the library measures both ways on its first calls (the first three
+        # read-backs try the kernel, the host's cores and the kernel) and settles on its split
         for _ in range(3):
             sw.set_spins_batch(ions)
             sw.get_spins_batch(ions)

@@ -804,7 +804,9 @@ static bool host_range_mapped(const void *p, size_t bytes) {
 //   parts end together.
 // * Read-back: not split (each 8-byte write is a read-modify-write of a line in host memory,
 //   whichever side makes it, and a split measured slower, 111-133 against 100 ms).  The first
-//   call runs the kernel, the second the host's cores, and later calls the faster of the two.
+//   three calls run the kernel, the host's cores and the kernel again (a process's first
+//   in-place read-back was seen slower than its later ones), later calls the way with the
+//   better of its measured rates.
 // Rates come from CUDA events around the kernel and the wall time of the host's conversion.
 static int spins_batch(Ctx &c, int32_t r0, int32_t n, double *ion, bool to_device) {
     if (!c.ion_direct) return spins_staged(c, r0, n, ion, to_device);
@@ -820,7 +822,8 @@ static int spins_batch(Ctx &c, int32_t r0, int32_t n, double *ion, bool to_devic
         else
             nk = n >= 8 && host_threads() >= 8 ? n - n * 3 / 8 : n;
     } else {
-        nk = rk <= 0.0 ? n : rh <= 0.0 ? 0 : (rk >= rh ? n : 0);
+        const int k = c.ion_gets++;
+        nk = k == 0 || k == 2 ? n : k == 1 ? 0 : (rk >= rh ? n : 0);
     }
     nk = std::max(0, std::min(n, nk));
     const char *who = to_device ? "ether_set_spins_batch: " : "ether_get_spins_batch: ";
@@ -847,14 +850,20 @@ static int spins_batch(Ctx &c, int32_t r0, int32_t n, double *ion, bool to_devic
             cudaStreamSynchronize(c.stream);
             return rc;
         }
-        if (host_s > 0.0) c.ion_rate_h[d] = (double)(n - nk) / host_s;
+        if (host_s > 0.0) {
+            // an upload's rates are those of the last split; a read-back keeps the best seen
+            const double r = (double)(n - nk) / host_s;
+            c.ion_rate_h[d] = to_device ? r : std::max(c.ion_rate_h[d], r);
+        }
     }
     if (nk > 0) {
         float ms = 0.f;
-        if (cudaEventElapsedTime(&ms, c.ion_ev[0], c.ion_ev[1]) == cudaSuccess && ms > 0.f)
-            c.ion_rate_k[d] = (double)nk / (1e-3 * ms);
-        else
+        if (cudaEventElapsedTime(&ms, c.ion_ev[0], c.ion_ev[1]) == cudaSuccess && ms > 0.f) {
+            const double r = (double)nk / (1e-3 * ms);
+            c.ion_rate_k[d] = to_device ? r : std::max(c.ion_rate_k[d], r);
+        } else {
             cudaGetLastError();
+        }
     }
     c.ion_last_kernel[d] = nk;
     return ETHER_OK;

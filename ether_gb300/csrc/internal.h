@@ -135,6 +135,7 @@ struct Ctx {
     // upload), the replicas the kernel moved in the last call, and the kernel's timing events
     double ion_rate_k[2] = {0.0, 0.0}, ion_rate_h[2] = {0.0, 0.0};
     int ion_last_kernel[2] = {0, 0};
+    int ion_gets = 0;  // read-backs so far (the first three try the kernel, the cores, the kernel)
     cudaEvent_t ion_ev[2] = {nullptr, nullptr};
     size_t stage_bytes = 0;
     int32_t *spiral_ptr = nullptr, *spiral_nbr = nullptr;  // spiral partners, CSR in storage order
