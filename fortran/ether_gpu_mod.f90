@@ -110,6 +110,12 @@ module ether_gpu_mod
             integer(c_int32_t), value :: r0, n
             real(c_double), intent(inout) :: ion(0:8, *)
         end function
+        integer(c_int) function ether_spins_batch_split(ctx, get_kernel, set_kernel) &
+                bind(C, name="ether_spins_batch_split")
+            import :: c_int, c_ptr, c_int32_t
+            type(c_ptr), value :: ctx
+            integer(c_int32_t), intent(out) :: get_kernel, set_kernel
+        end function
         integer(c_int) function ether_fresh_spins(ctx) bind(C, name="ether_fresh_spins")
             import :: c_int, c_ptr
             type(c_ptr), value :: ctx
