@@ -267,6 +267,55 @@ module ether_gpu_mod
             type(c_ptr), value :: ctx
             real(c_double), intent(out) :: out(3, *)
         end function
+        ! get_moment_vectors (src/ether.f90:219) and get_spiral_state's setup (:69) and
+        ! per-sample value (:207)
+        integer(c_int) function ether_moment_vectors(ctx, mm) bind(C, name="ether_moment_vectors")
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(out) :: mm(3, *)
+        end function
+        integer(c_int) function ether_spiral_setup(ctx, ss_dis, ss_direc, ss_latency, capacity, count) &
+                bind(C, name="ether_spiral_setup")
+            import :: c_int, c_ptr, c_double, c_int32_t, c_int64_t
+            type(c_ptr), value :: ctx
+            real(c_double), value :: ss_dis, ss_latency
+            real(c_double), intent(in) :: ss_direc(3)
+            integer(c_int32_t), value :: capacity
+            integer(c_int64_t), intent(out) :: count
+        end function
+        integer(c_int) function ether_spiral_state(ctx, ss) bind(C, name="ether_spiral_state")
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(out) :: ss(*)
+        end function
+        ! the structure factor of utility/Structure_Factor/structure_factor.f90:99-183, nq(1)
+        ! a multiple of 64
+        integer(c_int) function ether_structure_factor(ctx, abc, nq, q0, dq, sq, comp) &
+                bind(C, name="ether_structure_factor")
+            import :: c_int, c_ptr, c_double, c_float, c_int32_t
+            type(c_ptr), value :: ctx
+            real(c_double), intent(in) :: abc(3, 3), q0(3), dq(3)
+            integer(c_int32_t), intent(in) :: nq(3)
+            real(c_float), intent(out) :: sq(*), comp(3, *)
+        end function
+        ! accumulators, slots and the stream's end
+        integer(c_int) function ether_get_sums(ctx, sums) bind(C, name="ether_get_sums")
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(out) :: sums(7, *)
+        end function
+        integer(c_int) function ether_get_slots(ctx, slot_of_replica) bind(C, name="ether_get_slots")
+            import :: c_int, c_ptr, c_int32_t
+            type(c_ptr), value :: ctx
+            integer(c_int32_t), intent(out) :: slot_of_replica(*)
+        end function
+        integer(c_int) function ether_sync(ctx) bind(C, name="ether_sync")
+            import :: c_int, c_ptr
+            type(c_ptr), value :: ctx
+        end function
+        integer(c_int) function ether_abi_version() bind(C, name="ether_abi_version")
+            import :: c_int
+        end function
         ! the whole program src/ether.f90 for one input directory; the directory names are
         ! C strings: trim(dir)//c_null_char
         integer(c_int) function ether_run(indir, outdir, flags, info) bind(C, name="ether_run")
