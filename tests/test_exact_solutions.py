@@ -101,7 +101,9 @@ def _torus_run(pt, flags=0):
     eq, meas, coa = 2000, 20000, 2 if pt else 1
     swaps = sw.mcs(0, eq + meas, eq, coa, pt=pt, exchange_interval=5)
     if pt:
-        assert swaps > 0 and not np.array_equal(sw.slots(), np.arange(sw.R) % len(temps))
+        assert swaps > 0
+        if not flags & eg.FLAG_PT_REFERENCE_COPY:  # a true swap exchanges slots
+            assert not np.array_equal(sw.slots(), np.arange(sw.R) % len(temps))
     sums = sw.sums().reshape(G, len(temps), 7)
     sw.close()
     out = []
@@ -122,14 +124,19 @@ def _torus_run(pt, flags=0):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("pt", [False, True])
+@pytest.mark.parametrize("pt", ["off", "swap", "copy"])
 def test_mcs_energy_and_heat_capacity_equal_the_exact_torus(pt):
     """pt: each chain is a ladder of kT = 2.0, 2.1, 2.269 and 2.5 J with parallel-tempering
-    swaps every 10 steps (src/parallel_tempering.f90:39-108) whose exponent uses the
+    steps every 10 steps (src/parallel_tempering.f90:39-108) whose exponent uses the
     Hamiltonian energy (ETHER_FLAG_PT_TRUE_ENERGY), which leaves every temperature's ensemble
-    exact; the statistics are per (chain, temperature slot)."""
+    exact; the statistics are per (chain, temperature slot).  "copy": on acceptance only the
+    colder slot takes the hotter one's configuration (the reference's effective copy,
+    ETHER_FLAG_PT_REFERENCE_COPY) -- for the colder slot a Metropolis-Hastings move with the
+    hotter slot's configuration as the proposal, so each slot's ensemble is still exact."""
     from scipy.special import erfcinv
-    res = _torus_run(pt, flags=eg.FLAG_PT_TRUE_ENERGY if pt else 0)
+    flags = {"off": 0, "swap": eg.FLAG_PT_TRUE_ENERGY,
+             "copy": eg.FLAG_PT_TRUE_ENERGY | eg.FLAG_PT_REFERENCE_COPY}[pt]
+    res = _torus_run(pt != "off", flags=flags)
     zmax = float(np.sqrt(2) * erfcinv(0.01 / len(res)))   # two-sided 0.01 / 6 (or / 8): |z| < 3.14 (3.23)
     for t, name, got, ref, z in res:
         assert abs(z) < zmax, (t, name, got, ref, z)
@@ -141,7 +148,9 @@ def test_reference_pt_exponent_biases_the_cold_end():
     twice (src/ether.f90:177, src/get_tot_energy.f90:33-47): the swap acceptance is
     exp(2 dbeta dH) instead of exp(dbeta dH), which breaks detailed balance.  The default mode
     reproduces it, and on the same ladder the coldest slot's energy is measurably below the
-    exact value (the chains are seeded, so the figure is reproducible)."""
+    exact value (the chains are seeded, so the figure is reproducible).  It is this exponent,
+    not the reference's copy in place of a swap, that biases its ladders: the copy with the
+    Hamiltonian exponent is exact (above)."""
     res = _torus_run(True)
     t, name, got, ref, z = res[0]
     assert (t, name) == (2.0, "E/N")
