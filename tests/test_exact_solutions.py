@@ -24,6 +24,10 @@ every step (src/ether.f90:163-172) at kT = 0.5, 1 and 2 J, the same rule as abov
 
 Ising in a field: the ring of 64 spins in a Zeeman field, against its transfer matrix (the
 reported energy per site and its variance).
+
+Independent Heisenberg spins in a single-ion anisotropy and a Zeeman field (no exchange): the
+averages are integrals over cos theta; the simple-cubic fast kernels with Marsaglia proposals,
+the general-lattice kernels with ANGLE proposals, and anisotropy about per-site local axes.
 """
 import numpy as np
 import pytest
@@ -274,4 +278,90 @@ def test_mcs_ising_ring_in_a_field_equals_the_transfer_matrix():
             print("Ising ring in H=%.0f T, kT=%.2f %s: GPU %.5f +- %.5f, exact %.5f, z = %.2f" %
                   (Hz, t, name, x.mean(), x.std(ddof=1) / np.sqrt(G), ref, z))
             assert abs(z) < zmax, (t, name, x.mean(), ref, z)
+    sw.close()
+
+
+def _single_spin_moments(A, B, kT):
+    """<u>, <u^2>, <u^3>, <u^4> of u = cos(theta) over the sphere with weight
+    exp(-(A u^2 + B u) / kT) (Simpson's rule on 200 001 points)."""
+    u = np.linspace(-1.0, 1.0, 200001)
+    w = np.exp(-(A * u * u + B * u - min(A + B, A - B, 0.0)) / kT)
+    h = u[1] - u[0]
+    c = np.ones_like(u)
+    c[1:-1:2], c[2:-1:2] = 4.0, 2.0
+    z = (c * w).sum()
+    return [float((c * w * u ** k).sum() / z) for k in (1, 2, 3, 4)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("form", ["sc_marsaglia", "general_angle", "local_axes"])
+def test_mcs_independent_spins_with_anisotropy_and_field_equal_the_integral(form):
+    """No exchange: each Heisenberg spin is alone in its single-ion anisotropy D and Zeeman
+    field, E(u) = A u^2 + B u with u the spin's component along the axis (cos theta), and the
+    thermal averages are one-dimensional integrals over the sphere.  The reported energy per
+    site is half of it (src/get_eng.f90:36: SIA and Zeeman enter E_raw once), and
+    N Var(e) = Var(E(u)) / 4.  A and B are read off the library itself (the energies of the
+    all-up and all-down states) and checked against D and g mu_B H.
+    sc_marsaglia: 8^3 simple cubic (the fast kernels), easy axis D = -0.3 meV along z, H = 1 T
+    along z, Marsaglia proposals.  general_angle: the same on the general-lattice kernels with
+    ANGLE proposals (dphi = 0.6).  local_axes: easy plane D = +0.4 meV about a random unit axis
+    (16 axes over the sites, ether_desc.sia_local), no field: the same integral for every
+    site."""
+    L, G = 8, 32
+    temps = (0.1, 0.4)   # kT in meV
+    lat = eg.simple_cubic(L)
+    zero = [[(1, 1, (0.0, 0.0, 0.0))]]
+    kw = {}
+    if form == "local_axes":
+        rng = np.random.default_rng(5)
+        ax = rng.normal(size=(16, 3))    # 16 axes (at most 256 distinct classes per context)
+        ax /= np.linalg.norm(ax, axis=1, keepdims=True)
+        ax = ax[rng.integers(0, 16, size=lat.N)]
+        kw = dict(sia_local=np.concatenate([ax, np.full((lat.N, 1), 0.4e-3)], axis=1))
+        D, Hz = 0.4, 0.0
+    else:
+        D, Hz = -0.3, 1.0
+        kw = dict(sia=True, sia_vec=np.array([[0.0, 0.0, D * 1e-3]]), zeeman=True, h=(0.0, 0.0, Hz),
+                  g_factor=2.0)
+        if form == "general_angle":
+            kw.update(angle=True, dphi=0.6)
+    flags = eg.FLAG_FORCE_GENERAL if form == "general_angle" else 0
+    seed = {"sc_marsaglia": 1992, "general_angle": 2024, "local_axes": 77}[form]  # independent draws
+    sw, _ = make_pair(lat, eg.MODEL_XYZ, zero, replicas=G * len(temps), flags=flags, seed=seed, **kw)
+    assert sw.info().fast_path == (0 if form == "general_angle" else 1)
+    sw.set_ladder([1.0 / (t * 1e-3) for t in temps])
+    # E(u) = A u^2 + B u: the all-up and all-down states (along z, or along each site's axis)
+    st = lat.ion.copy()
+    st[:, 1:4] = kw["sia_local"][:, :3] if form == "local_axes" else (0.0, 0.0, 1.0)
+    sw.set_spins(st)
+    e_up = float(np.asarray(sw.tot_energy())[0]) / (2 * lat.N) / 1e-3
+    st[:, 1:4] *= -1.0
+    sw.set_spins(st)
+    e_dn = float(np.asarray(sw.tot_energy())[0]) / (2 * lat.N) / 1e-3
+    A, B = e_up + e_dn, e_up - e_dn     # twice the reported halves
+    assert np.isclose(A, D, rtol=1e-6)
+    assert np.isclose(B, -2.0 * eg.MB_EV * Hz * 1e3, rtol=1e-6, atol=1e-9)
+    sw.set_streams(stream=list(range(sw.R)), step=[0] * sw.R)
+    sw.set_spins(random_xyz(lat, 17))
+    sw.zero_avg()
+    # ANGLE moves cross the 3 kT barrier between the field-split wells slowly: a long start
+    eq, meas = 5000, 10000
+    sw.mcs(0, eq + meas, eq, 1)
+    sums = sw.sums().reshape(G, len(temps), 7)
+    from scipy.special import erfcinv
+    zmax = float(np.sqrt(2) * erfcinv(0.01 / (2 * len(temps))))
+    for k, t in enumerate(temps):
+        m1, m2, m3, m4 = _single_spin_moments(A, B, t)
+        mean_E = A * m2 + B * m1
+        var_E = A * A * m4 + 2 * A * B * m3 + B * B * m2 - mean_E ** 2
+        e_ex, var_ex = mean_E / 2, var_E / 4
+        cnt = sums[:, k, 0]
+        assert np.all(cnt == meas)
+        e = sums[:, k, 1] / cnt / 1e-3
+        var = lat.N * (sums[:, k, 2] / cnt / 1e-6 - e * e)
+        for name, x, ref in (("E/N", e, e_ex), ("N Var(E/N)", var, var_ex)):
+            z = (x.mean() - ref) / (x.std(ddof=1) / np.sqrt(G))
+            print("%s kT=%.2f meV %s: GPU %.6f +- %.6f, exact %.6f, z = %.2f" %
+                  (form, t, name, x.mean(), x.std(ddof=1) / np.sqrt(G), ref, z))
+            assert abs(z) < zmax, (form, t, name, x.mean(), ref, z)
     sw.close()
