@@ -365,3 +365,45 @@ def test_mcs_independent_spins_with_anisotropy_and_field_equal_the_integral(form
                   (form, t, name, x.mean(), x.std(ddof=1) / np.sqrt(G), ref, z))
             assert abs(z) < zmax, (form, t, name, x.mean(), ref, z)
     sw.close()
+
+
+@pytest.mark.gpu
+def test_mcs_independent_ising_spins_in_a_field_equal_tanh():
+    """No exchange: each Ising spin of a 32^3 simple-cubic lattice (the fast kernels with
+    16-byte vectors, as the benchmark runs them) is alone in a Zeeman field, E(s) = B s with
+    B = -g mu_B H, so <s> = -tanh(B / kT) and the reported energy per site (half the Zeeman
+    term) is B <s> / 2 with N Var(e) = (B / 2)^2 (1 - <s>^2).  H = 2 T, kT = 0.1 and 0.3 meV,
+    16 chains each; the same family-wise rule."""
+    L, G, Hz = 32, 16, 2.0
+    temps = (0.1, 0.3)
+    lat = eg.simple_cubic(L)
+    sw, _ = make_pair(lat, eg.MODEL_ISING, [[(1, 1, (0.0, 0.0, 0.0))]], replicas=G * len(temps),
+                      zeeman=True, h=(0.0, 0.0, Hz), g_factor=2.0, seed=31)
+    assert sw.info().fast_path == 1
+    sw.set_ladder([1.0 / (t * 1e-3) for t in temps])
+    B = -2.0 * eg.MB_EV * Hz * 1e3
+    st = lat.ion.copy()
+    st[:, 3] = 1.0
+    sw.set_spins(st)
+    assert np.isclose(float(np.asarray(sw.tot_energy())[0]) / (2 * lat.N) / 1e-3, B / 2, rtol=1e-9)
+    sw.set_streams(stream=list(range(sw.R)), step=[0] * sw.R)
+    sw.set_spins(random_ising(lat, 19))
+    sw.zero_avg()
+    eq, meas = 200, 2000
+    sw.mcs(0, eq + meas, eq, 1)
+    sums = sw.sums().reshape(G, len(temps), 7)
+    from scipy.special import erfcinv
+    zmax = float(np.sqrt(2) * erfcinv(0.01 / (2 * len(temps))))
+    for k, t in enumerate(temps):
+        s_mean = -np.tanh(B / t)
+        e_ex, var_ex = B * s_mean / 2, (B / 2) ** 2 * (1 - s_mean ** 2)
+        cnt = sums[:, k, 0]
+        assert np.all(cnt == meas)
+        e = sums[:, k, 1] / cnt / 1e-3
+        var = lat.N * (sums[:, k, 2] / cnt / 1e-6 - e * e)
+        for name, x, ref in (("E/N", e, e_ex), ("N Var(E/N)", var, var_ex)):
+            z = (x.mean() - ref) / (x.std(ddof=1) / np.sqrt(G))
+            print("Ising spins in H=%.0f T, kT=%.2f meV %s: GPU %.7f +- %.7f, exact %.7f, z = %.2f" %
+                  (Hz, t, name, x.mean(), x.std(ddof=1) / np.sqrt(G), ref, z))
+            assert abs(z) < zmax, (t, name, x.mean(), ref, z)
+    sw.close()
