@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <atomic>
 #include <numeric>
 #include <string>
@@ -215,6 +216,7 @@ void free_ctx(Ctx &c) {
     if (c.stage) cudaFreeHost(c.stage);
     for (cudaEvent_t e : c.ion_ev)
         if (e) cudaEventDestroy(e);
+    if (c.ion_copy) cudaStreamDestroy(c.ion_copy);
     for (auto &kv : c.graphs) cudaGraphExecDestroy(kv.second);
     if (c.ev_fork) cudaEventDestroy(c.ev_fork);
     for (int k = 0; k < Ctx::kMaxParts - 1; ++k) {
@@ -791,17 +793,103 @@ static bool host_range_mapped(const void *p, size_t bytes) {
     return msync(reinterpret_cast<void *>(a), (size_t)(b - a), MS_ASYNC) == 0;
 }
 
+// An upload of n replicas shared between the in-place kernel and the host's cores as they go:
+// the replicas are cut into about 32 chunks; this thread hands chunks from the front to the
+// kernel, keeping two in flight on c.stream (so a chunk is claimed only when the device is about
+// to need it), while the host's other threads take chunks from the back, convert them into the
+// staging area and copy them on c.ion_copy.  The two ends meet where the two rates put them, in
+// this call, whatever the link does.  kernel_reps: replicas the kernel moved.
+static int spins_upload_shared(Ctx &c, int32_t r0, int32_t n, double *ion, int *kernel_reps) {
+    const size_t per_rep = c.model == ETHER_MODEL_ISING ? (size_t)c.N : sizeof(float4) * c.N;
+    const size_t ion_rep = (size_t)9 * c.N;
+    uint8_t *dev = c.model == ETHER_MODEL_ISING ? c.spins : reinterpret_cast<uint8_t *>(c.spins4);
+    const int chunk = std::max(1, (n + 31) / 32);
+    const int nch = (n + chunk - 1) / chunk;
+    {
+        const int rc = ensure_stage(c, per_rep * (size_t)n);
+        if (rc) return rc;
+    }
+    if (!c.ion_copy) CUDA_TRY(cudaStreamCreateWithFlags(&c.ion_copy, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; ++k)  // timing events: the read-back times its kernel with them
+        if (!c.ion_ev[k]) CUDA_TRY(cudaEventCreate(&c.ion_ev[k]));
+    uint8_t *stage = static_cast<uint8_t *>(c.stage);
+    std::mutex mu;
+    int front = 0, back = nch;  // chunks [0, front) to the kernel, [back, nch) to the host
+    std::atomic<int> err{0};
+    auto count = [&](int k) { return std::min(n, (k + 1) * chunk) - k * chunk; };
+    int dev_id = 0;
+    cudaGetDevice(&dev_id);
+    const int T = std::max(1, std::min(nch, host_threads() - 1));
+    std::vector<std::thread> pool;
+    pool.reserve(T);
+    for (int t = 0; t < T; ++t)
+        pool.emplace_back([&]() {
+            cudaSetDevice(dev_id);
+            for (;;) {
+                int k;
+                {
+                    std::lock_guard<std::mutex> g(mu);
+                    if (front >= back || err.load()) return;
+                    k = --back;
+                }
+                const int a = k * chunk, m = count(k);
+                for (int r = a; r < a + m; ++r)
+                    ion_to_device_layout(c, ion + ion_rep * (size_t)r, stage + per_rep * r);
+                const cudaError_t e = cudaMemcpyAsync(dev + per_rep * (size_t)(r0 + a), stage + per_rep * a,
+                                                      per_rep * m, cudaMemcpyHostToDevice, c.ion_copy);
+                if (e != cudaSuccess) err.store((int)e);
+            }
+        });
+    cudaError_t e = cudaSuccess;
+    int launched = 0;
+    for (;;) {
+        int k;
+        {
+            std::lock_guard<std::mutex> g(mu);
+            if (front >= back || err.load()) break;
+            k = front++;
+        }
+        const int a = k * chunk;
+        e = launch_ion_copy(c, r0 + a, count(k), ion + ion_rep * (size_t)a, true);
+        if (e == cudaSuccess) e = cudaEventRecord(c.ion_ev[launched & 1], c.stream);
+        if (e != cudaSuccess) {
+            err.store((int)e);
+            break;
+        }
+        ++launched;
+        // two chunks in flight: wait for the one before the last
+        if (launched >= 2) e = cudaEventSynchronize(c.ion_ev[launched & 1]);
+        if (e != cudaSuccess) {
+            err.store((int)e);
+            break;
+        }
+    }
+    for (auto &th : pool) th.join();
+    // the kernel's chunks and the copies both end before the call returns (the records and the
+    // staging area are the caller's and this context's again)
+    cudaError_t e2 = cudaStreamSynchronize(c.stream);
+    const cudaError_t e3 = cudaStreamSynchronize(c.ion_copy);
+    if (e2 == cudaSuccess) e2 = e3;
+    if (e2 == cudaSuccess && err.load()) e2 = (cudaError_t)err.load();
+    if (e2 != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ETHER_ERR_CUDA, std::string("ether_set_spins_batch: ") + cudaGetErrorString(e2));
+    }
+    *kernel_reps = std::min(n, front * chunk);
+    return ETHER_OK;
+}
+
 // Where the device reads and writes host memory in place (c.ion_direct) a kernel can move the
 // records, and the host's cores can convert them through the staging area at the same time;
 // which does how much is measured per context and direction, because the in-place path's
 // speed depends on the host: on most Grace machines it is the faster (64^3 x 1024 Ising records:
 // upload 77 ms by the kernel alone, 83-86 by the cores alone, 53-61 split 5/8; read-back 100
 // against 148 ms), on some it was several times slower (0.23 s and 0.72 s in one process).
-// * Upload: the kernel reads the first share of the replicas while the host's cores convert
-//   the rest, the staged copies following the kernel on the stream.  The first call splits
-//   5/8 : 3/8 (8 or more replicas and host threads; 1/2 and 3/4 measured 67 and 59 ms), later
-//   calls in proportion to the two rates measured side by side in the previous one, so both
-//   parts end together.
+// * Upload: shared as it runs (spins_upload_shared) when the staging area holds all of it;
+//   otherwise the kernel reads the first share of the replicas while the host's cores convert
+//   the rest, the staged copies following the kernel on the stream: 5/8 : 3/8 the first time
+//   (8 or more replicas and host threads; 1/2 and 3/4 measured 67 and 59 ms), later in
+//   proportion to the two rates measured side by side in the previous upload.
 // * Read-back: not split (each 8-byte write is a read-modify-write of a line in host memory,
 //   whichever side makes it, and a split measured slower, 111-133 against 100 ms).  The first
 //   three calls run the kernel, the host's cores and the kernel again (a process's first
@@ -813,6 +901,13 @@ static int spins_batch(Ctx &c, int32_t r0, int32_t n, double *ion, bool to_devic
     if (!host_range_mapped(ion, sizeof(double) * 9 * (size_t)c.N * n))
         return fail(ETHER_ERR_ARG, std::string(to_device ? "ether_set_spins_batch" : "ether_get_spins_batch") +
                                        ": ion is not host memory mapped for n replicas' records");
+    const size_t per_rep = c.model == ETHER_MODEL_ISING ? (size_t)c.N : sizeof(float4) * c.N;
+    if (to_device && n >= 2 && host_threads() >= 2 && per_rep * (size_t)n <= kStageMax) {
+        int nk = 0;
+        const int rc = spins_upload_shared(c, r0, n, ion, &nk);
+        if (rc == ETHER_OK) c.ion_last_kernel[1] = nk;
+        return rc;
+    }
     const int d = to_device ? 1 : 0;
     const double rk = c.ion_rate_k[d], rh = c.ion_rate_h[d];
     int nk;

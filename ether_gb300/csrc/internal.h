@@ -137,6 +137,7 @@ struct Ctx {
     int ion_last_kernel[2] = {0, 0};
     int ion_gets = 0;  // read-backs so far (the first three try the kernel, the cores, the kernel)
     cudaEvent_t ion_ev[2] = {nullptr, nullptr};
+    cudaStream_t ion_copy = nullptr;  // the host's staged copies beside the in-place kernel
     size_t stage_bytes = 0;
     int32_t *spiral_ptr = nullptr, *spiral_nbr = nullptr;  // spiral partners, CSR in storage order
     long spiral_count = 0;

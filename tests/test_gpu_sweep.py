@@ -391,9 +391,10 @@ def test_spins_batch_equals_per_replica_calls(model, L, R, staged):
 
 
 def test_spins_batch_measures_both_ways_and_keeps_the_records():
-    """Where the records can move in place: the first upload splits 5/8 of the replicas to the
-    kernel, later ones by the measured rates; the read-backs run the kernel, the host's cores
-    and the kernel, then the faster way.  Every call leaves the same device state and records."""
+    """Where the records can move in place: an upload shares its replicas between the kernel
+    (chunks from the front) and the host's cores (chunks from the back) as they go; the
+    read-backs run the kernel, the host's cores and the kernel, then the faster way.  Every
+    call leaves the same device state and records."""
     lat = eg.simple_cubic((32, 16, 16))
     R = 40
     sw, _ = make_pair(lat, eg.MODEL_ISING, FM, replicas=R)
@@ -413,7 +414,6 @@ def test_spins_batch_measures_both_ways_and_keeps_the_records():
         np.testing.assert_array_equal(back[:, :, 3], ions[:, :, 3])
         assert np.all(back[:, :, 0] == 5.0)
     print("kernel share of the uploads", sets, "of the read-backs", gets, "of", R)
-    assert sets[0] == R - R * 3 // 8
     assert all(0 <= k <= R for k in sets)
     assert gets[:3] == [R, 0, R] and gets[3] in (0, R) and gets[4] == gets[3]
     sw.close()
