@@ -793,64 +793,93 @@ static bool host_range_mapped(const void *p, size_t bytes) {
     return msync(reinterpret_cast<void *>(a), (size_t)(b - a), MS_ASYNC) == 0;
 }
 
-// An upload of n replicas shared between the in-place kernel and the host's cores as they go:
-// the replicas are cut into about 32 chunks; this thread hands chunks from the front to the
-// kernel, keeping two in flight on c.stream (so a chunk is claimed only when the device is about
-// to need it), while the host's other threads take chunks from the back, convert them into the
-// staging area and copy them on c.ion_copy.  The two ends meet where the two rates put them, in
-// this call, whatever the link does.  kernel_reps: replicas the kernel moved.
-static int spins_upload_shared(Ctx &c, int32_t r0, int32_t n, double *ion, int *kernel_reps) {
+// A transfer of n replicas shared between the in-place kernel and the host's cores as it runs:
+// this thread hands chunks of about n/32 replicas from the front to the kernel, keeping two in
+// flight on c.stream (so a chunk is claimed only when the device is about to need it), while
+// the host's other threads take chunks of an eighth of that from the back through the staging
+// area (an upload: convert, then copy on c.ion_copy; a read-back: copy on c.ion_copy, wait for
+// it, convert).  The two ends meet where the two rates put them in this call, whatever the
+// link does.  kernel_reps: replicas the kernel moved.
+static int spins_shared(Ctx &c, int32_t r0, int32_t n, double *ion, bool to_device, int *kernel_reps) {
     const size_t per_rep = c.model == ETHER_MODEL_ISING ? (size_t)c.N : sizeof(float4) * c.N;
     const size_t ion_rep = (size_t)9 * c.N;
     uint8_t *dev = c.model == ETHER_MODEL_ISING ? c.spins : reinterpret_cast<uint8_t *>(c.spins4);
-    const int chunk = std::max(1, (n + 31) / 32);
-    const int nch = (n + chunk - 1) / chunk;
+    const char *who = to_device ? "ether_set_spins_batch: " : "ether_get_spins_batch: ";
+    // claims in replicas: the kernel takes kc at a time from the front (about 1/32 of the call,
+    // a few milliseconds of device work), a host thread hc from the back (about a millisecond
+    // of a core's work), so the meeting point follows the two rates closely
+    const int kc = std::max(1, (n + 31) / 32);
+    const int hc = std::max(1, kc / 8);
     {
         const int rc = ensure_stage(c, per_rep * (size_t)n);
         if (rc) return rc;
     }
     if (!c.ion_copy) CUDA_TRY(cudaStreamCreateWithFlags(&c.ion_copy, cudaStreamNonBlocking));
-    for (int k = 0; k < 2; ++k)  // timing events: the read-back times its kernel with them
+    for (int k = 0; k < 2; ++k)  // timing events: the rate-based path times its kernel with them
         if (!c.ion_ev[k]) CUDA_TRY(cudaEventCreate(&c.ion_ev[k]));
+    // the copies start after the work already on the context's stream (sweeps still reading or
+    // writing the spins), as the kernel's chunks do
+    CUDA_TRY(cudaEventRecord(c.ion_ev[0], c.stream));
+    CUDA_TRY(cudaStreamWaitEvent(c.ion_copy, c.ion_ev[0], 0));
     uint8_t *stage = static_cast<uint8_t *>(c.stage);
     std::mutex mu;
-    int front = 0, back = nch;  // chunks [0, front) to the kernel, [back, nch) to the host
+    int front = 0, back = n;  // replicas [0, front) to the kernel, [back, n) to the host
     std::atomic<int> err{0};
-    auto count = [&](int k) { return std::min(n, (k + 1) * chunk) - k * chunk; };
     int dev_id = 0;
     cudaGetDevice(&dev_id);
-    const int T = std::max(1, std::min(nch, host_threads() - 1));
+    const int T = std::max(1, std::min((n + hc - 1) / hc, host_threads() - 1));
     std::vector<std::thread> pool;
     pool.reserve(T);
     for (int t = 0; t < T; ++t)
         pool.emplace_back([&]() {
             cudaSetDevice(dev_id);
+            cudaEvent_t done = nullptr;  // a read-back waits for its own copy only
+            if (!to_device && cudaEventCreateWithFlags(&done, cudaEventDisableTiming) != cudaSuccess) {
+                err.store((int)cudaErrorMemoryAllocation);
+                return;
+            }
             for (;;) {
-                int k;
+                int a, m;
                 {
                     std::lock_guard<std::mutex> g(mu);
-                    if (front >= back || err.load()) return;
-                    k = --back;
+                    if (front >= back || err.load()) break;
+                    m = std::min(hc, back - front);
+                    back -= m;
+                    a = back;
                 }
-                const int a = k * chunk, m = count(k);
-                for (int r = a; r < a + m; ++r)
-                    ion_to_device_layout(c, ion + ion_rep * (size_t)r, stage + per_rep * r);
-                const cudaError_t e = cudaMemcpyAsync(dev + per_rep * (size_t)(r0 + a), stage + per_rep * a,
-                                                      per_rep * m, cudaMemcpyHostToDevice, c.ion_copy);
-                if (e != cudaSuccess) err.store((int)e);
+                uint8_t *sd = dev + per_rep * (size_t)(r0 + a);
+                uint8_t *ss = stage + per_rep * a;
+                if (to_device) {
+                    for (int r = a; r < a + m; ++r)
+                        ion_to_device_layout(c, ion + ion_rep * (size_t)r, stage + per_rep * r);
+                    const cudaError_t e = cudaMemcpyAsync(sd, ss, per_rep * m, cudaMemcpyHostToDevice, c.ion_copy);
+                    if (e != cudaSuccess) err.store((int)e);
+                } else {
+                    cudaError_t e = cudaMemcpyAsync(ss, sd, per_rep * m, cudaMemcpyDeviceToHost, c.ion_copy);
+                    if (e == cudaSuccess) e = cudaEventRecord(done, c.ion_copy);
+                    if (e == cudaSuccess) e = cudaEventSynchronize(done);
+                    if (e != cudaSuccess) {
+                        err.store((int)e);
+                        break;
+                    }
+                    for (int r = a; r < a + m; ++r)
+                        device_layout_to_ion(c, stage + per_rep * r, ion + ion_rep * (size_t)r);
+                }
             }
+            if (done) cudaEventDestroy(done);
         });
     cudaError_t e = cudaSuccess;
     int launched = 0;
     for (;;) {
-        int k;
+        int a, m;
         {
             std::lock_guard<std::mutex> g(mu);
             if (front >= back || err.load()) break;
-            k = front++;
+            a = front;
+            m = std::min(kc, back - front);
+            front += m;
         }
-        const int a = k * chunk;
-        e = launch_ion_copy(c, r0 + a, count(k), ion + ion_rep * (size_t)a, true);
+        e = launch_ion_copy(c, r0 + a, m, ion + ion_rep * (size_t)a, to_device);
         if (e == cudaSuccess) e = cudaEventRecord(c.ion_ev[launched & 1], c.stream);
         if (e != cudaSuccess) {
             err.store((int)e);
@@ -873,9 +902,9 @@ static int spins_upload_shared(Ctx &c, int32_t r0, int32_t n, double *ion, int *
     if (e2 == cudaSuccess && err.load()) e2 = (cudaError_t)err.load();
     if (e2 != cudaSuccess) {
         cudaGetLastError();
-        return fail(ETHER_ERR_CUDA, std::string("ether_set_spins_batch: ") + cudaGetErrorString(e2));
+        return fail(ETHER_ERR_CUDA, std::string(who) + cudaGetErrorString(e2));
     }
-    *kernel_reps = std::min(n, front * chunk);
+    *kernel_reps = front;
     return ETHER_OK;
 }
 
@@ -885,16 +914,18 @@ static int spins_upload_shared(Ctx &c, int32_t r0, int32_t n, double *ion, int *
 // speed depends on the host: on most Grace machines it is the faster (64^3 x 1024 Ising records:
 // upload 77 ms by the kernel alone, 83-86 by the cores alone, 53-61 split 5/8; read-back 100
 // against 148 ms), on some it was several times slower (0.23 s and 0.72 s in one process).
-// * Upload: shared as it runs (spins_upload_shared) when the staging area holds all of it;
-//   otherwise the kernel reads the first share of the replicas while the host's cores convert
+// Both directions are shared as they run (spins_shared) when the staging area holds the whole
+// call; the kernel's rate on one box changed between calls by up to 4x, so only a division made
+// during the call itself holds.  (On a good box a shared read-back costs a little against the
+// kernel alone, 100 ms: each 8-byte write is a read-modify-write of a line in host memory and
+// the two sides compete for it.)  A call too large for the staging area is divided by rates
+// measured in earlier calls:
+// * Upload: the kernel reads the first share of the replicas while the host's cores convert
 //   the rest, the staged copies following the kernel on the stream: 5/8 : 3/8 the first time
 //   (8 or more replicas and host threads; 1/2 and 3/4 measured 67 and 59 ms), later in
 //   proportion to the two rates measured side by side in the previous upload.
-// * Read-back: not split (each 8-byte write is a read-modify-write of a line in host memory,
-//   whichever side makes it, and a split measured slower, 111-133 against 100 ms).  The first
-//   three calls run the kernel, the host's cores and the kernel again (a process's first
-//   in-place read-back was seen slower than its later ones), later calls the way with the
-//   better of its measured rates.
+// * Read-back: not split.  The first three calls run the kernel, the host's cores and the
+//   kernel again, later calls the way with the better of its measured rates.
 // Rates come from CUDA events around the kernel and the wall time of the host's conversion.
 static int spins_batch(Ctx &c, int32_t r0, int32_t n, double *ion, bool to_device) {
     if (!c.ion_direct) return spins_staged(c, r0, n, ion, to_device);
@@ -902,10 +933,10 @@ static int spins_batch(Ctx &c, int32_t r0, int32_t n, double *ion, bool to_devic
         return fail(ETHER_ERR_ARG, std::string(to_device ? "ether_set_spins_batch" : "ether_get_spins_batch") +
                                        ": ion is not host memory mapped for n replicas' records");
     const size_t per_rep = c.model == ETHER_MODEL_ISING ? (size_t)c.N : sizeof(float4) * c.N;
-    if (to_device && n >= 2 && host_threads() >= 2 && per_rep * (size_t)n <= kStageMax) {
+    if (n >= 2 && host_threads() >= 2 && per_rep * (size_t)n <= kStageMax) {
         int nk = 0;
-        const int rc = spins_upload_shared(c, r0, n, ion, &nk);
-        if (rc == ETHER_OK) c.ion_last_kernel[1] = nk;
+        const int rc = spins_shared(c, r0, n, ion, to_device, &nk);
+        if (rc == ETHER_OK) c.ion_last_kernel[to_device ? 1 : 0] = nk;
         return rc;
     }
     const int d = to_device ? 1 : 0;

@@ -148,10 +148,9 @@ int ether_set_spins_batch(ether_ctx *ctx, int32_t r0, int32_t n, const double *i
 int ether_get_spins_batch(ether_ctx *ctx, int32_t r0, int32_t n, double *ion);
 /* How the last ether_get_spins_batch / ether_set_spins_batch divided its replicas: the number
  * moved in place by a kernel (the rest went through the host's staging).  Where both ways are
- * open, an upload is shared as it runs: the kernel takes chunks of replicas from the front
- * while the host's cores take chunks from the back, until they meet; the first three
- * read-backs use the kernel, the host's cores and the kernel, later ones the way with the
- * better rate seen. */
+ * open, a call is shared as it runs: the kernel takes chunks of replicas from the front while
+ * the host's cores take chunks from the back, until they meet (a call larger than the 512 MB
+ * staging area is divided by rates measured in earlier calls). */
 int ether_spins_batch_split(ether_ctx *ctx, int32_t *get_kernel, int32_t *set_kernel);
 
 /* fresh_spins (src/fresh_spins.f90:31-38), called at src/ether.f90:155: Ising flips every

@@ -390,11 +390,11 @@ def test_spins_batch_equals_per_replica_calls(model, L, R, staged):
     sw.close()
 
 
-def test_spins_batch_measures_both_ways_and_keeps_the_records():
+def test_spins_batch_shares_the_work_and_keeps_the_records():
     """Where the records can move in place: an upload shares its replicas between the kernel
-    (chunks from the front) and the host's cores (chunks from the back) as they go; the
-    read-backs run the kernel, the host's cores and the kernel, then the faster way.  Every
-    call leaves the same device state and records."""
+    (chunks from the front) and the host's cores (chunks from the back) as it runs, and so does
+    a read-back.  Every call leaves the same device state and records, also right after a
+    sweep that is still running."""
     lat = eg.simple_cubic((32, 16, 16))
     R = 40
     sw, _ = make_pair(lat, eg.MODEL_ISING, FM, replicas=R)
@@ -405,6 +405,7 @@ def test_spins_batch_measures_both_ways_and_keeps_the_records():
     ions = np.stack([random_ising(lat, 40 + r) for r in range(R)])
     gets, sets = [], []
     for k in range(5):
+        sw.metropolis(1, accept=False)   # left running: the upload must wait for it
         sw.set_spins_batch(ions)
         sets.append(sw.spins_batch_split()[1])
         back = np.stack([lat.ion] * R).copy()
@@ -414,8 +415,7 @@ def test_spins_batch_measures_both_ways_and_keeps_the_records():
         np.testing.assert_array_equal(back[:, :, 3], ions[:, :, 3])
         assert np.all(back[:, :, 0] == 5.0)
     print("kernel share of the uploads", sets, "of the read-backs", gets, "of", R)
-    assert all(0 <= k <= R for k in sets)
-    assert gets[:3] == [R, 0, R] and gets[3] in (0, R) and gets[4] == gets[3]
+    assert all(0 <= k <= R for k in sets + gets)
     sw.close()
 
 
