@@ -215,9 +215,9 @@ def run_sweeps(model, L, replicas, steps, warmup, rank, world, force_variant=0, 
         # C-ABI; the acceptance ratios of all replicas come back to the host every sweep
         ions = np.empty((R, N, 9))
         ions[:] = ion
-        # untimed rounds: the first allocates the pinned staging area, and where the records can
-        # also move in place the library measures both ways on its first calls (the first three
-        # read-backs try the kernel, the host's cores and the kernel) and settles on its split
+        # untimed rounds: the first allocates the pinned staging area and the copy stream (where
+        # the records can also move in place, each call shares its replicas between the kernel
+        # and the host's cores as it runs)
         for _ in range(3):
             sw.set_spins_batch(ions)
             sw.get_spins_batch(ions)
