@@ -298,8 +298,9 @@ def run_sq(cells=12, replicas=64, M=64, calls=3, warmup=1, model=MODEL_XYZ):
             "tensor_tflops": products * useful / ms / 1e9, "useful_tflops": useful / ms / 1e9}
 
 
-def run_tau(L=64, replicas=128, equil=20000, sweeps=100000, stride=10):
-    """tau_int(|M|) of the plain Checkerboard sweep at T_c, and the independent samples/s."""
+def run_tau(L=64, replicas=1024, equil=20000, sweeps=100000, stride=10):
+    """tau_int(|M|) of the plain Checkerboard sweep at T_c, and the independent samples/s, on
+    the headline's 1024 replicas (|M| of every replica recorded every `stride` sweeps)."""
     import ether_gb300 as eg
     from ether_gb300.analysis import tau_int
     lat, j, sw, ion, beta = make_workload(eg.MODEL_ISING, L, replicas, seed=4242)
