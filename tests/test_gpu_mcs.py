@@ -404,9 +404,13 @@ def test_ising_pt_ladder_same_ensemble_as_reference_order():
     assert_same_ensemble(mine, ref)
 
 
+@pytest.mark.parametrize("L", [16, (16, 8, 16)])
 @pytest.mark.parametrize("model", [eg.MODEL_ISING, eg.MODEL_XYZ])
-def test_record_series_equals_step_by_step(model):
-    lat = eg.simple_cubic(16)
+def test_record_series_equals_step_by_step(model, L):
+    """ether_record_series against the same sweeps with ether_tot_energy /
+    ether_tot_magnetisation after each stride.  (16, 8, 16): 2048 sites, one reduction block
+    per replica, where the Ising magnetisation is counted 16 bytes at a time."""
+    lat = eg.simple_cubic(L)
     runs = []
     for way in ("series", "steps"):
         sw, _ = make_pair(lat, model, FM, replicas=3)
