@@ -892,6 +892,13 @@ static int spins_shared(Ctx &c, int32_t r0, int32_t n, double *ion, bool to_devi
             err.store((int)e);
             break;
         }
+        // a link far slower than the cores: its traffic only competes with theirs for the
+        // host's memory, so after a few chunks the kernel is given no more once the cores have
+        // claimed more than twice what it has finished (at most two chunks still in flight)
+        if (launched >= 4) {
+            std::lock_guard<std::mutex> g(mu);
+            if (n - back > 2 * (front - 2 * kc)) break;
+        }
     }
     for (auto &th : pool) th.join();
     // the kernel's chunks and the copies both end before the call returns (the records and the
